@@ -1,0 +1,142 @@
+/*
+ * C ABI of the GB300 path integrator (libnarval_gb300.so).
+ *
+ * It replaces the reference's CPU render path at the point where OfflineEngine
+ * hands camera rays to the integrator:
+ *   OfflineEngine::renderTile / coreLoop  (core/OfflineEngine.cpp:54-113)   -> ne_render
+ *   Integrator::Li(Ray, Scene*)           (integrators/Integrator.h:13-25)   -> ne_li_batch
+ *   Scene::intersectScene                 (core/Scene.cpp:30-56)            -> ne_trace_closest
+ *   SceneReader::loadScene                (io/SceneReader.cpp:10-54)        -> ne_scene_host_load_json
+ * Every function returns ne_status (0 = success, negative = failure) and never
+ * aborts; the reference instead stops the process with LOG(FATAL) on bad input.
+ * Buffers are owned by the caller; device memory of a scene is owned by the library.
+ * A context owns one CUDA stream. A context and its scenes must not be used from
+ * two threads at once; separate contexts are independent.
+ */
+#ifndef NARVAL_GB300_H_
+#define NARVAL_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+#include "narval_scene.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t ne_status;
+#define NE_OK 0
+#define NE_ERR_INVALID_ARG (-1)
+#define NE_ERR_PARSE (-2)
+#define NE_ERR_MISSING_ASSET (-3)
+#define NE_ERR_CUDA (-4)
+#define NE_ERR_TIMEOUT (-5)
+#define NE_ERR_UNSUPPORTED (-6)
+#define NE_ERR_NO_DEVICE (-7)
+#define NE_ERR_OUT_OF_MEMORY (-8)
+
+typedef struct ne_context ne_context;
+typedef struct ne_scene ne_scene;
+typedef struct ne_scene_host ne_scene_host;
+
+/* A ray as the reference's Ray (primitives/Ray.h:182-197). */
+typedef struct ne_ray {
+  float o[3];
+  float d[3];
+} ne_ray;
+
+/* Identity of a camera path: pixel = y * width + x, sample = index in the pixel. */
+typedef struct ne_path_key {
+  uint32_t pixel;
+  uint32_t sample;
+} ne_path_key;
+
+/* Closest hit, the fields of RayIntersection (primitives/Ray.h:173-180) the integrator uses. */
+typedef struct ne_hit {
+  float t_near, t_far;
+  float point[3];
+  float normal[3];
+  int32_t instance;  /* index into ne_scene_desc.instances, -1 on a miss */
+  int32_t primitive; /* index into ne_scene_desc.prims, -1 on a miss */
+  int32_t hit;       /* 1 when Scene::intersectScene returned true */
+  int32_t pad;
+} ne_hit;
+
+/* ne_render_params.flags */
+#define NE_RENDER_OUT_DEVICE (1u << 0)   /* out_rgb is device memory */
+#define NE_RENDER_REF_TILES (1u << 1)    /* render only the 40x10 tile grid the reference covers */
+#define NE_RENDER_COUNT_WORK (1u << 2)   /* count density lookups and scene queries (slower) */
+#define NE_RENDER_NO_SYNC (1u << 3)      /* return after enqueueing; stats carry no timings */
+
+typedef struct ne_render_params {
+  uint64_t seed;
+  int32_t spp;            /* <= 0: SceneSettings::spp */
+  int32_t bounces;        /* < 0: SceneSettings::bounces */
+  int32_t rr;             /* < 0: scene setting, 0: off, 1: on */
+  int32_t rr_after;       /* used when rr == 1 */
+  uint32_t sample_offset; /* index of the first sample (progressive rendering) */
+  uint32_t flags;
+} ne_render_params;
+
+typedef struct ne_render_stats {
+  double kernel_ms;           /* CUDA-event time of the path kernel */
+  double total_ms;            /* CUDA-event time of the whole call, copies included */
+  uint64_t paths;             /* camera paths traced */
+  uint64_t density_lookups;   /* trilinear density lookups (NE_RENDER_COUNT_WORK) */
+  uint64_t scene_queries;     /* Scene::intersectScene calls (NE_RENDER_COUNT_WORK) */
+  uint64_t bvh_nodes;         /* BVH nodes visited (NE_RENDER_COUNT_WORK) */
+  uint64_t prim_tests;        /* primitive intersection tests (NE_RENDER_COUNT_WORK) */
+  uint32_t kernel_launches;   /* kernels this call launched */
+  uint32_t pad;
+} ne_render_stats;
+
+/* ---- host-side scene description (no GPU needed) ---- */
+
+/* Parses a reference JSON scene descriptor (SceneReader semantics). resources_dir
+ * plays the role of RESOURCES_DIR for relative asset paths (.vol grids). */
+ne_status ne_scene_host_load_json(const char* path, const char* resources_dir, ne_scene_host** out,
+                                  char* err, size_t err_len);
+ne_status ne_scene_host_load_json_string(const char* json, const char* resources_dir, ne_scene_host** out,
+                                         char* err, size_t err_len);
+const ne_scene_desc* ne_scene_host_desc(const ne_scene_host* s);
+void ne_scene_host_destroy(ne_scene_host* s);
+
+/* ---- device ---- */
+
+ne_status ne_context_create(int device, ne_context** out);
+void ne_context_destroy(ne_context* ctx);
+const char* ne_last_error(const ne_context* ctx);
+
+/* Copies a scene description to the device (grids, primitives, BVHs). */
+ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene** out);
+void ne_scene_destroy(ne_scene* scene);
+
+/* Renders every pixel (or the reference's tile grid) and writes the per-pixel mean
+ * radiance, before tone mapping, as width*height*3 floats, pixel y*width+x. */
+ne_status ne_render(ne_scene* scene, const ne_render_params* params, float* out_rgb, ne_render_stats* stats);
+
+/* Camera path per key: camera ray (draws 0-3) then Li (draws from 4). out_L: n*3 floats. */
+ne_status ne_trace_paths(ne_scene* scene, const ne_render_params* params, const ne_path_key* keys, size_t n,
+                         float* out_L);
+
+/* Integrator::Li for n given rays; draw numbering of each path starts at first_dim. */
+ne_status ne_li_batch(ne_scene* scene, const ne_render_params* params, const ne_ray* rays,
+                      const ne_path_key* keys, size_t n, uint32_t first_dim, float* out_L);
+
+/* Scene::intersectScene for n rays with the given tMin/tMax. */
+ne_status ne_trace_closest(ne_scene* scene, const ne_ray* rays, size_t n, float t_min, float t_max,
+                           ne_hit* out);
+
+/* Device copies of the shared elementary functions, for bit-exactness checks.
+ * fn: 0 log, 1 exp, 2 sin, 3 cos, 4 acos, 5 pow5. */
+ne_status ne_debug_fmath(ne_context* ctx, int fn, const float* x, size_t n, float* out);
+
+/* Device copy of the shared counter-based generator: u01 for (seed, pixel, sample, dim). */
+ne_status ne_debug_rng(ne_context* ctx, uint64_t seed, const ne_path_key* keys, const uint32_t* dims, size_t n,
+                       float* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NARVAL_GB300_H_ */

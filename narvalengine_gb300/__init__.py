@@ -1,0 +1,329 @@
+"""GB300 path integrator for NarvalEngine scenes.
+
+Python face of libnarval_gb300.so (include/narval_gb300.h). The classes mirror the
+reference's render interface:
+
+  SceneReader(path)                  io/SceneReader.cpp:10-54   -> scene, camera, settings
+  VolumetricPathIntegrator.Li(...)   integrators/Integrator.h:13-25 (batched: li_batch)
+  OfflineEngine(scene).coreLoop()    core/OfflineEngine.cpp:78-146 (tone map + PPM out)
+
+All path tracing runs in the CUDA library; there is no CPU fallback. Importing this
+package needs no GPU; creating a Context does, and fails loudly without one.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _abi
+from ._abi import (NE_RENDER_COUNT_WORK, NE_RENDER_NO_SYNC, NE_RENDER_OUT_DEVICE, NE_RENDER_REF_TILES,
+                   NeHit, NePathKey, NeRay, NeRenderParams, NeRenderStats)
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG_DIR, "libnarval_gb300.so")
+SCENES_DIR = os.path.join(PKG_DIR, "scenes")
+
+_lib = None
+
+
+class NarvalError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"status {status}: {message}")
+        self.status = status
+
+
+def library() -> C.CDLL:
+    """Loads libnarval_gb300.so (built in-tree by __graft_entry__.build())."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build the CUDA library first (__graft_entry__.build())")
+        lib = C.CDLL(LIB_PATH)
+        for name, (res, args) in _abi.SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def _ptr(a: np.ndarray) -> C.c_void_p:
+    return C.c_void_p(a.ctypes.data)
+
+
+class SceneHost:
+    """A parsed scene descriptor (host memory), the reference's SceneReader result."""
+
+    def __init__(self, handle: C.c_void_p):
+        self._h = handle
+        self.desc = library().ne_scene_host_desc(self._h).contents
+
+    @classmethod
+    def from_json(cls, path: str, resources_dir: str | None = None) -> "SceneHost":
+        lib = library()
+        h = C.c_void_p()
+        err = C.create_string_buffer(1024)
+        rd = resources_dir if resources_dir is not None else os.path.dirname(os.path.abspath(path))
+        st = lib.ne_scene_host_load_json(path.encode(), rd.encode(), C.byref(h), err, len(err))
+        if st != 0:
+            raise NarvalError(st, err.value.decode())
+        return cls(h)
+
+    @classmethod
+    def from_string(cls, text: str, resources_dir: str = "") -> "SceneHost":
+        lib = library()
+        h = C.c_void_p()
+        err = C.create_string_buffer(1024)
+        st = lib.ne_scene_host_load_json_string(text.encode(), resources_dir.encode(), C.byref(h), err, len(err))
+        if st != 0:
+            raise NarvalError(st, err.value.decode())
+        return cls(h)
+
+    @property
+    def desc_ptr(self):
+        return library().ne_scene_host_desc(self._h)
+
+    @property
+    def width(self) -> int:
+        return self.desc.settings.width
+
+    @property
+    def height(self) -> int:
+        return self.desc.settings.height
+
+    @property
+    def spp(self) -> int:
+        return self.desc.settings.spp
+
+    @property
+    def bounces(self) -> int:
+        return self.desc.settings.bounces
+
+    def camera_dict(self) -> dict:
+        c = self.desc.camera
+        return {k: list(getattr(c, k)) for k in ("position", "lower_left", "horizontal", "vertical", "side", "up")} | {
+            "lens_radius": c.lens_radius}
+
+    def close(self):
+        if self._h:
+            library().ne_scene_host_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def render_params(seed: int = 0, spp: int | None = None, bounces: int | None = None, rr: int | None = None,
+                  rr_after: int = 3, sample_offset: int = 0, flags: int = 0) -> NeRenderParams:
+    p = NeRenderParams()
+    p.seed = seed
+    p.spp = spp if spp is not None else 0
+    p.bounces = bounces if bounces is not None else -1
+    p.rr = rr if rr is not None else -1
+    p.rr_after = rr_after
+    p.sample_offset = sample_offset
+    p.flags = flags
+    return p
+
+
+class Context:
+    """One CUDA device and stream (ne_context)."""
+
+    def __init__(self, device: int = 0):
+        lib = library()
+        h = C.c_void_p()
+        st = lib.ne_context_create(device, C.byref(h))
+        if st != 0:
+            raise NarvalError(st, "ne_context_create failed (no CUDA device?)")
+        self._h = h
+
+    def error(self) -> str:
+        return library().ne_last_error(self._h).decode()
+
+    def check(self, st: int):
+        if st != 0:
+            raise NarvalError(st, self.error())
+
+    def upload(self, host: SceneHost) -> "Scene":
+        h = C.c_void_p()
+        self.check(library().ne_scene_upload(self._h, host.desc_ptr, C.byref(h)))
+        return Scene(self, h, host)
+
+    def fmath(self, fn: int, x: np.ndarray) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        out = np.empty_like(x)
+        self.check(library().ne_debug_fmath(self._h, fn, _ptr(x), x.size, _ptr(out)))
+        return out
+
+    def rng(self, seed: int, keys: np.ndarray, dims: np.ndarray) -> np.ndarray:
+        keys = np.ascontiguousarray(keys, dtype=np.uint32)
+        dims = np.ascontiguousarray(dims, dtype=np.uint32)
+        out = np.empty(len(dims), dtype=np.float32)
+        self.check(library().ne_debug_rng(self._h, seed, _ptr(keys), _ptr(dims), len(dims), _ptr(out)))
+        return out
+
+    def close(self):
+        if self._h:
+            library().ne_context_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Scene:
+    """A scene resident on the device (ne_scene)."""
+
+    def __init__(self, ctx: Context, handle: C.c_void_p, host: SceneHost):
+        self.ctx = ctx
+        self._h = handle
+        self.host = host
+
+    def render(self, params: NeRenderParams | None = None, out: np.ndarray | None = None, **kw):
+        """Per-pixel mean radiance (H, W, 3) float32 before tone mapping, and the stats."""
+        p = params if params is not None else render_params(**kw)
+        W, H = self.host.width, self.host.height
+        if p.flags & NE_RENDER_OUT_DEVICE:
+            if out is None:
+                raise ValueError("NE_RENDER_OUT_DEVICE needs a device pointer in out")
+            ptr = C.c_void_p(int(out))
+            img = None
+        else:
+            img = out if out is not None else np.empty((H, W, 3), dtype=np.float32)
+            ptr = _ptr(img)
+        stats = NeRenderStats()
+        self.ctx.check(library().ne_render(self._h, C.byref(p), ptr, C.byref(stats)))
+        return img, {f: getattr(stats, f) for f, _ in NeRenderStats._fields_ if f != "pad"}
+
+    def trace_paths(self, keys: np.ndarray, params: NeRenderParams | None = None, **kw) -> np.ndarray:
+        """Camera path radiance for (pixel, sample) keys, shape (n, 3)."""
+        p = params if params is not None else render_params(**kw)
+        keys = np.ascontiguousarray(keys, dtype=np.uint32).reshape(-1, 2)
+        out = np.empty((len(keys), 3), dtype=np.float32)
+        self.ctx.check(library().ne_trace_paths(self._h, C.byref(p), _ptr(keys), len(keys), _ptr(out)))
+        return out
+
+    def li_batch(self, rays: np.ndarray, keys: np.ndarray, first_dim: int = 0,
+                 params: NeRenderParams | None = None, **kw) -> np.ndarray:
+        """Integrator::Li for rays (n, 6) = origin, direction."""
+        p = params if params is not None else render_params(**kw)
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 6)
+        keys = np.ascontiguousarray(keys, dtype=np.uint32).reshape(-1, 2)
+        out = np.empty((len(rays), 3), dtype=np.float32)
+        self.ctx.check(library().ne_li_batch(self._h, C.byref(p), _ptr(rays), _ptr(keys), len(rays), first_dim,
+                                             _ptr(out)))
+        return out
+
+    def trace_closest(self, rays: np.ndarray, t_min: float = 1e-11, t_max: float = float("inf")) -> np.ndarray:
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 6)
+        out = (NeHit * len(rays))()
+        self.ctx.check(library().ne_trace_closest(self._h, _ptr(rays), len(rays), t_min, t_max, C.addressof(out)))
+        return hits_to_numpy(out)
+
+    def close(self):
+        if self._h:
+            library().ne_scene_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+HIT_DTYPE = np.dtype([("t_near", np.float32), ("t_far", np.float32), ("point", np.float32, 3),
+                      ("normal", np.float32, 3), ("instance", np.int32), ("primitive", np.int32),
+                      ("hit", np.int32), ("pad", np.int32)])
+
+
+def hits_to_numpy(arr) -> np.ndarray:
+    buf = (C.c_char * C.sizeof(arr)).from_address(C.addressof(arr))
+    return np.frombuffer(bytes(buf), dtype=HIT_DTYPE).copy()
+
+
+# ---------------------------------------------------------------- output stage
+def tone_map(hdr: np.ndarray) -> np.ndarray:
+    """OfflineEngine::postProcessing (core/OfflineEngine.cpp:39-52): exposure 0.5, gamma 2.2, clamp."""
+    mapped = np.float32(1.0) - np.exp(-hdr.astype(np.float32) * np.float32(0.5))
+    mapped = np.power(mapped, np.float32(1.0 / 2.2))
+    return np.clip(mapped, 0.0, 1.0).astype(np.float32)
+
+
+def write_ppm(path: str, ldr: np.ndarray) -> None:
+    """16-bit P6 in the reference's order: pixels written from the last to the first
+    (core/OfflineEngine.cpp:80-138), each channel truncated to uint16 big-endian."""
+    H, W, _ = ldr.shape
+    flat = ldr.reshape(-1, 3)[::-1]
+    vals = (flat * np.float32(65535)).astype(np.uint16)
+    with open(path, "wb") as f:
+        f.write(f"P6\n{W} {H}\n65535\n".encode())
+        f.write(vals.astype(">u2").tobytes())
+
+
+# ---------------------------------------------------------------- reference-shaped interface
+class SceneReader:
+    """io/SceneReader.h:51-54: loadScene(path) then getScene/getMainCamera/getSettings."""
+
+    def __init__(self, path: str | None = None, resources_dir: str | None = None):
+        self.host = None
+        if path:
+            self.loadScene(path, resources_dir)
+
+    def loadScene(self, path: str, resources_dir: str | None = None):
+        self.host = SceneHost.from_json(path, resources_dir)
+
+    def getScene(self) -> SceneHost:
+        return self.host
+
+    def getMainCamera(self) -> dict:
+        return self.host.camera_dict()
+
+    def getSettings(self) -> dict:
+        s = self.host.desc.settings
+        return {"resolution": (s.width, s.height), "spp": s.spp, "bounces": s.bounces, "hdr": bool(s.hdr)}
+
+
+class VolumetricPathIntegrator:
+    """integrators/VolumetricPathIntegrator.h: Li(ray, scene) on the GPU, batched."""
+
+    def __init__(self, scene: Scene, seed: int = 0):
+        self.scene = scene
+        self.seed = seed
+
+    def Li(self, rays: np.ndarray, keys: np.ndarray, first_dim: int = 0) -> np.ndarray:
+        return self.scene.li_batch(rays, keys, first_dim, seed=self.seed)
+
+    def clone(self) -> "VolumetricPathIntegrator":
+        return VolumetricPathIntegrator(self.scene, self.seed)
+
+
+class OfflineEngine:
+    """core/OfflineEngine.h:169-193: renders the scene's settings and writes output.ppm."""
+
+    def __init__(self, scene: Scene, seed: int = 0, ref_tiles: bool = True):
+        self.scene = scene
+        self.seed = seed
+        self.ref_tiles = ref_tiles
+        self.pixels = None
+
+    def coreLoop(self, path: str = "output.ppm") -> dict:
+        flags = NE_RENDER_REF_TILES if self.ref_tiles else 0
+        hdr, stats = self.scene.render(seed=self.seed, flags=flags)
+        self.pixels = tone_map(hdr)
+        write_ppm(path, self.pixels)
+        return stats
+
+
+__all__ = ["Context", "Scene", "SceneHost", "SceneReader", "VolumetricPathIntegrator", "OfflineEngine",
+           "NarvalError", "render_params", "tone_map", "write_ppm", "library", "SCENES_DIR",
+           "NE_RENDER_OUT_DEVICE", "NE_RENDER_REF_TILES", "NE_RENDER_COUNT_WORK", "NE_RENDER_NO_SYNC",
+           "NeRay", "NePathKey"]

@@ -1,0 +1,777 @@
+// C ABI of the GB300 path integrator: contexts, scene upload and the path kernels.
+//
+// Kernels (all sm_103a, one CUDA stream per context):
+//  k_paths      persistent camera-path kernel: warps take 32 consecutive (pixel, sample)
+//               work items at a time from a global counter, trace camera ray + Li
+//               (core/OfflineEngine.cpp:61-68) and store each path's radiance.
+//  k_reduce     per-pixel mean over its samples in sample order (OfflineEngine.cpp:63-70),
+//               so the image is the same sum the reference forms.
+//  k_li         Integrator::Li for caller rays (integrators/Integrator.h:13-25).
+//  k_closest    Scene::intersectScene (core/Scene.cpp:30-56).
+//  k_cells      builds the 8-corner cell layout of a density grid at upload.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "narval_gb300.h"
+#include "kernels.cuh"
+
+using namespace nedev;
+
+struct ne_context {
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  std::string err;
+  unsigned long long* d_counter = nullptr;  // [0] work counter, [1..4] work counters
+  uint32_t* d_err = nullptr;
+};
+
+struct ne_scene {
+  ne_context* ctx = nullptr;
+  DScene d;
+  ne_settings settings;
+  std::vector<void*> allocs;
+  float* d_paths = nullptr;  // per-path radiance scratch of ne_render
+  size_t paths_cap = 0;
+  int blocks_per_sm = 1;
+};
+
+namespace {
+
+ne_status fail(ne_context* c, ne_status code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+ne_status cudaFail(ne_context* c, cudaError_t e, const char* where) {
+  return fail(c, e == cudaErrorMemoryAllocation ? NE_ERR_OUT_OF_MEMORY : NE_ERR_CUDA,
+              std::string(where) + ": " + cudaGetErrorString(e));
+}
+#define NE_CUDA(call, where)                          \
+  do {                                                \
+    cudaError_t e_ = (call);                          \
+    if (e_ != cudaSuccess) return cudaFail(ctx, e_, where); \
+  } while (0)
+
+template <class T>
+ne_status upload(ne_scene* sc, const T* host, size_t n, const T** out) {
+  ne_context* ctx = sc->ctx;
+  *out = nullptr;
+  if (n == 0) return NE_OK;
+  void* p = nullptr;
+  NE_CUDA(cudaMalloc(&p, n * sizeof(T)), "cudaMalloc");
+  sc->allocs.push_back(p);
+  NE_CUDA(cudaMemcpyAsync(p, host, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream), "cudaMemcpyAsync");
+  *out = (const T*)p;
+  return NE_OK;
+}
+
+// ---- host helpers shared by the upload (same arithmetic as the integrator's host side)
+struct H3 {
+  float x, y, z;
+};
+inline H3 h3(float x, float y, float z) { return H3{x, y, z}; }
+inline H3 hsub(H3 a, H3 b) { return h3(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline H3 hmul(H3 a, float s) { return h3(a.x * s, a.y * s, a.z * s); }
+inline H3 hdiv(H3 a, float s) { return h3(a.x / s, a.y / s, a.z / s); }
+inline H3 hadd(H3 a, H3 b) { return h3(a.x + b.x, a.y + b.y, a.z + b.z); }
+inline float hdot(H3 a, H3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+inline float hlen(H3 a) { return nefm::fsqrt(hdot(a, a)); }
+inline float hmin(float a, float b) { return (b < a) ? b : a; }
+inline float hmax(float a, float b) { return (a < b) ? b : a; }
+inline H3 hvmin(H3 a, H3 b) { return h3(hmin(a.x, b.x), hmin(a.y, b.y), hmin(a.z, b.z)); }
+inline H3 hvmax(H3 a, H3 b) { return h3(hmax(a.x, b.x), hmax(a.y, b.y), hmax(a.z, b.z)); }
+inline float hcomp(H3 a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }
+
+// utils/Math.h:874-912 getScale: scale part of glm's decomposition.
+H3 getScale(const float* t) {
+  float w = t[15];
+  H3 r0 = h3(t[0] / w, t[1] / w, t[2] / w);
+  H3 r1 = h3(t[4] / w, t[5] / w, t[6] / w);
+  H3 r2 = h3(t[8] / w, t[9] / w, t[10] / w);
+  H3 s;
+  s.x = hlen(r0);
+  r0 = hdiv(hmul(r0, 1.0f), hlen(r0));
+  float skz = hdot(r0, r1);
+  r1 = hadd(hmul(r1, 1.0f), hmul(r0, -skz));
+  s.y = hlen(r1);
+  r1 = hdiv(hmul(r1, 1.0f), hlen(r1));
+  float sky = hdot(r0, r2);
+  r2 = hadd(hmul(r2, 1.0f), hmul(r0, -sky));
+  float skx = hdot(r1, r2);
+  r2 = hadd(hmul(r2, 1.0f), hmul(r1, -skx));
+  s.z = hlen(r2);
+  return s;
+}
+
+struct HNode {
+  H3 mn, mx;
+  uint32_t start, count, rightOffset;
+};
+
+void triBounds(const ne_primitive& p, H3& mn, H3& mx) {
+  H3 a = h3(p.p0[0], p.p0[1], p.p0[2]), b = h3(p.p1[0], p.p1[1], p.p1[2]), c = h3(p.p2[0], p.p2[1], p.p2[2]);
+  mn = hvmin(a, hvmin(b, c));
+  mx = hvmax(a, hvmax(b, c));
+}
+inline H3 boxCenter(H3 mn, H3 mx) { return hsub(mx, hdiv(hsub(mx, mn), 2.0f)); }
+
+// primitives/BVH.cpp:6-106 BVH::init: depth-first node order, left child = i + 1,
+// right child = i + rightOffset, leaves of <= 4 triangles, midpoint split on the
+// longest axis of the centroid bounds with a median fallback.
+void buildBvh(const ne_primitive* prims, std::vector<uint32_t>& order, std::vector<HNode>& nodes) {
+  const uint32_t perLeaf = 4, notVisited = 0xffffffffu, visitedTwice = 0xfffffffdu, rootParent = 0xfffffffcu;
+  struct Item { uint32_t parent, start, end; };
+  nodes.assign(order.size() * 2 + 1, HNode{});
+  std::vector<Item> stack;
+  uint32_t nodeCount = 0;
+  stack.push_back(Item{rootParent, 0, (uint32_t)order.size()});
+  const float inf = INFINITY;
+  while (!stack.empty()) {
+    Item it = stack.back();
+    stack.pop_back();
+    nodeCount++;
+    HNode node;
+    node.start = it.start;
+    node.count = it.end - it.start;
+    node.rightOffset = notVisited;
+    H3 bbMin = h3(inf, inf, inf), bbMax = h3(-inf, -inf, -inf), pmn, pmx;
+    triBounds(prims[order[node.start]], pmn, pmx);
+    bbMin = hvmin(bbMin, pmn);
+    bbMax = hvmax(bbMax, pmx);
+    H3 bcMin = boxCenter(bbMin, bbMax), bcMax = bcMin;
+    for (uint32_t i = it.start + 1; i < it.end; i++) {
+      triBounds(prims[order[i]], pmn, pmx);
+      bbMin = hvmin(bbMin, pmn);
+      bbMax = hvmax(bbMax, pmx);
+      H3 c = boxCenter(pmn, pmx);
+      bcMin = hvmin(bcMin, c);
+      bcMax = hvmax(bcMax, c);
+    }
+    node.mn = bbMin;
+    node.mx = bbMax;
+    if (node.count <= perLeaf) node.rightOffset = 0;
+    nodes[nodeCount - 1] = node;
+    if (it.parent != rootParent) {
+      nodes[it.parent].rightOffset--;
+      if (nodes[it.parent].rightOffset == visitedTwice) nodes[it.parent].rightOffset = nodeCount - 1 - it.parent;
+    }
+    if (node.rightOffset == 0) continue;
+    H3 ext = hsub(bcMax, bcMin);
+    int dim = 0;
+    if (hcomp(ext, 1) > hcomp(ext, dim)) dim = 1;
+    if (hcomp(ext, 2) > hcomp(ext, dim)) dim = 2;
+    float split = 0.5f * (hcomp(bcMin, dim) + hcomp(bcMax, dim));
+    uint32_t mid = it.start;
+    for (uint32_t i = it.start; i < it.end; i++) {
+      triBounds(prims[order[i]], pmn, pmx);
+      if (hcomp(boxCenter(pmn, pmx), dim) < split) {
+        std::swap(order[i], order[mid]);
+        mid++;
+      }
+    }
+    if (mid == it.start || mid == it.end) mid = it.start + (it.end - it.start) / 2;
+    stack.push_back(Item{nodeCount - 1, mid, it.end});
+    stack.push_back(Item{nodeCount - 1, it.start, mid});
+  }
+  nodes.resize(nodeCount);
+}
+
+// ---------------------------------------------------------------- kernels
+__global__ void k_cells(const float* __restrict__ grid, uint32_t W, uint32_t H, uint32_t D, float4* __restrict__ cells) {
+  size_t n = (size_t)(W + 1) * (H + 1) * (D + 1);
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    uint32_t x = (uint32_t)(i % (W + 1));
+    uint32_t y = (uint32_t)((i / (W + 1)) % (H + 1));
+    uint32_t z = (uint32_t)(i / ((size_t)(W + 1) * (H + 1)));
+    auto den = [&](uint32_t a, uint32_t b, uint32_t c) -> float {
+      if (a >= W || b >= H || c >= D) return 0.0f;
+      return grid[(size_t)H * W * c + (size_t)W * b + a];
+    };
+    cells[2 * i] = make_float4(den(x, y, z), den(x + 1, y, z), den(x, y + 1, z), den(x + 1, y + 1, z));
+    cells[2 * i + 1] = make_float4(den(x, y, z + 1), den(x + 1, y, z + 1), den(x, y + 1, z + 1), den(x + 1, y + 1, z + 1));
+  }
+}
+
+// Per-pixel mean in sample order: color += Li for s = 0..spp-1, then color / spp.
+__global__ void k_reduce(const float* __restrict__ paths, uint32_t n_pix, uint32_t spp, uint32_t cover_w, int W,
+                         float* __restrict__ out) {
+  for (uint32_t pi = blockIdx.x * blockDim.x + threadIdx.x; pi < n_pix; pi += gridDim.x * blockDim.x) {
+    const float* p = paths + (size_t)pi * spp * 3;
+    float r = 0, g = 0, b = 0;
+    for (uint32_t k = 0; k < spp; k++) {
+      r = r + p[3 * k + 0];
+      g = g + p[3 * k + 1];
+      b = b + p[3 * k + 2];
+    }
+    float fs = (float)spp;
+    size_t pixel = (size_t)(pi / cover_w) * (size_t)W + (pi % cover_w);
+    out[3 * pixel + 0] = r / fs;
+    out[3 * pixel + 1] = g / fs;
+    out[3 * pixel + 2] = b / fs;
+  }
+}
+
+__global__ void k_fmath(int fn, const float* __restrict__ x, size_t n, float* __restrict__ out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    float v = x[i], r;
+    switch (fn) {
+      case 0: r = nefm::log(v); break;
+      case 1: r = nefm::exp(v); break;
+      case 2: r = nefm::sin(v); break;
+      case 3: r = nefm::cos(v); break;
+      case 4: r = nefm::acos(v); break;
+      default: r = nefm::pow5(v); break;
+    }
+    out[i] = r;
+  }
+}
+
+__global__ void k_rng(nerng::PathKey base, const ne_path_key* __restrict__ keys, const uint32_t* __restrict__ dims,
+                      size_t n, float* __restrict__ out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    nerng::PathKey k = base;
+    k.pixel = keys[i].pixel;
+    k.sample = keys[i].sample;
+    out[i] = nerng::u01(k, dims[i]);
+  }
+}
+
+PathParams pathParams(const ne_scene* sc, const ne_render_params* p) {
+  PathParams P;
+  P.bounces = (p && p->bounces >= 0) ? p->bounces : sc->settings.bounces;
+  int rr = (p && p->rr >= 0) ? p->rr : sc->settings.rr_enabled;
+  P.rr = rr;
+  P.rr_after = (p && p->rr >= 0) ? p->rr_after : sc->settings.rr_after;
+  return P;
+}
+nerng::PathKey baseKey(const ne_render_params* p) {
+  uint64_t seed = p ? p->seed : 0;
+  nerng::PathKey k;
+  k.seed_lo = (uint32_t)seed;
+  k.seed_hi = (uint32_t)(seed >> 32);
+  k.pixel = 0;
+  k.sample = 0;
+  k.stream = 0;
+  return k;
+}
+
+ne_status checkErr(ne_context* ctx) {
+  uint32_t e = 0;
+  NE_CUDA(cudaMemcpyAsync(&e, ctx->d_err, 4, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync(err)");
+  NE_CUDA(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  if (e & ERR_BVH_STACK) return fail(ctx, NE_ERR_UNSUPPORTED, "BVH traversal stack exceeded 64 entries");
+  return NE_OK;
+}
+
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+};
+
+int persistentBlocks(ne_scene* sc) { return sc->ctx->sm_count * sc->blocks_per_sm; }
+
+ne_status launchPaths(ne_scene* sc, const PathArgs& a, bool count) {
+  ne_context* ctx = sc->ctx;
+  NE_CUDA(cudaMemsetAsync(ctx->d_counter, 0, 5 * sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync");
+  int blocks = persistentBlocks(sc);
+  unsigned long long needed = (a.total + kThreads - 1) / kThreads;
+  if ((unsigned long long)blocks > needed) blocks = (int)std::max<unsigned long long>(1, needed);
+  NE_CUDA(ne_launch_paths(count, blocks, ctx->stream, sc->d, a, ctx->d_counter, ctx->d_err), "k_paths launch");
+  return NE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+ne_status ne_context_create(int device, ne_context** out) {
+  if (!out) return NE_ERR_INVALID_ARG;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return NE_ERR_NO_DEVICE;
+  }
+  if (device < 0 || device >= n) return NE_ERR_INVALID_ARG;
+  ne_context* ctx = new ne_context();
+  ctx->device = device;
+  auto bad = [&](cudaError_t e, const char* w) {
+    ne_status st = cudaFail(ctx, e, w);
+    ne_context_destroy(ctx);
+    return st;
+  };
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) return bad(e, "cudaSetDevice");
+  e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+  if (e != cudaSuccess) return bad(e, "cudaDeviceGetAttribute");
+  e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return bad(e, "cudaStreamCreate");
+  for (int i = 0; i < 4; i++) {
+    e = cudaEventCreate(&ctx->ev[i]);
+    if (e != cudaSuccess) return bad(e, "cudaEventCreate");
+  }
+  e = cudaMalloc(&ctx->d_counter, 8 * sizeof(unsigned long long));
+  if (e != cudaSuccess) return bad(e, "cudaMalloc");
+  e = cudaMalloc(&ctx->d_err, sizeof(uint32_t));
+  if (e != cudaSuccess) return bad(e, "cudaMalloc");
+  e = cudaMemset(ctx->d_err, 0, sizeof(uint32_t));
+  if (e != cudaSuccess) return bad(e, "cudaMemset");
+  *out = ctx;
+  return NE_OK;
+}
+
+void ne_context_destroy(ne_context* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  for (int i = 0; i < 4; i++)
+    if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+  if (ctx->d_counter) cudaFree(ctx->d_counter);
+  if (ctx->d_err) cudaFree(ctx->d_err);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+const char* ne_last_error(const ne_context* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene** out) {
+  if (!ctx || !desc || !out) return NE_ERR_INVALID_ARG;
+  *out = nullptr;
+  const ne_scene_desc& D = *desc;
+  uint32_t ninst = D.n_instances + D.n_light_instances;
+  if (D.settings.width <= 0 || D.settings.height <= 0) return fail(ctx, NE_ERR_INVALID_ARG, "scene has no resolution");
+  // validate indices so that no kernel reads out of bounds
+  for (uint32_t i = 0; i < ninst; i++)
+    if (D.instances[i].model >= D.n_models) return fail(ctx, NE_ERR_INVALID_ARG, "instance model index out of range");
+  for (uint32_t i = 0; i < D.n_models; i++) {
+    const ne_model& m = D.models[i];
+    if ((uint64_t)m.prim_begin + m.prim_count > D.n_prims || (uint64_t)m.light_begin + m.light_count > D.n_prims ||
+        (uint64_t)m.mat_begin + m.mat_count > D.n_model_materials)
+      return fail(ctx, NE_ERR_INVALID_ARG, "model ranges out of range");
+    for (uint32_t k = 0; k < m.light_count; k++) {
+      int mat = D.prims[m.light_begin + k].material;
+      if (mat < 0 || mat >= (int)D.n_materials || D.materials[mat].light < 0)
+        return fail(ctx, NE_ERR_INVALID_ARG, "emissive primitive without a light material");
+    }
+    for (uint32_t k = 0; k < m.prim_count; k++)
+      if (m.use_bvh && D.prims[m.prim_begin + k].type != NE_PRIM_TRIANGLE)
+        return fail(ctx, NE_ERR_INVALID_ARG, "BVH models hold triangles only");
+  }
+  for (uint32_t i = 0; i < D.n_light_instances; i++) {
+    const ne_model& m = D.models[D.instances[D.n_instances + i].model];
+    for (uint32_t k = 0; k < m.mat_count; k++) {
+      uint32_t mm = D.model_materials[m.mat_begin + k];
+      if (mm >= D.n_materials || D.materials[mm].light < 0)
+        return fail(ctx, NE_ERR_INVALID_ARG, "light instance material without a light");
+    }
+  }
+  for (uint32_t i = 0; i < D.n_prims; i++) {
+    int mat = D.prims[i].material;
+    if (mat >= (int)D.n_materials) return fail(ctx, NE_ERR_INVALID_ARG, "primitive material out of range");
+    if (D.prims[i].type < 0 || D.prims[i].type > NE_PRIM_POINT) return fail(ctx, NE_ERR_INVALID_ARG, "bad primitive type");
+  }
+  for (uint32_t i = 0; i < D.n_materials; i++) {
+    const ne_material& m = D.materials[i];
+    if (m.light >= (int)D.n_lights || m.medium >= (int)D.n_media) return fail(ctx, NE_ERR_INVALID_ARG, "material index out of range");
+    if (m.bsdf == NE_BSDF_VOLUME && m.medium < 0) return fail(ctx, NE_ERR_INVALID_ARG, "volume material without a medium");
+  }
+  for (uint32_t i = 0; i < D.n_lights; i++)
+    if (D.lights[i].primitive >= (int)D.n_prims) return fail(ctx, NE_ERR_INVALID_ARG, "light primitive out of range");
+  // every light reachable from a light instance is sampled through Light::primitive
+  for (uint32_t i = 0; i < D.n_light_instances; i++) {
+    const ne_model& m = D.models[D.instances[D.n_instances + i].model];
+    for (uint32_t k = 0; k < m.light_count; k++) {
+      const ne_light& L = D.lights[D.materials[D.prims[m.light_begin + k].material].light];
+      if (L.primitive < 0) return fail(ctx, NE_ERR_INVALID_ARG, "light without a primitive");
+    }
+  }
+
+  NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  ne_scene* sc = new ne_scene();
+  sc->ctx = ctx;
+  sc->settings = D.settings;
+  memset(&sc->d, 0, sizeof(sc->d));
+  auto cleanup = [&](ne_status st) {
+    ne_scene_destroy(sc);
+    return st;
+  };
+
+  // instances
+  std::vector<DInstance> inst(ninst);
+  for (uint32_t i = 0; i < ninst; i++) {
+    const ne_instance& s = D.instances[i];
+    DInstance& d = inst[i];
+    memset(&d, 0, sizeof(d));
+    for (int c = 0; c < 4; c++)
+      for (int r = 0; r < 3; r++) {
+        d.wcs[c * 3 + r] = s.to_wcs[c * 4 + r];
+        d.ocs[c * 3 + r] = s.to_ocs[c * 4 + r];
+      }
+    H3 sc3 = getScale(s.to_wcs);
+    d.scale[0] = sc3.x; d.scale[1] = sc3.y; d.scale[2] = sc3.z;
+    d.model = s.model;
+    d.collision = s.collision;
+  }
+  // primitives
+  std::vector<DPrim> prims(D.n_prims);
+  for (uint32_t i = 0; i < D.n_prims; i++) {
+    const ne_primitive& s = D.prims[i];
+    DPrim& d = prims[i];
+    memset(&d, 0, sizeof(d));
+    d.type = s.type;
+    d.material = s.material;
+    d.radius = s.radius;
+    memcpy(d.p0, s.p0, 12); memcpy(d.p1, s.p1, 12); memcpy(d.p2, s.p2, 12);
+    if (s.type == NE_PRIM_TRIANGLE) {  // Triangle::calculateArea
+      H3 a = h3(s.p0[0], s.p0[1], s.p0[2]), b = h3(s.p1[0], s.p1[1], s.p1[2]), c = h3(s.p2[0], s.p2[1], s.p2[2]);
+      H3 e1 = hsub(b, a), e2 = hsub(c, a);
+      H3 n = h3(e1.y * e2.z - e2.y * e1.z, e1.z * e2.x - e2.z * e1.x, e1.x * e2.y - e2.x * e1.y);
+      d.area = hlen(n) / 2.0f;
+    }
+    if (s.material >= 0) {
+      const ne_material& m = D.materials[s.material];
+      if (m.medium >= 0 && D.media[m.medium].type == NE_MEDIUM_GRID) d.flags |= DPRIM_GRID_MEDIUM;
+    }
+  }
+  // models + BVHs
+  std::vector<DModel> models(D.n_models);
+  std::vector<DNode> nodes;
+  std::vector<uint32_t> slots;
+  for (uint32_t i = 0; i < D.n_models; i++) {
+    const ne_model& s = D.models[i];
+    DModel& d = models[i];
+    memset(&d, 0, sizeof(d));
+    d.prim_begin = s.prim_begin; d.prim_count = s.prim_count;
+    d.light_begin = s.light_begin; d.light_count = s.light_count;
+    d.mat_begin = s.mat_begin; d.mat_count = s.mat_count;
+    d.has_bbox = s.has_bbox;
+    memcpy(d.bbox_min, s.bbox_min, 12);
+    memcpy(d.bbox_max, s.bbox_max, 12);
+    if (s.use_bvh && s.prim_count > 0) {
+      std::vector<uint32_t> order(s.prim_count);
+      for (uint32_t k = 0; k < s.prim_count; k++) order[k] = s.prim_begin + k;
+      std::vector<HNode> hn;
+      buildBvh(D.prims, order, hn);
+      d.use_bvh = 1;
+      d.bvh_node0 = (uint32_t)nodes.size();
+      d.bvh_slot0 = (uint32_t)slots.size();
+      for (const HNode& h : hn) {
+        DNode n;
+        n.lo[0] = h.mn.x; n.lo[1] = h.mn.y; n.lo[2] = h.mn.z;
+        n.hi[0] = h.mx.x; n.hi[1] = h.mx.y; n.hi[2] = h.mx.z;
+        uint32_t a, b;
+        if (h.rightOffset == 0) { a = h.start; b = h.count | 0x80000000u; }
+        else { a = h.rightOffset; b = 0; }
+        memcpy(&n.lo[3], &a, 4);
+        memcpy(&n.hi[3], &b, 4);
+        nodes.push_back(n);
+      }
+      slots.insert(slots.end(), order.begin(), order.end());
+    }
+  }
+  // materials, lights
+  std::vector<DMaterial> mats(D.n_materials);
+  for (uint32_t i = 0; i < D.n_materials; i++) {
+    const ne_material& s = D.materials[i];
+    DMaterial& d = mats[i];
+    memset(&d, 0, sizeof(d));
+    d.bsdf = s.bsdf; d.light = s.light; d.medium = s.medium; d.phase = s.phase; d.g = s.g;
+    memcpy(d.albedo, s.albedo, 12);
+    d.roughness = s.roughness; d.metallic = s.metallic;
+    memcpy(d.normal_map, s.normal_map, 12);
+    d.tex_present = s.tex_present; d.tex_types = s.tex_types;
+  }
+  std::vector<DLight> lights(D.n_lights);
+  for (uint32_t i = 0; i < D.n_lights; i++) {
+    const ne_light& s = D.lights[i];
+    DLight& d = lights[i];
+    memset(&d, 0, sizeof(d));
+    d.type = s.type; d.primitive = s.primitive;
+    memcpy(d.li, s.li, 12); memcpy(d.le, s.le, 12);
+    memcpy(d.direction, s.direction, 12); memcpy(d.env_radiance, s.env_radiance, 12);
+    d.env_map_pdf = s.env_map_pdf;
+  }
+  // media: dense grid + 8-corner cells
+  std::vector<DMedium> media(D.n_media);
+  for (uint32_t i = 0; i < D.n_media; i++) {
+    const ne_medium& s = D.media[i];
+    DMedium& d = media[i];
+    memset(&d, 0, sizeof(d));
+    d.type = s.type;
+    memcpy(d.sigma_s, s.sigma_s, 12);
+    for (int k = 0; k < 3; k++) d.sigma_t[k] = s.sigma_a[k] + s.sigma_s[k];
+    d.density = s.density;
+    // avg(extinction * densityMultiplier) (GridMedia.cpp:208)
+    float e0 = d.sigma_t[0] * s.density, e1 = d.sigma_t[1] * s.density, e2 = d.sigma_t[2] * s.density;
+    d.mu = (e0 + e1 + e2) / 3.0f;
+    d.inv_max_density = 1.0f;
+    if (s.type == NE_MEDIUM_GRID) {
+      if (!s.grid || !s.res[0] || !s.res[1] || !s.res[2]) return cleanup(fail(ctx, NE_ERR_INVALID_ARG, "grid medium without voxels"));
+      size_t n = (size_t)s.res[0] * s.res[1] * s.res[2];
+      float mx = 0;
+      for (size_t k = 0; k < n; k++) mx = (mx < s.grid[k]) ? s.grid[k] : mx;  // GridMedia.h:16-21
+      d.inv_max_density = 1.0f / mx;
+      memcpy(d.res, s.res, 12);
+      d.resf[0] = (float)s.res[0]; d.resf[1] = (float)s.res[1]; d.resf[2] = (float)s.res[2];
+      const float* dg = nullptr;
+      ne_status st = upload(sc, s.grid, n, &dg);
+      if (st) return cleanup(st);
+      d.grid = dg;
+      size_t ncell = (size_t)(s.res[0] + 1) * (s.res[1] + 1) * (s.res[2] + 1);
+      void* cp = nullptr;
+      cudaError_t e = cudaMalloc(&cp, ncell * 2 * sizeof(float4));
+      if (e != cudaSuccess) return cleanup(cudaFail(ctx, e, "cudaMalloc(cells)"));
+      sc->allocs.push_back(cp);
+      int blocks = ctx->sm_count * 8;
+      k_cells<<<blocks, 256, 0, ctx->stream>>>(dg, s.res[0], s.res[1], s.res[2], (float4*)cp);
+      e = cudaGetLastError();
+      if (e != cudaSuccess) return cleanup(cudaFail(ctx, e, "k_cells launch"));
+      d.cells = (const float4*)cp;
+    }
+  }
+  ne_status st = NE_OK;
+  if ((st = upload(sc, inst.data(), inst.size(), &sc->d.instances))) return cleanup(st);
+  if ((st = upload(sc, models.data(), models.size(), &sc->d.models))) return cleanup(st);
+  if ((st = upload(sc, prims.data(), prims.size(), &sc->d.prims))) return cleanup(st);
+  if ((st = upload(sc, mats.data(), mats.size(), &sc->d.materials))) return cleanup(st);
+  if ((st = upload(sc, D.model_materials, D.n_model_materials, &sc->d.model_materials))) return cleanup(st);
+  if ((st = upload(sc, lights.data(), lights.size(), &sc->d.lights))) return cleanup(st);
+  if ((st = upload(sc, media.data(), media.size(), &sc->d.media))) return cleanup(st);
+  if ((st = upload(sc, nodes.data(), nodes.size(), &sc->d.bvh))) return cleanup(st);
+  if ((st = upload(sc, slots.data(), slots.size(), &sc->d.bvh_prims))) return cleanup(st);
+  sc->d.n_instances = D.n_instances;
+  sc->d.n_light_instances = D.n_light_instances;
+  sc->d.n_prims = D.n_prims;
+  sc->d.n_media = D.n_media;
+  const ne_camera& cm = D.camera;
+  memcpy(sc->d.camera.position, cm.position, 12);
+  memcpy(sc->d.camera.lower_left, cm.lower_left, 12);
+  memcpy(sc->d.camera.horizontal, cm.horizontal, 12);
+  memcpy(sc->d.camera.vertical, cm.vertical, 12);
+  memcpy(sc->d.camera.side, cm.side, 12);
+  memcpy(sc->d.camera.up, cm.up, 12);
+  sc->d.camera.lens_radius = cm.lens_radius;
+  sc->d.width = D.settings.width;
+  sc->d.height = D.settings.height;
+  int bps = 1;
+  if (ne_paths_occupancy(&bps) != cudaSuccess || bps < 1) bps = 1;
+  sc->blocks_per_sm = bps;
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cleanup(cudaFail(ctx, e, "scene upload"));
+  *out = sc;
+  return NE_OK;
+}
+
+void ne_scene_destroy(ne_scene* sc) {
+  if (!sc) return;
+  cudaSetDevice(sc->ctx->device);
+  cudaStreamSynchronize(sc->ctx->stream);
+  for (void* p : sc->allocs) cudaFree(p);
+  if (sc->d_paths) cudaFree(sc->d_paths);
+  delete sc;
+}
+
+ne_status ne_render(ne_scene* sc, const ne_render_params* p, float* out_rgb, ne_render_stats* stats) {
+  if (!sc || !out_rgb) return NE_ERR_INVALID_ARG;
+  ne_context* ctx = sc->ctx;
+  NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  const int W = sc->settings.width, H = sc->settings.height;
+  int spp = (p && p->spp > 0) ? p->spp : sc->settings.spp;
+  if (spp <= 0) return fail(ctx, NE_ERR_INVALID_ARG, "spp must be positive");
+  uint32_t flags = p ? p->flags : 0;
+  uint32_t cw = (uint32_t)W, ch = (uint32_t)H;
+  if (flags & NE_RENDER_REF_TILES) {  // OfflineEngine.cpp:18-21: 40 x 10 tiles of (W/40, H/10)
+    cw = 40u * (uint32_t)(W / 40);
+    ch = 10u * (uint32_t)(H / 10);
+  }
+  uint64_t npix = (uint64_t)cw * ch;
+  uint64_t total = npix * (uint64_t)spp;
+  if (sc->paths_cap < total) {
+    if (sc->d_paths) cudaFree(sc->d_paths);
+    sc->d_paths = nullptr;
+    sc->paths_cap = 0;
+    NE_CUDA(cudaMalloc(&sc->d_paths, total * 3 * sizeof(float)), "cudaMalloc(paths)");
+    sc->paths_cap = total;
+  }
+  bool devOut = flags & NE_RENDER_OUT_DEVICE;
+  float* d_img = nullptr;
+  DevBuf<float> tmpImg;
+  size_t imgBytes = (size_t)W * H * 3 * sizeof(float);
+  if (devOut) {
+    d_img = out_rgb;
+  } else {
+    NE_CUDA(cudaMalloc(&tmpImg.p, imgBytes), "cudaMalloc(image)");
+    d_img = tmpImg.p;
+  }
+  bool timed = !(flags & NE_RENDER_NO_SYNC);
+  NE_CUDA(cudaMemsetAsync(ctx->d_err, 0, 4, ctx->stream), "cudaMemsetAsync");
+  if (timed) NE_CUDA(cudaEventRecord(ctx->ev[0], ctx->stream), "cudaEventRecord");
+  if (cw != (uint32_t)W || ch != (uint32_t)H) NE_CUDA(cudaMemsetAsync(d_img, 0, imgBytes, ctx->stream), "cudaMemsetAsync");
+  PathArgs a;
+  a.P = pathParams(sc, p);
+  a.base = baseKey(p);
+  a.total = total;
+  a.spp = (uint32_t)spp;
+  a.sample_offset = p ? p->sample_offset : 0;
+  a.cover_w = cw;
+  a.keys = nullptr;
+  a.out = sc->d_paths;
+  if (timed) NE_CUDA(cudaEventRecord(ctx->ev[1], ctx->stream), "cudaEventRecord");
+  ne_status st = launchPaths(sc, a, (flags & NE_RENDER_COUNT_WORK) != 0);
+  if (st) return st;
+  if (timed) NE_CUDA(cudaEventRecord(ctx->ev[2], ctx->stream), "cudaEventRecord");
+  int rblocks = (int)std::min<uint64_t>((npix + 255) / 256, (uint64_t)ctx->sm_count * 16);
+  k_reduce<<<std::max(1, rblocks), 256, 0, ctx->stream>>>(sc->d_paths, (uint32_t)npix, (uint32_t)spp, cw, W, d_img);
+  NE_CUDA(cudaGetLastError(), "k_reduce launch");
+  if (!devOut) NE_CUDA(cudaMemcpyAsync(out_rgb, d_img, imgBytes, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync(image)");
+  if (timed) NE_CUDA(cudaEventRecord(ctx->ev[3], ctx->stream), "cudaEventRecord");
+  if (!timed) {
+    if (stats) {
+      memset(stats, 0, sizeof(*stats));
+      stats->paths = total;
+      stats->kernel_launches = 2;
+    }
+    return NE_OK;
+  }
+  unsigned long long cnt[5] = {0, 0, 0, 0, 0};
+  NE_CUDA(cudaMemcpyAsync(cnt, ctx->d_counter, sizeof(cnt), cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync");
+  st = checkErr(ctx);
+  if (st) return st;
+  if (stats) {
+    memset(stats, 0, sizeof(*stats));
+    float kms = 0, tms = 0;
+    cudaEventElapsedTime(&kms, ctx->ev[1], ctx->ev[2]);
+    cudaEventElapsedTime(&tms, ctx->ev[0], ctx->ev[3]);
+    stats->kernel_ms = kms;
+    stats->total_ms = tms;
+    stats->paths = total;
+    stats->density_lookups = cnt[1];
+    stats->scene_queries = cnt[2];
+    stats->bvh_nodes = cnt[3];
+    stats->prim_tests = cnt[4];
+    stats->kernel_launches = 2;
+  }
+  return NE_OK;
+}
+
+ne_status ne_trace_paths(ne_scene* sc, const ne_render_params* p, const ne_path_key* keys, size_t n, float* out_L) {
+  if (!sc || (!keys && n) || (!out_L && n)) return NE_ERR_INVALID_ARG;
+  if (n == 0) return NE_OK;
+  ne_context* ctx = sc->ctx;
+  NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  uint32_t npix = (uint32_t)sc->settings.width * (uint32_t)sc->settings.height;
+  for (size_t i = 0; i < n; i++)
+    if (keys[i].pixel >= npix) return fail(ctx, NE_ERR_INVALID_ARG, "path key pixel out of range");
+  DevBuf<ne_path_key> dk;
+  DevBuf<float> dout;
+  NE_CUDA(cudaMalloc(&dk.p, n * sizeof(ne_path_key)), "cudaMalloc");
+  NE_CUDA(cudaMalloc(&dout.p, n * 3 * sizeof(float)), "cudaMalloc");
+  NE_CUDA(cudaMemcpyAsync(dk.p, keys, n * sizeof(ne_path_key), cudaMemcpyHostToDevice, ctx->stream), "cudaMemcpyAsync");
+  NE_CUDA(cudaMemsetAsync(ctx->d_err, 0, 4, ctx->stream), "cudaMemsetAsync");
+  PathArgs a;
+  a.P = pathParams(sc, p);
+  a.base = baseKey(p);
+  a.total = n;
+  a.spp = 1;
+  a.sample_offset = p ? p->sample_offset : 0;
+  a.cover_w = (uint32_t)sc->settings.width;
+  a.keys = dk.p;
+  a.out = dout.p;
+  ne_status st = launchPaths(sc, a, false);
+  if (st) return st;
+  NE_CUDA(cudaMemcpyAsync(out_L, dout.p, n * 3 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync");
+  return checkErr(ctx);
+}
+
+ne_status ne_li_batch(ne_scene* sc, const ne_render_params* p, const ne_ray* rays, const ne_path_key* keys, size_t n,
+                      uint32_t first_dim, float* out_L) {
+  if (!sc || (n && (!rays || !keys || !out_L))) return NE_ERR_INVALID_ARG;
+  if (n == 0) return NE_OK;
+  ne_context* ctx = sc->ctx;
+  NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  DevBuf<ne_ray> dr;
+  DevBuf<ne_path_key> dk;
+  DevBuf<float> dout;
+  NE_CUDA(cudaMalloc(&dr.p, n * sizeof(ne_ray)), "cudaMalloc");
+  NE_CUDA(cudaMalloc(&dk.p, n * sizeof(ne_path_key)), "cudaMalloc");
+  NE_CUDA(cudaMalloc(&dout.p, n * 3 * sizeof(float)), "cudaMalloc");
+  NE_CUDA(cudaMemcpyAsync(dr.p, rays, n * sizeof(ne_ray), cudaMemcpyHostToDevice, ctx->stream), "cudaMemcpyAsync");
+  NE_CUDA(cudaMemcpyAsync(dk.p, keys, n * sizeof(ne_path_key), cudaMemcpyHostToDevice, ctx->stream), "cudaMemcpyAsync");
+  NE_CUDA(cudaMemsetAsync(ctx->d_err, 0, 4, ctx->stream), "cudaMemsetAsync");
+  int blocks = (int)std::min<size_t>((n + kThreads - 1) / kThreads, (size_t)ctx->sm_count * 8);
+  NE_CUDA(ne_launch_li(std::max(1, blocks), ctx->stream, sc->d, pathParams(sc, p), baseKey(p), dr.p, dk.p, n, first_dim,
+                       dout.p, ctx->d_err),
+          "k_li launch");
+  NE_CUDA(cudaMemcpyAsync(out_L, dout.p, n * 3 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync");
+  return checkErr(ctx);
+}
+
+ne_status ne_trace_closest(ne_scene* sc, const ne_ray* rays, size_t n, float t_min, float t_max, ne_hit* out) {
+  if (!sc || (n && (!rays || !out))) return NE_ERR_INVALID_ARG;
+  if (n == 0) return NE_OK;
+  ne_context* ctx = sc->ctx;
+  NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  DevBuf<ne_ray> dr;
+  DevBuf<ne_hit> dh;
+  NE_CUDA(cudaMalloc(&dr.p, n * sizeof(ne_ray)), "cudaMalloc");
+  NE_CUDA(cudaMalloc(&dh.p, n * sizeof(ne_hit)), "cudaMalloc");
+  NE_CUDA(cudaMemcpyAsync(dr.p, rays, n * sizeof(ne_ray), cudaMemcpyHostToDevice, ctx->stream), "cudaMemcpyAsync");
+  NE_CUDA(cudaMemsetAsync(ctx->d_err, 0, 4, ctx->stream), "cudaMemsetAsync");
+  int blocks = (int)std::min<size_t>((n + kThreads - 1) / kThreads, (size_t)ctx->sm_count * 8);
+  NE_CUDA(ne_launch_closest(std::max(1, blocks), ctx->stream, sc->d, dr.p, n, t_min, t_max, dh.p, ctx->d_err),
+          "k_closest launch");
+  NE_CUDA(cudaMemcpyAsync(out, dh.p, n * sizeof(ne_hit), cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync");
+  return checkErr(ctx);
+}
+
+ne_status ne_debug_fmath(ne_context* ctx, int fn, const float* x, size_t n, float* out) {
+  if (!ctx || (n && (!x || !out))) return NE_ERR_INVALID_ARG;
+  if (n == 0) return NE_OK;
+  NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  DevBuf<float> dx, dy;
+  NE_CUDA(cudaMalloc(&dx.p, n * 4), "cudaMalloc");
+  NE_CUDA(cudaMalloc(&dy.p, n * 4), "cudaMalloc");
+  NE_CUDA(cudaMemcpyAsync(dx.p, x, n * 4, cudaMemcpyHostToDevice, ctx->stream), "cudaMemcpyAsync");
+  int blocks = (int)std::min<size_t>((n + 255) / 256, (size_t)ctx->sm_count * 8);
+  k_fmath<<<std::max(1, blocks), 256, 0, ctx->stream>>>(fn, dx.p, n, dy.p);
+  NE_CUDA(cudaGetLastError(), "k_fmath launch");
+  NE_CUDA(cudaMemcpyAsync(out, dy.p, n * 4, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync");
+  NE_CUDA(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  return NE_OK;
+}
+
+ne_status ne_debug_rng(ne_context* ctx, uint64_t seed, const ne_path_key* keys, const uint32_t* dims, size_t n,
+                       float* out) {
+  if (!ctx || (n && (!keys || !dims || !out))) return NE_ERR_INVALID_ARG;
+  if (n == 0) return NE_OK;
+  NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  DevBuf<ne_path_key> dk;
+  DevBuf<uint32_t> dd;
+  DevBuf<float> dy;
+  NE_CUDA(cudaMalloc(&dk.p, n * sizeof(ne_path_key)), "cudaMalloc");
+  NE_CUDA(cudaMalloc(&dd.p, n * 4), "cudaMalloc");
+  NE_CUDA(cudaMalloc(&dy.p, n * 4), "cudaMalloc");
+  NE_CUDA(cudaMemcpyAsync(dk.p, keys, n * sizeof(ne_path_key), cudaMemcpyHostToDevice, ctx->stream), "cudaMemcpyAsync");
+  NE_CUDA(cudaMemcpyAsync(dd.p, dims, n * 4, cudaMemcpyHostToDevice, ctx->stream), "cudaMemcpyAsync");
+  ne_render_params p;
+  memset(&p, 0, sizeof(p));
+  p.seed = seed;
+  int blocks = (int)std::min<size_t>((n + 255) / 256, (size_t)ctx->sm_count * 8);
+  k_rng<<<std::max(1, blocks), 256, 0, ctx->stream>>>(baseKey(&p), dk.p, dd.p, n, dy.p);
+  NE_CUDA(cudaGetLastError(), "k_rng launch");
+  NE_CUDA(cudaMemcpyAsync(out, dy.p, n * 4, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync");
+  NE_CUDA(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  return NE_OK;
+}
+
+}  // extern "C"

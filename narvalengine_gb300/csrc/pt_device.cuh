@@ -1,0 +1,1104 @@
+// Device implementation of the NarvalEngine path integrator for sm_103a.
+//
+// One function per reference function, named after it; each cites the reference
+// file:line it implements (paths relative to the reference's src/). Arithmetic keeps
+// the reference's expression order and types (float, with double where a double
+// literal such as PI or EPSILON promotes the expression) and glm's evaluation order:
+// dot = (x*x' + y*y') + z*z', mat4*vec4 = (c0 v0 + c1 v1) + (c2 v2 + c3 v3),
+// min(a,b) = b<a?b:a, max(a,b) = a<b?b:a, mix(x,y,a) = x(1-a) + y a. The file is
+// compiled with -fmad=false and IEEE division and square root, so each operation
+// rounds exactly as on the host.
+//
+// Deliberate deviations from the reference (taken identically by the CPU oracle):
+//  * random() is the counter-based generator of ne_rng.h in the reference's draw order;
+//  * libm functions are those of ne_fmath.h;
+//  * intersectTr stops when the next segment would start at the same point or after
+//    256 segments (the reference loops forever there), tracking loops stop after 2^20
+//    steps, a path ends after 2^16 medium pass-throughs (which the reference does not
+//    count as bounces), and a scene without lights contributes no direct light;
+//  * a BVH traversal stack deeper than 64 entries raises an error flag.
+#pragma once
+#include <stdint.h>
+
+#include "device_scene.h"
+#include "ne_fmath.h"
+#include "ne_rng.h"
+
+namespace nedev {
+
+#define NE_D __device__ __forceinline__
+
+constexpr double kPiD = 3.14159265358979323846264338327950288;
+constexpr double kTwoPiD = 6.283185307179586476925286766559;
+constexpr double kFourPiD = 12.566370614359172953850573533118;
+constexpr double kEpsilonD = 0.0000000001;
+constexpr float kInv4Pi = float(0.07957747154594766788);
+constexpr float kEps3F = float(0.001);
+constexpr float kEps12F = float(0.00000000001);
+constexpr int kMaxTrackSteps = 1 << 20;
+constexpr int kMaxTrSegments = 256;
+constexpr int kMaxPassThrough = 1 << 16;
+constexpr int kBvhStack = 64;
+
+enum : uint32_t { ERR_BVH_STACK = 1u };
+
+// ---------------------------------------------------------------- vectors
+struct V3 {
+  float x, y, z;
+};
+NE_D V3 v3(float x, float y, float z) { return V3{x, y, z}; }
+NE_D V3 operator+(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+NE_D V3 operator-(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+NE_D V3 operator*(V3 a, V3 b) { return v3(a.x * b.x, a.y * b.y, a.z * b.z); }
+NE_D V3 operator/(V3 a, V3 b) { return v3(a.x / b.x, a.y / b.y, a.z / b.z); }
+NE_D V3 operator*(V3 a, float s) { return v3(a.x * s, a.y * s, a.z * s); }
+NE_D V3 operator*(float s, V3 a) { return v3(s * a.x, s * a.y, s * a.z); }
+NE_D V3 operator/(V3 a, float s) { return v3(a.x / s, a.y / s, a.z / s); }
+NE_D V3 operator-(V3 a) { return v3(-a.x, -a.y, -a.z); }
+NE_D float dot(V3 a, V3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+NE_D V3 cross(V3 a, V3 b) { return v3(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y); }
+NE_D float length(V3 a) { return nefm::fsqrt(dot(a, a)); }
+NE_D V3 normalize(V3 a) { return a * (1.0f / nefm::fsqrt(dot(a, a))); }
+NE_D float gmin(float a, float b) { return (b < a) ? b : a; }
+NE_D float gmax(float a, float b) { return (a < b) ? b : a; }
+NE_D double gmaxd(double a, double b) { return (a < b) ? b : a; }
+NE_D V3 vmin(V3 a, V3 b) { return v3(gmin(a.x, b.x), gmin(a.y, b.y), gmin(a.z, b.z)); }
+NE_D V3 vmax(V3 a, V3 b) { return v3(gmax(a.x, b.x), gmax(a.y, b.y), gmax(a.z, b.z)); }
+NE_D V3 vabs(V3 a) { return v3(fabsf(a.x), fabsf(a.y), fabsf(a.z)); }
+NE_D V3 ld3(const float* p) { return v3(p[0], p[1], p[2]); }
+NE_D bool isBlack(V3 v) { return v.x == 0 && v.y == 0 && v.z == 0; }
+NE_D bool areAllOne(V3 v) { return v.x == 1 && v.y == 1 && v.z == 1; }
+NE_D float avg(V3 v) { return (v.x + v.y + v.z) / 3.0f; }
+NE_D float absDot(V3 a, V3 b) { return fabsf(dot(a, b)); }
+NE_D float maxc(V3 v) { return gmax(gmax(v.x, v.y), v.z); }
+NE_D bool sameBits(V3 a, V3 b) {
+  return __float_as_uint(a.x) == __float_as_uint(b.x) && __float_as_uint(a.y) == __float_as_uint(b.y) &&
+         __float_as_uint(a.z) == __float_as_uint(b.z);
+}
+
+// glm::mat4 (affine, 12 stored floats) times vec4(p, w).
+NE_D V3 mul4(const float* m, V3 p, float w) {
+  return v3((m[0] * p.x + m[3] * p.y) + (m[6] * p.z + m[9] * w),
+            (m[1] * p.x + m[4] * p.y) + (m[7] * p.z + m[10] * w),
+            (m[2] * p.x + m[5] * p.y) + (m[8] * p.z + m[11] * w));
+}
+
+struct Ray {
+  V3 o, d;
+  NE_D V3 at(float t) const { return o + t * d; }
+};
+
+struct Hit {
+  V3 hitPoint, normal;
+  float tNear, tFar;
+  int inst, prim;
+};
+
+NE_D Hit emptyHit() {
+  Hit h;
+  h.hitPoint = v3(0, 0, 0);
+  h.normal = v3(0, 0, 0);
+  h.tNear = 0;
+  h.tFar = 0;
+  h.inst = -1;
+  h.prim = -1;
+  return h;
+}
+
+// Counter RNG with the current four-word block cached in registers.
+struct Sampler {
+  nerng::PathKey key;
+  uint32_t dim;
+  uint32_t blk;
+  uint32_t w0, w1, w2, w3;
+  NE_D void reset(const nerng::PathKey& k, uint32_t d) {
+    key = k;
+    dim = d;
+    blk = 0xffffffffu;
+  }
+  NE_D float random() {
+    uint32_t b = dim >> 2;
+    if (b != blk) {
+      nerng::Block r = nerng::philox4x32_10(b, key.sample, key.pixel, key.stream, key.seed_lo, key.seed_hi);
+      w0 = r.w[0]; w1 = r.w[1]; w2 = r.w[2]; w3 = r.w[3];
+      blk = b;
+    }
+    uint32_t s = dim & 3u;
+    dim++;
+    uint32_t w = (s == 0) ? w0 : (s == 1) ? w1 : (s == 2) ? w2 : w3;
+    return nerng::word_to_u01(w);
+  }
+};
+
+struct Counters {
+  unsigned long long lookups, queries, nodes, tests;
+};
+
+template <bool COUNT>
+struct Ctx {
+  const DScene& s;
+  Sampler S;
+  Counters c;
+  uint32_t* err;
+};
+
+NE_D Ray transformRay(const Ray& r, const float* m) { return Ray{mul4(m, r.o, 1.0f), mul4(m, r.d, 0.0f)}; }
+
+// utils/Math.h:591-599 generateOrthonormalCS.
+NE_D void orthonormal(V3 n, V3& v, V3& u) {
+  if (fabsf(n.x) > fabsf(n.y))
+    v = v3(-n.z, 0, n.x) / nefm::fsqrt(n.x * n.x + n.z * n.z);
+  else
+    v = v3(0, n.z, -n.y) / nefm::fsqrt(n.y * n.y + n.z * n.z);
+  u = normalize(cross(n, v));
+}
+NE_D V3 toWorld(V3 v, V3 ns, V3 ss, V3 ts) {  // utils/Math.h:612-617
+  return v3(ss.x * v.x + ts.x * v.y + ns.x * v.z, ss.y * v.x + ts.y * v.y + ns.y * v.z,
+            ss.z * v.x + ts.z * v.y + ns.z * v.z);
+}
+NE_D V3 toLCS(V3 v, V3 ns, V3 ss, V3 ts) { return v3(dot(v, ss), dot(v, ts), dot(v, ns)); }  // Math.h:629-631
+NE_D bool sameHemisphere(V3 a, V3 b) { return dot(a, b) > 0; }
+NE_D float powerHeuristic(float p0, float p1) { return (p0 * p0) / (p0 * p0 + p1 * p1); }
+
+// utils/Math.h:442-457 sampleUnitSphere.
+NE_D V3 sampleUnitSphere(float e1, float e2) {
+  float theta = __double2float_rn(kTwoPiD * (double)e1);
+  float phi = nefm::acos(1.0f - 2.0f * e2);
+  return v3(nefm::sin(phi) * nefm::cos(theta), nefm::sin(phi) * nefm::sin(theta), nefm::cos(phi));
+}
+NE_D V3 reflect(V3 i, V3 n) { return i - (n * dot(n, i)) * 2.0f; }
+
+// utils/Math.h:1112-1126 convertAreaToSolidAngle.
+NE_D float convertAreaToSolidAngle(float pdfArea, V3 normal, V3 p1, V3 p2) {
+  V3 wi = p1 - p2;
+  if (dot(wi, wi) == 0) return 0;
+  wi = normalize(wi);
+  V3 d = p2 - p1;
+  pdfArea = pdfArea * (dot(d, d) / absDot(normal, -wi));
+  if (nefm::isinf_(pdfArea)) return 0;
+  return pdfArea;
+}
+
+NE_D V3 convertNormalFromTextureMap(V3 texNormal, V3 worldNormal) {
+  V3 nts = texNormal * 2.0f - v3(1, 1, 1);
+  V3 t = cross(worldNormal, v3(0, 1, 0));
+  V3 b = normalize(cross(worldNormal, t));
+  V3 r = (t * nts.x + b * nts.y) + worldNormal * nts.z;
+  return normalize(r);
+}
+
+// ---------------------------------------------------------------- primitives (OCS)
+// primitives/AABB.cpp:48-80 AABB::intersect.
+NE_D bool aabbIntersect(V3 mn, V3 mx, const Ray& r, Hit& h) {
+  V3 s = v3((r.d.x < 0.0f) ? 1.0f : -1.0f, (r.d.y < 0.0f) ? 1.0f : -1.0f, (r.d.z < 0.0f) ? 1.0f : -1.0f);
+  V3 invD = v3(1.0f / r.d.x, 1.0f / r.d.y, 1.0f / r.d.z);
+  V3 size = mx - mn;
+  V3 center = mx - size / 2.0f;
+  V3 half = size / 2.0f;
+  V3 t1 = ((center - r.o) + s * half) * invD;
+  V3 t2 = ((center - r.o) - s * half) * invD;
+  V3 tmin = vmin(t1, t2);
+  V3 tmax = vmax(t1, t2);
+  float tNear = gmax(gmax(tmin.x, tmin.y), tmin.z);
+  float tFar = gmin(gmin(tmax.x, tmax.y), tmax.z);
+  auto sgn = [](float x) { return float((0.0f < x) - (x < 0.0f)); };
+  auto step = [](float edge, float x) { return x < edge ? 0.0f : 1.0f; };
+  V3 nsg = -v3(sgn(r.d.x), sgn(r.d.y), sgn(r.d.z));
+  V3 st1 = v3(step(t1.y, t1.x), step(t1.z, t1.y), step(t1.x, t1.z));
+  V3 st2 = v3(step(t1.z, t1.x), step(t1.x, t1.y), step(t1.y, t1.z));
+  h.normal = (nsg * st1) * st2;
+  h.tNear = tNear;
+  h.tFar = tFar;
+  h.hitPoint = r.at(h.tNear);
+  if (tNear > tFar) {
+    h.tNear = __int_as_float(0x7f800000);
+    h.tFar = -__int_as_float(0x7f800000);
+    return false;
+  }
+  return true;
+}
+
+// Box test used only to steer BVH traversal: same arithmetic, no hit record.
+NE_D bool aabbNear(V3 mn, V3 mx, const Ray& r, V3 invD, V3 s, float& tNearOut) {
+  V3 size = mx - mn;
+  V3 center = mx - size / 2.0f;
+  V3 half = size / 2.0f;
+  V3 t1 = ((center - r.o) + s * half) * invD;
+  V3 t2 = ((center - r.o) - s * half) * invD;
+  V3 tmin = vmin(t1, t2);
+  V3 tmax = vmax(t1, t2);
+  float tNear = gmax(gmax(tmin.x, tmin.y), tmin.z);
+  float tFar = gmin(gmin(tmax.x, tmax.y), tmax.z);
+  tNearOut = tNear;
+  return !(tNear > tFar);
+}
+
+// primitives/Sphere.cpp:21-44.
+NE_D bool sphereIntersect(const DPrim& p, const Ray& r, Hit& h) {
+  V3 center = ld3(p.p0);
+  V3 oc = r.o - center;
+  float a = dot(r.d, r.d);
+  float b = dot(oc, r.d);
+  float c = dot(oc, oc) - p.radius * p.radius;
+  float disc = b * b - a * c;
+  if (disc >= 0) {
+    float sq = nefm::fsqrt(disc);
+    float t1 = (-b - sq) / a;
+    float t2 = (-b + sq) / a;
+    h.tNear = gmin(t1, t2);
+    h.tFar = gmax(t1, t2);
+    h.hitPoint = r.at(h.tNear);
+    h.normal = normalize((h.hitPoint - center) / p.radius);
+    return true;
+  }
+  return false;
+}
+
+// primitives/Rectangle.cpp:16-25 getSize.
+NE_D V3 rectSize(V3 v0, V3 v1) {
+  if (v0.x == v1.x) { v0.x = 0; v1.x = 0; }
+  if (v0.y == v1.y) { v0.y = 0; v1.y = 0; }
+  if (v0.z == v1.z) { v0.z = 0; v1.z = 0; }
+  return vabs(v0) + vabs(v1);
+}
+
+// primitives/Rectangle.cpp:50-76 and :32-48.
+NE_D bool rectIntersect(const DPrim& p, const Ray& r, Hit& h) {
+  V3 v0 = ld3(p.p0), v1 = ld3(p.p1), n = ld3(p.p2);
+  float denom = dot(n, r.d);
+  if ((double)fabsf(denom) < kEpsilonD) return false;
+  float num = dot(n, v1 - r.o);
+  float t = num / denom;
+  if (t < 0) return false;
+  V3 q = r.at(t);
+  V3 mn = vmin(v0, v1), mx = vmax(v0, v1), size = rectSize(v0, v1);
+  if (size.x > 0 && (q.x < mn.x || q.x > mx.x)) return false;
+  if (size.y > 0 && (q.y < mn.y || q.y > mx.y)) return false;
+  if (size.z > 0 && (q.z < mn.z || q.z > mx.z)) return false;
+  h.tNear = t;
+  h.tFar = t;
+  h.normal = n;
+  h.hitPoint = q;
+  return true;
+}
+
+// primitives/Triangle.cpp:49-80.
+NE_D bool triIntersect(const DScene& s, const DPrim& p, const Ray& r, Hit& h) {
+  V3 a = ld3(p.p0), b = ld3(p.p1), c = ld3(p.p2);
+  V3 v1v0 = b - a, v2v0 = c - a, rov0 = r.o - a;
+  V3 normal = cross(v1v0, v2v0);
+  V3 q = cross(rov0, r.d);
+  float denom = 1.0f / dot(r.d, normal);  // equals (float)(1.0 / (double)dot)
+  float u = dot(-q, v2v0) * denom;
+  float v = dot(q, v1v0) * denom;
+  float t = dot(-normal, rov0) * denom;
+  if (nefm::isnan_(t) || t < 0) return false;
+  if (u < 0.0f || u > 1.0f || v < 0.0f || (u + v) > 1.0f) return false;
+  h.tNear = t;
+  h.tFar = t;
+  h.hitPoint = r.at(h.tNear);
+  if (p.material >= 0 && (s.materials[p.material].tex_types & NE_TEX_NORMAL)) {
+    const DMaterial& m = s.materials[p.material];
+    V3 tn = (m.tex_present & NE_TEX_NORMAL) ? ld3(m.normal_map) : v3(0, 0, 0);
+    h.normal = convertNormalFromTextureMap(tn, normalize(normal));
+  } else {
+    h.normal = normalize(normal);
+  }
+  return true;
+}
+
+template <bool C>
+NE_D bool primIntersect(Ctx<C>& c, int idx, const Ray& r, Hit& h) {
+  const DPrim& p = c.s.prims[idx];
+  if (C) c.c.tests++;
+  bool hit = false;
+  switch (p.type) {
+    case NE_PRIM_SPHERE: hit = sphereIntersect(p, r, h); break;
+    case NE_PRIM_RECTANGLE: hit = rectIntersect(p, r, h); break;
+    case NE_PRIM_AABB:
+      hit = aabbIntersect(ld3(p.p0), ld3(p.p1), r, h);
+      h.prim = idx;
+      return hit;
+    case NE_PRIM_TRIANGLE: hit = triIntersect(c.s, p, r, h); break;
+    default: return false;
+  }
+  if (hit) h.prim = idx;
+  return hit;
+}
+
+// primitives/BVH.cpp:108-193 BVH::intersect (near-first stack traversal).
+template <bool C>
+NE_D bool bvhIntersect(Ctx<C>& c, const DModel& m, const Ray& r, Hit& out) {
+  const float inf = __int_as_float(0x7f800000);
+  uint32_t stackNode[kBvhStack];
+  float stackT[kBvhStack];
+  int sp = 0;
+  stackNode[0] = 0;
+  stackT[0] = inf;
+  Hit closest = emptyHit();
+  closest.tNear = inf;
+  closest.tFar = -inf;
+  bool anyHit = false;
+  V3 s = v3((r.d.x < 0.0f) ? 1.0f : -1.0f, (r.d.y < 0.0f) ? 1.0f : -1.0f, (r.d.z < 0.0f) ? 1.0f : -1.0f);
+  V3 invD = v3(1.0f / r.d.x, 1.0f / r.d.y, 1.0f / r.d.z);
+  const DNode* nodes = c.s.bvh + m.bvh_node0;
+  const uint32_t* slots = c.s.bvh_prims + m.bvh_slot0;
+  while (sp >= 0) {
+    uint32_t ni = stackNode[sp];
+    float nearest = stackT[sp];
+    sp--;
+    if (nearest > closest.tNear) continue;
+    float4 hi = __ldg(reinterpret_cast<const float4*>(&nodes[ni].hi));
+    uint32_t b = __float_as_uint(hi.w);
+    if (C) c.c.nodes++;
+    if (b & 0x80000000u) {
+      float4 lo = __ldg(reinterpret_cast<const float4*>(&nodes[ni].lo));
+      uint32_t start = __float_as_uint(lo.w), count = b & 0x7fffffffu;
+      for (uint32_t i = 0; i < count; i++) {
+        Hit tmp = emptyHit();
+        bool cur = primIntersect(c, (int)slots[start + i], r, tmp);
+        anyHit = anyHit || cur;
+        if (cur && tmp.tNear < closest.tNear) closest = tmp;
+      }
+    } else {
+      float4 lo = __ldg(reinterpret_cast<const float4*>(&nodes[ni].lo));
+      uint32_t ro = __float_as_uint(lo.w);
+      uint32_t c0 = ni + 1, c1 = ni + ro;
+      float4 l0 = __ldg(reinterpret_cast<const float4*>(&nodes[c0].lo));
+      float4 h0 = __ldg(reinterpret_cast<const float4*>(&nodes[c0].hi));
+      float4 l1 = __ldg(reinterpret_cast<const float4*>(&nodes[c1].lo));
+      float4 h1 = __ldg(reinterpret_cast<const float4*>(&nodes[c1].hi));
+      float tn0, tn1;
+      bool hit0 = aabbNear(v3(l0.x, l0.y, l0.z), v3(h0.x, h0.y, h0.z), r, invD, s, tn0);
+      bool hit1 = aabbNear(v3(l1.x, l1.y, l1.z), v3(h1.x, h1.y, h1.z), r, invD, s, tn1);
+      if (hit0 && hit1) {
+        uint32_t closer = c0, other = c1;
+        float tc = tn0, to = tn1;
+        if (tn1 < tn0) {
+          closer = c1; other = c0;
+          tc = tn1; to = tn0;
+        }
+        if (sp + 2 >= kBvhStack) { atomicOr(c.err, ERR_BVH_STACK); break; }
+        stackNode[++sp] = other; stackT[sp] = to;
+        stackNode[++sp] = closer; stackT[sp] = tc;
+      } else if (hit0) {
+        if (sp + 1 >= kBvhStack) { atomicOr(c.err, ERR_BVH_STACK); break; }
+        stackNode[++sp] = c0; stackT[sp] = tn0;
+      } else if (hit1) {
+        if (sp + 1 >= kBvhStack) { atomicOr(c.err, ERR_BVH_STACK); break; }
+        stackNode[++sp] = c1; stackT[sp] = tn1;
+      }
+    }
+  }
+  out = closest;
+  return anyHit;
+}
+
+NE_D V3 lightLe(const DLight& L) {  // Light::Le, DirectionalLight::Le, InfiniteAreaLight::Le
+  if (L.type == NE_LIGHT_INFINITE) return ld3(L.env_radiance);
+  return ld3(L.le);
+}
+NE_D V3 lightLi(const DLight& L) {  // Light::Li, DirectionalLight::Li
+  if (L.type == NE_LIGHT_DIRECTIONAL) return ld3(L.le);
+  return ld3(L.li);
+}
+
+// primitives/Model.cpp:372-447 Model::intersect.
+template <bool C>
+NE_D bool modelIntersect(Ctx<C>& c, uint32_t mi, const Ray& ray, Hit& hit, float& tMin, float& tMax) {
+  const DModel& m = c.s.models[mi];
+  bool did = false;
+  Hit temp = emptyHit();
+  if (m.has_bbox)
+    if (!aabbIntersect(ld3(m.bbox_min), ld3(m.bbox_max), ray, temp)) return false;
+  if (m.use_bvh) {
+    bool local = bvhIntersect(c, m, ray, temp);
+    if (local && temp.tNear > tMin && temp.tNear < tMax) {
+      tMax = temp.tNear;
+      hit = temp;
+      did = true;
+    }
+    return did;
+  }
+  for (uint32_t k = 0; k < m.prim_count; k++) {
+    int pi = (int)(m.prim_begin + k);
+    const DPrim& p = c.s.prims[pi];
+    if (p.flags & DPRIM_GRID_MEDIUM) {
+      primIntersect(c, pi, ray, temp);
+      float rx = gmax(0.0f, temp.tNear), ry = temp.tFar;
+      if (rx <= ry && !nefm::isinf_(ry) && !nefm::isinf_(rx)) {
+        temp.prim = pi;
+        temp.tNear = rx;
+        temp.tFar = ry;
+        temp.hitPoint = ray.at(rx);
+        temp.normal = -ray.d;
+        tMax = temp.tNear;
+        hit = temp;
+        did = true;
+      }
+      continue;
+    }
+    bool local = primIntersect(c, pi, ray, temp);
+    if (local && temp.tNear != temp.tFar && temp.tNear < 0 && temp.tFar > 0) {
+      temp.tNear = 0;
+      temp.hitPoint = ray.o;
+      tMax = temp.tNear;
+      hit = temp;
+      did = true;
+    }
+    if (local && temp.tNear > tMin && temp.tNear < tMax) {
+      tMax = temp.tNear;
+      hit = temp;
+      did = true;
+    }
+  }
+  for (uint32_t k = 0; k < m.light_count; k++) {
+    int pi = (int)(m.light_begin + k);
+    const DPrim& p = c.s.prims[pi];
+    const DLight& L = c.s.lights[c.s.materials[p.material].light];
+    if (!isBlack(lightLe(L))) continue;
+    bool local = primIntersect(c, pi, ray, temp);
+    if (local && temp.tNear > tMin && temp.tNear < tMax) {
+      tMax = temp.tNear;
+      hit = temp;
+      did = true;
+    }
+  }
+  return did;
+}
+
+// primitives/InstancedModel.cpp:24-38.
+template <bool C>
+NE_D bool instanceIntersect(Ctx<C>& c, uint32_t ii, const Ray& ray, Hit& hit, float& tMin, float& tMax) {
+  const DInstance& in = c.s.instances[ii];
+  if (!in.collision) return false;
+  Ray r = transformRay(ray, in.ocs);
+  bool did = modelIntersect(c, in.model, r, hit, tMin, tMax);
+  if (did) {
+    hit.hitPoint = mul4(in.wcs, hit.hitPoint, 1.0f);
+    hit.normal = normalize(mul4(in.wcs, hit.normal, 0.0f));
+    hit.inst = (int)ii;
+  }
+  return did;
+}
+
+// core/Scene.cpp:30-56.
+template <bool C>
+NE_D bool intersectScene(Ctx<C>& c, const Ray& ray, Hit& hit, float tMin, float tMax) {
+  bool did = false;
+  hit.prim = -1;
+  if (C) c.c.queries++;
+  Hit temp = emptyHit();
+  float curMin = tMin, curMax = tMax;
+  uint32_t total = c.s.n_instances + c.s.n_light_instances;
+  for (uint32_t i = 0; i < total; i++) {
+    bool t = instanceIntersect(c, i, ray, temp, curMin, curMax);
+    if (t) hit = temp;
+    did = did || t;
+  }
+  return did;
+}
+
+// ---------------------------------------------------------------- materials
+NE_D V3 texValue(const DMaterial& m, int bit) {  // Material::sampleMaterial, constant textures
+  if (!(m.tex_present & bit)) return v3(0, 0, 0);
+  switch (bit) {
+    case NE_TEX_ALBEDO: return ld3(m.albedo);
+    case NE_TEX_ROUGHNESS: return v3(m.roughness, 0, 0);
+    case NE_TEX_METALLIC: return v3(m.metallic, 0, 0);
+    case NE_TEX_NORMAL: return ld3(m.normal_map);
+  }
+  return v3(0, 0, 0);
+}
+// core/Microfacet.cpp:5-14.
+NE_D float ggxD(float alpha, V3 m) {
+  float a2 = alpha * alpha;
+  float NdotH = m.z;
+  float NdotH2 = NdotH * NdotH;
+  float denom = NdotH2 * (a2 - 1.0f) + 1.0f;
+  denom = __double2float_rn(gmaxd(kEpsilonD, kPiD * (double)denom * (double)denom));
+  return a2 / denom;
+}
+// core/Microfacet.cpp:16-23.
+NE_D float schlickGGX(float alpha, float NdotV) {
+  float k = alpha / 2.0f;
+  float nom = NdotV;
+  float denom = __double2float_rn(gmaxd(kEpsilonD, (double)NdotV * (1.0 - (double)k) + (double)k));
+  return nom / denom;
+}
+// core/Microfacet.cpp:25-35.
+NE_D float ggxG(float alpha, V3 wi, V3 wo) {
+  V3 n = normalize(wi + wo);
+  float NoV = dot(n, wi), NoL = dot(n, wo);
+  float NdotV = gmax(NoV, 0.0f), NdotL = gmax(NoL, 0.0f);
+  return schlickGGX(alpha, NdotV) * schlickGGX(alpha, NdotL);
+}
+// core/Microfacet.cpp:37-56.
+NE_D V3 ggxSample(float alpha, V3 wi, Sampler& S) {
+  float rx = S.random();
+  float ry = S.random();
+  float a2 = alpha * alpha;
+  float theta = nefm::acos(gmin(1.0f, nefm::fsqrt((1.0f - rx) / gmax(float(kEpsilonD), (rx * (a2 - 1.0f) + 1.0f)))));
+  float phi = __double2float_rn(kTwoPiD * (double)ry);
+  V3 m = v3(nefm::sin(theta) * nefm::cos(phi), nefm::sin(theta) * nefm::sin(phi), nefm::cos(theta));
+  return reflect(normalize(wi), normalize(m));
+}
+// core/Microfacet.cpp:58-65.
+NE_D float ggxPdf(float alpha, V3 scattered, V3 m) {
+  float NdotH = m.z;
+  float VdotH = dot(scattered, m);
+  float Dp = ggxD(alpha, m) * NdotH;
+  return Dp / (4 * VdotH);
+}
+// core/BSDF.h:150-157.
+NE_D V3 fresnel(float cosTheta) {
+  V3 f0 = v3(0.04f, 0.04f, 0.04f);
+  return f0 + (v3(1, 1, 1) - f0) * nefm::pow5(1.0f - cosTheta);
+}
+// core/GlossyBSDF.cpp:25-48.
+NE_D V3 glossyEval(const DMaterial& m, V3 wi, V3 wo) {
+  float rough = texValue(m, NE_TEX_ROUGHNESS).x;
+  float alpha = rough * rough;
+  V3 H = normalize(wi + wo);
+  float HdotV = dot(wi, H);
+  float NdotV = wi.z, NdotL = wo.z;
+  float D = ggxD(alpha, H);
+  float G = ggxG(alpha, wi, wo);
+  V3 F = fresnel(HdotV);
+  V3 numerator = (D * G) * F;
+  float denominator = (4.0f * gmax(NdotV, 0.0f)) * gmax(NdotL, 0.0f);
+  V3 specular = numerator / gmax(denominator, float(kEpsilonD));
+  V3 kD = v3(1, 1, 1) - F;
+  float metallic = texValue(m, NE_TEX_METALLIC).x;
+  V3 albedo = texValue(m, NE_TEX_ALBEDO);
+  kD = kD * __double2float_rn(1.0 - (double)metallic);
+  return ((albedo / float(kPiD)) * kD + specular) * NdotL;
+}
+NE_D float glossyPdf(const DMaterial& m, V3 wi, V3 wo) {  // GlossyBSDF.cpp:17-23
+  V3 mh = normalize(wi + wo);
+  float rough = texValue(m, NE_TEX_ROUGHNESS).x;
+  return ggxPdf(rough * rough, wo, mh);
+}
+NE_D V3 glossySample(const DMaterial& m, V3 wi, Sampler& S) {  // GlossyBSDF.cpp:10-15
+  float rough = texValue(m, NE_TEX_ROUGHNESS).x;
+  return ggxSample(rough * rough, wi, S);
+}
+// materials/Medium.h:116-128 HG eval/pdf, :56-62 isotropic.
+NE_D float phaseEval(const DMaterial& m, V3 wi, V3 wo) {
+  if (m.phase == NE_PHASE_ISOTROPIC) return __double2float_rn(1.0 / kFourPiD);
+  float g = m.g;
+  float cosT = dot(normalize(wi), normalize(wo));
+  float denom = (1.0f + g * g) - (2.0f * g) * cosT;
+  return (kInv4Pi * (1.0f - g * g)) / (denom * nefm::fsqrt(denom));
+}
+// materials/Medium.h:96-114 HG sample, :45-47 isotropic.
+NE_D V3 phaseSample(const DMaterial& m, Sampler& S) {
+  if (m.phase == NE_PHASE_ISOTROPIC) {
+    float e1 = S.random();
+    float e2 = S.random();
+    return sampleUnitSphere(e1, e2);
+  }
+  float g = m.g;
+  float u0 = S.random();
+  float u1 = S.random();
+  float cosTheta;
+  if (fabsf(g) < 1e-3f)
+    cosTheta = 1.0f - 2.0f * u0;
+  else {
+    float sqr = (1.0f - g * g) / ((1.0f + g) - (2.0f * g) * u0);
+    sqr = sqr * sqr;
+    cosTheta = (-1.0f / (2.0f * g)) * ((1.0f + g * g) - sqr);
+  }
+  float sinTheta = nefm::fsqrt(1.0f - cosTheta * cosTheta);
+  float phi = __double2float_rn((2.0 * kPiD) * (double)u1);
+  return v3(nefm::cos(phi) * sinTheta, nefm::sin(phi) * sinTheta, cosTheta);
+}
+// core/BSDF.h:100-106.
+NE_D V3 bsdfSample(const DMaterial& m, V3 incoming, V3 normal, Sampler& S) {
+  V3 ss, ts;
+  orthonormal(normal, ss, ts);
+  V3 wi = toLCS(-normalize(incoming), normal, ss, ts);
+  V3 sc = (m.bsdf == NE_BSDF_VOLUME) ? phaseSample(m, S) : glossySample(m, wi, S);
+  return toWorld(sc, normal, ss, ts);
+}
+// core/BSDF.h:117-125.
+NE_D float bsdfPdf(const DMaterial& m, V3 incoming, V3 scattered, V3 normal) {
+  bool trans = (m.bsdf == NE_BSDF_VOLUME);
+  if (!trans && (!sameHemisphere(-incoming, normal) || !sameHemisphere(scattered, normal))) return 0;
+  V3 ss, ts;
+  orthonormal(normal, ss, ts);
+  V3 wi = toLCS(-normalize(incoming), normal, ss, ts);
+  V3 wo = toLCS(scattered, normal, ss, ts);
+  return trans ? phaseEval(m, wi, wo) : glossyPdf(m, wi, wo);
+}
+// core/BSDF.h:135-142.
+NE_D V3 bsdfEval(const DMaterial& m, V3 incoming, V3 scattered, V3 normal) {
+  bool trans = (m.bsdf == NE_BSDF_VOLUME);
+  if (!trans && (!sameHemisphere(-incoming, normal) || !sameHemisphere(scattered, normal))) return v3(0, 0, 0);
+  V3 ss, ts;
+  orthonormal(normal, ss, ts);
+  V3 wi = toLCS(-normalize(incoming), normal, ss, ts);
+  V3 wo = toLCS(scattered, normal, ss, ts);
+  if (trans) {
+    float p = phaseEval(m, wi, wo);
+    return v3(p, p, p);
+  }
+  return glossyEval(m, wi, wo);
+}
+
+// ---------------------------------------------------------------- media
+NE_D float lerp(float a, float b, float t) { return a * (1.0f - t) + b * t; }
+
+// materials/GridMedia.cpp:25-43 interpolatedDensity(fromOCStoGCS(p)): clamp to [0,res],
+// floor, trilinear over the 8 corners with density 0 at index >= res. The 8 corners of
+// cell (ix,iy,iz) are stored together (two float4, one 32-byte sector), so a lookup is
+// one aligned read; the values and the interpolation order are those of the dense grid.
+template <bool C>
+NE_D float sampleAt(Ctx<C>& c, const DMedium& M, const Ray& r, float t) {
+  if (C) c.c.lookups++;
+  V3 p = r.at(t);
+  V3 res = ld3(M.resf);
+  V3 g = (p + v3(0.5f, 0.5f, 0.5f)) * res;
+  g = vmin(vmax(v3(0, 0, 0), g), res);
+  float fx = floorf(g.x), fy = floorf(g.y), fz = floorf(g.z);
+  int ix = (int)fx, iy = (int)fy, iz = (int)fz;
+  V3 d = g - v3((float)ix, (float)iy, (float)iz);
+  float c000, c100, c010, c110, c001, c101, c011, c111;
+  if (M.cells) {
+    size_t cell = ((size_t)iz * (M.res[1] + 1) + (size_t)iy) * (M.res[0] + 1) + (size_t)ix;
+    float4 a = __ldg(&M.cells[2 * cell]);
+    float4 b = __ldg(&M.cells[2 * cell + 1]);
+    c000 = a.x; c100 = a.y; c010 = a.z; c110 = a.w;
+    c001 = b.x; c101 = b.y; c011 = b.z; c111 = b.w;
+  } else {
+    const uint32_t W = M.res[0], H = M.res[1], D = M.res[2];
+    auto den = [&](int x, int y, int z) -> float {
+      if ((uint32_t)x >= W || (uint32_t)y >= H || (uint32_t)z >= D) return 0.0f;
+      return __ldg(&M.grid[(size_t)H * W * (uint32_t)z + (size_t)W * (uint32_t)y + (uint32_t)x]);
+    };
+    c000 = den(ix, iy, iz); c100 = den(ix + 1, iy, iz);
+    c010 = den(ix, iy + 1, iz); c110 = den(ix + 1, iy + 1, iz);
+    c001 = den(ix, iy, iz + 1); c101 = den(ix + 1, iy, iz + 1);
+    c011 = den(ix, iy + 1, iz + 1); c111 = den(ix + 1, iy + 1, iz + 1);
+  }
+  float d00 = lerp(c000, c100, d.x);
+  float d10 = lerp(c010, c110, d.x);
+  float d01 = lerp(c001, c101, d.x);
+  float d11 = lerp(c011, c111, d.x);
+  float d0 = lerp(d00, d10, d.y);
+  float d1 = lerp(d01, d11, d.y);
+  return lerp(d0, d1, d.z);
+}
+
+// materials/GridMedia.cpp:45-69 GridMedia::Tr (ratio tracking).
+template <bool C>
+NE_D V3 gridTr(Ctx<C>& c, const DMedium& M, Ray incoming, Hit isect) {
+  incoming = transformRay(incoming, c.s.instances[isect.inst].ocs);
+  incoming.o = incoming.at(isect.tNear);
+  isect.tFar = isect.tFar - isect.tNear;
+  isect.tNear = 0;
+  float invMax = M.inv_max_density;
+  float mu = M.mu;
+  float Tr = 1, t = isect.tNear;
+  for (int step = 0; step < kMaxTrackSteps; step++) {
+    t -= (nefm::log(1 - c.S.random()) * invMax) / mu;
+    if (t >= isect.tFar) break;
+    float density = sampleAt(c, M, incoming, t);
+    float x = density * invMax;
+    Tr *= 1 - ((0.0f < x) ? x : 0.0f);
+    if (Tr < 0.1f) {
+      float q = (0.05f < 1.0f - Tr) ? (1.0f - Tr) : 0.05f;
+      if (c.S.random() < q) return v3(0, 0, 0);
+      Tr /= 1 - q;
+    }
+  }
+  return v3(Tr, Tr, Tr);
+}
+
+// materials/GridMedia.cpp:71-99 GridMedia::sample (delta tracking).
+template <bool C>
+NE_D V3 gridSample(Ctx<C>& c, const DMedium& M, Ray incoming, Ray& scattered, const Hit& isect) {
+  scattered.o = incoming.o;
+  scattered.d = incoming.d;
+  const DInstance& in = c.s.instances[isect.inst];
+  incoming = transformRay(incoming, in.ocs);
+  float invMax = M.inv_max_density;
+  float mu = M.mu;
+  float t = isect.tNear;
+  for (int step = 0; step < kMaxTrackSteps; step++) {
+    float r = c.S.random();
+    float sampledDist = (nefm::log(1 - r) * invMax) / mu;
+    t -= sampledDist;
+    if (t >= isect.tFar) {
+      scattered.o = incoming.at(isect.tFar + 0.0001f);
+      break;
+    }
+    float density = sampleAt(c, M, incoming, t);
+    float ra = c.S.random();
+    if (density * invMax > ra) {
+      scattered.o = incoming.at(t);
+      const DMaterial& m = c.s.materials[c.s.prims[isect.prim].material];
+      scattered.d = bsdfSample(m, incoming.d, v3(0, 1, 0), c.S);
+      scattered = transformRay(scattered, in.wcs);
+      return ld3(M.sigma_s) / ld3(M.sigma_t);
+    }
+  }
+  return v3(1, 1, 1);
+}
+
+// materials/HomogeneousMedia.cpp:15-51.
+NE_D V3 homogTr(const DMedium& M, float distance) {
+  V3 v = (ld3(M.sigma_t) * distance) * M.density;
+  return v3(nefm::exp(-v.x), nefm::exp(-v.y), nefm::exp(-v.z));
+}
+template <bool C>
+NE_D V3 homogSample(Ctx<C>& c, const DMedium& M, Ray incoming, Ray& scattered, const Hit& isect) {
+  float t = (-nefm::log(1 - c.S.random())) / avg(ld3(M.sigma_t));
+  float dist = isect.tFar - isect.tNear;
+  t = t / dist;
+  bool sampled = t < dist;
+  if (sampled) {
+    scattered.o = incoming.at(t);
+    scattered.d = bsdfSample(c.s.materials[c.s.prims[isect.prim].material], incoming.d, isect.normal, c.S);
+  } else {
+    scattered.o = incoming.at(dist + 0.001f);
+    scattered.d = incoming.d;
+  }
+  V3 Tr = homogTr(M, t);
+  V3 density = sampled ? (ld3(M.sigma_t) * Tr) : Tr;
+  float pdf = avg(density);
+  if (pdf == 0) pdf = 1;
+  return sampled ? ((Tr * ld3(M.sigma_s)) / pdf) : Tr / pdf;
+}
+
+template <bool C>
+NE_D V3 mediumTr(Ctx<C>& c, int med, const Ray& r, const Hit& isect) {
+  const DMedium& M = c.s.media[med];
+  if (M.type == NE_MEDIUM_GRID) return gridTr(c, M, r, isect);
+  return homogTr(M, isect.tFar - isect.tNear);
+}
+template <bool C>
+NE_D V3 mediumSample(Ctx<C>& c, int med, const Ray& r, Ray& scattered, const Hit& isect) {
+  const DMedium& M = c.s.media[med];
+  if (M.type == NE_MEDIUM_GRID) return gridSample(c, M, r, scattered, isect);
+  return homogSample(c, M, r, scattered, isect);
+}
+
+// ---------------------------------------------------------------- lights
+// Primitive::samplePointOnSurface (Rectangle.cpp:78-88, Sphere.cpp:46-52,
+// Triangle.cpp:114-119, Point.cpp:14-18, AABB.cpp:81-83).
+NE_D V3 samplePointOnSurface(const DScene& s, int pi, const Hit& isect, const float* M, Sampler& S) {
+  const DPrim& p = s.prims[pi];
+  switch (p.type) {
+    case NE_PRIM_RECTANGLE: {
+      float e0 = S.random();
+      float e1 = S.random();
+      float e2 = S.random();
+      V3 v0 = ld3(p.p0);
+      V3 size = rectSize(ld3(p.p0), ld3(p.p1));
+      V3 q = v3(v0.x + size.x * e0, v0.y + size.y * e1, v0.z + size.z * e2);
+      return mul4(M, q, 1.0f);
+    }
+    case NE_PRIM_SPHERE: {
+      V3 cc = mul4(M, ld3(p.p0), 1.0f);
+      V3 n = normalize(isect.hitPoint - cc);
+      return cc + n * p.radius;
+    }
+    case NE_PRIM_TRIANGLE: {
+      float ex = S.random();
+      float ey = S.random();
+      float sq = nefm::fsqrt(ex);
+      float a = 1.0f - sq, b = ey * sq;
+      return (a * ld3(p.p0) + b * ld3(p.p1)) + ((1 - a) - b) * ld3(p.p2);
+    }
+    case NE_PRIM_POINT: return mul4(M, ld3(p.p0), 1.0f);
+    default: return v3(0, 0, 0);
+  }
+}
+// Primitive::pdf (Rectangle.cpp:159-171, Sphere.cpp:58-68, Triangle.cpp:159-161).
+NE_D float primPdf(const DScene& s, int pi, const Hit& isect, const DInstance& lin, Sampler& S) {
+  const DPrim& p = s.prims[pi];
+  switch (p.type) {
+    case NE_PRIM_RECTANGLE: {
+      V3 size = rectSize(ld3(p.p0), ld3(p.p1));
+      V3 sizeWCS = ld3(lin.scale) * size;
+      float area = 1;
+      if (sizeWCS.x != 0) area = area * sizeWCS.x;
+      if (sizeWCS.y != 0) area = area * sizeWCS.y;
+      if (sizeWCS.z != 0) area = area * sizeWCS.z;
+      return convertAreaToSolidAngle(1.0f / area, isect.normal, isect.hitPoint,
+                                     samplePointOnSurface(s, pi, isect, lin.wcs, S));
+    }
+    case NE_PRIM_SPHERE: {
+      float pdfArea = __double2float_rn((double)(1.0f / 4.0f) * kPiD * (double)p.radius * (double)p.radius);
+      return convertAreaToSolidAngle(pdfArea, isect.normal, isect.hitPoint, samplePointOnSurface(s, pi, isect, lin.wcs, S));
+    }
+    case NE_PRIM_TRIANGLE:
+      return convertAreaToSolidAngle(1.0f / p.area, isect.normal, isect.hitPoint,
+                                     samplePointOnSurface(s, pi, isect, lin.wcs, S));
+    default: return 1;
+  }
+}
+
+// Light::sampleLi (DiffuseLight.cpp:8-20, DirectionalLight.cpp:12-18, InfiniteAreaLight.h:83-113).
+NE_D V3 sampleLi(const DScene& s, const DLight& L, const Hit& isect, const DInstance& lin, Ray& wo, float& pdf,
+                 Sampler& S) {
+  switch (L.type) {
+    case NE_LIGHT_DIFFUSE: {
+      wo.o = isect.hitPoint;
+      V3 q = samplePointOnSurface(s, L.primitive, isect, lin.wcs, S);
+      V3 d = q - wo.o;
+      wo.d = normalize(d);
+      pdf = primPdf(s, L.primitive, isect, lin, S);
+      return ld3(L.li);
+    }
+    case NE_LIGHT_DIRECTIONAL:
+      wo.o = isect.hitPoint;
+      wo.d = -ld3(L.direction);
+      pdf = 1;
+      return ld3(L.li);
+    default: {
+      float u0 = S.random();
+      float u1 = S.random();
+      float mapPdf = L.env_map_pdf;
+      if (mapPdf == 0) return v3(0, 0, 0);
+      float theta = __double2float_rn((double)u1 * kPiD);
+      float phi = __double2float_rn((double)(u0 * 2) * kPiD);
+      float cosTheta = nefm::cos(theta), sinTheta = nefm::sin(theta);
+      float sinPhi = nefm::sin(phi), cosPhi = nefm::cos(phi);
+      wo.o = isect.hitPoint;
+      V3 polar = v3(sinTheta * cosPhi, sinTheta * sinPhi, cosTheta);
+      V3 ss, ts;
+      orthonormal(v3(0, 1, 0), ss, ts);
+      wo.d = toLCS(polar, v3(0, 1, 0), ss, ts);
+      pdf = __double2float_rn((double)mapPdf / (2 * kPiD * kPiD * (double)sinTheta));
+      if (sinTheta == 0) pdf = 0;
+      return ld3(L.env_radiance);
+    }
+  }
+}
+
+// ---------------------------------------------------------------- integrator
+NE_D const DMaterial* matOf(const DScene& s, int prim) {
+  if (prim < 0) return nullptr;
+  int m = s.prims[prim].material;
+  return m < 0 ? nullptr : &s.materials[m];
+}
+
+// integrators/VolumetricPathIntegrator.cpp:10-32 intersectTr.
+template <bool C>
+NE_D bool intersectTr(Ctx<C>& c, Ray ray, Hit& intersection, V3* Tr) {
+  const float inf = __int_as_float(0x7f800000);
+  *Tr = v3(1, 1, 1);
+  for (int seg = 0; seg < kMaxTrSegments; seg++) {
+    Hit isect = emptyHit();
+    bool hitSurface = intersectScene(c, ray, isect, kEps3F, inf);
+    intersection = isect;
+    int m = -1;
+    const DMaterial* mat = hitSurface ? matOf(c.s, isect.prim) : nullptr;
+    if (mat) m = mat->medium;
+    if (m >= 0) *Tr = *Tr * mediumTr(c, m, ray, isect);
+    if (!hitSurface) return false;
+    if (m >= 0) return true;
+    if (sameBits(isect.hitPoint, ray.o)) return false;
+    ray.o = isect.hitPoint;
+  }
+  return false;
+}
+
+// integrators/VolumetricPathIntegrator.cpp:34-72 visibilityTr.
+template <bool C>
+NE_D V3 visibilityTr(Ctx<C>& c, V3 p, V3 lightPoint) {
+  const float inf = __int_as_float(0x7f800000);
+  Ray ray{p, lightPoint - p};
+  V3 Tr = v3(1, 1, 1);
+  Hit isect = emptyHit();
+  bool hitSurface = intersectScene(c, ray, isect, kEps3F, inf);
+  if (!hitSurface) return Tr;
+  const DMaterial* mat = matOf(c.s, isect.prim);
+  if (!mat) return v3(0, 0, 0);
+  if (mat->light >= 0) return Tr;
+  if (mat->medium >= 0) Tr = Tr * mediumTr(c, mat->medium, ray, isect);
+  return v3(0, 0, 0);
+}
+
+// integrators/VolumetricPathIntegrator.cpp:74-157 estimateDirect.
+template <bool C>
+NE_D V3 estimateDirect(Ctx<C>& c, const Ray& incoming, const Hit& isect, const DLight& light, uint32_t lightInst) {
+  const DScene& s = c.s;
+  const DInstance& lin = s.instances[lightInst];
+  V3 Ld = v3(0, 0, 0);
+  Ray wo{v3(0, 0, 0), v3(0, 0, 0)};
+  float lightPdf = 0, scatteringPdf = 0;
+  V3 Li = sampleLi(s, light, isect, lin, wo, lightPdf, c.S);
+  V3 f = v3(0, 0, 0);
+  const DMaterial& mat = *matOf(s, isect.prim);
+  bool surface = !(mat.medium >= 0);
+  if (lightPdf > 0 && !isBlack(Li)) {
+    if (surface) {
+      f = bsdfEval(mat, incoming.d, wo.d, isect.normal) * fabsf(dot(wo.d, isect.normal));
+      scatteringPdf = bsdfPdf(mat, incoming.d, wo.d, isect.normal);
+    } else {
+      f = bsdfEval(mat, incoming.d, wo.d, isect.normal);
+      scatteringPdf = f.x;
+    }
+    if (!isBlack(f)) {
+      V3 pointOnLight = samplePointOnSurface(s, light.primitive, isect, lin.wcs, c.S);
+      Li = Li * visibilityTr(c, isect.hitPoint, pointOnLight);
+      if (!isBlack(Li)) {
+        float weight = powerHeuristic(lightPdf, scatteringPdf);
+        Ld = Ld + ((f * Li) * weight) / lightPdf;
+      }
+    }
+  }
+  if (surface) {
+    wo.d = bsdfSample(mat, incoming.d, isect.normal, c.S);
+    f = bsdfEval(mat, incoming.d, wo.d, isect.normal);
+    f = f * fabsf(dot(wo.d, isect.normal));
+    scatteringPdf = bsdfPdf(mat, incoming.d, wo.d, isect.normal);
+  } else {
+    f = bsdfEval(mat, incoming.d, wo.d, isect.normal);
+    wo.d = bsdfSample(mat, incoming.d, v3(0, 1, 0), c.S);
+    scatteringPdf = f.x;
+  }
+  if (!isBlack(f) && scatteringPdf > 0) {
+    float weight = 1;
+    lightPdf = primPdf(s, light.primitive, isect, lin, c.S);
+    if (lightPdf == 0) return Ld;
+    weight = powerHeuristic(scatteringPdf, lightPdf);
+    Hit lightIsect = emptyHit();
+    Ray ray{isect.hitPoint, wo.d};
+    V3 Tr = v3(1, 1, 1);
+    bool found = intersectTr(c, ray, lightIsect, &Tr);
+    V3 Li2 = v3(0, 0, 0);
+    if (found) Li2 = lightLi(light);
+    if (!isBlack(Li2)) Ld = Ld + (((f * Li2) * Tr) * weight) / scatteringPdf;
+  }
+  return Ld;
+}
+
+// integrators/VolumetricPathIntegrator.cpp:159-174 and primitives/Model.cpp:478-485.
+template <bool C>
+NE_D V3 uniformSampleOneLight(Ctx<C>& c, const Ray& incoming, const Hit& isect) {
+  const DScene& s = c.s;
+  float r = c.S.random();
+  uint32_t nL = s.n_light_instances;
+  if (nL == 0) return v3(0, 0, 0);
+  int i = (int)((float)nL * r);
+  float lightPdf = 1.0f / (float)nL;
+  uint32_t inst = s.n_instances + (uint32_t)i;
+  const DModel& m = s.models[s.instances[inst].model];
+  if (m.light_count == 0) return v3(0, 0, 0);
+  c.S.random();
+  float r2 = c.S.random();
+  int k = (int)((float)m.light_count * r2);
+  const DPrim& lp = s.prims[m.light_begin + k];
+  const DLight& light = s.lights[s.materials[lp.material].light];
+  return estimateDirect(c, incoming, isect, light, inst) / lightPdf;
+}
+
+struct PathParams {
+  int bounces;
+  int rr;
+  int rr_after;
+};
+
+// integrators/VolumetricPathIntegrator.cpp:176-301 Li, plus the optional Russian
+// roulette of resources/shaders/MS_monteCarlo.frag:539-544.
+template <bool C>
+NE_D V3 Li(Ctx<C>& c, const PathParams& P, Ray incoming) {
+  const DScene& s = c.s;
+  const float inf = __int_as_float(0x7f800000);
+  V3 L = v3(0, 0, 0);
+  V3 T = v3(1, 1, 1);
+  Hit isect = emptyHit();
+  int passes = 0;
+  for (int b = 0; b < P.bounces; b++) {
+    bool did = intersectScene(c, incoming, isect, kEps12F, inf);
+    if (isBlack(T)) break;
+    const DMaterial* mat = did ? matOf(s, isect.prim) : nullptr;
+    if (did && mat && mat->bsdf == NE_BSDF_VOLUME) {
+      incoming.o = incoming.at(isect.tNear);
+      isect.tFar = isect.tFar - isect.tNear;
+      isect.tNear = 0;
+      Ray scattered{v3(0, 0, 0), v3(0, 0, 0)};
+      V3 sampledT = mediumSample(c, mat->medium, incoming, scattered, isect);
+      if (areAllOne(sampledT)) {
+        incoming.o = incoming.at(isect.tFar + 0.01f);
+        if (++passes >= kMaxPassThrough) break;
+        b--;
+        continue;
+      }
+      T = T * sampledT;
+      V3 phaseFr = bsdfEval(*mat, incoming.d, scattered.d, isect.normal);
+      float phasePdf = bsdfPdf(*mat, incoming.d, scattered.d, isect.normal);
+      if (isBlack(phaseFr) || phasePdf == 0.f) break;
+      V3 lightSample = uniformSampleOneLight(c, scattered, isect);
+      T = T * (phaseFr / phasePdf);
+      L = L + T * lightSample;
+      incoming = scattered;
+    } else {
+      if (b == 0) {
+        if (did && mat && mat->light >= 0) {
+          L = L + T * lightLi(s.lights[mat->light]);
+        } else {
+          for (uint32_t li = 0; li < s.n_light_instances; li++) {
+            const DModel& lm = s.models[s.instances[s.n_instances + li].model];
+            for (uint32_t k = 0; k < lm.mat_count; k++) {
+              const DMaterial& mm = s.materials[s.model_materials[lm.mat_begin + k]];
+              L = L + T * lightLe(s.lights[mm.light]);
+            }
+          }
+        }
+      }
+      if (!did || !mat || mat->bsdf == NE_BSDF_NONE) break;
+      L = L + T * uniformSampleOneLight(c, incoming, isect);
+      Ray scattered;
+      scattered.o = isect.hitPoint;
+      scattered.d = bsdfSample(*mat, incoming.d, isect.normal, c.S);
+      float pdf = bsdfPdf(*mat, incoming.d, scattered.d, isect.normal);
+      V3 fr = bsdfEval(*mat, incoming.d, scattered.d, isect.normal);
+      if (isBlack(fr) || pdf == 0.f) break;
+      T = T * ((fr * absDot(incoming.d, isect.normal)) / pdf);
+      incoming = scattered;
+    }
+    if (P.rr && b > P.rr_after) {
+      float mx = maxc(T);
+      if (mx < 0.01f) {
+        float q = gmax(0.05f, 1.0f - mx);
+        if (c.S.random() < q) break;
+        T = T / (1.0f - q);
+      }
+    }
+  }
+  return L;
+}
+
+// core/Camera.cpp:140-144 with utils/Math.h:502-507.
+NE_D Ray cameraRay(const DCamera& cam, float u, float v, Sampler& S) {
+  float theta = __double2float_rn((2 * kPiD) * (double)S.random());
+  float r = nefm::fsqrt(S.random());
+  V3 disk = r * v3(nefm::cos(theta), nefm::sin(theta), 0);
+  V3 rd = cam.lens_radius * disk;
+  V3 offset = ld3(cam.side) * rd.x + ld3(cam.up) * rd.y;
+  V3 pos = ld3(cam.position);
+  V3 dir = ((((ld3(cam.lower_left) + u * ld3(cam.horizontal)) + v * ld3(cam.vertical)) - pos) - offset);
+  return Ray{pos + offset, -normalize(dir)};
+}
+
+// core/OfflineEngine.cpp:61-68.
+template <bool C>
+NE_D V3 cameraPath(Ctx<C>& c, const PathParams& P, const nerng::PathKey& base, uint32_t pixel, uint32_t sample) {
+  uint32_t W = (uint32_t)c.s.width;
+  uint32_t x = pixel % W, y = pixel / W;
+  nerng::PathKey k = base;
+  k.pixel = pixel;
+  k.sample = sample;
+  c.S.reset(k, 0);
+  float u = (float)((float)(int)x + c.S.random()) / (float)c.s.width;
+  float v = (float)((float)(int)y + c.S.random()) / (float)c.s.height;
+  Ray r = cameraRay(c.s.camera, u, v, c.S);
+  return Li(c, P, r);
+}
+
+}  // namespace nedev

@@ -1,0 +1,816 @@
+// Host side of the scene interface: the reference's JSON scene descriptor turned into
+// the flat ne_scene_desc that ne_scene_upload copies to the device.
+//
+// Follows io/SceneReader.cpp (loadScene :10-54, processMaterial :67-222,
+// processPrimitives :224-648, processCameraAndRenderer :650-675), core/Camera.cpp:7-26,
+// utils/Math.h:848-859 (getTransform) and core/ResourceManager.cpp:222-288 (.vol grids).
+// Instead of aborting with LOG(FATAL) on a malformed scene it returns NE_ERR_PARSE or
+// NE_ERR_MISSING_ASSET with a message.
+//
+// Extensions of the descriptor (not in the reference; every one is opt-in):
+//  * material "volume": "grid": {"generator": "fbm", ...} builds the density grid from
+//    seeded simplex fBm; "grid": {"path": "x.f32", "resolution": [W,H,D]} reads raw
+//    little-endian float32 voxels.
+//  * material "infiniteAreaLight": "radiance": [r,g,b] is a constant environment, i.e.
+//    the reference's InfiniteAreaLight over a 1x1 map of that value.
+//  * primitive "mesh": a triangle mesh given inline ("positions", "indices") or by the
+//    "icosphere" generator, loaded as the reference loads an obj/gltf model (bounding
+//    box and BVH); optional "groups" assign seeded GGX materials per triangle group.
+//  * renderer "rr": {"after": n} enables Russian roulette after bounce n.
+// Elementary functions come from ne_fmath.h so that the same descriptor yields the
+// same matrices on x86-64 and aarch64 hosts.
+
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <cmath>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "narval_gb300.h"
+#include "ne_fmath.h"
+#include "scene_gen.h"
+
+namespace {
+
+// ---------------------------------------------------------------- minimal JSON
+struct JVal {
+  enum Kind { NUL, BOOL, NUM, STR, ARR, OBJ } kind = NUL;
+  bool b = false;
+  double num = 0;
+  std::string str;
+  std::vector<JVal> arr;
+  std::vector<std::pair<std::string, JVal>> obj;
+  const JVal* get(const char* k) const {
+    if (kind != OBJ) return nullptr;
+    for (auto& kv : obj)
+      if (kv.first == k) return &kv.second;
+    return nullptr;
+  }
+};
+
+struct ParseError : std::runtime_error {
+  int code;
+  ParseError(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+struct JParser {
+  const char* p;
+  const char* end;
+  void ws() {
+    while (p < end && (*p == ' ' || *p == '\t' || *p == '\n' || *p == '\r')) p++;
+  }
+  [[noreturn]] void fail(const char* what) { throw ParseError(NE_ERR_PARSE, std::string("malformed json: ") + what); }
+  JVal parse() {
+    ws();
+    if (p >= end) fail("unexpected end");
+    JVal v;
+    char c = *p;
+    if (c == '{') {
+      v.kind = JVal::OBJ;
+      p++;
+      ws();
+      if (p < end && *p == '}') { p++; return v; }
+      for (;;) {
+        ws();
+        if (p >= end || *p != '"') fail("expected key");
+        std::string k = str();
+        ws();
+        if (p >= end || *p != ':') fail("expected ':'");
+        p++;
+        JVal x = parse();
+        v.obj.emplace_back(k, std::move(x));
+        ws();
+        if (p < end && *p == ',') { p++; continue; }
+        if (p < end && *p == '}') { p++; break; }
+        fail("expected ',' or '}'");
+      }
+    } else if (c == '[') {
+      v.kind = JVal::ARR;
+      p++;
+      ws();
+      if (p < end && *p == ']') { p++; return v; }
+      for (;;) {
+        v.arr.push_back(parse());
+        ws();
+        if (p < end && *p == ',') { p++; continue; }
+        if (p < end && *p == ']') { p++; break; }
+        fail("expected ',' or ']'");
+      }
+    } else if (c == '"') {
+      v.kind = JVal::STR;
+      v.str = str();
+    } else if (c == 't' && end - p >= 4 && !strncmp(p, "true", 4)) {
+      v.kind = JVal::BOOL; v.b = true; p += 4;
+    } else if (c == 'f' && end - p >= 5 && !strncmp(p, "false", 5)) {
+      v.kind = JVal::BOOL; v.b = false; p += 5;
+    } else if (c == 'n' && end - p >= 4 && !strncmp(p, "null", 4)) {
+      p += 4;
+    } else {
+      char* e = nullptr;
+      v.num = strtod(p, &e);
+      if (e == p) fail("bad value");
+      v.kind = JVal::NUM;
+      p = e;
+    }
+    return v;
+  }
+  std::string str() {
+    std::string s;
+    p++;
+    while (p < end && *p != '"') {
+      if (*p == '\\' && p + 1 < end) {
+        p++;
+        char e = *p;
+        s.push_back(e == 'n' ? '\n' : e == 't' ? '\t' : e);
+      } else {
+        s.push_back(*p);
+      }
+      p++;
+    }
+    if (p >= end) fail("unterminated string");
+    p++;
+    return s;
+  }
+};
+
+const JVal& need(const JVal& o, const char* k, const std::string& ctx) {
+  const JVal* v = o.get(k);
+  if (!v) throw ParseError(NE_ERR_PARSE, ctx + " is missing the property " + k + ".");
+  return *v;
+}
+float num(const JVal& v, const std::string& ctx) {
+  if (v.kind == JVal::NUM) return (float)v.num;
+  if (v.kind == JVal::BOOL) return v.b ? 1.0f : 0.0f;
+  throw ParseError(NE_ERR_PARSE, ctx + " is not a number.");
+}
+std::string sval(const JVal& v, const std::string& ctx) {
+  if (v.kind != JVal::STR) throw ParseError(NE_ERR_PARSE, ctx + " is not a string.");
+  return v.str;
+}
+// SceneReader::getVec3 (:60-65): reads up to three components.
+void vec3(const JVal& v, float* out, const std::string& ctx) {
+  if (v.kind != JVal::ARR) throw ParseError(NE_ERR_PARSE, ctx + " is not an array.");
+  for (size_t i = 0; i < v.arr.size() && i < 3; i++) out[i] = num(v.arr[i], ctx);
+}
+
+// ---------------------------------------------------------------- matrices (glm layout)
+struct M4 {
+  float m[16];  // column-major
+  float& at(int r, int c) { return m[c * 4 + r]; }
+  float at(int r, int c) const { return m[c * 4 + r]; }
+};
+M4 ident() {
+  M4 r;
+  memset(r.m, 0, sizeof(r.m));
+  r.m[0] = r.m[5] = r.m[10] = r.m[15] = 1.0f;
+  return r;
+}
+// glm operator* for mat4: column j of the product = (a0 b0j + a1 b1j) + a2 b2j) + a3 b3j.
+M4 mul(const M4& a, const M4& b) {
+  M4 r;
+  for (int j = 0; j < 4; j++)
+    for (int i = 0; i < 4; i++) {
+      float s = a.at(i, 0) * b.at(0, j) + a.at(i, 1) * b.at(1, j);
+      s = s + a.at(i, 2) * b.at(2, j);
+      s = s + a.at(i, 3) * b.at(3, j);
+      r.at(i, j) = s;
+    }
+  return r;
+}
+// glm::eulerAngleXYZ(t1, t2, t3) = eulerAngleX(t1) * eulerAngleY(t2) * eulerAngleZ(t3).
+M4 eulerXYZ(float t1, float t2, float t3) {
+  M4 rx = ident(), ry = ident(), rz = ident();
+  float c1 = nefm::cos(t1), s1 = nefm::sin(t1);
+  float c2 = nefm::cos(t2), s2 = nefm::sin(t2);
+  float c3 = nefm::cos(t3), s3 = nefm::sin(t3);
+  rx.at(1, 1) = c1; rx.at(2, 1) = s1; rx.at(1, 2) = -s1; rx.at(2, 2) = c1;
+  ry.at(0, 0) = c2; ry.at(2, 0) = -s2; ry.at(0, 2) = s2; ry.at(2, 2) = c2;
+  rz.at(0, 0) = c3; rz.at(1, 0) = s3; rz.at(0, 1) = -s3; rz.at(1, 1) = c3;
+  return mul(mul(rx, ry), rz);
+}
+// utils/Math.h:852-859 getTransform = translate(I, t) * rotate(r) * scale(s); degrees.
+M4 getTransform(const float* t, const float* rdeg, const float* s) {
+  const float toRad = 0.01745329251994329576923690768489f;  // glm::radians
+  M4 tr = ident();
+  tr.m[12] = t[0]; tr.m[13] = t[1]; tr.m[14] = t[2];
+  M4 r = mul(tr, eulerXYZ(rdeg[0] * toRad, rdeg[1] * toRad, rdeg[2] * toRad));
+  for (int c = 0; c < 3; c++)
+    for (int k = 0; k < 4; k++) r.m[c * 4 + k] = r.m[c * 4 + k] * s[c];
+  return r;
+}
+// Inverse of a 4x4 by cofactor expansion (glm::inverse computes the same adjugate / det).
+M4 inverse(const M4& a) {
+  const float* m = a.m;
+  float inv[16];
+  inv[0] = m[5] * m[10] * m[15] - m[5] * m[11] * m[14] - m[9] * m[6] * m[15] + m[9] * m[7] * m[14] + m[13] * m[6] * m[11] - m[13] * m[7] * m[10];
+  inv[4] = -m[4] * m[10] * m[15] + m[4] * m[11] * m[14] + m[8] * m[6] * m[15] - m[8] * m[7] * m[14] - m[12] * m[6] * m[11] + m[12] * m[7] * m[10];
+  inv[8] = m[4] * m[9] * m[15] - m[4] * m[11] * m[13] - m[8] * m[5] * m[15] + m[8] * m[7] * m[13] + m[12] * m[5] * m[11] - m[12] * m[7] * m[9];
+  inv[12] = -m[4] * m[9] * m[14] + m[4] * m[10] * m[13] + m[8] * m[5] * m[14] - m[8] * m[6] * m[13] - m[12] * m[5] * m[10] + m[12] * m[6] * m[9];
+  inv[1] = -m[1] * m[10] * m[15] + m[1] * m[11] * m[14] + m[9] * m[2] * m[15] - m[9] * m[3] * m[14] - m[13] * m[2] * m[11] + m[13] * m[3] * m[10];
+  inv[5] = m[0] * m[10] * m[15] - m[0] * m[11] * m[14] - m[8] * m[2] * m[15] + m[8] * m[3] * m[14] + m[12] * m[2] * m[11] - m[12] * m[3] * m[10];
+  inv[9] = -m[0] * m[9] * m[15] + m[0] * m[11] * m[13] + m[8] * m[1] * m[15] - m[8] * m[3] * m[13] - m[12] * m[1] * m[11] + m[12] * m[3] * m[9];
+  inv[13] = m[0] * m[9] * m[14] - m[0] * m[10] * m[13] - m[8] * m[1] * m[14] + m[8] * m[2] * m[13] + m[12] * m[1] * m[10] - m[12] * m[2] * m[9];
+  inv[2] = m[1] * m[6] * m[15] - m[1] * m[7] * m[14] - m[5] * m[2] * m[15] + m[5] * m[3] * m[14] + m[13] * m[2] * m[7] - m[13] * m[3] * m[6];
+  inv[6] = -m[0] * m[6] * m[15] + m[0] * m[7] * m[14] + m[4] * m[2] * m[15] - m[4] * m[3] * m[14] - m[12] * m[2] * m[7] + m[12] * m[3] * m[6];
+  inv[10] = m[0] * m[5] * m[15] - m[0] * m[7] * m[13] - m[4] * m[1] * m[15] + m[4] * m[3] * m[13] + m[12] * m[1] * m[7] - m[12] * m[3] * m[5];
+  inv[14] = -m[0] * m[5] * m[14] + m[0] * m[6] * m[13] + m[4] * m[1] * m[14] - m[4] * m[2] * m[13] - m[12] * m[1] * m[6] + m[12] * m[2] * m[5];
+  inv[3] = -m[1] * m[6] * m[11] + m[1] * m[7] * m[10] + m[5] * m[2] * m[11] - m[5] * m[3] * m[10] - m[9] * m[2] * m[7] + m[9] * m[3] * m[6];
+  inv[7] = m[0] * m[6] * m[11] - m[0] * m[7] * m[10] - m[4] * m[2] * m[11] + m[4] * m[3] * m[10] + m[8] * m[2] * m[7] - m[8] * m[3] * m[6];
+  inv[11] = -m[0] * m[5] * m[11] + m[0] * m[7] * m[9] + m[4] * m[1] * m[11] - m[4] * m[3] * m[9] - m[8] * m[1] * m[7] + m[8] * m[3] * m[5];
+  inv[15] = m[0] * m[5] * m[10] - m[0] * m[6] * m[9] - m[4] * m[1] * m[10] + m[4] * m[2] * m[9] + m[8] * m[1] * m[6] - m[8] * m[2] * m[5];
+  float det = m[0] * inv[0] + m[1] * inv[4] + m[2] * inv[8] + m[3] * inv[12];
+  float od = 1.0f / det;
+  M4 r;
+  for (int i = 0; i < 16; i++) r.m[i] = inv[i] * od;
+  return r;
+}
+
+// small float3 helpers for the camera (glm order)
+struct F3 {
+  float x, y, z;
+};
+F3 f3(const float* p) { return F3{p[0], p[1], p[2]}; }
+F3 operator-(F3 a, F3 b) { return F3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+F3 operator-(F3 a) { return F3{-a.x, -a.y, -a.z}; }
+F3 operator*(float s, F3 a) { return F3{s * a.x, s * a.y, s * a.z}; }
+float dot(F3 a, F3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+F3 normalize(F3 a) {
+  float k = 1.0f / nefm::fsqrt(dot(a, a));
+  return F3{a.x * k, a.y * k, a.z * k};
+}
+F3 cross(F3 a, F3 b) { return F3{a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y}; }
+void put(float* o, F3 v) { o[0] = v.x; o[1] = v.y; o[2] = v.z; }
+
+}  // namespace
+
+struct ne_scene_host {
+  std::vector<ne_instance> instances;       // instancedModels
+  std::vector<ne_instance> light_instances; // lights
+  std::vector<ne_model> models;
+  std::vector<ne_primitive> prims;
+  std::vector<ne_material> materials;
+  std::vector<uint32_t> model_materials;
+  std::vector<ne_light> lights;
+  std::vector<ne_medium> media;
+  std::vector<std::vector<float>> grids;
+  std::vector<ne_instance> all_instances;
+  ne_scene_desc desc;
+  std::map<std::string, int> material_by_name;
+};
+
+namespace {
+
+struct Reader {
+  ne_scene_host& S;
+  std::string res_dir;
+
+  std::string assetPath(const std::string& rel) const {
+    if (!rel.empty() && rel[0] == '/') return rel;
+    if (res_dir.empty()) return rel;
+    std::string d = res_dir;
+    if (d.back() != '/') d.push_back('/');
+    return d + rel;
+  }
+
+  int addGrid(std::vector<float>&& g) {
+    S.grids.push_back(std::move(g));
+    return (int)S.grids.size() - 1;
+  }
+
+  // core/ResourceManager.cpp:222-288 loadVolasTexture: first line "X Y Z " (values
+  // followed by a space), second line skipped, then space-separated floats.
+  void loadVol(const std::string& path, uint32_t res[3], std::vector<float>& grid) {
+    FILE* f = fopen(assetPath(path).c_str(), "rb");
+    if (!f) throw ParseError(NE_ERR_MISSING_ASSET, "Couldn't read the file at " + assetPath(path) + ".");
+    std::string text;
+    char buf[1 << 16];
+    size_t n;
+    while ((n = fread(buf, 1, sizeof(buf), f)) > 0) text.append(buf, n);
+    fclose(f);
+    size_t l1 = text.find('\n');
+    std::string first = text.substr(0, l1 == std::string::npos ? text.size() : l1);
+    float r3[3] = {0, 0, 0};
+    int count = 0;
+    size_t start = 0, e = first.find(' ');
+    while (e != std::string::npos && count < 3) {
+      r3[count++] = strtof(first.substr(start, e - start).c_str(), nullptr);
+      start = e + 1;
+      e = first.find(' ', start);
+    }
+    if (count < 3) throw ParseError(NE_ERR_PARSE, "volume " + path + ": resolution line needs three values.");
+    res[0] = (uint32_t)r3[0]; res[1] = (uint32_t)r3[1]; res[2] = (uint32_t)r3[2];
+    size_t total = (size_t)res[0] * res[1] * res[2];
+    grid.assign(total, 0.0f);
+    size_t l2 = (l1 == std::string::npos) ? std::string::npos : text.find('\n', l1 + 1);
+    std::string data = (l2 == std::string::npos) ? std::string() : text.substr(l2 + 1);
+    size_t k = 0;
+    start = 0;
+    e = data.find(' ');
+    while (e != std::string::npos) {
+      if (k >= total) throw ParseError(NE_ERR_PARSE, "volume " + path + ": more values than the resolution.");
+      grid[k++] = strtof(data.substr(start, e - start).c_str(), nullptr);
+      start = e + 1;
+      e = data.find(' ', start);
+    }
+  }
+
+  void loadF32(const std::string& path, const uint32_t res[3], std::vector<float>& grid) {
+    FILE* f = fopen(assetPath(path).c_str(), "rb");
+    if (!f) throw ParseError(NE_ERR_MISSING_ASSET, "Couldn't read the file at " + assetPath(path) + ".");
+    size_t total = (size_t)res[0] * res[1] * res[2];
+    grid.assign(total, 0.0f);
+    size_t got = fread(grid.data(), sizeof(float), total, f);
+    fclose(f);
+    if (got != total) throw ParseError(NE_ERR_PARSE, "grid " + path + ": file shorter than the resolution.");
+  }
+
+  // io/SceneReader.cpp:67-222 processMaterial.
+  void material(const JVal& m) {
+    std::string name = sval(need(m, "name", "Material"), "Material name");
+    std::string type = sval(need(m, "type", "Material " + name), "Material type");
+    ne_material mat;
+    memset(&mat, 0, sizeof(mat));
+    mat.light = -1;
+    mat.medium = -1;
+    std::string ctx = "Material " + name;
+    if (type == "microfacet") {
+      const JVal& alb = need(m, "albedo", ctx);
+      if (alb.kind == JVal::STR)
+        throw ParseError(NE_ERR_UNSUPPORTED, ctx + ": albedo textures are not supported (constant albedo only).");
+      float albedo[3] = {1, 0, 1};
+      vec3(alb, albedo, ctx + " albedo");
+      memcpy(mat.albedo, albedo, sizeof(albedo));
+      float nm[3] = {0, 0, 1};
+      bool hasNormal = m.get("normalMap") != nullptr;
+      if (hasNormal) vec3(*m.get("normalMap"), nm, ctx + " normalMap");
+      memcpy(mat.normal_map, nm, sizeof(nm));
+      mat.roughness = num(need(m, "roughness", ctx), ctx + " roughness");
+      mat.metallic = num(need(m, "metallic", ctx), ctx + " metallic");
+      mat.bsdf = NE_BSDF_GLOSSY;
+      // addTexture order ALBEDO, METALLIC, ROUGHNESS[, NORMAL]; textureTypes keeps the
+      // last one only (materials/Material.h:38-44).
+      mat.tex_present = NE_TEX_ALBEDO | NE_TEX_METALLIC | NE_TEX_ROUGHNESS | (hasNormal ? NE_TEX_NORMAL : 0);
+      mat.tex_types = hasNormal ? NE_TEX_NORMAL : NE_TEX_ROUGHNESS;
+    } else if (type == "emitter") {
+      ne_light L;
+      memset(&L, 0, sizeof(L));
+      L.type = NE_LIGHT_DIFFUSE;
+      L.primitive = -1;
+      vec3(need(m, "albedo", ctx), L.li, ctx + " albedo");
+      memcpy(mat.albedo, L.li, sizeof(L.li));
+      S.lights.push_back(L);
+      mat.light = (int)S.lights.size() - 1;
+      mat.tex_present = NE_TEX_ALBEDO;
+      mat.tex_types = NE_TEX_ALBEDO;
+    } else if (type == "directionalLight") {
+      ne_light L;
+      memset(&L, 0, sizeof(L));
+      L.type = NE_LIGHT_DIRECTIONAL;
+      L.primitive = -1;
+      vec3(need(m, "albedo", ctx), L.le, ctx + " albedo");
+      float pos[3] = {0, 0, 0};
+      vec3(need(m, "position", ctx), pos, ctx + " position");
+      F3 dir = normalize(F3{0.0f - pos[0], 0.0f - pos[1], 0.0f - pos[2]});
+      put(L.direction, dir);
+      S.lights.push_back(L);
+      mat.light = (int)S.lights.size() - 1;
+    } else if (type == "infiniteAreaLight") {
+      ne_light L;
+      memset(&L, 0, sizeof(L));
+      L.type = NE_LIGHT_INFINITE;
+      L.primitive = -1;
+      if (m.get("path") && !m.get("radiance"))
+        throw ParseError(NE_ERR_UNSUPPORTED, ctx + ": environment-map textures are not supported; give \"radiance\".");
+      vec3(need(m, "radiance", ctx), L.env_radiance, ctx + " radiance");
+      // Distribution2D over a 1x1 map of value G (InfiniteAreaLight.h:51-65, Sampling.h:12-28):
+      // the sampled pdf is func/funcInt = 1 when G > 0, else 0.
+      L.env_map_pdf = (L.env_radiance[1] > 0.0f) ? 1.0f : 0.0f;
+      S.lights.push_back(L);
+      mat.light = (int)S.lights.size() - 1;
+      mat.tex_present = NE_TEX_TEX1;
+      mat.tex_types = NE_TEX_TEX1;
+    } else if (type == "volume") {
+      ne_medium md;
+      memset(&md, 0, sizeof(md));
+      vec3(need(m, "scattering", ctx), md.sigma_s, ctx + " scattering");
+      vec3(need(m, "absorption", ctx), md.sigma_a, ctx + " absorption");
+      std::string pf = sval(need(m, "phaseFunction", ctx), ctx + " phaseFunction");
+      if (pf == "isotropic") {
+        mat.phase = NE_PHASE_ISOTROPIC;
+      } else if (pf == "hg" || pf == "henyey-greenstein") {
+        mat.phase = NE_PHASE_HG;
+        mat.g = num(need(m, "g", ctx), ctx + " g");
+      } else {
+        throw ParseError(NE_ERR_PARSE, ctx + ": unknown phase function " + pf + ".");
+      }
+      md.density = num(need(m, "density", ctx), ctx + " density");
+      std::vector<float> grid;
+      bool isGrid = false;
+      if (const JVal* p = m.get("path")) {
+        std::string path = sval(*p, ctx + " path");
+        if (path.find(".vdb") != std::string::npos)
+          throw ParseError(NE_ERR_UNSUPPORTED, ctx + ": OpenVDB grids are not supported; convert to .vol or .f32.");
+        if (path.find(".vol") == std::string::npos)
+          throw ParseError(NE_ERR_PARSE, ctx + ": volume path must be a .vol file.");
+        loadVol(path, md.res, grid);
+        isGrid = true;
+      } else if (const JVal* g = m.get("grid")) {
+        const JVal& r = need(*g, "resolution", ctx + " grid");
+        float rf[3] = {0, 0, 0};
+        vec3(r, rf, ctx + " grid resolution");
+        md.res[0] = (uint32_t)rf[0]; md.res[1] = (uint32_t)rf[1]; md.res[2] = (uint32_t)rf[2];
+        if (!md.res[0] || !md.res[1] || !md.res[2]) throw ParseError(NE_ERR_PARSE, ctx + ": empty grid.");
+        if (const JVal* gp = g->get("path")) {
+          loadF32(sval(*gp, ctx + " grid path"), md.res, grid);
+        } else {
+          std::string gen = sval(need(*g, "generator", ctx + " grid"), ctx + " grid generator");
+          if (gen != "fbm") throw ParseError(NE_ERR_PARSE, ctx + ": unknown grid generator " + gen + ".");
+          negen::FbmParams fp;
+          fp.octaves = g->get("octaves") ? (int)num(*g->get("octaves"), "octaves") : 5;
+          fp.frequency = g->get("frequency") ? g->get("frequency")->num : 4.0 / md.res[0];
+          fp.lacunarity = g->get("lacunarity") ? g->get("lacunarity")->num : 2.0;
+          fp.gain = g->get("gain") ? g->get("gain")->num : 0.5;
+          fp.falloff_radius = g->get("falloff_radius") ? g->get("falloff_radius")->num : md.res[0] * 0.5;
+          fp.seed = g->get("seed") ? (uint64_t)g->get("seed")->num : 0x4E415256ull;
+          negen::fbm_grid(md.res, fp, grid);
+        }
+        isGrid = true;
+      }
+      if (isGrid) {
+        md.type = NE_MEDIUM_GRID;
+        int gi = addGrid(std::move(grid));
+        (void)gi;
+        md.grid = nullptr;  // bound after all grids are stored
+        md.res[0] = md.res[0];
+        grids_of_media.push_back(gi);
+      } else {
+        md.type = NE_MEDIUM_HOMOGENEOUS;
+        grids_of_media.push_back(-1);
+      }
+      S.media.push_back(md);
+      mat.medium = (int)S.media.size() - 1;
+      mat.bsdf = NE_BSDF_VOLUME;
+      mat.tex_present = NE_TEX_TEX1;
+      mat.tex_types = NE_TEX_TEX1;
+    } else {
+      throw ParseError(NE_ERR_PARSE, "Invalid material type while reading scene from json file.");
+    }
+    S.materials.push_back(mat);
+    S.material_by_name[name] = (int)S.materials.size() - 1;
+  }
+  std::vector<int> grids_of_media;
+
+  int materialNamed(const std::string& name, const std::string& ctx) {
+    auto it = S.material_by_name.find(name);
+    if (it == S.material_by_name.end()) throw ParseError(NE_ERR_PARSE, ctx + ": unknown material " + name + ".");
+    return it->second;
+  }
+
+  void addInstance(const M4& M, uint32_t model, bool collision, bool isLight) {
+    ne_instance in;
+    memset(&in, 0, sizeof(in));
+    memcpy(in.to_wcs, M.m, sizeof(M.m));
+    M4 inv = inverse(M);
+    memcpy(in.to_ocs, inv.m, sizeof(inv.m));
+    in.model = model;
+    in.collision = collision ? 1 : 0;
+    (isLight ? S.light_instances : S.instances).push_back(in);
+  }
+
+  // A Model holding one primitive, either in Model::lights (emissive material) or in
+  // Model::primitives, with Model::materials = [material].
+  uint32_t singlePrimModel(ne_primitive p, int mat, bool emissive) {
+    ne_model md;
+    memset(&md, 0, sizeof(md));
+    p.material = mat;
+    S.prims.push_back(p);
+    uint32_t pi = (uint32_t)S.prims.size() - 1;
+    if (emissive) {
+      md.light_begin = pi; md.light_count = 1;
+      md.prim_begin = pi; md.prim_count = 0;
+      S.lights[S.materials[mat].light].primitive = (int)pi;  // material->light->primitive = prim
+    } else {
+      md.prim_begin = pi; md.prim_count = 1;
+      md.light_begin = pi; md.light_count = 0;
+    }
+    md.mat_begin = (uint32_t)S.model_materials.size();
+    md.mat_count = 1;
+    S.model_materials.push_back((uint32_t)mat);
+    S.models.push_back(md);
+    return (uint32_t)S.models.size() - 1;
+  }
+
+  // io/SceneReader.cpp:224-648 processPrimitives.
+  void primitive(const JVal& p) {
+    std::string name = sval(need(p, "name", "Primitive"), "Primitive name");
+    std::string ctx = "Primitive " + name;
+    std::string type = sval(need(p, "type", ctx), ctx + " type");
+    const JVal& tr = need(p, "transform", ctx);
+    float pos[3] = {0, 0, 0}, scale[3] = {1, 1, 1}, rot[3] = {0, 0, 0};
+    vec3(need(tr, "position", ctx + " transform"), pos, ctx + " position");
+    bool collision = true;
+    if (const JVal* c = p.get("collision")) collision = c->kind == JVal::BOOL ? c->b : num(*c, "collision") != 0;
+    auto readSR = [&]() {
+      vec3(need(tr, "scale", ctx + " transform"), scale, ctx + " scale");
+      vec3(need(tr, "rotation", ctx + " transform"), rot, ctx + " rotation");
+    };
+    ne_primitive pr;
+    memset(&pr, 0, sizeof(pr));
+    if (type == "obj" || type == "gltf") {
+      throw ParseError(NE_ERR_UNSUPPORTED, ctx + ": " + type + " models need an asset importer; use a \"mesh\" primitive.");
+    } else if (type == "point") {
+      readSR();
+      int mat = materialNamed(sval(need(p, "materialName", ctx), ctx), ctx);
+      pr.type = NE_PRIM_POINT;
+      memcpy(pr.p0, pos, sizeof(pos));
+      bool em = S.materials[mat].light >= 0;
+      uint32_t mi = singlePrimModel(pr, mat, em);
+      addInstance(getTransform(pos, rot, scale), mi, true, em);
+    } else if (type == "sphere") {
+      pr.type = NE_PRIM_SPHERE;
+      pr.radius = num(need(p, "radius", ctx), ctx + " radius");
+      int mat = materialNamed(sval(need(p, "materialName", ctx), ctx), ctx);
+      bool em = S.materials[mat].light >= 0;
+      uint32_t mi = singlePrimModel(pr, mat, em);
+      float zero[3] = {0, 0, 0}, one[3] = {1, 1, 1};
+      addInstance(getTransform(pos, zero, one), mi, collision, em);
+    } else if (type == "rectangle") {
+      readSR();
+      int mat = materialNamed(sval(need(p, "materialName", ctx), ctx), ctx);
+      pr.type = NE_PRIM_RECTANGLE;
+      // OCS unit square z = 0; vertexData[0] = bottom left, vertexData[1] = vertex 2
+      // (top right); normal (0,0,-1) (SceneReader.cpp:407-482).
+      pr.p0[0] = -0.5f; pr.p0[1] = -0.5f; pr.p0[2] = 0.0f;
+      pr.p1[0] = 0.5f; pr.p1[1] = 0.5f; pr.p1[2] = 0.0f;
+      pr.p2[0] = 0.0f; pr.p2[1] = 0.0f; pr.p2[2] = -1.0f;
+      bool em = S.materials[mat].light >= 0;
+      uint32_t mi = singlePrimModel(pr, mat, em);
+      addInstance(getTransform(pos, rot, scale), mi, true, em);
+    } else if (type == "volume") {
+      readSR();
+      int mat = materialNamed(sval(need(p, "materialName", ctx), ctx), ctx);
+      pr.type = NE_PRIM_AABB;
+      for (int i = 0; i < 3; i++) { pr.p0[i] = -0.5f; pr.p1[i] = 0.5f; }
+      uint32_t mi = singlePrimModel(pr, mat, false);
+      addInstance(getTransform(pos, rot, scale), mi, true, false);
+    } else if (type == "mesh") {
+      readSR();
+      mesh(p, ctx);
+      addInstance(getTransform(pos, rot, scale), (uint32_t)S.models.size() - 1, collision, false);
+    } else {
+      throw ParseError(NE_ERR_PARSE, "Invalid primitive type while reading scene from json file.");
+    }
+  }
+
+  // Extension: triangle mesh loaded like Model(aiScene) (primitives/Model.cpp:4-7, 337-370):
+  // bounding box over the vertices, BVH over the triangles.
+  void mesh(const JVal& p, const std::string& ctx) {
+    std::vector<float> pos;
+    std::vector<uint32_t> idx;
+    if (const JVal* g = p.get("generator")) {
+      std::string gen = sval(*g, ctx + " generator");
+      if (gen != "icosphere") throw ParseError(NE_ERR_PARSE, ctx + ": unknown mesh generator " + gen + ".");
+      negen::IcoParams ip;
+      ip.subdivisions = p.get("subdivisions") ? (int)num(*p.get("subdivisions"), "subdivisions") : 3;
+      if (const JVal* d = p.get("displacement")) {
+        ip.amplitude = d->get("amplitude") ? d->get("amplitude")->num : 0.0;
+        ip.frequency = d->get("frequency") ? d->get("frequency")->num : 1.0;
+        ip.seed = d->get("seed") ? (uint64_t)d->get("seed")->num : 0x4E415256ull;
+      }
+      negen::icosphere(ip, pos, idx);
+    } else {
+      const JVal& P = need(p, "positions", ctx);
+      const JVal& I = need(p, "indices", ctx);
+      for (auto& v : P.arr) pos.push_back(num(v, ctx + " positions"));
+      for (auto& v : I.arr) idx.push_back((uint32_t)num(v, ctx + " indices"));
+      if (pos.size() % 3 || idx.size() % 3) throw ParseError(NE_ERR_PARSE, ctx + ": positions/indices not multiples of 3.");
+      for (uint32_t i : idx)
+        if ((size_t)i * 3 + 2 >= pos.size()) throw ParseError(NE_ERR_PARSE, ctx + ": index out of range.");
+    }
+    uint32_t nt = (uint32_t)(idx.size() / 3);
+    if (nt == 0) throw ParseError(NE_ERR_PARSE, ctx + ": mesh has no triangles.");
+    // materials: one named material, or seeded groups
+    std::vector<int> triMat(nt, -1);
+    ne_model md;
+    memset(&md, 0, sizeof(md));
+    md.mat_begin = (uint32_t)S.model_materials.size();
+    if (const JVal* gr = p.get("groups")) {
+      int count = gr->get("count") ? (int)num(*gr->get("count"), "count") : 1;
+      float rr[2] = {0.05f, 0.9f}, ar[2] = {0.2f, 0.9f};
+      if (const JVal* v = gr->get("roughness")) { rr[0] = num(v->arr.at(0), "roughness"); rr[1] = num(v->arr.at(1), "roughness"); }
+      if (const JVal* v = gr->get("albedo")) { ar[0] = num(v->arr.at(0), "albedo"); ar[1] = num(v->arr.at(1), "albedo"); }
+      uint64_t seed = gr->get("seed") ? (uint64_t)gr->get("seed")->num : 0x4E415256ull;
+      int first = (int)S.materials.size();
+      for (int k = 0; k < count; k++) {
+        ne_material mat;
+        memset(&mat, 0, sizeof(mat));
+        mat.light = -1;
+        mat.medium = -1;
+        mat.bsdf = NE_BSDF_GLOSSY;
+        double u0 = negen::hash_u01(seed, (uint64_t)k * 4 + 0);
+        double u1 = negen::hash_u01(seed, (uint64_t)k * 4 + 1);
+        mat.roughness = (float)(rr[0] + (rr[1] - rr[0]) * u0);
+        float a = (float)(ar[0] + (ar[1] - ar[0]) * u1);
+        mat.albedo[0] = mat.albedo[1] = mat.albedo[2] = a;
+        mat.metallic = 0.0f;
+        mat.tex_present = NE_TEX_ALBEDO | NE_TEX_METALLIC | NE_TEX_ROUGHNESS;
+        mat.tex_types = NE_TEX_ROUGHNESS;
+        S.materials.push_back(mat);
+        S.model_materials.push_back((uint32_t)(first + k));
+      }
+      for (uint32_t t = 0; t < nt; t++) triMat[t] = first + (int)((uint64_t)t * (uint64_t)count / nt);
+      md.mat_count = (uint32_t)count;
+    } else if (const JVal* mn = p.get("materialName")) {
+      int mat = materialNamed(sval(*mn, ctx), ctx);
+      for (auto& m : triMat) m = mat;
+      S.model_materials.push_back((uint32_t)mat);
+      md.mat_count = 1;
+    }
+    md.prim_begin = (uint32_t)S.prims.size();
+    md.prim_count = nt;
+    md.light_begin = md.prim_begin + nt;
+    md.light_count = 0;
+    const float inf = INFINITY;
+    float mn[3] = {inf, inf, inf}, mx[3] = {-inf, -inf, -inf};
+    for (uint32_t t = 0; t < nt; t++) {
+      ne_primitive pr;
+      memset(&pr, 0, sizeof(pr));
+      pr.type = NE_PRIM_TRIANGLE;
+      pr.material = triMat[t];
+      float* dst[3] = {pr.p0, pr.p1, pr.p2};
+      for (int k = 0; k < 3; k++) {
+        const float* v = &pos[(size_t)idx[3 * t + k] * 3];
+        memcpy(dst[k], v, 12);
+        for (int c = 0; c < 3; c++) {
+          mn[c] = (v[c] < mn[c]) ? v[c] : mn[c];
+          mx[c] = (mx[c] < v[c]) ? v[c] : mx[c];
+        }
+      }
+      // Triangle::calculateArea (primitives/Triangle.cpp:131-139)
+      F3 a = f3(pr.p0), b = f3(pr.p1), c = f3(pr.p2);
+      F3 n = cross(b - a, c - a);
+      pr.area = nefm::fsqrt(dot(n, n)) / 2.0f;
+      S.prims.push_back(pr);
+    }
+    md.has_bbox = 1;
+    memcpy(md.bbox_min, mn, 12);
+    memcpy(md.bbox_max, mx, 12);
+    md.use_bvh = 1;
+    S.models.push_back(md);
+  }
+
+  // io/SceneReader.cpp:650-675 processCameraAndRenderer and core/Camera.cpp:7-26.
+  void cameraAndRenderer(const JVal& cam, const JVal& ren) {
+    float position[3], lookAt[3], up[3];
+    vec3(need(cam, "position", "camera"), position, "camera position");
+    vec3(need(cam, "lookAt", "camera"), lookAt, "camera lookAt");
+    vec3(need(cam, "up", "camera"), up, "camera up");
+    float vfov = num(need(cam, "vfov", "camera"), "camera vfov");
+    const JVal& res = need(ren, "resolution", "renderer");
+    if (res.kind != JVal::ARR || res.arr.size() < 2) throw ParseError(NE_ERR_PARSE, "renderer resolution needs [W, H].");
+    int W = (int)res.arr[0].num, H = (int)res.arr[1].num;
+    if (W <= 0 || H <= 0) throw ParseError(NE_ERR_PARSE, "renderer resolution must be positive.");
+    float focus;
+    const JVal* af = cam.get("autoFocus");
+    if (af && af->kind == JVal::BOOL && af->b)
+      focus = 3.0f;  // (position - lookAt).length(): glm's component count
+    else
+      focus = num(need(cam, "focus", "camera"), "camera focus");
+    float aspect = float(W) / float(H);
+    float aperture = 0.0001f;  // SceneReader.cpp:668 passes 0.0001f, ignoring "aperture"
+    F3 upv = F3{0, 1, 0};      // and glm::vec3(0, 1, 0) as up
+    (void)up;
+    ne_camera& c = S.desc.camera;
+    c.lens_radius = aperture / 2.0f;
+    const float toRad = 0.01745329251994329576923690768489f;
+    float half = (vfov * toRad) / 2.0f;
+    float halfHeight = nefm::sin(half) / nefm::cos(half);
+    float halfWidth = aspect * halfHeight;
+    F3 pos = f3(position), la = f3(lookAt);
+    F3 front = normalize(pos - la);
+    F3 side = normalize(cross(upv, front));
+    F3 t1 = (focus * halfWidth) * (-side);
+    F3 t2 = (focus * halfHeight) * upv;
+    F3 t3 = focus * (-front);
+    F3 ll = ((pos - t1) - t2) - t3;
+    F3 hz = ((2.0f * focus) * halfWidth) * (-side);
+    F3 vt = ((2.0f * focus) * halfHeight) * upv;
+    put(c.position, pos);
+    put(c.lower_left, ll);
+    put(c.horizontal, hz);
+    put(c.vertical, vt);
+    put(c.side, side);
+    put(c.up, upv);
+    ne_settings& st = S.desc.settings;
+    st.width = W;
+    st.height = H;
+    st.spp = (int)num(need(ren, "spp", "renderer"), "renderer spp");
+    st.bounces = (int)num(need(ren, "bounces", "renderer"), "renderer bounces");
+    const JVal* hdr = ren.get("HDR");
+    st.hdr = (hdr && hdr->kind == JVal::BOOL && hdr->b) ? 1 : 0;
+    st.rr_enabled = 0;
+    st.rr_after = 3;
+    if (const JVal* rr = ren.get("rr")) {
+      st.rr_enabled = 1;
+      if (const JVal* a = rr->get("after")) st.rr_after = (int)num(*a, "rr after");
+    }
+  }
+
+  // io/SceneReader.cpp:10-54 loadScene.
+  void load(const JVal& doc) {
+    if (doc.kind != JVal::OBJ) throw ParseError(NE_ERR_PARSE, "Malformatted json file. Not a valid json object.");
+    if (!doc.get("version")) throw ParseError(NE_ERR_PARSE, "Incomplete json file. Version is not present.");
+    const JVal& mats = need(doc, "materials", "scene");
+    for (auto& m : mats.arr) material(m);
+    const JVal& prims = need(doc, "primitives", "scene");
+    for (auto& p : prims.arr) primitive(p);
+    cameraAndRenderer(need(doc, "camera", "scene"), need(doc, "renderer", "scene"));
+  }
+};
+
+void finalize(ne_scene_host& S, const std::vector<int>& grids_of_media) {
+  S.all_instances = S.instances;
+  S.all_instances.insert(S.all_instances.end(), S.light_instances.begin(), S.light_instances.end());
+  for (size_t i = 0; i < S.media.size(); i++) {
+    int g = grids_of_media[i];
+    S.media[i].grid = g >= 0 ? S.grids[g].data() : nullptr;
+  }
+  ne_scene_desc& d = S.desc;
+  d.n_instances = (uint32_t)S.instances.size();
+  d.n_light_instances = (uint32_t)S.light_instances.size();
+  d.instances = S.all_instances.data();
+  d.n_models = (uint32_t)S.models.size();
+  d.models = S.models.data();
+  d.n_prims = (uint32_t)S.prims.size();
+  d.prims = S.prims.data();
+  d.n_materials = (uint32_t)S.materials.size();
+  d.materials = S.materials.data();
+  d.n_model_materials = (uint32_t)S.model_materials.size();
+  d.model_materials = S.model_materials.data();
+  d.n_lights = (uint32_t)S.lights.size();
+  d.lights = S.lights.data();
+  d.n_media = (uint32_t)S.media.size();
+  d.media = S.media.data();
+}
+
+ne_status loadFromText(const std::string& text, const char* resources_dir, ne_scene_host** out, char* err,
+                       size_t err_len) {
+  if (!out) return NE_ERR_INVALID_ARG;
+  *out = nullptr;
+  std::unique_ptr<ne_scene_host> S(new ne_scene_host());
+  memset(&S->desc, 0, sizeof(S->desc));
+  try {
+    JParser jp{text.data(), text.data() + text.size()};
+    JVal doc = jp.parse();
+    Reader r{*S, resources_dir ? resources_dir : ""};
+    r.load(doc);
+    finalize(*S, r.grids_of_media);
+  } catch (const ParseError& e) {
+    if (err && err_len) snprintf(err, err_len, "%s", e.what());
+    return e.code;
+  } catch (const std::exception& e) {
+    if (err && err_len) snprintf(err, err_len, "%s", e.what());
+    return NE_ERR_PARSE;
+  }
+  *out = S.release();
+  return NE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+ne_status ne_scene_host_load_json(const char* path, const char* resources_dir, ne_scene_host** out, char* err,
+                                  size_t err_len) {
+  if (!path || !out) return NE_ERR_INVALID_ARG;
+  FILE* f = fopen(path, "rb");
+  if (!f) {
+    if (err && err_len) snprintf(err, err_len, "Couldn't read %s.", path);
+    return NE_ERR_MISSING_ASSET;
+  }
+  std::string text;
+  char buf[1 << 16];
+  size_t n;
+  while ((n = fread(buf, 1, sizeof(buf), f)) > 0) text.append(buf, n);
+  fclose(f);
+  return loadFromText(text, resources_dir, out, err, err_len);
+}
+
+ne_status ne_scene_host_load_json_string(const char* json, const char* resources_dir, ne_scene_host** out, char* err,
+                                         size_t err_len) {
+  if (!json || !out) return NE_ERR_INVALID_ARG;
+  return loadFromText(std::string(json), resources_dir, out, err, err_len);
+}
+
+const ne_scene_desc* ne_scene_host_desc(const ne_scene_host* s) { return s ? &s->desc : nullptr; }
+
+void ne_scene_host_destroy(ne_scene_host* s) { delete s; }
+
+}  // extern "C"

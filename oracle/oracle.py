@@ -1,0 +1,163 @@
+"""ctypes binding of the CPU oracle (liboracle.so).
+
+TEST INFRASTRUCTURE: imported only by tests/, __graft_entry__.smoke() and bench.py's
+CPU-baseline leg, as the checker or the timed CPU restatement of the reference; the
+product (narvalengine_gb300) never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+from narvalengine_gb300 import _abi  # noqa: E402  (struct layouts only)
+from narvalengine_gb300._abi import NeHit, NeRenderParams  # noqa: E402
+
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+_lib = None
+
+_F = C.POINTER(C.c_float)
+SIGNATURES = {
+    "orc_scene_create": (C.c_void_p, [C.POINTER(_abi.NeSceneDesc)]),
+    "orc_scene_destroy": (None, [C.c_void_p]),
+    "orc_trace_paths": (None, [C.c_void_p, C.POINTER(NeRenderParams), C.c_void_p, C.c_size_t, C.c_void_p, C.c_int]),
+    "orc_li_batch": (None, [C.c_void_p, C.POINTER(NeRenderParams), C.c_void_p, C.c_void_p, C.c_size_t, C.c_uint32,
+                            C.c_void_p, C.c_int]),
+    "orc_render": (C.c_double, [C.c_void_p, C.POINTER(NeRenderParams), C.c_void_p, C.c_int]),
+    "orc_render_pixels": (C.c_double, [C.c_void_p, C.POINTER(NeRenderParams), C.c_uint32, C.c_uint32, C.c_void_p,
+                                       C.c_int, C.POINTER(C.c_uint64)]),
+    "orc_trace_closest": (None, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_float, C.c_float, C.c_void_p]),
+    "orc_triangle_intersect": (C.c_int, [_F, _F, _F, C.c_void_p, _F, _F, _F, _F]),
+    "orc_aabb_intersect": (C.c_int, [_F, _F, C.c_void_p, _F, _F, _F, _F]),
+    "orc_orthonormal": (None, [_F, _F, _F]),
+    "orc_to_lcs": (None, [_F, _F, _F, _F, _F]),
+    "orc_to_world": (None, [_F, _F, _F, _F, _F]),
+    "orc_sample_unit_sphere": (None, [C.c_float, C.c_float, _F]),
+    "orc_hg_eval": (C.c_float, [C.c_float, _F, _F]),
+    "orc_hg_sample": (None, [C.c_float, C.c_float, C.c_float, _F]),
+    "orc_iso_pdf": (C.c_float, []),
+    "orc_barycentric": (None, [_F, _F, _F, _F, _F]),
+    "orc_triangle_area": (C.c_float, [_F, _F, _F]),
+    "orc_triangle_contains": (C.c_int, [_F, _F, _F, _F]),
+    "orc_point_in_triangle_range": (C.c_int, [_F, _F, _F, _F]),
+    "orc_triangle_model_intersect": (C.c_int, [_F, C.c_uint32, C.POINTER(C.c_uint32), C.c_uint32, C.c_void_p,
+                                               C.c_float, C.c_float, _F]),
+    "orc_bvh_build_count": (C.c_uint32, [_F, C.POINTER(C.c_uint32), C.c_uint32]),
+    "orc_fmath": (None, [C.c_int, C.c_void_p, C.c_size_t, C.c_void_p]),
+    "orc_rng": (None, [C.c_uint64, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
+    "orc_philox": (None, [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
+}
+
+
+def library() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            import importlib.util
+            spec = importlib.util.spec_from_file_location("oracle_build", os.path.join(HERE, "build.py"))
+            mod = importlib.util.module_from_spec(spec)
+            spec.loader.exec_module(mod)
+            mod.build()
+        lib = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def fv(*vals) -> C.Array:
+    return (C.c_float * len(vals))(*vals)
+
+
+def _p(a: np.ndarray) -> C.c_void_p:
+    return C.c_void_p(a.ctypes.data)
+
+
+class OracleScene:
+    """CPU restatement of the reference integrator over a scene description."""
+
+    def __init__(self, desc_ptr):
+        self._lib = library()
+        self._h = self._lib.orc_scene_create(desc_ptr)
+        if not self._h:
+            raise RuntimeError("orc_scene_create failed")
+        self.width = desc_ptr.contents.settings.width
+        self.height = desc_ptr.contents.settings.height
+
+    def trace_paths(self, keys: np.ndarray, params: NeRenderParams, threads: int = 0) -> np.ndarray:
+        keys = np.ascontiguousarray(keys, dtype=np.uint32).reshape(-1, 2)
+        out = np.empty((len(keys), 3), dtype=np.float32)
+        self._lib.orc_trace_paths(self._h, C.byref(params), _p(keys), len(keys), _p(out), threads or os.cpu_count())
+        return out
+
+    def li_batch(self, rays: np.ndarray, keys: np.ndarray, first_dim: int, params: NeRenderParams,
+                 threads: int = 0) -> np.ndarray:
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 6)
+        keys = np.ascontiguousarray(keys, dtype=np.uint32).reshape(-1, 2)
+        out = np.empty((len(rays), 3), dtype=np.float32)
+        self._lib.orc_li_batch(self._h, C.byref(params), _p(rays), _p(keys), len(rays), first_dim, _p(out),
+                               threads or os.cpu_count())
+        return out
+
+    def render(self, params: NeRenderParams, threads: int = 0):
+        out = np.zeros((self.height, self.width, 3), dtype=np.float32)
+        secs = self._lib.orc_render(self._h, C.byref(params), _p(out), threads or os.cpu_count())
+        return out, secs
+
+    def render_pixels(self, params: NeRenderParams, first: int, count: int, threads: int = 0):
+        out = np.zeros((count, 3), dtype=np.float32)
+        lookups = C.c_uint64(0)
+        secs = self._lib.orc_render_pixels(self._h, C.byref(params), first, count, _p(out),
+                                           threads or os.cpu_count(), C.byref(lookups))
+        return out, secs, lookups.value
+
+    def trace_closest(self, rays: np.ndarray, t_min: float, t_max: float) -> np.ndarray:
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 6)
+        out = (NeHit * len(rays))()
+        self._lib.orc_trace_closest(self._h, _p(rays), len(rays), t_min, t_max, C.addressof(out))
+        buf = (C.c_char * C.sizeof(out)).from_address(C.addressof(out))
+        from narvalengine_gb300 import HIT_DTYPE
+        return np.frombuffer(bytes(buf), dtype=HIT_DTYPE).copy()
+
+    def close(self):
+        if self._h:
+            self._lib.orc_scene_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def fmath(fn: int, x: np.ndarray) -> np.ndarray:
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    out = np.empty_like(x)
+    library().orc_fmath(fn, _p(x), x.size, _p(out))
+    return out
+
+
+def rng(seed: int, keys: np.ndarray, dims: np.ndarray) -> np.ndarray:
+    keys = np.ascontiguousarray(keys, dtype=np.uint32)
+    dims = np.ascontiguousarray(dims, dtype=np.uint32)
+    out = np.empty(len(dims), dtype=np.float32)
+    library().orc_rng(seed, _p(keys), _p(dims), len(dims), _p(out))
+    return out
+
+
+def philox(ctr, key):
+    c = (C.c_uint32 * 4)(*ctr)
+    k = (C.c_uint32 * 2)(*key)
+    o = (C.c_uint32 * 4)()
+    library().orc_philox(c, k, o)
+    return list(o)

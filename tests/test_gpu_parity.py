@@ -1,0 +1,178 @@
+"""GPU parity: the CUDA integrator against the CPU oracle, through the C ABI.
+
+Bar: bit-exact for hit/miss decisions, hit indices, t values, random numbers and the
+shared elementary functions; per-path radiance within 1e-4 relative (per channel,
+denominator max(|oracle|, 1e-6)) on identical (seed, pixel, sample) keys. In practice the
+two sides perform the same IEEE operations, so the radiance is expected to match exactly
+and the tests also report the exact-match fraction.
+"""
+import numpy as np
+import pytest
+
+from conftest import scene_path
+
+pytestmark = pytest.mark.gpu
+
+REL_TOL = 1e-4
+
+
+@pytest.fixture(scope="module")
+def ne(built):
+    import narvalengine_gb300 as ne
+    return ne
+
+
+@pytest.fixture(scope="module")
+def ctx(ne):
+    return ne.Context(0)
+
+
+@pytest.fixture(scope="module", params=["cornell_c1", "medium_c2"])
+def scenes(request, ne, ctx, oracle_lib):
+    host = ne.SceneHost.from_json(scene_path(request.param))
+    return request.param, host, ctx.upload(host), oracle_lib.OracleScene(host.desc_ptr)
+
+
+def rel_err(gpu, cpu):
+    return np.abs(gpu - cpu) / np.maximum(np.abs(cpu), 1e-6)
+
+
+def spread_keys(host, n_pixels, spp, seed=0):
+    rng = np.random.default_rng(seed)
+    pix = rng.choice(host.width * host.height, size=n_pixels, replace=False)
+    return np.array([[p, s] for p in pix for s in range(spp)], dtype=np.uint32)
+
+
+@pytest.mark.parametrize("fn,lo,hi", [(0, 1e-30, 1e30), (1, -100.0, 88.0), (2, -60.0, 60.0), (3, -60.0, 60.0),
+                                      (4, -1.0, 1.0), (5, -3.0, 3.0)])
+def test_fmath_bit_exact(ctx, oracle_lib, fn, lo, hi):
+    rng = np.random.default_rng(fn)
+    if fn == 0:
+        x = np.exp(rng.uniform(np.log(lo), np.log(hi), 200000)).astype(np.float32)
+        x = np.concatenate([x, np.array([1.0, 2.0, 0.5, 1e-45, 3.4e38, 1 - 2 ** -24, 2 ** -24], np.float32)])
+    else:
+        x = rng.uniform(lo, hi, 200000).astype(np.float32)
+        x = np.concatenate([x, np.array([0.0, -0.0, lo, hi], np.float32)])
+    g = ctx.fmath(fn, x)
+    c = oracle_lib.fmath(fn, x)
+    assert np.array_equal(g.view(np.uint32), c.view(np.uint32)), f"fn {fn}: {np.sum(g != c)} mismatches"
+
+
+def test_rng_bit_exact(ctx, oracle_lib):
+    rng = np.random.default_rng(3)
+    n = 100000
+    keys = rng.integers(0, 2 ** 32, size=(n, 2), dtype=np.uint64).astype(np.uint32)
+    dims = rng.integers(0, 5000, size=n, dtype=np.uint64).astype(np.uint32)
+    for seed in (0, 0x4E415256, 2 ** 63 + 12345):
+        g = ctx.rng(seed, keys, dims)
+        c = oracle_lib.rng(seed, keys, dims)
+        assert np.array_equal(g.view(np.uint32), c.view(np.uint32))
+        assert g.min() >= 0.0 and g.max() < 1.0
+
+
+def camera_rays(host, n, seed):
+    """Rays from the camera through random pixels, plus rays from random interior points."""
+    rng = np.random.default_rng(seed)
+    cam = host.camera_dict()
+    u = rng.random(n, dtype=np.float32)
+    v = rng.random(n, dtype=np.float32)
+    ll = np.array(cam["lower_left"], np.float32)
+    pos = np.array(cam["position"], np.float32)
+    pt = ll + u[:, None] * np.array(cam["horizontal"], np.float32) + v[:, None] * np.array(cam["vertical"], np.float32)
+    d = -(pt - pos)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    o = np.broadcast_to(pos, d.shape)
+    o2 = rng.uniform(-0.9, 0.9, size=(n, 3)).astype(np.float32) + np.array([0, 1.0, 0], np.float32)
+    d2 = rng.normal(size=(n, 3)).astype(np.float32)
+    d2 /= np.linalg.norm(d2, axis=1, keepdims=True)
+    rays = np.concatenate([np.concatenate([o, d], 1), np.concatenate([o2, d2], 1)]).astype(np.float32)
+    return rays
+
+
+@pytest.mark.parametrize("tmin", [1e-11, 1e-3])
+def test_closest_hit_bit_exact(scenes, tmin):
+    name, host, scene, orc = scenes
+    rays = camera_rays(host, 20000, 5)
+    g = scene.trace_closest(rays, tmin, float("inf"))
+    c = orc.trace_closest(rays, tmin, float("inf"))
+    assert np.array_equal(g["hit"], c["hit"])
+    assert np.array_equal(g["instance"], c["instance"])
+    assert np.array_equal(g["primitive"], c["primitive"])
+    for f in ("t_near", "t_far", "point", "normal"):
+        assert np.array_equal(g[f].view(np.uint32), c[f].view(np.uint32)), f"{name}: field {f} differs"
+    assert g["hit"].sum() > 0
+
+
+def test_camera_paths_parity(scenes, ne):
+    name, host, scene, orc = scenes
+    keys = spread_keys(host, 1024, 4, seed=1)
+    for seed in (0, 77):
+        p = ne.render_params(seed=seed)
+        g = scene.trace_paths(keys, p)
+        c = orc.trace_paths(keys, p)
+        assert np.isfinite(g).all()
+        err = rel_err(g, c)
+        exact = np.mean(np.all(g == c, axis=1))
+        assert err.max() <= REL_TOL, f"{name} seed {seed}: max rel {err.max():.3e}, exact {exact:.4f}"
+        assert exact == 1.0, f"{name}: only {exact:.4f} of paths bit-identical"
+
+
+def test_li_batch_parity(scenes, ne):
+    name, host, scene, orc = scenes
+    rays = camera_rays(host, 2048, 9)
+    rng = np.random.default_rng(2)
+    keys = rng.integers(0, 1 << 20, size=(len(rays), 2), dtype=np.uint64).astype(np.uint32)
+    p = ne.render_params(seed=5)
+    for first_dim in (0, 4, 1001):
+        g = scene.li_batch(rays, keys, first_dim, p)
+        c = orc.li_batch(rays, keys, first_dim, p)
+        assert rel_err(g, c).max() <= REL_TOL, f"{name} first_dim {first_dim}"
+
+
+def test_render_matches_oracle(scenes, ne):
+    name, host, scene, orc = scenes
+    p = ne.render_params(seed=3, spp=2)
+    g, stats = scene.render(p)
+    c, _ = orc.render(p)
+    assert stats["paths"] == host.width * host.height * 2
+    assert rel_err(g, c).max() <= REL_TOL, f"{name}: image differs"
+    assert np.array_equal(g, c), f"{name}: image not bit-identical"
+
+
+def test_render_ref_tiles(ne, ctx, oracle_lib):
+    # 250 x 130: the reference's 40 x 10 tiles of (6, 13) cover 240 x 130 pixels only
+    host = ne.SceneHost.from_json(scene_path("cornell_c1"))
+    import json
+    d = json.load(open(scene_path("cornell_c1")))
+    d["renderer"]["resolution"] = [250, 130]
+    host = ne.SceneHost.from_string(json.dumps(d))
+    scene = ctx.upload(host)
+    p = ne.render_params(seed=1, spp=1, flags=ne.NE_RENDER_REF_TILES)
+    g, stats = scene.render(p)
+    c, _ = oracle_lib.OracleScene(host.desc_ptr).render(p)
+    assert stats["paths"] == 240 * 130
+    assert np.all(g[:, 240:] == 0)
+    assert np.array_equal(g, c)
+
+
+def test_progressive_and_deterministic(ne, ctx):
+    host = ne.SceneHost.from_json(scene_path("cornell_c1"))
+    scene = ctx.upload(host)
+    a, _ = scene.render(ne.render_params(seed=9, spp=4))
+    b, _ = scene.render(ne.render_params(seed=9, spp=4))
+    assert np.array_equal(a, b)
+    # samples [0, 2) and [2, 4) rendered separately: their means average to the 4-sample mean
+    lo, _ = scene.render(ne.render_params(seed=9, spp=2, sample_offset=0))
+    hi, _ = scene.render(ne.render_params(seed=9, spp=2, sample_offset=2))
+    assert np.allclose((lo + hi) / 2, a, rtol=1e-5, atol=1e-6)
+
+
+def test_invalid_arguments(ne, ctx):
+    host = ne.SceneHost.from_json(scene_path("cornell_c1"))
+    scene = ctx.upload(host)
+    with pytest.raises(ne.NarvalError) as e:
+        scene.trace_paths(np.array([[host.width * host.height, 0]], np.uint32))
+    assert e.value.status == -1
+    out = scene.trace_paths(np.zeros((0, 2), np.uint32))
+    assert out.shape == (0, 3)
+    assert scene.trace_closest(np.zeros((0, 6), np.float32)).shape == (0,)
