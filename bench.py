@@ -1,0 +1,338 @@
+"""Benchmark: camera paths per second of the GB300 path integrator vs the CPU restatement.
+
+Workload (one step): a full render of the single heterogeneous medium scene
+(narvalengine_gb300/scenes/medium_c2.json): 128^3 seeded simplex-fBm density grid, density
+scale 20, albedo 0.9, HG g = 0.8, directional sun 3.0 at 30 deg elevation plus a constant
+environment 0.2, 512 x 512 pixels x 64 spp, depth 64: 16 777 216 camera paths in the
+reference's integrator semantics.
+
+  value   Mpaths/s of ne_render with the scene resident in HBM and the image written to
+          device memory; each step timed with CUDA events on the library's stream, the
+          L2 cache flushed (256 MiB write) between steps outside the timed events.
+  e2e     Mpaths/s through the public C ABI with host buffers: every step uploads the
+          scene from pinned host memory (ne_scene_upload), renders, and reads the image
+          back to pinned host memory (ne_render), timed on the host clock.
+  roofline  the path kernel against HBM bandwidth: algorithmic bytes = 32 B per trilinear
+          density lookup (8 FP32 voxels), lookups counted by an instrumented run of the same
+          kernel on the same paths, divided by the kernel's event-timed duration.
+  cpu_baseline  the CPU restatement of the reference integrator (oracle/, the reference
+          itself does not build here) on all host cores over a bounded pixel sample.
+
+--impl reference times that CPU restatement alone on the same workload and metric.
+Under torchrun (N > 1), rank r renders samples [r*64, (r+1)*64) of the same image on its
+own GPU (weak scaling, no collective on the data path); rank 0 reports total paths over
+the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SCENE = "medium_c2.json"
+WORKLOAD = "medium_c2: 128^3 fBm grid (scale 20, albedo 0.9, HG g=0.8), sun 3.0 @30deg + env 0.2, 512x512x64spp, depth 64"
+METRIC = "Mpaths/s (camera paths x spp per second, reference integrator semantics)"
+BYTES_PER_LOOKUP = 32  # 8 FP32 voxels per trilinear density lookup
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    """Barrier and max-reduction across ranks (torch.distributed when WORLD_SIZE > 1)."""
+
+    def __init__(self, world: int, backend: str):
+        self.world = world
+        self.dist = None
+        if world > 1:
+            import torch.distributed as dist
+            dist.init_process_group(backend=backend)
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.dist:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        if self.dist.get_backend() == "nccl":
+            t = t.cuda()
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.dist:
+            self.dist.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def load_peaks() -> tuple[float, str]:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        try:
+            return float(json.load(open(p))["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def cpu_baseline(host, spp: int, target_s: float, threads: int) -> dict:
+    """The CPU restatement of the reference integrator on a bounded pixel sample."""
+    from oracle import oracle as orc
+    import narvalengine_gb300 as ne
+    o = orc.OracleScene(host.desc_ptr)
+    params = ne.render_params(seed=1, spp=spp)
+    W, H = host.width, host.height
+    # calibrate on one row of pixels through the image centre, then size the sample
+    row = (H // 2) * W
+    n = 64
+    _, secs, _ = o.render_pixels(params, row, n, threads)
+    per_pixel = max(secs / n, 1e-7)
+    n = int(min(W * H, max(n, target_s / per_pixel)))
+    first = max(0, (W * H - n) // 2)
+    _, secs, _ = o.render_pixels(params, first, n, threads)
+    paths = n * spp
+    o.close()
+    return {"value": paths / secs / 1e6, "unit": "Mpaths/s", "cores": threads, "kind": "port",
+            "sample": f"{n} consecutive pixels centred on the image x {spp} spp = {paths} paths, {secs:.2f} s"}
+
+
+def run_reference(args, rank: int, world: int):
+    import narvalengine_gb300 as ne
+    if rank != 0:
+        return
+    host = ne.SceneHost.from_json(os.path.join(ne.SCENES_DIR, SCENE))
+    threads = os.cpu_count() or 1
+    per = max(2.0, 20.0 / max(1, args.steps))
+    for _ in range(args.warmup):
+        cpu_baseline(host, host.spp, 0.5, threads)
+    vals = [cpu_baseline(host, host.spp, per, threads) for _ in range(args.steps)]
+    v = statistics.median(x["value"] for x in vals)
+    line = {"metric": METRIC, "value": v, "unit": "Mpaths/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded fBm grid)", "impl": "reference",
+            "config": {"workload": WORKLOAD, "sample": "bounded pixel sample per step"},
+            "cpu_baseline": dict(vals[-1], value=v),
+            "e2e": {"value": v, "unit": "Mpaths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_profile_case(spp: int):
+    """Small case for ncu: the same scene at a reduced sample count, rendered twice."""
+    import narvalengine_gb300 as ne
+    ctx = ne.Context(0)
+    host = ne.SceneHost.from_json(os.path.join(ne.SCENES_DIR, SCENE))
+    scene = ctx.upload(host)
+    for i in range(2):
+        _, st = scene.render(ne.render_params(seed=1, spp=spp))
+    _, cst = scene.render(ne.render_params(seed=1, spp=spp, flags=ne.NE_RENDER_COUNT_WORK))
+    print(json.dumps({"profile_case": {"spp": spp, "paths": st["paths"], "kernel_ms": st["kernel_ms"],
+                                       "density_lookups": cst["density_lookups"],
+                                       "scene_queries": cst["scene_queries"]}}), flush=True)
+    scene.close()
+    ctx.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile-spp", type=int, default=0,
+                    help="profiling case: two renders of the workload at this spp (the second is the one to capture)")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if args.profile_spp > 0:
+        run_profile_case(args.profile_spp)
+        return
+
+    import narvalengine_gb300 as ne
+    d = Dist(world, "nccl")
+    ctx = ne.Context(local)
+    host = ne.SceneHost.from_json(os.path.join(ne.SCENES_DIR, SCENE))
+    scene = ctx.upload(host)
+    W, H, spp = host.width, host.height, host.spp
+    paths_per_step = W * H * spp
+    img_bytes = W * H * 3 * 4
+
+    # device output buffer for the resident-input leg
+    import torch
+    dev_img = torch.empty(W * H * 3, dtype=torch.float32, device=f"cuda:{local}")
+    base = rank * spp  # weak scaling: rank r renders samples [r*spp, (r+1)*spp)
+    p = ne.render_params(seed=1, sample_offset=base, flags=ne.NE_RENDER_OUT_DEVICE)
+
+    # work counters of one launch (instrumented kernel, outside the timed region)
+    pc = ne.render_params(seed=1, sample_offset=base, flags=ne.NE_RENDER_OUT_DEVICE | ne.NE_RENDER_COUNT_WORK)
+    _, cstats = scene.render(pc, out=dev_img.data_ptr())
+
+    for _ in range(args.warmup):
+        scene.render(p, out=dev_img.data_ptr())
+    ctx.synchronize()
+    d.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    kernel_ms, step_ms = [], []
+    for _ in range(args.steps):
+        ctx.flush_l2(256 << 20)
+        ctx.record(0)
+        _, st = scene.render(p, out=dev_img.data_ptr())
+        ctx.record(1)
+        step_ms.append(ctx.elapsed_ms(0, 1))
+        kernel_ms.append(st["kernel_ms"])
+    ctx.synchronize()
+    clk = clocks.stop()
+    local_ms = sum(step_ms)
+    d.barrier()
+    total_ms = d.max(local_ms)
+    value = paths_per_step * args.steps * world / (total_ms / 1e3) / 1e6
+
+    # e2e: host buffers through the public API, copies inside the timed region
+    import ctypes
+    pinned_grid = None
+    desc = host.desc
+    h2d = 0
+    for i in range(desc.n_media):
+        m = desc.media[i]
+        if m.type == 0:
+            n = m.res[0] * m.res[1] * m.res[2]
+            pinned_grid = torch.empty(n, dtype=torch.float32, pin_memory=True)
+            ctypes.memmove(pinned_grid.data_ptr(), ctypes.addressof(m.grid.contents), n * 4)
+            m.grid = ctypes.cast(pinned_grid.data_ptr(), ctypes.POINTER(ctypes.c_float))
+            h2d += n * 4
+    # instance, model, primitive, material and light tables (a few KB next to the grid)
+    from narvalengine_gb300 import _abi
+    h2d += (desc.n_instances + desc.n_light_instances) * ctypes.sizeof(_abi.NeInstance) + \
+        desc.n_models * ctypes.sizeof(_abi.NeModel) + desc.n_prims * ctypes.sizeof(_abi.NePrimitive) + \
+        desc.n_materials * ctypes.sizeof(_abi.NeMaterial) + desc.n_lights * ctypes.sizeof(_abi.NeLight) + \
+        desc.n_media * ctypes.sizeof(_abi.NeMedium) + desc.n_model_materials * 4
+    out_host = torch.empty((H, W, 3), dtype=torch.float32, pin_memory=True).numpy()
+    pe = ne.render_params(seed=1, sample_offset=base)
+    for _ in range(1):
+        s2 = ctx.upload(host)
+        s2.render(pe, out=out_host)
+        s2.close()
+    d.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s2 = ctx.upload(host)
+        s2.render(pe, out=out_host)
+        s2.close()
+    e2e_s = time.perf_counter() - t0
+    d.barrier()
+    e2e_s = d.max(e2e_s)
+    e2e = paths_per_step * args.steps * world / e2e_s / 1e6
+
+    peak, peak_kind = load_peaks()
+    k_ms = statistics.mean(kernel_ms)
+    lookups = cstats["density_lookups"]
+    achieved = lookups * BYTES_PER_LOOKUP / (k_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_source": peak_kind, "traffic": None,
+                "kernel": "k_paths (persistent camera-path kernel)",
+                "algorithmic_bytes_per_launch": lookups * BYTES_PER_LOOKUP,
+                "density_lookups_per_launch": lookups, "scene_queries_per_launch": cstats["scene_queries"],
+                "kernel_ms": k_ms}
+    traffic_file = os.path.join(ROOT, "profiles", "k_paths_medium_c2_traffic.json")
+    if os.path.exists(traffic_file):
+        try:
+            roofline["traffic"] = json.load(open(traffic_file))["dram_bytes_per_launch"]
+        except Exception:
+            pass
+
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu and world == 1:
+            cpu = cpu_baseline(host, spp, args.cpu_seconds, os.cpu_count() or 1)
+        line = {"metric": METRIC, "value": value, "unit": "Mpaths/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded fBm grid)",
+                "config": {"workload": WORKLOAD, "paths_per_step": paths_per_step, "pixels": [W, H], "spp": spp,
+                           "bounces": host.bounces, "l2": "flushed between steps (256 MiB write, outside events)",
+                           "parallelism": f"{world} GPU(s), sample ranges per rank"},
+                "e2e": {"value": e2e, "unit": "Mpaths/s", "h2d_bytes_per_step": h2d,
+                        "d2h_bytes_per_step": img_bytes},
+                "gpu_launches": 2 * args.steps,
+                "roofline": roofline, "cpu_baseline": cpu, "clocks": clk}
+        print(json.dumps(line), flush=True)
+    scene.close()
+    ctx.close()
+    d.close()
+
+
+if __name__ == "__main__":
+    main()

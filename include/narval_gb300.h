@@ -127,6 +127,16 @@ ne_status ne_li_batch(ne_scene* scene, const ne_render_params* params, const ne_
 ne_status ne_trace_closest(ne_scene* scene, const ne_ray* rays, size_t n, float t_min, float t_max,
                            ne_hit* out);
 
+/* ---- timing utilities on the context's stream (for benchmarks) ---- */
+
+/* Records CUDA event `slot` (0-7) on the context's stream. */
+ne_status ne_context_event_record(ne_context* ctx, int slot);
+/* Milliseconds between two recorded events; waits for the later one. */
+ne_status ne_context_event_elapsed(ne_context* ctx, int slot_begin, int slot_end, float* ms);
+ne_status ne_context_synchronize(ne_context* ctx);
+/* Writes `bytes` of scratch memory on the context's stream, evicting the L2 cache. */
+ne_status ne_context_flush_l2(ne_context* ctx, size_t bytes);
+
 /* Device copies of the shared elementary functions, for bit-exactness checks.
  * fn: 0 log, 1 exp, 2 sin, 3 cos, 4 acos, 5 pow5. */
 ne_status ne_debug_fmath(ne_context* ctx, int fn, const float* x, size_t n, float* out);

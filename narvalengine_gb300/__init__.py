@@ -154,6 +154,20 @@ class Context:
         self.check(library().ne_scene_upload(self._h, host.desc_ptr, C.byref(h)))
         return Scene(self, h, host)
 
+    def record(self, slot: int):
+        self.check(library().ne_context_event_record(self._h, slot))
+
+    def elapsed_ms(self, a: int, b: int) -> float:
+        ms = C.c_float()
+        self.check(library().ne_context_event_elapsed(self._h, a, b, C.byref(ms)))
+        return ms.value
+
+    def synchronize(self):
+        self.check(library().ne_context_synchronize(self._h))
+
+    def flush_l2(self, nbytes: int = 256 << 20):
+        self.check(library().ne_context_flush_l2(self._h, nbytes))
+
     def fmath(self, fn: int, x: np.ndarray) -> np.ndarray:
         x = np.ascontiguousarray(x, dtype=np.float32)
         out = np.empty_like(x)

@@ -118,6 +118,10 @@ SIGNATURES = {
     "ne_li_batch": (C.c_int32, [C.c_void_p, C.POINTER(NeRenderParams), C.c_void_p, C.c_void_p, C.c_size_t,
                                 C.c_uint32, C.c_void_p]),
     "ne_trace_closest": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_float, C.c_float, C.c_void_p]),
+    "ne_context_event_record": (C.c_int32, [C.c_void_p, C.c_int]),
+    "ne_context_event_elapsed": (C.c_int32, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_float)]),
+    "ne_context_synchronize": (C.c_int32, [C.c_void_p]),
+    "ne_context_flush_l2": (C.c_int32, [C.c_void_p, C.c_size_t]),
     "ne_debug_fmath": (C.c_int32, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t, C.c_void_p]),
     "ne_debug_rng": (C.c_int32, [C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
 }

@@ -28,6 +28,9 @@ struct ne_context {
   int sm_count = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t user_ev[8] = {};
+  void* flush_buf = nullptr;
+  size_t flush_bytes = 0;
   std::string err;
   unsigned long long* d_counter = nullptr;  // [0] work counter, [1..4] work counters
   uint32_t* d_err = nullptr;
@@ -336,6 +339,9 @@ void ne_context_destroy(ne_context* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (int i = 0; i < 4; i++)
     if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+  for (int i = 0; i < 8; i++)
+    if (ctx->user_ev[i]) cudaEventDestroy(ctx->user_ev[i]);
+  if (ctx->flush_buf) cudaFree(ctx->flush_buf);
   if (ctx->d_counter) cudaFree(ctx->d_counter);
   if (ctx->d_err) cudaFree(ctx->d_err);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -732,6 +738,42 @@ ne_status ne_trace_closest(ne_scene* sc, const ne_ray* rays, size_t n, float t_m
           "k_closest launch");
   NE_CUDA(cudaMemcpyAsync(out, dh.p, n * sizeof(ne_hit), cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync");
   return checkErr(ctx);
+}
+
+ne_status ne_context_event_record(ne_context* ctx, int slot) {
+  if (!ctx || slot < 0 || slot >= 8) return NE_ERR_INVALID_ARG;
+  NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  if (!ctx->user_ev[slot]) NE_CUDA(cudaEventCreate(&ctx->user_ev[slot]), "cudaEventCreate");
+  NE_CUDA(cudaEventRecord(ctx->user_ev[slot], ctx->stream), "cudaEventRecord");
+  return NE_OK;
+}
+
+ne_status ne_context_event_elapsed(ne_context* ctx, int a, int b, float* ms) {
+  if (!ctx || !ms || a < 0 || a >= 8 || b < 0 || b >= 8 || !ctx->user_ev[a] || !ctx->user_ev[b]) return NE_ERR_INVALID_ARG;
+  NE_CUDA(cudaEventSynchronize(ctx->user_ev[b]), "cudaEventSynchronize");
+  NE_CUDA(cudaEventElapsedTime(ms, ctx->user_ev[a], ctx->user_ev[b]), "cudaEventElapsedTime");
+  return NE_OK;
+}
+
+ne_status ne_context_synchronize(ne_context* ctx) {
+  if (!ctx) return NE_ERR_INVALID_ARG;
+  NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  NE_CUDA(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  return NE_OK;
+}
+
+ne_status ne_context_flush_l2(ne_context* ctx, size_t bytes) {
+  if (!ctx || bytes == 0) return NE_ERR_INVALID_ARG;
+  NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  if (ctx->flush_bytes < bytes) {
+    if (ctx->flush_buf) cudaFree(ctx->flush_buf);
+    ctx->flush_buf = nullptr;
+    ctx->flush_bytes = 0;
+    NE_CUDA(cudaMalloc(&ctx->flush_buf, bytes), "cudaMalloc(flush)");
+    ctx->flush_bytes = bytes;
+  }
+  NE_CUDA(cudaMemsetAsync(ctx->flush_buf, (int)(bytes & 0xff), bytes, ctx->stream), "cudaMemsetAsync(flush)");
+  return NE_OK;
 }
 
 ne_status ne_debug_fmath(ne_context* ctx, int fn, const float* x, size_t n, float* out) {
