@@ -185,12 +185,13 @@ def run_reference(args, rank: int, world: int):
     print(json.dumps(line), flush=True)
 
 
-def run_profile_case(spp: int):
+def run_profile_case(spp: int, kernel: int, track_share: int):
     """Small case for ncu: the same scene at a reduced sample count, rendered twice."""
     import narvalengine_gb300 as ne
     ctx = ne.Context(0)
     host = ne.SceneHost.from_json(os.path.join(ne.SCENES_DIR, SCENE))
     scene = ctx.upload(host)
+    scene.set_tuning(kernel=kernel, track_share=track_share)
     for i in range(2):
         _, st = scene.render(ne.render_params(seed=1, spp=spp))
     _, cst = scene.render(ne.render_params(seed=1, spp=spp, flags=ne.NE_RENDER_COUNT_WORK))
@@ -209,6 +210,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--kernel", type=int, default=3, help="path kernel (ne_tuning.kernel): 0 straight, 3 regrouped")
+    ap.add_argument("--track-share", type=int, default=16, help="regrouped kernel tracking threshold, 32nds")
     ap.add_argument("--profile-spp", type=int, default=0,
                     help="profiling case: two renders of the workload at this spp (the second is the one to capture)")
     args = ap.parse_args()
@@ -218,7 +221,7 @@ def main():
         run_reference(args, rank, world)
         return
     if args.profile_spp > 0:
-        run_profile_case(args.profile_spp)
+        run_profile_case(args.profile_spp, args.kernel, args.track_share)
         return
 
     import narvalengine_gb300 as ne
@@ -226,6 +229,7 @@ def main():
     ctx = ne.Context(local)
     host = ne.SceneHost.from_json(os.path.join(ne.SCENES_DIR, SCENE))
     scene = ctx.upload(host)
+    scene.set_tuning(kernel=args.kernel, track_share=args.track_share)
     W, H, spp = host.width, host.height, host.spp
     paths_per_step = W * H * spp
     img_bytes = W * H * 3 * 4
@@ -284,12 +288,14 @@ def main():
     pe = ne.render_params(seed=1, sample_offset=base)
     for _ in range(1):
         s2 = ctx.upload(host)
+        s2.set_tuning(kernel=args.kernel, track_share=args.track_share)
         s2.render(pe, out=out_host)
         s2.close()
     d.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         s2 = ctx.upload(host)
+        s2.set_tuning(kernel=args.kernel, track_share=args.track_share)
         s2.render(pe, out=out_host)
         s2.close()
     e2e_s = time.perf_counter() - t0
@@ -303,7 +309,7 @@ def main():
     achieved = lookups * BYTES_PER_LOOKUP / (k_ms / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": peak_kind, "traffic": None,
-                "kernel": "k_paths (persistent camera-path kernel)",
+                "kernel": "k_sched (regrouped path kernel)" if args.kernel == 3 else "k_paths (straight path kernel)",
                 "algorithmic_bytes_per_launch": lookups * BYTES_PER_LOOKUP,
                 "density_lookups_per_launch": lookups, "scene_queries_per_launch": cstats["scene_queries"],
                 "kernel_ms": k_ms}
@@ -323,7 +329,8 @@ def main():
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded fBm grid)",
                 "config": {"workload": WORKLOAD, "paths_per_step": paths_per_step, "pixels": [W, H], "spp": spp,
                            "bounces": host.bounces, "l2": "flushed between steps (256 MiB write, outside events)",
-                           "parallelism": f"{world} GPU(s), sample ranges per rank"},
+                           "parallelism": f"{world} GPU(s), sample ranges per rank",
+                           "tuning": scene.tuning()},
                 "e2e": {"value": e2e, "unit": "Mpaths/s", "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": img_bytes},
                 "gpu_launches": 2 * args.steps,

@@ -127,6 +127,21 @@ ne_status ne_li_batch(ne_scene* scene, const ne_render_params* params, const ne_
 ne_status ne_trace_closest(ne_scene* scene, const ne_ray* rays, size_t n, float t_min, float t_max,
                            ne_hit* out);
 
+/* Launch configuration of the path kernels of one scene (picked by an autotuner or by hand).
+ * kernel: 0 = straight kernel (one path per lane to completion), 1/2 = the same with at most
+ * 80/64 registers per thread, 3 = regrouped state-machine kernel (lanes refill as paths finish;
+ * a warp steps tracking walks together while at least track_share/32 of its live lanes are in
+ * one). blocks_per_sm: persistent blocks per SM, 0 = as many as fit. */
+typedef struct ne_tuning {
+  int32_t kernel;
+  int32_t track_share;
+  int32_t blocks_per_sm;
+  int32_t pad;
+} ne_tuning;
+
+ne_status ne_scene_set_tuning(ne_scene* scene, const ne_tuning* tuning);
+ne_status ne_scene_get_tuning(const ne_scene* scene, ne_tuning* tuning);
+
 /* ---- timing utilities on the context's stream (for benchmarks) ---- */
 
 /* Records CUDA event `slot` (0-7) on the context's stream. */

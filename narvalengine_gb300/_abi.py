@@ -78,6 +78,10 @@ class NeRenderParams(C.Structure):
                 ("rr_after", C.c_int32), ("sample_offset", C.c_uint32), ("flags", C.c_uint32)]
 
 
+class NeTuning(C.Structure):
+    _fields_ = [("kernel", C.c_int32), ("track_share", C.c_int32), ("blocks_per_sm", C.c_int32), ("pad", C.c_int32)]
+
+
 class NeRenderStats(C.Structure):
     _fields_ = [("kernel_ms", C.c_double), ("total_ms", C.c_double), ("paths", C.c_uint64),
                 ("density_lookups", C.c_uint64), ("scene_queries", C.c_uint64), ("bvh_nodes", C.c_uint64),
@@ -118,6 +122,8 @@ SIGNATURES = {
     "ne_li_batch": (C.c_int32, [C.c_void_p, C.POINTER(NeRenderParams), C.c_void_p, C.c_void_p, C.c_size_t,
                                 C.c_uint32, C.c_void_p]),
     "ne_trace_closest": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_float, C.c_float, C.c_void_p]),
+    "ne_scene_set_tuning": (C.c_int32, [C.c_void_p, C.POINTER(NeTuning)]),
+    "ne_scene_get_tuning": (C.c_int32, [C.c_void_p, C.POINTER(NeTuning)]),
     "ne_context_event_record": (C.c_int32, [C.c_void_p, C.c_int]),
     "ne_context_event_elapsed": (C.c_int32, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_float)]),
     "ne_context_synchronize": (C.c_int32, [C.c_void_p]),

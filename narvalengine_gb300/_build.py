@@ -20,7 +20,7 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libnarval_gb300.so")
 
-CUDA_SOURCES = ["api.cu", "k_paths_plain.cu", "k_paths_count.cu", "k_query.cu"]
+CUDA_SOURCES = ["api.cu", "k_paths_plain.cu", "k_paths_occ.cu", "k_paths_count.cu", "k_sched.cu", "k_query.cu"]
 HOST_SOURCES = ["scene_host.cpp", "scene_gen.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [

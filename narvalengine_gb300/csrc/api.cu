@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -44,6 +45,8 @@ struct ne_scene {
   float* d_paths = nullptr;  // per-path radiance scratch of ne_render
   size_t paths_cap = 0;
   int blocks_per_sm = 1;
+  int variant = 0;           // path kernel (NE_PATHS_VARIANT: 0-2 straight k_paths, 3 regrouped k_sched)
+  int track_share = 16;      // k_sched tracking-phase threshold (NE_TRACK_SHARE, 32nds of live lanes)
 };
 
 namespace {
@@ -289,7 +292,14 @@ ne_status launchPaths(ne_scene* sc, const PathArgs& a, bool count) {
   int blocks = persistentBlocks(sc);
   unsigned long long needed = (a.total + kThreads - 1) / kThreads;
   if ((unsigned long long)blocks > needed) blocks = (int)std::max<unsigned long long>(1, needed);
-  NE_CUDA(ne_launch_paths(count, blocks, ctx->stream, sc->d, a, ctx->d_counter, ctx->d_err), "k_paths launch");
+  if (sc->variant == 3) {
+    PathArgs b = a;
+    b.track_share = sc->track_share;
+    NE_CUDA(ne_launch_sched(count, blocks, ctx->stream, sc->d, b, ctx->d_counter, ctx->d_err), "k_sched launch");
+  } else {
+    NE_CUDA(ne_launch_paths(count, count ? 0 : sc->variant, blocks, ctx->stream, sc->d, a, ctx->d_counter, ctx->d_err),
+            "k_paths launch");
+  }
   return NE_OK;
 }
 
@@ -569,12 +579,41 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
   sc->d.camera.lens_radius = cm.lens_radius;
   sc->d.width = D.settings.width;
   sc->d.height = D.settings.height;
-  int bps = 1;
-  if (ne_paths_occupancy(&bps) != cudaSuccess || bps < 1) bps = 1;
-  sc->blocks_per_sm = bps;
+  ne_tuning tn;
+  tn.kernel = sc->variant;
+  tn.track_share = sc->track_share;
+  tn.blocks_per_sm = 0;
+  tn.pad = 0;
+  if (const char* v = getenv("NE_PATHS_VARIANT")) tn.kernel = atoi(v);
+  if (const char* v = getenv("NE_TRACK_SHARE")) tn.track_share = atoi(v);
+  if (ne_scene_set_tuning(sc, &tn) != NE_OK) return cleanup(NE_ERR_INVALID_ARG);
   cudaError_t e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return cleanup(cudaFail(ctx, e, "scene upload"));
   *out = sc;
+  return NE_OK;
+}
+
+ne_status ne_scene_set_tuning(ne_scene* sc, const ne_tuning* t) {
+  if (!sc || !t || t->kernel < 0 || t->kernel > 3 || t->track_share < 1 || t->track_share > 32 ||
+      t->blocks_per_sm < 0 || t->blocks_per_sm > 64)
+    return NE_ERR_INVALID_ARG;
+  ne_context* ctx = sc->ctx;
+  int fit = 1;
+  cudaError_t e = t->kernel == 3 ? ne_sched_occupancy(&fit) : ne_paths_occupancy(t->kernel, &fit);
+  if (e != cudaSuccess) return cudaFail(ctx, e, "occupancy query");
+  if (fit < 1) fit = 1;
+  sc->variant = t->kernel;
+  sc->track_share = t->track_share;
+  sc->blocks_per_sm = t->blocks_per_sm > 0 ? std::min(t->blocks_per_sm, fit) : fit;
+  return NE_OK;
+}
+
+ne_status ne_scene_get_tuning(const ne_scene* sc, ne_tuning* t) {
+  if (!sc || !t) return NE_ERR_INVALID_ARG;
+  t->kernel = sc->variant;
+  t->track_share = sc->track_share;
+  t->blocks_per_sm = sc->blocks_per_sm;
+  t->pad = 0;
   return NE_OK;
 }
 
@@ -632,6 +671,7 @@ ne_status ne_render(ne_scene* sc, const ne_render_params* p, float* out_rgb, ne_
   a.cover_w = cw;
   a.keys = nullptr;
   a.out = sc->d_paths;
+  a.track_share = 16;
   if (timed) NE_CUDA(cudaEventRecord(ctx->ev[1], ctx->stream), "cudaEventRecord");
   ne_status st = launchPaths(sc, a, (flags & NE_RENDER_COUNT_WORK) != 0);
   if (st) return st;
@@ -693,6 +733,7 @@ ne_status ne_trace_paths(ne_scene* sc, const ne_render_params* p, const ne_path_
   a.cover_w = (uint32_t)sc->settings.width;
   a.keys = dk.p;
   a.out = dout.p;
+  a.track_share = 16;
   ne_status st = launchPaths(sc, a, false);
   if (st) return st;
   NE_CUDA(cudaMemcpyAsync(out_L, dout.p, n * 3 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync");

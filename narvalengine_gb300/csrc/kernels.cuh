@@ -6,6 +6,7 @@
 
 #include "narval_gb300.h"
 #include "pt_device.cuh"
+#include "pt_sched.cuh"
 
 namespace nedev {
 
@@ -20,7 +21,15 @@ struct PathArgs {
   uint32_t cover_w;          // rendered rectangle width (pixels)
   const ne_path_key* keys;   // explicit keys (ne_trace_paths) or null
   float* out;                // total * 3 floats
+  int track_share;           // regrouped kernel: tracking-phase threshold in 32nds of live lanes
 };
+
+template <bool C>
+__global__ void __launch_bounds__(kThreads) k_sched(const __grid_constant__ DScene s, const PathArgs a,
+                                                    unsigned long long* __restrict__ counter, uint32_t* err) {
+  schedLoop<C>(s, a.P, a.base, a.total, a.spp, a.sample_offset, a.cover_w, a.keys, a.out, counter, err,
+               a.track_share);
+}
 
 template <bool C>
 __device__ __forceinline__ void flushCounters(const Counters& cn, unsigned long long* g) {
@@ -34,8 +43,9 @@ __device__ __forceinline__ void flushCounters(const Counters& cn, unsigned long 
   }
 }
 
-template <bool C>
-__global__ void __launch_bounds__(kThreads) k_paths(const __grid_constant__ DScene s, const PathArgs a,
+// MINB > 1 caps registers per thread (65536 / (128 * MINB)) so more warps stay resident.
+template <bool C, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) k_paths(const __grid_constant__ DScene s, const PathArgs a,
                                                       unsigned long long* __restrict__ counter, uint32_t* err) {
   Ctx<C> c{s, Sampler{}, Counters{0, 0, 0, 0}, err};
   const int lane = threadIdx.x & 31;
@@ -69,9 +79,17 @@ __global__ void __launch_bounds__(kThreads) k_paths(const __grid_constant__ DSce
 }  // namespace nedev
 
 // Launchers (defined next to each kernel instantiation).
-cudaError_t ne_launch_paths(bool count, int blocks, cudaStream_t st, const nedev::DScene& s, const nedev::PathArgs& a,
+// variant: 0 = compiler's register choice, 1 = at most 80 registers, 2 = at most 64 registers,
+// 3 = regrouped state-machine kernel (k_sched).
+cudaError_t ne_launch_paths(bool count, int variant, int blocks, cudaStream_t st, const nedev::DScene& s,
+                            const nedev::PathArgs& a, unsigned long long* counter, uint32_t* err);
+cudaError_t ne_paths_occupancy(int variant, int* blocks_per_sm);
+cudaError_t ne_launch_paths_variant(int variant, int blocks, cudaStream_t st, const nedev::DScene& s,
+                                    const nedev::PathArgs& a, unsigned long long* counter, uint32_t* err);
+cudaError_t ne_paths_occupancy_variant(int variant, int* blocks_per_sm);
+cudaError_t ne_launch_sched(bool count, int blocks, cudaStream_t st, const nedev::DScene& s, const nedev::PathArgs& a,
                             unsigned long long* counter, uint32_t* err);
-cudaError_t ne_paths_occupancy(int* blocks_per_sm);
+cudaError_t ne_sched_occupancy(int* blocks_per_sm);
 cudaError_t ne_launch_li(int blocks, cudaStream_t st, const nedev::DScene& s, nedev::PathParams P, nerng::PathKey base,
                          const ne_ray* rays, const ne_path_key* keys, size_t n, uint32_t first_dim, float* out,
                          uint32_t* err);

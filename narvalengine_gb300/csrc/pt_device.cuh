@@ -27,6 +27,9 @@
 namespace nedev {
 
 #define NE_D __device__ __forceinline__
+// Large functions called from several places stay out of line so that their code exists
+// once: with divergent lanes the fully inlined kernel stalls on instruction fetch.
+#define NE_NI static __device__ __noinline__
 
 constexpr double kPiD = 3.14159265358979323846264338327950288;
 constexpr double kTwoPiD = 6.283185307179586476925286766559;
@@ -111,6 +114,11 @@ struct Sampler {
   uint32_t dim;
   uint32_t blk;
   uint32_t w0, w1, w2, w3;
+  __device__ __noinline__ void refill(uint32_t b) {
+    nerng::Block r = nerng::philox4x32_10(b, key.sample, key.pixel, key.stream, key.seed_lo, key.seed_hi);
+    w0 = r.w[0]; w1 = r.w[1]; w2 = r.w[2]; w3 = r.w[3];
+    blk = b;
+  }
   NE_D void reset(const nerng::PathKey& k, uint32_t d) {
     key = k;
     dim = d;
@@ -118,11 +126,7 @@ struct Sampler {
   }
   NE_D float random() {
     uint32_t b = dim >> 2;
-    if (b != blk) {
-      nerng::Block r = nerng::philox4x32_10(b, key.sample, key.pixel, key.stream, key.seed_lo, key.seed_hi);
-      w0 = r.w[0]; w1 = r.w[1]; w2 = r.w[2]; w3 = r.w[3];
-      blk = b;
-    }
+    if (b != blk) refill(b);
     uint32_t s = dim & 3u;
     dim++;
     uint32_t w = (s == 0) ? w0 : (s == 1) ? w1 : (s == 2) ? w2 : w3;
@@ -484,7 +488,7 @@ NE_D bool instanceIntersect(Ctx<C>& c, uint32_t ii, const Ray& ray, Hit& hit, fl
 
 // core/Scene.cpp:30-56.
 template <bool C>
-NE_D bool intersectScene(Ctx<C>& c, const Ray& ray, Hit& hit, float tMin, float tMax) {
+NE_NI bool intersectScene(Ctx<C>& c, const Ray& ray, Hit& hit, float tMin, float tMax) {
   bool did = false;
   hit.prim = -1;
   if (C) c.c.queries++;
@@ -614,7 +618,7 @@ NE_D V3 phaseSample(const DMaterial& m, Sampler& S) {
   return v3(nefm::cos(phi) * sinTheta, nefm::sin(phi) * sinTheta, cosTheta);
 }
 // core/BSDF.h:100-106.
-NE_D V3 bsdfSample(const DMaterial& m, V3 incoming, V3 normal, Sampler& S) {
+NE_NI V3 bsdfSample(const DMaterial& m, V3 incoming, V3 normal, Sampler& S) {
   V3 ss, ts;
   orthonormal(normal, ss, ts);
   V3 wi = toLCS(-normalize(incoming), normal, ss, ts);
@@ -622,7 +626,7 @@ NE_D V3 bsdfSample(const DMaterial& m, V3 incoming, V3 normal, Sampler& S) {
   return toWorld(sc, normal, ss, ts);
 }
 // core/BSDF.h:117-125.
-NE_D float bsdfPdf(const DMaterial& m, V3 incoming, V3 scattered, V3 normal) {
+NE_NI float bsdfPdf(const DMaterial& m, V3 incoming, V3 scattered, V3 normal) {
   bool trans = (m.bsdf == NE_BSDF_VOLUME);
   if (!trans && (!sameHemisphere(-incoming, normal) || !sameHemisphere(scattered, normal))) return 0;
   V3 ss, ts;
@@ -632,7 +636,7 @@ NE_D float bsdfPdf(const DMaterial& m, V3 incoming, V3 scattered, V3 normal) {
   return trans ? phaseEval(m, wi, wo) : glossyPdf(m, wi, wo);
 }
 // core/BSDF.h:135-142.
-NE_D V3 bsdfEval(const DMaterial& m, V3 incoming, V3 scattered, V3 normal) {
+NE_NI V3 bsdfEval(const DMaterial& m, V3 incoming, V3 scattered, V3 normal) {
   bool trans = (m.bsdf == NE_BSDF_VOLUME);
   if (!trans && (!sameHemisphere(-incoming, normal) || !sameHemisphere(scattered, normal))) return v3(0, 0, 0);
   V3 ss, ts;
@@ -692,7 +696,7 @@ NE_D float sampleAt(Ctx<C>& c, const DMedium& M, const Ray& r, float t) {
 
 // materials/GridMedia.cpp:45-69 GridMedia::Tr (ratio tracking).
 template <bool C>
-NE_D V3 gridTr(Ctx<C>& c, const DMedium& M, Ray incoming, Hit isect) {
+NE_NI V3 gridTr(Ctx<C>& c, const DMedium& M, Ray incoming, Hit isect) {
   incoming = transformRay(incoming, c.s.instances[isect.inst].ocs);
   incoming.o = incoming.at(isect.tNear);
   isect.tFar = isect.tFar - isect.tNear;
@@ -787,7 +791,7 @@ NE_D V3 mediumSample(Ctx<C>& c, int med, const Ray& r, Ray& scattered, const Hit
 // ---------------------------------------------------------------- lights
 // Primitive::samplePointOnSurface (Rectangle.cpp:78-88, Sphere.cpp:46-52,
 // Triangle.cpp:114-119, Point.cpp:14-18, AABB.cpp:81-83).
-NE_D V3 samplePointOnSurface(const DScene& s, int pi, const Hit& isect, const float* M, Sampler& S) {
+NE_NI V3 samplePointOnSurface(const DScene& s, int pi, const Hit& isect, const float* M, Sampler& S) {
   const DPrim& p = s.prims[pi];
   switch (p.type) {
     case NE_PRIM_RECTANGLE: {
@@ -816,7 +820,7 @@ NE_D V3 samplePointOnSurface(const DScene& s, int pi, const Hit& isect, const fl
   }
 }
 // Primitive::pdf (Rectangle.cpp:159-171, Sphere.cpp:58-68, Triangle.cpp:159-161).
-NE_D float primPdf(const DScene& s, int pi, const Hit& isect, const DInstance& lin, Sampler& S) {
+NE_NI float primPdf(const DScene& s, int pi, const Hit& isect, const DInstance& lin, Sampler& S) {
   const DPrim& p = s.prims[pi];
   switch (p.type) {
     case NE_PRIM_RECTANGLE: {
@@ -841,7 +845,7 @@ NE_D float primPdf(const DScene& s, int pi, const Hit& isect, const DInstance& l
 }
 
 // Light::sampleLi (DiffuseLight.cpp:8-20, DirectionalLight.cpp:12-18, InfiniteAreaLight.h:83-113).
-NE_D V3 sampleLi(const DScene& s, const DLight& L, const Hit& isect, const DInstance& lin, Ray& wo, float& pdf,
+NE_NI V3 sampleLi(const DScene& s, const DLight& L, const Hit& isect, const DInstance& lin, Ray& wo, float& pdf,
                  Sampler& S) {
   switch (L.type) {
     case NE_LIGHT_DIFFUSE: {
@@ -924,7 +928,7 @@ NE_D V3 visibilityTr(Ctx<C>& c, V3 p, V3 lightPoint) {
 
 // integrators/VolumetricPathIntegrator.cpp:74-157 estimateDirect.
 template <bool C>
-NE_D V3 estimateDirect(Ctx<C>& c, const Ray& incoming, const Hit& isect, const DLight& light, uint32_t lightInst) {
+NE_NI V3 estimateDirect(Ctx<C>& c, const Ray& incoming, const Hit& isect, const DLight& light, uint32_t lightInst) {
   const DScene& s = c.s;
   const DInstance& lin = s.instances[lightInst];
   V3 Ld = v3(0, 0, 0);

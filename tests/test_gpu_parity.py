@@ -27,10 +27,17 @@ def ctx(ne):
     return ne.Context(0)
 
 
-@pytest.fixture(scope="module", params=["cornell_c1", "medium_c2"])
+KERNELS = {0: "straight", 3: "regrouped"}
+
+
+@pytest.fixture(scope="module", params=[(s, k) for s in ("cornell_c1", "medium_c2") for k in KERNELS],
+                ids=lambda p: f"{p[0]}-{KERNELS[p[1]]}")
 def scenes(request, ne, ctx, oracle_lib):
-    host = ne.SceneHost.from_json(scene_path(request.param))
-    return request.param, host, ctx.upload(host), oracle_lib.OracleScene(host.desc_ptr)
+    name, kernel = request.param
+    host = ne.SceneHost.from_json(scene_path(name))
+    scene = ctx.upload(host)
+    scene.set_tuning(kernel=kernel)
+    return name, host, scene, oracle_lib.OracleScene(host.desc_ptr)
 
 
 def rel_err(gpu, cpu):
@@ -176,3 +183,34 @@ def test_invalid_arguments(ne, ctx):
     out = scene.trace_paths(np.zeros((0, 2), np.uint32))
     assert out.shape == (0, 3)
     assert scene.trace_closest(np.zeros((0, 6), np.float32)).shape == (0,)
+
+
+def test_kernels_and_tunings_agree(ne, ctx):
+    """Every path kernel and launch configuration renders the same bits."""
+    host = ne.SceneHost.from_json(scene_path("medium_c2"))
+    scene = ctx.upload(host)
+    p = ne.render_params(seed=21, spp=2)
+    ref = None
+    for kernel, share, bps in [(0, 16, 0), (1, 16, 0), (2, 16, 0), (3, 16, 0), (3, 1, 0), (3, 32, 0), (3, 8, 1)]:
+        scene.set_tuning(kernel=kernel, track_share=share, blocks_per_sm=bps)
+        img, stats = scene.render(p)
+        if ref is None:
+            ref = img
+        assert np.array_equal(img, ref), (kernel, share, bps)
+    with pytest.raises(ne.NarvalError):
+        scene.set_tuning(kernel=7)
+    with pytest.raises(ne.NarvalError):
+        scene.set_tuning(kernel=3, track_share=0)
+
+
+def test_counting_kernels_agree(ne, ctx):
+    """The instrumented variants count the same work on both kernels and render the same image."""
+    host = ne.SceneHost.from_json(scene_path("medium_c2"))
+    scene = ctx.upload(host)
+    out = {}
+    for kernel in (0, 3):
+        scene.set_tuning(kernel=kernel)
+        img, st = scene.render(ne.render_params(seed=2, spp=1, flags=ne.NE_RENDER_COUNT_WORK))
+        out[kernel] = (img, st["density_lookups"], st["scene_queries"])
+    assert np.array_equal(out[0][0], out[3][0])
+    assert out[0][1] == out[3][1] and out[0][2] == out[3][2] and out[0][1] > 0
