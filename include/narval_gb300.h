@@ -104,6 +104,7 @@ void ne_scene_host_destroy(ne_scene_host* s);
 /* ---- device ---- */
 
 ne_status ne_context_create(int device, ne_context** out);
+/* Destroys the context and every scene still uploaded to it; their handles become invalid. */
 void ne_context_destroy(ne_context* ctx);
 const char* ne_last_error(const ne_context* ctx);
 

@@ -14,6 +14,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import weakref
 
 import numpy as np
 
@@ -141,6 +142,7 @@ class Context:
         if st != 0:
             raise NarvalError(st, "ne_context_create failed (no CUDA device?)")
         self._h = h
+        self._scenes = weakref.WeakSet()
 
     def error(self) -> str:
         return library().ne_last_error(self._h).decode()
@@ -152,7 +154,9 @@ class Context:
     def upload(self, host: SceneHost) -> "Scene":
         h = C.c_void_p()
         self.check(library().ne_scene_upload(self._h, host.desc_ptr, C.byref(h)))
-        return Scene(self, h, host)
+        s = Scene(self, h, host)
+        self._scenes.add(s)
+        return s
 
     def record(self, slot: int):
         self.check(library().ne_context_event_record(self._h, slot))
@@ -183,6 +187,9 @@ class Context:
 
     def close(self):
         if self._h:
+            # scenes first: the library destroys them with the context, so their handles die here
+            for s in list(self._scenes):
+                s._h = None
             library().ne_context_destroy(self._h)
             self._h = None
 
@@ -253,9 +260,9 @@ class Scene:
         return hits_to_numpy(out)
 
     def close(self):
-        if self._h:
+        if self._h and self.ctx._h:
             library().ne_scene_destroy(self._h)
-            self._h = None
+        self._h = None
 
     def __del__(self):
         try:

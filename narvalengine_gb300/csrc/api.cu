@@ -35,6 +35,7 @@ struct ne_context {
   std::string err;
   unsigned long long* d_counter = nullptr;  // [0] work counter, [1..4] work counters
   uint32_t* d_err = nullptr;
+  std::vector<ne_scene*> scenes;            // live scenes, destroyed with the context
 };
 
 struct ne_scene {
@@ -345,6 +346,7 @@ ne_status ne_context_create(int device, ne_context** out) {
 
 void ne_context_destroy(ne_context* ctx) {
   if (!ctx) return;
+  while (!ctx->scenes.empty()) ne_scene_destroy(ctx->scenes.back());
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (int i = 0; i < 4; i++)
@@ -415,6 +417,7 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
   NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
   ne_scene* sc = new ne_scene();
   sc->ctx = ctx;
+  ctx->scenes.push_back(sc);
   sc->settings = D.settings;
   memset(&sc->d, 0, sizeof(sc->d));
   auto cleanup = [&](ne_status st) {
@@ -619,6 +622,8 @@ ne_status ne_scene_get_tuning(const ne_scene* sc, ne_tuning* t) {
 
 void ne_scene_destroy(ne_scene* sc) {
   if (!sc) return;
+  auto& v = sc->ctx->scenes;
+  v.erase(std::remove(v.begin(), v.end(), sc), v.end());
   cudaSetDevice(sc->ctx->device);
   cudaStreamSynchronize(sc->ctx->stream);
   for (void* p : sc->allocs) cudaFree(p);
