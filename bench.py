@@ -40,7 +40,17 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 SCENE = "medium_c2.json"
-WORKLOAD = "medium_c2: 128^3 fBm grid (scale 20, albedo 0.9, HG g=0.8), sun 3.0 @30deg + env 0.2, 512x512x64spp, depth 64"
+WORKLOADS = {
+    "medium_c2": "medium_c2: 128^3 fBm grid (scale 20, albedo 0.9, HG g=0.8), sun 3.0 @30deg + env 0.2, "
+                 "512x512x64spp, depth 64",
+    "cornell_c1": "cornell_c1: Cornell box, 5 rectangles + 2 GGX spheres, 0.5x0.5 emitter (17,12,4), "
+                  "256x256x16spp, depth 8, RR after 3",
+    "mesh_c3": "mesh_c3: 1.31M-triangle displaced icosphere (1024 GGX groups) on a 10x10 ground, two emitters 10, "
+               "1024x1024x32spp, depth 12, reference midpoint BVH",
+}
+WORKLOAD = WORKLOADS["medium_c2"]
+BYTES_PER_NODE = 32   # BVH node: two float4 (bounds + child/leaf words)
+BYTES_PER_TRI = 36    # triangle: 9 FP32 vertex coordinates
 METRIC = "Mpaths/s (camera paths x spp per second, reference integrator semantics)"
 BYTES_PER_LOOKUP = 32  # 8 FP32 voxels per trilinear density lookup
 
@@ -210,12 +220,17 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--kernel", type=int, default=3, help="path kernel (ne_tuning.kernel): 0 straight, 3 regrouped")
+    ap.add_argument("--scene", default="medium_c2", choices=sorted(WORKLOADS),
+                    help="workload (the default is the configuration the metric is quoted on)")
+    ap.add_argument("--kernel", type=int, default=0, help="path kernel (ne_tuning.kernel): 0 straight, 1 regrouped")
     ap.add_argument("--track-share", type=int, default=16, help="regrouped kernel tracking threshold, 32nds")
     ap.add_argument("--profile-spp", type=int, default=0,
                     help="profiling case: two renders of the workload at this spp (the second is the one to capture)")
     args = ap.parse_args()
     rank, world, local = dist_env()
+    global SCENE, WORKLOAD
+    SCENE = args.scene + ".json"
+    WORKLOAD = WORKLOADS[args.scene]
 
     if args.impl == "reference":
         run_reference(args, rank, world)
@@ -306,14 +321,17 @@ def main():
     peak, peak_kind = load_peaks()
     k_ms = statistics.mean(kernel_ms)
     lookups = cstats["density_lookups"]
-    achieved = lookups * BYTES_PER_LOOKUP / (k_ms / 1e3) / 1e9
+    alg_bytes = lookups * BYTES_PER_LOOKUP + cstats["bvh_nodes"] * BYTES_PER_NODE + cstats["prim_tests"] * BYTES_PER_TRI
+    achieved = alg_bytes / (k_ms / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": peak_kind, "traffic": None,
-                "kernel": "k_sched (regrouped path kernel)" if args.kernel == 3 else "k_paths (straight path kernel)",
-                "algorithmic_bytes_per_launch": lookups * BYTES_PER_LOOKUP,
+                "kernel": "k_sched (regrouped path kernel)" if args.kernel == 1 else "k_paths (straight path kernel)",
+                "algorithmic_bytes_per_launch": alg_bytes,
+                "bytes_rule": "32 B per density lookup + 32 B per BVH node visit + 36 B per triangle test",
                 "density_lookups_per_launch": lookups, "scene_queries_per_launch": cstats["scene_queries"],
+                "bvh_nodes_per_launch": cstats["bvh_nodes"], "triangle_tests_per_launch": cstats["prim_tests"],
                 "kernel_ms": k_ms}
-    traffic_file = os.path.join(ROOT, "profiles", "k_paths_medium_c2_traffic.json")
+    traffic_file = os.path.join(ROOT, "profiles", f"traffic_{args.scene}.json")
     if os.path.exists(traffic_file):
         try:
             roofline["traffic"] = json.load(open(traffic_file))["dram_bytes_per_launch"]

@@ -85,7 +85,7 @@ typedef struct ne_render_stats {
   uint64_t density_lookups;   /* trilinear density lookups (NE_RENDER_COUNT_WORK) */
   uint64_t scene_queries;     /* Scene::intersectScene calls (NE_RENDER_COUNT_WORK) */
   uint64_t bvh_nodes;         /* BVH nodes visited (NE_RENDER_COUNT_WORK) */
-  uint64_t prim_tests;        /* primitive intersection tests (NE_RENDER_COUNT_WORK) */
+  uint64_t prim_tests;        /* ray-triangle tests (NE_RENDER_COUNT_WORK) */
   uint32_t kernel_launches;   /* kernels this call launched */
   uint32_t pad;
 } ne_render_stats;
@@ -129,10 +129,10 @@ ne_status ne_trace_closest(ne_scene* scene, const ne_ray* rays, size_t n, float 
                            ne_hit* out);
 
 /* Launch configuration of the path kernels of one scene (picked by an autotuner or by hand).
- * kernel: 0 = straight kernel (one path per lane to completion), 1/2 = the same with at most
- * 80/64 registers per thread, 3 = regrouped state-machine kernel (lanes refill as paths finish;
- * a warp steps tracking walks together while at least track_share/32 of its live lanes are in
- * one). blocks_per_sm: persistent blocks per SM, 0 = as many as fit. */
+ * kernel: 0 = straight kernel (one path per lane to completion), 1 = regrouped state-machine
+ * kernel (lanes refill as paths finish; a warp steps tracking walks together while at least
+ * track_share/32 of its live lanes are in one). blocks_per_sm: persistent blocks per SM,
+ * 0 = as many as fit. Every configuration renders the same bits. */
 typedef struct ne_tuning {
   int32_t kernel;
   int32_t track_share;

@@ -224,7 +224,7 @@ class Scene:
         self.ctx.check(library().ne_render(self._h, C.byref(p), ptr, C.byref(stats)))
         return img, {f: getattr(stats, f) for f, _ in NeRenderStats._fields_ if f != "pad"}
 
-    def set_tuning(self, kernel: int = 3, track_share: int = 16, blocks_per_sm: int = 0):
+    def set_tuning(self, kernel: int = 0, track_share: int = 16, blocks_per_sm: int = 0):
         """Launch configuration of the path kernels (see ne_tuning in include/narval_gb300.h)."""
         t = _abi.NeTuning(kernel, track_share, blocks_per_sm, 0)
         self.ctx.check(library().ne_scene_set_tuning(self._h, C.byref(t)))

@@ -46,8 +46,10 @@ struct ne_scene {
   float* d_paths = nullptr;  // per-path radiance scratch of ne_render
   size_t paths_cap = 0;
   int blocks_per_sm = 1;
-  int variant = 0;           // path kernel (NE_PATHS_VARIANT: 0-2 straight k_paths, 3 regrouped k_sched)
-  int track_share = 16;      // k_sched tracking-phase threshold (NE_TRACK_SHARE, 32nds of live lanes)
+  int variant = 0;           // path kernel: 0 straight k_paths, 1 regrouped k_sched
+  int track_share = 16;      // k_sched tracking-phase threshold (32nds of live lanes)
+  uint32_t features = 0;     // FT_* bits of the scene
+  uint32_t feature_set = 0;  // compiled kernel specialisation covering them
 };
 
 namespace {
@@ -293,18 +295,52 @@ ne_status launchPaths(ne_scene* sc, const PathArgs& a, bool count) {
   int blocks = persistentBlocks(sc);
   unsigned long long needed = (a.total + kThreads - 1) / kThreads;
   if ((unsigned long long)blocks > needed) blocks = (int)std::max<unsigned long long>(1, needed);
-  if (sc->variant == 3) {
-    PathArgs b = a;
-    b.track_share = sc->track_share;
-    NE_CUDA(ne_launch_sched(count, blocks, ctx->stream, sc->d, b, ctx->d_counter, ctx->d_err), "k_sched launch");
-  } else {
-    NE_CUDA(ne_launch_paths(count, count ? 0 : sc->variant, blocks, ctx->stream, sc->d, a, ctx->d_counter, ctx->d_err),
-            "k_paths launch");
-  }
+  PathArgs b = a;
+  b.track_share = sc->track_share;
+  NE_CUDA(ne_launch_path_kernel(sc->variant, sc->feature_set, count, blocks, ctx->stream, sc->d, b, ctx->d_counter,
+                                ctx->d_err),
+          "path kernel launch");
   return NE_OK;
 }
 
 }  // namespace
+
+uint32_t ne_feature_set_for(uint32_t f) {
+  const uint32_t sets[3] = {K_VOLUME, K_SURFACE, K_MESH};
+  for (uint32_t s : sets)
+    if ((f & ~s) == 0) return s;
+  return K_GENERAL;
+}
+
+cudaError_t ne_launch_path_kernel(int kernel, uint32_t set, bool count, int blocks, cudaStream_t st, const DScene& s,
+                                  const PathArgs& a, unsigned long long* counter, uint32_t* err) {
+  if (count)
+    return kernel == 0 ? launchPathKernel<0, K_GENERAL | K_COUNT>(blocks, st, s, a, counter, err)
+                       : launchPathKernel<1, K_GENERAL | K_COUNT>(blocks, st, s, a, counter, err);
+  switch (set) {
+    case K_VOLUME:
+      return kernel == 0 ? launchPathKernel<0, K_VOLUME>(blocks, st, s, a, counter, err)
+                         : launchPathKernel<1, K_VOLUME>(blocks, st, s, a, counter, err);
+    case K_SURFACE:
+      return kernel == 0 ? launchPathKernel<0, K_SURFACE>(blocks, st, s, a, counter, err)
+                         : launchPathKernel<1, K_SURFACE>(blocks, st, s, a, counter, err);
+    case K_MESH:
+      return kernel == 0 ? launchPathKernel<0, K_MESH>(blocks, st, s, a, counter, err)
+                         : launchPathKernel<1, K_MESH>(blocks, st, s, a, counter, err);
+    default:
+      return kernel == 0 ? launchPathKernel<0, K_GENERAL>(blocks, st, s, a, counter, err)
+                         : launchPathKernel<1, K_GENERAL>(blocks, st, s, a, counter, err);
+  }
+}
+
+cudaError_t ne_path_kernel_occupancy(int kernel, uint32_t set, int* bps) {
+  switch (set) {
+    case K_VOLUME: return kernel == 0 ? pathKernelOccupancy<0, K_VOLUME>(bps) : pathKernelOccupancy<1, K_VOLUME>(bps);
+    case K_SURFACE: return kernel == 0 ? pathKernelOccupancy<0, K_SURFACE>(bps) : pathKernelOccupancy<1, K_SURFACE>(bps);
+    case K_MESH: return kernel == 0 ? pathKernelOccupancy<0, K_MESH>(bps) : pathKernelOccupancy<1, K_MESH>(bps);
+    default: return kernel == 0 ? pathKernelOccupancy<0, K_GENERAL>(bps) : pathKernelOccupancy<1, K_GENERAL>(bps);
+  }
+}
 
 extern "C" {
 
@@ -582,13 +618,37 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
   sc->d.camera.lens_radius = cm.lens_radius;
   sc->d.width = D.settings.width;
   sc->d.height = D.settings.height;
+  // feature bits: which primitive, BSDF, medium and light kinds the kernels must handle
+  uint32_t F = 0;
+  for (uint32_t i = 0; i < D.n_prims; i++) {
+    switch (D.prims[i].type) {
+      case NE_PRIM_SPHERE: F |= FT_SPHERE; break;
+      case NE_PRIM_RECTANGLE: F |= FT_RECT; break;
+      case NE_PRIM_AABB: F |= FT_AABB; break;
+      case NE_PRIM_TRIANGLE: F |= FT_TRI; break;
+      default: F |= FT_POINT; break;
+    }
+  }
+  for (uint32_t i = 0; i < D.n_models; i++) {
+    if (D.models[i].has_bbox) F |= FT_BBOX;
+    if (D.models[i].use_bvh) F |= FT_TRI;
+  }
+  for (uint32_t i = 0; i < D.n_materials; i++) {
+    const ne_material& m = D.materials[i];
+    if (m.bsdf == NE_BSDF_GLOSSY) F |= FT_GLOSSY;
+    if (m.bsdf == NE_BSDF_VOLUME) F |= FT_VOLBSDF;
+    if (m.tex_types & NE_TEX_NORMAL) F |= FT_NORMALMAP;
+  }
+  for (uint32_t i = 0; i < D.n_media; i++) F |= D.media[i].type == NE_MEDIUM_GRID ? FT_GRID : FT_HOMOG;
+  for (uint32_t i = 0; i < D.n_lights; i++)
+    F |= D.lights[i].type == NE_LIGHT_DIFFUSE ? FT_LDIFF : (D.lights[i].type == NE_LIGHT_DIRECTIONAL ? FT_LDIR : FT_LINF);
+  sc->features = F;
+  sc->feature_set = ne_feature_set_for(F);
   ne_tuning tn;
   tn.kernel = sc->variant;
   tn.track_share = sc->track_share;
   tn.blocks_per_sm = 0;
   tn.pad = 0;
-  if (const char* v = getenv("NE_PATHS_VARIANT")) tn.kernel = atoi(v);
-  if (const char* v = getenv("NE_TRACK_SHARE")) tn.track_share = atoi(v);
   if (ne_scene_set_tuning(sc, &tn) != NE_OK) return cleanup(NE_ERR_INVALID_ARG);
   cudaError_t e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return cleanup(cudaFail(ctx, e, "scene upload"));
@@ -597,12 +657,12 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
 }
 
 ne_status ne_scene_set_tuning(ne_scene* sc, const ne_tuning* t) {
-  if (!sc || !t || t->kernel < 0 || t->kernel > 3 || t->track_share < 1 || t->track_share > 32 ||
+  if (!sc || !t || t->kernel < 0 || t->kernel > 1 || t->track_share < 1 || t->track_share > 32 ||
       t->blocks_per_sm < 0 || t->blocks_per_sm > 64)
     return NE_ERR_INVALID_ARG;
   ne_context* ctx = sc->ctx;
   int fit = 1;
-  cudaError_t e = t->kernel == 3 ? ne_sched_occupancy(&fit) : ne_paths_occupancy(t->kernel, &fit);
+  cudaError_t e = ne_path_kernel_occupancy(t->kernel, sc->feature_set, &fit);
   if (e != cudaSuccess) return cudaFail(ctx, e, "occupancy query");
   if (fit < 1) fit = 1;
   sc->variant = t->kernel;

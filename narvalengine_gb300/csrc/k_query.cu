@@ -6,7 +6,7 @@ namespace nedev {
 __global__ void k_li(const __grid_constant__ DScene s, PathParams P, nerng::PathKey base, const ne_ray* __restrict__ rays,
                      const ne_path_key* __restrict__ keys, size_t n, uint32_t first_dim, float* __restrict__ out,
                      uint32_t* err) {
-  Ctx<false> c{s, Sampler{}, Counters{0, 0, 0, 0}, err};
+  Ctx<K_GENERAL> c{s, Sampler{}, Counters{0, 0, 0, 0}, err};
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     nerng::PathKey k = base;
     k.pixel = keys[i].pixel;
@@ -22,7 +22,7 @@ __global__ void k_li(const __grid_constant__ DScene s, PathParams P, nerng::Path
 
 __global__ void k_closest(const __grid_constant__ DScene s, const ne_ray* __restrict__ rays, size_t n, float tmin,
                           float tmax, ne_hit* __restrict__ out, uint32_t* err) {
-  Ctx<false> c{s, Sampler{}, Counters{0, 0, 0, 0}, err};
+  Ctx<K_GENERAL> c{s, Sampler{}, Counters{0, 0, 0, 0}, err};
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     Ray r{v3(rays[i].o[0], rays[i].o[1], rays[i].o[2]), v3(rays[i].d[0], rays[i].d[1], rays[i].d[2])};
     Hit h = emptyHit();

@@ -1,6 +1,10 @@
-// Path kernels and their launchers. Each heavy kernel is instantiated in its own
-// translation unit (k_paths_plain.cu, k_paths_count.cu, k_query.cu) so the build
-// compiles them in parallel.
+// Path kernels and their launchers.
+//
+// Two path kernels: k_paths (straight: one path per lane to completion, warps take 32
+// work items at a time) and k_sched (regrouped state machine, pt_sched.cuh). Each is
+// specialised on the scene's feature set K (pt_device.cuh: K_VOLUME, K_SURFACE, K_MESH,
+// K_GENERAL) and instantiated in its own translation unit (k_path_<kernel>_<set>.cu) so the
+// build compiles them in parallel; the counting variants (K | K_COUNT) use K_GENERAL.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -24,16 +28,16 @@ struct PathArgs {
   int track_share;           // regrouped kernel: tracking-phase threshold in 32nds of live lanes
 };
 
-template <bool C>
+template <uint32_t K>
 __global__ void __launch_bounds__(kThreads) k_sched(const __grid_constant__ DScene s, const PathArgs a,
                                                     unsigned long long* __restrict__ counter, uint32_t* err) {
-  schedLoop<C>(s, a.P, a.base, a.total, a.spp, a.sample_offset, a.cover_w, a.keys, a.out, counter, err,
+  schedLoop<K>(s, a.P, a.base, a.total, a.spp, a.sample_offset, a.cover_w, a.keys, a.out, counter, err,
                a.track_share);
 }
 
-template <bool C>
+template <uint32_t K>
 __device__ __forceinline__ void flushCounters(const Counters& cn, unsigned long long* g) {
-  if (!C) return;
+  if (!(K & K_COUNT)) return;
   unsigned long long v[4] = {cn.lookups, cn.queries, cn.nodes, cn.tests};
 #pragma unroll
   for (int k = 0; k < 4; k++) {
@@ -43,11 +47,10 @@ __device__ __forceinline__ void flushCounters(const Counters& cn, unsigned long 
   }
 }
 
-// MINB > 1 caps registers per thread (65536 / (128 * MINB)) so more warps stay resident.
-template <bool C, int MINB>
-__global__ void __launch_bounds__(kThreads, MINB) k_paths(const __grid_constant__ DScene s, const PathArgs a,
-                                                      unsigned long long* __restrict__ counter, uint32_t* err) {
-  Ctx<C> c{s, Sampler{}, Counters{0, 0, 0, 0}, err};
+template <uint32_t K>
+__global__ void __launch_bounds__(kThreads) k_paths(const __grid_constant__ DScene s, const PathArgs a,
+                                                    unsigned long long* __restrict__ counter, uint32_t* err) {
+  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err};
   const int lane = threadIdx.x & 31;
   for (;;) {
     unsigned long long base = 0;
@@ -72,24 +75,55 @@ __global__ void __launch_bounds__(kThreads, MINB) k_paths(const __grid_constant_
       a.out[3 * idx + 2] = L.z;
     }
   }
-  flushCounters<C>(c.c, counter);
+  flushCounters<K>(c.c, counter);
 }
 
+// One launcher per (kernel, feature set); KERNEL 0 = k_paths, 1 = k_sched.
+template <int KERNEL, uint32_t K>
+cudaError_t launchPathKernel(int blocks, cudaStream_t st, const DScene& s, const PathArgs& a,
+                             unsigned long long* counter, uint32_t* err) {
+  if (KERNEL == 0)
+    k_paths<K><<<blocks, kThreads, 0, st>>>(s, a, counter, err);
+  else
+    k_sched<K><<<blocks, kThreads, 0, st>>>(s, a, counter, err);
+  return cudaGetLastError();
+}
+
+template <int KERNEL, uint32_t K>
+cudaError_t pathKernelOccupancy(int* blocks_per_sm) {
+  if (KERNEL == 0) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_paths<K>, kThreads, 0);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_sched<K>, kThreads, 0);
+}
+
+#define NE_PATH_KERNEL_INSTANCE(EXT, KERNEL, K)                                                              \
+  EXT template cudaError_t launchPathKernel<KERNEL, K>(int, cudaStream_t, const DScene&, const PathArgs&,    \
+                                                       unsigned long long*, uint32_t*);                      \
+  EXT template cudaError_t pathKernelOccupancy<KERNEL, K>(int*);
+
+#define NE_PATH_KERNEL_ALL(EXT)                          \
+  NE_PATH_KERNEL_INSTANCE(EXT, 0, K_VOLUME)              \
+  NE_PATH_KERNEL_INSTANCE(EXT, 0, K_SURFACE)             \
+  NE_PATH_KERNEL_INSTANCE(EXT, 0, K_MESH)                \
+  NE_PATH_KERNEL_INSTANCE(EXT, 0, K_GENERAL)             \
+  NE_PATH_KERNEL_INSTANCE(EXT, 1, K_VOLUME)              \
+  NE_PATH_KERNEL_INSTANCE(EXT, 1, K_SURFACE)             \
+  NE_PATH_KERNEL_INSTANCE(EXT, 1, K_MESH)                \
+  NE_PATH_KERNEL_INSTANCE(EXT, 1, K_GENERAL)             \
+  NE_PATH_KERNEL_INSTANCE(EXT, 0, K_GENERAL | K_COUNT)   \
+  NE_PATH_KERNEL_INSTANCE(EXT, 1, K_GENERAL | K_COUNT)
+
+// Declared here, instantiated in the k_path_*.cu units only.
+NE_PATH_KERNEL_ALL(extern)
 
 }  // namespace nedev
 
-// Launchers (defined next to each kernel instantiation).
-// variant: 0 = compiler's register choice, 1 = at most 80 registers, 2 = at most 64 registers,
-// 3 = regrouped state-machine kernel (k_sched).
-cudaError_t ne_launch_paths(bool count, int variant, int blocks, cudaStream_t st, const nedev::DScene& s,
-                            const nedev::PathArgs& a, unsigned long long* counter, uint32_t* err);
-cudaError_t ne_paths_occupancy(int variant, int* blocks_per_sm);
-cudaError_t ne_launch_paths_variant(int variant, int blocks, cudaStream_t st, const nedev::DScene& s,
-                                    const nedev::PathArgs& a, unsigned long long* counter, uint32_t* err);
-cudaError_t ne_paths_occupancy_variant(int variant, int* blocks_per_sm);
-cudaError_t ne_launch_sched(bool count, int blocks, cudaStream_t st, const nedev::DScene& s, const nedev::PathArgs& a,
-                            unsigned long long* counter, uint32_t* err);
-cudaError_t ne_sched_occupancy(int* blocks_per_sm);
+// Dispatch over the instantiated kernels. features: the scene's FT_* bits; the smallest
+// compiled set covering them is used (K_GENERAL covers everything).
+uint32_t ne_feature_set_for(uint32_t features);
+cudaError_t ne_launch_path_kernel(int kernel, uint32_t set, bool count, int blocks, cudaStream_t st,
+                                  const nedev::DScene& s, const nedev::PathArgs& a, unsigned long long* counter,
+                                  uint32_t* err);
+cudaError_t ne_path_kernel_occupancy(int kernel, uint32_t set, int* blocks_per_sm);
 cudaError_t ne_launch_li(int blocks, cudaStream_t st, const nedev::DScene& s, nedev::PathParams P, nerng::PathKey base,
                          const ne_ray* rays, const ne_path_key* keys, size_t n, uint32_t first_dim, float* out,
                          uint32_t* err);

@@ -27,9 +27,7 @@
 namespace nedev {
 
 #define NE_D __device__ __forceinline__
-// Large functions called from several places stay out of line so that their code exists
-// once: with divergent lanes the fully inlined kernel stalls on instruction fetch.
-#define NE_NI static __device__ __noinline__
+#define NE_NI __device__ __forceinline__
 
 constexpr double kPiD = 3.14159265358979323846264338327950288;
 constexpr double kTwoPiD = 6.283185307179586476925286766559;
@@ -44,6 +42,34 @@ constexpr int kMaxPassThrough = 1 << 16;
 constexpr int kBvhStack = 64;
 
 enum : uint32_t { ERR_BVH_STACK = 1u };
+
+// Kernel specialisation: K = feature bits of the scene (which primitive, BSDF, medium and
+// light kinds occur) | K_COUNT for the instrumented variant. Every type switch below tests
+// the feature bit first, so a kernel compiled for a scene's features carries no code for the
+// rest: the fully general kernel is large enough to stall on instruction fetch.
+enum : uint32_t {
+  FT_SPHERE = 1u << 0,
+  FT_RECT = 1u << 1,
+  FT_AABB = 1u << 2,
+  FT_TRI = 1u << 3,       // triangles and their BVH
+  FT_POINT = 1u << 4,
+  FT_GLOSSY = 1u << 5,
+  FT_VOLBSDF = 1u << 6,   // VolumeBSDF with HG or isotropic phase
+  FT_GRID = 1u << 7,
+  FT_HOMOG = 1u << 8,
+  FT_LDIFF = 1u << 9,
+  FT_LDIR = 1u << 10,
+  FT_LINF = 1u << 11,
+  FT_NORMALMAP = 1u << 12,
+  FT_BBOX = 1u << 13,     // model bounding boxes (meshes)
+  FT_ALL = (1u << 14) - 1,
+  K_COUNT = 1u << 31,
+  // feature sets with a compiled kernel (the host picks the smallest superset)
+  K_VOLUME = FT_AABB | FT_POINT | FT_SPHERE | FT_VOLBSDF | FT_GRID | FT_LDIR | FT_LINF,
+  K_SURFACE = FT_RECT | FT_SPHERE | FT_GLOSSY | FT_LDIFF,
+  K_MESH = FT_TRI | FT_BBOX | FT_RECT | FT_SPHERE | FT_GLOSSY | FT_LDIFF,
+  K_GENERAL = FT_ALL
+};
 
 // ---------------------------------------------------------------- vectors
 struct V3 {
@@ -138,7 +164,7 @@ struct Counters {
   unsigned long long lookups, queries, nodes, tests;
 };
 
-template <bool COUNT>
+template <uint32_t K>
 struct Ctx {
   const DScene& s;
   Sampler S;
@@ -287,6 +313,7 @@ NE_D bool rectIntersect(const DPrim& p, const Ray& r, Hit& h) {
 }
 
 // primitives/Triangle.cpp:49-80.
+template <uint32_t K>
 NE_D bool triIntersect(const DScene& s, const DPrim& p, const Ray& r, Hit& h) {
   V3 a = ld3(p.p0), b = ld3(p.p1), c = ld3(p.p2);
   V3 v1v0 = b - a, v2v0 = c - a, rov0 = r.o - a;
@@ -301,7 +328,7 @@ NE_D bool triIntersect(const DScene& s, const DPrim& p, const Ray& r, Hit& h) {
   h.tNear = t;
   h.tFar = t;
   h.hitPoint = r.at(h.tNear);
-  if (p.material >= 0 && (s.materials[p.material].tex_types & NE_TEX_NORMAL)) {
+  if ((K & FT_NORMALMAP) && p.material >= 0 && (s.materials[p.material].tex_types & NE_TEX_NORMAL)) {
     const DMaterial& m = s.materials[p.material];
     V3 tn = (m.tex_present & NE_TEX_NORMAL) ? ld3(m.normal_map) : v3(0, 0, 0);
     h.normal = convertNormalFromTextureMap(tn, normalize(normal));
@@ -311,28 +338,31 @@ NE_D bool triIntersect(const DScene& s, const DPrim& p, const Ray& r, Hit& h) {
   return true;
 }
 
-template <bool C>
-NE_D bool primIntersect(Ctx<C>& c, int idx, const Ray& r, Hit& h) {
+template <uint32_t K>
+NE_D bool primIntersect(Ctx<K>& c, int idx, const Ray& r, Hit& h) {
   const DPrim& p = c.s.prims[idx];
-  if (C) c.c.tests++;
+  if ((K & K_COUNT) && p.type == NE_PRIM_TRIANGLE) c.c.tests++;
   bool hit = false;
-  switch (p.type) {
-    case NE_PRIM_SPHERE: hit = sphereIntersect(p, r, h); break;
-    case NE_PRIM_RECTANGLE: hit = rectIntersect(p, r, h); break;
-    case NE_PRIM_AABB:
-      hit = aabbIntersect(ld3(p.p0), ld3(p.p1), r, h);
-      h.prim = idx;
-      return hit;
-    case NE_PRIM_TRIANGLE: hit = triIntersect(c.s, p, r, h); break;
-    default: return false;
+  if ((K & FT_SPHERE) && p.type == NE_PRIM_SPHERE) {
+    hit = sphereIntersect(p, r, h);
+  } else if ((K & FT_RECT) && p.type == NE_PRIM_RECTANGLE) {
+    hit = rectIntersect(p, r, h);
+  } else if ((K & FT_AABB) && p.type == NE_PRIM_AABB) {
+    hit = aabbIntersect(ld3(p.p0), ld3(p.p1), r, h);
+    h.prim = idx;
+    return hit;
+  } else if ((K & FT_TRI) && p.type == NE_PRIM_TRIANGLE) {
+    hit = triIntersect<K>(c.s, p, r, h);
+  } else {
+    return false;
   }
   if (hit) h.prim = idx;
   return hit;
 }
 
 // primitives/BVH.cpp:108-193 BVH::intersect (near-first stack traversal).
-template <bool C>
-NE_D bool bvhIntersect(Ctx<C>& c, const DModel& m, const Ray& r, Hit& out) {
+template <uint32_t K>
+NE_D bool bvhIntersect(Ctx<K>& c, const DModel& m, const Ray& r, Hit& out) {
   const float inf = __int_as_float(0x7f800000);
   uint32_t stackNode[kBvhStack];
   float stackT[kBvhStack];
@@ -354,7 +384,7 @@ NE_D bool bvhIntersect(Ctx<C>& c, const DModel& m, const Ray& r, Hit& out) {
     if (nearest > closest.tNear) continue;
     float4 hi = __ldg(reinterpret_cast<const float4*>(&nodes[ni].hi));
     uint32_t b = __float_as_uint(hi.w);
-    if (C) c.c.nodes++;
+    if (K & K_COUNT) c.c.nodes++;
     if (b & 0x80000000u) {
       float4 lo = __ldg(reinterpret_cast<const float4*>(&nodes[ni].lo));
       uint32_t start = __float_as_uint(lo.w), count = b & 0x7fffffffu;
@@ -408,14 +438,14 @@ NE_D V3 lightLi(const DLight& L) {  // Light::Li, DirectionalLight::Li
 }
 
 // primitives/Model.cpp:372-447 Model::intersect.
-template <bool C>
-NE_D bool modelIntersect(Ctx<C>& c, uint32_t mi, const Ray& ray, Hit& hit, float& tMin, float& tMax) {
+template <uint32_t K>
+NE_D bool modelIntersect(Ctx<K>& c, uint32_t mi, const Ray& ray, Hit& hit, float& tMin, float& tMax) {
   const DModel& m = c.s.models[mi];
   bool did = false;
   Hit temp = emptyHit();
-  if (m.has_bbox)
+  if ((K & FT_BBOX) && m.has_bbox)
     if (!aabbIntersect(ld3(m.bbox_min), ld3(m.bbox_max), ray, temp)) return false;
-  if (m.use_bvh) {
+  if ((K & FT_TRI) && m.use_bvh) {
     bool local = bvhIntersect(c, m, ray, temp);
     if (local && temp.tNear > tMin && temp.tNear < tMax) {
       tMax = temp.tNear;
@@ -427,7 +457,7 @@ NE_D bool modelIntersect(Ctx<C>& c, uint32_t mi, const Ray& ray, Hit& hit, float
   for (uint32_t k = 0; k < m.prim_count; k++) {
     int pi = (int)(m.prim_begin + k);
     const DPrim& p = c.s.prims[pi];
-    if (p.flags & DPRIM_GRID_MEDIUM) {
+    if ((K & FT_GRID) && (p.flags & DPRIM_GRID_MEDIUM)) {
       primIntersect(c, pi, ray, temp);
       float rx = gmax(0.0f, temp.tNear), ry = temp.tFar;
       if (rx <= ry && !nefm::isinf_(ry) && !nefm::isinf_(rx)) {
@@ -472,8 +502,8 @@ NE_D bool modelIntersect(Ctx<C>& c, uint32_t mi, const Ray& ray, Hit& hit, float
 }
 
 // primitives/InstancedModel.cpp:24-38.
-template <bool C>
-NE_D bool instanceIntersect(Ctx<C>& c, uint32_t ii, const Ray& ray, Hit& hit, float& tMin, float& tMax) {
+template <uint32_t K>
+NE_D bool instanceIntersect(Ctx<K>& c, uint32_t ii, const Ray& ray, Hit& hit, float& tMin, float& tMax) {
   const DInstance& in = c.s.instances[ii];
   if (!in.collision) return false;
   Ray r = transformRay(ray, in.ocs);
@@ -487,11 +517,11 @@ NE_D bool instanceIntersect(Ctx<C>& c, uint32_t ii, const Ray& ray, Hit& hit, fl
 }
 
 // core/Scene.cpp:30-56.
-template <bool C>
-NE_NI bool intersectScene(Ctx<C>& c, const Ray& ray, Hit& hit, float tMin, float tMax) {
+template <uint32_t K>
+NE_NI bool intersectScene(Ctx<K>& c, const Ray& ray, Hit& hit, float tMin, float tMax) {
   bool did = false;
   hit.prim = -1;
-  if (C) c.c.queries++;
+  if (K & K_COUNT) c.c.queries++;
   Hit temp = emptyHit();
   float curMin = tMin, curMax = tMax;
   uint32_t total = c.s.n_instances + c.s.n_light_instances;
@@ -588,6 +618,7 @@ NE_D V3 glossySample(const DMaterial& m, V3 wi, Sampler& S) {  // GlossyBSDF.cpp
   return ggxSample(rough * rough, wi, S);
 }
 // materials/Medium.h:116-128 HG eval/pdf, :56-62 isotropic.
+template <uint32_t K>
 NE_D float phaseEval(const DMaterial& m, V3 wi, V3 wo) {
   if (m.phase == NE_PHASE_ISOTROPIC) return __double2float_rn(1.0 / kFourPiD);
   float g = m.g;
@@ -596,6 +627,7 @@ NE_D float phaseEval(const DMaterial& m, V3 wi, V3 wo) {
   return (kInv4Pi * (1.0f - g * g)) / (denom * nefm::fsqrt(denom));
 }
 // materials/Medium.h:96-114 HG sample, :45-47 isotropic.
+template <uint32_t K>
 NE_D V3 phaseSample(const DMaterial& m, Sampler& S) {
   if (m.phase == NE_PHASE_ISOTROPIC) {
     float e1 = S.random();
@@ -618,36 +650,44 @@ NE_D V3 phaseSample(const DMaterial& m, Sampler& S) {
   return v3(nefm::cos(phi) * sinTheta, nefm::sin(phi) * sinTheta, cosTheta);
 }
 // core/BSDF.h:100-106.
+template <uint32_t K>
 NE_NI V3 bsdfSample(const DMaterial& m, V3 incoming, V3 normal, Sampler& S) {
   V3 ss, ts;
   orthonormal(normal, ss, ts);
   V3 wi = toLCS(-normalize(incoming), normal, ss, ts);
-  V3 sc = (m.bsdf == NE_BSDF_VOLUME) ? phaseSample(m, S) : glossySample(m, wi, S);
+  V3 sc = v3(0, 0, 0);
+  if ((K & FT_VOLBSDF) && m.bsdf == NE_BSDF_VOLUME)
+    sc = phaseSample<K>(m, S);
+  else if (K & FT_GLOSSY)
+    sc = glossySample(m, wi, S);
   return toWorld(sc, normal, ss, ts);
 }
 // core/BSDF.h:117-125.
+template <uint32_t K>
 NE_NI float bsdfPdf(const DMaterial& m, V3 incoming, V3 scattered, V3 normal) {
-  bool trans = (m.bsdf == NE_BSDF_VOLUME);
+  bool trans = (K & FT_VOLBSDF) && (m.bsdf == NE_BSDF_VOLUME);
   if (!trans && (!sameHemisphere(-incoming, normal) || !sameHemisphere(scattered, normal))) return 0;
   V3 ss, ts;
   orthonormal(normal, ss, ts);
   V3 wi = toLCS(-normalize(incoming), normal, ss, ts);
   V3 wo = toLCS(scattered, normal, ss, ts);
-  return trans ? phaseEval(m, wi, wo) : glossyPdf(m, wi, wo);
+  if (trans) return phaseEval<K>(m, wi, wo);
+  return (K & FT_GLOSSY) ? glossyPdf(m, wi, wo) : 0.0f;
 }
 // core/BSDF.h:135-142.
+template <uint32_t K>
 NE_NI V3 bsdfEval(const DMaterial& m, V3 incoming, V3 scattered, V3 normal) {
-  bool trans = (m.bsdf == NE_BSDF_VOLUME);
+  bool trans = (K & FT_VOLBSDF) && (m.bsdf == NE_BSDF_VOLUME);
   if (!trans && (!sameHemisphere(-incoming, normal) || !sameHemisphere(scattered, normal))) return v3(0, 0, 0);
   V3 ss, ts;
   orthonormal(normal, ss, ts);
   V3 wi = toLCS(-normalize(incoming), normal, ss, ts);
   V3 wo = toLCS(scattered, normal, ss, ts);
   if (trans) {
-    float p = phaseEval(m, wi, wo);
+    float p = phaseEval<K>(m, wi, wo);
     return v3(p, p, p);
   }
-  return glossyEval(m, wi, wo);
+  return (K & FT_GLOSSY) ? glossyEval(m, wi, wo) : v3(0, 0, 0);
 }
 
 // ---------------------------------------------------------------- media
@@ -657,9 +697,9 @@ NE_D float lerp(float a, float b, float t) { return a * (1.0f - t) + b * t; }
 // floor, trilinear over the 8 corners with density 0 at index >= res. The 8 corners of
 // cell (ix,iy,iz) are stored together (two float4, one 32-byte sector), so a lookup is
 // one aligned read; the values and the interpolation order are those of the dense grid.
-template <bool C>
-NE_D float sampleAt(Ctx<C>& c, const DMedium& M, const Ray& r, float t) {
-  if (C) c.c.lookups++;
+template <uint32_t K>
+NE_D float sampleAt(Ctx<K>& c, const DMedium& M, const Ray& r, float t) {
+  if (K & K_COUNT) c.c.lookups++;
   V3 p = r.at(t);
   V3 res = ld3(M.resf);
   V3 g = (p + v3(0.5f, 0.5f, 0.5f)) * res;
@@ -695,8 +735,8 @@ NE_D float sampleAt(Ctx<C>& c, const DMedium& M, const Ray& r, float t) {
 }
 
 // materials/GridMedia.cpp:45-69 GridMedia::Tr (ratio tracking).
-template <bool C>
-NE_NI V3 gridTr(Ctx<C>& c, const DMedium& M, Ray incoming, Hit isect) {
+template <uint32_t K>
+NE_NI V3 gridTr(Ctx<K>& c, const DMedium& M, Ray incoming, Hit isect) {
   incoming = transformRay(incoming, c.s.instances[isect.inst].ocs);
   incoming.o = incoming.at(isect.tNear);
   isect.tFar = isect.tFar - isect.tNear;
@@ -720,8 +760,8 @@ NE_NI V3 gridTr(Ctx<C>& c, const DMedium& M, Ray incoming, Hit isect) {
 }
 
 // materials/GridMedia.cpp:71-99 GridMedia::sample (delta tracking).
-template <bool C>
-NE_D V3 gridSample(Ctx<C>& c, const DMedium& M, Ray incoming, Ray& scattered, const Hit& isect) {
+template <uint32_t K>
+NE_D V3 gridSample(Ctx<K>& c, const DMedium& M, Ray incoming, Ray& scattered, const Hit& isect) {
   scattered.o = incoming.o;
   scattered.d = incoming.d;
   const DInstance& in = c.s.instances[isect.inst];
@@ -742,7 +782,7 @@ NE_D V3 gridSample(Ctx<C>& c, const DMedium& M, Ray incoming, Ray& scattered, co
     if (density * invMax > ra) {
       scattered.o = incoming.at(t);
       const DMaterial& m = c.s.materials[c.s.prims[isect.prim].material];
-      scattered.d = bsdfSample(m, incoming.d, v3(0, 1, 0), c.S);
+      scattered.d = bsdfSample<K>(m, incoming.d, v3(0, 1, 0), c.S);
       scattered = transformRay(scattered, in.wcs);
       return ld3(M.sigma_s) / ld3(M.sigma_t);
     }
@@ -755,15 +795,15 @@ NE_D V3 homogTr(const DMedium& M, float distance) {
   V3 v = (ld3(M.sigma_t) * distance) * M.density;
   return v3(nefm::exp(-v.x), nefm::exp(-v.y), nefm::exp(-v.z));
 }
-template <bool C>
-NE_D V3 homogSample(Ctx<C>& c, const DMedium& M, Ray incoming, Ray& scattered, const Hit& isect) {
+template <uint32_t K>
+NE_D V3 homogSample(Ctx<K>& c, const DMedium& M, Ray incoming, Ray& scattered, const Hit& isect) {
   float t = (-nefm::log(1 - c.S.random())) / avg(ld3(M.sigma_t));
   float dist = isect.tFar - isect.tNear;
   t = t / dist;
   bool sampled = t < dist;
   if (sampled) {
     scattered.o = incoming.at(t);
-    scattered.d = bsdfSample(c.s.materials[c.s.prims[isect.prim].material], incoming.d, isect.normal, c.S);
+    scattered.d = bsdfSample<K>(c.s.materials[c.s.prims[isect.prim].material], incoming.d, isect.normal, c.S);
   } else {
     scattered.o = incoming.at(dist + 0.001f);
     scattered.d = incoming.d;
@@ -775,26 +815,30 @@ NE_D V3 homogSample(Ctx<C>& c, const DMedium& M, Ray incoming, Ray& scattered, c
   return sampled ? ((Tr * ld3(M.sigma_s)) / pdf) : Tr / pdf;
 }
 
-template <bool C>
-NE_D V3 mediumTr(Ctx<C>& c, int med, const Ray& r, const Hit& isect) {
+template <uint32_t K>
+NE_D V3 mediumTr(Ctx<K>& c, int med, const Ray& r, const Hit& isect) {
   const DMedium& M = c.s.media[med];
-  if (M.type == NE_MEDIUM_GRID) return gridTr(c, M, r, isect);
-  return homogTr(M, isect.tFar - isect.tNear);
+  if ((K & FT_GRID) && M.type == NE_MEDIUM_GRID) return gridTr(c, M, r, isect);
+  if (K & FT_HOMOG) return homogTr(M, isect.tFar - isect.tNear);
+  return v3(1, 1, 1);
 }
-template <bool C>
-NE_D V3 mediumSample(Ctx<C>& c, int med, const Ray& r, Ray& scattered, const Hit& isect) {
+template <uint32_t K>
+NE_D V3 mediumSample(Ctx<K>& c, int med, const Ray& r, Ray& scattered, const Hit& isect) {
   const DMedium& M = c.s.media[med];
-  if (M.type == NE_MEDIUM_GRID) return gridSample(c, M, r, scattered, isect);
-  return homogSample(c, M, r, scattered, isect);
+  if ((K & FT_GRID) && M.type == NE_MEDIUM_GRID) return gridSample(c, M, r, scattered, isect);
+  if (K & FT_HOMOG) return homogSample(c, M, r, scattered, isect);
+  return v3(1, 1, 1);
 }
 
 // ---------------------------------------------------------------- lights
 // Primitive::samplePointOnSurface (Rectangle.cpp:78-88, Sphere.cpp:46-52,
 // Triangle.cpp:114-119, Point.cpp:14-18, AABB.cpp:81-83).
+template <uint32_t K>
 NE_NI V3 samplePointOnSurface(const DScene& s, int pi, const Hit& isect, const float* M, Sampler& S) {
   const DPrim& p = s.prims[pi];
   switch (p.type) {
     case NE_PRIM_RECTANGLE: {
+      if (!(K & FT_RECT)) break;
       float e0 = S.random();
       float e1 = S.random();
       float e2 = S.random();
@@ -804,26 +848,33 @@ NE_NI V3 samplePointOnSurface(const DScene& s, int pi, const Hit& isect, const f
       return mul4(M, q, 1.0f);
     }
     case NE_PRIM_SPHERE: {
+      if (!(K & FT_SPHERE)) break;
       V3 cc = mul4(M, ld3(p.p0), 1.0f);
       V3 n = normalize(isect.hitPoint - cc);
       return cc + n * p.radius;
     }
     case NE_PRIM_TRIANGLE: {
+      if (!(K & FT_TRI)) break;
       float ex = S.random();
       float ey = S.random();
       float sq = nefm::fsqrt(ex);
       float a = 1.0f - sq, b = ey * sq;
       return (a * ld3(p.p0) + b * ld3(p.p1)) + ((1 - a) - b) * ld3(p.p2);
     }
-    case NE_PRIM_POINT: return mul4(M, ld3(p.p0), 1.0f);
-    default: return v3(0, 0, 0);
+    case NE_PRIM_POINT:
+      if (K & FT_POINT) return mul4(M, ld3(p.p0), 1.0f);
+      break;
+    default: break;
   }
+  return v3(0, 0, 0);
 }
 // Primitive::pdf (Rectangle.cpp:159-171, Sphere.cpp:58-68, Triangle.cpp:159-161).
+template <uint32_t K>
 NE_NI float primPdf(const DScene& s, int pi, const Hit& isect, const DInstance& lin, Sampler& S) {
   const DPrim& p = s.prims[pi];
   switch (p.type) {
     case NE_PRIM_RECTANGLE: {
+      if (!(K & FT_RECT)) return 1;
       V3 size = rectSize(ld3(p.p0), ld3(p.p1));
       V3 sizeWCS = ld3(lin.scale) * size;
       float area = 1;
@@ -831,37 +882,43 @@ NE_NI float primPdf(const DScene& s, int pi, const Hit& isect, const DInstance& 
       if (sizeWCS.y != 0) area = area * sizeWCS.y;
       if (sizeWCS.z != 0) area = area * sizeWCS.z;
       return convertAreaToSolidAngle(1.0f / area, isect.normal, isect.hitPoint,
-                                     samplePointOnSurface(s, pi, isect, lin.wcs, S));
+                                     samplePointOnSurface<K>(s, pi, isect, lin.wcs, S));
     }
     case NE_PRIM_SPHERE: {
+      if (!(K & FT_SPHERE)) return 1;
       float pdfArea = __double2float_rn((double)(1.0f / 4.0f) * kPiD * (double)p.radius * (double)p.radius);
-      return convertAreaToSolidAngle(pdfArea, isect.normal, isect.hitPoint, samplePointOnSurface(s, pi, isect, lin.wcs, S));
+      return convertAreaToSolidAngle(pdfArea, isect.normal, isect.hitPoint, samplePointOnSurface<K>(s, pi, isect, lin.wcs, S));
     }
     case NE_PRIM_TRIANGLE:
+      if (!(K & FT_TRI)) return 1;
       return convertAreaToSolidAngle(1.0f / p.area, isect.normal, isect.hitPoint,
-                                     samplePointOnSurface(s, pi, isect, lin.wcs, S));
+                                     samplePointOnSurface<K>(s, pi, isect, lin.wcs, S));
     default: return 1;
   }
 }
 
 // Light::sampleLi (DiffuseLight.cpp:8-20, DirectionalLight.cpp:12-18, InfiniteAreaLight.h:83-113).
+template <uint32_t K>
 NE_NI V3 sampleLi(const DScene& s, const DLight& L, const Hit& isect, const DInstance& lin, Ray& wo, float& pdf,
                  Sampler& S) {
   switch (L.type) {
     case NE_LIGHT_DIFFUSE: {
+      if (!(K & FT_LDIFF)) return v3(0, 0, 0);
       wo.o = isect.hitPoint;
-      V3 q = samplePointOnSurface(s, L.primitive, isect, lin.wcs, S);
+      V3 q = samplePointOnSurface<K>(s, L.primitive, isect, lin.wcs, S);
       V3 d = q - wo.o;
       wo.d = normalize(d);
-      pdf = primPdf(s, L.primitive, isect, lin, S);
+      pdf = primPdf<K>(s, L.primitive, isect, lin, S);
       return ld3(L.li);
     }
     case NE_LIGHT_DIRECTIONAL:
+      if (!(K & FT_LDIR)) return v3(0, 0, 0);
       wo.o = isect.hitPoint;
       wo.d = -ld3(L.direction);
       pdf = 1;
       return ld3(L.li);
     default: {
+      if (!(K & FT_LINF)) return v3(0, 0, 0);
       float u0 = S.random();
       float u1 = S.random();
       float mapPdf = L.env_map_pdf;
@@ -890,8 +947,8 @@ NE_D const DMaterial* matOf(const DScene& s, int prim) {
 }
 
 // integrators/VolumetricPathIntegrator.cpp:10-32 intersectTr.
-template <bool C>
-NE_D bool intersectTr(Ctx<C>& c, Ray ray, Hit& intersection, V3* Tr) {
+template <uint32_t K>
+NE_D bool intersectTr(Ctx<K>& c, Ray ray, Hit& intersection, V3* Tr) {
   const float inf = __int_as_float(0x7f800000);
   *Tr = v3(1, 1, 1);
   for (int seg = 0; seg < kMaxTrSegments; seg++) {
@@ -911,8 +968,8 @@ NE_D bool intersectTr(Ctx<C>& c, Ray ray, Hit& intersection, V3* Tr) {
 }
 
 // integrators/VolumetricPathIntegrator.cpp:34-72 visibilityTr.
-template <bool C>
-NE_D V3 visibilityTr(Ctx<C>& c, V3 p, V3 lightPoint) {
+template <uint32_t K>
+NE_D V3 visibilityTr(Ctx<K>& c, V3 p, V3 lightPoint) {
   const float inf = __int_as_float(0x7f800000);
   Ray ray{p, lightPoint - p};
   V3 Tr = v3(1, 1, 1);
@@ -927,27 +984,27 @@ NE_D V3 visibilityTr(Ctx<C>& c, V3 p, V3 lightPoint) {
 }
 
 // integrators/VolumetricPathIntegrator.cpp:74-157 estimateDirect.
-template <bool C>
-NE_NI V3 estimateDirect(Ctx<C>& c, const Ray& incoming, const Hit& isect, const DLight& light, uint32_t lightInst) {
+template <uint32_t K>
+NE_NI V3 estimateDirect(Ctx<K>& c, const Ray& incoming, const Hit& isect, const DLight& light, uint32_t lightInst) {
   const DScene& s = c.s;
   const DInstance& lin = s.instances[lightInst];
   V3 Ld = v3(0, 0, 0);
   Ray wo{v3(0, 0, 0), v3(0, 0, 0)};
   float lightPdf = 0, scatteringPdf = 0;
-  V3 Li = sampleLi(s, light, isect, lin, wo, lightPdf, c.S);
+  V3 Li = sampleLi<K>(s, light, isect, lin, wo, lightPdf, c.S);
   V3 f = v3(0, 0, 0);
   const DMaterial& mat = *matOf(s, isect.prim);
   bool surface = !(mat.medium >= 0);
   if (lightPdf > 0 && !isBlack(Li)) {
     if (surface) {
-      f = bsdfEval(mat, incoming.d, wo.d, isect.normal) * fabsf(dot(wo.d, isect.normal));
-      scatteringPdf = bsdfPdf(mat, incoming.d, wo.d, isect.normal);
+      f = bsdfEval<K>(mat, incoming.d, wo.d, isect.normal) * fabsf(dot(wo.d, isect.normal));
+      scatteringPdf = bsdfPdf<K>(mat, incoming.d, wo.d, isect.normal);
     } else {
-      f = bsdfEval(mat, incoming.d, wo.d, isect.normal);
+      f = bsdfEval<K>(mat, incoming.d, wo.d, isect.normal);
       scatteringPdf = f.x;
     }
     if (!isBlack(f)) {
-      V3 pointOnLight = samplePointOnSurface(s, light.primitive, isect, lin.wcs, c.S);
+      V3 pointOnLight = samplePointOnSurface<K>(s, light.primitive, isect, lin.wcs, c.S);
       Li = Li * visibilityTr(c, isect.hitPoint, pointOnLight);
       if (!isBlack(Li)) {
         float weight = powerHeuristic(lightPdf, scatteringPdf);
@@ -956,18 +1013,18 @@ NE_NI V3 estimateDirect(Ctx<C>& c, const Ray& incoming, const Hit& isect, const 
     }
   }
   if (surface) {
-    wo.d = bsdfSample(mat, incoming.d, isect.normal, c.S);
-    f = bsdfEval(mat, incoming.d, wo.d, isect.normal);
+    wo.d = bsdfSample<K>(mat, incoming.d, isect.normal, c.S);
+    f = bsdfEval<K>(mat, incoming.d, wo.d, isect.normal);
     f = f * fabsf(dot(wo.d, isect.normal));
-    scatteringPdf = bsdfPdf(mat, incoming.d, wo.d, isect.normal);
+    scatteringPdf = bsdfPdf<K>(mat, incoming.d, wo.d, isect.normal);
   } else {
-    f = bsdfEval(mat, incoming.d, wo.d, isect.normal);
-    wo.d = bsdfSample(mat, incoming.d, v3(0, 1, 0), c.S);
+    f = bsdfEval<K>(mat, incoming.d, wo.d, isect.normal);
+    wo.d = bsdfSample<K>(mat, incoming.d, v3(0, 1, 0), c.S);
     scatteringPdf = f.x;
   }
   if (!isBlack(f) && scatteringPdf > 0) {
     float weight = 1;
-    lightPdf = primPdf(s, light.primitive, isect, lin, c.S);
+    lightPdf = primPdf<K>(s, light.primitive, isect, lin, c.S);
     if (lightPdf == 0) return Ld;
     weight = powerHeuristic(scatteringPdf, lightPdf);
     Hit lightIsect = emptyHit();
@@ -982,8 +1039,8 @@ NE_NI V3 estimateDirect(Ctx<C>& c, const Ray& incoming, const Hit& isect, const 
 }
 
 // integrators/VolumetricPathIntegrator.cpp:159-174 and primitives/Model.cpp:478-485.
-template <bool C>
-NE_D V3 uniformSampleOneLight(Ctx<C>& c, const Ray& incoming, const Hit& isect) {
+template <uint32_t K>
+NE_D V3 uniformSampleOneLight(Ctx<K>& c, const Ray& incoming, const Hit& isect) {
   const DScene& s = c.s;
   float r = c.S.random();
   uint32_t nL = s.n_light_instances;
@@ -1009,8 +1066,8 @@ struct PathParams {
 
 // integrators/VolumetricPathIntegrator.cpp:176-301 Li, plus the optional Russian
 // roulette of resources/shaders/MS_monteCarlo.frag:539-544.
-template <bool C>
-NE_D V3 Li(Ctx<C>& c, const PathParams& P, Ray incoming) {
+template <uint32_t K>
+NE_D V3 Li(Ctx<K>& c, const PathParams& P, Ray incoming) {
   const DScene& s = c.s;
   const float inf = __int_as_float(0x7f800000);
   V3 L = v3(0, 0, 0);
@@ -1021,7 +1078,7 @@ NE_D V3 Li(Ctx<C>& c, const PathParams& P, Ray incoming) {
     bool did = intersectScene(c, incoming, isect, kEps12F, inf);
     if (isBlack(T)) break;
     const DMaterial* mat = did ? matOf(s, isect.prim) : nullptr;
-    if (did && mat && mat->bsdf == NE_BSDF_VOLUME) {
+    if ((K & FT_VOLBSDF) && did && mat && mat->bsdf == NE_BSDF_VOLUME) {
       incoming.o = incoming.at(isect.tNear);
       isect.tFar = isect.tFar - isect.tNear;
       isect.tNear = 0;
@@ -1034,8 +1091,8 @@ NE_D V3 Li(Ctx<C>& c, const PathParams& P, Ray incoming) {
         continue;
       }
       T = T * sampledT;
-      V3 phaseFr = bsdfEval(*mat, incoming.d, scattered.d, isect.normal);
-      float phasePdf = bsdfPdf(*mat, incoming.d, scattered.d, isect.normal);
+      V3 phaseFr = bsdfEval<K>(*mat, incoming.d, scattered.d, isect.normal);
+      float phasePdf = bsdfPdf<K>(*mat, incoming.d, scattered.d, isect.normal);
       if (isBlack(phaseFr) || phasePdf == 0.f) break;
       V3 lightSample = uniformSampleOneLight(c, scattered, isect);
       T = T * (phaseFr / phasePdf);
@@ -1059,9 +1116,9 @@ NE_D V3 Li(Ctx<C>& c, const PathParams& P, Ray incoming) {
       L = L + T * uniformSampleOneLight(c, incoming, isect);
       Ray scattered;
       scattered.o = isect.hitPoint;
-      scattered.d = bsdfSample(*mat, incoming.d, isect.normal, c.S);
-      float pdf = bsdfPdf(*mat, incoming.d, scattered.d, isect.normal);
-      V3 fr = bsdfEval(*mat, incoming.d, scattered.d, isect.normal);
+      scattered.d = bsdfSample<K>(*mat, incoming.d, isect.normal, c.S);
+      float pdf = bsdfPdf<K>(*mat, incoming.d, scattered.d, isect.normal);
+      V3 fr = bsdfEval<K>(*mat, incoming.d, scattered.d, isect.normal);
       if (isBlack(fr) || pdf == 0.f) break;
       T = T * ((fr * absDot(incoming.d, isect.normal)) / pdf);
       incoming = scattered;
@@ -1091,8 +1148,8 @@ NE_D Ray cameraRay(const DCamera& cam, float u, float v, Sampler& S) {
 }
 
 // core/OfflineEngine.cpp:61-68.
-template <bool C>
-NE_D V3 cameraPath(Ctx<C>& c, const PathParams& P, const nerng::PathKey& base, uint32_t pixel, uint32_t sample) {
+template <uint32_t K>
+NE_D V3 cameraPath(Ctx<K>& c, const PathParams& P, const nerng::PathKey& base, uint32_t pixel, uint32_t sample) {
   uint32_t W = (uint32_t)c.s.width;
   uint32_t x = pixel % W, y = pixel / W;
   nerng::PathKey k = base;

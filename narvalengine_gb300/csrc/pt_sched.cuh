@@ -99,8 +99,8 @@ NE_D void startRatio(const DScene& s, Lane& st, const Ray& rayWcs, const Hit& h,
 // One iteration of the loops of GridMedia::sample (GridMedia.cpp:80-97) or GridMedia::Tr
 // (GridMedia.cpp:56-67). On leaving the walk the lane's pc becomes w.resume with the
 // walk's result in sampledT/scattered (delta) or walkResult (ratio).
-template <bool C>
-NE_D void walkStep(Ctx<C>& c, Lane& st) {
+template <uint32_t K>
+NE_D void walkStep(Ctx<K>& c, Lane& st) {
   Walk& w = st.w;
   const DMedium& M = c.s.media[w.med];
   float u = c.S.random();
@@ -119,7 +119,7 @@ NE_D void walkStep(Ctx<C>& c, Lane& st) {
       if (density * M.inv_max_density > ra) {
         Ray sc;
         sc.o = w.o + w.t * w.d;
-        sc.d = bsdfSample(c.s.materials[w.mat], w.d, v3(0, 1, 0), c.S);
+        sc.d = bsdfSample<K>(c.s.materials[w.mat], w.d, v3(0, 1, 0), c.S);
         st.scattered = transformRay(sc, c.s.instances[w.inst].wcs);
         st.sampledT = ld3(M.sigma_s) / ld3(M.sigma_t);
         leave = true;
@@ -175,8 +175,8 @@ NE_D void startPath(const DScene& s, Sampler& S, Lane& st, const nerng::PathKey&
 // Runs the straight-line code of Li, uniformSampleOneLight, estimateDirect, visibilityTr
 // and intersectTr (integrators/VolumetricPathIntegrator.cpp:10-300) from st.pc until the
 // lane enters a tracking walk (PC_TRACK) or its path ends (PC_DONE).
-template <bool C>
-NE_NI void transition(Ctx<C>& c, Lane& st, const PathParams& P) {
+template <uint32_t K>
+NE_NI void transition(Ctx<K>& c, Lane& st, const PathParams& P) {
   const DScene& s = c.s;
   const float inf = __int_as_float(0x7f800000);
   for (;;) {
@@ -186,12 +186,12 @@ NE_NI void transition(Ctx<C>& c, Lane& st, const PathParams& P) {
         bool did = intersectScene(c, st.incoming, st.isect, kEps12F, inf);
         if (isBlack(st.T)) { st.pc = PC_DONE; return; }
         const DMaterial* mat = did ? matOf(s, st.isect.prim) : nullptr;
-        if (did && mat && mat->bsdf == NE_BSDF_VOLUME) {
+        if ((K & FT_VOLBSDF) && did && mat && mat->bsdf == NE_BSDF_VOLUME) {
           st.incoming.o = st.incoming.at(st.isect.tNear);
           st.isect.tFar = st.isect.tFar - st.isect.tNear;
           st.isect.tNear = 0;
           const DMedium& M = s.media[mat->medium];
-          if (M.type == NE_MEDIUM_GRID) {
+          if ((K & FT_GRID) && M.type == NE_MEDIUM_GRID) {
             // GridMedia::sample (GridMedia.cpp:71-79): scattered starts as the incoming ray
             st.scattered = st.incoming;
             Ray r = transformRay(st.incoming, s.instances[st.isect.inst].ocs);
@@ -209,7 +209,7 @@ NE_NI void transition(Ctx<C>& c, Lane& st, const PathParams& P) {
             return;
           }
           st.scattered = Ray{v3(0, 0, 0), v3(0, 0, 0)};
-          st.sampledT = homogSample(c, M, st.incoming, st.scattered, st.isect);
+          st.sampledT = (K & FT_HOMOG) ? homogSample(c, M, st.incoming, st.scattered, st.isect) : v3(1, 1, 1);
           st.pc = PC_AFTER_DELTA;
           break;
         }
@@ -241,8 +241,8 @@ NE_NI void transition(Ctx<C>& c, Lane& st, const PathParams& P) {
           break;
         }
         st.T = st.T * st.sampledT;
-        V3 phaseFr = bsdfEval(mat, st.incoming.d, st.scattered.d, st.isect.normal);
-        float phasePdf = bsdfPdf(mat, st.incoming.d, st.scattered.d, st.isect.normal);
+        V3 phaseFr = bsdfEval<K>(mat, st.incoming.d, st.scattered.d, st.isect.normal);
+        float phasePdf = bsdfPdf<K>(mat, st.incoming.d, st.scattered.d, st.isect.normal);
         if (isBlack(phaseFr) || phasePdf == 0.f) { st.pc = PC_DONE; return; }
         st.phaseRatio = phaseFr / phasePdf;
         st.neeD = st.scattered.d;
@@ -261,9 +261,9 @@ NE_NI void transition(Ctx<C>& c, Lane& st, const PathParams& P) {
         st.L = st.L + st.T * st.ls;
         Ray sc;
         sc.o = st.isect.hitPoint;
-        sc.d = bsdfSample(mat, st.incoming.d, st.isect.normal, c.S);
-        float pdf = bsdfPdf(mat, st.incoming.d, sc.d, st.isect.normal);
-        V3 fr = bsdfEval(mat, st.incoming.d, sc.d, st.isect.normal);
+        sc.d = bsdfSample<K>(mat, st.incoming.d, st.isect.normal, c.S);
+        float pdf = bsdfPdf<K>(mat, st.incoming.d, sc.d, st.isect.normal);
+        V3 fr = bsdfEval<K>(mat, st.incoming.d, sc.d, st.isect.normal);
         if (isBlack(fr) || pdf == 0.f) { st.pc = PC_DONE; return; }
         st.T = st.T * ((fr * absDot(st.incoming.d, st.isect.normal)) / pdf);
         st.incoming = sc;
@@ -304,21 +304,21 @@ NE_NI void transition(Ctx<C>& c, Lane& st, const PathParams& P) {
         Ray wo{v3(0, 0, 0), v3(0, 0, 0)};
         st.lightPdf = 0;
         st.scatPdf = 0;
-        st.Li = sampleLi(s, light, st.isect, lin, wo, st.lightPdf, c.S);
+        st.Li = sampleLi<K>(s, light, st.isect, lin, wo, st.lightPdf, c.S);
         st.woD = wo.d;
         st.f = v3(0, 0, 0);
         st.surface = !(mat.medium >= 0);
         st.pc = PC_NEE_BSDF;
         if (st.lightPdf > 0 && !isBlack(st.Li)) {
           if (st.surface) {
-            st.f = bsdfEval(mat, st.neeD, st.woD, st.isect.normal) * fabsf(dot(st.woD, st.isect.normal));
-            st.scatPdf = bsdfPdf(mat, st.neeD, st.woD, st.isect.normal);
+            st.f = bsdfEval<K>(mat, st.neeD, st.woD, st.isect.normal) * fabsf(dot(st.woD, st.isect.normal));
+            st.scatPdf = bsdfPdf<K>(mat, st.neeD, st.woD, st.isect.normal);
           } else {
-            st.f = bsdfEval(mat, st.neeD, st.woD, st.isect.normal);
+            st.f = bsdfEval<K>(mat, st.neeD, st.woD, st.isect.normal);
             st.scatPdf = st.f.x;
           }
           if (!isBlack(st.f)) {
-            V3 pointOnLight = samplePointOnSurface(s, light.primitive, st.isect, lin.wcs, c.S);
+            V3 pointOnLight = samplePointOnSurface<K>(s, light.primitive, st.isect, lin.wcs, c.S);
             // visibilityTr (VolumetricPathIntegrator.cpp:34-72)
             Ray ray{st.isect.hitPoint, pointOnLight - st.isect.hitPoint};
             Hit vh = emptyHit();
@@ -331,7 +331,7 @@ NE_NI void transition(Ctx<C>& c, Lane& st, const PathParams& P) {
               } else if (vm->light < 0) {
                 if (vm->medium >= 0) {
                   const DMedium& VM = s.media[vm->medium];
-                  if (VM.type == NE_MEDIUM_GRID) {
+                  if ((K & FT_GRID) && VM.type == NE_MEDIUM_GRID) {
                     startRatio(s, st, ray, vh, vm->medium, PC_NEE_VIS_RATIO_DONE);
                     return;
                   }
@@ -361,19 +361,19 @@ NE_NI void transition(Ctx<C>& c, Lane& st, const PathParams& P) {
         // estimateDirect, BSDF sampling branch (VolumetricPathIntegrator.cpp:113-143)
         const DMaterial& mat = *matOf(s, st.isect.prim);
         if (st.surface) {
-          st.woD = bsdfSample(mat, st.neeD, st.isect.normal, c.S);
-          st.f = bsdfEval(mat, st.neeD, st.woD, st.isect.normal);
+          st.woD = bsdfSample<K>(mat, st.neeD, st.isect.normal, c.S);
+          st.f = bsdfEval<K>(mat, st.neeD, st.woD, st.isect.normal);
           st.f = st.f * fabsf(dot(st.woD, st.isect.normal));
-          st.scatPdf = bsdfPdf(mat, st.neeD, st.woD, st.isect.normal);
+          st.scatPdf = bsdfPdf<K>(mat, st.neeD, st.woD, st.isect.normal);
         } else {
-          st.f = bsdfEval(mat, st.neeD, st.woD, st.isect.normal);
-          st.woD = bsdfSample(mat, st.neeD, v3(0, 1, 0), c.S);
+          st.f = bsdfEval<K>(mat, st.neeD, st.woD, st.isect.normal);
+          st.woD = bsdfSample<K>(mat, st.neeD, v3(0, 1, 0), c.S);
           st.scatPdf = st.f.x;
         }
         st.pc = PC_NEE_END;
         if (!isBlack(st.f) && st.scatPdf > 0) {
           const DLight& light = s.lights[st.light];
-          st.lightPdf = primPdf(s, light.primitive, st.isect, s.instances[st.lightInst], c.S);
+          st.lightPdf = primPdf<K>(s, light.primitive, st.isect, s.instances[st.lightInst], c.S);
           if (st.lightPdf == 0) break;
           st.weight = powerHeuristic(st.scatPdf, st.lightPdf);
           st.trRay = Ray{st.isect.hitPoint, st.woD};
@@ -392,11 +392,11 @@ NE_NI void transition(Ctx<C>& c, Lane& st, const PathParams& P) {
         int m = tm ? tm->medium : -1;
         if (m >= 0) {
           const DMedium& TM = s.media[m];
-          if (TM.type == NE_MEDIUM_GRID) {
+          if ((K & FT_GRID) && TM.type == NE_MEDIUM_GRID) {
             startRatio(s, st, st.trRay, th, m, PC_NEE_TR_RATIO_DONE);
             return;
           }
-          st.trTr = st.trTr * homogTr(TM, th.tFar - th.tNear);
+          if (K & FT_HOMOG) st.trTr = st.trTr * homogTr(TM, th.tFar - th.tNear);
         }
         if (!hitSurface) { st.found = false; st.pc = PC_NEE_TR_DONE; break; }
         if (m >= 0) { st.found = true; st.pc = PC_NEE_TR_DONE; break; }
@@ -430,12 +430,12 @@ NE_NI void transition(Ctx<C>& c, Lane& st, const PathParams& P) {
 // The regrouped persistent kernel. Work items are (pixel, sample) as in k_paths.
 // trackShare: a warp keeps stepping walks while at least trackShare/32 of its live
 // lanes are inside one (the rest wait); otherwise it runs transitions.
-template <bool C>
+template <uint32_t K>
 __device__ __forceinline__ void schedLoop(const DScene& s, const PathParams& P, const nerng::PathKey& base,
                                           unsigned long long total, uint32_t spp, uint32_t sampleOffset,
                                           uint32_t coverW, const ne_path_key* keys, float* out,
                                           unsigned long long* counter, uint32_t* err, int trackShare) {
-  Ctx<C> c{s, Sampler{}, Counters{0, 0, 0, 0}, err};
+  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err};
   const unsigned lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
   trackShare = trackShare < 1 ? 1 : (trackShare > 32 ? 32 : trackShare);
@@ -490,7 +490,7 @@ __device__ __forceinline__ void schedLoop(const DScene& s, const PathParams& P, 
       }
     }
   }
-  if (C) {
+  if (K & K_COUNT) {
     unsigned long long v[4] = {c.c.lookups, c.c.queries, c.c.nodes, c.c.tests};
 #pragma unroll
     for (int k = 0; k < 4; k++) {
