@@ -129,9 +129,10 @@ ne_status ne_trace_closest(ne_scene* scene, const ne_ray* rays, size_t n, float 
                            ne_hit* out);
 
 /* Launch configuration of the path kernels of one scene (picked by an autotuner or by hand).
- * kernel: 0 = straight kernel (one path per lane to completion), 1 = regrouped state-machine
- * kernel (lanes refill as paths finish; a warp steps tracking walks together while at least
- * track_share/32 of its live lanes are in one). blocks_per_sm: persistent blocks per SM,
+ * kernel: 0 = straight kernel (warps take 32 paths and run them to completion), 1 = regrouped
+ * state-machine kernel (a warp steps tracking walks together while at least track_share/32 of
+ * its live lanes are in one), 2 = straight kernel whose lanes take a new path as soon as
+ * theirs ends. blocks_per_sm: persistent blocks per SM,
  * 0 = as many as fit. Every configuration renders the same bits. */
 typedef struct ne_tuning {
   int32_t kernel;

@@ -312,33 +312,38 @@ uint32_t ne_feature_set_for(uint32_t f) {
   return K_GENERAL;
 }
 
+template <uint32_t K>
+static cudaError_t launchK(int kernel, int blocks, cudaStream_t st, const DScene& s, const PathArgs& a,
+                           unsigned long long* counter, uint32_t* err) {
+  if (kernel == 0) return launchPathKernel<0, K>(blocks, st, s, a, counter, err);
+  if (kernel == 1) return launchPathKernel<1, K>(blocks, st, s, a, counter, err);
+  return launchPathKernel<2, K>(blocks, st, s, a, counter, err);
+}
+
+template <uint32_t K>
+static cudaError_t occupancyK(int kernel, int* bps) {
+  if (kernel == 0) return pathKernelOccupancy<0, K>(bps);
+  if (kernel == 1) return pathKernelOccupancy<1, K>(bps);
+  return pathKernelOccupancy<2, K>(bps);
+}
+
 cudaError_t ne_launch_path_kernel(int kernel, uint32_t set, bool count, int blocks, cudaStream_t st, const DScene& s,
                                   const PathArgs& a, unsigned long long* counter, uint32_t* err) {
-  if (count)
-    return kernel == 0 ? launchPathKernel<0, K_GENERAL | K_COUNT>(blocks, st, s, a, counter, err)
-                       : launchPathKernel<1, K_GENERAL | K_COUNT>(blocks, st, s, a, counter, err);
+  if (count) return launchK<K_GENERAL | K_COUNT>(kernel, blocks, st, s, a, counter, err);
   switch (set) {
-    case K_VOLUME:
-      return kernel == 0 ? launchPathKernel<0, K_VOLUME>(blocks, st, s, a, counter, err)
-                         : launchPathKernel<1, K_VOLUME>(blocks, st, s, a, counter, err);
-    case K_SURFACE:
-      return kernel == 0 ? launchPathKernel<0, K_SURFACE>(blocks, st, s, a, counter, err)
-                         : launchPathKernel<1, K_SURFACE>(blocks, st, s, a, counter, err);
-    case K_MESH:
-      return kernel == 0 ? launchPathKernel<0, K_MESH>(blocks, st, s, a, counter, err)
-                         : launchPathKernel<1, K_MESH>(blocks, st, s, a, counter, err);
-    default:
-      return kernel == 0 ? launchPathKernel<0, K_GENERAL>(blocks, st, s, a, counter, err)
-                         : launchPathKernel<1, K_GENERAL>(blocks, st, s, a, counter, err);
+    case K_VOLUME: return launchK<K_VOLUME>(kernel, blocks, st, s, a, counter, err);
+    case K_SURFACE: return launchK<K_SURFACE>(kernel, blocks, st, s, a, counter, err);
+    case K_MESH: return launchK<K_MESH>(kernel, blocks, st, s, a, counter, err);
+    default: return launchK<K_GENERAL>(kernel, blocks, st, s, a, counter, err);
   }
 }
 
 cudaError_t ne_path_kernel_occupancy(int kernel, uint32_t set, int* bps) {
   switch (set) {
-    case K_VOLUME: return kernel == 0 ? pathKernelOccupancy<0, K_VOLUME>(bps) : pathKernelOccupancy<1, K_VOLUME>(bps);
-    case K_SURFACE: return kernel == 0 ? pathKernelOccupancy<0, K_SURFACE>(bps) : pathKernelOccupancy<1, K_SURFACE>(bps);
-    case K_MESH: return kernel == 0 ? pathKernelOccupancy<0, K_MESH>(bps) : pathKernelOccupancy<1, K_MESH>(bps);
-    default: return kernel == 0 ? pathKernelOccupancy<0, K_GENERAL>(bps) : pathKernelOccupancy<1, K_GENERAL>(bps);
+    case K_VOLUME: return occupancyK<K_VOLUME>(kernel, bps);
+    case K_SURFACE: return occupancyK<K_SURFACE>(kernel, bps);
+    case K_MESH: return occupancyK<K_MESH>(kernel, bps);
+    default: return occupancyK<K_GENERAL>(kernel, bps);
   }
 }
 
@@ -657,7 +662,7 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
 }
 
 ne_status ne_scene_set_tuning(ne_scene* sc, const ne_tuning* t) {
-  if (!sc || !t || t->kernel < 0 || t->kernel > 1 || t->track_share < 1 || t->track_share > 32 ||
+  if (!sc || !t || t->kernel < 0 || t->kernel > 2 || t->track_share < 1 || t->track_share > 32 ||
       t->blocks_per_sm < 0 || t->blocks_per_sm > 64)
     return NE_ERR_INVALID_ARG;
   ne_context* ctx = sc->ctx;

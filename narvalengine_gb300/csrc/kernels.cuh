@@ -6,6 +6,7 @@
 // K_GENERAL) and instantiated in its own translation unit (k_path_<kernel>_<set>.cu) so the
 // build compiles them in parallel; the counting variants (K | K_COUNT) use K_GENERAL.
 #pragma once
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include "narval_gb300.h"
@@ -78,21 +79,57 @@ __global__ void __launch_bounds__(kThreads) k_paths(const __grid_constant__ DSce
   flushCounters<K>(c.c, counter);
 }
 
-// One launcher per (kernel, feature set); KERNEL 0 = k_paths, 1 = k_sched.
+// Straight kernel with lane-level refill: a lane that finishes its path takes the next
+// work item at once, together with whichever lanes finish at the same time (coalesced-group
+// atomic), instead of waiting for the longest path of its warp.
+template <uint32_t K>
+__global__ void __launch_bounds__(kThreads) k_lanes(const __grid_constant__ DScene s, const PathArgs a,
+                                                    unsigned long long* __restrict__ counter, uint32_t* err) {
+  namespace cg = cooperative_groups;
+  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err};
+  for (;;) {
+    cg::coalesced_group g = cg::coalesced_threads();
+    unsigned long long base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(&counter[0], (unsigned long long)g.size());
+    unsigned long long idx = g.shfl(base, 0) + g.thread_rank();
+    if (idx >= a.total) break;
+    uint32_t pixel, sample;
+    if (a.keys) {
+      ne_path_key k = a.keys[idx];
+      pixel = k.pixel;
+      sample = k.sample + a.sample_offset;
+    } else {
+      uint32_t pi = (uint32_t)(idx / a.spp);
+      sample = (uint32_t)(idx % a.spp) + a.sample_offset;
+      pixel = (pi / a.cover_w) * (uint32_t)s.width + (pi % a.cover_w);
+    }
+    V3 L = cameraPath(c, a.P, a.base, pixel, sample);
+    a.out[3 * idx + 0] = L.x;
+    a.out[3 * idx + 1] = L.y;
+    a.out[3 * idx + 2] = L.z;
+  }
+  __syncwarp();
+  flushCounters<K>(c.c, counter);
+}
+
+// One launcher per (kernel, feature set); KERNEL 0 = k_paths, 1 = k_sched, 2 = k_lanes.
 template <int KERNEL, uint32_t K>
 cudaError_t launchPathKernel(int blocks, cudaStream_t st, const DScene& s, const PathArgs& a,
                              unsigned long long* counter, uint32_t* err) {
   if (KERNEL == 0)
     k_paths<K><<<blocks, kThreads, 0, st>>>(s, a, counter, err);
-  else
+  else if (KERNEL == 1)
     k_sched<K><<<blocks, kThreads, 0, st>>>(s, a, counter, err);
+  else
+    k_lanes<K><<<blocks, kThreads, 0, st>>>(s, a, counter, err);
   return cudaGetLastError();
 }
 
 template <int KERNEL, uint32_t K>
 cudaError_t pathKernelOccupancy(int* blocks_per_sm) {
   if (KERNEL == 0) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_paths<K>, kThreads, 0);
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_sched<K>, kThreads, 0);
+  if (KERNEL == 1) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_sched<K>, kThreads, 0);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_lanes<K>, kThreads, 0);
 }
 
 #define NE_PATH_KERNEL_INSTANCE(EXT, KERNEL, K)                                                              \
@@ -109,8 +146,13 @@ cudaError_t pathKernelOccupancy(int* blocks_per_sm) {
   NE_PATH_KERNEL_INSTANCE(EXT, 1, K_SURFACE)             \
   NE_PATH_KERNEL_INSTANCE(EXT, 1, K_MESH)                \
   NE_PATH_KERNEL_INSTANCE(EXT, 1, K_GENERAL)             \
+  NE_PATH_KERNEL_INSTANCE(EXT, 2, K_VOLUME)              \
+  NE_PATH_KERNEL_INSTANCE(EXT, 2, K_SURFACE)             \
+  NE_PATH_KERNEL_INSTANCE(EXT, 2, K_MESH)                \
+  NE_PATH_KERNEL_INSTANCE(EXT, 2, K_GENERAL)             \
   NE_PATH_KERNEL_INSTANCE(EXT, 0, K_GENERAL | K_COUNT)   \
-  NE_PATH_KERNEL_INSTANCE(EXT, 1, K_GENERAL | K_COUNT)
+  NE_PATH_KERNEL_INSTANCE(EXT, 1, K_GENERAL | K_COUNT)   \
+  NE_PATH_KERNEL_INSTANCE(EXT, 2, K_GENERAL | K_COUNT)
 
 // Declared here, instantiated in the k_path_*.cu units only.
 NE_PATH_KERNEL_ALL(extern)

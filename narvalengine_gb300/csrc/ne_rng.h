@@ -41,8 +41,10 @@ NE_RNG_HD void mulhilo(uint32_t a, uint32_t b, uint32_t* hi, uint32_t* lo) {
 NE_RNG_HD Block philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1) {
   const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
   const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+  // Rounds stay a loop on the device: the generator is inlined at every draw site and an
+  // unrolled copy at each would dominate the path kernel's code size.
 #if defined(__CUDA_ARCH__)
-#pragma unroll
+#pragma unroll 1
 #endif
   for (int r = 0; r < 10; ++r) {
     uint32_t hi0, lo0, hi1, lo1;

@@ -29,7 +29,7 @@ def ctx(ne):
     c.close()
 
 
-KERNELS = {0: "straight", 1: "regrouped"}
+KERNELS = {0: "straight", 1: "regrouped", 2: "lanes"}
 
 
 @pytest.fixture(scope="module", params=[(s, k) for s in ("cornell_c1", "medium_c2") for k in KERNELS],
@@ -196,14 +196,14 @@ def test_kernels_and_tunings_agree(ne, ctx):
     scene = ctx.upload(host)
     p = ne.render_params(seed=21, spp=2)
     ref = None
-    for kernel, share, bps in [(0, 16, 0), (0, 16, 1), (1, 16, 0), (1, 1, 0), (1, 32, 0), (1, 8, 1)]:
+    for kernel, share, bps in [(0, 16, 0), (0, 16, 1), (1, 16, 0), (1, 1, 0), (1, 32, 0), (1, 8, 1), (2, 16, 0), (2, 16, 1)]:
         scene.set_tuning(kernel=kernel, track_share=share, blocks_per_sm=bps)
         img, stats = scene.render(p)
         if ref is None:
             ref = img
         assert np.array_equal(img, ref), (kernel, share, bps)
     with pytest.raises(ne.NarvalError):
-        scene.set_tuning(kernel=7)
+        scene.set_tuning(kernel=3)
     with pytest.raises(ne.NarvalError):
         scene.set_tuning(kernel=1, track_share=0)
 
@@ -213,12 +213,13 @@ def test_counting_kernels_agree(ne, ctx):
     host = ne.SceneHost.from_json(scene_path("medium_c2"))
     scene = ctx.upload(host)
     out = {}
-    for kernel in (0, 1):
+    for kernel in (0, 1, 2):
         scene.set_tuning(kernel=kernel)
         img, st = scene.render(ne.render_params(seed=2, spp=1, flags=ne.NE_RENDER_COUNT_WORK))
         out[kernel] = (img, st["density_lookups"], st["scene_queries"])
-    assert np.array_equal(out[0][0], out[1][0])
-    assert out[0][1] == out[1][1] and out[0][2] == out[1][2] and out[0][1] > 0
+    for k in (1, 2):
+        assert np.array_equal(out[0][0], out[k][0])
+        assert out[0][1] == out[k][1] and out[0][2] == out[k][2] and out[0][1] > 0
 
 
 def mesh_scene_json(subdivisions):
@@ -243,7 +244,7 @@ def test_mesh_bvh_parity(ne, ctx, oracle_lib, subdivisions):
     assert np.array_equal(g["t_near"].view(np.uint32), c["t_near"].view(np.uint32))
     assert (g["primitive"] >= 0).sum() > 1000
     keys = spread_keys(host, 512, 4, seed=3)
-    for kernel in (0, 1):
+    for kernel in (0, 1, 2):
         scene.set_tuning(kernel=kernel)
         gp = scene.trace_paths(keys, ne.render_params(seed=8))
         cp = orc.trace_paths(keys, ne.render_params(seed=8))
