@@ -116,6 +116,13 @@ void ne_scene_destroy(ne_scene* scene);
  * radiance, before tone mapping, as width*height*3 floats, pixel y*width+x. */
 ne_status ne_render(ne_scene* scene, const ne_render_params* params, float* out_rgb, ne_render_stats* stats);
 
+/* Adds the radiance of samples [sample_offset, sample_offset + spp) of every pixel to a
+ * width*height*3 FP64 accumulator, each path converted to double and summed in sample order
+ * (for converged reference images; divide by the total sample count). With
+ * NE_RENDER_OUT_DEVICE the accumulator is device memory, else host memory. */
+ne_status ne_render_accumulate(ne_scene* scene, const ne_render_params* params, double* accum,
+                               ne_render_stats* stats);
+
 /* Camera path per key: camera ray (draws 0-3) then Li (draws from 4). out_L: n*3 floats. */
 ne_status ne_trace_paths(ne_scene* scene, const ne_render_params* params, const ne_path_key* keys, size_t n,
                          float* out_L);

@@ -224,6 +224,15 @@ class Scene:
         self.ctx.check(library().ne_render(self._h, C.byref(p), ptr, C.byref(stats)))
         return img, {f: getattr(stats, f) for f, _ in NeRenderStats._fields_ if f != "pad"}
 
+    def accumulate(self, accum: np.ndarray, params: NeRenderParams | None = None, **kw) -> dict:
+        """Adds samples to an FP64 (H, W, 3) accumulator (ne_render_accumulate)."""
+        p = params if params is not None else render_params(**kw)
+        if accum.dtype != np.float64 or not accum.flags.c_contiguous or accum.size != self.host.width * self.host.height * 3:
+            raise ValueError("accum must be a C-contiguous float64 array of width*height*3 values")
+        stats = NeRenderStats()
+        self.ctx.check(library().ne_render_accumulate(self._h, C.byref(p), _ptr(accum), C.byref(stats)))
+        return {f: getattr(stats, f) for f, _ in NeRenderStats._fields_ if f != "pad"}
+
     def set_tuning(self, kernel: int = 0, track_share: int = 16, blocks_per_sm: int = 0):
         """Launch configuration of the path kernels (see ne_tuning in include/narval_gb300.h)."""
         t = _abi.NeTuning(kernel, track_share, blocks_per_sm, 0)

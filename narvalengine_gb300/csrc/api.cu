@@ -227,6 +227,24 @@ __global__ void k_reduce(const float* __restrict__ paths, uint32_t n_pix, uint32
   }
 }
 
+// FP64 accumulation of per-path radiance, samples in order.
+__global__ void k_accum(const float* __restrict__ paths, uint32_t n_pix, uint32_t spp, uint32_t cover_w, int W,
+                        double* __restrict__ acc) {
+  for (uint32_t pi = blockIdx.x * blockDim.x + threadIdx.x; pi < n_pix; pi += gridDim.x * blockDim.x) {
+    const float* p = paths + (size_t)pi * spp * 3;
+    size_t pixel = (size_t)(pi / cover_w) * (size_t)W + (pi % cover_w);
+    double r = acc[3 * pixel + 0], g = acc[3 * pixel + 1], b = acc[3 * pixel + 2];
+    for (uint32_t k = 0; k < spp; k++) {
+      r += (double)p[3 * k + 0];
+      g += (double)p[3 * k + 1];
+      b += (double)p[3 * k + 2];
+    }
+    acc[3 * pixel + 0] = r;
+    acc[3 * pixel + 1] = g;
+    acc[3 * pixel + 2] = b;
+  }
+}
+
 __global__ void k_fmath(int fn, const float* __restrict__ x, size_t n, float* __restrict__ out) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     float v = x[i], r;
@@ -770,6 +788,74 @@ ne_status ne_render(ne_scene* sc, const ne_render_params* p, float* out_rgb, ne_
     cudaEventElapsedTime(&tms, ctx->ev[0], ctx->ev[3]);
     stats->kernel_ms = kms;
     stats->total_ms = tms;
+    stats->paths = total;
+    stats->density_lookups = cnt[1];
+    stats->scene_queries = cnt[2];
+    stats->bvh_nodes = cnt[3];
+    stats->prim_tests = cnt[4];
+    stats->kernel_launches = 2;
+  }
+  return NE_OK;
+}
+
+ne_status ne_render_accumulate(ne_scene* sc, const ne_render_params* p, double* accum, ne_render_stats* stats) {
+  if (!sc || !accum) return NE_ERR_INVALID_ARG;
+  ne_context* ctx = sc->ctx;
+  NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  const int W = sc->settings.width, H = sc->settings.height;
+  int spp = (p && p->spp > 0) ? p->spp : sc->settings.spp;
+  if (spp <= 0) return fail(ctx, NE_ERR_INVALID_ARG, "spp must be positive");
+  uint32_t flags = p ? p->flags : 0;
+  uint32_t cw = (uint32_t)W, ch = (uint32_t)H;
+  if (flags & NE_RENDER_REF_TILES) {
+    cw = 40u * (uint32_t)(W / 40);
+    ch = 10u * (uint32_t)(H / 10);
+  }
+  uint64_t npix = (uint64_t)cw * ch, total = npix * (uint64_t)spp;
+  if (sc->paths_cap < total) {
+    if (sc->d_paths) cudaFree(sc->d_paths);
+    sc->d_paths = nullptr;
+    sc->paths_cap = 0;
+    NE_CUDA(cudaMalloc(&sc->d_paths, total * 3 * sizeof(float)), "cudaMalloc(paths)");
+    sc->paths_cap = total;
+  }
+  bool devAcc = flags & NE_RENDER_OUT_DEVICE;
+  size_t accBytes = (size_t)W * H * 3 * sizeof(double);
+  DevBuf<double> tmp;
+  double* d_acc = accum;
+  if (!devAcc) {
+    NE_CUDA(cudaMalloc(&tmp.p, accBytes), "cudaMalloc(accum)");
+    d_acc = tmp.p;
+    NE_CUDA(cudaMemcpyAsync(d_acc, accum, accBytes, cudaMemcpyHostToDevice, ctx->stream), "cudaMemcpyAsync");
+  }
+  NE_CUDA(cudaMemsetAsync(ctx->d_err, 0, 4, ctx->stream), "cudaMemsetAsync");
+  NE_CUDA(cudaEventRecord(ctx->ev[1], ctx->stream), "cudaEventRecord");
+  PathArgs a;
+  a.P = pathParams(sc, p);
+  a.base = baseKey(p);
+  a.total = total;
+  a.spp = (uint32_t)spp;
+  a.sample_offset = p ? p->sample_offset : 0;
+  a.cover_w = cw;
+  a.keys = nullptr;
+  a.out = sc->d_paths;
+  a.track_share = sc->track_share;
+  ne_status st = launchPaths(sc, a, (flags & NE_RENDER_COUNT_WORK) != 0);
+  if (st) return st;
+  NE_CUDA(cudaEventRecord(ctx->ev[2], ctx->stream), "cudaEventRecord");
+  int rblocks = (int)std::min<uint64_t>((npix + 255) / 256, (uint64_t)ctx->sm_count * 16);
+  k_accum<<<std::max(1, rblocks), 256, 0, ctx->stream>>>(sc->d_paths, (uint32_t)npix, (uint32_t)spp, cw, W, d_acc);
+  NE_CUDA(cudaGetLastError(), "k_accum launch");
+  if (!devAcc) NE_CUDA(cudaMemcpyAsync(accum, d_acc, accBytes, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync");
+  unsigned long long cnt[5] = {0, 0, 0, 0, 0};
+  NE_CUDA(cudaMemcpyAsync(cnt, ctx->d_counter, sizeof(cnt), cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync");
+  st = checkErr(ctx);
+  if (st) return st;
+  if (stats) {
+    memset(stats, 0, sizeof(*stats));
+    float kms = 0;
+    cudaEventElapsedTime(&kms, ctx->ev[1], ctx->ev[2]);
+    stats->kernel_ms = kms;
     stats->paths = total;
     stats->density_lookups = cnt[1];
     stats->scene_queries = cnt[2];

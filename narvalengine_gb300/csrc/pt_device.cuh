@@ -135,14 +135,23 @@ NE_D Hit emptyHit() {
 }
 
 // Counter RNG with the current four-word block cached in registers.
+// One Philox block, compiled once and called from every draw site. A free function with
+// value arguments: a member function would take the sampler's address and push the whole
+// per-path context out of registers into local memory.
+static __device__ __noinline__ uint4 philoxBlock(uint32_t b, uint32_t sample, uint32_t pixel, uint32_t stream,
+                                                  uint32_t k0, uint32_t k1) {
+  nerng::Block r = nerng::philox4x32_10(b, sample, pixel, stream, k0, k1);
+  return make_uint4(r.w[0], r.w[1], r.w[2], r.w[3]);
+}
+
 struct Sampler {
   nerng::PathKey key;
   uint32_t dim;
   uint32_t blk;
   uint32_t w0, w1, w2, w3;
-  __device__ __noinline__ void refill(uint32_t b) {
-    nerng::Block r = nerng::philox4x32_10(b, key.sample, key.pixel, key.stream, key.seed_lo, key.seed_hi);
-    w0 = r.w[0]; w1 = r.w[1]; w2 = r.w[2]; w3 = r.w[3];
+  NE_D void refill(uint32_t b) {
+    uint4 r = philoxBlock(b, key.sample, key.pixel, key.stream, key.seed_lo, key.seed_hi);
+    w0 = r.x; w1 = r.y; w2 = r.z; w3 = r.w;
     blk = b;
   }
   NE_D void reset(const nerng::PathKey& k, uint32_t d) {

@@ -262,3 +262,17 @@ def test_destroy_order(ne):
     s2.close()
     s1.close()
     c.close()
+
+
+def test_fp64_accumulation(ne, ctx):
+    """ne_render_accumulate sums the same per-path radiance as ne_render, in FP64."""
+    host = ne.SceneHost.from_json(scene_path("cornell_c1"))
+    scene = ctx.upload(host)
+    acc = np.zeros((host.height, host.width, 3), np.float64)
+    for off in (0, 3):
+        scene.accumulate(acc, seed=6, spp=3, sample_offset=off)
+    img, _ = scene.render(seed=6, spp=6)
+    assert np.allclose(acc / 6, img, rtol=1e-5, atol=1e-6)
+    keys = np.array([[1000, s] for s in range(6)], np.uint32)
+    L = scene.trace_paths(keys, seed=6).astype(np.float64)
+    assert np.allclose(acc.reshape(-1, 3)[1000], L.sum(0), rtol=1e-12, atol=1e-12)
