@@ -116,6 +116,24 @@ void ne_scene_destroy(ne_scene* scene);
  * radiance, before tone mapping, as width*height*3 floats, pixel y*width+x. */
 ne_status ne_render(ne_scene* scene, const ne_render_params* params, float* out_rgb, ne_render_stats* stats);
 
+/* ne_render without allocation: no counterpart in the reference (whose CPU render
+ * allocates freely). For callers that cannot call cudaMalloc while rendering: a host
+ * application that has reserved the device's memory for its own pool (cudaMalloc then
+ * fails) and frame loops that must not stall on cudaFree, which synchronises the device.
+ * The image (width*height*3 floats, as ne_render) must be DEVICE memory owned by the
+ * caller; NE_RENDER_OUT_DEVICE is implied and NE_RENDER_NO_SYNC is ignored (the call waits
+ * for the render to read its error flag). Per-path
+ * scratch comes from a fixed array of the library of NE_NOALLOC_MAX_PATHS paths (12 MiB),
+ * held on every GPU that loads the library until the process exits; a call with more
+ * paths (covered pixels x spp) fails with NE_ERR_INVALID_ARG. The first call on a device
+ * looks up the array's address (cudaGetSymbolAddress) and should come before any stream
+ * capture. All calls on a device share the array, which keeps the last call's contents:
+ * calls whose work overlaps on the GPU (contexts on one device, unordered streams) race
+ * and must be serialised by the caller. */
+#define NE_NOALLOC_MAX_PATHS (1u << 20)
+ne_status ne_render_noalloc(ne_scene* scene, const ne_render_params* params, float* out_rgb_device,
+                            ne_render_stats* stats);
+
 /* Adds the radiance of samples [sample_offset, sample_offset + spp) of every pixel to a
  * width*height*3 FP64 accumulator, each path converted to double and summed in sample order
  * (for converged reference images; divide by the total sample count). With

@@ -118,6 +118,7 @@ SIGNATURES = {
     "ne_scene_upload": (C.c_int32, [C.c_void_p, C.POINTER(NeSceneDesc), C.POINTER(C.c_void_p)]),
     "ne_scene_destroy": (None, [C.c_void_p]),
     "ne_render": (C.c_int32, [C.c_void_p, C.POINTER(NeRenderParams), C.c_void_p, C.POINTER(NeRenderStats)]),
+    "ne_render_noalloc": (C.c_int32, [C.c_void_p, C.POINTER(NeRenderParams), C.c_void_p, C.POINTER(NeRenderStats)]),
     "ne_render_accumulate": (C.c_int32, [C.c_void_p, C.POINTER(NeRenderParams), C.c_void_p,
                                          C.POINTER(NeRenderStats)]),
     "ne_trace_paths": (C.c_int32, [C.c_void_p, C.POINTER(NeRenderParams), C.c_void_p, C.c_size_t, C.c_void_p]),

@@ -16,6 +16,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -364,6 +365,53 @@ cudaError_t ne_path_kernel_occupancy(int kernel, uint32_t set, int* bps) {
     default: return occupancyK<K_GENERAL>(kernel, bps);
   }
 }
+
+// ---------------------------------------------------------------------------------------
+// Allocation-free render. Some callers cannot call cudaMalloc at render time: a host
+// application that reserves the device's memory up front for its own pool (cudaMalloc then
+// fails), and frame loops that must not stall, since cudaFree synchronises the whole device.
+// ne_render allocates its per-path radiance buffer lazily and, for a host image, a device
+// image; ne_render_noalloc renders into a caller-owned device image and takes its scratch
+// (per-path radiance, work counters, error flag) from the fixed array below.
+//
+// The array is file-scope device memory: every GPU that loads this library holds its
+// kNoAllocScratchBytes until the process exits. All calls on a device share it and it keeps
+// the last call's contents; the counters and error flag are cleared at the start of each
+// call (per-path radiance is written in full before it is read). Calls whose work overlaps
+// on the GPU (two contexts on one device, or streams not ordered with one another) race on
+// the array and must be serialised by the caller.
+// ---------------------------------------------------------------------------------------
+namespace {
+
+constexpr uint64_t kNoAllocMaxPaths = NE_NOALLOC_MAX_PATHS;  // e.g. 256 x 256 pixels x 16 samples
+constexpr size_t kNoAllocHeaderBytes = 256;        // work counters [0..7], error flag
+constexpr size_t kNoAllocScratchBytes = kNoAllocHeaderBytes + kNoAllocMaxPaths * 3 * sizeof(float);
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+std::mutex g_noalloc_mutex;
+unsigned char* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// Device address of the array on the current device, looked up once per device. In host
+// code g_noalloc_scratch names a host-side stand-in, so the address must come from the
+// runtime.
+ne_status noallocScratch(ne_context* ctx, unsigned char** out) {
+  if (ctx->device < 0 || ctx->device >= kNoAllocMaxDevices)
+    return fail(ctx, NE_ERR_UNSUPPORTED, "ne_render_noalloc supports device ordinals below 64");
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[ctx->device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+      return fail(ctx, NE_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+    g_noalloc_ptr[ctx->device] = (unsigned char*)p;
+  }
+  *out = g_noalloc_ptr[ctx->device];
+  return NE_OK;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -1010,6 +1058,82 @@ ne_status ne_debug_rng(ne_context* ctx, uint64_t seed, const ne_path_key* keys, 
   NE_CUDA(cudaGetLastError(), "k_rng launch");
   NE_CUDA(cudaMemcpyAsync(out, dy.p, n * 4, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync");
   NE_CUDA(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  return NE_OK;
+}
+
+ne_status ne_render_noalloc(ne_scene* sc, const ne_render_params* p, float* out_rgb_device, ne_render_stats* stats) {
+  if (!sc || !out_rgb_device) return NE_ERR_INVALID_ARG;
+  ne_context* ctx = sc->ctx;
+  NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  const int W = sc->settings.width, H = sc->settings.height;
+  int spp = (p && p->spp > 0) ? p->spp : sc->settings.spp;
+  if (spp <= 0) return fail(ctx, NE_ERR_INVALID_ARG, "spp must be positive");
+  uint32_t flags = p ? p->flags : 0;
+  uint32_t cw = (uint32_t)W, ch = (uint32_t)H;
+  if (flags & NE_RENDER_REF_TILES) {
+    cw = 40u * (uint32_t)(W / 40);
+    ch = 10u * (uint32_t)(H / 10);
+  }
+  uint64_t npix = (uint64_t)cw * ch;
+  uint64_t total = npix * (uint64_t)spp;
+  if (total > kNoAllocMaxPaths)
+    return fail(ctx, NE_ERR_INVALID_ARG,
+                "ne_render_noalloc: " + std::to_string(total) + " paths (pixels x spp) exceed its scratch of " +
+                    std::to_string(kNoAllocMaxPaths) + " paths; render fewer samples per call");
+  unsigned char* scratch = nullptr;
+  ne_status st = noallocScratch(ctx, &scratch);
+  if (st) return st;
+  unsigned long long* d_counter = (unsigned long long*)scratch;
+  uint32_t* d_err = (uint32_t*)(scratch + 8 * sizeof(unsigned long long));
+  float* d_paths = (float*)(scratch + kNoAllocHeaderBytes);
+  NE_CUDA(cudaMemsetAsync(scratch, 0, kNoAllocHeaderBytes, ctx->stream), "cudaMemsetAsync");
+  size_t imgBytes = (size_t)W * H * 3 * sizeof(float);
+  NE_CUDA(cudaEventRecord(ctx->ev[0], ctx->stream), "cudaEventRecord");
+  if (cw != (uint32_t)W || ch != (uint32_t)H)
+    NE_CUDA(cudaMemsetAsync(out_rgb_device, 0, imgBytes, ctx->stream), "cudaMemsetAsync");
+  PathArgs a;
+  a.P = pathParams(sc, p);
+  a.base = baseKey(p);
+  a.total = total;
+  a.spp = (uint32_t)spp;
+  a.sample_offset = p ? p->sample_offset : 0;
+  a.cover_w = cw;
+  a.keys = nullptr;
+  a.out = d_paths;
+  a.track_share = sc->track_share;
+  int blocks = persistentBlocks(sc);
+  unsigned long long needed = (total + kThreads - 1) / kThreads;
+  if ((unsigned long long)blocks > needed) blocks = (int)std::max<unsigned long long>(1, needed);
+  NE_CUDA(cudaEventRecord(ctx->ev[1], ctx->stream), "cudaEventRecord");
+  NE_CUDA(ne_launch_path_kernel(sc->variant, sc->feature_set, (flags & NE_RENDER_COUNT_WORK) != 0, blocks,
+                                ctx->stream, sc->d, a, d_counter, d_err),
+          "path kernel launch");
+  NE_CUDA(cudaEventRecord(ctx->ev[2], ctx->stream), "cudaEventRecord");
+  int rblocks = (int)std::min<uint64_t>((npix + 255) / 256, (uint64_t)ctx->sm_count * 16);
+  k_reduce<<<std::max(1, rblocks), 256, 0, ctx->stream>>>(d_paths, (uint32_t)npix, (uint32_t)spp, cw, W,
+                                                          out_rgb_device);
+  NE_CUDA(cudaGetLastError(), "k_reduce launch");
+  NE_CUDA(cudaEventRecord(ctx->ev[3], ctx->stream), "cudaEventRecord");
+  unsigned long long cnt[5] = {0, 0, 0, 0, 0};
+  uint32_t e = 0;
+  NE_CUDA(cudaMemcpyAsync(cnt, d_counter, sizeof(cnt), cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync");
+  NE_CUDA(cudaMemcpyAsync(&e, d_err, 4, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync(err)");
+  NE_CUDA(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  if (e & ERR_BVH_STACK) return fail(ctx, NE_ERR_UNSUPPORTED, "BVH traversal stack exceeded 64 entries");
+  if (stats) {
+    memset(stats, 0, sizeof(*stats));
+    float kms = 0, tms = 0;
+    cudaEventElapsedTime(&kms, ctx->ev[1], ctx->ev[2]);
+    cudaEventElapsedTime(&tms, ctx->ev[0], ctx->ev[3]);
+    stats->kernel_ms = kms;
+    stats->total_ms = tms;
+    stats->paths = total;
+    stats->density_lookups = cnt[1];
+    stats->scene_queries = cnt[2];
+    stats->bvh_nodes = cnt[3];
+    stats->prim_tests = cnt[4];
+    stats->kernel_launches = 2;
+  }
   return NE_OK;
 }
 
