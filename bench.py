@@ -47,6 +47,8 @@ WORKLOADS = {
                   "256x256x16spp, depth 8, RR after 3",
     "mesh_c3": "mesh_c3: 1.31M-triangle displaced icosphere (1024 GGX groups) on a 10x10 ground, two emitters 10, "
                "1024x1024x32spp, depth 12, reference midpoint BVH",
+    "cloud_c4": "cloud_c4: 512^3 fBm cloud (7 octaves, scale 80, albedo 0.99, HG g=0.85), sun 3.0 @30deg + env 0.2, "
+                "1024x1024x16spp, depth 256, plain integrator",
 }
 WORKLOAD = WORKLOADS["medium_c2"]
 BYTES_PER_NODE = 32   # BVH node: two float4 (bounds + child/leaf words)
@@ -188,7 +190,7 @@ def run_reference(args, rank: int, world: int):
     v = statistics.median(x["value"] for x in vals)
     line = {"metric": METRIC, "value": v, "unit": "Mpaths/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded fBm grid)", "impl": "reference",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)", "impl": "reference",
             "config": {"workload": WORKLOAD, "sample": "bounded pixel sample per step"},
             "cpu_baseline": dict(vals[-1], value=v),
             "e2e": {"value": v, "unit": "Mpaths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -201,7 +203,8 @@ def run_profile_case(spp: int, kernel: int, track_share: int):
     ctx = ne.Context(0)
     host = ne.SceneHost.from_json(os.path.join(ne.SCENES_DIR, SCENE))
     scene = ctx.upload(host)
-    scene.set_tuning(kernel=kernel, track_share=track_share)
+    if kernel >= 0:
+        scene.set_tuning(kernel=kernel, track_share=track_share)
     for i in range(2):
         _, st = scene.render(ne.render_params(seed=1, spp=spp))
     _, cst = scene.render(ne.render_params(seed=1, spp=spp, flags=ne.NE_RENDER_COUNT_WORK))
@@ -222,7 +225,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--scene", default="medium_c2", choices=sorted(WORKLOADS),
                     help="workload (the default is the configuration the metric is quoted on)")
-    ap.add_argument("--kernel", type=int, default=0, help="path kernel (ne_tuning.kernel): 0 straight, 1 regrouped")
+    ap.add_argument("--kernel", type=int, default=-1,
+                    help="path kernel (ne_tuning.kernel): 0 straight, 1 regrouped, 2 lane refill; "
+                         "default: the library's choice for the scene")
     ap.add_argument("--track-share", type=int, default=16, help="regrouped kernel tracking threshold, 32nds")
     ap.add_argument("--profile-spp", type=int, default=0,
                     help="profiling case: two renders of the workload at this spp (the second is the one to capture)")
@@ -244,7 +249,8 @@ def main():
     ctx = ne.Context(local)
     host = ne.SceneHost.from_json(os.path.join(ne.SCENES_DIR, SCENE))
     scene = ctx.upload(host)
-    scene.set_tuning(kernel=args.kernel, track_share=args.track_share)
+    if args.kernel >= 0:
+        scene.set_tuning(kernel=args.kernel, track_share=args.track_share)
     W, H, spp = host.width, host.height, host.spp
     paths_per_step = W * H * spp
     img_bytes = W * H * 3 * 4
@@ -303,14 +309,16 @@ def main():
     pe = ne.render_params(seed=1, sample_offset=base)
     for _ in range(1):
         s2 = ctx.upload(host)
-        s2.set_tuning(kernel=args.kernel, track_share=args.track_share)
+        if args.kernel >= 0:
+            s2.set_tuning(kernel=args.kernel, track_share=args.track_share)
         s2.render(pe, out=out_host)
         s2.close()
     d.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         s2 = ctx.upload(host)
-        s2.set_tuning(kernel=args.kernel, track_share=args.track_share)
+        if args.kernel >= 0:
+            s2.set_tuning(kernel=args.kernel, track_share=args.track_share)
         s2.render(pe, out=out_host)
         s2.close()
     e2e_s = time.perf_counter() - t0
@@ -325,7 +333,8 @@ def main():
     achieved = alg_bytes / (k_ms / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": peak_kind, "traffic": None,
-                "kernel": "k_sched (regrouped path kernel)" if args.kernel == 1 else "k_paths (straight path kernel)",
+                "kernel": {0: "k_paths (straight path kernel)", 1: "k_sched (regrouped path kernel)",
+                           2: "k_lanes (lane-refill path kernel)"}.get(scene.tuning()["kernel"]),
                 "algorithmic_bytes_per_launch": alg_bytes,
                 "bytes_rule": "32 B per density lookup + 32 B per BVH node visit + 36 B per triangle test",
                 "density_lookups_per_launch": lookups, "scene_queries_per_launch": cstats["scene_queries"],
@@ -344,7 +353,7 @@ def main():
             cpu = cpu_baseline(host, spp, args.cpu_seconds, os.cpu_count() or 1)
         line = {"metric": METRIC, "value": value, "unit": "Mpaths/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded fBm grid)",
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
                 "config": {"workload": WORKLOAD, "paths_per_step": paths_per_step, "pixels": [W, H], "spp": spp,
                            "bounces": host.bounces, "l2": "flushed between steps (256 MiB write, outside events)",
                            "parallelism": f"{world} GPU(s), sample ranges per rank",

@@ -67,6 +67,8 @@ typedef struct ne_hit {
 #define NE_RENDER_REF_TILES (1u << 1)    /* render only the 40x10 tile grid the reference covers */
 #define NE_RENDER_COUNT_WORK (1u << 2)   /* count density lookups and scene queries (slower) */
 #define NE_RENDER_NO_SYNC (1u << 3)      /* return after enqueueing; stats carry no timings */
+#define NE_RENDER_DROP_NONFINITE (1u << 4) /* ne_render_accumulate: skip paths whose radiance is
+                                              not finite (counted in dropped_paths) */
 
 typedef struct ne_render_params {
   uint64_t seed;
@@ -87,7 +89,7 @@ typedef struct ne_render_stats {
   uint64_t bvh_nodes;         /* BVH nodes visited (NE_RENDER_COUNT_WORK) */
   uint64_t prim_tests;        /* ray-triangle tests (NE_RENDER_COUNT_WORK) */
   uint32_t kernel_launches;   /* kernels this call launched */
-  uint32_t pad;
+  uint32_t dropped_paths;     /* paths skipped by NE_RENDER_DROP_NONFINITE */
 } ne_render_stats;
 
 /* ---- host-side scene description (no GPU needed) ---- */
@@ -186,6 +188,38 @@ ne_status ne_debug_fmath(ne_context* ctx, int fn, const float* x, size_t n, floa
 /* Device copy of the shared counter-based generator: u01 for (seed, pixel, sample, dim). */
 ne_status ne_debug_rng(ne_context* ctx, uint64_t seed, const ne_path_key* keys, const uint32_t* dims, size_t n,
                        float* out);
+
+/* ---- learned radiance cache (no counterpart in the reference) ----
+ * A small network (features 96 -> 4 x 64 ReLU -> RGB) that predicts the radiance a medium
+ * path would still gather from a scattering vertex (position in the medium's object space,
+ * incoming direction), trained online on the integrator's own path suffixes with BF16
+ * tensor-core products and FP32 accumulation. Parameters: NE_CACHE_PARAMS floats, per layer
+ * W[out][in] then b[out] (96->64, 64->64 x3, 64->16 with output rows 0..2 = RGB). Arrays are
+ * host memory unless NE_CACHE_DEVICE_PTRS is set. A context destroys its caches with it. */
+typedef struct ne_cache ne_cache;
+#define NE_CACHE_PARAMS 19728
+#define NE_CACHE_DEVICE_PTRS (1u << 0)
+/* He-uniform initial weights from `seed`, zero biases, Adam state cleared. */
+ne_status ne_cache_create(ne_context* ctx, uint64_t seed, ne_cache** out);
+void ne_cache_destroy(ne_cache* cache);
+/* Replaces the parameters and clears the optimiser state. */
+ne_status ne_cache_set_params(ne_cache* cache, const float* params);
+ne_status ne_cache_get_params(ne_cache* cache, float* params);
+/* The 96 input features of n queries (pos: n*3 object-space positions, dirs: n*3 unit). */
+ne_status ne_cache_encode(ne_cache* cache, const float* pos, const float* dirs, size_t n, float* feats);
+/* Raw network outputs (n*3). Queries as pos/dirs, or as precomputed features (n*96). */
+ne_status ne_cache_infer(ne_cache* cache, const float* pos, const float* dirs, const float* feats, size_t n,
+                         float* rgb, uint32_t flags);
+/* One training step on n samples (targets n*3): forward, relative-L2 loss, backward, and
+ * with apply != 0 an Adam step (lr 1e-2, betas 0.9/0.99). loss (optional) receives the mean
+ * loss, grads (optional, NE_CACHE_PARAMS) the summed gradient. */
+ne_status ne_cache_train(ne_cache* cache, const float* pos, const float* dirs, const float* feats,
+                         const float* targets, size_t n, int apply, float* loss, float* grads, uint32_t flags);
+
+/* One 128 x n x k tensor-core product D = A * B^T (BF16 bit patterns, row-major A[128][k],
+ * B[n][k]; FP32 D[128][n]) through the same shared-memory and tensor-memory conventions as
+ * the radiance-cache kernels. n in 16..256 step 16, k in 16..128 step 16. */
+ne_status ne_debug_mma(ne_context* ctx, const uint16_t* a, const uint16_t* b, int n, int k, float* d);
 
 #ifdef __cplusplus
 }

@@ -19,7 +19,8 @@ import weakref
 import numpy as np
 
 from . import _abi
-from ._abi import (NE_RENDER_COUNT_WORK, NE_RENDER_NO_SYNC, NE_RENDER_OUT_DEVICE, NE_RENDER_REF_TILES,
+from ._abi import (NE_RENDER_COUNT_WORK, NE_RENDER_DROP_NONFINITE, NE_RENDER_NO_SYNC, NE_RENDER_OUT_DEVICE,
+                   NE_RENDER_REF_TILES,
                    NeHit, NePathKey, NeRay, NeRenderParams, NeRenderStats)
 
 PKG_DIR = os.path.dirname(os.path.abspath(__file__))
@@ -142,6 +143,7 @@ class Context:
         if st != 0:
             raise NarvalError(st, "ne_context_create failed (no CUDA device?)")
         self._h = h
+        self.device = device
         self._scenes = weakref.WeakSet()
 
     def error(self) -> str:
@@ -222,16 +224,22 @@ class Scene:
             ptr = _ptr(img)
         stats = NeRenderStats()
         self.ctx.check(library().ne_render(self._h, C.byref(p), ptr, C.byref(stats)))
-        return img, {f: getattr(stats, f) for f, _ in NeRenderStats._fields_ if f != "pad"}
+        return img, {f: getattr(stats, f) for f, _ in NeRenderStats._fields_ }
 
-    def accumulate(self, accum: np.ndarray, params: NeRenderParams | None = None, **kw) -> dict:
-        """Adds samples to an FP64 (H, W, 3) accumulator (ne_render_accumulate)."""
+    def accumulate(self, accum, params: NeRenderParams | None = None, **kw) -> dict:
+        """Adds samples to an FP64 (H, W, 3) accumulator (ne_render_accumulate): a host
+        float64 array, or with NE_RENDER_OUT_DEVICE in the flags a device pointer (int)."""
         p = params if params is not None else render_params(**kw)
-        if accum.dtype != np.float64 or not accum.flags.c_contiguous or accum.size != self.host.width * self.host.height * 3:
-            raise ValueError("accum must be a C-contiguous float64 array of width*height*3 values")
+        if p.flags & NE_RENDER_OUT_DEVICE:
+            ptr = C.c_void_p(int(accum))
+        else:
+            if (not isinstance(accum, np.ndarray) or accum.dtype != np.float64 or not accum.flags.c_contiguous
+                    or accum.size != self.host.width * self.host.height * 3):
+                raise ValueError("accum must be a C-contiguous float64 array of width*height*3 values")
+            ptr = _ptr(accum)
         stats = NeRenderStats()
-        self.ctx.check(library().ne_render_accumulate(self._h, C.byref(p), _ptr(accum), C.byref(stats)))
-        return {f: getattr(stats, f) for f, _ in NeRenderStats._fields_ if f != "pad"}
+        self.ctx.check(library().ne_render_accumulate(self._h, C.byref(p), ptr, C.byref(stats)))
+        return {f: getattr(stats, f) for f, _ in NeRenderStats._fields_ }
 
     def set_tuning(self, kernel: int = 0, track_share: int = 16, blocks_per_sm: int = 0):
         """Launch configuration of the path kernels (see ne_tuning in include/narval_gb300.h)."""
@@ -291,6 +299,64 @@ def hits_to_numpy(arr) -> np.ndarray:
 
 
 # ---------------------------------------------------------------- output stage
+class RadianceCache:
+    """The learned radiance cache (ne_cache): a 96 -> 4x64 -> RGB network on the tensor cores."""
+
+    N_PARAMS = 19728
+
+    def __init__(self, ctx: Context, seed: int = 0):
+        self.ctx = ctx
+        h = C.c_void_p()
+        ctx.check(library().ne_cache_create(ctx._h, seed, C.byref(h)))
+        self._h = h
+
+    def set_params(self, params: np.ndarray):
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        if p.size != self.N_PARAMS:
+            raise ValueError(f"expected {self.N_PARAMS} parameters")
+        self.ctx.check(library().ne_cache_set_params(self._h, _ptr(p)))
+
+    def params(self) -> np.ndarray:
+        p = np.empty(self.N_PARAMS, np.float32)
+        self.ctx.check(library().ne_cache_get_params(self._h, _ptr(p)))
+        return p
+
+    def encode(self, pos: np.ndarray, dirs: np.ndarray) -> np.ndarray:
+        pos = np.ascontiguousarray(pos, np.float32)
+        dirs = np.ascontiguousarray(dirs, np.float32)
+        f = np.empty((len(pos), 96), np.float32)
+        self.ctx.check(library().ne_cache_encode(self._h, _ptr(pos), _ptr(dirs), len(pos), _ptr(f)))
+        return f
+
+    def infer(self, pos=None, dirs=None, feats=None) -> np.ndarray:
+        args, n = self._inputs(pos, dirs, feats)
+        out = np.empty((n, 3), np.float32)
+        self.ctx.check(library().ne_cache_infer(self._h, *args, n, _ptr(out), 0))
+        return out
+
+    def train(self, targets, pos=None, dirs=None, feats=None, apply: bool = True, want_grads: bool = False):
+        """One training step; returns (mean loss, summed gradient or None)."""
+        args, n = self._inputs(pos, dirs, feats)
+        t = np.ascontiguousarray(targets, np.float32)
+        loss = C.c_float()
+        g = np.empty(self.N_PARAMS, np.float32) if want_grads else None
+        self.ctx.check(library().ne_cache_train(self._h, *args, _ptr(t), n, int(apply), C.byref(loss),
+                                                _ptr(g) if g is not None else None, 0))
+        return loss.value, g
+
+    def _inputs(self, pos, dirs, feats):
+        if feats is not None:
+            self._keep = np.ascontiguousarray(feats, np.float32)
+            return (None, None, _ptr(self._keep)), len(self._keep)
+        self._keep = (np.ascontiguousarray(pos, np.float32), np.ascontiguousarray(dirs, np.float32))
+        return (_ptr(self._keep[0]), _ptr(self._keep[1]), None), len(self._keep[0])
+
+    def close(self):
+        if self._h and self.ctx._h:
+            library().ne_cache_destroy(self._h)
+        self._h = None
+
+
 def tone_map(hdr: np.ndarray) -> np.ndarray:
     """OfflineEngine::postProcessing (core/OfflineEngine.cpp:39-52): exposure 0.5, gamma 2.2, clamp."""
     mapped = np.float32(1.0) - np.exp(-hdr.astype(np.float32) * np.float32(0.5))

@@ -85,7 +85,7 @@ class NeTuning(C.Structure):
 class NeRenderStats(C.Structure):
     _fields_ = [("kernel_ms", C.c_double), ("total_ms", C.c_double), ("paths", C.c_uint64),
                 ("density_lookups", C.c_uint64), ("scene_queries", C.c_uint64), ("bvh_nodes", C.c_uint64),
-                ("prim_tests", C.c_uint64), ("kernel_launches", C.c_uint32), ("pad", C.c_uint32)]
+                ("prim_tests", C.c_uint64), ("kernel_launches", C.c_uint32), ("dropped_paths", C.c_uint32)]
 
 
 # status codes
@@ -104,6 +104,7 @@ NE_RENDER_OUT_DEVICE = 1 << 0
 NE_RENDER_REF_TILES = 1 << 1
 NE_RENDER_COUNT_WORK = 1 << 2
 NE_RENDER_NO_SYNC = 1 << 3
+NE_RENDER_DROP_NONFINITE = 1 << 4
 
 # every symbol include/narval_gb300.h declares, with its ctypes signature
 SIGNATURES = {
@@ -133,4 +134,14 @@ SIGNATURES = {
     "ne_context_flush_l2": (C.c_int32, [C.c_void_p, C.c_size_t]),
     "ne_debug_fmath": (C.c_int32, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t, C.c_void_p]),
     "ne_debug_rng": (C.c_int32, [C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
+    "ne_cache_create": (C.c_int32, [C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p)]),
+    "ne_cache_destroy": (None, [C.c_void_p]),
+    "ne_cache_set_params": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "ne_cache_get_params": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "ne_cache_encode": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
+    "ne_cache_infer": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p,
+                                   C.c_uint32]),
+    "ne_cache_train": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_int,
+                                   C.c_void_p, C.c_void_p, C.c_uint32]),
+    "ne_debug_mma": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
 }

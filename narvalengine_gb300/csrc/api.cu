@@ -22,6 +22,7 @@
 
 #include "narval_gb300.h"
 #include "kernels.cuh"
+#include "mlp.h"
 
 using namespace nedev;
 
@@ -37,6 +38,26 @@ struct ne_context {
   unsigned long long* d_counter = nullptr;  // [0] work counter, [1..4] work counters
   uint32_t* d_err = nullptr;
   std::vector<ne_scene*> scenes;            // live scenes, destroyed with the context
+  std::vector<ne_cache*> caches;            // live radiance caches, destroyed with the context
+};
+
+struct ne_cache {
+  ne_context* ctx = nullptr;
+  float* P = nullptr;        // FP32 master parameters
+  float* m = nullptr;        // Adam moments
+  float* v = nullptr;
+  uint8_t* wfwd = nullptr;   // packed BF16 tiles
+  uint8_t* wbwd = nullptr;
+  float* bias = nullptr;
+  float* part = nullptr;     // per-block partial gradients
+  int part_blocks = 0;
+  float* loss_part = nullptr;
+  float* d_loss = nullptr;
+  float* grad = nullptr;
+  uint16_t* acts = nullptr;  // training activations
+  float* out = nullptr;      // training outputs
+  size_t cap = 0;
+  int step = 0;
 };
 
 struct ne_scene {
@@ -228,18 +249,26 @@ __global__ void k_reduce(const float* __restrict__ paths, uint32_t n_pix, uint32
   }
 }
 
-// FP64 accumulation of per-path radiance, samples in order.
+// FP64 accumulation of per-path radiance, samples in order. With `drop`, a path whose
+// radiance has a non-finite channel is skipped and counted in *dropped.
 __global__ void k_accum(const float* __restrict__ paths, uint32_t n_pix, uint32_t spp, uint32_t cover_w, int W,
-                        double* __restrict__ acc) {
+                        double* __restrict__ acc, int drop, unsigned long long* dropped) {
   for (uint32_t pi = blockIdx.x * blockDim.x + threadIdx.x; pi < n_pix; pi += gridDim.x * blockDim.x) {
     const float* p = paths + (size_t)pi * spp * 3;
     size_t pixel = (size_t)(pi / cover_w) * (size_t)W + (pi % cover_w);
     double r = acc[3 * pixel + 0], g = acc[3 * pixel + 1], b = acc[3 * pixel + 2];
+    unsigned long long nd = 0;
     for (uint32_t k = 0; k < spp; k++) {
-      r += (double)p[3 * k + 0];
-      g += (double)p[3 * k + 1];
-      b += (double)p[3 * k + 2];
+      float x = p[3 * k + 0], y = p[3 * k + 1], z = p[3 * k + 2];
+      if (drop && !(isfinite(x) && isfinite(y) && isfinite(z))) {
+        nd++;
+        continue;
+      }
+      r += (double)x;
+      g += (double)y;
+      b += (double)z;
     }
+    if (nd) atomicAdd(dropped, nd);
     acc[3 * pixel + 0] = r;
     acc[3 * pixel + 1] = g;
     acc[3 * pixel + 2] = b;
@@ -413,6 +442,73 @@ ne_status noallocScratch(ne_context* ctx, unsigned char** out) {
 
 }  // namespace
 
+// ---------------------------------------------------------------- radiance cache
+namespace {
+
+uint64_t splitmix64(uint64_t& s) {
+  uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+// He-uniform initial weights (bound sqrt(6 / fan_in)), zero biases; the unused output rows
+// 3..15 and input columns 88..95 stay zero.
+void cacheInitParams(uint64_t seed, std::vector<float>& P) {
+  static const int in[5] = {96, 64, 64, 64, 64}, out[5] = {64, 64, 64, 64, 16};
+  P.assign(kNeMlpParams, 0.0f);
+  uint64_t s = seed;
+  size_t off = 0;
+  for (int l = 0; l < 5; l++) {
+    float bound = (float)sqrt(6.0 / in[l]);
+    for (int o = 0; o < out[l]; o++)
+      for (int k = 0; k < in[l]; k++) {
+        float u = (float)((splitmix64(s) >> 40) * (1.0 / 16777216.0));
+        bool used = !(l == 4 && o >= 3) && !(l == 0 && k >= 88);
+        P[off + (size_t)o * in[l] + k] = used ? (2.0f * u - 1.0f) * bound : 0.0f;
+      }
+    off += (size_t)in[l] * out[l] + out[l];
+  }
+}
+
+ne_status cacheUpload(ne_cache* c, const float* host) {
+  ne_context* ctx = c->ctx;
+  NE_CUDA(cudaMemcpyAsync(c->P, host, kNeMlpParams * 4, cudaMemcpyHostToDevice, ctx->stream), "cudaMemcpyAsync");
+  NE_CUDA(cudaMemsetAsync(c->m, 0, kNeMlpParams * 4, ctx->stream), "cudaMemsetAsync");
+  NE_CUDA(cudaMemsetAsync(c->v, 0, kNeMlpParams * 4, ctx->stream), "cudaMemsetAsync");
+  NE_CUDA(cudaMemsetAsync(c->wfwd, 0, kNeMlpFwdBytes, ctx->stream), "cudaMemsetAsync");
+  NE_CUDA(cudaMemsetAsync(c->wbwd, 0, kNeMlpBwdBytes, ctx->stream), "cudaMemsetAsync");
+  NE_CUDA(ne_mlp_pack(ctx->stream, c->P, c->wfwd, c->wbwd, c->bias), "k_mlp_pack launch");
+  NE_CUDA(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  c->step = 0;
+  return NE_OK;
+}
+
+// Device view of a caller array: the pointer itself with NE_CACHE_DEVICE_PTRS, else a copy.
+template <class T>
+ne_status stageIn(ne_context* ctx, const T* src, size_t n, bool dev, DevBuf<T>& tmp, const T** out) {
+  *out = nullptr;
+  if (!src) return NE_OK;
+  if (dev) {
+    *out = src;
+    return NE_OK;
+  }
+  NE_CUDA(cudaMalloc(&tmp.p, n * sizeof(T)), "cudaMalloc");
+  NE_CUDA(cudaMemcpyAsync(tmp.p, src, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream), "cudaMemcpyAsync");
+  *out = tmp.p;
+  return NE_OK;
+}
+
+ne_status cacheErr(ne_context* ctx) {
+  uint32_t e = 0;
+  NE_CUDA(cudaMemcpyAsync(&e, ctx->d_err, 4, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync(err)");
+  NE_CUDA(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  if (e & 6u) return fail(ctx, NE_ERR_TIMEOUT, "radiance cache: a tensor-core product did not complete");
+  return NE_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 ne_status ne_context_create(int device, ne_context** out) {
@@ -454,6 +550,7 @@ ne_status ne_context_create(int device, ne_context** out) {
 void ne_context_destroy(ne_context* ctx) {
   if (!ctx) return;
   while (!ctx->scenes.empty()) ne_scene_destroy(ctx->scenes.back());
+  while (!ctx->caches.empty()) ne_cache_destroy(ctx->caches.back());
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (int i = 0; i < 4; i++)
@@ -716,7 +813,9 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
   sc->features = F;
   sc->feature_set = ne_feature_set_for(F);
   ne_tuning tn;
-  tn.kernel = sc->variant;
+  // surface-only scenes run fastest with lane refill (Cornell box: 235 vs 210 Mpaths/s); media
+  // and meshes with the straight kernel (mesh scene: 127 vs 50)
+  tn.kernel = sc->feature_set == K_SURFACE ? 2 : 0;
   tn.track_share = sc->track_share;
   tn.blocks_per_sm = 0;
   tn.pad = 0;
@@ -892,10 +991,13 @@ ne_status ne_render_accumulate(ne_scene* sc, const ne_render_params* p, double* 
   if (st) return st;
   NE_CUDA(cudaEventRecord(ctx->ev[2], ctx->stream), "cudaEventRecord");
   int rblocks = (int)std::min<uint64_t>((npix + 255) / 256, (uint64_t)ctx->sm_count * 16);
-  k_accum<<<std::max(1, rblocks), 256, 0, ctx->stream>>>(sc->d_paths, (uint32_t)npix, (uint32_t)spp, cw, W, d_acc);
+  NE_CUDA(cudaMemsetAsync(ctx->d_counter + 5, 0, sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync");
+  k_accum<<<std::max(1, rblocks), 256, 0, ctx->stream>>>(sc->d_paths, (uint32_t)npix, (uint32_t)spp, cw, W, d_acc,
+                                                         (flags & NE_RENDER_DROP_NONFINITE) ? 1 : 0,
+                                                         ctx->d_counter + 5);
   NE_CUDA(cudaGetLastError(), "k_accum launch");
   if (!devAcc) NE_CUDA(cudaMemcpyAsync(accum, d_acc, accBytes, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync");
-  unsigned long long cnt[5] = {0, 0, 0, 0, 0};
+  unsigned long long cnt[6] = {0, 0, 0, 0, 0, 0};
   NE_CUDA(cudaMemcpyAsync(cnt, ctx->d_counter, sizeof(cnt), cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync");
   st = checkErr(ctx);
   if (st) return st;
@@ -910,6 +1012,7 @@ ne_status ne_render_accumulate(ne_scene* sc, const ne_render_params* p, double* 
     stats->bvh_nodes = cnt[3];
     stats->prim_tests = cnt[4];
     stats->kernel_launches = 2;
+    stats->dropped_paths = (uint32_t)std::min<unsigned long long>(cnt[5], 0xFFFFFFFFull);
   }
   return NE_OK;
 }
@@ -1134,6 +1237,195 @@ ne_status ne_render_noalloc(ne_scene* sc, const ne_render_params* p, float* out_
     stats->prim_tests = cnt[4];
     stats->kernel_launches = 2;
   }
+  return NE_OK;
+}
+
+ne_status ne_debug_mma(ne_context* ctx, const uint16_t* a, const uint16_t* b, int n, int k, float* d) {
+  if (!ctx || !a || !b || !d) return NE_ERR_INVALID_ARG;
+  if (n < 16 || n > 256 || n % 16 || k < 16 || k > 128 || k % 16)
+    return fail(ctx, NE_ERR_INVALID_ARG, "ne_debug_mma: n must be 16..256 and k 16..128, multiples of 16");
+  NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  DevBuf<uint16_t> da, db;
+  DevBuf<float> dd;
+  NE_CUDA(cudaMalloc(&da.p, (size_t)128 * k * 2), "cudaMalloc");
+  NE_CUDA(cudaMalloc(&db.p, (size_t)n * k * 2), "cudaMalloc");
+  NE_CUDA(cudaMalloc(&dd.p, (size_t)128 * n * 4), "cudaMalloc");
+  NE_CUDA(cudaMemcpyAsync(da.p, a, (size_t)128 * k * 2, cudaMemcpyHostToDevice, ctx->stream), "cudaMemcpyAsync");
+  NE_CUDA(cudaMemcpyAsync(db.p, b, (size_t)n * k * 2, cudaMemcpyHostToDevice, ctx->stream), "cudaMemcpyAsync");
+  NE_CUDA(cudaMemsetAsync(ctx->d_err, 0, 4, ctx->stream), "cudaMemsetAsync");
+  NE_CUDA(ne_launch_debug_mma(ctx->stream, da.p, db.p, n, k, dd.p, ctx->d_err), "k_debug_mma launch");
+  NE_CUDA(cudaMemcpyAsync(d, dd.p, (size_t)128 * n * 4, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync");
+  uint32_t e = 0;
+  NE_CUDA(cudaMemcpyAsync(&e, ctx->d_err, 4, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync");
+  NE_CUDA(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  if (e) return fail(ctx, NE_ERR_TIMEOUT, "tensor-core product did not complete");
+  return NE_OK;
+}
+
+
+ne_status ne_cache_create(ne_context* ctx, uint64_t seed, ne_cache** out) {
+  if (!ctx || !out) return NE_ERR_INVALID_ARG;
+  *out = nullptr;
+  NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  ne_cache* c = new ne_cache();
+  c->ctx = ctx;
+  cudaError_t e = cudaSuccess;
+  if (e == cudaSuccess) e = cudaMalloc(&c->P, kNeMlpParams * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&c->m, kNeMlpParams * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&c->v, kNeMlpParams * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&c->wfwd, kNeMlpFwdBytes);
+  if (e == cudaSuccess) e = cudaMalloc(&c->wbwd, kNeMlpBwdBytes);
+  if (e == cudaSuccess) e = cudaMalloc(&c->bias, kNeMlpBiasFloats * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&c->d_loss, 4);
+  if (e == cudaSuccess) e = cudaMalloc(&c->grad, kNeMlpParams * 4);
+  ctx->caches.push_back(c);
+  if (e != cudaSuccess) {
+    ne_cache_destroy(c);
+    return fail(ctx, NE_ERR_OUT_OF_MEMORY, std::string("radiance cache: ") + cudaGetErrorString(e));
+  }
+  std::vector<float> P;
+  cacheInitParams(seed, P);
+  ne_status st = cacheUpload(c, P.data());
+  if (st) {
+    ne_cache_destroy(c);
+    return st;
+  }
+  *out = c;
+  return NE_OK;
+}
+
+void ne_cache_destroy(ne_cache* c) {
+  if (!c) return;
+  auto& v = c->ctx->caches;
+  v.erase(std::remove(v.begin(), v.end(), c), v.end());
+  cudaSetDevice(c->ctx->device);
+  cudaStreamSynchronize(c->ctx->stream);
+  void* bufs[] = {c->P, c->m, c->v, c->wfwd, c->wbwd, c->bias, c->part, c->loss_part, c->d_loss, c->grad, c->acts,
+                  c->out};
+  for (void* p : bufs)
+    if (p) cudaFree(p);
+  delete c;
+}
+
+ne_status ne_cache_set_params(ne_cache* c, const float* params) {
+  if (!c || !params) return NE_ERR_INVALID_ARG;
+  ne_context* ctx = c->ctx;
+  NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  return cacheUpload(c, params);
+}
+
+ne_status ne_cache_get_params(ne_cache* c, float* params) {
+  if (!c || !params) return NE_ERR_INVALID_ARG;
+  ne_context* ctx = c->ctx;
+  NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  NE_CUDA(cudaMemcpyAsync(params, c->P, kNeMlpParams * 4, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync");
+  NE_CUDA(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  return NE_OK;
+}
+
+ne_status ne_cache_encode(ne_cache* c, const float* pos, const float* dirs, size_t n, float* feats) {
+  if (!c || (n && (!pos || !dirs || !feats))) return NE_ERR_INVALID_ARG;
+  if (n == 0) return NE_OK;
+  ne_context* ctx = c->ctx;
+  NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  DevBuf<float> tp, td, tf;
+  const float *dp, *dd;
+  ne_status st = stageIn(ctx, pos, n * 3, false, tp, &dp);
+  if (!st) st = stageIn(ctx, dirs, n * 3, false, td, &dd);
+  if (st) return st;
+  NE_CUDA(cudaMalloc(&tf.p, n * 96 * 4), "cudaMalloc");
+  NE_CUDA(ne_mlp_encode(ctx->stream, dp, dd, (uint32_t)n, tf.p), "k_mlp_encode launch");
+  NE_CUDA(cudaMemcpyAsync(feats, tf.p, n * 96 * 4, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync");
+  NE_CUDA(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  return NE_OK;
+}
+
+ne_status ne_cache_infer(ne_cache* c, const float* pos, const float* dirs, const float* feats, size_t n, float* rgb,
+                         uint32_t flags) {
+  if (!c || !rgb || (n && !feats && (!pos || !dirs))) return NE_ERR_INVALID_ARG;
+  if (n == 0) return NE_OK;
+  if (n > 0xFFFFFF80u) return fail(c->ctx, NE_ERR_INVALID_ARG, "radiance cache: too many queries");
+  ne_context* ctx = c->ctx;
+  NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  bool dev = flags & NE_CACHE_DEVICE_PTRS;
+  DevBuf<float> tp, td, tf, to;
+  const float *dp = nullptr, *dd = nullptr, *df = nullptr;
+  ne_status st = NE_OK;
+  if (feats) st = stageIn(ctx, feats, n * 96, dev, tf, &df);
+  else {
+    st = stageIn(ctx, pos, n * 3, dev, tp, &dp);
+    if (!st) st = stageIn(ctx, dirs, n * 3, dev, td, &dd);
+  }
+  if (st) return st;
+  float* dout = rgb;
+  if (!dev) {
+    NE_CUDA(cudaMalloc(&to.p, n * 3 * 4), "cudaMalloc");
+    dout = to.p;
+  }
+  NE_CUDA(cudaMemsetAsync(ctx->d_err, 0, 4, ctx->stream), "cudaMemsetAsync");
+  NeMlpForward f = {dp, dd, df, (uint32_t)n, c->wfwd, c->bias, dout, nullptr, nullptr, nullptr, nullptr};
+  NE_CUDA(ne_mlp_forward(ctx->stream, f, ctx->d_err), "k_mlp_forward launch");
+  if (!dev) NE_CUDA(cudaMemcpyAsync(rgb, dout, n * 3 * 4, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync");
+  return cacheErr(ctx);
+}
+
+ne_status ne_cache_train(ne_cache* c, const float* pos, const float* dirs, const float* feats, const float* targets,
+                         size_t n, int apply, float* loss, float* grads, uint32_t flags) {
+  if (!c || !targets || n == 0 || (!feats && (!pos || !dirs))) return NE_ERR_INVALID_ARG;
+  if (n > (1u << 24)) return fail(c->ctx, NE_ERR_INVALID_ARG, "radiance cache: at most 2^24 samples per step");
+  ne_context* ctx = c->ctx;
+  NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  bool dev = flags & NE_CACHE_DEVICE_PTRS;
+  DevBuf<float> tp, td, tf, tt;
+  const float *dp = nullptr, *dd = nullptr, *df = nullptr, *dt = nullptr;
+  ne_status st = NE_OK;
+  if (feats) st = stageIn(ctx, feats, n * 96, dev, tf, &df);
+  else {
+    st = stageIn(ctx, pos, n * 3, dev, tp, &dp);
+    if (!st) st = stageIn(ctx, dirs, n * 3, dev, td, &dd);
+  }
+  if (!st) st = stageIn(ctx, targets, n * 3, dev, tt, &dt);
+  if (st) return st;
+  if (c->cap < n) {
+    if (c->acts) cudaFree(c->acts);
+    if (c->out) cudaFree(c->out);
+    c->acts = nullptr;
+    c->out = nullptr;
+    c->cap = 0;
+    NE_CUDA(cudaMalloc(&c->acts, n * kNeMlpActRow * 2), "cudaMalloc(activations)");
+    NE_CUDA(cudaMalloc(&c->out, n * 3 * 4), "cudaMalloc(outputs)");
+    c->cap = n;
+  }
+  int blocks = ne_mlp_backward_blocks((uint32_t)n);
+  if (c->part_blocks < blocks) {
+    if (c->part) cudaFree(c->part);
+    if (c->loss_part) cudaFree(c->loss_part);
+    c->part = nullptr;
+    c->loss_part = nullptr;
+    c->part_blocks = 0;
+    NE_CUDA(cudaMalloc(&c->part, (size_t)blocks * kNeMlpParams * 4), "cudaMalloc(partial gradients)");
+    NE_CUDA(cudaMalloc(&c->loss_part, (size_t)blocks * 4), "cudaMalloc");
+    c->part_blocks = blocks;
+  }
+  NE_CUDA(cudaMemsetAsync(ctx->d_err, 0, 4, ctx->stream), "cudaMemsetAsync");
+  NeMlpForward f = {dp, dd, df, (uint32_t)n, c->wfwd, c->bias, c->out, c->acts, nullptr, nullptr, nullptr};
+  NE_CUDA(ne_mlp_forward(ctx->stream, f, ctx->d_err), "k_mlp_forward launch");
+  NeMlpBackward b = {c->acts, c->out, dt, (uint32_t)n, c->wbwd, c->part, c->loss_part};
+  NE_CUDA(ne_mlp_backward(ctx->stream, b, ctx->d_err), "k_mlp_backward launch");
+  if (apply) c->step++;
+  NE_CUDA(ne_mlp_adam(ctx->stream, c->P, c->m, c->v, c->part, blocks, c->loss_part, grads ? c->grad : nullptr,
+                      c->d_loss, 1e-2f, apply ? c->step : 1, apply),
+          "k_mlp_adam launch");
+  if (apply) NE_CUDA(ne_mlp_pack(ctx->stream, c->P, c->wfwd, c->wbwd, c->bias), "k_mlp_pack launch");
+  float lsum = 0;
+  NE_CUDA(cudaMemcpyAsync(&lsum, c->d_loss, 4, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync");
+  if (grads)
+    NE_CUDA(cudaMemcpyAsync(grads, c->grad, kNeMlpParams * 4, dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                            ctx->stream),
+            "cudaMemcpyAsync");
+  st = cacheErr(ctx);
+  if (st) return st;
+  if (loss) *loss = lsum / (3.0f * (float)n);
   return NE_OK;
 }
 

@@ -16,6 +16,15 @@
 namespace nedev {
 
 constexpr int kThreads = 128;
+// Resident blocks per SM the straight and lane-refill kernels are compiled for: 10 x 128
+// threads caps them at 48 registers. The spills this costs are cheaper than the
+// instruction-fetch and latency stalls that fewer resident warps leave exposed. Measured
+// (Mpaths/s, medium / mesh scene): uncapped 123 registers 339 / 113, 8 blocks 383 / 127,
+// 10 blocks 397 / 139, 12 blocks 393 / 127.
+#ifndef NE_PATH_MIN_BLOCKS
+#define NE_PATH_MIN_BLOCKS 10
+#endif
+constexpr int kPathMinBlocks = NE_PATH_MIN_BLOCKS;
 
 struct PathArgs {
   PathParams P;
@@ -49,7 +58,7 @@ __device__ __forceinline__ void flushCounters(const Counters& cn, unsigned long 
 }
 
 template <uint32_t K>
-__global__ void __launch_bounds__(kThreads) k_paths(const __grid_constant__ DScene s, const PathArgs a,
+__global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_paths(const __grid_constant__ DScene s, const PathArgs a,
                                                     unsigned long long* __restrict__ counter, uint32_t* err) {
   Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err};
   const int lane = threadIdx.x & 31;
@@ -83,7 +92,7 @@ __global__ void __launch_bounds__(kThreads) k_paths(const __grid_constant__ DSce
 // work item at once, together with whichever lanes finish at the same time (coalesced-group
 // atomic), instead of waiting for the longest path of its warp.
 template <uint32_t K>
-__global__ void __launch_bounds__(kThreads) k_lanes(const __grid_constant__ DScene s, const PathArgs a,
+__global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_lanes(const __grid_constant__ DScene s, const PathArgs a,
                                                     unsigned long long* __restrict__ counter, uint32_t* err) {
   namespace cg = cooperative_groups;
   Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err};
