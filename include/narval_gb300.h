@@ -216,6 +216,29 @@ ne_status ne_cache_infer(ne_cache* cache, const float* pos, const float* dirs, c
 ne_status ne_cache_train(ne_cache* cache, const float* pos, const float* dirs, const float* feats,
                          const float* targets, size_t n, int apply, float* loss, float* grads, uint32_t flags);
 
+/* Rendering with the cache: paths reaching a scattering vertex in a grid medium at or
+ * after `bounce` stop there and add throughput x cache(vertex); one path in train_stride
+ * (hashed over the path index) runs to the end instead, contributes its full radiance, and
+ * records the radiance it gathered after that vertex as a training sample. After the image
+ * is formed the cache takes train_steps optimiser steps on the frame's samples. */
+typedef struct ne_cache_render_params {
+  int32_t bounce;         /* 2: paths end at their third scattering event */
+  uint32_t train_stride;  /* 0: no training paths */
+  int32_t train_steps;
+  uint32_t train_batch;   /* samples per optimiser step; 0: all of the frame's samples */
+} ne_cache_render_params;
+typedef struct ne_cache_render_stats {
+  uint64_t queries;        /* paths that ended in the cache */
+  uint64_t train_samples;  /* training samples recorded this frame */
+  float loss;              /* mean loss of the last optimiser step (0 without training) */
+  float path_ms, infer_ms, train_ms;
+} ne_cache_render_stats;
+/* As ne_render (same flags, output and stats) for scenes whose media are grid media;
+ * NE_ERR_UNSUPPORTED for other scenes. */
+ne_status ne_render_cached(ne_scene* scene, ne_cache* cache, const ne_render_params* params,
+                           const ne_cache_render_params* cache_params, float* out_rgb, ne_render_stats* stats,
+                           ne_cache_render_stats* cache_stats);
+
 /* One 128 x n x k tensor-core product D = A * B^T (BF16 bit patterns, row-major A[128][k],
  * B[n][k]; FP32 D[128][n]) through the same shared-memory and tensor-memory conventions as
  * the radiance-cache kernels. n in 16..256 step 16, k in 16..128 step 16. */

@@ -241,6 +241,27 @@ class Scene:
         self.ctx.check(library().ne_render_accumulate(self._h, C.byref(p), ptr, C.byref(stats)))
         return {f: getattr(stats, f) for f, _ in NeRenderStats._fields_ }
 
+    def render_cached(self, cache: "RadianceCache", bounce: int = 2, train_stride: int = 0, train_steps: int = 0,
+                      train_batch: int = 0, params: NeRenderParams | None = None, out=None, **kw):
+        """ne_render_cached: (image or None, render stats, cache stats)."""
+        p = params if params is not None else render_params(**kw)
+        W, H = self.host.width, self.host.height
+        if p.flags & NE_RENDER_OUT_DEVICE:
+            if out is None:
+                raise ValueError("NE_RENDER_OUT_DEVICE needs a device pointer in out")
+            ptr = C.c_void_p(int(out))
+            img = None
+        else:
+            img = out if out is not None else np.empty((H, W, 3), dtype=np.float32)
+            ptr = _ptr(img)
+        cp = _abi.NeCacheRenderParams(bounce, train_stride, train_steps, train_batch)
+        stats = NeRenderStats()
+        cst = _abi.NeCacheRenderStats()
+        self.ctx.check(library().ne_render_cached(self._h, cache._h, C.byref(p), C.byref(cp), ptr, C.byref(stats),
+                                                  C.byref(cst)))
+        return (img, {f: getattr(stats, f) for f, _ in NeRenderStats._fields_},
+                {f: getattr(cst, f) for f, _ in _abi.NeCacheRenderStats._fields_})
+
     def set_tuning(self, kernel: int = 0, track_share: int = 16, blocks_per_sm: int = 0):
         """Launch configuration of the path kernels (see ne_tuning in include/narval_gb300.h)."""
         t = _abi.NeTuning(kernel, track_share, blocks_per_sm, 0)

@@ -88,6 +88,16 @@ class NeRenderStats(C.Structure):
                 ("prim_tests", C.c_uint64), ("kernel_launches", C.c_uint32), ("dropped_paths", C.c_uint32)]
 
 
+class NeCacheRenderParams(C.Structure):
+    _fields_ = [("bounce", C.c_int32), ("train_stride", C.c_uint32), ("train_steps", C.c_int32),
+                ("train_batch", C.c_uint32)]
+
+
+class NeCacheRenderStats(C.Structure):
+    _fields_ = [("queries", C.c_uint64), ("train_samples", C.c_uint64), ("loss", C.c_float), ("path_ms", C.c_float),
+                ("infer_ms", C.c_float), ("train_ms", C.c_float)]
+
+
 # status codes
 NE_OK = 0
 NE_ERR_INVALID_ARG = -1
@@ -143,5 +153,8 @@ SIGNATURES = {
                                    C.c_uint32]),
     "ne_cache_train": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_int,
                                    C.c_void_p, C.c_void_p, C.c_uint32]),
+    "ne_render_cached": (C.c_int32, [C.c_void_p, C.c_void_p, C.POINTER(NeRenderParams),
+                                     C.POINTER(NeCacheRenderParams), C.c_void_p, C.POINTER(NeRenderStats),
+                                     C.POINTER(NeCacheRenderStats)]),
     "ne_debug_mma": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
 }

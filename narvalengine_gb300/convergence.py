@@ -5,9 +5,11 @@ relMSE(x, ref) = mean over pixels and channels of (x - ref)^2 / (ref^2 + 1e-2).
 The reference image is the mean of many samples per pixel, each path's radiance converted
 to FP64 and summed on the device in sample order (ne_render_accumulate), in chunks of
 samples so the per-path buffer stays bounded. It is rendered with its own seed, so its
-samples are independent of the images measured against it. The reference integrator can
-return a non-finite radiance on rare paths (a zero in a pdf denominator); those paths are
-dropped from every accumulated image and counted (`dropped_paths`).
+samples are independent of the images measured against it. The reference integrator
+returns a NaN radiance on rare medium paths (HG::sample, materials/Medium.h:109, takes
+sqrt(1 - cos^2) without clamping, which is NaN when cos rounds past +-1; about 1.3e-7 of
+the medium scene's paths); those paths are dropped from every accumulated image and
+counted (`dropped_paths`).
 
 Time-to-relMSE renders progressively, doubling the samples per pixel (1, 2, 4, ...), until
 the image's relMSE against the reference is at or below the target, and reports the
@@ -89,6 +91,37 @@ def time_to_relmse(scene, ref: np.ndarray, target: float = 1e-3, seed: int = 0, 
             "ms": hit["ms"] if hit else None, "dropped_paths": dropped[0], "curve": curve}
 
 
+def time_to_relmse_cached(scene, cache, ref: np.ndarray, target: float = 1e-3, seed: int = 0,
+                          max_spp: int = 1 << 16, frame_spp: int = 4, bounce: int = 2, train_stride: int = 16,
+                          train_steps: int = 4, train_batch: int = 1 << 16) -> dict:
+    """Progressive rendering with the radiance cache trained online: frames of `frame_spp`
+    samples, each rendered with the cache as it stands and then used for `train_steps`
+    optimiser steps on the frame's training samples. The running FP64 mean of the frames is
+    compared with the reference whenever the sample count reaches a power of two; `ms` is the
+    cumulative device time of the frames (path kernel, network inference, training)."""
+    acc = np.zeros_like(ref, dtype=np.float64)
+    curve = []
+    have, ms, check = 0, 0.0, frame_spp
+    hit = None
+    while have < max_spp:
+        img, st, cst = scene.render_cached(cache, bounce=bounce, train_stride=train_stride, train_steps=train_steps,
+                                           train_batch=train_batch, seed=seed, spp=frame_spp, sample_offset=have)
+        ms += st["total_ms"]
+        finite = np.isfinite(img)
+        acc += np.where(finite, img, 0.0) * frame_spp
+        have += frame_spp
+        if have >= check:
+            e = relmse(acc / have, ref)
+            curve.append({"spp": have, "relmse": e, "ms": ms, "loss": cst["loss"]})
+            check *= 2
+            if e <= target:
+                hit = curve[-1]
+                break
+    return {"target": target, "reached": hit is not None, "spp": hit["spp"] if hit else None,
+            "ms": hit["ms"] if hit else None, "frame_spp": frame_spp, "bounce": bounce,
+            "train_stride": train_stride, "train_steps": train_steps, "train_batch": train_batch, "curve": curve}
+
+
 def main(argv=None):
     import narvalengine_gb300 as ne
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
@@ -98,6 +131,9 @@ def main(argv=None):
     ap.add_argument("--target", type=float, default=1e-3)
     ap.add_argument("--resolution", type=int, nargs=2, default=None, help="override width height")
     ap.add_argument("--save", default=None, help="write the reference image (.npy)")
+    ap.add_argument("--cache", action="store_true", help="also measure the radiance-cache form")
+    ap.add_argument("--max-spp", type=int, default=1 << 16)
+    ap.add_argument("--frame-spp", type=int, default=4)
     args = ap.parse_args(argv)
     path = args.scene if args.scene.endswith(".json") else os.path.join(ne.SCENES_DIR, args.scene + ".json")
     if args.resolution:
@@ -113,7 +149,14 @@ def main(argv=None):
     ref, ref_ms = reference_image(scene, args.ref_spp, chunk=args.chunk, info=info)
     if args.save:
         np.save(args.save, ref)
-    res = time_to_relmse(scene, ref, args.target, chunk=args.chunk)
+    res = time_to_relmse(scene, ref, args.target, chunk=args.chunk, max_spp=args.max_spp)
+    if args.cache:
+        cache = ne.RadianceCache(ctx, seed=1)
+        res["cache"] = time_to_relmse_cached(scene, cache, ref, args.target, max_spp=args.max_spp,
+                                             frame_spp=args.frame_spp)
+        cache.close()
+        if res["reached"] and res["cache"]["reached"]:
+            res["cache_time_ratio"] = res["cache"]["ms"] / res["ms"]
     out = {"scene": os.path.basename(path), "resolution": [host.width, host.height], "ref_spp": args.ref_spp,
            "ref_paths": host.width * host.height * args.ref_spp, "ref_device_ms": ref_ms,
            "ref_wall_s": time.time() - t0, "ref_dropped_paths": info["dropped_paths"], "relmse_eps": EPS, **res}

@@ -58,6 +58,16 @@ struct ne_cache {
   float* out = nullptr;      // training outputs
   size_t cap = 0;
   int step = 0;
+  // ne_render_cached: query and training-sample buffers, counters, device copy of CacheIO
+  float* q = nullptr;        // q_cap x (pos 3, dir 3, thr 3)
+  uint32_t* q_idx = nullptr;
+  size_t q_cap = 0;
+  float* tr = nullptr;       // t_cap x (pos 3, dir 3, value 3)
+  size_t t_cap = 0;
+  uint32_t* counts = nullptr;  // [0] queries, [1] training samples
+  CacheIO* d_io = nullptr;
+  CacheIO io;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
 };
 
 struct ne_scene {
@@ -1301,9 +1311,11 @@ void ne_cache_destroy(ne_cache* c) {
   cudaSetDevice(c->ctx->device);
   cudaStreamSynchronize(c->ctx->stream);
   void* bufs[] = {c->P, c->m, c->v, c->wfwd, c->wbwd, c->bias, c->part, c->loss_part, c->d_loss, c->grad, c->acts,
-                  c->out};
+                  c->out, c->q, c->q_idx, c->tr, c->counts, c->d_io};
   for (void* p : bufs)
     if (p) cudaFree(p);
+  for (cudaEvent_t e : c->ev)
+    if (e) cudaEventDestroy(e);
   delete c;
 }
 
@@ -1369,23 +1381,10 @@ ne_status ne_cache_infer(ne_cache* c, const float* pos, const float* dirs, const
   return cacheErr(ctx);
 }
 
-ne_status ne_cache_train(ne_cache* c, const float* pos, const float* dirs, const float* feats, const float* targets,
-                         size_t n, int apply, float* loss, float* grads, uint32_t flags) {
-  if (!c || !targets || n == 0 || (!feats && (!pos || !dirs))) return NE_ERR_INVALID_ARG;
-  if (n > (1u << 24)) return fail(c->ctx, NE_ERR_INVALID_ARG, "radiance cache: at most 2^24 samples per step");
+// One optimiser step on device arrays (pos/dir or features, targets).
+static ne_status cacheTrainDevice(ne_cache* c, const float* dp, const float* dd, const float* df, const float* dt,
+                                  size_t n, int apply, bool wantGrads) {
   ne_context* ctx = c->ctx;
-  NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
-  bool dev = flags & NE_CACHE_DEVICE_PTRS;
-  DevBuf<float> tp, td, tf, tt;
-  const float *dp = nullptr, *dd = nullptr, *df = nullptr, *dt = nullptr;
-  ne_status st = NE_OK;
-  if (feats) st = stageIn(ctx, feats, n * 96, dev, tf, &df);
-  else {
-    st = stageIn(ctx, pos, n * 3, dev, tp, &dp);
-    if (!st) st = stageIn(ctx, dirs, n * 3, dev, td, &dd);
-  }
-  if (!st) st = stageIn(ctx, targets, n * 3, dev, tt, &dt);
-  if (st) return st;
   if (c->cap < n) {
     if (c->acts) cudaFree(c->acts);
     if (c->out) cudaFree(c->out);
@@ -1407,16 +1406,38 @@ ne_status ne_cache_train(ne_cache* c, const float* pos, const float* dirs, const
     NE_CUDA(cudaMalloc(&c->loss_part, (size_t)blocks * 4), "cudaMalloc");
     c->part_blocks = blocks;
   }
-  NE_CUDA(cudaMemsetAsync(ctx->d_err, 0, 4, ctx->stream), "cudaMemsetAsync");
   NeMlpForward f = {dp, dd, df, (uint32_t)n, c->wfwd, c->bias, c->out, c->acts, nullptr, nullptr, nullptr};
   NE_CUDA(ne_mlp_forward(ctx->stream, f, ctx->d_err), "k_mlp_forward launch");
   NeMlpBackward b = {c->acts, c->out, dt, (uint32_t)n, c->wbwd, c->part, c->loss_part};
   NE_CUDA(ne_mlp_backward(ctx->stream, b, ctx->d_err), "k_mlp_backward launch");
   if (apply) c->step++;
-  NE_CUDA(ne_mlp_adam(ctx->stream, c->P, c->m, c->v, c->part, blocks, c->loss_part, grads ? c->grad : nullptr,
+  NE_CUDA(ne_mlp_adam(ctx->stream, c->P, c->m, c->v, c->part, blocks, c->loss_part, wantGrads ? c->grad : nullptr,
                       c->d_loss, 1e-2f, apply ? c->step : 1, apply),
           "k_mlp_adam launch");
   if (apply) NE_CUDA(ne_mlp_pack(ctx->stream, c->P, c->wfwd, c->wbwd, c->bias), "k_mlp_pack launch");
+  return NE_OK;
+}
+
+ne_status ne_cache_train(ne_cache* c, const float* pos, const float* dirs, const float* feats, const float* targets,
+                         size_t n, int apply, float* loss, float* grads, uint32_t flags) {
+  if (!c || !targets || n == 0 || (!feats && (!pos || !dirs))) return NE_ERR_INVALID_ARG;
+  if (n > (1u << 24)) return fail(c->ctx, NE_ERR_INVALID_ARG, "radiance cache: at most 2^24 samples per step");
+  ne_context* ctx = c->ctx;
+  NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  bool dev = flags & NE_CACHE_DEVICE_PTRS;
+  DevBuf<float> tp, td, tf, tt;
+  const float *dp = nullptr, *dd = nullptr, *df = nullptr, *dt = nullptr;
+  ne_status st = NE_OK;
+  if (feats) st = stageIn(ctx, feats, n * 96, dev, tf, &df);
+  else {
+    st = stageIn(ctx, pos, n * 3, dev, tp, &dp);
+    if (!st) st = stageIn(ctx, dirs, n * 3, dev, td, &dd);
+  }
+  if (!st) st = stageIn(ctx, targets, n * 3, dev, tt, &dt);
+  if (st) return st;
+  NE_CUDA(cudaMemsetAsync(ctx->d_err, 0, 4, ctx->stream), "cudaMemsetAsync");
+  st = cacheTrainDevice(c, dp, dd, df, dt, n, apply, grads != nullptr);
+  if (st) return st;
   float lsum = 0;
   NE_CUDA(cudaMemcpyAsync(&lsum, c->d_loss, 4, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync");
   if (grads)
@@ -1426,6 +1447,158 @@ ne_status ne_cache_train(ne_cache* c, const float* pos, const float* dirs, const
   st = cacheErr(ctx);
   if (st) return st;
   if (loss) *loss = lsum / (3.0f * (float)n);
+  return NE_OK;
+}
+
+ne_status ne_render_cached(ne_scene* sc, ne_cache* c, const ne_render_params* p, const ne_cache_render_params* cp,
+                           float* out_rgb, ne_render_stats* stats, ne_cache_render_stats* cstats) {
+  if (!sc || !c || !cp || !out_rgb || c->ctx != sc->ctx) return NE_ERR_INVALID_ARG;
+  ne_context* ctx = sc->ctx;
+  if (sc->feature_set != K_VOLUME || !(sc->features & FT_GRID))
+    return fail(ctx, NE_ERR_UNSUPPORTED, "ne_render_cached: the scene's media must be grid media");
+  if (cp->bounce < 0 || cp->train_steps < 0) return fail(ctx, NE_ERR_INVALID_ARG, "ne_render_cached: bad parameters");
+  NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  const int W = sc->settings.width, H = sc->settings.height;
+  int spp = (p && p->spp > 0) ? p->spp : sc->settings.spp;
+  if (spp <= 0) return fail(ctx, NE_ERR_INVALID_ARG, "spp must be positive");
+  uint32_t flags = p ? p->flags : 0;
+  uint32_t cw = (uint32_t)W, ch = (uint32_t)H;
+  if (flags & NE_RENDER_REF_TILES) {
+    cw = 40u * (uint32_t)(W / 40);
+    ch = 10u * (uint32_t)(H / 10);
+  }
+  uint64_t npix = (uint64_t)cw * ch, total = npix * (uint64_t)spp;
+  if (total > 0xFFFFFFFFull) return fail(ctx, NE_ERR_INVALID_ARG, "ne_render_cached: at most 2^32 paths per call");
+  if (sc->paths_cap < total) {
+    if (sc->d_paths) cudaFree(sc->d_paths);
+    sc->d_paths = nullptr;
+    sc->paths_cap = 0;
+    NE_CUDA(cudaMalloc(&sc->d_paths, total * 3 * sizeof(float)), "cudaMalloc(paths)");
+    sc->paths_cap = total;
+  }
+  size_t tcap = cp->train_stride ? (size_t)std::min<uint64_t>(total, total / cp->train_stride * 2 + 4096) : 1;
+  if (c->q_cap < total) {
+    if (c->q) cudaFree(c->q);
+    if (c->q_idx) cudaFree(c->q_idx);
+    c->q = nullptr;
+    c->q_idx = nullptr;
+    c->q_cap = 0;
+    NE_CUDA(cudaMalloc(&c->q, total * 9 * sizeof(float)), "cudaMalloc(cache queries)");
+    NE_CUDA(cudaMalloc(&c->q_idx, total * sizeof(uint32_t)), "cudaMalloc(cache queries)");
+    c->q_cap = total;
+  }
+  if (c->t_cap < tcap) {
+    if (c->tr) cudaFree(c->tr);
+    c->tr = nullptr;
+    c->t_cap = 0;
+    NE_CUDA(cudaMalloc(&c->tr, tcap * 9 * sizeof(float)), "cudaMalloc(training samples)");
+    c->t_cap = tcap;
+  }
+  if (!c->counts) NE_CUDA(cudaMalloc(&c->counts, 2 * sizeof(uint32_t)), "cudaMalloc");
+  if (!c->d_io) NE_CUDA(cudaMalloc(&c->d_io, sizeof(CacheIO)), "cudaMalloc");
+  for (cudaEvent_t& e : c->ev)
+    if (!e) NE_CUDA(cudaEventCreate(&e), "cudaEventCreate");
+  CacheIO& io = c->io;
+  io.q_pos = c->q;
+  io.q_dir = c->q + 3 * c->q_cap;
+  io.q_thr = c->q + 6 * c->q_cap;
+  io.q_idx = c->q_idx;
+  io.q_count = c->counts;
+  io.q_cap = (uint32_t)c->q_cap;
+  io.t_pos = c->tr;
+  io.t_dir = c->tr + 3 * c->t_cap;
+  io.t_val = c->tr + 6 * c->t_cap;
+  io.t_count = c->counts + 1;
+  io.t_cap = (uint32_t)c->t_cap;
+  io.train_stride = cp->train_stride;
+  io.bounce = cp->bounce;
+  NE_CUDA(cudaMemcpyAsync(c->d_io, &io, sizeof(CacheIO), cudaMemcpyHostToDevice, ctx->stream), "cudaMemcpyAsync");
+  NE_CUDA(cudaMemsetAsync(c->counts, 0, 2 * sizeof(uint32_t), ctx->stream), "cudaMemsetAsync");
+  NE_CUDA(cudaMemsetAsync(ctx->d_err, 0, 4, ctx->stream), "cudaMemsetAsync");
+  NE_CUDA(cudaMemsetAsync(ctx->d_counter, 0, 5 * sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync");
+  bool devOut = flags & NE_RENDER_OUT_DEVICE;
+  size_t imgBytes = (size_t)W * H * 3 * sizeof(float);
+  DevBuf<float> tmpImg;
+  float* d_img = out_rgb;
+  if (!devOut) {
+    NE_CUDA(cudaMalloc(&tmpImg.p, imgBytes), "cudaMalloc(image)");
+    d_img = tmpImg.p;
+  }
+  NE_CUDA(cudaEventRecord(c->ev[0], ctx->stream), "cudaEventRecord");
+  if (cw != (uint32_t)W || ch != (uint32_t)H) NE_CUDA(cudaMemsetAsync(d_img, 0, imgBytes, ctx->stream), "cudaMemsetAsync");
+  PathArgs a;
+  a.P = pathParams(sc, p);
+  a.base = baseKey(p);
+  a.total = total;
+  a.spp = (uint32_t)spp;
+  a.sample_offset = p ? p->sample_offset : 0;
+  a.cover_w = cw;
+  a.keys = nullptr;
+  a.out = sc->d_paths;
+  a.track_share = sc->track_share;
+  a.cache = c->d_io;
+  int fit = 1;
+  NE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, k_paths<K_VOLUME | K_CACHE>, kThreads, 0),
+          "occupancy query");
+  int blocks = ctx->sm_count * std::max(1, fit);
+  unsigned long long needed = (total + kThreads - 1) / kThreads;
+  if ((unsigned long long)blocks > needed) blocks = (int)std::max<unsigned long long>(1, needed);
+  NE_CUDA(ne_launch_path_kernel_cache(blocks, ctx->stream, sc->d, a, ctx->d_counter, ctx->d_err), "path kernel launch");
+  NE_CUDA(cudaEventRecord(c->ev[1], ctx->stream), "cudaEventRecord");
+  uint32_t counts[2] = {0, 0};
+  NE_CUDA(cudaMemcpyAsync(counts, c->counts, sizeof(counts), cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync");
+  NE_CUDA(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  uint32_t nq = std::min<uint32_t>(counts[0], io.q_cap), nt = std::min<uint32_t>(counts[1], io.t_cap);
+  NeMlpForward f = {io.q_pos, io.q_dir, nullptr, nq, c->wfwd, c->bias, nullptr, nullptr, io.q_thr, io.q_idx,
+                    sc->d_paths};
+  NE_CUDA(ne_mlp_forward(ctx->stream, f, ctx->d_err), "k_mlp_forward launch");
+  int rblocks = (int)std::min<uint64_t>((npix + 255) / 256, (uint64_t)ctx->sm_count * 16);
+  k_reduce<<<std::max(1, rblocks), 256, 0, ctx->stream>>>(sc->d_paths, (uint32_t)npix, (uint32_t)spp, cw, W, d_img);
+  NE_CUDA(cudaGetLastError(), "k_reduce launch");
+  if (!devOut) NE_CUDA(cudaMemcpyAsync(out_rgb, d_img, imgBytes, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync");
+  NE_CUDA(cudaEventRecord(c->ev[2], ctx->stream), "cudaEventRecord");
+  float loss = 0;
+  int launches = 3;
+  if (cp->train_steps > 0 && nt > 0) {
+    uint32_t batch = cp->train_batch ? std::min<uint32_t>(cp->train_batch, nt) : nt;
+    uint32_t off = 0;
+    for (int s = 0; s < cp->train_steps; s++) {
+      if (off + batch > nt) off = 0;
+      ne_status st = cacheTrainDevice(c, io.t_pos + 3 * (size_t)off, io.t_dir + 3 * (size_t)off, nullptr,
+                                      io.t_val + 3 * (size_t)off, batch, 1, false);
+      if (st) return st;
+      off += batch;
+      launches += 4;
+    }
+    float lsum = 0;
+    NE_CUDA(cudaMemcpyAsync(&lsum, c->d_loss, 4, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync");
+    NE_CUDA(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+    loss = lsum / (3.0f * (float)batch);
+  }
+  NE_CUDA(cudaEventRecord(c->ev[3], ctx->stream), "cudaEventRecord");
+  ne_status st = checkErr(ctx);
+  if (st) return st;
+  st = cacheErr(ctx);
+  if (st) return st;
+  float pms = 0, ims = 0, tms = 0;
+  cudaEventElapsedTime(&pms, c->ev[0], c->ev[1]);
+  cudaEventElapsedTime(&ims, c->ev[1], c->ev[2]);
+  cudaEventElapsedTime(&tms, c->ev[2], c->ev[3]);
+  if (stats) {
+    memset(stats, 0, sizeof(*stats));
+    stats->kernel_ms = pms;
+    stats->total_ms = pms + ims + tms;
+    stats->paths = total;
+    stats->kernel_launches = (uint32_t)launches;
+  }
+  if (cstats) {
+    cstats->queries = nq;
+    cstats->train_samples = nt;
+    cstats->loss = loss;
+    cstats->path_ms = pms;
+    cstats->infer_ms = ims;
+    cstats->train_ms = tms;
+  }
   return NE_OK;
 }
 

@@ -36,7 +36,14 @@ struct PathArgs {
   const ne_path_key* keys;   // explicit keys (ne_trace_paths) or null
   float* out;                // total * 3 floats
   int track_share;           // regrouped kernel: tracking-phase threshold in 32nds of live lanes
+  const CacheIO* cache = nullptr;  // K_CACHE kernels: device copy of the cache buffers
 };
+
+// Training paths of a cached render: a multiplicative hash of the path index, so training
+// paths spread over pixels and samples.
+__device__ __forceinline__ bool isTrainingPath(unsigned long long idx, uint32_t stride) {
+  return stride && (((uint32_t)idx * 0x9E3779B1u) >> 8) % stride == 0;
+}
 
 template <uint32_t K>
 __global__ void __launch_bounds__(kThreads) k_sched(const __grid_constant__ DScene s, const PathArgs a,
@@ -60,7 +67,7 @@ __device__ __forceinline__ void flushCounters(const Counters& cn, unsigned long 
 template <uint32_t K>
 __global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_paths(const __grid_constant__ DScene s, const PathArgs a,
                                                     unsigned long long* __restrict__ counter, uint32_t* err) {
-  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err};
+  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, a.cache};
   const int lane = threadIdx.x & 31;
   for (;;) {
     unsigned long long base = 0;
@@ -69,6 +76,10 @@ __global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_paths(const __grid
     if (base >= a.total) break;
     unsigned long long idx = base + (unsigned long long)lane;
     if (idx < a.total) {
+      if (K & K_CACHE) {
+        c.pidx = (uint32_t)idx;
+        c.train = isTrainingPath(idx, a.cache->train_stride);
+      }
       uint32_t pixel, sample;
       if (a.keys) {
         ne_path_key k = a.keys[idx];
@@ -95,7 +106,7 @@ template <uint32_t K>
 __global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_lanes(const __grid_constant__ DScene s, const PathArgs a,
                                                     unsigned long long* __restrict__ counter, uint32_t* err) {
   namespace cg = cooperative_groups;
-  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err};
+  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, nullptr};
   for (;;) {
     cg::coalesced_group g = cg::coalesced_threads();
     unsigned long long base = 0;
@@ -165,6 +176,7 @@ cudaError_t pathKernelOccupancy(int* blocks_per_sm) {
 
 // Declared here, instantiated in the k_path_*.cu units only.
 NE_PATH_KERNEL_ALL(extern)
+NE_PATH_KERNEL_INSTANCE(extern, 0, K_VOLUME | K_CACHE)
 
 }  // namespace nedev
 
@@ -175,6 +187,9 @@ cudaError_t ne_launch_path_kernel(int kernel, uint32_t set, bool count, int bloc
                                   const nedev::DScene& s, const nedev::PathArgs& a, unsigned long long* counter,
                                   uint32_t* err);
 cudaError_t ne_path_kernel_occupancy(int kernel, uint32_t set, int* blocks_per_sm);
+// The straight kernel over grid-medium scenes with paths ending in the radiance cache.
+cudaError_t ne_launch_path_kernel_cache(int blocks, cudaStream_t st, const nedev::DScene& s, const nedev::PathArgs& a,
+                                        unsigned long long* counter, uint32_t* err);
 cudaError_t ne_launch_li(int blocks, cudaStream_t st, const nedev::DScene& s, nedev::PathParams P, nerng::PathKey base,
                          const ne_ray* rays, const ne_path_key* keys, size_t n, uint32_t first_dim, float* out,
                          uint32_t* err);

@@ -18,6 +18,7 @@
 //    count as bounces), and a scene without lights contributes no direct light;
 //  * a BVH traversal stack deeper than 64 entries raises an error flag.
 #pragma once
+#include <cooperative_groups.h>
 #include <stdint.h>
 
 #include "device_scene.h"
@@ -64,6 +65,7 @@ enum : uint32_t {
   FT_BBOX = 1u << 13,     // model bounding boxes (meshes)
   FT_ALL = (1u << 14) - 1,
   K_COUNT = 1u << 31,
+  K_CACHE = 1u << 30,  // paths end in the learned radiance cache (see CacheIO)
   // feature sets with a compiled kernel (the host picks the smallest superset)
   K_VOLUME = FT_AABB | FT_POINT | FT_SPHERE | FT_VOLBSDF | FT_GRID | FT_LDIR | FT_LINF,
   K_SURFACE = FT_RECT | FT_SPHERE | FT_GLOSSY | FT_LDIFF,
@@ -179,6 +181,31 @@ struct Ctx {
   Sampler S;
   Counters c;
   uint32_t* err;
+  // K_CACHE only: this path's index, whether it is a training path, and the cache buffers
+  uint32_t pidx;
+  bool train;
+  const struct CacheIO* cio;
+};
+
+// Buffers of a render that ends paths in the learned radiance cache. A path that reaches
+// a scattering vertex in a grid medium at or after bounce `bounce` either stops there and
+// appends a query (object-space position, incoming direction, throughput, path index) for
+// the network to answer, or, on a training path, runs on unchanged and appends a training
+// sample: the radiance gathered after that vertex divided by the throughput at it.
+struct CacheIO {
+  float* q_pos;
+  float* q_dir;
+  float* q_thr;
+  uint32_t* q_idx;
+  uint32_t* q_count;
+  uint32_t q_cap;
+  float* t_pos;
+  float* t_dir;
+  float* t_val;
+  uint32_t* t_count;
+  uint32_t t_cap;
+  uint32_t train_stride;  // a path is a training path when hash(index) % train_stride == 0
+  int bounce;
 };
 
 NE_D Ray transformRay(const Ray& r, const float* m) { return Ray{mul4(m, r.o, 1.0f), mul4(m, r.d, 0.0f)}; }
@@ -1067,6 +1094,15 @@ NE_D V3 uniformSampleOneLight(Ctx<K>& c, const Ray& incoming, const Hit& isect) 
   return estimateDirect(c, incoming, isect, light, inst) / lightPdf;
 }
 
+// Slot in an append-only buffer: one atomic per group of lanes that append together.
+NE_D uint32_t appendSlot(uint32_t* count) {
+  namespace cg = cooperative_groups;
+  cg::coalesced_group g = cg::coalesced_threads();
+  uint32_t base = 0;
+  if (g.thread_rank() == 0) base = atomicAdd(count, (uint32_t)g.size());
+  return g.shfl(base, 0) + g.thread_rank();
+}
+
 struct PathParams {
   int bounces;
   int rr;
@@ -1083,6 +1119,9 @@ NE_D V3 Li(Ctx<K>& c, const PathParams& P, Ray incoming) {
   V3 T = v3(1, 1, 1);
   Hit isect = emptyHit();
   int passes = 0;
+  // K_CACHE training paths: the vertex the sample is recorded at
+  bool recorded = false;
+  V3 vPos = v3(0, 0, 0), vDir = v3(0, 0, 0), vL = v3(0, 0, 0), vT = v3(0, 0, 0);
   for (int b = 0; b < P.bounces; b++) {
     bool did = intersectScene(c, incoming, isect, kEps12F, inf);
     if (isBlack(T)) break;
@@ -1100,6 +1139,25 @@ NE_D V3 Li(Ctx<K>& c, const PathParams& P, Ray incoming) {
         continue;
       }
       T = T * sampledT;
+      if ((K & K_CACHE) && b >= c.cio->bounce && !recorded) {
+        V3 xo = mul4(s.instances[isect.inst].ocs, scattered.o, 1.0f);
+        if (!c.train) {
+          const CacheIO& io = *c.cio;
+          uint32_t q = appendSlot(io.q_count);
+          if (q < io.q_cap) {
+            io.q_pos[3 * q] = xo.x; io.q_pos[3 * q + 1] = xo.y; io.q_pos[3 * q + 2] = xo.z;
+            io.q_dir[3 * q] = incoming.d.x; io.q_dir[3 * q + 1] = incoming.d.y; io.q_dir[3 * q + 2] = incoming.d.z;
+            io.q_thr[3 * q] = T.x; io.q_thr[3 * q + 1] = T.y; io.q_thr[3 * q + 2] = T.z;
+            io.q_idx[q] = c.pidx;
+          }
+          return L;
+        }
+        recorded = true;
+        vPos = xo;
+        vDir = incoming.d;
+        vL = L;
+        vT = T;
+      }
       V3 phaseFr = bsdfEval<K>(*mat, incoming.d, scattered.d, isect.normal);
       float phasePdf = bsdfPdf<K>(*mat, incoming.d, scattered.d, isect.normal);
       if (isBlack(phaseFr) || phasePdf == 0.f) break;
@@ -1139,6 +1197,18 @@ NE_D V3 Li(Ctx<K>& c, const PathParams& P, Ray incoming) {
         if (c.S.random() < q) break;
         T = T / (1.0f - q);
       }
+    }
+  }
+  if ((K & K_CACHE) && recorded) {
+    const CacheIO& io = *c.cio;
+    uint32_t q = appendSlot(io.t_count);
+    if (q < io.t_cap) {
+      V3 d = L - vL;
+      io.t_pos[3 * q] = vPos.x; io.t_pos[3 * q + 1] = vPos.y; io.t_pos[3 * q + 2] = vPos.z;
+      io.t_dir[3 * q] = vDir.x; io.t_dir[3 * q + 1] = vDir.y; io.t_dir[3 * q + 2] = vDir.z;
+      io.t_val[3 * q] = vT.x > 0 ? d.x / vT.x : 0.0f;
+      io.t_val[3 * q + 1] = vT.y > 0 ? d.y / vT.y : 0.0f;
+      io.t_val[3 * q + 2] = vT.z > 0 ? d.z / vT.z : 0.0f;
     }
   }
   return L;

@@ -1,0 +1,80 @@
+"""Rendering with the learned radiance cache (ne_render_cached) on the medium scene.
+
+* With no path reaching the termination bounce, and with every path a training path, the
+  cached render is the plain render, bit for bit (the cache changes nothing else).
+* With a zero network every terminated path keeps only the radiance gathered before its
+  termination vertex, so the image is at most the plain image in every pixel.
+* The gain of the trained network: against an FP64 plain reference, paths truncated at
+  bounce 2 without the network are strongly biased; after online training on the
+  integrator's own path suffixes the cached image's relMSE is several times lower.
+"""
+import json
+
+import numpy as np
+import pytest
+
+from conftest import scene_path
+
+pytestmark = pytest.mark.gpu
+
+
+def medium(ne, w=96, h=64):
+    d = json.load(open(scene_path("medium_c2")))
+    d["renderer"]["resolution"] = [w, h]
+    return ne.SceneHost.from_string(json.dumps(d))
+
+
+@pytest.fixture(scope="module")
+def env(built):
+    import narvalengine_gb300 as ne
+    ctx = ne.Context(0)
+    scene = ctx.upload(medium(ne))
+    cache = ne.RadianceCache(ctx, seed=5)
+    yield ne, ctx, scene, cache
+    cache.close()
+    ctx.close()
+
+
+def test_no_termination_is_plain(env):
+    ne, ctx, scene, cache = env
+    plain, _ = scene.render(seed=3, spp=4)
+    img, st, cst = scene.render_cached(cache, bounce=100000, seed=3, spp=4)
+    assert cst["queries"] == 0 and cst["train_samples"] == 0
+    assert np.array_equal(img.view(np.uint32), plain.view(np.uint32))
+    img, st, cst = scene.render_cached(cache, bounce=2, train_stride=1, seed=3, spp=4)
+    assert cst["queries"] == 0 and cst["train_samples"] > 100
+    assert np.array_equal(img.view(np.uint32), plain.view(np.uint32))
+
+
+def test_zero_network_only_truncates(env):
+    ne, ctx, scene, cache = env
+    cache.set_params(np.zeros(ne.RadianceCache.N_PARAMS, np.float32))
+    plain, _ = scene.render(seed=9, spp=4)
+    img, st, cst = scene.render_cached(cache, bounce=2, seed=9, spp=4)
+    assert cst["queries"] > 100
+    assert np.all(img <= plain)
+    assert img.sum() < plain.sum()
+
+
+def test_trained_cache_reduces_bias(env):
+    ne, ctx, scene, cache = env
+    from narvalengine_gb300.convergence import reference_image, relmse
+    ref, _ = reference_image(scene, 2048, chunk=1024)
+    cache.set_params(np.zeros(ne.RadianceCache.N_PARAMS, np.float32))
+    trunc, _, _ = scene.render_cached(cache, bounce=2, seed=1, spp=64)
+    e_trunc = relmse(trunc, ref)
+    fresh = ne.RadianceCache(ctx, seed=5)
+    try:
+        losses = []
+        for frame in range(40):
+            _, _, cst = scene.render_cached(fresh, bounce=2, train_stride=4, train_steps=4, train_batch=4096,
+                                            seed=100 + frame, spp=8)
+            losses.append(cst["loss"])
+        img, _, cst = scene.render_cached(fresh, bounce=2, seed=1, spp=64)
+        e_cache = relmse(img, ref)
+        plain, _ = scene.render(seed=1, spp=64)
+        e_plain = relmse(plain, ref)
+        assert np.mean(losses[-5:]) < np.mean(losses[:5]), losses
+        assert e_cache < e_trunc / 4, (e_cache, e_trunc, e_plain)
+    finally:
+        fresh.close()
