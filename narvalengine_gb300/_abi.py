@@ -116,6 +116,10 @@ NE_RENDER_COUNT_WORK = 1 << 2
 NE_RENDER_NO_SYNC = 1 << 3
 NE_RENDER_DROP_NONFINITE = 1 << 4
 
+# radiance cache
+NE_CACHE_PARAMS = 19728
+NE_CACHE_DEVICE_PTRS = 1 << 0
+
 # every symbol include/narval_gb300.h declares, with its ctypes signature
 SIGNATURES = {
     "ne_scene_host_load_json": (C.c_int32, [C.c_char_p, C.c_char_p, C.POINTER(C.c_void_p), C.c_char_p, C.c_size_t]),

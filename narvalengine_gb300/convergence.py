@@ -102,11 +102,15 @@ def time_to_relmse_cached(scene, cache, ref: np.ndarray, target: float = 1e-3, s
     acc = np.zeros_like(ref, dtype=np.float64)
     curve = []
     have, ms, check = 0, 0.0, frame_spp
+    parts = {"path_ms": 0.0, "infer_ms": 0.0, "train_ms": 0.0, "queries": 0, "train_samples": 0, "paths": 0}
     hit = None
     while have < max_spp:
         img, st, cst = scene.render_cached(cache, bounce=bounce, train_stride=train_stride, train_steps=train_steps,
                                            train_batch=train_batch, seed=seed, spp=frame_spp, sample_offset=have)
         ms += st["total_ms"]
+        for k in ("path_ms", "infer_ms", "train_ms", "queries", "train_samples"):
+            parts[k] += cst[k]
+        parts["paths"] += st["paths"]
         finite = np.isfinite(img)
         acc += np.where(finite, img, 0.0) * frame_spp
         have += frame_spp
@@ -119,7 +123,8 @@ def time_to_relmse_cached(scene, cache, ref: np.ndarray, target: float = 1e-3, s
                 break
     return {"target": target, "reached": hit is not None, "spp": hit["spp"] if hit else None,
             "ms": hit["ms"] if hit else None, "frame_spp": frame_spp, "bounce": bounce,
-            "train_stride": train_stride, "train_steps": train_steps, "train_batch": train_batch, "curve": curve}
+            "train_stride": train_stride, "train_steps": train_steps, "train_batch": train_batch, "totals": parts,
+            "curve": curve}
 
 
 def main(argv=None):
@@ -133,7 +138,9 @@ def main(argv=None):
     ap.add_argument("--save", default=None, help="write the reference image (.npy)")
     ap.add_argument("--cache", action="store_true", help="also measure the radiance-cache form")
     ap.add_argument("--max-spp", type=int, default=1 << 16)
-    ap.add_argument("--frame-spp", type=int, default=4)
+    ap.add_argument("--frame-spp", type=int, default=16)
+    ap.add_argument("--bounce", type=int, nargs="+", default=[2], help="cache termination bounce(s) to measure")
+    ap.add_argument("--train-steps", type=int, default=4)
     args = ap.parse_args(argv)
     path = args.scene if args.scene.endswith(".json") else os.path.join(ne.SCENES_DIR, args.scene + ".json")
     if args.resolution:
@@ -151,12 +158,15 @@ def main(argv=None):
         np.save(args.save, ref)
     res = time_to_relmse(scene, ref, args.target, chunk=args.chunk, max_spp=args.max_spp)
     if args.cache:
-        cache = ne.RadianceCache(ctx, seed=1)
-        res["cache"] = time_to_relmse_cached(scene, cache, ref, args.target, max_spp=args.max_spp,
-                                             frame_spp=args.frame_spp)
-        cache.close()
-        if res["reached"] and res["cache"]["reached"]:
-            res["cache_time_ratio"] = res["cache"]["ms"] / res["ms"]
+        res["cache"] = []
+        for bounce in args.bounce:
+            cache = ne.RadianceCache(ctx, seed=1)
+            r = time_to_relmse_cached(scene, cache, ref, args.target, max_spp=args.max_spp, frame_spp=args.frame_spp,
+                                      bounce=bounce, train_steps=args.train_steps)
+            cache.close()
+            if res["reached"] and r["reached"]:
+                r["time_ratio_vs_plain"] = r["ms"] / res["ms"]
+            res["cache"].append(r)
     out = {"scene": os.path.basename(path), "resolution": [host.width, host.height], "ref_spp": args.ref_spp,
            "ref_paths": host.width * host.height * args.ref_spp, "ref_device_ms": ref_ms,
            "ref_wall_s": time.time() - t0, "ref_dropped_paths": info["dropped_paths"], "relmse_eps": EPS, **res}

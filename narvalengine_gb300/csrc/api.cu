@@ -1375,7 +1375,7 @@ ne_status ne_cache_infer(ne_cache* c, const float* pos, const float* dirs, const
     dout = to.p;
   }
   NE_CUDA(cudaMemsetAsync(ctx->d_err, 0, 4, ctx->stream), "cudaMemsetAsync");
-  NeMlpForward f = {dp, dd, df, (uint32_t)n, c->wfwd, c->bias, dout, nullptr, nullptr, nullptr, nullptr};
+  NeMlpForward f = {dp, dd, df, (uint32_t)n, nullptr, c->wfwd, c->bias, dout, nullptr, nullptr, nullptr, nullptr};
   NE_CUDA(ne_mlp_forward(ctx->stream, f, ctx->d_err), "k_mlp_forward launch");
   if (!dev) NE_CUDA(cudaMemcpyAsync(rgb, dout, n * 3 * 4, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync");
   return cacheErr(ctx);
@@ -1406,7 +1406,7 @@ static ne_status cacheTrainDevice(ne_cache* c, const float* dp, const float* dd,
     NE_CUDA(cudaMalloc(&c->loss_part, (size_t)blocks * 4), "cudaMalloc");
     c->part_blocks = blocks;
   }
-  NeMlpForward f = {dp, dd, df, (uint32_t)n, c->wfwd, c->bias, c->out, c->acts, nullptr, nullptr, nullptr};
+  NeMlpForward f = {dp, dd, df, (uint32_t)n, nullptr, c->wfwd, c->bias, c->out, c->acts, nullptr, nullptr, nullptr};
   NE_CUDA(ne_mlp_forward(ctx->stream, f, ctx->d_err), "k_mlp_forward launch");
   NeMlpBackward b = {c->acts, c->out, dt, (uint32_t)n, c->wbwd, c->part, c->loss_part};
   NE_CUDA(ne_mlp_backward(ctx->stream, b, ctx->d_err), "k_mlp_backward launch");
@@ -1545,18 +1545,19 @@ ne_status ne_render_cached(ne_scene* sc, ne_cache* c, const ne_render_params* p,
   if ((unsigned long long)blocks > needed) blocks = (int)std::max<unsigned long long>(1, needed);
   NE_CUDA(ne_launch_path_kernel_cache(blocks, ctx->stream, sc->d, a, ctx->d_counter, ctx->d_err), "path kernel launch");
   NE_CUDA(cudaEventRecord(c->ev[1], ctx->stream), "cudaEventRecord");
-  uint32_t counts[2] = {0, 0};
-  NE_CUDA(cudaMemcpyAsync(counts, c->counts, sizeof(counts), cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync");
-  NE_CUDA(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
-  uint32_t nq = std::min<uint32_t>(counts[0], io.q_cap), nt = std::min<uint32_t>(counts[1], io.t_cap);
-  NeMlpForward f = {io.q_pos, io.q_dir, nullptr, nq, c->wfwd, c->bias, nullptr, nullptr, io.q_thr, io.q_idx,
-                    sc->d_paths};
+  // the network answers however many queries the path kernel appended (count read on the device)
+  NeMlpForward f = {io.q_pos, io.q_dir, nullptr, io.q_cap, c->counts, c->wfwd, c->bias, nullptr, nullptr, io.q_thr,
+                    io.q_idx, sc->d_paths};
   NE_CUDA(ne_mlp_forward(ctx->stream, f, ctx->d_err), "k_mlp_forward launch");
   int rblocks = (int)std::min<uint64_t>((npix + 255) / 256, (uint64_t)ctx->sm_count * 16);
   k_reduce<<<std::max(1, rblocks), 256, 0, ctx->stream>>>(sc->d_paths, (uint32_t)npix, (uint32_t)spp, cw, W, d_img);
   NE_CUDA(cudaGetLastError(), "k_reduce launch");
   if (!devOut) NE_CUDA(cudaMemcpyAsync(out_rgb, d_img, imgBytes, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync");
   NE_CUDA(cudaEventRecord(c->ev[2], ctx->stream), "cudaEventRecord");
+  uint32_t counts[2] = {0, 0};
+  NE_CUDA(cudaMemcpyAsync(counts, c->counts, sizeof(counts), cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync");
+  NE_CUDA(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  uint32_t nq = std::min<uint32_t>(counts[0], io.q_cap), nt = std::min<uint32_t>(counts[1], io.t_cap);
   float loss = 0;
   int launches = 3;
   if (cp->train_steps > 0 && nt > 0) {

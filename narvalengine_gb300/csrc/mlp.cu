@@ -174,6 +174,7 @@ struct FwdArgs {
   const float* dir;      // n x 3, unit
   const float* feats;    // n x 96 precomputed features, or null (encode pos/dir)
   uint32_t n;
+  const uint32_t* n_dev; // optional device count: the kernel runs min(*n_dev, n) queries
   const uint8_t* wfwd;   // packed forward tiles
   const float* bias;     // 272 floats
   float* out;            // n x 3 raw RGB outputs, or null
@@ -215,10 +216,11 @@ __global__ void __launch_bounds__(kTile) k_mlp_forward(const FwdArgs a, uint32_t
   const uint32_t tl = tmem_at(tb, 32 * warp, 0);
   uint32_t phase = 0;
   bool ok = true;
-  const uint32_t nTiles = (a.n + kTile - 1) / kTile;
+  const uint32_t n = a.n_dev ? min(*a.n_dev, a.n) : a.n;
+  const uint32_t nTiles = (n + kTile - 1) / kTile;
   for (uint32_t tile = blockIdx.x; tile < nTiles && ok; tile += gridDim.x) {
     const uint32_t row = tile * kTile + t;
-    const bool valid = row < a.n;
+    const bool valid = row < n;
     {
       float f[96];
       if (!valid) {
@@ -534,6 +536,7 @@ cudaError_t ne_mlp_forward(cudaStream_t st, const NeMlpForward& f, uint32_t* err
   a.dir = f.dir;
   a.feats = f.feats;
   a.n = f.n;
+  a.n_dev = f.n_dev;
   a.wfwd = f.wfwd;
   a.bias = f.bias;
   a.out = f.out;

@@ -21,6 +21,7 @@ struct NeMlpForward {
   const float* dir;          // n x 3 unit directions
   const float* feats;        // or n x 96 precomputed features (pos/dir ignored)
   uint32_t n;
+  const uint32_t* n_dev;     // optional device-side count: min(*n_dev, n) queries are run
   const uint8_t* wfwd;
   const float* bias;
   float* out;                // n x 3 raw outputs, or null

@@ -4,9 +4,10 @@
   cached render is the plain render, bit for bit (the cache changes nothing else).
 * With a zero network every terminated path keeps only the radiance gathered before its
   termination vertex, so the image is at most the plain image in every pixel.
-* The gain of the trained network: against an FP64 plain reference, paths truncated at
-  bounce 2 without the network are strongly biased; after online training on the
-  integrator's own path suffixes the cached image's relMSE is several times lower.
+* The gain of the trained network: against an FP64 plain reference, cloud paths truncated
+  at their second scattering event without the network are strongly biased; after online
+  training on the integrator's own path suffixes the cached image's relMSE is several times
+  lower.
 """
 import json
 
@@ -57,24 +58,33 @@ def test_zero_network_only_truncates(env):
 
 
 def test_trained_cache_reduces_bias(env):
-    ne, ctx, scene, cache = env
+    """On the dense cloud (albedo 0.99) paths ended at their second scattering event lose a
+    visible share of the light; the trained network restores most of it. relMSE against an
+    FP64 plain reference = bias^2 + noise; the plain image at the same sample count gives the
+    noise, so bias is measured as the excess over it."""
+    ne, ctx, _, _ = env
     from narvalengine_gb300.convergence import reference_image, relmse
-    ref, _ = reference_image(scene, 2048, chunk=1024)
-    cache.set_params(np.zeros(ne.RadianceCache.N_PARAMS, np.float32))
-    trunc, _, _ = scene.render_cached(cache, bounce=2, seed=1, spp=64)
-    e_trunc = relmse(trunc, ref)
+    d = json.load(open(scene_path("cloud_c4")))
+    d["renderer"]["resolution"] = [64, 64]
+    scene = ctx.upload(ne.SceneHost.from_string(json.dumps(d)))
+    zero = ne.RadianceCache(ctx, seed=5)
     fresh = ne.RadianceCache(ctx, seed=5)
     try:
-        losses = []
-        for frame in range(40):
-            _, _, cst = scene.render_cached(fresh, bounce=2, train_stride=4, train_steps=4, train_batch=4096,
-                                            seed=100 + frame, spp=8)
-            losses.append(cst["loss"])
-        img, _, cst = scene.render_cached(fresh, bounce=2, seed=1, spp=64)
-        e_cache = relmse(img, ref)
-        plain, _ = scene.render(seed=1, spp=64)
-        e_plain = relmse(plain, ref)
-        assert np.mean(losses[-5:]) < np.mean(losses[:5]), losses
-        assert e_cache < e_trunc / 4, (e_cache, e_trunc, e_plain)
+        ref, _ = reference_image(scene, 32768, chunk=4096)
+        zero.set_params(np.zeros(ne.RadianceCache.N_PARAMS, np.float32))
+        trunc, _, cst0 = scene.render_cached(zero, bounce=1, seed=1, spp=8192)
+        for frame in range(60):
+            scene.render_cached(fresh, bounce=1, train_stride=4, train_steps=4, train_batch=8192, seed=100 + frame,
+                                spp=16)
+        img, _, cst = scene.render_cached(fresh, bounce=1, seed=1, spp=8192)
+        plain, _ = scene.render(seed=1, spp=8192)
+        e_trunc, e_cache, e_plain = relmse(trunc, ref), relmse(img, ref), relmse(plain, ref)
+        assert cst0["queries"] > 0.05 * 64 * 64 * 8192
+        assert e_trunc - e_plain > 1e-4, (e_trunc, e_plain)
+        assert e_cache - e_plain < (e_trunc - e_plain) / 3, (e_cache, e_trunc, e_plain)
+        # what the network adds is light that truncation removed
+        assert img.sum() > trunc.sum()
     finally:
+        zero.close()
         fresh.close()
+        scene.close()
