@@ -47,6 +47,8 @@ WORKLOADS = {
                   "256x256x16spp, depth 8, RR after 3",
     "mesh_c3": "mesh_c3: 1.31M-triangle displaced icosphere (1024 GGX groups) on a 10x10 ground, two emitters 10, "
                "1024x1024x32spp, depth 12, reference midpoint BVH",
+    "views_c5": "views_c5: 64 orbiting views (seeded sizes from {64,128,256,512}^2) of the 128^3 medium + the "
+                "1.31M-triangle mesh, 16 spp, depth 32, one persistent launch replayed as a CUDA graph, autotuned",
     "cloud_c4": "cloud_c4: 512^3 fBm cloud (7 octaves, scale 80, albedo 0.99, HG g=0.85), sun 3.0 @30deg + env 0.2, "
                 "1024x1024x16spp, depth 256, plain integrator",
 }
@@ -197,6 +199,96 @@ def run_reference(args, rank: int, world: int):
     print(json.dumps(line), flush=True)
 
 
+def pin_scene_inputs(host):
+    """Moves the scene's density grids to pinned host memory (kept alive by the returned
+    tensors) and returns the bytes one upload copies: grids plus the instance, model,
+    primitive, material, light and medium tables."""
+    import ctypes
+    import torch
+    from narvalengine_gb300 import _abi
+    desc = host.desc
+    h2d, keep = 0, []
+    for i in range(desc.n_media):
+        m = desc.media[i]
+        if m.type == 0:
+            n = m.res[0] * m.res[1] * m.res[2]
+            t = torch.empty(n, dtype=torch.float32, pin_memory=True)
+            ctypes.memmove(t.data_ptr(), ctypes.addressof(m.grid.contents), n * 4)
+            m.grid = ctypes.cast(t.data_ptr(), ctypes.POINTER(ctypes.c_float))
+            keep.append(t)
+            h2d += n * 4
+    h2d += (desc.n_instances + desc.n_light_instances) * ctypes.sizeof(_abi.NeInstance) + \
+        desc.n_models * ctypes.sizeof(_abi.NeModel) + desc.n_prims * ctypes.sizeof(_abi.NePrimitive) + \
+        desc.n_materials * ctypes.sizeof(_abi.NeMaterial) + desc.n_lights * ctypes.sizeof(_abi.NeLight) + \
+        desc.n_media * ctypes.sizeof(_abi.NeMedium) + desc.n_model_materials * 4
+    return h2d, keep
+
+
+def run_views(args, rank: int, world: int, local: int):
+    """The multi-view workload: 64 views in one launch; `value` = aggregate Mpaths/s over all
+    views, with per-view completion latency (p50/p99) from the kernel's own timestamps."""
+    import narvalengine_gb300 as ne
+    from narvalengine_gb300.batch import orbit_views
+    d = Dist(world, "nccl")
+    ctx = ne.Context(local)
+    host = ne.SceneHost.from_json(os.path.join(ne.SCENES_DIR, SCENE))
+    scene = ctx.upload(host)
+    views = orbit_views(64, spp=host.spp)
+    p = ne.render_params(seed=1 + rank)
+    vb = ne.Views(scene, views, p)
+    best, _ = vb.autotune(repeats=1)
+    paths = sum(w * h * s for _, w, h, s in views)
+    for _ in range(args.warmup):
+        vb.render()
+    ctx.synchronize()
+    d.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms, p50, p99 = [], [], []
+    for _ in range(args.steps):
+        ctx.flush_l2(256 << 20)
+        st = vb.render()
+        ms.append(st["ms"])
+        p50.append(st["latency_p50_ms"])
+        p99.append(st["latency_p99_ms"])
+    clk = clocks.stop()
+    d.barrier()
+    total_ms = d.max(sum(ms))
+    value = paths * args.steps * world / (total_ms / 1e3) / 1e6
+    # e2e: upload the scene, build the batch, render, read every image back
+    out_bytes = sum(w * h * 12 for _, w, h, _ in views)
+    h2d, pinned = pin_scene_inputs(host)
+    d.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s2 = ctx.upload(host)
+        v2 = ne.Views(s2, views, p)
+        v2.set_tuning(**best)
+        v2.render()
+        for v in range(len(views)):
+            v2.image(v)
+        v2.close()
+        s2.close()
+    e2e_s = d.max(time.perf_counter() - t0)
+    e2e = paths * args.steps * world / e2e_s / 1e6
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "Mpaths/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+                "config": {"workload": WORKLOAD, "paths_per_step": paths, "views": len(views),
+                           "l2": "flushed between steps (256 MiB write, outside events)",
+                           "parallelism": f"{world} GPU(s), sample seeds per rank", "tuning": best},
+                "latency_ms": {"p50": statistics.median(p50), "p99": statistics.median(p99)},
+                "e2e": {"value": e2e, "unit": "Mpaths/s", "h2d_bytes_per_step": h2d,
+                        "d2h_bytes_per_step": out_bytes},
+                "gpu_launches": 2 * args.steps, "roofline": None, "cpu_baseline": None, "clocks": clk}
+        print(json.dumps(line), flush=True)
+    vb.close()
+    scene.close()
+    ctx.close()
+    d.close()
+
+
 def run_profile_case(spp: int, kernel: int, track_share: int):
     """Small case for ncu: the same scene at a reduced sample count, rendered twice."""
     import narvalengine_gb300 as ne
@@ -244,6 +336,10 @@ def main():
         run_profile_case(args.profile_spp, args.kernel, args.track_share)
         return
 
+    if args.scene == "views_c5":
+        run_views(args, rank, world, local)
+        return
+
     import narvalengine_gb300 as ne
     d = Dist(world, "nccl")
     ctx = ne.Context(local)
@@ -287,24 +383,7 @@ def main():
     value = paths_per_step * args.steps * world / (total_ms / 1e3) / 1e6
 
     # e2e: host buffers through the public API, copies inside the timed region
-    import ctypes
-    pinned_grid = None
-    desc = host.desc
-    h2d = 0
-    for i in range(desc.n_media):
-        m = desc.media[i]
-        if m.type == 0:
-            n = m.res[0] * m.res[1] * m.res[2]
-            pinned_grid = torch.empty(n, dtype=torch.float32, pin_memory=True)
-            ctypes.memmove(pinned_grid.data_ptr(), ctypes.addressof(m.grid.contents), n * 4)
-            m.grid = ctypes.cast(pinned_grid.data_ptr(), ctypes.POINTER(ctypes.c_float))
-            h2d += n * 4
-    # instance, model, primitive, material and light tables (a few KB next to the grid)
-    from narvalengine_gb300 import _abi
-    h2d += (desc.n_instances + desc.n_light_instances) * ctypes.sizeof(_abi.NeInstance) + \
-        desc.n_models * ctypes.sizeof(_abi.NeModel) + desc.n_prims * ctypes.sizeof(_abi.NePrimitive) + \
-        desc.n_materials * ctypes.sizeof(_abi.NeMaterial) + desc.n_lights * ctypes.sizeof(_abi.NeLight) + \
-        desc.n_media * ctypes.sizeof(_abi.NeMedium) + desc.n_model_materials * 4
+    h2d, pinned_grid = pin_scene_inputs(host)
     out_host = torch.empty((H, W, 3), dtype=torch.float32, pin_memory=True).numpy()
     pe = ne.render_params(seed=1, sample_offset=base)
     for _ in range(1):

@@ -101,6 +101,10 @@ ne_status ne_scene_host_load_json(const char* path, const char* resources_dir, n
 ne_status ne_scene_host_load_json_string(const char* json, const char* resources_dir, ne_scene_host** out,
                                          char* err, size_t err_len);
 const ne_scene_desc* ne_scene_host_desc(const ne_scene_host* s);
+/* Camera::Camera (core/Camera.cpp:7-26) as SceneReader sets it up (io/SceneReader.cpp:650-675:
+ * aperture 0.0001, up (0, 1, 0)); focus 3 reproduces "autoFocus". For views built in code. */
+ne_status ne_camera_look_at(const float position[3], const float look_at[3], float vfov_deg, int width,
+                            int height, float focus, ne_camera* out);
 void ne_scene_host_destroy(ne_scene_host* s);
 
 /* ---- device ---- */
@@ -188,6 +192,43 @@ ne_status ne_debug_fmath(ne_context* ctx, int fn, const float* x, size_t n, floa
 /* Device copy of the shared counter-based generator: u01 for (seed, pixel, sample, dim). */
 ne_status ne_debug_rng(ne_context* ctx, uint64_t seed, const ne_path_key* keys, const uint32_t* dims, size_t n,
                        float* out);
+
+/* ---- many views in one launch (no counterpart in the reference) ----
+ * A batch of cameras over one scene, each with its own resolution and samples per pixel,
+ * rendered by one persistent kernel launch (optionally replayed as a CUDA graph). Each view
+ * uses its own random stream. Completion latency = time from the launch's first warp to the
+ * view's last path. A batch belongs to its scene and is destroyed with it. */
+typedef struct ne_view {
+  ne_camera camera;
+  int32_t width, height, spp, pad;
+} ne_view;
+typedef struct ne_views ne_views;
+typedef struct ne_views_tuning {
+  uint32_t fetch;          /* path indices a warp takes at a time, multiple of 32 (default 32) */
+  int32_t blocks_per_sm;   /* resident blocks per SM, 0 = as many as fit */
+  int32_t order;           /* views in the launch: 0 as given, 1 largest first, 2 smallest first */
+  int32_t graph;           /* 1: capture the launch sequence once and replay it as a CUDA graph */
+} ne_views_tuning;
+typedef struct ne_views_stats {
+  double ms;               /* CUDA-event time of the batch */
+  uint64_t paths;
+  float latency_p50_ms, latency_p99_ms, latency_max_ms;
+  uint32_t kernel_launches;  /* kernels per batch (a graph launch counts its kernels) */
+} ne_views_stats;
+ne_status ne_views_create(ne_scene* scene, const ne_view* views, uint32_t n, const ne_render_params* params,
+                          ne_views** out);
+void ne_views_destroy(ne_views* views);
+ne_status ne_views_set_tuning(ne_views* views, const ne_views_tuning* tuning);
+ne_status ne_views_get_tuning(const ne_views* views, ne_views_tuning* tuning);
+/* Times every candidate configuration (fetch 32/128, all or half the resident blocks, given
+ * or largest-first order, as a graph) `repeats` times after one warm-up batch, keeps the
+ * fastest and returns it with its time. */
+ne_status ne_views_autotune(ne_views* views, int repeats, ne_views_tuning* best, double* best_ms);
+ne_status ne_views_render(ne_views* views, ne_views_stats* stats);
+/* Completion latency of each view of the last batch, in the caller's order (n floats, ms). */
+ne_status ne_views_latency(const ne_views* views, float* ms);
+/* Per-pixel mean radiance of view v of the last batch (width*height*3 floats, host memory). */
+ne_status ne_views_image(const ne_views* views, uint32_t v, float* out_rgb);
 
 /* ---- learned radiance cache (no counterpart in the reference) ----
  * A small network (features 96 -> 4 x 64 ReLU -> RGB) that predicts the radiance a medium

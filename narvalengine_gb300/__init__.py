@@ -320,6 +320,71 @@ def hits_to_numpy(arr) -> np.ndarray:
 
 
 # ---------------------------------------------------------------- output stage
+def camera_look_at(position, look_at, vfov: float, width: int, height: int, focus: float = 3.0) -> "_abi.NeCamera":
+    """Camera::Camera as SceneReader sets it up (focus 3 = the reference's autoFocus)."""
+    pos = np.ascontiguousarray(position, np.float32)
+    la = np.ascontiguousarray(look_at, np.float32)
+    cam = _abi.NeCamera()
+    st = library().ne_camera_look_at(_ptr(pos), _ptr(la), vfov, width, height, focus, C.byref(cam))
+    if st != 0:
+        raise NarvalError(st, "ne_camera_look_at: invalid arguments")
+    return cam
+
+
+class Views:
+    """A batch of views rendered by one persistent launch (ne_views)."""
+
+    def __init__(self, scene: "Scene", views: list, params: NeRenderParams | None = None, **kw):
+        """views: list of (camera, width, height, spp)."""
+        self.scene = scene
+        self.ctx = scene.ctx
+        arr = (_abi.NeView * len(views))()
+        for i, (cam, w, h, spp) in enumerate(views):
+            arr[i].camera = cam
+            arr[i].width, arr[i].height, arr[i].spp = w, h, spp
+        self.sizes = [(w, h, spp) for _, w, h, spp in views]
+        p = params if params is not None else render_params(**kw)
+        hnd = C.c_void_p()
+        self.ctx.check(library().ne_views_create(scene._h, arr, len(views), C.byref(p), C.byref(hnd)))
+        self._h = hnd
+
+    def set_tuning(self, fetch: int = 32, blocks_per_sm: int = 0, order: int = 0, graph: bool = True):
+        t = _abi.NeViewsTuning(fetch, blocks_per_sm, order, int(graph))
+        self.ctx.check(library().ne_views_set_tuning(self._h, C.byref(t)))
+
+    def tuning(self) -> dict:
+        t = _abi.NeViewsTuning()
+        self.ctx.check(library().ne_views_get_tuning(self._h, C.byref(t)))
+        return {f: getattr(t, f) for f, _ in t._fields_}
+
+    def autotune(self, repeats: int = 1):
+        t = _abi.NeViewsTuning()
+        ms = C.c_double()
+        self.ctx.check(library().ne_views_autotune(self._h, repeats, C.byref(t), C.byref(ms)))
+        return {f: getattr(t, f) for f, _ in t._fields_}, ms.value
+
+    def render(self) -> dict:
+        s = _abi.NeViewsStats()
+        self.ctx.check(library().ne_views_render(self._h, C.byref(s)))
+        return {f: getattr(s, f) for f, _ in s._fields_}
+
+    def latency(self) -> np.ndarray:
+        out = np.empty(len(self.sizes), np.float32)
+        self.ctx.check(library().ne_views_latency(self._h, _ptr(out)))
+        return out
+
+    def image(self, v: int) -> np.ndarray:
+        w, h, _ = self.sizes[v]
+        out = np.empty((h, w, 3), np.float32)
+        self.ctx.check(library().ne_views_image(self._h, v, _ptr(out)))
+        return out
+
+    def close(self):
+        if self._h and self.scene._h:
+            library().ne_views_destroy(self._h)
+        self._h = None
+
+
 class RadianceCache:
     """The learned radiance cache (ne_cache): a 96 -> 4x64 -> RGB network on the tensor cores."""
 

@@ -88,6 +88,20 @@ class NeRenderStats(C.Structure):
                 ("prim_tests", C.c_uint64), ("kernel_launches", C.c_uint32), ("dropped_paths", C.c_uint32)]
 
 
+class NeView(C.Structure):
+    _fields_ = [("camera", NeCamera), ("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32),
+                ("pad", C.c_int32)]
+
+
+class NeViewsTuning(C.Structure):
+    _fields_ = [("fetch", C.c_uint32), ("blocks_per_sm", C.c_int32), ("order", C.c_int32), ("graph", C.c_int32)]
+
+
+class NeViewsStats(C.Structure):
+    _fields_ = [("ms", C.c_double), ("paths", C.c_uint64), ("latency_p50_ms", C.c_float),
+                ("latency_p99_ms", C.c_float), ("latency_max_ms", C.c_float), ("kernel_launches", C.c_uint32)]
+
+
 class NeCacheRenderParams(C.Structure):
     _fields_ = [("bounce", C.c_int32), ("train_stride", C.c_uint32), ("train_steps", C.c_int32),
                 ("train_batch", C.c_uint32)]
@@ -160,5 +174,16 @@ SIGNATURES = {
     "ne_render_cached": (C.c_int32, [C.c_void_p, C.c_void_p, C.POINTER(NeRenderParams),
                                      C.POINTER(NeCacheRenderParams), C.c_void_p, C.POINTER(NeRenderStats),
                                      C.POINTER(NeCacheRenderStats)]),
+    "ne_camera_look_at": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_float, C.c_int, C.c_int, C.c_float,
+                                      C.POINTER(NeCamera)]),
+    "ne_views_create": (C.c_int32, [C.c_void_p, C.POINTER(NeView), C.c_uint32, C.POINTER(NeRenderParams),
+                                    C.POINTER(C.c_void_p)]),
+    "ne_views_destroy": (None, [C.c_void_p]),
+    "ne_views_set_tuning": (C.c_int32, [C.c_void_p, C.POINTER(NeViewsTuning)]),
+    "ne_views_get_tuning": (C.c_int32, [C.c_void_p, C.POINTER(NeViewsTuning)]),
+    "ne_views_autotune": (C.c_int32, [C.c_void_p, C.c_int, C.POINTER(NeViewsTuning), C.POINTER(C.c_double)]),
+    "ne_views_render": (C.c_int32, [C.c_void_p, C.POINTER(NeViewsStats)]),
+    "ne_views_latency": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "ne_views_image": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p]),
     "ne_debug_mma": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
 }

@@ -23,6 +23,7 @@
 #include "narval_gb300.h"
 #include "kernels.cuh"
 #include "mlp.h"
+#include "views.cuh"
 
 using namespace nedev;
 
@@ -82,6 +83,28 @@ struct ne_scene {
   int track_share = 16;      // k_sched tracking-phase threshold (32nds of live lanes)
   uint32_t features = 0;     // FT_* bits of the scene
   uint32_t feature_set = 0;  // compiled kernel specialisation covering them
+  std::vector<ne_views*> view_batches;  // destroyed with the scene
+};
+
+struct ne_views {
+  ne_scene* sc = nullptr;
+  std::vector<ne_view> views;      // caller order
+  std::vector<uint32_t> order;     // processing slot -> caller index
+  std::vector<uint32_t> slot_of;   // caller index -> processing slot
+  std::vector<DView> dv;           // processing order
+  DView* d_views = nullptr;
+  float* d_paths = nullptr;
+  float* d_img = nullptr;
+  unsigned long long* d_done = nullptr;   // n finished counts, n completion times, start time, work counter
+  uint64_t total = 0;
+  uint32_t total_pixels = 0;
+  PathParams P;
+  nerng::PathKey base;
+  ne_views_tuning tune = {32, 0, 0, 1};
+  int blocks = 1;
+  cudaGraphExec_t exec = nullptr;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  std::vector<float> latency;      // caller order, last batch
 };
 
 namespace {
@@ -519,6 +542,109 @@ ne_status cacheErr(ne_context* ctx) {
 
 }  // namespace
 
+// ---------------------------------------------------------------- view batches
+namespace {
+
+// Lays the views out in the tuning's order and uploads the table.
+ne_status viewsLayout(ne_views* vw) {
+  ne_context* ctx = vw->sc->ctx;
+  const uint32_t n = (uint32_t)vw->views.size();
+  vw->order.resize(n);
+  for (uint32_t i = 0; i < n; i++) vw->order[i] = i;
+  auto paths = [&](uint32_t i) { return (uint64_t)vw->views[i].width * vw->views[i].height * vw->views[i].spp; };
+  if (vw->tune.order == 1)
+    std::stable_sort(vw->order.begin(), vw->order.end(), [&](uint32_t x, uint32_t y) { return paths(x) > paths(y); });
+  else if (vw->tune.order == 2)
+    std::stable_sort(vw->order.begin(), vw->order.end(), [&](uint32_t x, uint32_t y) { return paths(x) < paths(y); });
+  vw->slot_of.assign(n, 0);
+  vw->dv.resize(n);
+  uint64_t pb = 0;
+  uint32_t pix = 0;
+  for (uint32_t s = 0; s < n; s++) {
+    const ne_view& v = vw->views[vw->order[s]];
+    vw->slot_of[vw->order[s]] = s;
+    DView& d = vw->dv[s];
+    memcpy(&d.cam, &v.camera, sizeof(DCamera));
+    d.width = v.width;
+    d.height = v.height;
+    d.spp = (uint32_t)v.spp;
+    d.pix_begin = pix;
+    d.stream = vw->order[s] + 1;
+    d.pad = 0;
+    d.path_begin = pb;
+    d.paths = (uint64_t)v.width * v.height * v.spp;
+    pb += d.paths;
+    pix += (uint32_t)(v.width * v.height);
+  }
+  NE_CUDA(cudaMemcpyAsync(vw->d_views, vw->dv.data(), n * sizeof(DView), cudaMemcpyHostToDevice, ctx->stream),
+          "cudaMemcpyAsync");
+  return NE_OK;
+}
+
+ne_status viewsEnqueue(ne_views* vw) {
+  ne_context* ctx = vw->sc->ctx;
+  const uint32_t n = (uint32_t)vw->views.size();
+  unsigned long long* done = vw->d_done;
+  unsigned long long* tdone = done + n;
+  unsigned long long* tstart = done + 2 * n;
+  unsigned long long* counter = done + 2 * n + 1;
+  NE_CUDA(cudaMemsetAsync(done, 0, 2 * n * sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync");
+  NE_CUDA(cudaMemsetAsync(tstart, 0xFF, sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync");
+  NE_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync");
+  NE_CUDA(cudaMemsetAsync(ctx->d_err, 0, 4, ctx->stream), "cudaMemsetAsync");
+  ViewArgs a;
+  a.P = vw->P;
+  a.base = vw->base;
+  a.views = vw->d_views;
+  a.n_views = n;
+  a.total = vw->total;
+  a.fetch = vw->tune.fetch;
+  a.out = vw->d_paths;
+  a.done = done;
+  a.t_done = tdone;
+  a.t_start = tstart;
+  NE_CUDA(ne_launch_views(vw->blocks, ctx->stream, vw->sc->d, a, counter, ctx->d_err), "k_views launch");
+  int rblocks = (int)std::min<uint64_t>((vw->total_pixels + 255) / 256, (uint64_t)ctx->sm_count * 16);
+  NE_CUDA(ne_launch_reduce_views(std::max(1, rblocks), ctx->stream, vw->d_paths, vw->d_views, n, vw->total_pixels,
+                                 vw->d_img),
+          "k_reduce_views launch");
+  return NE_OK;
+}
+
+// (Re)builds the launch configuration and, with tune.graph, the captured graph.
+ne_status viewsPrepare(ne_views* vw) {
+  ne_context* ctx = vw->sc->ctx;
+  if (vw->exec) {
+    cudaGraphExecDestroy(vw->exec);
+    vw->exec = nullptr;
+  }
+  int fit = 1;
+  NE_CUDA(ne_views_occupancy(&fit), "occupancy query");
+  fit = std::max(1, fit);
+  int bps = vw->tune.blocks_per_sm > 0 ? std::min(vw->tune.blocks_per_sm, fit) : fit;
+  vw->blocks = ctx->sm_count * bps;
+  ne_status st = viewsLayout(vw);
+  if (st) return st;
+  NE_CUDA(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  if (vw->tune.graph) {
+    cudaGraph_t g = nullptr;
+    NE_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+    st = viewsEnqueue(vw);
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    if (st) {
+      if (g) cudaGraphDestroy(g);
+      return st;
+    }
+    if (e != cudaSuccess) return cudaFail(ctx, e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&vw->exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cudaFail(ctx, e, "cudaGraphInstantiate");
+  }
+  return NE_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 ne_status ne_context_create(int device, ne_context** out) {
@@ -862,6 +988,7 @@ ne_status ne_scene_get_tuning(const ne_scene* sc, ne_tuning* t) {
 
 void ne_scene_destroy(ne_scene* sc) {
   if (!sc) return;
+  while (!sc->view_batches.empty()) ne_views_destroy(sc->view_batches.back());
   auto& v = sc->ctx->scenes;
   v.erase(std::remove(v.begin(), v.end(), sc), v.end());
   cudaSetDevice(sc->ctx->device);
@@ -1600,6 +1727,176 @@ ne_status ne_render_cached(ne_scene* sc, ne_cache* c, const ne_render_params* p,
     cstats->infer_ms = ims;
     cstats->train_ms = tms;
   }
+  return NE_OK;
+}
+
+ne_status ne_views_create(ne_scene* sc, const ne_view* views, uint32_t n, const ne_render_params* p, ne_views** out) {
+  if (!sc || !views || !out || n == 0) return NE_ERR_INVALID_ARG;
+  *out = nullptr;
+  ne_context* ctx = sc->ctx;
+  uint64_t total = 0, pixels = 0;
+  for (uint32_t i = 0; i < n; i++) {
+    if (views[i].width <= 0 || views[i].height <= 0 || views[i].spp <= 0)
+      return fail(ctx, NE_ERR_INVALID_ARG, "ne_views_create: every view needs a positive size and spp");
+    total += (uint64_t)views[i].width * views[i].height * views[i].spp;
+    pixels += (uint64_t)views[i].width * views[i].height;
+  }
+  if (pixels > 0xFFFFFFFFull) return fail(ctx, NE_ERR_INVALID_ARG, "ne_views_create: too many pixels");
+  NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  ne_views* vw = new ne_views();
+  vw->sc = sc;
+  vw->views.assign(views, views + n);
+  vw->total = total;
+  vw->total_pixels = (uint32_t)pixels;
+  vw->P = pathParams(sc, p);
+  vw->base = baseKey(p);
+  vw->latency.assign(n, 0.0f);
+  sc->view_batches.push_back(vw);
+  cudaError_t e = cudaSuccess;
+  if (e == cudaSuccess) e = cudaMalloc(&vw->d_views, n * sizeof(DView));
+  if (e == cudaSuccess) e = cudaMalloc(&vw->d_paths, total * 3 * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&vw->d_img, pixels * 3 * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&vw->d_done, (2 * (size_t)n + 2) * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaEventCreate(&vw->ev[0]);
+  if (e == cudaSuccess) e = cudaEventCreate(&vw->ev[1]);
+  if (e != cudaSuccess) {
+    ne_views_destroy(vw);
+    return fail(ctx, NE_ERR_OUT_OF_MEMORY, std::string("ne_views_create: ") + cudaGetErrorString(e));
+  }
+  ne_status st = viewsPrepare(vw);
+  if (st) {
+    ne_views_destroy(vw);
+    return st;
+  }
+  *out = vw;
+  return NE_OK;
+}
+
+void ne_views_destroy(ne_views* vw) {
+  if (!vw) return;
+  auto& v = vw->sc->view_batches;
+  v.erase(std::remove(v.begin(), v.end(), vw), v.end());
+  cudaSetDevice(vw->sc->ctx->device);
+  cudaStreamSynchronize(vw->sc->ctx->stream);
+  if (vw->exec) cudaGraphExecDestroy(vw->exec);
+  void* bufs[] = {vw->d_views, vw->d_paths, vw->d_img, vw->d_done};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  for (cudaEvent_t e : vw->ev)
+    if (e) cudaEventDestroy(e);
+  delete vw;
+}
+
+ne_status ne_views_set_tuning(ne_views* vw, const ne_views_tuning* t) {
+  if (!vw || !t || t->fetch < 32 || t->fetch > 4096 || t->fetch % 32 || t->blocks_per_sm < 0 ||
+      t->blocks_per_sm > 64 || t->order < 0 || t->order > 2 || t->graph < 0 || t->graph > 1)
+    return NE_ERR_INVALID_ARG;
+  ne_context* ctx = vw->sc->ctx;
+  NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  vw->tune = *t;
+  return viewsPrepare(vw);
+}
+
+ne_status ne_views_get_tuning(const ne_views* vw, ne_views_tuning* t) {
+  if (!vw || !t) return NE_ERR_INVALID_ARG;
+  *t = vw->tune;
+  return NE_OK;
+}
+
+ne_status ne_views_render(ne_views* vw, ne_views_stats* stats) {
+  if (!vw) return NE_ERR_INVALID_ARG;
+  ne_context* ctx = vw->sc->ctx;
+  NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  const uint32_t n = (uint32_t)vw->views.size();
+  NE_CUDA(cudaEventRecord(vw->ev[0], ctx->stream), "cudaEventRecord");
+  if (vw->exec) {
+    NE_CUDA(cudaGraphLaunch(vw->exec, ctx->stream), "cudaGraphLaunch");
+  } else {
+    ne_status st = viewsEnqueue(vw);
+    if (st) return st;
+  }
+  NE_CUDA(cudaEventRecord(vw->ev[1], ctx->stream), "cudaEventRecord");
+  std::vector<unsigned long long> t(n + 1);
+  NE_CUDA(cudaMemcpyAsync(t.data(), vw->d_done + n, (n + 1) * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                          ctx->stream),
+          "cudaMemcpyAsync");
+  ne_status st = checkErr(ctx);
+  if (st) return st;
+  std::vector<float> lat(n);
+  for (uint32_t s = 0; s < n; s++) {
+    float ms = t[s] >= t[n] ? (float)((double)(t[s] - t[n]) * 1e-6) : 0.0f;
+    vw->latency[vw->order[s]] = ms;
+    lat[s] = ms;
+  }
+  if (stats) {
+    memset(stats, 0, sizeof(*stats));
+    float ems = 0;
+    cudaEventElapsedTime(&ems, vw->ev[0], vw->ev[1]);
+    stats->ms = ems;
+    stats->paths = vw->total;
+    std::sort(lat.begin(), lat.end());
+    auto pct = [&](double q) { return lat[std::min<size_t>(n - 1, (size_t)(q * (n - 1) + 0.5))]; };
+    stats->latency_p50_ms = pct(0.5);
+    stats->latency_p99_ms = pct(0.99);
+    stats->latency_max_ms = lat[n - 1];
+    stats->kernel_launches = 2;
+  }
+  return NE_OK;
+}
+
+ne_status ne_views_autotune(ne_views* vw, int repeats, ne_views_tuning* best, double* best_ms) {
+  if (!vw || repeats < 1) return NE_ERR_INVALID_ARG;
+  ne_context* ctx = vw->sc->ctx;
+  int fit = 1;
+  NE_CUDA(ne_views_occupancy(&fit), "occupancy query");
+  fit = std::max(1, fit);
+  const uint32_t fetches[2] = {32, 128};
+  const int bpss[2] = {fit, std::max(1, fit / 2)};
+  const int orders[2] = {0, 1};
+  ne_views_tuning bt = vw->tune;
+  double bms = 1e30;
+  for (uint32_t f : fetches)
+    for (int b : bpss)
+      for (int o : orders) {
+        ne_views_tuning t = {f, b, o, 1};
+        ne_status st = ne_views_set_tuning(vw, &t);
+        if (st) return st;
+        ne_views_stats s;
+        st = ne_views_render(vw, &s);
+        if (st) return st;
+        double m = 1e30;
+        for (int r = 0; r < repeats; r++) {
+          st = ne_views_render(vw, &s);
+          if (st) return st;
+          m = std::min(m, s.ms);
+        }
+        if (m < bms) {
+          bms = m;
+          bt = t;
+        }
+      }
+  ne_status st = ne_views_set_tuning(vw, &bt);
+  if (st) return st;
+  if (best) *best = bt;
+  if (best_ms) *best_ms = bms;
+  return NE_OK;
+}
+
+ne_status ne_views_latency(const ne_views* vw, float* ms) {
+  if (!vw || !ms) return NE_ERR_INVALID_ARG;
+  memcpy(ms, vw->latency.data(), vw->latency.size() * sizeof(float));
+  return NE_OK;
+}
+
+ne_status ne_views_image(const ne_views* vw, uint32_t v, float* out) {
+  if (!vw || !out || v >= vw->views.size()) return NE_ERR_INVALID_ARG;
+  ne_context* ctx = vw->sc->ctx;
+  NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  const DView& d = vw->dv[vw->slot_of[v]];
+  size_t bytes = (size_t)d.width * d.height * 3 * sizeof(float);
+  NE_CUDA(cudaMemcpyAsync(out, vw->d_img + 3 * (size_t)d.pix_begin, bytes, cudaMemcpyDeviceToHost, ctx->stream),
+          "cudaMemcpyAsync");
+  NE_CUDA(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
   return NE_OK;
 }
 

@@ -1226,19 +1226,26 @@ NE_D Ray cameraRay(const DCamera& cam, float u, float v, Sampler& S) {
   return Ray{pos + offset, -normalize(dir)};
 }
 
-// core/OfflineEngine.cpp:61-68.
+// core/OfflineEngine.cpp:61-68 for a given camera and image size; `stream` selects an
+// independent random stream (views of a batch use their own).
 template <uint32_t K>
-NE_D V3 cameraPath(Ctx<K>& c, const PathParams& P, const nerng::PathKey& base, uint32_t pixel, uint32_t sample) {
-  uint32_t W = (uint32_t)c.s.width;
-  uint32_t x = pixel % W, y = pixel / W;
+NE_D V3 cameraPathCam(Ctx<K>& c, const PathParams& P, const nerng::PathKey& base, const DCamera& cam, int W, int H,
+                      uint32_t pixel, uint32_t sample, uint32_t stream) {
+  uint32_t x = pixel % (uint32_t)W, y = pixel / (uint32_t)W;
   nerng::PathKey k = base;
   k.pixel = pixel;
   k.sample = sample;
+  k.stream = stream;
   c.S.reset(k, 0);
-  float u = (float)((float)(int)x + c.S.random()) / (float)c.s.width;
-  float v = (float)((float)(int)y + c.S.random()) / (float)c.s.height;
-  Ray r = cameraRay(c.s.camera, u, v, c.S);
+  float u = (float)((float)(int)x + c.S.random()) / (float)W;
+  float v = (float)((float)(int)y + c.S.random()) / (float)H;
+  Ray r = cameraRay(cam, u, v, c.S);
   return Li(c, P, r);
+}
+
+template <uint32_t K>
+NE_D V3 cameraPath(Ctx<K>& c, const PathParams& P, const nerng::PathKey& base, uint32_t pixel, uint32_t sample) {
+  return cameraPathCam(c, P, base, c.s.camera, c.s.width, c.s.height, pixel, sample, base.stream);
 }
 
 }  // namespace nedev

@@ -248,6 +248,36 @@ F3 normalize(F3 a) {
 F3 cross(F3 a, F3 b) { return F3{a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y}; }
 void put(float* o, F3 v) { o[0] = v.x; o[1] = v.y; o[2] = v.z; }
 
+// core/Camera.cpp:7-26 Camera::Camera as SceneReader.cpp:650-675 calls it: aperture 0.0001
+// and up (0, 1, 0) whatever the file says.
+void lookAtCamera(const float position[3], const float lookAt[3], float vfov, int W, int H, float focus,
+                  ne_camera* out) {
+  float aspect = float(W) / float(H);
+  float aperture = 0.0001f;
+  F3 upv = F3{0, 1, 0};
+  ne_camera& c = *out;
+  c.lens_radius = aperture / 2.0f;
+  const float toRad = 0.01745329251994329576923690768489f;
+  float half = (vfov * toRad) / 2.0f;
+  float halfHeight = nefm::sin(half) / nefm::cos(half);
+  float halfWidth = aspect * halfHeight;
+  F3 pos = f3(position), la = f3(lookAt);
+  F3 front = normalize(pos - la);
+  F3 side = normalize(cross(upv, front));
+  F3 t1 = (focus * halfWidth) * (-side);
+  F3 t2 = (focus * halfHeight) * upv;
+  F3 t3 = focus * (-front);
+  F3 ll = ((pos - t1) - t2) - t3;
+  F3 hz = ((2.0f * focus) * halfWidth) * (-side);
+  F3 vt = ((2.0f * focus) * halfHeight) * upv;
+  put(c.position, pos);
+  put(c.lower_left, ll);
+  put(c.horizontal, hz);
+  put(c.vertical, vt);
+  put(c.side, side);
+  put(c.up, upv);
+}
+
 }  // namespace
 
 struct ne_scene_host {
@@ -683,31 +713,8 @@ struct Reader {
       focus = 3.0f;  // (position - lookAt).length(): glm's component count
     else
       focus = num(need(cam, "focus", "camera"), "camera focus");
-    float aspect = float(W) / float(H);
-    float aperture = 0.0001f;  // SceneReader.cpp:668 passes 0.0001f, ignoring "aperture"
-    F3 upv = F3{0, 1, 0};      // and glm::vec3(0, 1, 0) as up
     (void)up;
-    ne_camera& c = S.desc.camera;
-    c.lens_radius = aperture / 2.0f;
-    const float toRad = 0.01745329251994329576923690768489f;
-    float half = (vfov * toRad) / 2.0f;
-    float halfHeight = nefm::sin(half) / nefm::cos(half);
-    float halfWidth = aspect * halfHeight;
-    F3 pos = f3(position), la = f3(lookAt);
-    F3 front = normalize(pos - la);
-    F3 side = normalize(cross(upv, front));
-    F3 t1 = (focus * halfWidth) * (-side);
-    F3 t2 = (focus * halfHeight) * upv;
-    F3 t3 = focus * (-front);
-    F3 ll = ((pos - t1) - t2) - t3;
-    F3 hz = ((2.0f * focus) * halfWidth) * (-side);
-    F3 vt = ((2.0f * focus) * halfHeight) * upv;
-    put(c.position, pos);
-    put(c.lower_left, ll);
-    put(c.horizontal, hz);
-    put(c.vertical, vt);
-    put(c.side, side);
-    put(c.up, upv);
+    lookAtCamera(position, lookAt, vfov, W, H, focus, &S.desc.camera);
     ne_settings& st = S.desc.settings;
     st.width = W;
     st.height = H;
@@ -814,3 +821,10 @@ const ne_scene_desc* ne_scene_host_desc(const ne_scene_host* s) { return s ? &s-
 void ne_scene_host_destroy(ne_scene_host* s) { delete s; }
 
 }  // extern "C"
+
+extern "C" ne_status ne_camera_look_at(const float position[3], const float look_at[3], float vfov_deg, int width,
+                                       int height, float focus, ne_camera* out) {
+  if (!position || !look_at || !out || width <= 0 || height <= 0) return NE_ERR_INVALID_ARG;
+  lookAtCamera(position, look_at, vfov_deg, width, height, focus, out);
+  return NE_OK;
+}

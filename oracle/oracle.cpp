@@ -1151,18 +1151,25 @@ Params makeParams(const orc_scene& s, const ne_render_params* p) {
   return P;
 }
 
-// core/OfflineEngine.cpp:61-68: jittered pixel position, camera ray, Li.
-V3 cameraPath(Ctx& c, const Params& P, uint32_t pixel, uint32_t sample) {
-  const ne_settings& st = c.s.d.settings;
-  uint32_t x = pixel % (uint32_t)st.width, y = pixel / (uint32_t)st.width;
+// core/OfflineEngine.cpp:61-68: jittered pixel position, camera ray, Li; for a given
+// camera and image size, on random stream `stream` (0 for the scene's own camera).
+V3 cameraPathCam(Ctx& c, const Params& P, const ne_camera& cam, int W, int H, uint32_t pixel, uint32_t sample,
+                 uint32_t stream) {
+  uint32_t x = pixel % (uint32_t)W, y = pixel / (uint32_t)W;
   c.S.key = P.base;
   c.S.key.pixel = pixel;
   c.S.key.sample = sample;
+  c.S.key.stream = stream;
   c.S.dim = 0;
-  float u = (float)((float)(int)x + c.S.random()) / (float)st.width;
-  float v = (float)((float)(int)y + c.S.random()) / (float)st.height;
-  Ray r = cameraRay(c.s.d.camera, u, v, c.S);
+  float u = (float)((float)(int)x + c.S.random()) / (float)W;
+  float v = (float)((float)(int)y + c.S.random()) / (float)H;
+  Ray r = cameraRay(cam, u, v, c.S);
   return Li(c, P, r);
+}
+
+V3 cameraPath(Ctx& c, const Params& P, uint32_t pixel, uint32_t sample) {
+  const ne_settings& st = c.s.d.settings;
+  return cameraPathCam(c, P, c.s.d.camera, st.width, st.height, pixel, sample, 0);
 }
 
 template <class F>
@@ -1244,6 +1251,21 @@ void orc_trace_paths(const orc_scene* s, const ne_render_params* p, const ne_pat
     Ctx c{*s, Sampler{}, 0};
     for (size_t i = b; i < e; i++) {
       V3 L = cameraPath(c, P, keys[i].pixel, keys[i].sample + off);
+      out[i * 3 + 0] = L.x;
+      out[i * 3 + 1] = L.y;
+      out[i * 3 + 2] = L.z;
+    }
+  });
+}
+
+void orc_trace_view_paths(const orc_scene* s, const ne_render_params* p, const ne_camera* cam, int width, int height,
+                          uint32_t stream, const ne_path_key* keys, size_t n, float* out, int n_threads) {
+  Params P = makeParams(*s, p);
+  uint32_t off = p ? p->sample_offset : 0;
+  parallelFor(n, n_threads, [&](size_t b, size_t e) {
+    Ctx c{*s, Sampler{}, 0};
+    for (size_t i = b; i < e; i++) {
+      V3 L = cameraPathCam(c, P, *cam, width, height, keys[i].pixel, keys[i].sample + off, stream);
       out[i * 3 + 0] = L.x;
       out[i * 3 + 1] = L.y;
       out[i * 3 + 2] = L.z;

@@ -32,6 +32,9 @@ void orc_scene_destroy(orc_scene* s);
 /* Camera path per key (camera draws 0-3, Li from 4), like ne_trace_paths. */
 void orc_trace_paths(const orc_scene* s, const ne_render_params* p, const ne_path_key* keys, size_t n, float* out_L,
                      int n_threads);
+/* Camera paths of a view (camera, size, random stream), like one view of ne_views. */
+void orc_trace_view_paths(const orc_scene* s, const ne_render_params* p, const ne_camera* cam, int width, int height,
+                          uint32_t stream, const ne_path_key* keys, size_t n, float* out_L, int n_threads);
 /* Integrator::Li for given rays, like ne_li_batch. */
 void orc_li_batch(const orc_scene* s, const ne_render_params* p, const ne_ray* rays, const ne_path_key* keys,
                   size_t n, uint32_t first_dim, float* out_L, int n_threads);

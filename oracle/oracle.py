@@ -28,6 +28,8 @@ SIGNATURES = {
     "orc_scene_create": (C.c_void_p, [C.POINTER(_abi.NeSceneDesc)]),
     "orc_scene_destroy": (None, [C.c_void_p]),
     "orc_trace_paths": (None, [C.c_void_p, C.POINTER(NeRenderParams), C.c_void_p, C.c_size_t, C.c_void_p, C.c_int]),
+    "orc_trace_view_paths": (None, [C.c_void_p, C.POINTER(NeRenderParams), C.c_void_p, C.c_int, C.c_int, C.c_uint32,
+                                     C.c_void_p, C.c_size_t, C.c_void_p, C.c_int]),
     "orc_li_batch": (None, [C.c_void_p, C.POINTER(NeRenderParams), C.c_void_p, C.c_void_p, C.c_size_t, C.c_uint32,
                             C.c_void_p, C.c_int]),
     "orc_render": (C.c_double, [C.c_void_p, C.POINTER(NeRenderParams), C.c_void_p, C.c_int]),
@@ -97,6 +99,15 @@ class OracleScene:
         keys = np.ascontiguousarray(keys, dtype=np.uint32).reshape(-1, 2)
         out = np.empty((len(keys), 3), dtype=np.float32)
         self._lib.orc_trace_paths(self._h, C.byref(params), _p(keys), len(keys), _p(out), threads or os.cpu_count())
+        return out
+
+    def trace_view_paths(self, camera, width: int, height: int, stream: int, keys: np.ndarray,
+                         params: NeRenderParams, threads: int = 0) -> np.ndarray:
+        """Camera paths of one view: `camera` is an ne_camera structure (ctypes)."""
+        keys = np.ascontiguousarray(keys, dtype=np.uint32).reshape(-1, 2)
+        out = np.empty((len(keys), 3), dtype=np.float32)
+        self._lib.orc_trace_view_paths(self._h, C.byref(params), C.byref(camera), width, height, stream, _p(keys),
+                                       len(keys), _p(out), threads or os.cpu_count())
         return out
 
     def li_batch(self, rays: np.ndarray, keys: np.ndarray, first_dim: int, params: NeRenderParams,

@@ -1,0 +1,89 @@
+"""Many views in one launch (ne_views) against the oracle, view by view.
+
+Each view's image must equal the oracle's per-pixel mean of the same camera paths (the
+view's camera and size, random stream = view index + 1), summed in sample order, bit for
+bit; the launch order, the fetch size, the resident blocks and the CUDA-graph replay must
+not change any image."""
+import numpy as np
+import pytest
+
+from conftest import scene_path
+
+pytestmark = pytest.mark.gpu
+
+
+def oracle_mean(L, w, h, spp):
+    acc = np.zeros((w * h, 3), np.float32)
+    L = L.reshape(w * h, spp, 3)
+    for k in range(spp):
+        acc = (acc + L[:, k]).astype(np.float32)
+    return (acc / np.float32(spp)).reshape(h, w, 3)
+
+
+@pytest.fixture(scope="module", params=["cornell_c1", "medium_c2"])
+def batch(request, built, oracle_lib):
+    import narvalengine_gb300 as ne
+    ctx = ne.Context(0)
+    host = ne.SceneHost.from_json(scene_path(request.param))
+    scene = ctx.upload(host)
+    cam0 = host.desc.camera
+    look = [0, 1, 0] if request.param == "cornell_c1" else [0, 0, 0]
+    eye = list(cam0.position)
+    sizes = [(32, 32, 3), (48, 24, 2), (16, 16, 4), (40, 56, 1), (64, 40, 2)]
+    views = []
+    for i, (w, h, spp) in enumerate(sizes):
+        pos = [eye[0] + 0.15 * i, eye[1] + 0.05 * i, eye[2]]
+        views.append((ne.camera_look_at(pos, look, 50.0 + 3 * i, w, h), w, h, spp))
+    vb = ne.Views(scene, views, seed=11)
+    orc = oracle_lib.OracleScene(host.desc_ptr)
+    yield ne, scene, vb, views, orc
+    orc.close()
+    vb.close()
+    ctx.close()
+
+
+def oracle_images(ne, orc, views):
+    out = []
+    p = ne.render_params(seed=11)
+    for v, (cam, w, h, spp) in enumerate(views):
+        keys = np.array([[px, s] for px in range(w * h) for s in range(spp)], np.uint32)
+        L = orc.trace_view_paths(cam, w, h, v + 1, keys, p)
+        out.append(oracle_mean(L, w, h, spp))
+    return out
+
+
+def test_views_match_oracle(batch):
+    ne, scene, vb, views, orc = batch
+    st = vb.render()
+    assert st["paths"] == sum(w * h * s for _, w, h, s in views)
+    want = oracle_images(ne, orc, views)
+    for v in range(len(views)):
+        got = vb.image(v)
+        assert np.array_equal(got.view(np.uint32), want[v].view(np.uint32)), f"view {v}"
+
+
+def test_tunings_do_not_change_images(batch):
+    ne, scene, vb, views, orc = batch
+    vb.set_tuning(fetch=32, order=0, graph=False)
+    vb.render()
+    ref = [vb.image(v) for v in range(len(views))]
+    for fetch, bps, order, graph in [(128, 0, 1, True), (64, 2, 2, True), (32, 1, 1, False)]:
+        vb.set_tuning(fetch=fetch, blocks_per_sm=bps, order=order, graph=graph)
+        st = vb.render()
+        for v in range(len(views)):
+            assert np.array_equal(vb.image(v), ref[v]), (fetch, bps, order, graph, v)
+        lat = vb.latency()
+        assert np.all(lat > 0) and lat.max() <= st["ms"] * 1.5 + 1.0, (lat, st)
+        assert st["latency_p50_ms"] <= st["latency_p99_ms"] <= st["latency_max_ms"]
+
+
+def test_autotune(batch):
+    ne, scene, vb, views, orc = batch
+    vb.render()
+    ref = [vb.image(v) for v in range(len(views))]
+    best, ms = vb.autotune(repeats=1)
+    assert ms > 0 and best["fetch"] in (32, 128) and best["order"] in (0, 1) and best["graph"] == 1
+    assert vb.tuning() == best
+    vb.render()
+    for v in range(len(views)):
+        assert np.array_equal(vb.image(v), ref[v])
