@@ -220,9 +220,10 @@ ne_status ne_views_create(ne_scene* scene, const ne_view* views, uint32_t n, con
 void ne_views_destroy(ne_views* views);
 ne_status ne_views_set_tuning(ne_views* views, const ne_views_tuning* tuning);
 ne_status ne_views_get_tuning(const ne_views* views, ne_views_tuning* tuning);
-/* Times every candidate configuration (fetch 32/128, all or half the resident blocks, given
- * or largest-first order, as a graph) `repeats` times after one warm-up batch, keeps the
- * fastest and returns it with its time. */
+/* Times every candidate configuration (fetch 32/128, all or half the resident blocks, given,
+ * largest-first or smallest-first order, as a graph) `repeats` times after one warm-up batch;
+ * among those within 3% of the fastest it keeps the one with the lowest median view latency,
+ * and returns it with its time. */
 ne_status ne_views_autotune(ne_views* views, int repeats, ne_views_tuning* best, double* best_ms);
 ne_status ne_views_render(ne_views* views, ne_views_stats* stats);
 /* Completion latency of each view of the last batch, in the caller's order (n floats, ms). */

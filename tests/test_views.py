@@ -82,7 +82,7 @@ def test_autotune(batch):
     vb.render()
     ref = [vb.image(v) for v in range(len(views))]
     best, ms = vb.autotune(repeats=1)
-    assert ms > 0 and best["fetch"] in (32, 128) and best["order"] in (0, 1) and best["graph"] == 1
+    assert ms > 0 and best["fetch"] in (32, 128) and best["order"] in (0, 1, 2) and best["graph"] == 1
     assert vb.tuning() == best
     vb.render()
     for v in range(len(views)):
