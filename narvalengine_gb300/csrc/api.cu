@@ -79,7 +79,12 @@ struct ne_scene {
   float* d_paths = nullptr;  // per-path radiance scratch of ne_render
   size_t paths_cap = 0;
   int blocks_per_sm = 1;
-  int variant = 0;           // path kernel: 0 straight k_paths, 1 regrouped k_sched
+  int variant = 0;           // path kernel: 0 straight, 1 regrouped, 2 lane refill, 3 split
+  PathState* d_defer = nullptr;  // split renders: deferred paths
+  size_t defer_cap = 0;
+  DeferQueue* d_dq = nullptr;
+  uint32_t* d_dcount = nullptr;
+  DeferQueue dq;
   int track_share = 16;      // k_sched tracking-phase threshold (32nds of live lanes)
   uint32_t features = 0;     // FT_* bits of the scene
   uint32_t feature_set = 0;  // compiled kernel specialisation covering them
@@ -378,6 +383,32 @@ ne_status launchPaths(ne_scene* sc, const PathArgs& a, bool count) {
   if ((unsigned long long)blocks > needed) blocks = (int)std::max<unsigned long long>(1, needed);
   PathArgs b = a;
   b.track_share = sc->track_share;
+  if (sc->variant == 3 && !count) {
+    // split render: paths that scatter are queued (up to a quarter of the paths; the rest
+    // finish in the first pass) and resumed, packed together, by the second pass
+    size_t cap = std::max<size_t>(1024, (size_t)(a.total / 4));
+    if (sc->defer_cap < cap) {
+      if (sc->d_defer) cudaFree(sc->d_defer);
+      sc->d_defer = nullptr;
+      sc->defer_cap = 0;
+      NE_CUDA(cudaMalloc(&sc->d_defer, cap * sizeof(PathState)), "cudaMalloc(deferred paths)");
+      sc->defer_cap = cap;
+    }
+    if (!sc->d_dq) NE_CUDA(cudaMalloc(&sc->d_dq, sizeof(DeferQueue)), "cudaMalloc");
+    if (!sc->d_dcount) NE_CUDA(cudaMalloc(&sc->d_dcount, sizeof(uint32_t)), "cudaMalloc");
+    sc->dq.items = sc->d_defer;
+    sc->dq.count = sc->d_dcount;
+    sc->dq.cap = (uint32_t)std::min<size_t>(sc->defer_cap, 0xFFFFFFFFu);
+    NE_CUDA(cudaMemcpyAsync(sc->d_dq, &sc->dq, sizeof(DeferQueue), cudaMemcpyHostToDevice, ctx->stream),
+            "cudaMemcpyAsync");
+    NE_CUDA(cudaMemsetAsync(sc->d_dcount, 0, sizeof(uint32_t), ctx->stream), "cudaMemsetAsync");
+    b.defer = sc->d_dq;
+    NE_CUDA(ne_launch_path_split(0, blocks, ctx->stream, sc->d, b, ctx->d_counter, ctx->d_err), "path kernel launch");
+    NE_CUDA(cudaMemsetAsync(ctx->d_counter, 0, sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync");
+    NE_CUDA(ne_launch_path_split(1, persistentBlocks(sc), ctx->stream, sc->d, b, ctx->d_counter, ctx->d_err),
+            "resume kernel launch");
+    return NE_OK;
+  }
   NE_CUDA(ne_launch_path_kernel(sc->variant, sc->feature_set, count, blocks, ctx->stream, sc->d, b, ctx->d_counter,
                                 ctx->d_err),
           "path kernel launch");
@@ -396,7 +427,8 @@ uint32_t ne_feature_set_for(uint32_t f) {
 template <uint32_t K>
 static cudaError_t launchK(int kernel, int blocks, cudaStream_t st, const DScene& s, const PathArgs& a,
                            unsigned long long* counter, uint32_t* err) {
-  if (kernel == 0) return launchPathKernel<0, K>(blocks, st, s, a, counter, err);
+  // kernel 3 (split) runs through launchPaths; callers without its queue use the straight kernel
+  if (kernel == 0 || kernel == 3) return launchPathKernel<0, K>(blocks, st, s, a, counter, err);
   if (kernel == 1) return launchPathKernel<1, K>(blocks, st, s, a, counter, err);
   return launchPathKernel<2, K>(blocks, st, s, a, counter, err);
 }
@@ -405,6 +437,7 @@ template <uint32_t K>
 static cudaError_t occupancyK(int kernel, int* bps) {
   if (kernel == 0) return pathKernelOccupancy<0, K>(bps);
   if (kernel == 1) return pathKernelOccupancy<1, K>(bps);
+  if (kernel == 3) return ne_path_split_occupancy(bps);
   return pathKernelOccupancy<2, K>(bps);
 }
 
@@ -963,10 +996,12 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
 }
 
 ne_status ne_scene_set_tuning(ne_scene* sc, const ne_tuning* t) {
-  if (!sc || !t || t->kernel < 0 || t->kernel > 2 || t->track_share < 1 || t->track_share > 32 ||
+  if (!sc || !t || t->kernel < 0 || t->kernel > 3 || t->track_share < 1 || t->track_share > 32 ||
       t->blocks_per_sm < 0 || t->blocks_per_sm > 64)
     return NE_ERR_INVALID_ARG;
   ne_context* ctx = sc->ctx;
+  if (t->kernel == 3 && sc->feature_set != K_VOLUME)
+    return fail(ctx, NE_ERR_UNSUPPORTED, "the split kernel is compiled for grid-medium scenes only");
   int fit = 1;
   cudaError_t e = ne_path_kernel_occupancy(t->kernel, sc->feature_set, &fit);
   if (e != cudaSuccess) return cudaFail(ctx, e, "occupancy query");
@@ -995,6 +1030,9 @@ void ne_scene_destroy(ne_scene* sc) {
   cudaStreamSynchronize(sc->ctx->stream);
   for (void* p : sc->allocs) cudaFree(p);
   if (sc->d_paths) cudaFree(sc->d_paths);
+  if (sc->d_defer) cudaFree(sc->d_defer);
+  if (sc->d_dq) cudaFree(sc->d_dq);
+  if (sc->d_dcount) cudaFree(sc->d_dcount);
   delete sc;
 }
 

@@ -37,6 +37,7 @@ struct PathArgs {
   float* out;                // total * 3 floats
   int track_share;           // regrouped kernel: tracking-phase threshold in 32nds of live lanes
   const CacheIO* cache = nullptr;  // K_CACHE kernels: device copy of the cache buffers
+  const DeferQueue* defer = nullptr;  // K_SPLIT kernels: device copy of the deferred-path queue
 };
 
 // Training paths of a cached render: a multiplicative hash of the path index, so training
@@ -67,7 +68,7 @@ __device__ __forceinline__ void flushCounters(const Counters& cn, unsigned long 
 template <uint32_t K>
 __global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_paths(const __grid_constant__ DScene s, const PathArgs a,
                                                     unsigned long long* __restrict__ counter, uint32_t* err) {
-  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, a.cache};
+  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, a.cache, a.defer, 0ull, false};
   const int lane = threadIdx.x & 31;
   for (;;) {
     unsigned long long base = 0;
@@ -80,6 +81,10 @@ __global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_paths(const __grid
         c.pidx = (uint32_t)idx;
         c.train = isTrainingPath(idx, a.cache->train_stride);
       }
+      if (K & K_SPLIT) {
+        c.idx = idx;
+        c.deferred = false;
+      }
       uint32_t pixel, sample;
       if (a.keys) {
         ne_path_key k = a.keys[idx];
@@ -91,12 +96,43 @@ __global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_paths(const __grid
         pixel = (pi / a.cover_w) * (uint32_t)s.width + (pi % a.cover_w);
       }
       V3 L = cameraPath(c, a.P, a.base, pixel, sample);
-      a.out[3 * idx + 0] = L.x;
-      a.out[3 * idx + 1] = L.y;
-      a.out[3 * idx + 2] = L.z;
+      if (!((K & K_SPLIT) && c.deferred)) {
+        a.out[3 * idx + 0] = L.x;
+        a.out[3 * idx + 1] = L.y;
+        a.out[3 * idx + 2] = L.z;
+      }
     }
   }
   flushCounters<K>(c.c, counter);
+}
+
+// Second pass of a split render: warps take 32 deferred paths at a time and run each from
+// its saved scattering point to the end (same operations and draws as an undivided path).
+template <uint32_t K>
+__global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_resume(const __grid_constant__ DScene s,
+                                                                     const PathArgs a,
+                                                                     unsigned long long* __restrict__ counter,
+                                                                     uint32_t* err) {
+  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, nullptr, nullptr, 0ull, false};
+  const DeferQueue& q = *a.defer;
+  const unsigned long long n = min(*q.count, q.cap);
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(&counter[0], 32ull);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= n) break;
+    unsigned long long i = base + (unsigned long long)lane;
+    if (i < n) {
+      const PathState& ps = q.items[i];
+      LiVars v = ps.v;
+      c.S.reset(ps.key, ps.dim);
+      V3 L = liLoop(c, a.P, v, true);
+      a.out[3 * ps.idx + 0] = L.x;
+      a.out[3 * ps.idx + 1] = L.y;
+      a.out[3 * ps.idx + 2] = L.z;
+    }
+  }
 }
 
 // Straight kernel with lane-level refill: a lane that finishes its path takes the next
@@ -106,7 +142,7 @@ template <uint32_t K>
 __global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_lanes(const __grid_constant__ DScene s, const PathArgs a,
                                                     unsigned long long* __restrict__ counter, uint32_t* err) {
   namespace cg = cooperative_groups;
-  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, nullptr};
+  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, nullptr, nullptr, 0ull, false};
   for (;;) {
     cg::coalesced_group g = cg::coalesced_threads();
     unsigned long long base = 0;
@@ -187,6 +223,12 @@ cudaError_t ne_launch_path_kernel(int kernel, uint32_t set, bool count, int bloc
                                   const nedev::DScene& s, const nedev::PathArgs& a, unsigned long long* counter,
                                   uint32_t* err);
 cudaError_t ne_path_kernel_occupancy(int kernel, uint32_t set, int* blocks_per_sm);
+// Split render of grid-medium scenes: first pass (deferring paths at their first scattering
+// event into a->defer) and the resume pass over the deferred paths; counter[0] must be zero
+// before each.
+cudaError_t ne_launch_path_split(int pass, int blocks, cudaStream_t st, const nedev::DScene& s,
+                                 const nedev::PathArgs& a, unsigned long long* counter, uint32_t* err);
+cudaError_t ne_path_split_occupancy(int* blocks_per_sm);
 // The straight kernel over grid-medium scenes with paths ending in the radiance cache.
 cudaError_t ne_launch_path_kernel_cache(int blocks, cudaStream_t st, const nedev::DScene& s, const nedev::PathArgs& a,
                                         unsigned long long* counter, uint32_t* err);

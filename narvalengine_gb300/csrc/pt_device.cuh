@@ -66,6 +66,7 @@ enum : uint32_t {
   FT_ALL = (1u << 14) - 1,
   K_COUNT = 1u << 31,
   K_CACHE = 1u << 30,  // paths end in the learned radiance cache (see CacheIO)
+  K_SPLIT = 1u << 29,  // paths are deferred at their first medium scattering (see DeferQueue)
   // feature sets with a compiled kernel (the host picks the smallest superset)
   K_VOLUME = FT_AABB | FT_POINT | FT_SPHERE | FT_VOLBSDF | FT_GRID | FT_LDIR | FT_LINF,
   K_SURFACE = FT_RECT | FT_SPHERE | FT_GLOSSY | FT_LDIFF,
@@ -185,6 +186,10 @@ struct Ctx {
   uint32_t pidx;
   bool train;
   const struct CacheIO* cio;
+  // K_SPLIT only: the queue of deferred paths; set when the current path was deferred
+  const struct DeferQueue* dq;
+  unsigned long long idx;
+  bool deferred;
 };
 
 // Buffers of a render that ends paths in the learned radiance cache. A path that reaches
@@ -1109,93 +1114,142 @@ struct PathParams {
   int rr_after;
 };
 
+// Everything Li keeps across its bounce loop.
+struct LiVars {
+  V3 L, T;
+  Ray incoming, scattered;
+  Hit isect;
+  int b, passes;
+};
+
+// A path deferred at its first scattering event in a grid medium, right after the
+// throughput took the medium's sampled albedo: the loop state, the sampler position and
+// the index of the path's radiance slot.
+struct PathState {
+  LiVars v;
+  nerng::PathKey key;
+  uint32_t dim;
+  unsigned long long idx;
+};
+
+struct DeferQueue {
+  PathState* items;
+  uint32_t* count;
+  uint32_t cap;
+};
+
 // integrators/VolumetricPathIntegrator.cpp:176-301 Li, plus the optional Russian
-// roulette of resources/shaders/MS_monteCarlo.frag:539-544.
+// roulette of resources/shaders/MS_monteCarlo.frag:539-544, written as a loop over `v` that
+// can start at the scattering point where a K_SPLIT path was deferred (`resume`): every
+// operation and every random draw happens in the same order either way.
 template <uint32_t K>
-NE_D V3 Li(Ctx<K>& c, const PathParams& P, Ray incoming) {
+NE_D V3 liLoop(Ctx<K>& c, const PathParams& P, LiVars& v, bool resume) {
   const DScene& s = c.s;
   const float inf = __int_as_float(0x7f800000);
-  V3 L = v3(0, 0, 0);
-  V3 T = v3(1, 1, 1);
-  Hit isect = emptyHit();
-  int passes = 0;
   // K_CACHE training paths: the vertex the sample is recorded at
   bool recorded = false;
   V3 vPos = v3(0, 0, 0), vDir = v3(0, 0, 0), vL = v3(0, 0, 0), vT = v3(0, 0, 0);
-  for (int b = 0; b < P.bounces; b++) {
-    bool did = intersectScene(c, incoming, isect, kEps12F, inf);
-    if (isBlack(T)) break;
-    const DMaterial* mat = did ? matOf(s, isect.prim) : nullptr;
-    if ((K & FT_VOLBSDF) && did && mat && mat->bsdf == NE_BSDF_VOLUME) {
-      incoming.o = incoming.at(isect.tNear);
-      isect.tFar = isect.tFar - isect.tNear;
-      isect.tNear = 0;
-      Ray scattered{v3(0, 0, 0), v3(0, 0, 0)};
-      V3 sampledT = mediumSample(c, mat->medium, incoming, scattered, isect);
-      if (areAllOne(sampledT)) {
-        incoming.o = incoming.at(isect.tFar + 0.01f);
-        if (++passes >= kMaxPassThrough) break;
-        b--;
-        continue;
-      }
-      T = T * sampledT;
-      if ((K & K_CACHE) && b >= c.cio->bounce && !recorded) {
-        V3 xo = mul4(s.instances[isect.inst].ocs, scattered.o, 1.0f);
-        if (!c.train) {
-          const CacheIO& io = *c.cio;
-          uint32_t q = appendSlot(io.q_count);
-          if (q < io.q_cap) {
-            io.q_pos[3 * q] = xo.x; io.q_pos[3 * q + 1] = xo.y; io.q_pos[3 * q + 2] = xo.z;
-            io.q_dir[3 * q] = incoming.d.x; io.q_dir[3 * q + 1] = incoming.d.y; io.q_dir[3 * q + 2] = incoming.d.z;
-            io.q_thr[3 * q] = T.x; io.q_thr[3 * q + 1] = T.y; io.q_thr[3 * q + 2] = T.z;
-            io.q_idx[q] = c.pidx;
-          }
-          return L;
+  for (; v.b < P.bounces; v.b++) {
+    const int b = v.b;
+    bool did = true;
+    const DMaterial* mat;
+    bool medium;
+    if ((K & K_SPLIT) && resume) {
+      resume = false;
+      mat = matOf(s, v.isect.prim);
+      medium = true;
+    } else {
+      did = intersectScene(c, v.incoming, v.isect, kEps12F, inf);
+      if (isBlack(v.T)) break;
+      mat = did ? matOf(s, v.isect.prim) : nullptr;
+      medium = (K & FT_VOLBSDF) && did && mat && mat->bsdf == NE_BSDF_VOLUME;
+      if (medium) {
+        v.incoming.o = v.incoming.at(v.isect.tNear);
+        v.isect.tFar = v.isect.tFar - v.isect.tNear;
+        v.isect.tNear = 0;
+        v.scattered = Ray{v3(0, 0, 0), v3(0, 0, 0)};
+        V3 sampledT = mediumSample(c, mat->medium, v.incoming, v.scattered, v.isect);
+        if (areAllOne(sampledT)) {
+          v.incoming.o = v.incoming.at(v.isect.tFar + 0.01f);
+          if (++v.passes >= kMaxPassThrough) break;
+          v.b--;
+          continue;
         }
-        recorded = true;
-        vPos = xo;
-        vDir = incoming.d;
-        vL = L;
-        vT = T;
+        v.T = v.T * sampledT;
+        if ((K & K_SPLIT) && b == 0) {
+          const DeferQueue& q = *c.dq;
+          uint32_t slot = appendSlot(q.count);
+          if (slot < q.cap) {
+            PathState& ps = q.items[slot];
+            ps.v = v;
+            ps.key = c.S.key;
+            ps.dim = c.S.dim;
+            ps.idx = c.idx;
+            c.deferred = true;
+            return v.L;
+          }
+        }
+        if ((K & K_CACHE) && b >= c.cio->bounce && !recorded) {
+          V3 xo = mul4(s.instances[v.isect.inst].ocs, v.scattered.o, 1.0f);
+          if (!c.train) {
+            const CacheIO& io = *c.cio;
+            uint32_t q = appendSlot(io.q_count);
+            if (q < io.q_cap) {
+              io.q_pos[3 * q] = xo.x; io.q_pos[3 * q + 1] = xo.y; io.q_pos[3 * q + 2] = xo.z;
+              io.q_dir[3 * q] = v.incoming.d.x; io.q_dir[3 * q + 1] = v.incoming.d.y;
+              io.q_dir[3 * q + 2] = v.incoming.d.z;
+              io.q_thr[3 * q] = v.T.x; io.q_thr[3 * q + 1] = v.T.y; io.q_thr[3 * q + 2] = v.T.z;
+              io.q_idx[q] = c.pidx;
+            }
+            return v.L;
+          }
+          recorded = true;
+          vPos = xo;
+          vDir = v.incoming.d;
+          vL = v.L;
+          vT = v.T;
+        }
       }
-      V3 phaseFr = bsdfEval<K>(*mat, incoming.d, scattered.d, isect.normal);
-      float phasePdf = bsdfPdf<K>(*mat, incoming.d, scattered.d, isect.normal);
+    }
+    if (medium) {
+      V3 phaseFr = bsdfEval<K>(*mat, v.incoming.d, v.scattered.d, v.isect.normal);
+      float phasePdf = bsdfPdf<K>(*mat, v.incoming.d, v.scattered.d, v.isect.normal);
       if (isBlack(phaseFr) || phasePdf == 0.f) break;
-      V3 lightSample = uniformSampleOneLight(c, scattered, isect);
-      T = T * (phaseFr / phasePdf);
-      L = L + T * lightSample;
-      incoming = scattered;
+      V3 lightSample = uniformSampleOneLight(c, v.scattered, v.isect);
+      v.T = v.T * (phaseFr / phasePdf);
+      v.L = v.L + v.T * lightSample;
+      v.incoming = v.scattered;
     } else {
       if (b == 0) {
         if (did && mat && mat->light >= 0) {
-          L = L + T * lightLi(s.lights[mat->light]);
+          v.L = v.L + v.T * lightLi(s.lights[mat->light]);
         } else {
           for (uint32_t li = 0; li < s.n_light_instances; li++) {
             const DModel& lm = s.models[s.instances[s.n_instances + li].model];
             for (uint32_t k = 0; k < lm.mat_count; k++) {
               const DMaterial& mm = s.materials[s.model_materials[lm.mat_begin + k]];
-              L = L + T * lightLe(s.lights[mm.light]);
+              v.L = v.L + v.T * lightLe(s.lights[mm.light]);
             }
           }
         }
       }
       if (!did || !mat || mat->bsdf == NE_BSDF_NONE) break;
-      L = L + T * uniformSampleOneLight(c, incoming, isect);
+      v.L = v.L + v.T * uniformSampleOneLight(c, v.incoming, v.isect);
       Ray scattered;
-      scattered.o = isect.hitPoint;
-      scattered.d = bsdfSample<K>(*mat, incoming.d, isect.normal, c.S);
-      float pdf = bsdfPdf<K>(*mat, incoming.d, scattered.d, isect.normal);
-      V3 fr = bsdfEval<K>(*mat, incoming.d, scattered.d, isect.normal);
+      scattered.o = v.isect.hitPoint;
+      scattered.d = bsdfSample<K>(*mat, v.incoming.d, v.isect.normal, c.S);
+      float pdf = bsdfPdf<K>(*mat, v.incoming.d, scattered.d, v.isect.normal);
+      V3 fr = bsdfEval<K>(*mat, v.incoming.d, scattered.d, v.isect.normal);
       if (isBlack(fr) || pdf == 0.f) break;
-      T = T * ((fr * absDot(incoming.d, isect.normal)) / pdf);
-      incoming = scattered;
+      v.T = v.T * ((fr * absDot(v.incoming.d, v.isect.normal)) / pdf);
+      v.incoming = scattered;
     }
     if (P.rr && b > P.rr_after) {
-      float mx = maxc(T);
+      float mx = maxc(v.T);
       if (mx < 0.01f) {
         float q = gmax(0.05f, 1.0f - mx);
         if (c.S.random() < q) break;
-        T = T / (1.0f - q);
+        v.T = v.T / (1.0f - q);
       }
     }
   }
@@ -1203,7 +1257,7 @@ NE_D V3 Li(Ctx<K>& c, const PathParams& P, Ray incoming) {
     const CacheIO& io = *c.cio;
     uint32_t q = appendSlot(io.t_count);
     if (q < io.t_cap) {
-      V3 d = L - vL;
+      V3 d = v.L - vL;
       io.t_pos[3 * q] = vPos.x; io.t_pos[3 * q + 1] = vPos.y; io.t_pos[3 * q + 2] = vPos.z;
       io.t_dir[3 * q] = vDir.x; io.t_dir[3 * q + 1] = vDir.y; io.t_dir[3 * q + 2] = vDir.z;
       io.t_val[3 * q] = vT.x > 0 ? d.x / vT.x : 0.0f;
@@ -1211,7 +1265,20 @@ NE_D V3 Li(Ctx<K>& c, const PathParams& P, Ray incoming) {
       io.t_val[3 * q + 2] = vT.z > 0 ? d.z / vT.z : 0.0f;
     }
   }
-  return L;
+  return v.L;
+}
+
+template <uint32_t K>
+NE_D V3 Li(Ctx<K>& c, const PathParams& P, Ray incoming) {
+  LiVars v;
+  v.L = v3(0, 0, 0);
+  v.T = v3(1, 1, 1);
+  v.incoming = incoming;
+  v.scattered = Ray{v3(0, 0, 0), v3(0, 0, 0)};
+  v.isect = emptyHit();
+  v.b = 0;
+  v.passes = 0;
+  return liLoop(c, P, v, false);
 }
 
 // core/Camera.cpp:140-144 with utils/Math.h:502-507.

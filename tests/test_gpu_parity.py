@@ -29,10 +29,11 @@ def ctx(ne):
     c.close()
 
 
-KERNELS = {0: "straight", 1: "regrouped", 2: "lanes"}
+KERNELS = {0: "straight", 1: "regrouped", 2: "lanes", 3: "split"}
 
 
-@pytest.fixture(scope="module", params=[(s, k) for s in ("cornell_c1", "medium_c2") for k in KERNELS],
+@pytest.fixture(scope="module", params=[(s, k) for s in ("cornell_c1", "medium_c2") for k in KERNELS
+                                        if k != 3 or s == "medium_c2"],
                 ids=lambda p: f"{p[0]}-{KERNELS[p[1]]}")
 def scenes(request, ne, ctx, oracle_lib):
     name, kernel = request.param
@@ -196,14 +197,18 @@ def test_kernels_and_tunings_agree(ne, ctx):
     scene = ctx.upload(host)
     p = ne.render_params(seed=21, spp=2)
     ref = None
-    for kernel, share, bps in [(0, 16, 0), (0, 16, 1), (1, 16, 0), (1, 1, 0), (1, 32, 0), (1, 8, 1), (2, 16, 0), (2, 16, 1)]:
+    for kernel, share, bps in [(0, 16, 0), (0, 16, 1), (1, 16, 0), (1, 1, 0), (1, 32, 0), (1, 8, 1), (2, 16, 0), (2, 16, 1),
+                               (3, 16, 0), (3, 16, 1)]:
         scene.set_tuning(kernel=kernel, track_share=share, blocks_per_sm=bps)
         img, stats = scene.render(p)
         if ref is None:
             ref = img
         assert np.array_equal(img, ref), (kernel, share, bps)
     with pytest.raises(ne.NarvalError):
-        scene.set_tuning(kernel=3)
+        scene.set_tuning(kernel=4)
+    cornell = ctx.upload(ne.SceneHost.from_json(scene_path("cornell_c1")))
+    with pytest.raises(ne.NarvalError):
+        cornell.set_tuning(kernel=3)
     with pytest.raises(ne.NarvalError):
         scene.set_tuning(kernel=1, track_share=0)
 
@@ -298,6 +303,27 @@ def test_dense_cloud_parity(ne, ctx, oracle_lib):
         img, _ = scene.render(seed=2, spp=2)
         ref, _ = orc.render(ne.render_params(seed=2, spp=2))
         assert np.array_equal(img.view(np.uint32), ref.view(np.uint32))
+    finally:
+        scene.close()
+        orc.close()
+
+
+def test_split_queue_overflow(ne, ctx, oracle_lib):
+    """The split kernel's queue holds a quarter of the paths (at least 1024). All paths here
+    start through the dense centre of the medium, so far more than a quarter scatter; those
+    beyond the queue finish in the first pass, and every path still matches the oracle bit
+    for bit."""
+    host = ne.SceneHost.from_json(scene_path("medium_c2"))
+    scene = ctx.upload(host)
+    scene.set_tuning(kernel=3)
+    orc = oracle_lib.OracleScene(host.desc_ptr)
+    try:
+        centre = (host.height // 2) * host.width + host.width // 2
+        keys = np.array([[centre, s] for s in range(8192)], np.uint32)
+        p = ne.render_params(seed=5)
+        g = scene.trace_paths(keys, p)
+        c = orc.trace_paths(keys, p)
+        assert np.array_equal(g.view(np.uint32), c.view(np.uint32))
     finally:
         scene.close()
         orc.close()
