@@ -318,8 +318,9 @@ def main():
     ap.add_argument("--scene", default="medium_c2", choices=sorted(WORKLOADS),
                     help="workload (the default is the configuration the metric is quoted on)")
     ap.add_argument("--kernel", type=int, default=-1,
-                    help="path kernel (ne_tuning.kernel): 0 straight, 1 regrouped, 2 lane refill; "
+                    help="path kernel (ne_tuning.kernel): 0 straight, 1 regrouped, 2 lane refill, 3 split; "
                          "default: the library's choice for the scene")
+    ap.add_argument("--split-passes", type=int, default=0, help="split kernel passes (0: library default)")
     ap.add_argument("--track-share", type=int, default=16, help="regrouped kernel tracking threshold, 32nds")
     ap.add_argument("--profile-spp", type=int, default=0,
                     help="profiling case: two renders of the workload at this spp (the second is the one to capture)")
@@ -346,7 +347,7 @@ def main():
     host = ne.SceneHost.from_json(os.path.join(ne.SCENES_DIR, SCENE))
     scene = ctx.upload(host)
     if args.kernel >= 0:
-        scene.set_tuning(kernel=args.kernel, track_share=args.track_share)
+        scene.set_tuning(kernel=args.kernel, track_share=args.track_share, split_passes=args.split_passes)
     W, H, spp = host.width, host.height, host.spp
     paths_per_step = W * H * spp
     img_bytes = W * H * 3 * 4
@@ -389,7 +390,7 @@ def main():
     for _ in range(1):
         s2 = ctx.upload(host)
         if args.kernel >= 0:
-            s2.set_tuning(kernel=args.kernel, track_share=args.track_share)
+            s2.set_tuning(kernel=args.kernel, track_share=args.track_share, split_passes=args.split_passes)
         s2.render(pe, out=out_host)
         s2.close()
     d.barrier()
@@ -397,7 +398,7 @@ def main():
     for _ in range(args.steps):
         s2 = ctx.upload(host)
         if args.kernel >= 0:
-            s2.set_tuning(kernel=args.kernel, track_share=args.track_share)
+            s2.set_tuning(kernel=args.kernel, track_share=args.track_share, split_passes=args.split_passes)
         s2.render(pe, out=out_host)
         s2.close()
     e2e_s = time.perf_counter() - t0
@@ -413,7 +414,9 @@ def main():
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": peak_kind, "traffic": None,
                 "kernel": {0: "k_paths (straight path kernel)", 1: "k_sched (regrouped path kernel)",
-                           2: "k_lanes (lane-refill path kernel)"}.get(scene.tuning()["kernel"]),
+                           2: "k_lanes (lane-refill path kernel)",
+                           3: "k_paths + k_resume (split path kernel, passes as in config.tuning)"}.get(
+                               scene.tuning()["kernel"]),
                 "algorithmic_bytes_per_launch": alg_bytes,
                 "bytes_rule": "32 B per density lookup + 32 B per BVH node visit + 36 B per triangle test",
                 "density_lookups_per_launch": lookups, "scene_queries_per_launch": cstats["scene_queries"],

@@ -171,7 +171,9 @@ typedef struct ne_tuning {
   int32_t kernel;
   int32_t track_share;
   int32_t blocks_per_sm;
-  int32_t pad;
+  int32_t split_passes;  /* kernel 3: passes, 2..16 (0: 3); pass p > 0 resumes the paths queued
+                            at bounce p - 1 and queues them again at bounce p, the last runs
+                            them to the end */
 } ne_tuning;
 
 ne_status ne_scene_set_tuning(ne_scene* scene, const ne_tuning* tuning);

@@ -262,15 +262,16 @@ class Scene:
         return (img, {f: getattr(stats, f) for f, _ in NeRenderStats._fields_},
                 {f: getattr(cst, f) for f, _ in _abi.NeCacheRenderStats._fields_})
 
-    def set_tuning(self, kernel: int = 0, track_share: int = 16, blocks_per_sm: int = 0):
+    def set_tuning(self, kernel: int = 0, track_share: int = 16, blocks_per_sm: int = 0, split_passes: int = 0):
         """Launch configuration of the path kernels (see ne_tuning in include/narval_gb300.h)."""
-        t = _abi.NeTuning(kernel, track_share, blocks_per_sm, 0)
+        t = _abi.NeTuning(kernel, track_share, blocks_per_sm, split_passes)
         self.ctx.check(library().ne_scene_set_tuning(self._h, C.byref(t)))
 
     def tuning(self) -> dict:
         t = _abi.NeTuning()
         self.ctx.check(library().ne_scene_get_tuning(self._h, C.byref(t)))
-        return {"kernel": t.kernel, "track_share": t.track_share, "blocks_per_sm": t.blocks_per_sm}
+        return {"kernel": t.kernel, "track_share": t.track_share, "blocks_per_sm": t.blocks_per_sm,
+                "split_passes": t.split_passes}
 
     def trace_paths(self, keys: np.ndarray, params: NeRenderParams | None = None, **kw) -> np.ndarray:
         """Camera path radiance for (pixel, sample) keys, shape (n, 3)."""

@@ -80,11 +80,12 @@ struct ne_scene {
   size_t paths_cap = 0;
   int blocks_per_sm = 1;
   int variant = 0;           // path kernel: 0 straight, 1 regrouped, 2 lane refill, 3 split
-  PathState* d_defer = nullptr;  // split renders: deferred paths
+  int split_passes = 3;       // kernel 3: passes (the last runs deferred paths to the end)
+  PathState* d_defer[2] = {nullptr, nullptr};  // split renders: two queues of deferred paths
   size_t defer_cap = 0;
-  DeferQueue* d_dq = nullptr;
-  uint32_t* d_dcount = nullptr;
-  DeferQueue dq;
+  DeferQueue* d_dq = nullptr;    // the two queues' descriptors (device)
+  uint32_t* d_dcount = nullptr;  // their counts
+  DeferQueue dq[2];
   int track_share = 16;      // k_sched tracking-phase threshold (32nds of live lanes)
   uint32_t features = 0;     // FT_* bits of the scene
   uint32_t feature_set = 0;  // compiled kernel specialisation covering them
@@ -384,29 +385,44 @@ ne_status launchPaths(ne_scene* sc, const PathArgs& a, bool count) {
   PathArgs b = a;
   b.track_share = sc->track_share;
   if (sc->variant == 3 && !count) {
-    // split render: paths that scatter are queued (up to a quarter of the paths; the rest
-    // finish in the first pass) and resumed, packed together, by the second pass
-    size_t cap = std::max<size_t>(1024, (size_t)(a.total / 4));
+    // split render: the first pass finishes every path that does not scatter and queues the
+    // others at their first scattering event; pass p resumes the queued paths and queues
+    // them again at the scattering event of bounce p, the last pass runs them to the end.
+    // A queue holds half the paths; paths beyond it continue in the pass that had them.
+    size_t cap = std::max<size_t>(1024, (size_t)(a.total / 2));
     if (sc->defer_cap < cap) {
-      if (sc->d_defer) cudaFree(sc->d_defer);
-      sc->d_defer = nullptr;
+      for (PathState*& q : sc->d_defer) {
+        if (q) cudaFree(q);
+        q = nullptr;
+      }
       sc->defer_cap = 0;
-      NE_CUDA(cudaMalloc(&sc->d_defer, cap * sizeof(PathState)), "cudaMalloc(deferred paths)");
+      for (PathState*& q : sc->d_defer) NE_CUDA(cudaMalloc(&q, cap * sizeof(PathState)), "cudaMalloc(deferred paths)");
       sc->defer_cap = cap;
     }
-    if (!sc->d_dq) NE_CUDA(cudaMalloc(&sc->d_dq, sizeof(DeferQueue)), "cudaMalloc");
-    if (!sc->d_dcount) NE_CUDA(cudaMalloc(&sc->d_dcount, sizeof(uint32_t)), "cudaMalloc");
-    sc->dq.items = sc->d_defer;
-    sc->dq.count = sc->d_dcount;
-    sc->dq.cap = (uint32_t)std::min<size_t>(sc->defer_cap, 0xFFFFFFFFu);
-    NE_CUDA(cudaMemcpyAsync(sc->d_dq, &sc->dq, sizeof(DeferQueue), cudaMemcpyHostToDevice, ctx->stream),
+    if (!sc->d_dq) NE_CUDA(cudaMalloc(&sc->d_dq, 2 * sizeof(DeferQueue)), "cudaMalloc");
+    if (!sc->d_dcount) NE_CUDA(cudaMalloc(&sc->d_dcount, 2 * sizeof(uint32_t)), "cudaMalloc");
+    for (int i = 0; i < 2; i++) {
+      sc->dq[i].items = sc->d_defer[i];
+      sc->dq[i].count = sc->d_dcount + i;
+      sc->dq[i].cap = (uint32_t)std::min<size_t>(sc->defer_cap, 0xFFFFFFFFu);
+    }
+    NE_CUDA(cudaMemcpyAsync(sc->d_dq, sc->dq, 2 * sizeof(DeferQueue), cudaMemcpyHostToDevice, ctx->stream),
             "cudaMemcpyAsync");
     NE_CUDA(cudaMemsetAsync(sc->d_dcount, 0, sizeof(uint32_t), ctx->stream), "cudaMemsetAsync");
-    b.defer = sc->d_dq;
+    const int passes = std::max(2, sc->split_passes);
+    b.defer_out = sc->d_dq;
+    b.defer_at = 0;
     NE_CUDA(ne_launch_path_split(0, blocks, ctx->stream, sc->d, b, ctx->d_counter, ctx->d_err), "path kernel launch");
-    NE_CUDA(cudaMemsetAsync(ctx->d_counter, 0, sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync");
-    NE_CUDA(ne_launch_path_split(1, persistentBlocks(sc), ctx->stream, sc->d, b, ctx->d_counter, ctx->d_err),
-            "resume kernel launch");
+    for (int pass = 1; pass < passes; pass++) {
+      const int in = (pass - 1) & 1, out = pass & 1;
+      b.defer_in = sc->d_dq + in;
+      b.defer_out = sc->d_dq + out;
+      b.defer_at = pass == passes - 1 ? -1 : pass;
+      NE_CUDA(cudaMemsetAsync(sc->d_dcount + out, 0, sizeof(uint32_t), ctx->stream), "cudaMemsetAsync");
+      NE_CUDA(cudaMemsetAsync(ctx->d_counter, 0, sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync");
+      NE_CUDA(ne_launch_path_split(1, persistentBlocks(sc), ctx->stream, sc->d, b, ctx->d_counter, ctx->d_err),
+              "resume kernel launch");
+    }
     return NE_OK;
   }
   NE_CUDA(ne_launch_path_kernel(sc->variant, sc->feature_set, count, blocks, ctx->stream, sc->d, b, ctx->d_counter,
@@ -982,12 +998,13 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
   sc->features = F;
   sc->feature_set = ne_feature_set_for(F);
   ne_tuning tn;
-  // surface-only scenes run fastest with lane refill (Cornell box: 235 vs 210 Mpaths/s); media
-  // and meshes with the straight kernel (mesh scene: 127 vs 50)
-  tn.kernel = sc->feature_set == K_SURFACE ? 2 : 0;
+  // surface-only scenes run fastest with lane refill (Cornell box: 235 vs 210 Mpaths/s), grid
+  // media with the split kernel (medium scene: 630 vs 397), meshes with the straight kernel
+  // (mesh scene: 139 vs 50 with lane refill)
+  tn.kernel = sc->feature_set == K_SURFACE ? 2 : (sc->feature_set == K_VOLUME && (F & FT_GRID)) ? 3 : 0;
   tn.track_share = sc->track_share;
   tn.blocks_per_sm = 0;
-  tn.pad = 0;
+  tn.split_passes = 0;
   if (ne_scene_set_tuning(sc, &tn) != NE_OK) return cleanup(NE_ERR_INVALID_ARG);
   cudaError_t e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return cleanup(cudaFail(ctx, e, "scene upload"));
@@ -997,7 +1014,8 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
 
 ne_status ne_scene_set_tuning(ne_scene* sc, const ne_tuning* t) {
   if (!sc || !t || t->kernel < 0 || t->kernel > 3 || t->track_share < 1 || t->track_share > 32 ||
-      t->blocks_per_sm < 0 || t->blocks_per_sm > 64)
+      t->blocks_per_sm < 0 || t->blocks_per_sm > 64 || t->split_passes < 0 || t->split_passes == 1 ||
+      t->split_passes > 16)
     return NE_ERR_INVALID_ARG;
   ne_context* ctx = sc->ctx;
   if (t->kernel == 3 && sc->feature_set != K_VOLUME)
@@ -1007,6 +1025,7 @@ ne_status ne_scene_set_tuning(ne_scene* sc, const ne_tuning* t) {
   if (e != cudaSuccess) return cudaFail(ctx, e, "occupancy query");
   if (fit < 1) fit = 1;
   sc->variant = t->kernel;
+  sc->split_passes = t->split_passes ? t->split_passes : 3;
   sc->track_share = t->track_share;
   sc->blocks_per_sm = t->blocks_per_sm > 0 ? std::min(t->blocks_per_sm, fit) : fit;
   return NE_OK;
@@ -1017,7 +1036,7 @@ ne_status ne_scene_get_tuning(const ne_scene* sc, ne_tuning* t) {
   t->kernel = sc->variant;
   t->track_share = sc->track_share;
   t->blocks_per_sm = sc->blocks_per_sm;
-  t->pad = 0;
+  t->split_passes = sc->split_passes;
   return NE_OK;
 }
 
@@ -1030,7 +1049,8 @@ void ne_scene_destroy(ne_scene* sc) {
   cudaStreamSynchronize(sc->ctx->stream);
   for (void* p : sc->allocs) cudaFree(p);
   if (sc->d_paths) cudaFree(sc->d_paths);
-  if (sc->d_defer) cudaFree(sc->d_defer);
+  for (PathState* q : sc->d_defer)
+    if (q) cudaFree(q);
   if (sc->d_dq) cudaFree(sc->d_dq);
   if (sc->d_dcount) cudaFree(sc->d_dcount);
   delete sc;

@@ -37,7 +37,11 @@ struct PathArgs {
   float* out;                // total * 3 floats
   int track_share;           // regrouped kernel: tracking-phase threshold in 32nds of live lanes
   const CacheIO* cache = nullptr;  // K_CACHE kernels: device copy of the cache buffers
-  const DeferQueue* defer = nullptr;  // K_SPLIT kernels: device copy of the deferred-path queue
+  // K_SPLIT kernels: queues (device memory) the pass reads from and defers into, and the
+  // bounce at whose scattering event paths are deferred (-1: run to the end)
+  const DeferQueue* defer_in = nullptr;
+  const DeferQueue* defer_out = nullptr;
+  int defer_at = -1;
 };
 
 // Training paths of a cached render: a multiplicative hash of the path index, so training
@@ -68,7 +72,7 @@ __device__ __forceinline__ void flushCounters(const Counters& cn, unsigned long 
 template <uint32_t K>
 __global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_paths(const __grid_constant__ DScene s, const PathArgs a,
                                                     unsigned long long* __restrict__ counter, uint32_t* err) {
-  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, a.cache, a.defer, 0ull, false};
+  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, a.cache, a.defer_out, 0ull, false, a.defer_at};
   const int lane = threadIdx.x & 31;
   for (;;) {
     unsigned long long base = 0;
@@ -106,15 +110,17 @@ __global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_paths(const __grid
   flushCounters<K>(c.c, counter);
 }
 
-// Second pass of a split render: warps take 32 deferred paths at a time and run each from
-// its saved scattering point to the end (same operations and draws as an undivided path).
+// Later passes of a split render: warps take 32 deferred paths at a time from the input
+// queue and run each from its saved scattering point, deferring it again at the scattering
+// event of bounce a.defer_at (or running it to the end when that is -1): the same operations
+// and draws as an undivided path.
 template <uint32_t K>
 __global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_resume(const __grid_constant__ DScene s,
                                                                      const PathArgs a,
                                                                      unsigned long long* __restrict__ counter,
                                                                      uint32_t* err) {
-  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, nullptr, nullptr, 0ull, false};
-  const DeferQueue& q = *a.defer;
+  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, nullptr, a.defer_out, 0ull, false, a.defer_at};
+  const DeferQueue& q = *a.defer_in;
   const unsigned long long n = min(*q.count, q.cap);
   const int lane = threadIdx.x & 31;
   for (;;) {
@@ -127,10 +133,14 @@ __global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_resume(const __gri
       const PathState& ps = q.items[i];
       LiVars v = ps.v;
       c.S.reset(ps.key, ps.dim);
+      c.idx = ps.idx;
+      c.deferred = false;
       V3 L = liLoop(c, a.P, v, true);
-      a.out[3 * ps.idx + 0] = L.x;
-      a.out[3 * ps.idx + 1] = L.y;
-      a.out[3 * ps.idx + 2] = L.z;
+      if (!c.deferred) {
+        a.out[3 * ps.idx + 0] = L.x;
+        a.out[3 * ps.idx + 1] = L.y;
+        a.out[3 * ps.idx + 2] = L.z;
+      }
     }
   }
 }
@@ -142,7 +152,7 @@ template <uint32_t K>
 __global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_lanes(const __grid_constant__ DScene s, const PathArgs a,
                                                     unsigned long long* __restrict__ counter, uint32_t* err) {
   namespace cg = cooperative_groups;
-  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, nullptr, nullptr, 0ull, false};
+  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, nullptr, nullptr, 0ull, false, -1};
   for (;;) {
     cg::coalesced_group g = cg::coalesced_threads();
     unsigned long long base = 0;

@@ -186,10 +186,12 @@ struct Ctx {
   uint32_t pidx;
   bool train;
   const struct CacheIO* cio;
-  // K_SPLIT only: the queue of deferred paths; set when the current path was deferred
+  // K_SPLIT only: the queue deferred paths go to, the bounce at whose scattering event they
+  // are deferred (-1: never), the path's radiance slot, set when the path was deferred
   const struct DeferQueue* dq;
   unsigned long long idx;
   bool deferred;
+  int deferAt;
 };
 
 // Buffers of a render that ends paths in the learned radiance cache. A path that reaches
@@ -1122,9 +1124,9 @@ struct LiVars {
   int b, passes;
 };
 
-// A path deferred at its first scattering event in a grid medium, right after the
-// throughput took the medium's sampled albedo: the loop state, the sampler position and
-// the index of the path's radiance slot.
+// A path deferred at a scattering event in a grid medium, right after the throughput took
+// the medium's sampled albedo: the loop state, the sampler position and the index of the
+// path's radiance slot.
 struct PathState {
   LiVars v;
   nerng::PathKey key;
@@ -1140,8 +1142,9 @@ struct DeferQueue {
 
 // integrators/VolumetricPathIntegrator.cpp:176-301 Li, plus the optional Russian
 // roulette of resources/shaders/MS_monteCarlo.frag:539-544, written as a loop over `v` that
-// can start at the scattering point where a K_SPLIT path was deferred (`resume`): every
-// operation and every random draw happens in the same order either way.
+// can start at the scattering point where a K_SPLIT path was deferred (`resume`) and can
+// stop at the scattering event of bounce c.deferAt to be deferred again: every operation and
+// every random draw happens in the same order either way.
 template <uint32_t K>
 NE_D V3 liLoop(Ctx<K>& c, const PathParams& P, LiVars& v, bool resume) {
   const DScene& s = c.s;
@@ -1176,7 +1179,7 @@ NE_D V3 liLoop(Ctx<K>& c, const PathParams& P, LiVars& v, bool resume) {
           continue;
         }
         v.T = v.T * sampledT;
-        if ((K & K_SPLIT) && b == 0) {
+        if ((K & K_SPLIT) && b == c.deferAt) {
           const DeferQueue& q = *c.dq;
           uint32_t slot = appendSlot(q.count);
           if (slot < q.cap) {

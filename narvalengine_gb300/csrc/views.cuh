@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_views(const __grid
                                                                     const ViewArgs a,
                                                                     unsigned long long* __restrict__ counter,
                                                                     uint32_t* err) {
-  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, nullptr};
+  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, nullptr, nullptr, 0ull, false, -1};
   const int lane = threadIdx.x & 31;
   if (threadIdx.x == 0 && blockIdx.x == 0) atomicMin(a.t_start, globalTimer());
   for (;;) {

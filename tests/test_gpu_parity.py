@@ -197,15 +197,18 @@ def test_kernels_and_tunings_agree(ne, ctx):
     scene = ctx.upload(host)
     p = ne.render_params(seed=21, spp=2)
     ref = None
-    for kernel, share, bps in [(0, 16, 0), (0, 16, 1), (1, 16, 0), (1, 1, 0), (1, 32, 0), (1, 8, 1), (2, 16, 0), (2, 16, 1),
-                               (3, 16, 0), (3, 16, 1)]:
-        scene.set_tuning(kernel=kernel, track_share=share, blocks_per_sm=bps)
+    for kernel, share, bps, passes in [(0, 16, 0, 0), (0, 16, 1, 0), (1, 16, 0, 0), (1, 1, 0, 0), (1, 32, 0, 0),
+                                       (1, 8, 1, 0), (2, 16, 0, 0), (2, 16, 1, 0), (3, 16, 0, 2), (3, 16, 1, 3),
+                                       (3, 16, 0, 5), (3, 16, 0, 16)]:
+        scene.set_tuning(kernel=kernel, track_share=share, blocks_per_sm=bps, split_passes=passes)
         img, stats = scene.render(p)
         if ref is None:
             ref = img
-        assert np.array_equal(img, ref), (kernel, share, bps)
+        assert np.array_equal(img, ref), (kernel, share, bps, passes)
     with pytest.raises(ne.NarvalError):
         scene.set_tuning(kernel=4)
+    with pytest.raises(ne.NarvalError):
+        scene.set_tuning(kernel=3, split_passes=1)
     cornell = ctx.upload(ne.SceneHost.from_json(scene_path("cornell_c1")))
     with pytest.raises(ne.NarvalError):
         cornell.set_tuning(kernel=3)
