@@ -163,15 +163,16 @@ ne_status ne_trace_closest(ne_scene* scene, const ne_ray* rays, size_t n, float 
  * kernel: 0 = straight kernel (warps take 32 paths and run them to completion), 1 = regrouped
  * state-machine kernel (a warp steps tracking walks together while at least track_share/32 of
  * its live lanes are in one), 2 = straight kernel whose lanes take a new path as soon as
- * theirs ends, 3 = split (grid-medium scenes only): a first pass finishes every path that
- * does not scatter and queues the others at their first scattering event, a second pass
- * resumes the queued paths packed together. blocks_per_sm: persistent blocks per SM,
+ * theirs ends, 3 = split: a first pass finishes every path that ends at its first event and
+ * queues the others (at their first scattering in a grid medium, or after their first surface
+ * bounce); each further pass resumes the queued paths packed together and queues them again
+ * one bounce later, the last runs them to the end. blocks_per_sm: persistent blocks per SM,
  * 0 = as many as fit. Every configuration renders the same bits. */
 typedef struct ne_tuning {
   int32_t kernel;
   int32_t track_share;
   int32_t blocks_per_sm;
-  int32_t split_passes;  /* kernel 3: passes, 2..16 (0: 3); pass p > 0 resumes the paths queued
+  int32_t split_passes;  /* kernel 3: passes, 2..64 (0: 3); pass p > 0 resumes the paths queued
                             at bounce p - 1 and queues them again at bounce p, the last runs
                             them to the end */
 } ne_tuning;

@@ -50,7 +50,7 @@ def _stale(target: str, deps: list[str]) -> bool:
     if not os.path.exists(target):
         return True
     t = os.path.getmtime(target)
-    return any(os.path.getmtime(d) > t for d in deps)
+    return any(os.path.getmtime(d) >= t for d in deps)
 
 
 def _run(cmd: list[str]) -> None:

@@ -412,7 +412,8 @@ ne_status launchPaths(ne_scene* sc, const PathArgs& a, bool count) {
     const int passes = std::max(2, sc->split_passes);
     b.defer_out = sc->d_dq;
     b.defer_at = 0;
-    NE_CUDA(ne_launch_path_split(0, blocks, ctx->stream, sc->d, b, ctx->d_counter, ctx->d_err), "path kernel launch");
+    NE_CUDA(ne_launch_path_split(0, sc->feature_set, blocks, ctx->stream, sc->d, b, ctx->d_counter, ctx->d_err),
+            "path kernel launch");
     for (int pass = 1; pass < passes; pass++) {
       const int in = (pass - 1) & 1, out = pass & 1;
       b.defer_in = sc->d_dq + in;
@@ -420,7 +421,8 @@ ne_status launchPaths(ne_scene* sc, const PathArgs& a, bool count) {
       b.defer_at = pass == passes - 1 ? -1 : pass;
       NE_CUDA(cudaMemsetAsync(sc->d_dcount + out, 0, sizeof(uint32_t), ctx->stream), "cudaMemsetAsync");
       NE_CUDA(cudaMemsetAsync(ctx->d_counter, 0, sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync");
-      NE_CUDA(ne_launch_path_split(1, persistentBlocks(sc), ctx->stream, sc->d, b, ctx->d_counter, ctx->d_err),
+      NE_CUDA(ne_launch_path_split(1, sc->feature_set, persistentBlocks(sc), ctx->stream, sc->d, b, ctx->d_counter,
+                                   ctx->d_err),
               "resume kernel launch");
     }
     return NE_OK;
@@ -453,7 +455,7 @@ template <uint32_t K>
 static cudaError_t occupancyK(int kernel, int* bps) {
   if (kernel == 0) return pathKernelOccupancy<0, K>(bps);
   if (kernel == 1) return pathKernelOccupancy<1, K>(bps);
-  if (kernel == 3) return ne_path_split_occupancy(bps);
+  if (kernel == 3) return ne_path_split_occupancy(K, bps);
   return pathKernelOccupancy<2, K>(bps);
 }
 
@@ -465,6 +467,37 @@ cudaError_t ne_launch_path_kernel(int kernel, uint32_t set, bool count, int bloc
     case K_SURFACE: return launchK<K_SURFACE>(kernel, blocks, st, s, a, counter, err);
     case K_MESH: return launchK<K_MESH>(kernel, blocks, st, s, a, counter, err);
     default: return launchK<K_GENERAL>(kernel, blocks, st, s, a, counter, err);
+  }
+}
+
+namespace nedev {
+#define NE_SPLIT_DECL(set)                                                                                \
+  cudaError_t launchSplit_##set(int, int, cudaStream_t, const DScene&, const PathArgs&, unsigned long long*, \
+                                uint32_t*);                                                             \
+  cudaError_t occupancySplit_##set(int*);
+NE_SPLIT_DECL(volume)
+NE_SPLIT_DECL(surface)
+NE_SPLIT_DECL(mesh)
+NE_SPLIT_DECL(general)
+#undef NE_SPLIT_DECL
+}  // namespace nedev
+
+cudaError_t ne_launch_path_split(int pass, uint32_t set, int blocks, cudaStream_t st, const DScene& s,
+                                 const PathArgs& a, unsigned long long* counter, uint32_t* err) {
+  switch (set) {
+    case K_VOLUME: return launchSplit_volume(pass, blocks, st, s, a, counter, err);
+    case K_SURFACE: return launchSplit_surface(pass, blocks, st, s, a, counter, err);
+    case K_MESH: return launchSplit_mesh(pass, blocks, st, s, a, counter, err);
+    default: return launchSplit_general(pass, blocks, st, s, a, counter, err);
+  }
+}
+
+cudaError_t ne_path_split_occupancy(uint32_t set, int* bps) {
+  switch (set) {
+    case K_VOLUME: return occupancySplit_volume(bps);
+    case K_SURFACE: return occupancySplit_surface(bps);
+    case K_MESH: return occupancySplit_mesh(bps);
+    default: return occupancySplit_general(bps);
   }
 }
 
@@ -1015,11 +1048,9 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
 ne_status ne_scene_set_tuning(ne_scene* sc, const ne_tuning* t) {
   if (!sc || !t || t->kernel < 0 || t->kernel > 3 || t->track_share < 1 || t->track_share > 32 ||
       t->blocks_per_sm < 0 || t->blocks_per_sm > 64 || t->split_passes < 0 || t->split_passes == 1 ||
-      t->split_passes > 16)
+      t->split_passes > 64)
     return NE_ERR_INVALID_ARG;
   ne_context* ctx = sc->ctx;
-  if (t->kernel == 3 && sc->feature_set != K_VOLUME)
-    return fail(ctx, NE_ERR_UNSUPPORTED, "the split kernel is compiled for grid-medium scenes only");
   int fit = 1;
   cudaError_t e = ne_path_kernel_occupancy(t->kernel, sc->feature_set, &fit);
   if (e != cudaSuccess) return cudaFail(ctx, e, "occupancy query");

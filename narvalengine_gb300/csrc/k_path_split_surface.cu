@@ -1,0 +1,20 @@
+// Path kernel instantiation unit (see kernels.cuh): split render, K_SURFACE feature set.
+#include "kernels.cuh"
+
+namespace nedev {
+
+cudaError_t launchSplit_surface(int pass, int blocks, cudaStream_t st, const DScene& s, const PathArgs& a,
+                             unsigned long long* counter, uint32_t* err) {
+  constexpr uint32_t K = K_SURFACE | K_SPLIT;
+  if (pass == 0)
+    k_paths<K><<<blocks, kThreads, 0, st>>>(s, a, counter, err);
+  else
+    k_resume<K><<<blocks, kThreads, 0, st>>>(s, a, counter, err);
+  return cudaGetLastError();
+}
+
+cudaError_t occupancySplit_surface(int* blocks_per_sm) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_paths<K_SURFACE | K_SPLIT>, kThreads, 0);
+}
+
+}  // namespace nedev

@@ -135,7 +135,7 @@ __global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_resume(const __gri
       c.S.reset(ps.key, ps.dim);
       c.idx = ps.idx;
       c.deferred = false;
-      V3 L = liLoop(c, a.P, v, true);
+      V3 L = liLoop(c, a.P, v, ps.mode == 0);
       if (!c.deferred) {
         a.out[3 * ps.idx + 0] = L.x;
         a.out[3 * ps.idx + 1] = L.y;
@@ -233,12 +233,12 @@ cudaError_t ne_launch_path_kernel(int kernel, uint32_t set, bool count, int bloc
                                   const nedev::DScene& s, const nedev::PathArgs& a, unsigned long long* counter,
                                   uint32_t* err);
 cudaError_t ne_path_kernel_occupancy(int kernel, uint32_t set, int* blocks_per_sm);
-// Split render of grid-medium scenes: first pass (deferring paths at their first scattering
-// event into a->defer) and the resume pass over the deferred paths; counter[0] must be zero
-// before each.
-cudaError_t ne_launch_path_split(int pass, int blocks, cudaStream_t st, const nedev::DScene& s,
+// Split render (kernel 3) of a feature set: pass 0 = the first pass (k_paths deferring at
+// bounce a.defer_at into a.defer_out), else a resume pass over a.defer_in; counter[0] must be
+// zero before each.
+cudaError_t ne_launch_path_split(int pass, uint32_t set, int blocks, cudaStream_t st, const nedev::DScene& s,
                                  const nedev::PathArgs& a, unsigned long long* counter, uint32_t* err);
-cudaError_t ne_path_split_occupancy(int* blocks_per_sm);
+cudaError_t ne_path_split_occupancy(uint32_t set, int* blocks_per_sm);
 // The straight kernel over grid-medium scenes with paths ending in the radiance cache.
 cudaError_t ne_launch_path_kernel_cache(int blocks, cudaStream_t st, const nedev::DScene& s, const nedev::PathArgs& a,
                                         unsigned long long* counter, uint32_t* err);

@@ -1131,6 +1131,7 @@ struct PathState {
   LiVars v;
   nerng::PathKey key;
   uint32_t dim;
+  uint32_t mode;  // 0: resume inside a medium bounce after sampling, 1: at the top of bounce v.b
   unsigned long long idx;
 };
 
@@ -1187,6 +1188,7 @@ NE_D V3 liLoop(Ctx<K>& c, const PathParams& P, LiVars& v, bool resume) {
             ps.v = v;
             ps.key = c.S.key;
             ps.dim = c.S.dim;
+            ps.mode = 0;
             ps.idx = c.idx;
             c.deferred = true;
             return v.L;
@@ -1253,6 +1255,22 @@ NE_D V3 liLoop(Ctx<K>& c, const PathParams& P, LiVars& v, bool resume) {
         float q = gmax(0.05f, 1.0f - mx);
         if (c.S.random() < q) break;
         v.T = v.T / (1.0f - q);
+      }
+    }
+    if ((K & K_SPLIT) && !medium && b == c.deferAt && b + 1 < P.bounces) {
+      // a surface bounce done: defer the path to the top of the next bounce
+      const DeferQueue& q = *c.dq;
+      uint32_t slot = appendSlot(q.count);
+      if (slot < q.cap) {
+        PathState& ps = q.items[slot];
+        ps.v = v;
+        ps.v.b = b + 1;
+        ps.key = c.S.key;
+        ps.dim = c.S.dim;
+        ps.mode = 1;
+        ps.idx = c.idx;
+        c.deferred = true;
+        return v.L;
       }
     }
   }
