@@ -319,7 +319,7 @@ def main():
                     help="workload (the default is the configuration the metric is quoted on)")
     ap.add_argument("--kernel", type=int, default=-1,
                     help="path kernel (ne_tuning.kernel): 0 straight, 1 regrouped, 2 lane refill, 3 split; "
-                         "default: the library's choice for the scene")
+                         "default: the library's autotuner picks")
     ap.add_argument("--split-passes", type=int, default=0, help="split kernel passes (0: library default)")
     ap.add_argument("--track-share", type=int, default=16, help="regrouped kernel tracking threshold, 32nds")
     ap.add_argument("--profile-spp", type=int, default=0,
@@ -348,6 +348,9 @@ def main():
     scene = ctx.upload(host)
     if args.kernel >= 0:
         scene.set_tuning(kernel=args.kernel, track_share=args.track_share, split_passes=args.split_passes)
+    else:
+        # the library's autotuner, on a quarter of the samples, outside the timed region
+        scene.autotune(repeats=2, seed=7, spp=max(1, host.spp // 4))
     W, H, spp = host.width, host.height, host.spp
     paths_per_step = W * H * spp
     img_bytes = W * H * 3 * 4
@@ -369,6 +372,7 @@ def main():
     clocks = ClockSampler(local)
     clocks.start()
     kernel_ms, step_ms = [], []
+    launches = 0
     for _ in range(args.steps):
         ctx.flush_l2(256 << 20)
         ctx.record(0)
@@ -376,6 +380,7 @@ def main():
         ctx.record(1)
         step_ms.append(ctx.elapsed_ms(0, 1))
         kernel_ms.append(st["kernel_ms"])
+        launches += st["kernel_launches"]
     ctx.synchronize()
     clk = clocks.stop()
     local_ms = sum(step_ms)
@@ -389,16 +394,14 @@ def main():
     pe = ne.render_params(seed=1, sample_offset=base)
     for _ in range(1):
         s2 = ctx.upload(host)
-        if args.kernel >= 0:
-            s2.set_tuning(kernel=args.kernel, track_share=args.track_share, split_passes=args.split_passes)
+        s2.set_tuning(**scene.tuning())
         s2.render(pe, out=out_host)
         s2.close()
     d.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         s2 = ctx.upload(host)
-        if args.kernel >= 0:
-            s2.set_tuning(kernel=args.kernel, track_share=args.track_share, split_passes=args.split_passes)
+        s2.set_tuning(**scene.tuning())
         s2.render(pe, out=out_host)
         s2.close()
     e2e_s = time.perf_counter() - t0
@@ -442,7 +445,7 @@ def main():
                            "tuning": scene.tuning()},
                 "e2e": {"value": e2e, "unit": "Mpaths/s", "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": img_bytes},
-                "gpu_launches": 2 * args.steps,
+                "gpu_launches": launches,
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": clk}
         print(json.dumps(line), flush=True)
     scene.close()

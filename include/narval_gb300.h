@@ -172,13 +172,19 @@ typedef struct ne_tuning {
   int32_t kernel;
   int32_t track_share;
   int32_t blocks_per_sm;
-  int32_t split_passes;  /* kernel 3: passes, 2..64 (0: 3); pass p > 0 resumes the paths queued
+  int32_t split_passes;  /* kernel 3: passes, 2..64 (0: 6); pass p > 0 resumes the paths queued
                             at bounce p - 1 and queues them again at bounce p, the last runs
                             them to the end */
 } ne_tuning;
 
 ne_status ne_scene_set_tuning(ne_scene* scene, const ne_tuning* tuning);
 ne_status ne_scene_get_tuning(const ne_scene* scene, ne_tuning* tuning);
+/* Autotuner: renders the scene with `params` (typically fewer samples than a frame) under
+ * each candidate (straight, lane refill, split with 3..24 passes; resident blocks as many as
+ * fit), `repeats` timed renders after one warm-up each, keeps the fastest path-kernel time
+ * and returns it. Every candidate renders the same bits. */
+ne_status ne_scene_autotune(ne_scene* scene, const ne_render_params* params, int repeats, ne_tuning* best,
+                            double* best_ms);
 
 /* ---- timing utilities on the context's stream (for benchmarks) ---- */
 

@@ -267,6 +267,14 @@ class Scene:
         t = _abi.NeTuning(kernel, track_share, blocks_per_sm, split_passes)
         self.ctx.check(library().ne_scene_set_tuning(self._h, C.byref(t)))
 
+    def autotune(self, repeats: int = 2, params: NeRenderParams | None = None, **kw):
+        """ne_scene_autotune: keeps the fastest kernel configuration; returns (tuning, ms)."""
+        p = params if params is not None else render_params(**kw)
+        t = _abi.NeTuning()
+        ms = C.c_double()
+        self.ctx.check(library().ne_scene_autotune(self._h, C.byref(p), repeats, C.byref(t), C.byref(ms)))
+        return self.tuning(), ms.value
+
     def tuning(self) -> dict:
         t = _abi.NeTuning()
         self.ctx.check(library().ne_scene_get_tuning(self._h, C.byref(t)))

@@ -175,6 +175,8 @@ SIGNATURES = {
     "ne_render_cached": (C.c_int32, [C.c_void_p, C.c_void_p, C.POINTER(NeRenderParams),
                                      C.POINTER(NeCacheRenderParams), C.c_void_p, C.POINTER(NeRenderStats),
                                      C.POINTER(NeCacheRenderStats)]),
+    "ne_scene_autotune": (C.c_int32, [C.c_void_p, C.POINTER(NeRenderParams), C.c_int, C.POINTER(NeTuning),
+                                      C.POINTER(C.c_double)]),
     "ne_camera_look_at": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_float, C.c_int, C.c_int, C.c_float,
                                       C.POINTER(NeCamera)]),
     "ne_views_create": (C.c_int32, [C.c_void_p, C.POINTER(NeView), C.c_uint32, C.POINTER(NeRenderParams),

@@ -80,7 +80,7 @@ struct ne_scene {
   size_t paths_cap = 0;
   int blocks_per_sm = 1;
   int variant = 0;           // path kernel: 0 straight, 1 regrouped, 2 lane refill, 3 split
-  int split_passes = 3;       // kernel 3: passes (the last runs deferred paths to the end)
+  int split_passes = 6;       // kernel 3: passes (the last runs deferred paths to the end)
   PathState* d_defer[2] = {nullptr, nullptr};  // split renders: two queues of deferred paths
   size_t defer_cap = 0;
   DeferQueue* d_dq = nullptr;    // the two queues' descriptors (device)
@@ -375,6 +375,11 @@ struct DevBuf {
 };
 
 int persistentBlocks(ne_scene* sc) { return sc->ctx->sm_count * sc->blocks_per_sm; }
+
+// Path-kernel launches of one launchPaths call.
+int pathLaunches(const ne_scene* sc, bool count) {
+  return (sc->variant == 3 && !count) ? std::max(2, sc->split_passes) : 1;
+}
 
 ne_status launchPaths(ne_scene* sc, const PathArgs& a, bool count) {
   ne_context* ctx = sc->ctx;
@@ -1056,7 +1061,7 @@ ne_status ne_scene_set_tuning(ne_scene* sc, const ne_tuning* t) {
   if (e != cudaSuccess) return cudaFail(ctx, e, "occupancy query");
   if (fit < 1) fit = 1;
   sc->variant = t->kernel;
-  sc->split_passes = t->split_passes ? t->split_passes : 3;
+  sc->split_passes = t->split_passes ? t->split_passes : 6;
   sc->track_share = t->track_share;
   sc->blocks_per_sm = t->blocks_per_sm > 0 ? std::min(t->blocks_per_sm, fit) : fit;
   return NE_OK;
@@ -1146,7 +1151,7 @@ ne_status ne_render(ne_scene* sc, const ne_render_params* p, float* out_rgb, ne_
     if (stats) {
       memset(stats, 0, sizeof(*stats));
       stats->paths = total;
-      stats->kernel_launches = 2;
+      stats->kernel_launches = (uint32_t)pathLaunches(sc, (flags & NE_RENDER_COUNT_WORK) != 0) + 1;
     }
     return NE_OK;
   }
@@ -1166,7 +1171,7 @@ ne_status ne_render(ne_scene* sc, const ne_render_params* p, float* out_rgb, ne_
     stats->scene_queries = cnt[2];
     stats->bvh_nodes = cnt[3];
     stats->prim_tests = cnt[4];
-    stats->kernel_launches = 2;
+    stats->kernel_launches = (uint32_t)pathLaunches(sc, (flags & NE_RENDER_COUNT_WORK) != 0) + 1;
   }
   return NE_OK;
 }
@@ -1237,7 +1242,7 @@ ne_status ne_render_accumulate(ne_scene* sc, const ne_render_params* p, double* 
     stats->scene_queries = cnt[2];
     stats->bvh_nodes = cnt[3];
     stats->prim_tests = cnt[4];
-    stats->kernel_launches = 2;
+    stats->kernel_launches = (uint32_t)pathLaunches(sc, (flags & NE_RENDER_COUNT_WORK) != 0) + 1;
     stats->dropped_paths = (uint32_t)std::min<unsigned long long>(cnt[5], 0xFFFFFFFFull);
   }
   return NE_OK;
@@ -1997,6 +2002,46 @@ ne_status ne_views_image(const ne_views* vw, uint32_t v, float* out) {
   NE_CUDA(cudaMemcpyAsync(out, vw->d_img + 3 * (size_t)d.pix_begin, bytes, cudaMemcpyDeviceToHost, ctx->stream),
           "cudaMemcpyAsync");
   NE_CUDA(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  return NE_OK;
+}
+
+ne_status ne_scene_autotune(ne_scene* sc, const ne_render_params* p, int repeats, ne_tuning* best, double* best_ms) {
+  if (!sc || repeats < 1) return NE_ERR_INVALID_ARG;
+  ne_context* ctx = sc->ctx;
+  NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  const int W = sc->settings.width, H = sc->settings.height;
+  DevBuf<float> img;
+  NE_CUDA(cudaMalloc(&img.p, (size_t)W * H * 3 * sizeof(float)), "cudaMalloc(image)");
+  ne_render_params rp = p ? *p : ne_render_params{0, 0, -1, -1, 3, 0, 0};
+  rp.flags = (rp.flags | NE_RENDER_OUT_DEVICE) & ~(NE_RENDER_COUNT_WORK | NE_RENDER_NO_SYNC);
+  ne_tuning keep;
+  ne_scene_get_tuning(sc, &keep);
+  std::vector<ne_tuning> cands;
+  for (int k : {0, 2}) cands.push_back(ne_tuning{k, sc->track_share, 0, 0});
+  for (int passes : {3, 4, 6, 8, 12, 16, 24}) cands.push_back(ne_tuning{3, sc->track_share, 0, passes});
+  ne_tuning bt = keep;
+  double bms = 1e30;
+  for (const ne_tuning& t : cands) {
+    ne_status st = ne_scene_set_tuning(sc, &t);
+    if (st) return st;
+    ne_render_stats s;
+    st = ne_render(sc, &rp, img.p, &s);  // warm-up
+    if (st) return st;
+    double m = 1e30;
+    for (int r = 0; r < repeats; r++) {
+      st = ne_render(sc, &rp, img.p, &s);
+      if (st) return st;
+      m = std::min(m, s.kernel_ms);
+    }
+    if (m < bms) {
+      bms = m;
+      bt = t;
+    }
+  }
+  ne_status st = ne_scene_set_tuning(sc, &bt);
+  if (st) return st;
+  if (best) ne_scene_get_tuning(sc, best);
+  if (best_ms) *best_ms = bms;
   return NE_OK;
 }
 

@@ -327,3 +327,17 @@ def test_split_queue_overflow(ne, ctx, oracle_lib):
     finally:
         scene.close()
         orc.close()
+
+
+def test_autotune_keeps_the_image(ne, ctx):
+    """The scene autotuner only changes how the paths are scheduled."""
+    host = ne.SceneHost.from_json(scene_path("cornell_c1"))
+    scene = ctx.upload(host)
+    ref, _ = scene.render(seed=13, spp=2)
+    best, ms = scene.autotune(repeats=1, seed=1, spp=1)
+    assert ms > 0 and best["kernel"] in (0, 2, 3)
+    img, st = scene.render(seed=13, spp=2)
+    assert np.array_equal(img, ref)
+    if best["kernel"] == 3:
+        assert st["kernel_launches"] == best["split_passes"] + 1
+    scene.close()
