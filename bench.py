@@ -130,6 +130,14 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
+        if not self.lines:
+            # a timed region shorter than the sampling period: one reading right after it
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=10)
+                self.lines = [ln.strip() for ln in out.stdout.splitlines() if ln.strip()]
+            except (OSError, subprocess.SubprocessError):
+                pass
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:

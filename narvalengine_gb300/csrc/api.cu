@@ -381,6 +381,51 @@ int pathLaunches(const ne_scene* sc, bool count) {
   return (sc->variant == 3 && !count) ? std::max(2, sc->split_passes) : 1;
 }
 
+// Split render: the first pass finishes every path that ends at its first event and queues
+// the others (at their first scattering in a grid medium or after their first surface
+// bounce); pass p resumes the queued paths and queues them again one bounce later, the last
+// pass runs them to the end. Two queues of half the paths each alternate; paths beyond a
+// queue's capacity continue in the pass that had them. `launch(pass, blocks, args)`
+// launches one pass (0: first pass).
+template <class F>
+ne_status launchSplit(ne_scene* sc, PathArgs b, int blocks, F launch) {
+  ne_context* ctx = sc->ctx;
+  size_t cap = std::max<size_t>(1024, (size_t)(b.total / 2));
+  if (sc->defer_cap < cap) {
+    for (PathState*& q : sc->d_defer) {
+      if (q) cudaFree(q);
+      q = nullptr;
+    }
+    sc->defer_cap = 0;
+    for (PathState*& q : sc->d_defer) NE_CUDA(cudaMalloc(&q, cap * sizeof(PathState)), "cudaMalloc(deferred paths)");
+    sc->defer_cap = cap;
+  }
+  if (!sc->d_dq) NE_CUDA(cudaMalloc(&sc->d_dq, 2 * sizeof(DeferQueue)), "cudaMalloc");
+  if (!sc->d_dcount) NE_CUDA(cudaMalloc(&sc->d_dcount, 2 * sizeof(uint32_t)), "cudaMalloc");
+  for (int i = 0; i < 2; i++) {
+    sc->dq[i].items = sc->d_defer[i];
+    sc->dq[i].count = sc->d_dcount + i;
+    sc->dq[i].cap = (uint32_t)std::min<size_t>(sc->defer_cap, 0xFFFFFFFFu);
+  }
+  NE_CUDA(cudaMemcpyAsync(sc->d_dq, sc->dq, 2 * sizeof(DeferQueue), cudaMemcpyHostToDevice, ctx->stream),
+          "cudaMemcpyAsync");
+  NE_CUDA(cudaMemsetAsync(sc->d_dcount, 0, sizeof(uint32_t), ctx->stream), "cudaMemsetAsync");
+  const int passes = std::max(2, sc->split_passes);
+  b.defer_out = sc->d_dq;
+  b.defer_at = 0;
+  NE_CUDA(launch(0, blocks, b), "path kernel launch");
+  for (int pass = 1; pass < passes; pass++) {
+    const int in = (pass - 1) & 1, out = pass & 1;
+    b.defer_in = sc->d_dq + in;
+    b.defer_out = sc->d_dq + out;
+    b.defer_at = pass == passes - 1 ? -1 : pass;
+    NE_CUDA(cudaMemsetAsync(sc->d_dcount + out, 0, sizeof(uint32_t), ctx->stream), "cudaMemsetAsync");
+    NE_CUDA(cudaMemsetAsync(ctx->d_counter, 0, sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync");
+    NE_CUDA(launch(pass, persistentBlocks(sc), b), "resume kernel launch");
+  }
+  return NE_OK;
+}
+
 ne_status launchPaths(ne_scene* sc, const PathArgs& a, bool count) {
   ne_context* ctx = sc->ctx;
   NE_CUDA(cudaMemsetAsync(ctx->d_counter, 0, 5 * sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync");
@@ -390,47 +435,9 @@ ne_status launchPaths(ne_scene* sc, const PathArgs& a, bool count) {
   PathArgs b = a;
   b.track_share = sc->track_share;
   if (sc->variant == 3 && !count) {
-    // split render: the first pass finishes every path that does not scatter and queues the
-    // others at their first scattering event; pass p resumes the queued paths and queues
-    // them again at the scattering event of bounce p, the last pass runs them to the end.
-    // A queue holds half the paths; paths beyond it continue in the pass that had them.
-    size_t cap = std::max<size_t>(1024, (size_t)(a.total / 2));
-    if (sc->defer_cap < cap) {
-      for (PathState*& q : sc->d_defer) {
-        if (q) cudaFree(q);
-        q = nullptr;
-      }
-      sc->defer_cap = 0;
-      for (PathState*& q : sc->d_defer) NE_CUDA(cudaMalloc(&q, cap * sizeof(PathState)), "cudaMalloc(deferred paths)");
-      sc->defer_cap = cap;
-    }
-    if (!sc->d_dq) NE_CUDA(cudaMalloc(&sc->d_dq, 2 * sizeof(DeferQueue)), "cudaMalloc");
-    if (!sc->d_dcount) NE_CUDA(cudaMalloc(&sc->d_dcount, 2 * sizeof(uint32_t)), "cudaMalloc");
-    for (int i = 0; i < 2; i++) {
-      sc->dq[i].items = sc->d_defer[i];
-      sc->dq[i].count = sc->d_dcount + i;
-      sc->dq[i].cap = (uint32_t)std::min<size_t>(sc->defer_cap, 0xFFFFFFFFu);
-    }
-    NE_CUDA(cudaMemcpyAsync(sc->d_dq, sc->dq, 2 * sizeof(DeferQueue), cudaMemcpyHostToDevice, ctx->stream),
-            "cudaMemcpyAsync");
-    NE_CUDA(cudaMemsetAsync(sc->d_dcount, 0, sizeof(uint32_t), ctx->stream), "cudaMemsetAsync");
-    const int passes = std::max(2, sc->split_passes);
-    b.defer_out = sc->d_dq;
-    b.defer_at = 0;
-    NE_CUDA(ne_launch_path_split(0, sc->feature_set, blocks, ctx->stream, sc->d, b, ctx->d_counter, ctx->d_err),
-            "path kernel launch");
-    for (int pass = 1; pass < passes; pass++) {
-      const int in = (pass - 1) & 1, out = pass & 1;
-      b.defer_in = sc->d_dq + in;
-      b.defer_out = sc->d_dq + out;
-      b.defer_at = pass == passes - 1 ? -1 : pass;
-      NE_CUDA(cudaMemsetAsync(sc->d_dcount + out, 0, sizeof(uint32_t), ctx->stream), "cudaMemsetAsync");
-      NE_CUDA(cudaMemsetAsync(ctx->d_counter, 0, sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync");
-      NE_CUDA(ne_launch_path_split(1, sc->feature_set, persistentBlocks(sc), ctx->stream, sc->d, b, ctx->d_counter,
-                                   ctx->d_err),
-              "resume kernel launch");
-    }
-    return NE_OK;
+    return launchSplit(sc, b, blocks, [&](int pass, int nb, const PathArgs& pa) {
+      return ne_launch_path_split(pass, sc->feature_set, nb, ctx->stream, sc->d, pa, ctx->d_counter, ctx->d_err);
+    });
   }
   NE_CUDA(ne_launch_path_kernel(sc->variant, sc->feature_set, count, blocks, ctx->stream, sc->d, b, ctx->d_counter,
                                 ctx->d_err),
@@ -1759,12 +1766,17 @@ ne_status ne_render_cached(ne_scene* sc, ne_cache* c, const ne_render_params* p,
   a.track_share = sc->track_share;
   a.cache = c->d_io;
   int fit = 1;
-  NE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, k_paths<K_VOLUME | K_CACHE>, kThreads, 0),
-          "occupancy query");
+  NE_CUDA(ne_path_cache_occupancy(&fit), "occupancy query");
   int blocks = ctx->sm_count * std::max(1, fit);
   unsigned long long needed = (total + kThreads - 1) / kThreads;
   if ((unsigned long long)blocks > needed) blocks = (int)std::max<unsigned long long>(1, needed);
-  NE_CUDA(ne_launch_path_kernel_cache(blocks, ctx->stream, sc->d, a, ctx->d_counter, ctx->d_err), "path kernel launch");
+  {
+    ne_status sst = launchSplit(sc, a, blocks, [&](int pass, int nb, const PathArgs& pa) {
+      return ne_launch_path_kernel_cache(pass, pass ? ctx->sm_count * std::max(1, fit) : nb, ctx->stream, sc->d, pa,
+                                         ctx->d_counter, ctx->d_err);
+    });
+    if (sst) return sst;
+  }
   NE_CUDA(cudaEventRecord(c->ev[1], ctx->stream), "cudaEventRecord");
   // the network answers however many queries the path kernel appended (count read on the device)
   NeMlpForward f = {io.q_pos, io.q_dir, nullptr, io.q_cap, c->counts, c->wfwd, c->bias, nullptr, nullptr, io.q_thr,

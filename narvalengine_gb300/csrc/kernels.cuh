@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_resume(const __gri
                                                                      const PathArgs a,
                                                                      unsigned long long* __restrict__ counter,
                                                                      uint32_t* err) {
-  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, nullptr, a.defer_out, 0ull, false, a.defer_at};
+  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, a.cache, a.defer_out, 0ull, false, a.defer_at};
   const DeferQueue& q = *a.defer_in;
   const unsigned long long n = min(*q.count, q.cap);
   const int lane = threadIdx.x & 31;
@@ -135,6 +135,10 @@ __global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_resume(const __gri
       c.S.reset(ps.key, ps.dim);
       c.idx = ps.idx;
       c.deferred = false;
+      if (K & K_CACHE) {
+        c.pidx = (uint32_t)ps.idx;
+        c.train = isTrainingPath(ps.idx, a.cache->train_stride);
+      }
       V3 L = liLoop(c, a.P, v, ps.mode == 0);
       if (!c.deferred) {
         a.out[3 * ps.idx + 0] = L.x;
@@ -222,7 +226,6 @@ cudaError_t pathKernelOccupancy(int* blocks_per_sm) {
 
 // Declared here, instantiated in the k_path_*.cu units only.
 NE_PATH_KERNEL_ALL(extern)
-NE_PATH_KERNEL_INSTANCE(extern, 0, K_VOLUME | K_CACHE)
 
 }  // namespace nedev
 
@@ -239,9 +242,11 @@ cudaError_t ne_path_kernel_occupancy(int kernel, uint32_t set, int* blocks_per_s
 cudaError_t ne_launch_path_split(int pass, uint32_t set, int blocks, cudaStream_t st, const nedev::DScene& s,
                                  const nedev::PathArgs& a, unsigned long long* counter, uint32_t* err);
 cudaError_t ne_path_split_occupancy(uint32_t set, int* blocks_per_sm);
-// The straight kernel over grid-medium scenes with paths ending in the radiance cache.
-cudaError_t ne_launch_path_kernel_cache(int blocks, cudaStream_t st, const nedev::DScene& s, const nedev::PathArgs& a,
-                                        unsigned long long* counter, uint32_t* err);
+// Grid-medium scenes with paths ending in the radiance cache, split like kernel 3: pass 0 =
+// first pass, else a resume pass (see ne_launch_path_split).
+cudaError_t ne_launch_path_kernel_cache(int pass, int blocks, cudaStream_t st, const nedev::DScene& s,
+                                        const nedev::PathArgs& a, unsigned long long* counter, uint32_t* err);
+cudaError_t ne_path_cache_occupancy(int* blocks_per_sm);
 cudaError_t ne_launch_li(int blocks, cudaStream_t st, const nedev::DScene& s, nedev::PathParams P, nerng::PathKey base,
                          const ne_ray* rays, const ne_path_key* keys, size_t n, uint32_t first_dim, float* out,
                          uint32_t* err);

@@ -1180,7 +1180,7 @@ NE_D V3 liLoop(Ctx<K>& c, const PathParams& P, LiVars& v, bool resume) {
           continue;
         }
         v.T = v.T * sampledT;
-        if ((K & K_SPLIT) && b == c.deferAt) {
+        if ((K & K_SPLIT) && b == c.deferAt && !recorded) {
           const DeferQueue& q = *c.dq;
           uint32_t slot = appendSlot(q.count);
           if (slot < q.cap) {
@@ -1194,27 +1194,27 @@ NE_D V3 liLoop(Ctx<K>& c, const PathParams& P, LiVars& v, bool resume) {
             return v.L;
           }
         }
-        if ((K & K_CACHE) && b >= c.cio->bounce && !recorded) {
-          V3 xo = mul4(s.instances[v.isect.inst].ocs, v.scattered.o, 1.0f);
-          if (!c.train) {
-            const CacheIO& io = *c.cio;
-            uint32_t q = appendSlot(io.q_count);
-            if (q < io.q_cap) {
-              io.q_pos[3 * q] = xo.x; io.q_pos[3 * q + 1] = xo.y; io.q_pos[3 * q + 2] = xo.z;
-              io.q_dir[3 * q] = v.incoming.d.x; io.q_dir[3 * q + 1] = v.incoming.d.y;
-              io.q_dir[3 * q + 2] = v.incoming.d.z;
-              io.q_thr[3 * q] = v.T.x; io.q_thr[3 * q + 1] = v.T.y; io.q_thr[3 * q + 2] = v.T.z;
-              io.q_idx[q] = c.pidx;
-            }
-            return v.L;
-          }
-          recorded = true;
-          vPos = xo;
-          vDir = v.incoming.d;
-          vL = v.L;
-          vT = v.T;
-        }
       }
+    }
+    if ((K & K_CACHE) && medium && b >= c.cio->bounce && !recorded) {
+      V3 xo = mul4(s.instances[v.isect.inst].ocs, v.scattered.o, 1.0f);
+      if (!c.train) {
+        const CacheIO& io = *c.cio;
+        uint32_t q = appendSlot(io.q_count);
+        if (q < io.q_cap) {
+          io.q_pos[3 * q] = xo.x; io.q_pos[3 * q + 1] = xo.y; io.q_pos[3 * q + 2] = xo.z;
+          io.q_dir[3 * q] = v.incoming.d.x; io.q_dir[3 * q + 1] = v.incoming.d.y;
+          io.q_dir[3 * q + 2] = v.incoming.d.z;
+          io.q_thr[3 * q] = v.T.x; io.q_thr[3 * q + 1] = v.T.y; io.q_thr[3 * q + 2] = v.T.z;
+          io.q_idx[q] = c.pidx;
+        }
+        return v.L;
+      }
+      recorded = true;
+      vPos = xo;
+      vDir = v.incoming.d;
+      vL = v.L;
+      vT = v.T;
     }
     if (medium) {
       V3 phaseFr = bsdfEval<K>(*mat, v.incoming.d, v.scattered.d, v.isect.normal);
@@ -1257,7 +1257,7 @@ NE_D V3 liLoop(Ctx<K>& c, const PathParams& P, LiVars& v, bool resume) {
         v.T = v.T / (1.0f - q);
       }
     }
-    if ((K & K_SPLIT) && !medium && b == c.deferAt && b + 1 < P.bounces) {
+    if ((K & K_SPLIT) && !medium && b == c.deferAt && b + 1 < P.bounces && !recorded) {
       // a surface bounce done: defer the path to the top of the next bounce
       const DeferQueue& q = *c.dq;
       uint32_t slot = appendSlot(q.count);
