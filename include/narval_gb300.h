@@ -219,6 +219,7 @@ typedef struct ne_views_tuning {
   int32_t blocks_per_sm;   /* resident blocks per SM, 0 = as many as fit */
   int32_t order;           /* views in the launch: 0 as given, 1 largest first, 2 smallest first */
   int32_t graph;           /* 1: capture the launch sequence once and replay it as a CUDA graph */
+  int32_t split_passes;    /* as ne_tuning.split_passes: 1 = one pass, 2..64, 0 = 6 */
 } ne_views_tuning;
 typedef struct ne_views_stats {
   double ms;               /* CUDA-event time of the batch */
@@ -231,8 +232,8 @@ ne_status ne_views_create(ne_scene* scene, const ne_view* views, uint32_t n, con
 void ne_views_destroy(ne_views* views);
 ne_status ne_views_set_tuning(ne_views* views, const ne_views_tuning* tuning);
 ne_status ne_views_get_tuning(const ne_views* views, ne_views_tuning* tuning);
-/* Times every candidate configuration (fetch 32/128, all or half the resident blocks, given,
- * largest-first or smallest-first order, as a graph) `repeats` times after one warm-up batch;
+/* Times every candidate configuration (fetch 32/128, largest-first or smallest-first order,
+ * 1, 4 or 8 split passes, as a graph) `repeats` times after one warm-up batch;
  * among those within 3% of the fastest it keeps the one with the lowest median view latency,
  * and returns it with its time. */
 ne_status ne_views_autotune(ne_views* views, int repeats, ne_views_tuning* best, double* best_ms);

@@ -106,8 +106,15 @@ struct ne_views {
   uint32_t total_pixels = 0;
   PathParams P;
   nerng::PathKey base;
-  ne_views_tuning tune = {32, 0, 0, 1};
+  ne_views_tuning tune = {32, 0, 0, 1, 0};
   int blocks = 1;
+  // split batches: two queues of deferred paths, the views' path spans, completion hook
+  PathState* d_defer[2] = {nullptr, nullptr};
+  size_t defer_cap = 0;
+  DeferQueue* d_dq = nullptr;
+  uint32_t* d_dcount = nullptr;
+  ViewSpan* d_spans = nullptr;
+  ViewDone* d_vd = nullptr;
   cudaGraphExec_t exec = nullptr;
   cudaEvent_t ev[2] = {nullptr, nullptr};
   std::vector<float> latency;      // caller order, last batch
@@ -672,8 +679,17 @@ ne_status viewsLayout(ne_views* vw) {
   }
   NE_CUDA(cudaMemcpyAsync(vw->d_views, vw->dv.data(), n * sizeof(DView), cudaMemcpyHostToDevice, ctx->stream),
           "cudaMemcpyAsync");
+  std::vector<ViewSpan> spans(n);
+  for (uint32_t s = 0; s < n; s++) spans[s] = ViewSpan{vw->dv[s].path_begin, vw->dv[s].paths};
+  NE_CUDA(cudaMemcpyAsync(vw->d_spans, spans.data(), n * sizeof(ViewSpan), cudaMemcpyHostToDevice, ctx->stream),
+          "cudaMemcpyAsync");
+  ViewDone vd = {vw->d_spans, n, vw->d_done, vw->d_done + n};
+  NE_CUDA(cudaMemcpyAsync(vw->d_vd, &vd, sizeof(ViewDone), cudaMemcpyHostToDevice, ctx->stream), "cudaMemcpyAsync");
+  NE_CUDA(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
   return NE_OK;
 }
+
+int viewsPasses(const ne_views* vw) { return vw->tune.split_passes == 0 ? 6 : vw->tune.split_passes; }
 
 ne_status viewsEnqueue(ne_views* vw) {
   ne_context* ctx = vw->sc->ctx;
@@ -686,6 +702,8 @@ ne_status viewsEnqueue(ne_views* vw) {
   NE_CUDA(cudaMemsetAsync(tstart, 0xFF, sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync");
   NE_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync");
   NE_CUDA(cudaMemsetAsync(ctx->d_err, 0, 4, ctx->stream), "cudaMemsetAsync");
+  const int passes = viewsPasses(vw);
+  const bool split = passes > 1;
   ViewArgs a;
   a.P = vw->P;
   a.base = vw->base;
@@ -697,7 +715,30 @@ ne_status viewsEnqueue(ne_views* vw) {
   a.done = done;
   a.t_done = tdone;
   a.t_start = tstart;
-  NE_CUDA(ne_launch_views(vw->blocks, ctx->stream, vw->sc->d, a, counter, ctx->d_err), "k_views launch");
+  a.defer_out = split ? vw->d_dq : nullptr;
+  if (split) NE_CUDA(cudaMemsetAsync(vw->d_dcount, 0, sizeof(uint32_t), ctx->stream), "cudaMemsetAsync");
+  NE_CUDA(ne_launch_views(split, vw->blocks, ctx->stream, vw->sc->d, a, counter, ctx->d_err), "k_views launch");
+  for (int pass = 1; pass < passes; pass++) {
+    const int in = (pass - 1) & 1, out = pass & 1;
+    PathArgs pa;
+    pa.P = vw->P;
+    pa.base = vw->base;
+    pa.total = 0;
+    pa.spp = 1;
+    pa.sample_offset = 0;
+    pa.cover_w = 1;
+    pa.keys = nullptr;
+    pa.out = vw->d_paths;
+    pa.track_share = 16;
+    pa.defer_in = vw->d_dq + in;
+    pa.defer_out = vw->d_dq + out;
+    pa.defer_at = pass == passes - 1 ? -1 : pass;
+    pa.views = vw->d_vd;
+    NE_CUDA(cudaMemsetAsync(vw->d_dcount + out, 0, sizeof(uint32_t), ctx->stream), "cudaMemsetAsync");
+    NE_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync");
+    NE_CUDA(ne_launch_path_split(pass, K_GENERAL, vw->blocks, ctx->stream, vw->sc->d, pa, counter, ctx->d_err),
+            "resume kernel launch");
+  }
   int rblocks = (int)std::min<uint64_t>((vw->total_pixels + 255) / 256, (uint64_t)ctx->sm_count * 16);
   NE_CUDA(ne_launch_reduce_views(std::max(1, rblocks), ctx->stream, vw->d_paths, vw->d_views, n, vw->total_pixels,
                                  vw->d_img),
@@ -1865,6 +1906,19 @@ ne_status ne_views_create(ne_scene* sc, const ne_view* views, uint32_t n, const 
   if (e == cudaSuccess) e = cudaMalloc(&vw->d_done, (2 * (size_t)n + 2) * sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaEventCreate(&vw->ev[0]);
   if (e == cudaSuccess) e = cudaEventCreate(&vw->ev[1]);
+  vw->defer_cap = std::max<size_t>(1024, (size_t)(total / 2));
+  for (PathState*& q : vw->d_defer)
+    if (e == cudaSuccess) e = cudaMalloc(&q, vw->defer_cap * sizeof(PathState));
+  if (e == cudaSuccess) e = cudaMalloc(&vw->d_dq, 2 * sizeof(DeferQueue));
+  if (e == cudaSuccess) e = cudaMalloc(&vw->d_dcount, 2 * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&vw->d_spans, n * sizeof(ViewSpan));
+  if (e == cudaSuccess) e = cudaMalloc(&vw->d_vd, sizeof(ViewDone));
+  if (e == cudaSuccess) {
+    DeferQueue dq[2];
+    for (int i = 0; i < 2; i++) dq[i] = DeferQueue{vw->d_defer[i], vw->d_dcount + i,
+                                                   (uint32_t)std::min<size_t>(vw->defer_cap, 0xFFFFFFFFu)};
+    e = cudaMemcpy(vw->d_dq, dq, sizeof(dq), cudaMemcpyHostToDevice);
+  }
   if (e != cudaSuccess) {
     ne_views_destroy(vw);
     return fail(ctx, NE_ERR_OUT_OF_MEMORY, std::string("ne_views_create: ") + cudaGetErrorString(e));
@@ -1885,7 +1939,8 @@ void ne_views_destroy(ne_views* vw) {
   cudaSetDevice(vw->sc->ctx->device);
   cudaStreamSynchronize(vw->sc->ctx->stream);
   if (vw->exec) cudaGraphExecDestroy(vw->exec);
-  void* bufs[] = {vw->d_views, vw->d_paths, vw->d_img, vw->d_done};
+  void* bufs[] = {vw->d_views, vw->d_paths, vw->d_img, vw->d_done, vw->d_defer[0], vw->d_defer[1], vw->d_dq,
+                  vw->d_dcount, vw->d_spans, vw->d_vd};
   for (void* b : bufs)
     if (b) cudaFree(b);
   for (cudaEvent_t e : vw->ev)
@@ -1895,7 +1950,8 @@ void ne_views_destroy(ne_views* vw) {
 
 ne_status ne_views_set_tuning(ne_views* vw, const ne_views_tuning* t) {
   if (!vw || !t || t->fetch < 32 || t->fetch > 4096 || t->fetch % 32 || t->blocks_per_sm < 0 ||
-      t->blocks_per_sm > 64 || t->order < 0 || t->order > 2 || t->graph < 0 || t->graph > 1)
+      t->blocks_per_sm > 64 || t->order < 0 || t->order > 2 || t->graph < 0 || t->graph > 1 || t->split_passes < 0 ||
+      t->split_passes > 64)
     return NE_ERR_INVALID_ARG;
   ne_context* ctx = vw->sc->ctx;
   NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
@@ -1957,8 +2013,9 @@ ne_status ne_views_autotune(ne_views* vw, int repeats, ne_views_tuning* best, do
   NE_CUDA(ne_views_occupancy(&fit), "occupancy query");
   fit = std::max(1, fit);
   const uint32_t fetches[2] = {32, 128};
-  const int bpss[2] = {fit, std::max(1, fit / 2)};
-  const int orders[3] = {0, 1, 2};
+  const int bpss[1] = {fit};
+  const int orders[2] = {1, 2};
+  const int passess[3] = {1, 4, 8};
   struct Trial {
     ne_views_tuning t;
     double ms;
@@ -1967,8 +2024,9 @@ ne_status ne_views_autotune(ne_views* vw, int repeats, ne_views_tuning* best, do
   std::vector<Trial> trials;
   for (uint32_t f : fetches)
     for (int b : bpss)
-      for (int o : orders) {
-        ne_views_tuning t = {f, b, o, 1};
+      for (int o : orders)
+        for (int sp : passess) {
+        ne_views_tuning t = {f, b, o, 1, sp};
         ne_status st = ne_views_set_tuning(vw, &t);
         if (st) return st;
         ne_views_stats s;

@@ -31,9 +31,12 @@ __global__ void k_reduce_views(const float* __restrict__ paths, const DView* __r
 
 }  // namespace nedev
 
-cudaError_t ne_launch_views(int blocks, cudaStream_t st, const nedev::DScene& s, const nedev::ViewArgs& a,
-                            unsigned long long* counter, uint32_t* err) {
-  nedev::k_views<nedev::K_GENERAL><<<blocks, nedev::kThreads, 0, st>>>(s, a, counter, err);
+cudaError_t ne_launch_views(bool split, int blocks, cudaStream_t st, const nedev::DScene& s,
+                            const nedev::ViewArgs& a, unsigned long long* counter, uint32_t* err) {
+  if (split)
+    nedev::k_views<nedev::K_GENERAL | nedev::K_SPLIT><<<blocks, nedev::kThreads, 0, st>>>(s, a, counter, err);
+  else
+    nedev::k_views<nedev::K_GENERAL><<<blocks, nedev::kThreads, 0, st>>>(s, a, counter, err);
   return cudaGetLastError();
 }
 

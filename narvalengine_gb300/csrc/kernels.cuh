@@ -26,6 +26,47 @@ constexpr int kThreads = 128;
 #endif
 constexpr int kPathMinBlocks = NE_PATH_MIN_BLOCKS;
 
+// Per-view completion accounting of a batch of views (see views.cuh): the path range of
+// every view in launch order, finished-path counts and completion times.
+struct ViewSpan {
+  unsigned long long path_begin, paths;
+};
+struct ViewDone {
+  const ViewSpan* spans;
+  uint32_t n;
+  unsigned long long* done;
+  unsigned long long* t_done;
+};
+
+__device__ __forceinline__ unsigned long long globalTimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ uint32_t findSpan(const ViewSpan* v, uint32_t n, unsigned long long idx) {
+  uint32_t lo = 0, hi = n - 1;
+  while (lo < hi) {
+    uint32_t mid = (lo + hi + 1) >> 1;
+    if (v[mid].path_begin <= idx) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Counts finished paths per view (one atomic per group of lanes of the same view; all 32
+// lanes call it, `v` = 0xffffffff for lanes without a finished path) and stamps the time of
+// each view's last path.
+__device__ __forceinline__ void countViewDone(const ViewDone& vd, uint32_t v) {
+  unsigned same = __match_any_sync(0xffffffffu, v);
+  const int lane = threadIdx.x & 31;
+  if (v != 0xffffffffu && lane == __ffs(same) - 1) {
+    unsigned long long n = (unsigned long long)__popc(same);
+    unsigned long long before = atomicAdd(&vd.done[v], n);
+    if (before + n == vd.spans[v].paths) vd.t_done[v] = globalTimer();
+  }
+}
+
 struct PathArgs {
   PathParams P;
   nerng::PathKey base;
@@ -42,6 +83,7 @@ struct PathArgs {
   const DeferQueue* defer_in = nullptr;
   const DeferQueue* defer_out = nullptr;
   int defer_at = -1;
+  const ViewDone* views = nullptr;  // resume passes of a batch of views: completion accounting
 };
 
 // Training paths of a cached render: a multiplicative hash of the path index, so training
@@ -129,6 +171,7 @@ __global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_resume(const __gri
     base = __shfl_sync(0xffffffffu, base, 0);
     if (base >= n) break;
     unsigned long long i = base + (unsigned long long)lane;
+    uint32_t finishedView = 0xffffffffu;
     if (i < n) {
       const PathState& ps = q.items[i];
       LiVars v = ps.v;
@@ -144,7 +187,12 @@ __global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_resume(const __gri
         a.out[3 * ps.idx + 0] = L.x;
         a.out[3 * ps.idx + 1] = L.y;
         a.out[3 * ps.idx + 2] = L.z;
+        if (a.views) finishedView = findSpan(a.views->spans, a.views->n, ps.idx);
       }
+    }
+    if (a.views) {
+      __syncwarp();
+      countViewDone(*a.views, finishedView);
     }
   }
 }

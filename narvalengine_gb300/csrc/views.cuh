@@ -36,13 +36,8 @@ struct ViewArgs {
   unsigned long long* done; // per view: finished paths
   unsigned long long* t_done;   // per view: global timer (ns) when its last path finished
   unsigned long long* t_start;  // global timer when the first warp started
+  const DeferQueue* defer_out;  // split batches: queue of paths deferred at their first event
 };
-
-__device__ __forceinline__ unsigned long long globalTimer() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
 
 // Index of the view owning path `idx` (views sorted by path_begin).
 __device__ __forceinline__ uint32_t findView(const DView* v, uint32_t n, unsigned long long idx) {
@@ -60,7 +55,7 @@ __global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_views(const __grid
                                                                     const ViewArgs a,
                                                                     unsigned long long* __restrict__ counter,
                                                                     uint32_t* err) {
-  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, nullptr, nullptr, 0ull, false, -1};
+  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, nullptr, a.defer_out, 0ull, false, 0};
   const int lane = threadIdx.x & 31;
   if (threadIdx.x == 0 && blockIdx.x == 0) atomicMin(a.t_start, globalTimer());
   for (;;) {
@@ -76,14 +71,22 @@ __global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_views(const __grid
         const DView& vw = a.views[v];
         unsigned long long local = idx - vw.path_begin;
         uint32_t pixel = (uint32_t)(local / vw.spp), sample = (uint32_t)(local % vw.spp);
+        if (K & K_SPLIT) {
+          c.idx = idx;
+          c.deferred = false;
+        }
         V3 L = cameraPathCam(c, a.P, a.base, vw.cam, vw.width, vw.height, pixel, sample, vw.stream);
-        a.out[3 * idx + 0] = L.x;
-        a.out[3 * idx + 1] = L.y;
-        a.out[3 * idx + 2] = L.z;
+        if ((K & K_SPLIT) && c.deferred) {
+          v = 0xffffffffu;  // counted when a resume pass finishes it
+        } else {
+          a.out[3 * idx + 0] = L.x;
+          a.out[3 * idx + 1] = L.y;
+          a.out[3 * idx + 2] = L.z;
+        }
       }
       __syncwarp();
       unsigned same = __match_any_sync(0xffffffffu, v);
-      if (live && lane == __ffs(same) - 1) {
+      if (v != 0xffffffffu && lane == __ffs(same) - 1) {
         unsigned long long n = (unsigned long long)__popc(same);
         unsigned long long before = atomicAdd(&a.done[v], n);
         if (before + n == a.views[v].paths) a.t_done[v] = globalTimer();
@@ -94,9 +97,10 @@ __global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_views(const __grid
 
 }  // namespace nedev
 
-// Launchers (k_views.cu): the general feature set covers every scene.
-cudaError_t ne_launch_views(int blocks, cudaStream_t st, const nedev::DScene& s, const nedev::ViewArgs& a,
-                            unsigned long long* counter, uint32_t* err);
+// Launchers (k_views.cu): the general feature set covers every scene. split: the first pass
+// of a split batch (paths deferred into a.defer_out at their first event).
+cudaError_t ne_launch_views(bool split, int blocks, cudaStream_t st, const nedev::DScene& s,
+                            const nedev::ViewArgs& a, unsigned long long* counter, uint32_t* err);
 cudaError_t ne_views_occupancy(int* blocks_per_sm);
 cudaError_t ne_launch_reduce_views(int blocks, cudaStream_t st, const float* paths, const nedev::DView* views,
                                    uint32_t n_views, uint32_t total_pixels, float* out);

@@ -64,14 +64,15 @@ def test_views_match_oracle(batch):
 
 def test_tunings_do_not_change_images(batch):
     ne, scene, vb, views, orc = batch
-    vb.set_tuning(fetch=32, order=0, graph=False)
+    vb.set_tuning(fetch=32, order=0, graph=False, split_passes=1)
     vb.render()
     ref = [vb.image(v) for v in range(len(views))]
-    for fetch, bps, order, graph in [(128, 0, 1, True), (64, 2, 2, True), (32, 1, 1, False)]:
-        vb.set_tuning(fetch=fetch, blocks_per_sm=bps, order=order, graph=graph)
+    for fetch, bps, order, graph, sp in [(128, 0, 1, True, 0), (64, 2, 2, True, 1), (32, 1, 1, False, 4),
+                                         (32, 0, 2, True, 8), (128, 0, 0, False, 2)]:
+        vb.set_tuning(fetch=fetch, blocks_per_sm=bps, order=order, graph=graph, split_passes=sp)
         st = vb.render()
         for v in range(len(views)):
-            assert np.array_equal(vb.image(v), ref[v]), (fetch, bps, order, graph, v)
+            assert np.array_equal(vb.image(v), ref[v]), (fetch, bps, order, graph, sp, v)
         lat = vb.latency()
         assert np.all(lat > 0) and lat.max() <= st["ms"] * 1.5 + 1.0, (lat, st)
         assert st["latency_p50_ms"] <= st["latency_p99_ms"] <= st["latency_max_ms"]
@@ -82,7 +83,8 @@ def test_autotune(batch):
     vb.render()
     ref = [vb.image(v) for v in range(len(views))]
     best, ms = vb.autotune(repeats=1)
-    assert ms > 0 and best["fetch"] in (32, 128) and best["order"] in (0, 1, 2) and best["graph"] == 1
+    assert ms > 0 and best["fetch"] in (32, 128) and best["order"] in (1, 2) and best["graph"] == 1
+    assert best["split_passes"] in (1, 4, 8)
     assert vb.tuning() == best
     vb.render()
     for v in range(len(views)):
