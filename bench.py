@@ -297,14 +297,14 @@ def run_views(args, rank: int, world: int, local: int):
     d.close()
 
 
-def run_profile_case(spp: int, kernel: int, track_share: int):
+def run_profile_case(spp: int, kernel: int, track_share: int, split_passes: int = 0):
     """Small case for ncu: the same scene at a reduced sample count, rendered twice."""
     import narvalengine_gb300 as ne
     ctx = ne.Context(0)
     host = ne.SceneHost.from_json(os.path.join(ne.SCENES_DIR, SCENE))
     scene = ctx.upload(host)
     if kernel >= 0:
-        scene.set_tuning(kernel=kernel, track_share=track_share)
+        scene.set_tuning(kernel=kernel, track_share=track_share, split_passes=split_passes)
     for i in range(2):
         _, st = scene.render(ne.render_params(seed=1, spp=spp))
     _, cst = scene.render(ne.render_params(seed=1, spp=spp, flags=ne.NE_RENDER_COUNT_WORK))
@@ -342,7 +342,7 @@ def main():
         run_reference(args, rank, world)
         return
     if args.profile_spp > 0:
-        run_profile_case(args.profile_spp, args.kernel, args.track_share)
+        run_profile_case(args.profile_spp, args.kernel, args.track_share, args.split_passes)
         return
 
     if args.scene == "views_c5":
