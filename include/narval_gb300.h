@@ -293,6 +293,12 @@ ne_status ne_render_cached(ne_scene* scene, ne_cache* cache, const ne_render_par
                            const ne_cache_render_params* cache_params, float* out_rgb, ne_render_stats* stats,
                            ne_cache_render_stats* cache_stats);
 
+/* BVH::init (primitives/BVH.cpp:6-106) as ne_scene_upload builds it, on the host (no GPU
+ * needed), over triangles prims[first, first + count): 9 words per node (min, max, then start,
+ * count, rightOffset as uint32 bits) and the primitive order. */
+ne_status ne_debug_bvh(const ne_primitive* prims, uint32_t first, uint32_t count, float* nodes, size_t cap,
+                       uint32_t* order, size_t* n_nodes);
+
 /* One 128 x n x k tensor-core product D = A * B^T (BF16 bit patterns, row-major A[128][k],
  * B[n][k]; FP32 D[128][n]) through the same shared-memory and tensor-memory conventions as
  * the radiance-cache kernels. n in 16..256 step 16, k in 16..128 step 16. */

@@ -189,5 +189,7 @@ SIGNATURES = {
     "ne_views_render": (C.c_int32, [C.c_void_p, C.POINTER(NeViewsStats)]),
     "ne_views_latency": (C.c_int32, [C.c_void_p, C.c_void_p]),
     "ne_views_image": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p]),
+    "ne_debug_bvh": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_size_t, C.c_void_p,
+                                 C.POINTER(C.c_size_t)]),
     "ne_debug_mma": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
 }

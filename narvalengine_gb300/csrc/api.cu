@@ -16,6 +16,8 @@
 #include <string.h>
 
 #include <algorithm>
+#include <future>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -199,65 +201,125 @@ void triBounds(const ne_primitive& p, H3& mn, H3& mx) {
 }
 inline H3 boxCenter(H3 mn, H3 mx) { return hsub(mx, hdiv(hsub(mx, mn), 2.0f)); }
 
-// primitives/BVH.cpp:6-106 BVH::init: depth-first node order, left child = i + 1,
-// right child = i + rightOffset, leaves of <= 4 triangles, midpoint split on the
-// longest axis of the centroid bounds with a median fallback.
-void buildBvh(const ne_primitive* prims, std::vector<uint32_t>& order, std::vector<HNode>& nodes) {
-  const uint32_t perLeaf = 4, notVisited = 0xffffffffu, visitedTwice = 0xfffffffdu, rootParent = 0xfffffffcu;
-  struct Item { uint32_t parent, start, end; };
-  nodes.assign(order.size() * 2 + 1, HNode{});
-  std::vector<Item> stack;
-  uint32_t nodeCount = 0;
-  stack.push_back(Item{rootParent, 0, (uint32_t)order.size()});
+// primitives/BVH.cpp:6-106 BVH::init, one node: bounds of order[start, end), the leaf
+// decision (<= 4 triangles) and, for an interior node, the midpoint split on the longest axis
+// of the centroid bounds with a median fallback, partitioning `order` in place. Returns the
+// node (rightOffset 0 for a leaf) and the split position in `mid`.
+HNode bvhNode(const ne_primitive* prims, uint32_t* order, uint32_t start, uint32_t end, uint32_t& mid) {
+  const uint32_t perLeaf = 4;
   const float inf = INFINITY;
+  HNode node;
+  node.start = start;
+  node.count = end - start;
+  node.rightOffset = 1;
+  H3 bbMin = h3(inf, inf, inf), bbMax = h3(-inf, -inf, -inf), pmn, pmx;
+  triBounds(prims[order[start]], pmn, pmx);
+  bbMin = hvmin(bbMin, pmn);
+  bbMax = hvmax(bbMax, pmx);
+  H3 bcMin = boxCenter(bbMin, bbMax), bcMax = bcMin;
+  for (uint32_t i = start + 1; i < end; i++) {
+    triBounds(prims[order[i]], pmn, pmx);
+    bbMin = hvmin(bbMin, pmn);
+    bbMax = hvmax(bbMax, pmx);
+    H3 c = boxCenter(pmn, pmx);
+    bcMin = hvmin(bcMin, c);
+    bcMax = hvmax(bcMax, c);
+  }
+  node.mn = bbMin;
+  node.mx = bbMax;
+  mid = 0;
+  if (node.count <= perLeaf) {
+    node.rightOffset = 0;
+    return node;
+  }
+  H3 ext = hsub(bcMax, bcMin);
+  int dim = 0;
+  if (hcomp(ext, 1) > hcomp(ext, dim)) dim = 1;
+  if (hcomp(ext, 2) > hcomp(ext, dim)) dim = 2;
+  float split = 0.5f * (hcomp(bcMin, dim) + hcomp(bcMax, dim));
+  mid = start;
+  for (uint32_t i = start; i < end; i++) {
+    triBounds(prims[order[i]], pmn, pmx);
+    if (hcomp(boxCenter(pmn, pmx), dim) < split) {
+      std::swap(order[i], order[mid]);
+      mid++;
+    }
+  }
+  if (mid == start || mid == end) mid = start + (end - start) / 2;
+  return node;
+}
+
+// BVH::init of order[start, end) appended to `nodes` in depth-first order (left child = i + 1,
+// right child = i + rightOffset), the reference's stack traversal.
+void buildRange(const ne_primitive* prims, uint32_t* order, uint32_t start, uint32_t end, std::vector<HNode>& nodes) {
+  struct Item { uint32_t parent, start, end; bool right; };
+  const uint32_t rootParent = 0xffffffffu;
+  const size_t base = nodes.size();
+  std::vector<Item> stack;
+  stack.push_back(Item{rootParent, start, end, false});
   while (!stack.empty()) {
     Item it = stack.back();
     stack.pop_back();
-    nodeCount++;
-    HNode node;
-    node.start = it.start;
-    node.count = it.end - it.start;
-    node.rightOffset = notVisited;
-    H3 bbMin = h3(inf, inf, inf), bbMax = h3(-inf, -inf, -inf), pmn, pmx;
-    triBounds(prims[order[node.start]], pmn, pmx);
-    bbMin = hvmin(bbMin, pmn);
-    bbMax = hvmax(bbMax, pmx);
-    H3 bcMin = boxCenter(bbMin, bbMax), bcMax = bcMin;
-    for (uint32_t i = it.start + 1; i < it.end; i++) {
-      triBounds(prims[order[i]], pmn, pmx);
-      bbMin = hvmin(bbMin, pmn);
-      bbMax = hvmax(bbMax, pmx);
-      H3 c = boxCenter(pmn, pmx);
-      bcMin = hvmin(bcMin, c);
-      bcMax = hvmax(bcMax, c);
-    }
-    node.mn = bbMin;
-    node.mx = bbMax;
-    if (node.count <= perLeaf) node.rightOffset = 0;
-    nodes[nodeCount - 1] = node;
-    if (it.parent != rootParent) {
-      nodes[it.parent].rightOffset--;
-      if (nodes[it.parent].rightOffset == visitedTwice) nodes[it.parent].rightOffset = nodeCount - 1 - it.parent;
-    }
+    uint32_t mid;
+    HNode node = bvhNode(prims, order, it.start, it.end, mid);
+    uint32_t self = (uint32_t)(nodes.size() - base);
+    nodes.push_back(node);
+    if (it.right) nodes[base + it.parent].rightOffset = self - it.parent;
     if (node.rightOffset == 0) continue;
-    H3 ext = hsub(bcMax, bcMin);
-    int dim = 0;
-    if (hcomp(ext, 1) > hcomp(ext, dim)) dim = 1;
-    if (hcomp(ext, 2) > hcomp(ext, dim)) dim = 2;
-    float split = 0.5f * (hcomp(bcMin, dim) + hcomp(bcMax, dim));
-    uint32_t mid = it.start;
-    for (uint32_t i = it.start; i < it.end; i++) {
-      triBounds(prims[order[i]], pmn, pmx);
-      if (hcomp(boxCenter(pmn, pmx), dim) < split) {
-        std::swap(order[i], order[mid]);
-        mid++;
-      }
-    }
-    if (mid == it.start || mid == it.end) mid = it.start + (it.end - it.start) / 2;
-    stack.push_back(Item{nodeCount - 1, mid, it.end});
-    stack.push_back(Item{nodeCount - 1, it.start, mid});
+    stack.push_back(Item{self, mid, it.end, true});
+    stack.push_back(Item{self, it.start, mid, false});
   }
-  nodes.resize(nodeCount);
+}
+
+// The same tree built with subtrees in parallel: nodes above depth kBvhTaskDepth are split by
+// one task while another builds their left child; every node is computed exactly as in the
+// sequential build (ranges of `order` are disjoint), and the subtrees are laid out in the
+// same depth-first order, so the node array is identical.
+struct BvhTop {
+  HNode node;
+  bool sub = false;
+  std::vector<HNode> subtree;
+  std::unique_ptr<BvhTop> l, r;
+};
+constexpr int kBvhTaskDepth = 6;
+constexpr uint32_t kBvhTaskMin = 4096;
+
+std::unique_ptr<BvhTop> buildTop(const ne_primitive* prims, uint32_t* order, uint32_t start, uint32_t end, int depth) {
+  std::unique_ptr<BvhTop> t(new BvhTop());
+  if (depth >= kBvhTaskDepth || end - start < kBvhTaskMin) {
+    t->sub = true;
+    t->subtree.reserve((size_t)(end - start) / 2 + 8);
+    buildRange(prims, order, start, end, t->subtree);
+    return t;
+  }
+  uint32_t mid;
+  t->node = bvhNode(prims, order, start, end, mid);
+  if (t->node.rightOffset == 0) return t;
+  auto left = std::async(std::launch::async, buildTop, prims, order, start, mid, depth + 1);
+  t->r = buildTop(prims, order, mid, end, depth + 1);
+  t->l = left.get();
+  return t;
+}
+
+void emitTop(BvhTop* t, std::vector<HNode>& out) {
+  if (t->sub) {
+    out.insert(out.end(), t->subtree.begin(), t->subtree.end());
+    return;
+  }
+  size_t self = out.size();
+  out.push_back(t->node);
+  if (t->node.rightOffset == 0) return;
+  emitTop(t->l.get(), out);
+  out[self].rightOffset = (uint32_t)(out.size() - self);
+  emitTop(t->r.get(), out);
+}
+
+void buildBvh(const ne_primitive* prims, std::vector<uint32_t>& order, std::vector<HNode>& nodes) {
+  nodes.clear();
+  if (order.empty()) return;
+  std::unique_ptr<BvhTop> top = buildTop(prims, order.data(), 0, (uint32_t)order.size(), 0);
+  nodes.reserve(order.size() / 2 + 16);
+  emitTop(top.get(), nodes);
 }
 
 // ---------------------------------------------------------------- kernels
@@ -2112,6 +2174,27 @@ ne_status ne_scene_autotune(ne_scene* sc, const ne_render_params* p, int repeats
   if (st) return st;
   if (best) ne_scene_get_tuning(sc, best);
   if (best_ms) *best_ms = bms;
+  return NE_OK;
+}
+
+ne_status ne_debug_bvh(const ne_primitive* prims, uint32_t first, uint32_t count, float* nodes, size_t cap,
+                       uint32_t* order, size_t* n_nodes) {
+  if (!prims || !nodes || !order || !n_nodes || count == 0) return NE_ERR_INVALID_ARG;
+  std::vector<uint32_t> ord(count);
+  for (uint32_t k = 0; k < count; k++) ord[k] = first + k;
+  std::vector<HNode> hn;
+  buildBvh(prims, ord, hn);
+  *n_nodes = hn.size();
+  if (hn.size() > cap) return NE_ERR_INVALID_ARG;
+  for (size_t i = 0; i < hn.size(); i++) {
+    float* o = nodes + 9 * i;
+    o[0] = hn[i].mn.x; o[1] = hn[i].mn.y; o[2] = hn[i].mn.z;
+    o[3] = hn[i].mx.x; o[4] = hn[i].mx.y; o[5] = hn[i].mx.z;
+    memcpy(o + 6, &hn[i].start, 4);
+    memcpy(o + 7, &hn[i].count, 4);
+    memcpy(o + 8, &hn[i].rightOffset, 4);
+  }
+  memcpy(order, ord.data(), count * sizeof(uint32_t));
   return NE_OK;
 }
 

@@ -1574,4 +1574,24 @@ void orc_philox(const uint32_t* c, const uint32_t* k, uint32_t* out) {
   for (int i = 0; i < 4; i++) out[i] = b.w[i];
 }
 
+// The BVH of model `m` as built by BVH::init: per node (min xyz, max xyz, start, count,
+// rightOffset) as 9 words (floats then uint32 bit patterns); `order` receives the primitive
+// order. Returns the node count (0 when the model has no BVH); writes at most `cap` nodes.
+size_t orc_model_bvh(const orc_scene* s, uint32_t m, float* nodes, size_t cap, uint32_t* order) {
+  if (!s || m >= s->omodels.size()) return 0;
+  const OModel& om = s->omodels[m];
+  if (om.nodeCount == 0) return 0;
+  for (size_t i = 0; i < om.nodeCount && i < cap; i++) {
+    const BVHNode& n = om.nodes[i];
+    float* o = nodes + 9 * i;
+    o[0] = n.mn.x; o[1] = n.mn.y; o[2] = n.mn.z;
+    o[3] = n.mx.x; o[4] = n.mx.y; o[5] = n.mx.z;
+    memcpy(o + 6, &n.start, 4);
+    memcpy(o + 7, &n.count, 4);
+    memcpy(o + 8, &n.rightOffset, 4);
+  }
+  if (order) memcpy(order, om.prims.data(), om.prims.size() * sizeof(uint32_t));
+  return om.nodeCount;
+}
+
 }  // extern "C"

@@ -46,6 +46,9 @@ double orc_render_pixels(const orc_scene* s, const ne_render_params* p, uint32_t
                          float* out_rgb, int n_threads, uint64_t* density_lookups);
 void orc_trace_closest(const orc_scene* s, const ne_ray* rays, size_t n, float t_min, float t_max, ne_hit* out);
 
+/* BVH::init result of model m: 9 words per node (min, max, start, count, rightOffset). */
+size_t orc_model_bvh(const orc_scene* s, uint32_t m, float* nodes, size_t cap, uint32_t* order);
+
 /* Unit-level restatements for known-answer tests. */
 int orc_triangle_intersect(const float* v0, const float* v1, const float* v2, const ne_ray* r, float* t_near,
                            float* t_far, float* point, float* normal);

@@ -30,6 +30,7 @@ SIGNATURES = {
     "orc_trace_paths": (None, [C.c_void_p, C.POINTER(NeRenderParams), C.c_void_p, C.c_size_t, C.c_void_p, C.c_int]),
     "orc_trace_view_paths": (None, [C.c_void_p, C.POINTER(NeRenderParams), C.c_void_p, C.c_int, C.c_int, C.c_uint32,
                                      C.c_void_p, C.c_size_t, C.c_void_p, C.c_int]),
+    "orc_model_bvh": (C.c_size_t, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_size_t, C.c_void_p]),
     "orc_li_batch": (None, [C.c_void_p, C.POINTER(NeRenderParams), C.c_void_p, C.c_void_p, C.c_size_t, C.c_uint32,
                             C.c_void_p, C.c_int]),
     "orc_render": (C.c_double, [C.c_void_p, C.POINTER(NeRenderParams), C.c_void_p, C.c_int]),
@@ -109,6 +110,13 @@ class OracleScene:
         self._lib.orc_trace_view_paths(self._h, C.byref(params), C.byref(camera), width, height, stream, _p(keys),
                                        len(keys), _p(out), threads or os.cpu_count())
         return out
+
+    def model_bvh(self, m: int, n_prims: int):
+        """(nodes (n, 9) float32 with the last three words as uint32 bits, primitive order)."""
+        nodes = np.empty((2 * n_prims + 1, 9), np.float32)
+        order = np.empty(n_prims, np.uint32)
+        n = self._lib.orc_model_bvh(self._h, m, _p(nodes), len(nodes), _p(order))
+        return nodes[:n], order
 
     def li_batch(self, rays: np.ndarray, keys: np.ndarray, first_dim: int, params: NeRenderParams,
                  threads: int = 0) -> np.ndarray:
