@@ -11,9 +11,10 @@ sqrt(1 - cos^2) without clamping, which is NaN when cos rounds past +-1; about 1
 the medium scene's paths); those paths are dropped from every accumulated image and
 counted (`dropped_paths`).
 
-Time-to-relMSE renders progressively, doubling the samples per pixel (1, 2, 4, ...), until
-the image's relMSE against the reference is at or below the target, and reports the
-cumulative device time of the samples rendered so far.
+Time-to-relMSE renders progressively, measuring relMSE whenever the sample count has grown
+by about 10% (16, 32, 48, ... samples per pixel), until the image's relMSE against the
+reference is at or below the target, and reports the cumulative device time of the samples
+rendered so far.
 
     python -m narvalengine_gb300.convergence --scene medium_c2 --ref-spp 65536 --target 1e-3
 """
@@ -65,9 +66,18 @@ def reference_image(scene, spp: int, seed: int = REF_SEED, chunk: int = 256, inf
     return (acc / float(spp)).cpu().numpy(), ms
 
 
+def checkpoints(first: int, max_spp: int, step: float = 1.1):
+    """Sample counts at which relMSE is measured: from `first`, growing by about 10% each."""
+    out, s = [], first
+    while s <= max_spp:
+        out.append(s)
+        s = max(s + first, int(round(s * step / first)) * first)
+    return out
+
+
 def time_to_relmse(scene, ref: np.ndarray, target: float = 1e-3, seed: int = 0, max_spp: int = 1 << 16,
-                   chunk: int = 256) -> dict:
-    """Progressive render (samples added in powers of two) until relMSE <= target.
+                   chunk: int = 256, first: int = 16) -> dict:
+    """Progressive render until relMSE <= target, measured at sample counts growing by ~10%.
 
     `ms` is the cumulative device time of all samples up to that point, the time a
     progressive renderer needs to reach the target."""
@@ -75,10 +85,10 @@ def time_to_relmse(scene, ref: np.ndarray, target: float = 1e-3, seed: int = 0, 
     H, W = scene.host.height, scene.host.width
     acc = torch.zeros((H, W, 3), dtype=torch.float64, device=f"cuda:{scene.ctx.device}")
     curve = []
-    have, spp, ms = 0, 1, 0.0
+    have, ms = 0, 0.0
     hit = None
     dropped = [0]
-    while spp <= max_spp:
+    for spp in checkpoints(first, max_spp):
         ms += _accumulate(scene, acc, seed, have, spp - have, chunk, dropped)
         have = spp
         e = relmse((acc / float(spp)).cpu().numpy(), ref)
@@ -86,7 +96,6 @@ def time_to_relmse(scene, ref: np.ndarray, target: float = 1e-3, seed: int = 0, 
         if e <= target:
             hit = curve[-1]
             break
-        spp *= 2
     return {"target": target, "reached": hit is not None, "spp": hit["spp"] if hit else None,
             "ms": hit["ms"] if hit else None, "dropped_paths": dropped[0], "curve": curve}
 
@@ -97,14 +106,16 @@ def time_to_relmse_cached(scene, cache, ref: np.ndarray, target: float = 1e-3, s
     """Progressive rendering with the radiance cache trained online: frames of `frame_spp`
     samples, each rendered with the cache as it stands and then used for `train_steps`
     optimiser steps on the frame's training samples. The running FP64 mean of the frames is
-    compared with the reference whenever the sample count reaches a power of two; `ms` is the
+    compared with the reference at the same checkpoints as the plain render; `ms` is the
     cumulative device time of the frames (path kernel, network inference, training)."""
     acc = np.zeros_like(ref, dtype=np.float64)
     curve = []
-    have, ms, check = 0, 0.0, frame_spp
+    have, ms = 0, 0.0
+    checks = checkpoints(frame_spp, max_spp)
+    ci = 0
     parts = {"path_ms": 0.0, "infer_ms": 0.0, "train_ms": 0.0, "queries": 0, "train_samples": 0, "paths": 0}
     hit = None
-    while have < max_spp:
+    while have < max_spp and ci < len(checks):
         img, st, cst = scene.render_cached(cache, bounce=bounce, train_stride=train_stride, train_steps=train_steps,
                                            train_batch=train_batch, seed=seed, spp=frame_spp, sample_offset=have)
         ms += st["total_ms"]
@@ -114,10 +125,10 @@ def time_to_relmse_cached(scene, cache, ref: np.ndarray, target: float = 1e-3, s
         finite = np.isfinite(img)
         acc += np.where(finite, img, 0.0) * frame_spp
         have += frame_spp
-        if have >= check:
+        if have >= checks[ci]:
+            ci += 1
             e = relmse(acc / have, ref)
             curve.append({"spp": have, "relmse": e, "ms": ms, "loss": cst["loss"]})
-            check *= 2
             if e <= target:
                 hit = curve[-1]
                 break

@@ -27,7 +27,7 @@ def test_relmse_definition():
 def test_relmse_falls_as_one_over_spp(built, name):
     """Monte Carlo error: relMSE ~ 1/spp, so on the medium scene 4x the samples gives about
     1/4 the relMSE. (The Cornell box is left out: its GGX paths produce rare radiance values
-    of order 1e6, so its relMSE falls irregularly even at 64k samples per pixel.)"""
+    of order 1e3-1e4, so its relMSE falls irregularly even at 64k samples per pixel.)"""
     import narvalengine_gb300 as ne
     from narvalengine_gb300.convergence import reference_image, time_to_relmse
     ctx = ne.Context(0)
@@ -37,8 +37,8 @@ def test_relmse_falls_as_one_over_spp(built, name):
         assert ms > 0 and np.all(np.isfinite(ref)) and ref.min() >= 0
         res = time_to_relmse(scene, ref, target=1e-9, max_spp=1024)
         curve = {c["spp"]: c["relmse"] for c in res["curve"]}
-        assert not res["reached"] and sorted(curve) == [2 ** k for k in range(11)]
-        for s in (16, 64, 256):
+        assert not res["reached"] and sorted(curve)[0] == 16 and 896 in curve
+        for s in (16, 32, 64, 224):
             ratio = curve[s] / curve[4 * s]
             assert 2.5 < ratio < 6.5, (s, ratio, curve)
         times = [c["ms"] for c in res["curve"]]
