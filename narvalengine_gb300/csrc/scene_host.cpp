@@ -13,6 +13,9 @@
 //    little-endian float32 voxels.
 //  * material "infiniteAreaLight": "radiance": [r,g,b] is a constant environment, i.e.
 //    the reference's InfiniteAreaLight over a 1x1 map of that value.
+//  * primitive "obj": read from the OBJ file directly (positions and faces) instead of through
+//    assimp, with the JSON materialName; primitives naming the same file and material share
+//    one model (one BVH), each with its own transform.
 //  * primitive "mesh": a triangle mesh given inline ("positions", "indices") or by the
 //    "icosphere" generator, loaded as the reference loads an obj/gltf model (bounding
 //    box and BVH); optional "groups" assign seeded GGX materials per triangle group.
@@ -300,6 +303,7 @@ namespace {
 struct Reader {
   ne_scene_host& S;
   std::string res_dir;
+  std::map<std::string, uint32_t> objModels;  // (path, material) -> model, shared by instances
 
   std::string assetPath(const std::string& rel) const {
     if (!rel.empty() && rel[0] == '/') return rel;
@@ -553,9 +557,7 @@ struct Reader {
     };
     ne_primitive pr;
     memset(&pr, 0, sizeof(pr));
-    if (type == "obj" || type == "gltf") {
-      throw ParseError(NE_ERR_UNSUPPORTED, ctx + ": " + type + " models need an asset importer; use a \"mesh\" primitive.");
-    } else if (type == "point") {
+    if (type == "point") {
       readSR();
       int mat = materialNamed(sval(need(p, "materialName", ctx), ctx), ctx);
       pr.type = NE_PRIM_POINT;
@@ -594,6 +596,31 @@ struct Reader {
       readSR();
       mesh(p, ctx);
       addInstance(getTransform(pos, rot, scale), (uint32_t)S.models.size() - 1, collision, false);
+    } else if (type == "obj") {
+      // SceneReader.cpp:245-266: a model file under RESOURCES_DIR with an InstancedModel. The
+      // reference loads it through assimp (ResourceManager::loadModel, Model.cpp:137-370); here
+      // the OBJ text is read directly, with the JSON materialName for every triangle.
+      readSR();
+      std::string path = sval(need(p, "path", ctx), ctx + " path");
+      if (!p.get("materialName"))
+        throw ParseError(NE_ERR_UNSUPPORTED, ctx + ": obj models need a materialName (MTL materials are not read).");
+      std::string matName = sval(*p.get("materialName"), ctx);
+      std::string key = path + "\n" + matName;
+      uint32_t mi;
+      auto it = objModels.find(key);
+      if (it != objModels.end()) {
+        mi = it->second;  // same file and material: instances share one model and its BVH
+      } else {
+        std::vector<float> vpos;
+        std::vector<uint32_t> vidx;
+        readObj(assetPath(path), vpos, vidx, ctx);
+        meshModel(vpos, vidx, p, ctx);
+        mi = (uint32_t)S.models.size() - 1;
+        objModels[key] = mi;
+      }
+      addInstance(getTransform(pos, rot, scale), mi, collision, false);
+    } else if (type == "gltf") {
+      throw ParseError(NE_ERR_UNSUPPORTED, ctx + ": gltf models are not supported (obj only).");
     } else {
       throw ParseError(NE_ERR_PARSE, "Invalid primitive type while reading scene from json file.");
     }
@@ -624,6 +651,69 @@ struct Reader {
       for (uint32_t i : idx)
         if ((size_t)i * 3 + 2 >= pos.size()) throw ParseError(NE_ERR_PARSE, ctx + ": index out of range.");
     }
+    meshModel(pos, idx, p, ctx);
+  }
+
+  // Wavefront OBJ positions and faces: "v x y z", "f a b c ..." with a, a/t, a/t/n or a//n
+  // (1-based, negative = relative to the end); polygons become triangle fans (v0, vi, vi+1),
+  // as assimp's triangulation of convex faces.
+  void readObj(const std::string& file, std::vector<float>& pos, std::vector<uint32_t>& idx, const std::string& ctx) {
+    FILE* f = fopen(file.c_str(), "rb");
+    if (!f) throw ParseError(NE_ERR_MISSING_ASSET, ctx + ": cannot open " + file);
+    std::string text;
+    char buf[1 << 16];
+    size_t r;
+    while ((r = fread(buf, 1, sizeof buf, f)) > 0) text.append(buf, r);
+    fclose(f);
+    size_t i = 0, line = 0;
+    std::vector<long> face;
+    while (i < text.size()) {
+      size_t e = text.find('\n', i);
+      if (e == std::string::npos) e = text.size();
+      std::string ln = text.substr(i, e - i);
+      i = e + 1;
+      line++;
+      if (!ln.empty() && ln.back() == '\r') ln.pop_back();
+      size_t k = ln.find_first_not_of(" \t");
+      if (k == std::string::npos || ln[k] == '#') continue;
+      const char* c = ln.c_str() + k;
+      if (c[0] == 'v' && (c[1] == ' ' || c[1] == '\t')) {
+        float x, y, z;
+        if (sscanf(c + 1, "%f %f %f", &x, &y, &z) != 3)
+          throw ParseError(NE_ERR_PARSE, ctx + ": bad vertex at line " + std::to_string(line));
+        pos.push_back(x);
+        pos.push_back(y);
+        pos.push_back(z);
+      } else if (c[0] == 'f' && (c[1] == ' ' || c[1] == '\t')) {
+        face.clear();
+        const char* q = c + 1;
+        for (;;) {
+          while (*q == ' ' || *q == '\t') q++;
+          if (!*q) break;
+          char* endp = nullptr;
+          long v = strtol(q, &endp, 10);
+          if (endp == q) throw ParseError(NE_ERR_PARSE, ctx + ": bad face at line " + std::to_string(line));
+          long nv = (long)(pos.size() / 3);
+          long vi = v > 0 ? v - 1 : nv + v;
+          if (vi < 0 || vi >= nv) throw ParseError(NE_ERR_PARSE, ctx + ": face index out of range at line " + std::to_string(line));
+          face.push_back(vi);
+          q = endp;
+          while (*q && *q != ' ' && *q != '\t') q++;  // skip /t/n
+        }
+        if (face.size() < 3) throw ParseError(NE_ERR_PARSE, ctx + ": face with fewer than 3 vertices at line " + std::to_string(line));
+        for (size_t t = 1; t + 1 < face.size(); t++) {
+          idx.push_back((uint32_t)face[0]);
+          idx.push_back((uint32_t)face[t]);
+          idx.push_back((uint32_t)face[t + 1]);
+        }
+      }
+    }
+  }
+
+  // A triangle model (primitives/Model.cpp:4-7, 337-370): bounding box over the vertices,
+  // BVH over the triangles; materials from "materialName" or seeded "groups".
+  void meshModel(const std::vector<float>& pos, const std::vector<uint32_t>& idx, const JVal& p,
+                 const std::string& ctx) {
     uint32_t nt = (uint32_t)(idx.size() / 3);
     if (nt == 0) throw ParseError(NE_ERR_PARSE, ctx + ": mesh has no triangles.");
     // materials: one named material, or seeded groups
