@@ -107,6 +107,12 @@ ne_status ne_camera_look_at(const float position[3], const float look_at[3], flo
                             int height, float focus, ne_camera* out);
 void ne_scene_host_destroy(ne_scene_host* s);
 
+/* Image files of a width*height*3 float image, row y*width+x (materials/Texture.h:44-75
+ * saveImage): PNG with each channel clamped to [0, 1] and stored as (uint8)(v * 255), and EXR
+ * with FP32 R, G, B channels. */
+ne_status ne_save_png(const char* path, const float* rgb, int width, int height);
+ne_status ne_save_exr(const char* path, const float* rgb, int width, int height);
+
 /* ---- device ---- */
 
 ne_status ne_context_create(int device, ne_context** out);

@@ -453,6 +453,21 @@ class RadianceCache:
         self._h = None
 
 
+def save_image(path: str, rgb: np.ndarray) -> None:
+    """saveImage (materials/Texture.h:44-75): PNG (clamped to [0, 1], 8 bits) or EXR (FP32) by
+    the file extension; rgb is an (H, W, 3) float image."""
+    img = np.ascontiguousarray(rgb, dtype=np.float32)
+    h, w = img.shape[:2]
+    if path.lower().endswith(".png"):
+        st = library().ne_save_png(path.encode(), _ptr(img), w, h)
+    elif path.lower().endswith(".exr"):
+        st = library().ne_save_exr(path.encode(), _ptr(img), w, h)
+    else:
+        raise ValueError("save_image writes .png or .exr")
+    if st != 0:
+        raise NarvalError(st, f"cannot write {path}")
+
+
 def tone_map(hdr: np.ndarray) -> np.ndarray:
     """OfflineEngine::postProcessing (core/OfflineEngine.cpp:39-52): exposure 0.5, gamma 2.2, clamp."""
     mapped = np.float32(1.0) - np.exp(-hdr.astype(np.float32) * np.float32(0.5))
