@@ -16,13 +16,14 @@
 namespace nedev {
 
 constexpr int kThreads = 128;
-// Resident blocks per SM the straight and lane-refill kernels are compiled for: 10 x 128
-// threads caps them at 48 registers. The spills this costs are cheaper than the
-// instruction-fetch and latency stalls that fewer resident warps leave exposed. Measured
-// (Mpaths/s, medium / mesh scene): uncapped 123 registers 339 / 113, 8 blocks 383 / 127,
-// 10 blocks 397 / 139, 12 blocks 393 / 127.
+// Resident blocks per SM the path kernels are compiled for: 8 x 128 threads caps them at 64
+// registers. The spills this costs are cheaper than the latency stalls that fewer resident
+// warps leave exposed. Measured (Mpaths/s, medium / Cornell / dense cloud, split kernel): 6
+// blocks 1338 / 589 / 264, 8 blocks 1316 / 573 / 282, 10 blocks 1186 / 546 / 252; before the
+// split (one pass, medium / mesh): uncapped 123 registers 339 / 113, 8 blocks 383 / 127,
+// 10 blocks 397 / 139.
 #ifndef NE_PATH_MIN_BLOCKS
-#define NE_PATH_MIN_BLOCKS 10
+#define NE_PATH_MIN_BLOCKS 8
 #endif
 constexpr int kPathMinBlocks = NE_PATH_MIN_BLOCKS;
 
