@@ -152,6 +152,7 @@ def main(argv=None):
     ap.add_argument("--frame-spp", type=int, default=16)
     ap.add_argument("--bounce", type=int, nargs="+", default=[2], help="cache termination bounce(s) to measure")
     ap.add_argument("--train-steps", type=int, default=4)
+    ap.add_argument("--train-stride", type=int, default=16)
     args = ap.parse_args(argv)
     path = args.scene if args.scene.endswith(".json") else os.path.join(ne.SCENES_DIR, args.scene + ".json")
     if args.resolution:
@@ -162,6 +163,7 @@ def main(argv=None):
         host = ne.SceneHost.from_json(path)
     ctx = ne.Context(0)
     scene = ctx.upload(host)
+    tuning, _ = scene.autotune(repeats=1, seed=3, spp=max(1, args.chunk // 4))
     t0 = time.time()
     info = {}
     ref, ref_ms = reference_image(scene, args.ref_spp, chunk=args.chunk, info=info)
@@ -173,14 +175,15 @@ def main(argv=None):
         for bounce in args.bounce:
             cache = ne.RadianceCache(ctx, seed=1)
             r = time_to_relmse_cached(scene, cache, ref, args.target, max_spp=args.max_spp, frame_spp=args.frame_spp,
-                                      bounce=bounce, train_steps=args.train_steps)
+                                      bounce=bounce, train_steps=args.train_steps, train_stride=args.train_stride)
             cache.close()
             if res["reached"] and r["reached"]:
                 r["time_ratio_vs_plain"] = r["ms"] / res["ms"]
             res["cache"].append(r)
     out = {"scene": os.path.basename(path), "resolution": [host.width, host.height], "ref_spp": args.ref_spp,
            "ref_paths": host.width * host.height * args.ref_spp, "ref_device_ms": ref_ms,
-           "ref_wall_s": time.time() - t0, "ref_dropped_paths": info["dropped_paths"], "relmse_eps": EPS, **res}
+           "ref_wall_s": time.time() - t0, "ref_dropped_paths": info["dropped_paths"], "relmse_eps": EPS,
+           "tuning": tuning, **res}
     print(json.dumps(out))
     scene.close()
     ctx.close()
