@@ -1146,10 +1146,9 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
   sc->features = F;
   sc->feature_set = ne_feature_set_for(F);
   ne_tuning tn;
-  // surface-only scenes run fastest with lane refill (Cornell box: 235 vs 210 Mpaths/s), grid
-  // media with the split kernel (medium scene: 630 vs 397), meshes with the straight kernel
-  // (mesh scene: 139 vs 50 with lane refill)
-  tn.kernel = sc->feature_set == K_SURFACE ? 2 : (sc->feature_set == K_VOLUME && (F & FT_GRID)) ? 3 : 0;
+  // the split kernel is the fastest measured on every scene (Mpaths/s, one pass -> split:
+  // medium 397 -> 1316, Cornell 235 -> 573, mesh 139 -> 182, dense cloud 116 -> 282)
+  tn.kernel = 3;
   tn.track_share = sc->track_share;
   tn.blocks_per_sm = 0;
   tn.split_passes = 0;
