@@ -103,10 +103,10 @@ def test_obj_scene_parity(built, oracle_lib, tmp_path):
     ctx = ne.Context(0)
     orc = oracle_lib.OracleScene(host.desc_ptr)
     try:
-        scene = ctx.upload(host)
+        gpu_scene = ctx.upload(host)
         for kernel in (0, 3):
-            scene.set_tuning(kernel=kernel)
-            img, _ = scene.render(seed=4, spp=2)
+            gpu_scene.set_tuning(kernel=kernel)
+            img, _ = gpu_scene.render(seed=4, spp=2)
             ref, _ = orc.render(ne.render_params(seed=4, spp=2))
             assert np.array_equal(img.view(np.uint32), ref.view(np.uint32)), kernel
     finally:
