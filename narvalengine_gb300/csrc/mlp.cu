@@ -100,40 +100,33 @@ constexpr int kTile = 128;
 
 __device__ __forceinline__ int biasIndex(int l) { return l * 64; }
 
-// Feature encoding of one query (96 values, 88 used).
+// Feature encoding of one query (96 values, 88 used): sin/cos of pi * scalar, then each
+// further band by angle doubling (sin 2x = 2 sin x cos x, cos 2x = cos^2 x - sin^2 x).
 __device__ void encodeQuery(float px, float py, float pz, float wx, float wy, float wz, float* f) {
   const float kPi = 3.14159265358979323846f;
-  float u[3] = {px + 0.5f, py + 0.5f, pz + 0.5f};
   float wyc = fminf(fmaxf(wy, -1.0f), 1.0f);
   float a = acosf(wyc) / kPi;
   float b = atan2f(wz, wx) / (2.0f * kPi) + 0.5f;
+  const float v[5] = {px + 0.5f, py + 0.5f, pz + 0.5f, a, b};
   int col = 0;
-  for (int s = 0; s < 3; s++) {
-    float fr = kPi;
-    for (int k = 0; k < 12; k++) {
-      float x = __fmul_rn(fr, u[s]);
-      float sn, cs;
-      sincosf(x, &sn, &cs);
+#pragma unroll
+  for (int s = 0; s < 5; s++) {
+    const int bands = s < 3 ? 12 : 4;
+    float sn, cs;
+    sincosf(__fmul_rn(kPi, v[s]), &sn, &cs);
+#pragma unroll
+    for (int k = 0; k < bands; k++) {
       f[col] = sn;
       f[col + 1] = cs;
       col += 2;
-      fr = __fmul_rn(fr, 2.0f);
+      float s2 = __fmul_rn(__fmul_rn(2.0f, sn), cs);
+      float c2 = __fsub_rn(__fmul_rn(cs, cs), __fmul_rn(sn, sn));
+      sn = s2;
+      cs = c2;
     }
   }
-  float v[2] = {a, b};
-  for (int s = 0; s < 2; s++) {
-    float fr = kPi;
-    for (int k = 0; k < 4; k++) {
-      float x = __fmul_rn(fr, v[s]);
-      float sn, cs;
-      sincosf(x, &sn, &cs);
-      f[col] = sn;
-      f[col + 1] = cs;
-      col += 2;
-      fr = __fmul_rn(fr, 2.0f);
-    }
-  }
-  for (; col < 96; col++) f[col] = 0.0f;
+#pragma unroll
+  for (int c = 88; c < 96; c++) f[c] = 0.0f;
 }
 
 // Stores 8 consecutive BF16 values (columns c..c+7 of row r) into a core-matrix tile.
@@ -194,8 +187,8 @@ __global__ void __launch_bounds__(kTile) k_mlp_forward(const FwdArgs a, uint32_t
   __shared__ uint32_t tbase;
   __shared__ float sBias[kBiasFloats];
   uint8_t* sW = smem;                    // kFwdBytes
-  uint8_t* sX = smem + kFwdBytes;        // 128 x 96 BF16
-  uint8_t* sH = sX + kTile * 96 * 2;     // 128 x 64 BF16
+  uint8_t* sX = smem + kFwdBytes;        // 128 x 96 BF16: the encoded input, then each layer's output
+  uint8_t* sH = sX;                      // (a layer's product has completed before its output is stored)
   const uint32_t t = threadIdx.x, warp = t / 32;
   for (uint32_t i = t; i < kFwdBytes / 16; i += kTile)
     reinterpret_cast<uint4*>(sW)[i] = reinterpret_cast<const uint4*>(a.wfwd)[i];
@@ -544,11 +537,11 @@ cudaError_t ne_mlp_forward(cudaStream_t st, const NeMlpForward& f, uint32_t* err
   a.thr = f.thr;
   a.idx = f.idx;
   a.radiance = f.radiance;
-  const size_t smem = kFwdBytes + (size_t)kTile * 96 * 2 + (size_t)kTile * 64 * 2;
+  const size_t smem = kFwdBytes + (size_t)kTile * 96 * 2;
   cudaError_t e = cudaFuncSetAttribute(k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   uint32_t tiles = (f.n + kTile - 1) / kTile;
-  uint32_t blocks = tiles < (uint32_t)smCount() * 2 ? tiles : (uint32_t)smCount() * 2;
+  uint32_t blocks = tiles < (uint32_t)smCount() * 3 ? tiles : (uint32_t)smCount() * 3;
   k_mlp_forward<<<blocks, kTile, smem, st>>>(a, err);
   return cudaGetLastError();
 }

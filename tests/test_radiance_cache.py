@@ -1,7 +1,7 @@
 """The learned radiance cache on the tensor cores against its numpy restatement
 (oracle/mlp.py): feature encoding, forward pass, gradients and training.
 
-Tolerances: features 1e-5 absolute (FP32 sin/cos of the same FP32 arguments); network
+Tolerances: features 5e-4 absolute (the band-0 sin/cos of the two sides differ by an ulp or two, which angle doubling amplifies up to 2^11 times); network
 outputs and gradients compare BF16 products accumulated in FP32 in different orders, so
 1e-2 of the output scale and 3e-2 relative norm per gradient tensor."""
 import numpy as np
@@ -60,7 +60,7 @@ def test_encoding(cache):
     pos, d = queries(4096, 1)
     g = cache.encode(pos, d)
     c = mlp.encode(pos, d)
-    assert np.abs(g - c).max() < 1e-5
+    assert np.abs(g - c).max() < 5e-4
     assert np.all(g[:, 88:] == 0)
 
 
