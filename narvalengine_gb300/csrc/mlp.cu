@@ -133,7 +133,7 @@ __device__ void encodeQuery(float px, float py, float pz, float wx, float wy, fl
 __device__ __forceinline__ void storeRow8(uint8_t* tile, uint32_t r, uint32_t c, uint32_t kcols, const float* v) {
   uint32_t w[4];
 #pragma unroll
-  for (int i = 0; i < 4; i++) w[i] = (uint32_t)f2bf(v[2 * i]) | ((uint32_t)f2bf(v[2 * i + 1]) << 16);
+  for (int i = 0; i < 4; i++) w[i] = f2bf2(v[2 * i], v[2 * i + 1]);
   *reinterpret_cast<uint4*>(tile + cm_offset(r, c, kcols)) = make_uint4(w[0], w[1], w[2], w[3]);
 }
 
@@ -226,8 +226,8 @@ __global__ void __launch_bounds__(kTile) k_mlp_forward(const FwdArgs a, uint32_t
       }
       for (int c = 0; c < 96; c += 8) storeRow8(sX, t, c, 96, f + c);
       if (a.acts && valid) {
-        uint16_t* dst = a.acts + (size_t)row * kActRow;
-        for (int c = 0; c < 96; c++) dst[c] = f2bf(f[c]);
+        uint32_t* dst = reinterpret_cast<uint32_t*>(a.acts + (size_t)row * kActRow);
+        for (int c = 0; c < 96; c += 2) dst[c / 2] = f2bf2(f[c], f[c + 1]);
       }
     }
     float o16[16];
@@ -260,9 +260,9 @@ __global__ void __launch_bounds__(kTile) k_mlp_forward(const FwdArgs a, uint32_t
           storeRow8(sH, t, c, 64, v);
           storeRow8(sH, t, c + 8, 64, v + 8);
           if (a.acts && valid) {
-            uint16_t* dst = a.acts + (size_t)row * kActRow + 96 + l * 64 + c;
+            uint32_t* dst = reinterpret_cast<uint32_t*>(a.acts + (size_t)row * kActRow + 96 + l * 64 + c);
 #pragma unroll
-            for (int j = 0; j < 16; j++) dst[j] = f2bf(v[j]);
+            for (int j = 0; j < 8; j++) dst[j] = f2bf2(v[2 * j], v[2 * j + 1]);
           }
         }
       } else {

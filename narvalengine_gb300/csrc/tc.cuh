@@ -12,6 +12,7 @@
 // Every wait on an mbarrier is bounded: after kTcMaxPolls polls it reports failure, the
 // caller sets an error flag, and TMEM is still released before the block exits.
 #pragma once
+#include <cuda_bf16.h>
 #include <stdint.h>
 
 namespace netc {
@@ -128,11 +129,12 @@ __device__ __forceinline__ uint32_t tmem_at(uint32_t base, uint32_t lane, uint32
   return base + (lane << 16) + col;
 }
 
-__device__ __forceinline__ uint16_t f2bf(float x) {
-  uint32_t u = __float_as_uint(x);
-  if ((u & 0x7F800000u) == 0x7F800000u && (u & 0x7FFFFFu)) return (uint16_t)((u >> 16) | 0x40u);  // NaN
-  u += 0x7FFFu + ((u >> 16) & 1u);
-  return (uint16_t)(u >> 16);
+// FP32 -> BF16, round to nearest even (cvt.rn).
+__device__ __forceinline__ uint16_t f2bf(float x) { return __bfloat16_as_ushort(__float2bfloat16_rn(x)); }
+// Two values packed low, high (one cvt.rn.bf16x2.f32).
+__device__ __forceinline__ uint32_t f2bf2(float lo, float hi) {
+  __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<uint32_t*>(&h);
 }
 __device__ __forceinline__ float bf2f(uint16_t h) { return __uint_as_float((uint32_t)h << 16); }
 
