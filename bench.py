@@ -297,14 +297,14 @@ def run_views(args, rank: int, world: int, local: int):
     d.close()
 
 
-def run_profile_case(spp: int, kernel: int, track_share: int, split_passes: int = 0):
+def run_profile_case(spp: int, kernel: int, track_share: int, split_passes: int = 0, split_half: int = 1):
     """Small case for ncu: the same scene at a reduced sample count, rendered twice."""
     import narvalengine_gb300 as ne
     ctx = ne.Context(0)
     host = ne.SceneHost.from_json(os.path.join(ne.SCENES_DIR, SCENE))
     scene = ctx.upload(host)
     if kernel >= 0:
-        scene.set_tuning(kernel=kernel, track_share=track_share, split_passes=split_passes)
+        scene.set_tuning(kernel=kernel, track_share=track_share, split_passes=split_passes, split_half=split_half)
     for i in range(2):
         _, st = scene.render(ne.render_params(seed=1, spp=spp))
     _, cst = scene.render(ne.render_params(seed=1, spp=spp, flags=ne.NE_RENDER_COUNT_WORK))
@@ -329,6 +329,7 @@ def main():
                     help="path kernel (ne_tuning.kernel): 0 straight, 1 regrouped, 2 lane refill, 3 split; "
                          "default: the library's autotuner picks")
     ap.add_argument("--split-passes", type=int, default=0, help="split kernel passes (0: library default)")
+    ap.add_argument("--split-half", type=int, default=1, help="split kernel: 1 = deferral every half bounce")
     ap.add_argument("--track-share", type=int, default=16, help="regrouped kernel tracking threshold, 32nds")
     ap.add_argument("--profile-spp", type=int, default=0,
                     help="profiling case: two renders of the workload at this spp (the second is the one to capture)")
@@ -342,7 +343,7 @@ def main():
         run_reference(args, rank, world)
         return
     if args.profile_spp > 0:
-        run_profile_case(args.profile_spp, args.kernel, args.track_share, args.split_passes)
+        run_profile_case(args.profile_spp, args.kernel, args.track_share, args.split_passes, args.split_half)
         return
 
     if args.scene == "views_c5":
@@ -355,10 +356,11 @@ def main():
     host = ne.SceneHost.from_json(os.path.join(ne.SCENES_DIR, SCENE))
     scene = ctx.upload(host)
     if args.kernel >= 0:
-        scene.set_tuning(kernel=args.kernel, track_share=args.track_share, split_passes=args.split_passes)
+        scene.set_tuning(kernel=args.kernel, track_share=args.track_share, split_passes=args.split_passes,
+                         split_half=args.split_half)
     else:
-        # the library's autotuner, on a quarter of the samples, outside the timed region
-        scene.autotune(repeats=2, seed=7, spp=max(1, host.spp // 4))
+        # the library's autotuner on the same frame size (another seed), outside the timed region
+        scene.autotune(repeats=2, seed=7, spp=host.spp)
     W, H, spp = host.width, host.height, host.spp
     paths_per_step = W * H * spp
     img_bytes = W * H * 3 * 4

@@ -172,23 +172,30 @@ ne_status ne_trace_closest(ne_scene* scene, const ne_ray* rays, size_t n, float 
  * theirs ends, 3 = split: a first pass finishes every path that ends at its first event and
  * queues the others (at their first scattering in a grid medium, or after their first surface
  * bounce); each further pass resumes the queued paths packed together and queues them again
- * one bounce later, the last runs them to the end. blocks_per_sm: persistent blocks per SM,
- * 0 = as many as fit. Every configuration renders the same bits. */
+ * one bounce (or half a bounce) later, the last runs them to the end. blocks_per_sm:
+ * persistent blocks per SM, 0 = as many as fit. Every configuration renders the same bits.
+ * A new scene starts with kernel 3, split_half 1, 16 passes. */
 typedef struct ne_tuning {
   int32_t kernel;
   int32_t track_share;
   int32_t blocks_per_sm;
-  int32_t split_passes;  /* kernel 3: passes, 2..64 (0: 6); pass p > 0 resumes the paths queued
-                            at bounce p - 1 and queues them again at bounce p, the last runs
-                            them to the end */
+  int32_t split_passes;  /* kernel 3: passes, 2..64 (0: 16 with split_half, else 8); pass p > 0
+                            resumes the paths queued at deferral point p - 1 and queues them
+                            again at point p, the last runs them to the end */
+  int32_t split_half;    /* kernel 3: 0 = deferral points once a bounce (point b: bounce b's
+                            scattering event in a medium, or the end of surface bounce b);
+                            1 = every half bounce (point 2b: bounce b's free-flight sample,
+                            2b + 1: the end of bounce b, after its light sampling), so passes
+                            alternate between the two variable-length walks */
 } ne_tuning;
 
 ne_status ne_scene_set_tuning(ne_scene* scene, const ne_tuning* tuning);
 ne_status ne_scene_get_tuning(const ne_scene* scene, ne_tuning* tuning);
-/* Autotuner: renders the scene with `params` (typically fewer samples than a frame) under
- * each candidate (straight, lane refill, split with 3..24 passes; resident blocks as many as
- * fit), `repeats` timed renders after one warm-up each, keeps the fastest path-kernel time
- * and returns it. Every candidate renders the same bits. */
+/* Autotuner: renders the scene with `params` under each candidate (straight, lane refill,
+ * split with 3..24 passes by bounce or 12..32 by half bounce; resident blocks as many as fit),
+ * `repeats` timed renders after one warm-up each, keeps the fastest path-kernel time and
+ * returns it. Every candidate renders the same bits. The split kernel's best pass count
+ * depends on the number of paths a render has: tune with the frame's own sample count. */
 ne_status ne_scene_autotune(ne_scene* scene, const ne_render_params* params, int repeats, ne_tuning* best,
                             double* best_ms);
 

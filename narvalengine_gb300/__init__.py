@@ -262,9 +262,10 @@ class Scene:
         return (img, {f: getattr(stats, f) for f, _ in NeRenderStats._fields_},
                 {f: getattr(cst, f) for f, _ in _abi.NeCacheRenderStats._fields_})
 
-    def set_tuning(self, kernel: int = 0, track_share: int = 16, blocks_per_sm: int = 0, split_passes: int = 0):
+    def set_tuning(self, kernel: int = 0, track_share: int = 16, blocks_per_sm: int = 0, split_passes: int = 0,
+                   split_half: int = 1):
         """Launch configuration of the path kernels (see ne_tuning in include/narval_gb300.h)."""
-        t = _abi.NeTuning(kernel, track_share, blocks_per_sm, split_passes)
+        t = _abi.NeTuning(kernel, track_share, blocks_per_sm, split_passes, split_half)
         self.ctx.check(library().ne_scene_set_tuning(self._h, C.byref(t)))
 
     def autotune(self, repeats: int = 2, params: NeRenderParams | None = None, **kw):
@@ -279,7 +280,7 @@ class Scene:
         t = _abi.NeTuning()
         self.ctx.check(library().ne_scene_get_tuning(self._h, C.byref(t)))
         return {"kernel": t.kernel, "track_share": t.track_share, "blocks_per_sm": t.blocks_per_sm,
-                "split_passes": t.split_passes}
+                "split_passes": t.split_passes, "split_half": t.split_half}
 
     def trace_paths(self, keys: np.ndarray, params: NeRenderParams | None = None, **kw) -> np.ndarray:
         """Camera path radiance for (pixel, sample) keys, shape (n, 3)."""
@@ -384,6 +385,8 @@ class Views:
         return out
 
     def image(self, v: int) -> np.ndarray:
+        if not 0 <= v < len(self.sizes):
+            raise NarvalError(_abi.NE_ERR_INVALID_ARG, f"view {v} out of range (0..{len(self.sizes) - 1})")
         w, h, _ = self.sizes[v]
         out = np.empty((h, w, 3), np.float32)
         self.ctx.check(library().ne_views_image(self._h, v, _ptr(out)))

@@ -163,7 +163,7 @@ def main(argv=None):
         host = ne.SceneHost.from_json(path)
     ctx = ne.Context(0)
     scene = ctx.upload(host)
-    tuning, _ = scene.autotune(repeats=1, seed=3, spp=max(1, args.chunk // 4))
+    tuning, _ = scene.autotune(repeats=1, seed=3, spp=args.chunk)
     t0 = time.time()
     info = {}
     ref, ref_ms = reference_image(scene, args.ref_spp, chunk=args.chunk, info=info)

@@ -82,12 +82,16 @@ struct ne_scene {
   size_t paths_cap = 0;
   int blocks_per_sm = 1;
   int variant = 0;           // path kernel: 0 straight, 1 regrouped, 2 lane refill, 3 split
-  int split_passes = 6;       // kernel 3: passes (the last runs deferred paths to the end)
+  int split_passes = 16;      // kernel 3: passes (the last runs deferred paths to the end)
+  int split_half = 1;         // kernel 3: deferral points every half bounce
   PathState* d_defer[2] = {nullptr, nullptr};  // split renders: two queues of deferred paths
   size_t defer_cap = 0;
-  DeferQueue* d_dq = nullptr;    // the two queues' descriptors (device)
-  uint32_t* d_dcount = nullptr;  // their counts
-  DeferQueue dq[2];
+  // split renders: queue descriptor p (device) is what pass p appends to, over buffer p & 1;
+  // d_pass holds the passes' queue counts (kMaxSplitPasses x u32) and then their work
+  // counters (kMaxSplitPasses x u64), all cleared by one memset per render
+  DeferQueue* d_dq = nullptr;
+  unsigned char* d_pass = nullptr;
+  bool dq_uploaded = false;
   int track_share = 16;      // k_sched tracking-phase threshold (32nds of live lanes)
   uint32_t features = 0;     // FT_* bits of the scene
   uint32_t feature_set = 0;  // compiled kernel specialisation covering them
@@ -452,10 +456,14 @@ int pathLaunches(const ne_scene* sc, bool count) {
 
 // Split render: the first pass finishes every path that ends at its first event and queues
 // the others (at their first scattering in a grid medium or after their first surface
-// bounce); pass p resumes the queued paths and queues them again one bounce later, the last
-// pass runs them to the end. Two queues of half the paths each alternate; paths beyond a
-// queue's capacity continue in the pass that had them. `launch(pass, blocks, args)`
-// launches one pass (0: first pass).
+// bounce); pass p resumes the queued paths and queues them again one bounce (or half a
+// bounce) later, the last pass runs them to the end. Two buffers of half the paths each
+// alternate; paths beyond a buffer's capacity continue in the pass that had them. Each pass
+// has its own queue count and work counter, so the passes follow one another with no
+// launches in between. `launch(pass, blocks, args, counter)` launches one pass (0: first
+// pass; pass 0 uses the context's counter, cleared by the caller).
+constexpr int kMaxSplitPasses = 64;
+
 template <class F>
 ne_status launchSplit(ne_scene* sc, PathArgs b, int blocks, F launch) {
   ne_context* ctx = sc->ctx;
@@ -466,31 +474,37 @@ ne_status launchSplit(ne_scene* sc, PathArgs b, int blocks, F launch) {
       q = nullptr;
     }
     sc->defer_cap = 0;
+    sc->dq_uploaded = false;
     for (PathState*& q : sc->d_defer) NE_CUDA(cudaMalloc(&q, cap * sizeof(PathState)), "cudaMalloc(deferred paths)");
     sc->defer_cap = cap;
   }
-  if (!sc->d_dq) NE_CUDA(cudaMalloc(&sc->d_dq, 2 * sizeof(DeferQueue)), "cudaMalloc");
-  if (!sc->d_dcount) NE_CUDA(cudaMalloc(&sc->d_dcount, 2 * sizeof(uint32_t)), "cudaMalloc");
-  for (int i = 0; i < 2; i++) {
-    sc->dq[i].items = sc->d_defer[i];
-    sc->dq[i].count = sc->d_dcount + i;
-    sc->dq[i].cap = (uint32_t)std::min<size_t>(sc->defer_cap, 0xFFFFFFFFu);
+  const size_t countBytes = kMaxSplitPasses * sizeof(uint32_t);
+  const size_t passBytes = countBytes + kMaxSplitPasses * sizeof(unsigned long long);
+  if (!sc->d_dq) NE_CUDA(cudaMalloc(&sc->d_dq, kMaxSplitPasses * sizeof(DeferQueue)), "cudaMalloc");
+  if (!sc->d_pass) NE_CUDA(cudaMalloc(&sc->d_pass, passBytes), "cudaMalloc");
+  if (!sc->dq_uploaded) {
+    DeferQueue dq[kMaxSplitPasses];
+    for (int p = 0; p < kMaxSplitPasses; p++) {
+      dq[p].items = sc->d_defer[p & 1];
+      dq[p].count = reinterpret_cast<uint32_t*>(sc->d_pass) + p;
+      dq[p].cap = (uint32_t)std::min<size_t>(sc->defer_cap, 0xFFFFFFFFu);
+    }
+    // from pageable memory: the call returns once `dq` has been staged
+    NE_CUDA(cudaMemcpyAsync(sc->d_dq, dq, sizeof(dq), cudaMemcpyHostToDevice, ctx->stream), "cudaMemcpyAsync");
+    sc->dq_uploaded = true;
   }
-  NE_CUDA(cudaMemcpyAsync(sc->d_dq, sc->dq, 2 * sizeof(DeferQueue), cudaMemcpyHostToDevice, ctx->stream),
-          "cudaMemcpyAsync");
-  NE_CUDA(cudaMemsetAsync(sc->d_dcount, 0, sizeof(uint32_t), ctx->stream), "cudaMemsetAsync");
-  const int passes = std::max(2, sc->split_passes);
+  NE_CUDA(cudaMemsetAsync(sc->d_pass, 0, passBytes, ctx->stream), "cudaMemsetAsync");
+  unsigned long long* counters = reinterpret_cast<unsigned long long*>(sc->d_pass + countBytes);
+  const int passes = std::min(kMaxSplitPasses, std::max(2, sc->split_passes));
   b.defer_out = sc->d_dq;
   b.defer_at = 0;
-  NE_CUDA(launch(0, blocks, b), "path kernel launch");
+  b.defer_half = sc->split_half;
+  NE_CUDA(launch(0, blocks, b, ctx->d_counter), "path kernel launch");
   for (int pass = 1; pass < passes; pass++) {
-    const int in = (pass - 1) & 1, out = pass & 1;
-    b.defer_in = sc->d_dq + in;
-    b.defer_out = sc->d_dq + out;
+    b.defer_in = sc->d_dq + pass - 1;
+    b.defer_out = sc->d_dq + pass;
     b.defer_at = pass == passes - 1 ? -1 : pass;
-    NE_CUDA(cudaMemsetAsync(sc->d_dcount + out, 0, sizeof(uint32_t), ctx->stream), "cudaMemsetAsync");
-    NE_CUDA(cudaMemsetAsync(ctx->d_counter, 0, sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync");
-    NE_CUDA(launch(pass, persistentBlocks(sc), b), "resume kernel launch");
+    NE_CUDA(launch(pass, persistentBlocks(sc), b, counters + pass), "resume kernel launch");
   }
   return NE_OK;
 }
@@ -504,8 +518,8 @@ ne_status launchPaths(ne_scene* sc, const PathArgs& a, bool count) {
   PathArgs b = a;
   b.track_share = sc->track_share;
   if (sc->variant == 3 && !count) {
-    return launchSplit(sc, b, blocks, [&](int pass, int nb, const PathArgs& pa) {
-      return ne_launch_path_split(pass, sc->feature_set, nb, ctx->stream, sc->d, pa, ctx->d_counter, ctx->d_err);
+    return launchSplit(sc, b, blocks, [&](int pass, int nb, const PathArgs& pa, unsigned long long* ctr) {
+      return ne_launch_path_split(pass, sc->feature_set, nb, ctx->stream, sc->d, pa, ctr, ctx->d_err);
     });
   }
   NE_CUDA(ne_launch_path_kernel(sc->variant, sc->feature_set, count, blocks, ctx->stream, sc->d, b, ctx->d_counter,
@@ -1146,12 +1160,14 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
   sc->features = F;
   sc->feature_set = ne_feature_set_for(F);
   ne_tuning tn;
-  // the split kernel is the fastest measured on every scene (Mpaths/s, one pass -> split:
-  // medium 397 -> 1316, Cornell 235 -> 573, mesh 139 -> 182, dense cloud 116 -> 282)
+  // the split kernel is the fastest measured on every scene (Mpaths/s, one pass -> split by
+  // bounce, 8 passes -> split by half bounce, 16 passes: medium 386 -> 1366 -> 1510, Cornell
+  // 209 -> 592 -> 574, mesh 127 -> 171 -> 171, dense cloud 115 -> 239 -> 268)
   tn.kernel = 3;
   tn.track_share = sc->track_share;
   tn.blocks_per_sm = 0;
   tn.split_passes = 0;
+  tn.split_half = 1;
   if (ne_scene_set_tuning(sc, &tn) != NE_OK) return cleanup(NE_ERR_INVALID_ARG);
   cudaError_t e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return cleanup(cudaFail(ctx, e, "scene upload"));
@@ -1162,7 +1178,7 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
 ne_status ne_scene_set_tuning(ne_scene* sc, const ne_tuning* t) {
   if (!sc || !t || t->kernel < 0 || t->kernel > 3 || t->track_share < 1 || t->track_share > 32 ||
       t->blocks_per_sm < 0 || t->blocks_per_sm > 64 || t->split_passes < 0 || t->split_passes == 1 ||
-      t->split_passes > 64)
+      t->split_passes > 64 || t->split_half < 0 || t->split_half > 1)
     return NE_ERR_INVALID_ARG;
   ne_context* ctx = sc->ctx;
   int fit = 1;
@@ -1170,7 +1186,8 @@ ne_status ne_scene_set_tuning(ne_scene* sc, const ne_tuning* t) {
   if (e != cudaSuccess) return cudaFail(ctx, e, "occupancy query");
   if (fit < 1) fit = 1;
   sc->variant = t->kernel;
-  sc->split_passes = t->split_passes ? t->split_passes : 6;
+  sc->split_passes = t->split_passes ? t->split_passes : (t->split_half ? 16 : 8);
+  sc->split_half = t->split_half;
   sc->track_share = t->track_share;
   sc->blocks_per_sm = t->blocks_per_sm > 0 ? std::min(t->blocks_per_sm, fit) : fit;
   return NE_OK;
@@ -1182,6 +1199,7 @@ ne_status ne_scene_get_tuning(const ne_scene* sc, ne_tuning* t) {
   t->track_share = sc->track_share;
   t->blocks_per_sm = sc->blocks_per_sm;
   t->split_passes = sc->split_passes;
+  t->split_half = sc->split_half;
   return NE_OK;
 }
 
@@ -1197,7 +1215,7 @@ void ne_scene_destroy(ne_scene* sc) {
   for (PathState* q : sc->d_defer)
     if (q) cudaFree(q);
   if (sc->d_dq) cudaFree(sc->d_dq);
-  if (sc->d_dcount) cudaFree(sc->d_dcount);
+  if (sc->d_pass) cudaFree(sc->d_pass);
   delete sc;
 }
 
@@ -1873,9 +1891,9 @@ ne_status ne_render_cached(ne_scene* sc, ne_cache* c, const ne_render_params* p,
   unsigned long long needed = (total + kThreads - 1) / kThreads;
   if ((unsigned long long)blocks > needed) blocks = (int)std::max<unsigned long long>(1, needed);
   {
-    ne_status sst = launchSplit(sc, a, blocks, [&](int pass, int nb, const PathArgs& pa) {
+    ne_status sst = launchSplit(sc, a, blocks, [&](int pass, int nb, const PathArgs& pa, unsigned long long* ctr) {
       return ne_launch_path_kernel_cache(pass, pass ? ctx->sm_count * std::max(1, fit) : nb, ctx->stream, sc->d, pa,
-                                         ctx->d_counter, ctx->d_err);
+                                         ctr, ctx->d_err);
     });
     if (sst) return sst;
   }
@@ -2148,8 +2166,9 @@ ne_status ne_scene_autotune(ne_scene* sc, const ne_render_params* p, int repeats
   ne_tuning keep;
   ne_scene_get_tuning(sc, &keep);
   std::vector<ne_tuning> cands;
-  for (int k : {0, 2}) cands.push_back(ne_tuning{k, sc->track_share, 0, 0});
-  for (int passes : {3, 4, 6, 8, 12, 16, 24}) cands.push_back(ne_tuning{3, sc->track_share, 0, passes});
+  for (int k : {0, 2}) cands.push_back(ne_tuning{k, sc->track_share, 0, 0, 0});
+  for (int passes : {3, 4, 6, 8, 12, 16, 24}) cands.push_back(ne_tuning{3, sc->track_share, 0, passes, 0});
+  for (int passes : {12, 16, 20, 24, 32}) cands.push_back(ne_tuning{3, sc->track_share, 0, passes, 1});
   ne_tuning bt = keep;
   double bms = 1e30;
   for (const ne_tuning& t : cands) {

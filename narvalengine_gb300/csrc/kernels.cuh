@@ -84,6 +84,7 @@ struct PathArgs {
   const DeferQueue* defer_in = nullptr;
   const DeferQueue* defer_out = nullptr;
   int defer_at = -1;
+  int defer_half = 0;  // 1: deferral points every half bounce
   const ViewDone* views = nullptr;  // resume passes of a batch of views: completion accounting
 };
 
@@ -115,7 +116,8 @@ __device__ __forceinline__ void flushCounters(const Counters& cn, unsigned long 
 template <uint32_t K>
 __global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_paths(const __grid_constant__ DScene s, const PathArgs a,
                                                     unsigned long long* __restrict__ counter, uint32_t* err) {
-  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, a.cache, a.defer_out, 0ull, false, a.defer_at};
+  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, a.cache, a.defer_out, 0ull, false, a.defer_at,
+           a.defer_half};
   const int lane = threadIdx.x & 31;
   for (;;) {
     unsigned long long base = 0;
@@ -162,7 +164,8 @@ __global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_resume(const __gri
                                                                      const PathArgs a,
                                                                      unsigned long long* __restrict__ counter,
                                                                      uint32_t* err) {
-  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, a.cache, a.defer_out, 0ull, false, a.defer_at};
+  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, a.cache, a.defer_out, 0ull, false, a.defer_at,
+           a.defer_half};
   const DeferQueue& q = *a.defer_in;
   const unsigned long long n = min(*q.count, q.cap);
   const int lane = threadIdx.x & 31;
@@ -205,7 +208,7 @@ template <uint32_t K>
 __global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_lanes(const __grid_constant__ DScene s, const PathArgs a,
                                                     unsigned long long* __restrict__ counter, uint32_t* err) {
   namespace cg = cooperative_groups;
-  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, nullptr, nullptr, 0ull, false, -1};
+  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, nullptr, nullptr, 0ull, false, -1, 0};
   for (;;) {
     cg::coalesced_group g = cg::coalesced_threads();
     unsigned long long base = 0;

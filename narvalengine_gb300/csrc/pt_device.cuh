@@ -192,6 +192,7 @@ struct Ctx {
   unsigned long long idx;
   bool deferred;
   int deferAt;
+  int deferHalf;  // 1: deferral points every half bounce (after sampling, and after the bounce)
 };
 
 // Buffers of a render that ends paths in the learned radiance cache. A path that reaches
@@ -1144,8 +1145,10 @@ struct DeferQueue {
 // integrators/VolumetricPathIntegrator.cpp:176-301 Li, plus the optional Russian
 // roulette of resources/shaders/MS_monteCarlo.frag:539-544, written as a loop over `v` that
 // can start at the scattering point where a K_SPLIT path was deferred (`resume`) and can
-// stop at the scattering event of bounce c.deferAt to be deferred again: every operation and
-// every random draw happens in the same order either way.
+// stop at the first deferral point at or after c.deferAt to be deferred again. Deferral
+// points: the scattering event of bounce b (position b, or 2b with half-bounce deferral) and
+// the end of bounce b (surfaces at position b; every bounce at 2b + 1 with half-bounce
+// deferral). Every operation and every random draw happens in the same order either way.
 template <uint32_t K>
 NE_D V3 liLoop(Ctx<K>& c, const PathParams& P, LiVars& v, bool resume) {
   const DScene& s = c.s;
@@ -1180,7 +1183,7 @@ NE_D V3 liLoop(Ctx<K>& c, const PathParams& P, LiVars& v, bool resume) {
           continue;
         }
         v.T = v.T * sampledT;
-        if ((K & K_SPLIT) && b == c.deferAt && !recorded) {
+        if ((K & K_SPLIT) && c.deferAt >= 0 && (b << c.deferHalf) >= c.deferAt && !recorded) {
           const DeferQueue& q = *c.dq;
           uint32_t slot = appendSlot(q.count);
           if (slot < q.cap) {
@@ -1257,8 +1260,10 @@ NE_D V3 liLoop(Ctx<K>& c, const PathParams& P, LiVars& v, bool resume) {
         v.T = v.T / (1.0f - q);
       }
     }
-    if ((K & K_SPLIT) && !medium && b == c.deferAt && b + 1 < P.bounces && !recorded) {
-      // a surface bounce done: defer the path to the top of the next bounce
+    if ((K & K_SPLIT) && c.deferAt >= 0 && (c.deferHalf || !medium) && (b << c.deferHalf) + c.deferHalf >= c.deferAt &&
+        b + 1 < P.bounces && !recorded) {
+      // a bounce done (a surface bounce, or any bounce with half-bounce deferral): defer the
+      // path to the top of the next bounce
       const DeferQueue& q = *c.dq;
       uint32_t slot = appendSlot(q.count);
       if (slot < q.cap) {

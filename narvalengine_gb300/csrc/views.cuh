@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_views(const __grid
                                                                     const ViewArgs a,
                                                                     unsigned long long* __restrict__ counter,
                                                                     uint32_t* err) {
-  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, nullptr, a.defer_out, 0ull, false, 0};
+  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, nullptr, a.defer_out, 0ull, false, 0, 0};
   const int lane = threadIdx.x & 31;
   if (threadIdx.x == 0 && blockIdx.x == 0) atomicMin(a.t_start, globalTimer());
   for (;;) {

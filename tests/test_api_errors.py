@@ -36,6 +36,10 @@ def test_views_errors(env):
             vb.set_tuning(**t)
     with pytest.raises(ne.NarvalError):
         vb.image(1)
+    out = np.empty((16, 16, 3), np.float32)
+    ptr = out.ctypes.data_as(C.POINTER(C.c_float))
+    assert lib.ne_views_image(vb._h, 1, ptr) == _abi.NE_ERR_INVALID_ARG
+    assert lib.ne_views_image(vb._h, -1, ptr) == _abi.NE_ERR_INVALID_ARG
     vb.close()
 
 
@@ -57,7 +61,8 @@ def test_cache_errors(env):
 def test_tuning_errors(env):
     ne, ctx, scene = env
     for t in [dict(kernel=-1), dict(kernel=4), dict(kernel=3, split_passes=1), dict(kernel=3, split_passes=65),
-              dict(blocks_per_sm=-1), dict(kernel=1, track_share=33)]:
+              dict(blocks_per_sm=-1), dict(kernel=1, track_share=33), dict(kernel=3, split_half=2),
+              dict(kernel=3, split_half=-1)]:
         with pytest.raises(ne.NarvalError):
             scene.set_tuning(**t)
     assert ne.library().ne_scene_autotune(scene._h, None, 0, None, None) != 0
