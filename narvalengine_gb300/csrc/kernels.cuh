@@ -16,14 +16,16 @@
 namespace nedev {
 
 constexpr int kThreads = 128;
-// Resident blocks per SM the path kernels are compiled for: 8 x 128 threads caps them at 64
+// Resident blocks per SM the path kernels are compiled for: 7 x 128 threads caps them at 72
 // registers. The spills this costs are cheaper than the latency stalls that fewer resident
-// warps leave exposed. Measured (Mpaths/s, medium / Cornell / dense cloud, split kernel): 6
-// blocks 1338 / 589 / 264, 8 blocks 1316 / 573 / 282, 10 blocks 1186 / 546 / 252; before the
-// split (one pass, medium / mesh): uncapped 123 registers 339 / 113, 8 blocks 383 / 127,
-// 10 blocks 397 / 139.
+// warps leave exposed. Measured (Mpaths/s, medium / dense cloud / Cornell / mesh, split by half
+// bounce): 6 blocks 1467 / 286 / 581 / 156, 7 blocks 1530 / 304 / 561 / 169, 8 blocks
+// 1468 / 309 / 558 / 170, 10 blocks 1350 / 282 / 531 / 176; split by bounce (medium /
+// Cornell / dense cloud): 6 blocks 1338 / 589 / 264, 8 blocks 1316 / 573 / 282, 10 blocks
+// 1186 / 546 / 252; one pass (medium / mesh): uncapped 123 registers 339 / 113, 8 blocks
+// 383 / 127, 10 blocks 397 / 139.
 #ifndef NE_PATH_MIN_BLOCKS
-#define NE_PATH_MIN_BLOCKS 8
+#define NE_PATH_MIN_BLOCKS 7
 #endif
 constexpr int kPathMinBlocks = NE_PATH_MIN_BLOCKS;
 
