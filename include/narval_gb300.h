@@ -113,6 +113,13 @@ void ne_scene_host_destroy(ne_scene_host* s);
 ne_status ne_save_png(const char* path, const float* rgb, int width, int height);
 ne_status ne_save_exr(const char* path, const float* rgb, int width, int height);
 
+/* Decodes an image file to 8-bit RGBA the way the reference loads textures (stbi_load with four
+ * channels, core/ResourceManager.cpp:288-315): PNG (every colour type and bit depth, Adam7 or
+ * not; 16-bit samples keep their high byte) and binary PNM (P5, P6). Sets width and height;
+ * with out != NULL also copies the width*height*4 bytes (cap: bytes available). JPEG and HDR
+ * files give NE_ERR_UNSUPPORTED. */
+ne_status ne_image_load_rgba8(const char* path, int32_t* width, int32_t* height, uint8_t* out, size_t cap);
+
 /* ---- device ---- */
 
 ne_status ne_context_create(int device, ne_context** out);
@@ -210,7 +217,8 @@ ne_status ne_context_synchronize(ne_context* ctx);
 ne_status ne_context_flush_l2(ne_context* ctx, size_t bytes);
 
 /* Device copies of the shared elementary functions, for bit-exactness checks.
- * fn: 0 log, 1 exp, 2 sin, 3 cos, 4 acos, 5 pow5. */
+ * fn: 0 log, 1 exp, 2 sin, 3 cos, 4 acos, 5 pow5, 6 atan2(x[i], x[i ^ 1]) (elements paired;
+ * an unpaired last element is paired with 1). */
 ne_status ne_debug_fmath(ne_context* ctx, int fn, const float* x, size_t n, float* out);
 
 /* Device copy of the shared counter-based generator: u01 for (seed, pixel, sample, dim). */

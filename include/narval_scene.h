@@ -98,8 +98,15 @@ typedef struct ne_light {
   float li[3];           /* Light::li */
   float le[3];           /* Light::le */
   float direction[3];    /* DirectionalLight::direction (pointing from the light) */
-  float env_radiance[3]; /* InfiniteAreaLight: value of its (1x1, constant) environment map */
-  float env_map_pdf;     /* InfiniteAreaLight: pdf Distribution2D returns for that map (1, or 0) */
+  float env_radiance[3]; /* InfiniteAreaLight without a texture: value of its (1x1, constant) map */
+  float env_map_pdf;     /* InfiniteAreaLight without a texture: pdf Distribution2D returns for
+                            that map (1, or 0) */
+  /* InfiniteAreaLight with a texture (lights/InfiniteAreaLight.h:20-40): its 8-bit RGBA texels
+   * as the reference's loader gives them, row-major from the top row, sampled with the mirror
+   * wrap and nearest lookup of Texture::sample. env_width = 0: no texture. The library builds
+   * the light's Distribution2D from them at upload. */
+  int32_t env_width, env_height;
+  const uint8_t* env_texels;
 } ne_light;
 
 enum ne_medium_kind { NE_MEDIUM_GRID = 0, NE_MEDIUM_HOMOGENEOUS = 1 };

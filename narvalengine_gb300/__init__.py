@@ -471,6 +471,20 @@ def save_image(path: str, rgb: np.ndarray) -> None:
         raise NarvalError(st, f"cannot write {path}")
 
 
+def load_image(path: str) -> np.ndarray:
+    """ne_image_load_rgba8: the (H, W, 4) uint8 texels a texture file gives the reference's
+    loader (stbi_load with four channels; PNG and binary PNM)."""
+    w, h = C.c_int32(), C.c_int32()
+    st = library().ne_image_load_rgba8(path.encode(), C.byref(w), C.byref(h), None, 0)
+    if st != 0:
+        raise NarvalError(st, f"cannot decode {path}")
+    out = np.empty((h.value, w.value, 4), np.uint8)
+    st = library().ne_image_load_rgba8(path.encode(), C.byref(w), C.byref(h), out.ctypes.data, out.nbytes)
+    if st != 0:
+        raise NarvalError(st, f"cannot decode {path}")
+    return out
+
+
 def tone_map(hdr: np.ndarray) -> np.ndarray:
     """OfflineEngine::postProcessing (core/OfflineEngine.cpp:39-52): exposure 0.5, gamma 2.2, clamp."""
     mapped = np.float32(1.0) - np.exp(-hdr.astype(np.float32) * np.float32(0.5))
@@ -544,6 +558,6 @@ class OfflineEngine:
 
 
 __all__ = ["Context", "Scene", "SceneHost", "SceneReader", "VolumetricPathIntegrator", "OfflineEngine",
-           "NarvalError", "render_params", "tone_map", "write_ppm", "library", "SCENES_DIR",
+           "NarvalError", "render_params", "tone_map", "write_ppm", "load_image", "library", "SCENES_DIR",
            "NE_RENDER_OUT_DEVICE", "NE_RENDER_REF_TILES", "NE_RENDER_COUNT_WORK", "NE_RENDER_NO_SYNC",
            "NeRay", "NePathKey"]

@@ -30,7 +30,8 @@ class NeMaterial(C.Structure):
 
 class NeLight(C.Structure):
     _fields_ = [("type", C.c_int32), ("primitive", C.c_int32), ("li", f3), ("le", f3), ("direction", f3),
-                ("env_radiance", f3), ("env_map_pdf", C.c_float)]
+                ("env_radiance", f3), ("env_map_pdf", C.c_float), ("env_width", C.c_int32),
+                ("env_height", C.c_int32), ("env_texels", C.POINTER(C.c_uint8))]
 
 
 class NeMedium(C.Structure):
@@ -193,5 +194,7 @@ SIGNATURES = {
                                  C.POINTER(C.c_size_t)]),
     "ne_save_png": (C.c_int32, [C.c_char_p, C.c_void_p, C.c_int, C.c_int]),
     "ne_save_exr": (C.c_int32, [C.c_char_p, C.c_void_p, C.c_int, C.c_int]),
+    "ne_image_load_rgba8": (C.c_int32, [C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_void_p,
+                                        C.c_size_t]),
     "ne_debug_mma": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
 }

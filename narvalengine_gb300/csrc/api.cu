@@ -16,6 +16,8 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cmath>
+#include <deque>
 #include <future>
 #include <memory>
 #include <mutex>
@@ -153,6 +155,64 @@ ne_status upload(ne_scene* sc, const T* host, size_t n, const T** out) {
   NE_CUDA(cudaMemcpyAsync(p, host, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream), "cudaMemcpyAsync");
   *out = (const T*)p;
   return NE_OK;
+}
+
+// ---- InfiniteAreaLight's importance-sampling tables (built at upload, read by envSample)
+// Distribution1D's constructor (utils/Sampling.h:12-28): func, CDF of func / n normalised by
+// its integral (a uniform CDF if the integral is 0).
+void dist1D(const float* f, int n, float* func, float* cdf, float* funcInt) {
+  for (int i = 0; i < n; i++) func[i] = f[i];
+  cdf[0] = 0;
+  for (int i = 1; i < n + 1; i++) cdf[i] = cdf[i - 1] + func[i - 1] / (float)n;
+  *funcInt = cdf[n];
+  if (*funcInt == 0)
+    for (int i = 1; i < n + 1; i++) cdf[i] = (float)i / (float)n;
+  else
+    for (int i = 1; i < n + 1; i++) cdf[i] /= *funcInt;
+}
+// Texture::sample's mirror-wrapped nearest texel coordinate (materials/Texture.cpp:88-129).
+int hostTexCoord(float u, int n) {
+  if (!(u >= -2147483520.0f && u <= 2147483520.0f)) return 0;
+  float a = u - (float)(int)u;
+  a = a < 0 ? -a : a;
+  a = (a < 0.0f) ? 0.0f : a;
+  a = (1.0f < a) ? 1.0f : a;
+  int x = (int)(a * (float)n);
+  if (x > 0 && x == n) x--;
+  return x;
+}
+struct EnvTables {
+  std::vector<float> condFunc, condCdf, condInt, margFunc, margCdf;
+  float margInt = 0;
+};
+// InfiniteAreaLight's constructor (lights/InfiniteAreaLight.h:20-40): the green channel of the
+// texel at (u/W, v/H) times sin(pi (v + 0.5) / H), then Distribution2D (utils/Sampling.h:82-96)
+// whose conditional rows take H values from the start of each image row (Sampling.h:87).
+EnvTables buildEnvTables(const ne_light& L) {
+  const int W = L.env_width, H = L.env_height;
+  std::vector<float> img((size_t)W * H);
+  for (int v = 0; v < H; v++) {
+    float vp = (float)v / (float)H;
+    // glm::sin(PI * float(v + 0.5f) / float(height)): the double literal PI promotes the product
+    float sinTheta = (float)std::sin(3.14159265358979323846264338327950288 * (double)((float)v + 0.5f) /
+                                     (double)(float)H);
+    for (int u = 0; u < W; u++) {
+      float up = (float)u / (float)W;
+      const uint8_t* t = L.env_texels + 4 * ((size_t)hostTexCoord(vp, H) * W + hostTexCoord(up, W));
+      img[u + (size_t)v * W] = (float)t[1] / 255.0f;
+      img[u + (size_t)v * W] *= sinTheta;
+    }
+  }
+  EnvTables e;
+  e.condFunc.resize((size_t)H * H);
+  e.condCdf.resize((size_t)H * (H + 1));
+  e.condInt.resize(H);
+  for (int v = 0; v < H; v++)
+    dist1D(&img[(size_t)v * W], H, &e.condFunc[(size_t)v * H], &e.condCdf[(size_t)v * (H + 1)], &e.condInt[v]);
+  e.margFunc.resize(H);
+  e.margCdf.resize(H + 1);
+  dist1D(e.condInt.data(), H, e.margFunc.data(), e.margCdf.data(), &e.margInt);
+  return e;
 }
 
 // ---- host helpers shared by the upload (same arithmetic as the integrator's host side)
@@ -396,6 +456,7 @@ __global__ void k_fmath(int fn, const float* __restrict__ x, size_t n, float* __
       case 2: r = nefm::sin(v); break;
       case 3: r = nefm::cos(v); break;
       case 4: r = nefm::acos(v); break;
+      case 6: r = nefm::atan2(v, (i ^ 1) < n ? x[i ^ 1] : 1.0f); break;
       default: r = nefm::pow5(v); break;
     }
     out[i] = r;
@@ -954,8 +1015,17 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
     if (m.light >= (int)D.n_lights || m.medium >= (int)D.n_media) return fail(ctx, NE_ERR_INVALID_ARG, "material index out of range");
     if (m.bsdf == NE_BSDF_VOLUME && m.medium < 0) return fail(ctx, NE_ERR_INVALID_ARG, "volume material without a medium");
   }
-  for (uint32_t i = 0; i < D.n_lights; i++)
-    if (D.lights[i].primitive >= (int)D.n_prims) return fail(ctx, NE_ERR_INVALID_ARG, "light primitive out of range");
+  for (uint32_t i = 0; i < D.n_lights; i++) {
+    const ne_light& L = D.lights[i];
+    if (L.primitive >= (int)D.n_prims) return fail(ctx, NE_ERR_INVALID_ARG, "light primitive out of range");
+    if (L.type == NE_LIGHT_INFINITE && L.env_width != 0 &&
+        (L.env_width < 0 || L.env_height <= 0 || !L.env_texels || L.env_width > (1 << 16)))
+      return fail(ctx, NE_ERR_INVALID_ARG, "environment map without texels");
+    if (L.type == NE_LIGHT_INFINITE && L.env_width > 0 && L.env_height > L.env_width)
+      return fail(ctx, NE_ERR_UNSUPPORTED,
+                  "environment maps taller than wide are not supported (the reference's Distribution2D reads past "
+                  "such an image)");
+  }
   // every light reachable from a light instance is sampled through Light::primitive
   for (uint32_t i = 0; i < D.n_light_instances; i++) {
     const ne_model& m = D.models[D.instances[D.n_instances + i].model];
@@ -1062,6 +1132,7 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
     d.tex_present = s.tex_present; d.tex_types = s.tex_types;
   }
   std::vector<DLight> lights(D.n_lights);
+  std::deque<EnvTables> envTables;  // host sources of the table copies, alive until the upload syncs
   for (uint32_t i = 0; i < D.n_lights; i++) {
     const ne_light& s = D.lights[i];
     DLight& d = lights[i];
@@ -1070,6 +1141,23 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
     memcpy(d.li, s.li, 12); memcpy(d.le, s.le, 12);
     memcpy(d.direction, s.direction, 12); memcpy(d.env_radiance, s.env_radiance, 12);
     d.env_map_pdf = s.env_map_pdf;
+    if (s.type == NE_LIGHT_INFINITE && s.env_width > 0) {
+      envTables.push_back(buildEnvTables(s));
+      const EnvTables& e = envTables.back();
+      d.env_w = s.env_width;
+      d.env_h = s.env_height;
+      d.env_marg_int = e.margInt;
+      const uint8_t* tex = nullptr;
+      ne_status st = NE_OK;
+      if ((st = upload(sc, s.env_texels, (size_t)s.env_width * s.env_height * 4, &tex)) ||
+          (st = upload(sc, e.condFunc.data(), e.condFunc.size(), &d.env_cond_func)) ||
+          (st = upload(sc, e.condCdf.data(), e.condCdf.size(), &d.env_cond_cdf)) ||
+          (st = upload(sc, e.condInt.data(), e.condInt.size(), &d.env_cond_int)) ||
+          (st = upload(sc, e.margFunc.data(), e.margFunc.size(), &d.env_marg_func)) ||
+          (st = upload(sc, e.margCdf.data(), e.margCdf.size(), &d.env_marg_cdf)))
+        return cleanup(st);
+      d.env_tex = (const uchar4*)tex;
+    }
   }
   // media: dense grid + 8-corner cells
   std::vector<DMedium> media(D.n_media);
@@ -1155,8 +1243,10 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
     if (m.tex_types & NE_TEX_NORMAL) F |= FT_NORMALMAP;
   }
   for (uint32_t i = 0; i < D.n_media; i++) F |= D.media[i].type == NE_MEDIUM_GRID ? FT_GRID : FT_HOMOG;
-  for (uint32_t i = 0; i < D.n_lights; i++)
+  for (uint32_t i = 0; i < D.n_lights; i++) {
     F |= D.lights[i].type == NE_LIGHT_DIFFUSE ? FT_LDIFF : (D.lights[i].type == NE_LIGHT_DIRECTIONAL ? FT_LDIR : FT_LINF);
+    if (D.lights[i].type == NE_LIGHT_INFINITE && D.lights[i].env_width > 0) F |= FT_ENVMAP;
+  }
   sc->features = F;
   sc->feature_set = ne_feature_set_for(F);
   ne_tuning tn;

@@ -68,7 +68,18 @@ struct DLight {
   int32_t type, primitive;
   float li[3], le[3], direction[3], env_radiance[3];
   float env_map_pdf;
-  int32_t pad;
+  // InfiniteAreaLight with a texture (env_w > 0): RGBA8 texels and its Distribution2D
+  // (utils/Sampling.h:71-112) as the reference builds it: `env_h` conditional rows of
+  // `env_h` values each (Sampling.h:87 passes the height as every row's length), their CDFs
+  // (env_h + 1 each) and integrals, and the marginal over the rows' integrals.
+  int32_t env_w, env_h;
+  float env_marg_int;
+  const uchar4* env_tex;
+  const float* env_cond_func;  // env_h x env_h
+  const float* env_cond_cdf;   // env_h x (env_h + 1)
+  const float* env_cond_int;   // env_h
+  const float* env_marg_func;  // env_h
+  const float* env_marg_cdf;   // env_h + 1
 };
 
 struct DMedium {

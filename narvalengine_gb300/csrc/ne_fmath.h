@@ -22,6 +22,9 @@
 //    Accurate for |x| < 2^12 pi/2, which covers every angle the integrator forms.
 //  * acos: acos(x) = pi/2 - asin(x) for |x| <= 1/2, 2 asin(sqrt((1-x)/2)) above,
 //    pi - 2 asin(sqrt((1+x)/2)) below; asin by its Taylor series (10 terms, |y| <= 1/2).
+//  * atan2: atan on [0, 1] (the larger magnitude divides the smaller; pi/2 - atan above 1),
+//    reduced past tan(pi/12) by atan(t) = pi/6 + atan((t sqrt3 - 1)/(t + sqrt3)), then the odd
+//    Taylor series of atan (7 terms, |r| <= tan(pi/12)); quadrants and signed zeros as C99.
 //  * pow(x, 5): ((x x)(x x)) x.
 // Measured accuracy against a double-precision libm is checked by the test suite.
 #pragma once
@@ -184,6 +187,41 @@ NE_HD float acos(float x) {
   }
   float y = fsqrt((1.0f + x) * 0.5f);
   return kPi - 2.0f * asin_small(y);
+}
+
+// atan on |r| <= tan(pi/12) by its Taylor series r - r^3/3 + r^5/5 - ... - r^11/11 + r^13/13.
+NE_HD float atan_small(float r) {
+  float z = r * r;
+  float p = -0x1.555556p-2f + z * (0x1.99999ap-3f + z * (-0x1.24924ap-3f + z * (0x1.c71c72p-4f +
+            z * (-0x1.745d18p-4f + z * 0x1.3b13b2p-4f))));
+  return r + r * z * p;
+}
+// atan on [0, 1].
+NE_HD float atan01(float t) {
+  if (t <= 0x1.126146p-2f) return atan_small(t);  // tan(pi/12)
+  const float sqrt3 = 0x1.bb67aep+0f;
+  float r = (t * sqrt3 - 1.0f) / (t + sqrt3);
+  return 0x1.0c1524p-1f + atan_small(r);  // pi/6 + atan(r)
+}
+NE_HD bool signbit_(float x) { return (f2u(x) >> 31) != 0; }
+// atan2(y, x) in [-pi, pi].
+NE_HD float atan2(float y, float x) {
+  if (isnan_(x) || isnan_(y)) return u2f(0x7fc00000u);
+  float ax = x < 0.0f ? -x : x, ay = y < 0.0f ? -y : y;
+  float a;
+  if (isinf_(ax) && isinf_(ay)) {
+    a = 0x1.921fb6p-1f;  // pi/4
+  } else if (isinf_(ay) || (ax == 0.0f && ay != 0.0f)) {
+    a = kPiO2;
+  } else if (isinf_(ax) || ay == 0.0f) {
+    a = 0.0f;
+  } else if (ay <= ax) {
+    a = atan01(ay / ax);
+  } else {
+    a = kPiO2 - atan01(ax / ay);
+  }
+  if (signbit_(x)) a = kPi - a;
+  return signbit_(y) ? -a : a;
 }
 
 NE_HD float pow5(float x) {

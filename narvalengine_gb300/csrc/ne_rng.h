@@ -27,15 +27,11 @@ namespace nerng {
 
 struct Block { uint32_t w[4]; };
 
+// One widening multiply (a single 32x32->64 instruction on the device) gives both halves.
 NE_RNG_HD void mulhilo(uint32_t a, uint32_t b, uint32_t* hi, uint32_t* lo) {
-#if defined(__CUDA_ARCH__)
-  *hi = __umulhi(a, b);
-  *lo = a * b;
-#else
   uint64_t p = (uint64_t)a * (uint64_t)b;
   *hi = (uint32_t)(p >> 32);
   *lo = (uint32_t)p;
-#endif
 }
 
 NE_RNG_HD Block philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1) {

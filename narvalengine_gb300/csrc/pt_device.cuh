@@ -34,6 +34,8 @@ constexpr double kPiD = 3.14159265358979323846264338327950288;
 constexpr double kTwoPiD = 6.283185307179586476925286766559;
 constexpr double kFourPiD = 12.566370614359172953850573533118;
 constexpr double kEpsilonD = 0.0000000001;
+constexpr double kInvPiD = 0.31830988618379067154;   // INVPI (utils/Math.h:24)
+constexpr double kInv2PiD = 0.15915494309189533577;  // INV2PI (utils/Math.h:25)
 constexpr float kInv4Pi = float(0.07957747154594766788);
 constexpr float kEps3F = float(0.001);
 constexpr float kEps12F = float(0.00000000001);
@@ -63,7 +65,8 @@ enum : uint32_t {
   FT_LINF = 1u << 11,
   FT_NORMALMAP = 1u << 12,
   FT_BBOX = 1u << 13,     // model bounding boxes (meshes)
-  FT_ALL = (1u << 14) - 1,
+  FT_ENVMAP = 1u << 14,   // InfiniteAreaLight with a texture and its Distribution2D
+  FT_ALL = (1u << 15) - 1,
   K_COUNT = 1u << 31,
   K_CACHE = 1u << 30,  // paths end in the learned radiance cache (see CacheIO)
   K_SPLIT = 1u << 29,  // paths are deferred at their first medium scattering (see DeferQueue)
@@ -472,10 +475,79 @@ NE_D bool bvhIntersect(Ctx<K>& c, const DModel& m, const Ray& r, Hit& out) {
   return anyHit;
 }
 
-NE_D V3 lightLe(const DLight& L) {  // Light::Le, DirectionalLight::Le, InfiniteAreaLight::Le
-  if (L.type == NE_LIGHT_INFINITE) return ld3(L.env_radiance);
+// ---------------------------------------------------------------- environment maps
+// One texture coordinate of Texture::sample with NE_TEX_SAMPLER_UVW_MIRROR and nearest lookup
+// (materials/Texture.cpp:88-129): mirror wrap |u - (int)u| clamped to [0, 1], texel (int)(u n),
+// the edge u = 1 folded onto the last texel. A coordinate that is not a number or exceeds the
+// int range (a NaN direction; undefined behaviour in the reference) reads texel 0.
+NE_D int texCoord(float u, int n) {
+  if (!(u >= -2147483520.0f && u <= 2147483520.0f)) return 0;
+  u = gmin(gmax(fabsf(u - (float)(int)u), 0.0f), 1.0f);
+  int x = (int)(u * (float)n);
+  if (x > 0 && x == n) x--;
+  return x;
+}
+// RGB of an RGBA8 texel, each channel / 255 (Texture.cpp:69-81).
+NE_D V3 envTexel(const DLight& L, float u, float v) {
+  uchar4 t = L.env_tex[(uint32_t)texCoord(v, L.env_h) * (uint32_t)L.env_w + (uint32_t)texCoord(u, L.env_w)];
+  return v3((float)t.x / 255.0f, (float)t.y / 255.0f, (float)t.z / 255.0f);
+}
+// InfiniteAreaLight::Le (lights/InfiniteAreaLight.h:46-55): the direction through `M` (the
+// light instance's invTransformToWCS, or the identity), normalised, in the frame of (0, 0, 1);
+// (getSphericalPhi / 2pi, getSphericalTheta / pi) of it (utils/Math.h:1148-1155) indexes the map.
+NE_D V3 envLe(const DLight& L, const float* M, V3 d) {
+  V3 w = normalize(mul4(M, d, 0.0f));
+  V3 n = v3(0, 0, 1), ss, ts;
+  orthonormal(n, ss, ts);
+  V3 inc = toLCS(w, n, ss, ts);
+  float p = nefm::atan2(inc.y, inc.x);
+  float phi = (p < 0) ? __double2float_rn((double)p + kTwoPiD) : p;
+  float theta = nefm::acos(gmin(gmax(inc.z, -1.0f), 1.0f));
+  return envTexel(L, __double2float_rn((double)phi * kInv2PiD), __double2float_rn((double)theta * kInvPiD));
+}
+// Distribution1D::sampleContinuous (utils/Sampling.h:34-51) with binarySearch
+// (utils/Math.h:1130-1146) over the n + 1 CDF entries.
+NE_D float sample1D(const float* func, const float* cdf, int n, float funcInt, float u, float* pdf, int* off) {
+  int first = 0, len = n + 1;
+  while (len > 0) {
+    int half = len >> 1, middle = first + half;
+    if (cdf[middle] <= u) {
+      first = middle + 1;
+      len -= half + 1;
+    } else {
+      len = half;
+    }
+  }
+  int o = first - 1 < 0 ? 0 : (first - 1 > n - 1 ? n - 1 : first - 1);
+  float du = u - cdf[o];
+  if ((cdf[o + 1] - cdf[o]) > 0) du /= (cdf[o + 1] - cdf[o]);
+  *pdf = (funcInt > 0) ? func[o] / funcInt : 0;
+  *off = o;
+  return ((float)o + du) / (float)n;
+}
+// Distribution2D::sampleContinuous (utils/Sampling.h:98-105): the row from the marginal, then
+// the position within it.
+NE_D void envSample(const DLight& L, float u0, float u1, float& d0, float& d1, float& pdf) {
+  const int H = L.env_h;
+  float p0, p1;
+  int v, unused;
+  d1 = sample1D(L.env_marg_func, L.env_marg_cdf, H, L.env_marg_int, u1, &p1, &v);
+  d0 = sample1D(L.env_cond_func + (size_t)v * H, L.env_cond_cdf + (size_t)v * (H + 1), H, L.env_cond_int[v], u0, &p0,
+                &unused);
+  pdf = p0 * p1;
+}
+
+// Light::Le(ray, M) (lights/Light.h:177-179), DirectionalLight::Le, InfiniteAreaLight::Le.
+template <uint32_t K>
+NE_D V3 lightLe(const DLight& L, const float* M, V3 d) {
+  if (L.type == NE_LIGHT_INFINITE) {
+    if ((K & FT_ENVMAP) && L.env_w > 0) return envLe(L, M, d);
+    return ld3(L.env_radiance);
+  }
   return ld3(L.le);
 }
+// The identity matrix Model::intersect passes to Light::Le (primitives/Model.cpp:433).
+__device__ __constant__ const float kIdentity12[12] = {1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0};
 NE_D V3 lightLi(const DLight& L) {  // Light::Li, DirectionalLight::Li
   if (L.type == NE_LIGHT_DIRECTIONAL) return ld3(L.le);
   return ld3(L.li);
@@ -534,7 +606,7 @@ NE_D bool modelIntersect(Ctx<K>& c, uint32_t mi, const Ray& ray, Hit& hit, float
     int pi = (int)(m.light_begin + k);
     const DPrim& p = c.s.prims[pi];
     const DLight& L = c.s.lights[c.s.materials[p.material].light];
-    if (!isBlack(lightLe(L))) continue;
+    if (!isBlack(lightLe<K>(L, kIdentity12, ray.d))) continue;
     bool local = primIntersect(c, pi, ray, temp);
     if (local && temp.tNear > tMin && temp.tNear < tMax) {
       tMax = temp.tNear;
@@ -965,10 +1037,13 @@ NE_NI V3 sampleLi(const DScene& s, const DLight& L, const Hit& isect, const DIns
       if (!(K & FT_LINF)) return v3(0, 0, 0);
       float u0 = S.random();
       float u1 = S.random();
-      float mapPdf = L.env_map_pdf;
+      // Distribution2D::sampleContinuous; over the 1x1 map of a constant environment it returns
+      // (u0, u1) itself with pdf 1 (or 0 for a black map)
+      float uv0 = u0, uv1 = u1, mapPdf = L.env_map_pdf;
+      if ((K & FT_ENVMAP) && L.env_w > 0) envSample(L, u0, u1, uv0, uv1, mapPdf);
       if (mapPdf == 0) return v3(0, 0, 0);
-      float theta = __double2float_rn((double)u1 * kPiD);
-      float phi = __double2float_rn((double)(u0 * 2) * kPiD);
+      float theta = __double2float_rn((double)uv1 * kPiD);
+      float phi = __double2float_rn((double)(uv0 * 2) * kPiD);
       float cosTheta = nefm::cos(theta), sinTheta = nefm::sin(theta);
       float sinPhi = nefm::sin(phi), cosPhi = nefm::cos(phi);
       wo.o = isect.hitPoint;
@@ -978,6 +1053,7 @@ NE_NI V3 sampleLi(const DScene& s, const DLight& L, const Hit& isect, const DIns
       wo.d = toLCS(polar, v3(0, 1, 0), ss, ts);
       pdf = __double2float_rn((double)mapPdf / (2 * kPiD * kPiD * (double)sinTheta));
       if (sinTheta == 0) pdf = 0;
+      if ((K & FT_ENVMAP) && L.env_w > 0) return envTexel(L, uv0, uv1);
       return ld3(L.env_radiance);
     }
   }
@@ -1233,10 +1309,11 @@ NE_D V3 liLoop(Ctx<K>& c, const PathParams& P, LiVars& v, bool resume) {
           v.L = v.L + v.T * lightLi(s.lights[mat->light]);
         } else {
           for (uint32_t li = 0; li < s.n_light_instances; li++) {
-            const DModel& lm = s.models[s.instances[s.n_instances + li].model];
+            const DInstance& inst = s.instances[s.n_instances + li];
+            const DModel& lm = s.models[inst.model];
             for (uint32_t k = 0; k < lm.mat_count; k++) {
               const DMaterial& mm = s.materials[s.model_materials[lm.mat_begin + k]];
-              v.L = v.L + v.T * lightLe(s.lights[mm.light]);
+              v.L = v.L + v.T * lightLe<K>(s.lights[mm.light], inst.ocs, v.incoming.d);
             }
           }
         }

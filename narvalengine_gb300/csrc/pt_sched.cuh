@@ -218,10 +218,11 @@ NE_NI void transition(Ctx<K>& c, Lane& st, const PathParams& P) {
             st.L = st.L + st.T * lightLi(s.lights[mat->light]);
           } else {
             for (uint32_t li = 0; li < s.n_light_instances; li++) {
-              const DModel& lm = s.models[s.instances[s.n_instances + li].model];
+              const DInstance& inst = s.instances[s.n_instances + li];
+              const DModel& lm = s.models[inst.model];
               for (uint32_t k = 0; k < lm.mat_count; k++) {
                 const DMaterial& mm = s.materials[s.model_materials[lm.mat_begin + k]];
-                st.L = st.L + st.T * lightLe(s.lights[mm.light]);
+                st.L = st.L + st.T * lightLe<K>(s.lights[mm.light], inst.ocs, st.incoming.d);
               }
             }
           }

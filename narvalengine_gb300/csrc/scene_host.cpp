@@ -11,8 +11,9 @@
 //  * material "volume": "grid": {"generator": "fbm", ...} builds the density grid from
 //    seeded simplex fBm; "grid": {"path": "x.f32", "resolution": [W,H,D]} reads raw
 //    little-endian float32 voxels.
-//  * material "infiniteAreaLight": "radiance": [r,g,b] is a constant environment, i.e.
-//    the reference's InfiniteAreaLight over a 1x1 map of that value.
+//  * material "infiniteAreaLight": "radiance": [r,g,b] (instead of "path") is a constant
+//    environment, i.e. the reference's InfiniteAreaLight over a 1x1 map of that value. A
+//    "path" texture is decoded by image_load.cpp (PNG, binary PNM).
 //  * primitive "obj": read from the OBJ file directly (positions and faces) instead of through
 //    assimp, with the JSON materialName; primitives naming the same file and material share
 //    one model (one BVH), each with its own transform.
@@ -37,6 +38,7 @@
 #include <vector>
 
 #include "narval_gb300.h"
+#include "image_load.h"
 #include "ne_fmath.h"
 #include "scene_gen.h"
 
@@ -293,6 +295,7 @@ struct ne_scene_host {
   std::vector<ne_light> lights;
   std::vector<ne_medium> media;
   std::vector<std::vector<float>> grids;
+  std::vector<std::vector<uint8_t>> textures;  // RGBA8 environment maps (their buffers never move)
   std::vector<ne_instance> all_instances;
   ne_scene_desc desc;
   std::map<std::string, int> material_by_name;
@@ -420,12 +423,25 @@ struct Reader {
       memset(&L, 0, sizeof(L));
       L.type = NE_LIGHT_INFINITE;
       L.primitive = -1;
-      if (m.get("path") && !m.get("radiance"))
-        throw ParseError(NE_ERR_UNSUPPORTED, ctx + ": environment-map textures are not supported; give \"radiance\".");
-      vec3(need(m, "radiance", ctx), L.env_radiance, ctx + " radiance");
-      // Distribution2D over a 1x1 map of value G (InfiniteAreaLight.h:51-65, Sampling.h:12-28):
-      // the sampled pdf is func/funcInt = 1 when G > 0, else 0.
-      L.env_map_pdf = (L.env_radiance[1] > 0.0f) ? 1.0f : 0.0f;
+      if (const JVal* p = m.get("path")) {
+        // SceneReader.cpp:169-185: the texture at resources/path, decoded to RGBA8
+        neimg::Image img;
+        std::string err;
+        ne_status st = neimg::loadRGBA8(assetPath(sval(*p, ctx + " path")), img, err);
+        if (st != NE_OK) throw ParseError(st, ctx + ": " + err);
+        if (img.height > img.width)
+          throw ParseError(NE_ERR_UNSUPPORTED, ctx + ": environment maps taller than wide are not supported (the "
+                                               "reference's Distribution2D reads past such an image).");
+        S.textures.push_back(std::move(img.rgba));
+        L.env_width = img.width;
+        L.env_height = img.height;
+        L.env_texels = S.textures.back().data();
+      } else {
+        vec3(need(m, "radiance", ctx), L.env_radiance, ctx + " radiance");
+        // Distribution2D over a 1x1 map of value G (InfiniteAreaLight.h:51-65, Sampling.h:12-28):
+        // the sampled pdf is func/funcInt = 1 when G > 0, else 0.
+        L.env_map_pdf = (L.env_radiance[1] > 0.0f) ? 1.0f : 0.0f;
+      }
       S.lights.push_back(L);
       mat.light = (int)S.lights.size() - 1;
       mat.tex_present = NE_TEX_TEX1;

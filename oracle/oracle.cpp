@@ -48,6 +48,8 @@ using std::vector;
 const float kInf = std::numeric_limits<float>::infinity();
 const double kPiD = 3.14159265358979323846264338327950288;     // utils/Math.h:23
 const double kTwoPiD = 6.283185307179586476925286766559;       // utils/Math.h:27
+const double kInvPiD = 0.31830988618379067154;                 // utils/Math.h:24
+const double kInv2PiD = 0.15915494309189533577;                // utils/Math.h:25
 const double kFourPiD = 12.566370614359172953850573533118;     // utils/Math.h:28
 const double kEpsilonD = 0.0000000001;                         // utils/Math.h:20
 const float kInv4Pi = float(0.07957747154594766788);           // utils/Math.h:26
@@ -202,6 +204,52 @@ struct OModel {
   uint32_t nodeCount = 0;
 };
 
+// Distribution1D (utils/Sampling.h:5-69).
+struct ODist1D {
+  vector<float> func, cdf;
+  float funcInt = 0;
+  ODist1D() {}
+  ODist1D(const float* f, int n) {  // Sampling.h:12-28
+    func.assign(f, f + n);
+    cdf.assign(n + 1, 0.0f);
+    cdf[0] = 0;
+    for (int i = 1; i < n + 1; i++) cdf[i] = cdf[i - 1] + func[i - 1] / n;
+    funcInt = cdf[n];
+    if (funcInt == 0)
+      for (int i = 1; i < n + 1; i++) cdf[i] = float(i) / float(n);
+    else
+      for (int i = 1; i < n + 1; i++) cdf[i] /= funcInt;
+  }
+  int count() const { return (int)func.size(); }
+  float sampleContinuous(float u, float* pdf, int* off) const {  // Sampling.h:34-51
+    // binarySearch (utils/Math.h:1130-1146) over the CDF
+    int size = (int)cdf.size(), first = 0, len = size;
+    while (len > 0) {
+      int half = len >> 1, middle = first + half;
+      if (cdf[middle] <= u) {
+        first = middle + 1;
+        len -= half + 1;
+      } else {
+        len = half;
+      }
+    }
+    int offset = std::min(std::max(first - 1, 0), size - 2);
+    if (off) *off = offset;
+    float du = u - cdf[offset];
+    if ((cdf[offset + 1] - cdf[offset]) > 0) du /= (cdf[offset + 1] - cdf[offset]);
+    if (pdf) *pdf = (funcInt > 0) ? func[offset] / funcInt : 0;
+    return (offset + du) / count();
+  }
+};
+
+// InfiniteAreaLight's texture (RGBA8) and Distribution2D (utils/Sampling.h:71-112).
+struct OEnv {
+  int W = 0, H = 0;
+  vector<uint8_t> texels;
+  vector<ODist1D> cond;
+  ODist1D marg;
+};
+
 }  // namespace
 
 struct orc_scene {
@@ -218,6 +266,7 @@ struct orc_scene {
   vector<V3> sigmaT;      // GridMedia::extinction = absorption + scattering
   vector<float> triArea;  // Triangle::area per primitive
   vector<OModel> omodels;
+  vector<OEnv> env;       // per light: InfiniteAreaLight texture and Distribution2D (empty otherwise)
 };
 
 namespace {
@@ -485,12 +534,49 @@ bool bvhIntersect(const orc_scene& s, const OModel& om, const Ray& r, Hit& out) 
 
 const ne_light& lightOfMaterial(const orc_scene& s, int mat) { return s.lights[s.materials[mat].light]; }
 
-// Light::Le (lights/Light.h:177-179), DirectionalLight::Le (DirectionalLight.cpp:4-6),
-// InfiniteAreaLight::Le (InfiniteAreaLight.h:46-55, constant map).
-inline V3 lightLe(const ne_light& L) {
-  if (L.type == NE_LIGHT_INFINITE) return ld3(L.env_radiance);
+// Texture::sample, NE_TEX_SAMPLER_UVW_MIRROR, nearest (materials/Texture.cpp:88-129): one
+// coordinate. Not-a-number or beyond the int range (undefined in the reference): texel 0.
+int texCoord(float u, int n) {
+  if (!(u >= -2147483520.0f && u <= 2147483520.0f)) return 0;
+  u = gmin(gmax(std::fabs(u - (int)u), 0.0f), 1.0f);
+  int x = (int)(u * n);
+  if (x > 0 && x == n) x--;
+  return x;
+}
+// RGBA8 texel as Texture::sampleAtIndex reads it (Texture.cpp:69-81), RGB.
+V3 envTexel(const OEnv& e, float u, float v) {
+  const uint8_t* p = &e.texels[4 * ((size_t)texCoord(v, e.H) * e.W + texCoord(u, e.W))];
+  return v3(p[0] / 255.0f, p[1] / 255.0f, p[2] / 255.0f);
+}
+// getSphericalPhi / getSphericalTheta (utils/Math.h:1148-1155).
+float sphericalPhi(V3 v) {
+  float p = nefm::atan2(v.y, v.x);
+  return (p < 0) ? (float)(p + kTwoPiD) : p;
+}
+float sphericalTheta(V3 v) { return nefm::acos(gmin(gmax(v.z, -1.0f), 1.0f)); }
+// InfiniteAreaLight::Le (lights/InfiniteAreaLight.h:46-55).
+V3 envLe(const OEnv& e, const float* M, V3 d) {
+  V3 w = normalize(mul4(M, d, 0.0f));
+  V3 normal = v3(0, 0, 1), ss, ts;
+  orthonormal(normal, ss, ts);
+  V3 incoming = toLCS(w, normal, ss, ts);
+  float stx = (float)(sphericalPhi(incoming) * kInv2PiD), sty = (float)(sphericalTheta(incoming) * kInvPiD);
+  return envTexel(e, stx, sty);
+}
+const OEnv* envOf(const orc_scene& s, const ne_light& L) {
+  size_t i = &L - s.lights.data();
+  return (i < s.env.size() && s.env[i].W > 0) ? &s.env[i] : nullptr;
+}
+// Light::Le(ray, M) (lights/Light.h:177-179), DirectionalLight::Le (DirectionalLight.cpp:4-6),
+// InfiniteAreaLight::Le (InfiniteAreaLight.h:46-55; a constant map without a texture).
+inline V3 lightLe(const orc_scene& s, const ne_light& L, const float* M, V3 d) {
+  if (L.type == NE_LIGHT_INFINITE) {
+    if (const OEnv* e = envOf(s, L)) return envLe(*e, M, d);
+    return ld3(L.env_radiance);
+  }
   return ld3(L.le);
 }
+const float kIdentity16[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};  // glm::mat4(1)
 // Light::Li / DirectionalLight::Li (returns le) / InfiniteAreaLight::Li.
 inline V3 lightLi(const ne_light& L) {
   if (L.type == NE_LIGHT_DIRECTIONAL) return ld3(L.le);
@@ -550,7 +636,7 @@ bool modelIntersect(const orc_scene& s, uint32_t mi, const Ray& ray, Hit& hit, f
   for (uint32_t k = 0; k < m.light_count; k++) {
     int pi = (int)(m.light_begin + k);
     const ne_primitive& p = s.prims[pi];
-    if (!isBlack(lightLe(lightOfMaterial(s, p.material)))) continue;
+    if (!isBlack(lightLe(s, lightOfMaterial(s, p.material), kIdentity16, ray.d))) continue;  // Model.cpp:433
     bool local = primIntersect(s, pi, ray, temp);
     if (local && temp.tNear > tMin && temp.tNear < tMax) {
       tMax = temp.tNear;
@@ -929,10 +1015,18 @@ V3 sampleLi(const orc_scene& s, const ne_light& L, const Hit& isect, const float
     default: {
       float u0 = S.random();
       float u1 = S.random();
-      float mapPdf = L.env_map_pdf;
+      const OEnv* e = envOf(s, L);
+      float uv0 = u0, uv1 = u1, mapPdf = L.env_map_pdf;  // the 1x1 map returns u with pdf 1 (or 0)
+      if (e) {  // Distribution2D::sampleContinuous (Sampling.h:98-105)
+        float pdfs[2];
+        int v;
+        uv1 = e->marg.sampleContinuous(u1, &pdfs[1], &v);
+        uv0 = e->cond[v].sampleContinuous(u0, &pdfs[0], nullptr);
+        mapPdf = pdfs[0] * pdfs[1];
+      }
       if (mapPdf == 0) return v3(0, 0, 0);
-      float theta = (float)((double)u1 * kPiD);
-      float phi = (float)((double)(u0 * 2) * kPiD);
+      float theta = (float)((double)uv1 * kPiD);
+      float phi = (float)((double)(uv0 * 2) * kPiD);
       float cosTheta = nefm::cos(theta), sinTheta = nefm::sin(theta);
       float sinPhi = nefm::sin(phi), cosPhi = nefm::cos(phi);
       wo.o = isect.hitPoint;
@@ -942,6 +1036,7 @@ V3 sampleLi(const orc_scene& s, const ne_light& L, const Hit& isect, const float
       wo.d = toLCS(polar, v3(0, 1, 0), ss, ts);
       pdf = (float)((double)mapPdf / (2 * kPiD * kPiD * (double)sinTheta));
       if (sinTheta == 0) pdf = 0;
+      if (e) return envTexel(*e, uv0, uv1);
       return ld3(L.env_radiance);
     }
   }
@@ -1093,10 +1188,11 @@ V3 Li(Ctx& c, const Params& P, Ray incoming) {
           L = L + T * lightLi(s.lights[mat->light]);
         } else {
           for (uint32_t li = 0; li < s.d.n_light_instances; li++) {
-            const ne_model& lm = s.models[s.instances[s.d.n_instances + li].model];
+            const ne_instance& inst = s.instances[s.d.n_instances + li];
+            const ne_model& lm = s.models[inst.model];
             for (uint32_t k = 0; k < lm.mat_count; k++) {
               const ne_material& mm = s.materials[s.model_materials[lm.mat_begin + k]];
-              L = L + T * lightLe(s.lights[mm.light]);
+              L = L + T * lightLe(s, s.lights[mm.light], inst.to_ocs, incoming.d);
             }
           }
         }
@@ -1222,6 +1318,32 @@ orc_scene* orc_scene_create(const ne_scene_desc* d) {
       for (size_t k = 0; k < n; k++) mx = gmax(mx, s->grids[i][k]);  // GridMedia.h:16-21
       s->invMax[i] = 1.0f / mx;
     }
+  }
+  // InfiniteAreaLight's constructor (lights/InfiniteAreaLight.h:20-40) for textured lights
+  s->env.resize(d->n_lights);
+  for (uint32_t i = 0; i < d->n_lights; i++) {
+    const ne_light& L = s->lights[i];
+    if (L.type != NE_LIGHT_INFINITE || L.env_width <= 0 || L.env_height <= 0 || !L.env_texels ||
+        L.env_height > L.env_width)
+      continue;
+    OEnv& e = s->env[i];
+    e.W = L.env_width;
+    e.H = L.env_height;
+    e.texels.assign(L.env_texels, L.env_texels + (size_t)e.W * e.H * 4);
+    vector<float> img((size_t)e.W * e.H);
+    for (int v = 0; v < e.H; v++) {
+      float vp = (float)v / (float)e.H;
+      float sinTheta = std::sin(kPiD * float(v + 0.5f) / float(e.H));
+      for (int u = 0; u < e.W; u++) {
+        float up = (float)u / (float)e.W;
+        img[u + v * e.W] = envTexel(e, up, vp).y;
+        img[u + v * e.W] *= sinTheta;
+      }
+    }
+    for (int v = 0; v < e.H; ++v) e.cond.emplace_back(&img[v * e.W], e.H);  // Sampling.h:87: length = height
+    vector<float> marginalFunc;
+    for (int v = 0; v < e.H; ++v) marginalFunc.push_back(e.cond[v].funcInt);
+    e.marg = ODist1D(&marginalFunc[0], e.H);
   }
   s->triArea.assign(d->n_prims, 0.0f);
   for (uint32_t i = 0; i < d->n_prims; i++) {
@@ -1552,6 +1674,7 @@ void orc_fmath(int fn, const float* x, size_t n, float* out) {
       case 2: out[i] = nefm::sin(v); break;
       case 3: out[i] = nefm::cos(v); break;
       case 4: out[i] = nefm::acos(v); break;
+      case 6: out[i] = nefm::atan2(v, (i ^ 1) < n ? x[i ^ 1] : 1.0f); break;
       default: out[i] = nefm::pow5(v); break;
     }
   }

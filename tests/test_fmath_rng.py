@@ -39,6 +39,29 @@ def test_fmath_accuracy(oracle_lib, fn, gen, ref, max_ulp):
         assert e.max() <= max_ulp, (fn, e.max(), x[np.argmax(e)])
 
 
+def test_atan2_accuracy(oracle_lib):
+    rng = np.random.default_rng(6)
+    n = 200000
+    yx = np.empty(2 * n, np.float32)
+    yx[0::2] = rng.normal(size=n) * np.exp(rng.uniform(-8, 8, n))
+    yx[1::2] = rng.normal(size=n) * np.exp(rng.uniform(-8, 8, n))
+    got = oracle_lib.fmath(6, yx)[0::2]
+    want = np.arctan2(yx[0::2].astype(np.float64), yx[1::2].astype(np.float64))
+    e = ulp_err(got, want)
+    assert e.max() <= 3.0, (e.max(), yx[2 * np.argmax(e)], yx[2 * np.argmax(e) + 1])
+
+
+def test_atan2_quadrants_and_zeros(oracle_lib):
+    y = np.array([0.0, -0.0, 0.0, -0.0, 1.0, -1.0, 1.0, -1.0, np.inf, np.inf, -np.inf, 2.0, 3.0], np.float32)
+    x = np.array([0.0, 0.0, -0.0, -0.0, 0.0, 0.0, -1.0, -1.0, np.inf, -np.inf, 5.0, np.inf, -np.inf], np.float32)
+    yx = np.empty(2 * len(y), np.float32)
+    yx[0::2], yx[1::2] = y, x
+    got = oracle_lib.fmath(6, yx)[0::2].astype(np.float64)
+    want = np.arctan2(y.astype(np.float64), x.astype(np.float64))
+    assert np.all(np.abs(got - want) <= 4e-7), (got, want)
+    assert np.array_equal(np.signbit(got), np.signbit(want))
+
+
 def test_fmath_special_values(oracle_lib):
     log = oracle_lib.fmath(0, np.array([0.0, -1.0, np.inf, np.nan, 1.0, 2.0 ** -149], np.float32))
     assert log[0] == -np.inf and np.isnan(log[1]) and log[2] == np.inf and np.isnan(log[3]) and log[4] == 0.0
