@@ -518,17 +518,23 @@ int pathLaunches(const ne_scene* sc, bool count) {
 // Split render: the first pass finishes every path that ends at its first event and queues
 // the others (at their first scattering in a grid medium or after their first surface
 // bounce); pass p resumes the queued paths and queues them again one bounce (or half a
-// bounce) later, the last pass runs them to the end. Two buffers of half the paths each
-// alternate; paths beyond a buffer's capacity continue in the pass that had them. Each pass
+// bounce) later, the last pass runs them to the end. Two buffers alternate, each with room for
+// three quarters of the render's paths (at most kMaxDeferEntries): half in class 0, a quarter
+// in class 1 (see DeferQueue); paths beyond a class's capacity continue in the pass that had
+// them. Each pass
 // has its own queue count and work counter, so the passes follow one another with no
 // launches in between. `launch(pass, blocks, args, counter)` launches one pass (0: first
 // pass; pass 0 uses the context's counter, cleared by the caller).
 constexpr int kMaxSplitPasses = 64;
+// Entries of each deferred-path buffer at most (2^26 paths, 10 GiB): a render with more
+// paths lets the rest continue in the pass that has them.
+constexpr size_t kMaxDeferEntries = size_t(1) << 26;
 
 template <class F>
 ne_status launchSplit(ne_scene* sc, PathArgs b, int blocks, F launch) {
   ne_context* ctx = sc->ctx;
-  size_t cap = std::max<size_t>(1024, (size_t)(b.total / 2));
+  // class 0: half the paths, class 1: a quarter
+  size_t cap = std::min(kMaxDeferEntries, std::max<size_t>(3072, (size_t)(b.total / 4) * 3));
   if (sc->defer_cap < cap) {
     for (PathState*& q : sc->d_defer) {
       if (q) cudaFree(q);
@@ -539,7 +545,7 @@ ne_status launchSplit(ne_scene* sc, PathArgs b, int blocks, F launch) {
     for (PathState*& q : sc->d_defer) NE_CUDA(cudaMalloc(&q, cap * sizeof(PathState)), "cudaMalloc(deferred paths)");
     sc->defer_cap = cap;
   }
-  const size_t countBytes = kMaxSplitPasses * sizeof(uint32_t);
+  const size_t countBytes = 2 * kMaxSplitPasses * sizeof(uint32_t);  // both classes
   const size_t passBytes = countBytes + kMaxSplitPasses * sizeof(unsigned long long);
   if (!sc->d_dq) NE_CUDA(cudaMalloc(&sc->d_dq, kMaxSplitPasses * sizeof(DeferQueue)), "cudaMalloc");
   if (!sc->d_pass) NE_CUDA(cudaMalloc(&sc->d_pass, passBytes), "cudaMalloc");
@@ -548,7 +554,9 @@ ne_status launchSplit(ne_scene* sc, PathArgs b, int blocks, F launch) {
     for (int p = 0; p < kMaxSplitPasses; p++) {
       dq[p].items = sc->d_defer[p & 1];
       dq[p].count = reinterpret_cast<uint32_t*>(sc->d_pass) + p;
-      dq[p].cap = (uint32_t)std::min<size_t>(sc->defer_cap, 0xFFFFFFFFu);
+      dq[p].count_hi = reinterpret_cast<uint32_t*>(sc->d_pass) + kMaxSplitPasses + p;
+      dq[p].cap = (uint32_t)(sc->defer_cap / 3 * 2);
+      dq[p].cap_hi = (uint32_t)(sc->defer_cap - dq[p].cap);
     }
     // from pageable memory: the call returns once `dq` has been staged
     NE_CUDA(cudaMemcpyAsync(sc->d_dq, dq, sizeof(dq), cudaMemcpyHostToDevice, ctx->stream), "cudaMemcpyAsync");

@@ -169,7 +169,8 @@ __global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_resume(const __gri
   Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, a.cache, a.defer_out, 0ull, false, a.defer_at,
            a.defer_half};
   const DeferQueue& q = *a.defer_in;
-  const unsigned long long n = min(*q.count, q.cap);
+  const unsigned long long n0 = min(*q.count, q.cap);
+  const unsigned long long n = n0 + (q.count_hi ? min(*q.count_hi, q.cap_hi) : 0u);
   const int lane = threadIdx.x & 31;
   for (;;) {
     unsigned long long base = 0;
@@ -179,7 +180,7 @@ __global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_resume(const __gri
     unsigned long long i = base + (unsigned long long)lane;
     uint32_t finishedView = 0xffffffffu;
     if (i < n) {
-      const PathState& ps = q.items[i];
+      const PathState& ps = q.items[i < n0 ? i : q.cap + (i - n0)];
       LiVars v = ps.v;
       c.S.reset(ps.key, ps.dim);
       c.idx = ps.idx;

@@ -166,10 +166,15 @@ struct Sampler {
     blk = 0xffffffffu;
   }
   NE_D float random() {
+    float r = peek();
+    dim++;
+    return r;
+  }
+  // The next draw, without consuming it.
+  NE_D float peek() {
     uint32_t b = dim >> 2;
     if (b != blk) refill(b);
     uint32_t s = dim & 3u;
-    dim++;
     uint32_t w = (s == 0) ? w0 : (s == 1) ? w1 : (s == 2) ? w2 : w3;
     return nerng::word_to_u01(w);
   }
@@ -1212,10 +1217,17 @@ struct PathState {
   unsigned long long idx;
 };
 
+// Deferred paths of one pass. With count_hi set, paths deferred right after a free-flight
+// sample are binned by the light their next draw will pick (uniformSampleOneLight's first draw,
+// peeked, not consumed): class 0 in items[0, cap), class 1 in items[cap, cap + cap_hi), so
+// that the warps of the next pass mostly run one light's sampling code. Every other deferral
+// is class 0. Without count_hi: one class.
 struct DeferQueue {
   PathState* items;
   uint32_t* count;
-  uint32_t cap;
+  uint32_t cap;                  // class 0 entries
+  uint32_t* count_hi = nullptr;  // class 1 count (null: one class)
+  uint32_t cap_hi = 0;           // class 1 entries
 };
 
 // integrators/VolumetricPathIntegrator.cpp:176-301 Li, plus the optional Russian
@@ -1261,9 +1273,12 @@ NE_D V3 liLoop(Ctx<K>& c, const PathParams& P, LiVars& v, bool resume) {
         v.T = v.T * sampledT;
         if ((K & K_SPLIT) && c.deferAt >= 0 && (b << c.deferHalf) >= c.deferAt && !recorded) {
           const DeferQueue& q = *c.dq;
-          uint32_t slot = appendSlot(q.count);
-          if (slot < q.cap) {
-            PathState& ps = q.items[slot];
+          uint32_t cls = 0;
+          if (q.count_hi && s.n_light_instances > 1)
+            cls = (uint32_t)(int)((float)s.n_light_instances * c.S.peek()) & 1u;
+          uint32_t slot = cls ? appendSlot(q.count_hi) : appendSlot(q.count);
+          if (slot < (cls ? q.cap_hi : q.cap)) {
+            PathState& ps = q.items[(cls ? (size_t)q.cap : 0) + slot];
             ps.v = v;
             ps.key = c.S.key;
             ps.dim = c.S.dim;

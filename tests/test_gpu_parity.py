@@ -311,10 +311,10 @@ def test_dense_cloud_parity(ne, ctx, oracle_lib):
 
 
 def test_split_queue_overflow(ne, ctx, oracle_lib):
-    """The split kernel's queue holds a quarter of the paths (at least 1024). All paths here
-    start through the dense centre of the medium, so far more than a quarter scatter; those
-    beyond the queue finish in the first pass, and every path still matches the oracle bit
-    for bit."""
+    """The split kernel's queue classes (by the light the next draw picks) hold half and a
+    quarter of the paths (at least 2048 and 1024). All paths here start through the dense
+    centre of the medium, so far more than that scatter towards each light; those beyond the
+    queue finish in the first pass, and every path still matches the oracle bit for bit."""
     host = ne.SceneHost.from_json(scene_path("medium_c2"))
     scene = ctx.upload(host)
     scene.set_tuning(kernel=3)
