@@ -46,9 +46,10 @@ WORKLOADS = {
     "cornell_c1": "cornell_c1: Cornell box, 5 rectangles + 2 GGX spheres, 0.5x0.5 emitter (17,12,4), "
                   "256x256x16spp, depth 8, RR after 3",
     "mesh_c3": "mesh_c3: 1.31M-triangle displaced icosphere (1024 GGX groups) on a 10x10 ground, two emitters 10, "
-               "1024x1024x32spp, depth 12, reference midpoint BVH",
+               "1024x1024x32spp, depth 12, binned-SAH BVH built on the GPU at upload",
     "views_c5": "views_c5: 64 orbiting views (seeded sizes from {64,128,256,512}^2) of the 128^3 medium + the "
-                "1.31M-triangle mesh, 16 spp, depth 32, one persistent launch replayed as a CUDA graph, autotuned",
+                "1.31M-triangle mesh (GPU binned-SAH BVH), 16 spp, depth 32, one persistent launch replayed as a CUDA "
+                "graph, autotuned",
     "cloud_c4": "cloud_c4: 512^3 fBm cloud (7 octaves, scale 80, albedo 0.99, HG g=0.85), sun 3.0 @30deg + env 0.2, "
                 "1024x1024x16spp, depth 256, plain integrator",
 }

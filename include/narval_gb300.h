@@ -320,6 +320,13 @@ ne_status ne_render_cached(ne_scene* scene, ne_cache* cache, const ne_render_par
 ne_status ne_debug_bvh(const ne_primitive* prims, uint32_t first, uint32_t count, float* nodes, size_t cap,
                        uint32_t* order, size_t* n_nodes);
 
+/* The BVH of model `model` of an uploaded scene, read back from the device in ne_debug_bvh's
+ * format (an interior node's start and count are 0) with its primitive order (the model's
+ * prim_count global primitive indices). nodes = NULL: sets *n_nodes only (0: no BVH). Lets a
+ * CPU check traverse the tree the GPU built ("bvh": "sah"). */
+ne_status ne_scene_bvh(const ne_scene* scene, uint32_t model, float* nodes, size_t cap, uint32_t* order,
+                       size_t* n_nodes);
+
 /* One 128 x n x k tensor-core product D = A * B^T (BF16 bit patterns, row-major A[128][k],
  * B[n][k]; FP32 D[128][n]) through the same shared-memory and tensor-memory conventions as
  * the radiance-cache kernels. n in 16..256 step 16, k in 16..128 step 16. */

@@ -140,6 +140,8 @@ typedef struct ne_settings {
   int32_t hdr;
   int32_t rr_enabled; /* extension: Russian roulette on the path throughput */
   int32_t rr_after;   /* extension: first bounce index (exclusive) where it applies */
+  int32_t bvh_build;  /* extension: 0 = BVH::init's midpoint build on the host (the reference's
+                         tree), 1 = binned-SAH build on the GPU (same layout and leaf size) */
 } ne_settings;
 
 typedef struct ne_scene_desc {

@@ -83,6 +83,18 @@ class SceneHost:
             raise NarvalError(st, err.value.decode())
         return cls(h)
 
+    def model_prim_count(self, model: int) -> int:
+        d = C.cast(self.desc_ptr, C.POINTER(_abi.NeSceneDesc)).contents
+        return int(d.models[model].prim_count)
+
+    @property
+    def n_models(self) -> int:
+        return int(C.cast(self.desc_ptr, C.POINTER(_abi.NeSceneDesc)).contents.n_models)
+
+    def model_uses_bvh(self, model: int) -> bool:
+        d = C.cast(self.desc_ptr, C.POINTER(_abi.NeSceneDesc)).contents
+        return bool(d.models[model].use_bvh)
+
     @property
     def desc_ptr(self):
         return library().ne_scene_host_desc(self._h)
@@ -261,6 +273,19 @@ class Scene:
                                                   C.byref(cst)))
         return (img, {f: getattr(stats, f) for f, _ in NeRenderStats._fields_},
                 {f: getattr(cst, f) for f, _ in _abi.NeCacheRenderStats._fields_})
+
+    def bvh(self, model: int):
+        """ne_scene_bvh: (nodes (n, 9) float32 as ne_debug_bvh writes them, primitive order) of
+        one model's device BVH, or None for a model without one."""
+        n = C.c_size_t()
+        self.ctx.check(library().ne_scene_bvh(self._h, model, None, 0, None, C.byref(n)))
+        if n.value == 0:
+            return None
+        prim_count = self.host.model_prim_count(model)
+        nodes = np.empty((n.value, 9), np.float32)
+        order = np.empty(prim_count, np.uint32)
+        self.ctx.check(library().ne_scene_bvh(self._h, model, _ptr(nodes), n.value, _ptr(order), C.byref(n)))
+        return nodes, order
 
     def set_tuning(self, kernel: int = 0, track_share: int = 16, blocks_per_sm: int = 0, split_passes: int = 0,
                    split_half: int = 1):

@@ -46,7 +46,7 @@ class NeCamera(C.Structure):
 
 class NeSettings(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32), ("bounces", C.c_int32),
-                ("hdr", C.c_int32), ("rr_enabled", C.c_int32), ("rr_after", C.c_int32)]
+                ("hdr", C.c_int32), ("rr_enabled", C.c_int32), ("rr_after", C.c_int32), ("bvh_build", C.c_int32)]
 
 
 class NeSceneDesc(C.Structure):
@@ -192,6 +192,7 @@ SIGNATURES = {
     "ne_views_image": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p]),
     "ne_debug_bvh": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_size_t, C.c_void_p,
                                  C.POINTER(C.c_size_t)]),
+    "ne_scene_bvh": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_size_t, C.c_void_p, C.POINTER(C.c_size_t)]),
     "ne_save_png": (C.c_int32, [C.c_char_p, C.c_void_p, C.c_int, C.c_int]),
     "ne_save_exr": (C.c_int32, [C.c_char_p, C.c_void_p, C.c_int, C.c_int]),
     "ne_image_load_rgba8": (C.c_int32, [C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_void_p,

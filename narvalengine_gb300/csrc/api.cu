@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "narval_gb300.h"
+#include "bvh_build.h"
 #include "kernels.cuh"
 #include "mlp.h"
 #include "views.cuh"
@@ -93,6 +94,8 @@ struct ne_scene {
   // counters (kMaxSplitPasses x u64), all cleared by one memset per render
   DeferQueue* d_dq = nullptr;
   unsigned char* d_pass = nullptr;
+  std::vector<uint32_t> bvh_nodes_of;  // BVH node count per model (0: none), for ne_scene_bvh
+  std::vector<DModel> bvh_models;      // host copy of the device models (their BVH offsets)
   bool dq_uploaded = false;
   int track_share = 16;      // k_sched tracking-phase threshold (32nds of live lanes)
   uint32_t features = 0;     // FT_* bits of the scene
@@ -1105,7 +1108,9 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
     d.has_bbox = s.has_bbox;
     memcpy(d.bbox_min, s.bbox_min, 12);
     memcpy(d.bbox_max, s.bbox_max, 12);
-    if (s.use_bvh && s.prim_count > 0) {
+    if (s.use_bvh && s.prim_count > 0 && D.settings.bvh_build == 1) {
+      d.use_bvh = 1;  // built on the GPU once the primitives are there (below)
+    } else if (s.use_bvh && s.prim_count > 0) {
       std::vector<uint32_t> order(s.prim_count);
       for (uint32_t k = 0; k < s.prim_count; k++) order[k] = s.prim_begin + k;
       std::vector<HNode> hn;
@@ -1206,9 +1211,37 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
     }
   }
   ne_status st = NE_OK;
+  if ((st = upload(sc, prims.data(), prims.size(), &sc->d.prims))) return cleanup(st);
+  if (D.settings.bvh_build == 1) {
+    // binned-SAH trees built on the GPU from the uploaded primitives
+    for (uint32_t i = 0; i < D.n_models; i++) {
+      const ne_model& s = D.models[i];
+      if (!s.use_bvh || s.prim_count == 0) continue;
+      std::vector<DNode> bn;
+      std::vector<uint32_t> bs;
+      std::string err;
+      cudaError_t e = buildSahBvh(ctx->stream, sc->d.prims, s.prim_begin, s.prim_count, bn, bs, err);
+      if (e != cudaSuccess) {
+        if (!err.empty()) return cleanup(fail(ctx, NE_ERR_CUDA, err.c_str()));
+        return cleanup(cudaFail(ctx, e, "GPU BVH build"));
+      }
+      models[i].bvh_node0 = (uint32_t)nodes.size();
+      models[i].bvh_slot0 = (uint32_t)slots.size();
+      nodes.insert(nodes.end(), bn.begin(), bn.end());
+      slots.insert(slots.end(), bs.begin(), bs.end());
+    }
+  }
+  sc->bvh_nodes_of.assign(D.n_models, 0);
+  for (uint32_t i = 0; i < D.n_models; i++) {
+    if (!models[i].use_bvh) continue;
+    uint32_t end = (uint32_t)nodes.size();
+    for (uint32_t j = 0; j < D.n_models; j++)
+      if (models[j].use_bvh && models[j].bvh_node0 > models[i].bvh_node0) end = std::min(end, models[j].bvh_node0);
+    sc->bvh_nodes_of[i] = end - models[i].bvh_node0;
+  }
+  sc->bvh_models.assign(models.begin(), models.end());
   if ((st = upload(sc, inst.data(), inst.size(), &sc->d.instances))) return cleanup(st);
   if ((st = upload(sc, models.data(), models.size(), &sc->d.models))) return cleanup(st);
-  if ((st = upload(sc, prims.data(), prims.size(), &sc->d.prims))) return cleanup(st);
   if ((st = upload(sc, mats.data(), mats.size(), &sc->d.materials))) return cleanup(st);
   if ((st = upload(sc, D.model_materials, D.n_model_materials, &sc->d.model_materials))) return cleanup(st);
   if ((st = upload(sc, lights.data(), lights.size(), &sc->d.lights))) return cleanup(st);
@@ -2290,6 +2323,45 @@ ne_status ne_scene_autotune(ne_scene* sc, const ne_render_params* p, int repeats
   if (st) return st;
   if (best) ne_scene_get_tuning(sc, best);
   if (best_ms) *best_ms = bms;
+  return NE_OK;
+}
+
+ne_status ne_scene_bvh(const ne_scene* sc, uint32_t model, float* nodes, size_t cap, uint32_t* order,
+                       size_t* n_nodes) {
+  if (!sc || !n_nodes || model >= sc->bvh_nodes_of.size()) return NE_ERR_INVALID_ARG;
+  const uint32_t nn = sc->bvh_nodes_of[model];
+  *n_nodes = nn;
+  if (!nodes) return NE_OK;
+  if (nn == 0) return NE_OK;
+  if (cap < nn || !order) return NE_ERR_INVALID_ARG;
+  ne_context* ctx = sc->ctx;
+  NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  const DModel& m = sc->bvh_models[model];
+  std::vector<DNode> dn(nn);
+  NE_CUDA(cudaMemcpyAsync(dn.data(), sc->d.bvh + m.bvh_node0, nn * sizeof(DNode), cudaMemcpyDeviceToHost, ctx->stream),
+          "cudaMemcpyAsync");
+  NE_CUDA(cudaMemcpyAsync(order, sc->d.bvh_prims + m.bvh_slot0, m.prim_count * sizeof(uint32_t),
+                          cudaMemcpyDeviceToHost, ctx->stream),
+          "cudaMemcpyAsync");
+  NE_CUDA(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  for (uint32_t i = 0; i < nn; i++) {
+    float* o = nodes + 9 * (size_t)i;
+    memcpy(o, dn[i].lo, 12);
+    memcpy(o + 3, dn[i].hi, 12);
+    uint32_t a, b, zero = 0;
+    memcpy(&a, &dn[i].lo[3], 4);
+    memcpy(&b, &dn[i].hi[3], 4);
+    if (b & 0x80000000u) {  // leaf: start, count, rightOffset 0
+      uint32_t cnt = b & 0x7fffffffu;
+      memcpy(o + 6, &a, 4);
+      memcpy(o + 7, &cnt, 4);
+      memcpy(o + 8, &zero, 4);
+    } else {  // interior: rightOffset
+      memcpy(o + 6, &zero, 4);
+      memcpy(o + 7, &zero, 4);
+      memcpy(o + 8, &a, 4);
+    }
+  }
   return NE_OK;
 }
 

@@ -1,0 +1,390 @@
+// GPU binned-SAH BVH build for triangle meshes.
+//
+// The reference builds its BVH on the CPU by midpoint splits (primitives/BVH.cpp:6-106); a scene
+// may instead ask for this builder ("bvh": "sah" in its renderer block). The tree has the
+// reference's node layout and leaf size, so the same traversal (BVH.cpp:108-193) runs over it:
+// depth-first node order (left child = i + 1, right child = i + rightOffset), at most four
+// triangles per leaf. Closest hits equal those over the reference's tree except where two
+// triangles are hit at exactly the same distance (the traversal order decides those).
+//
+// The build runs level by level. Each level's tasks (contiguous ranges of the primitive order)
+// get one CTA each in two kernels:
+//  * k_sah_bin: node bounds and centroid bounds (block reduction), then 32 bins per axis over the
+//    centroid bounds (shared-memory atomics on order-preserving float keys), then the split of
+//    least surface-area cost A_L N_L + A_R N_R; a range of at most four triangles becomes a
+//    leaf; no split with both sides non-empty, or depth 36 and beyond, gives the median split.
+//  * k_sah_partition: stable partition of the range by the chosen split (block scans of the
+//    side flags), through a scratch array.
+// The host reads each level's results back, numbers the nodes and issues the next level; at
+// the end it lays the nodes out depth first. Every step is deterministic (integer counts,
+// min/max, stable partitions), so a scene always gets the same tree.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "bvh_build.h"
+
+namespace nedev {
+namespace {
+
+constexpr int kBins = 32;
+constexpr uint32_t kLeafPrims = 4;      // BVH::init's primitives per leaf (BVH.cpp)
+constexpr uint32_t kMedianDepth = 36;   // from this depth on every split is the median
+constexpr int kMaxLevels = 64;
+constexpr int kThreads = 256;
+
+struct Task {
+  uint32_t begin, end, depth, pad;
+};
+struct TaskResult {
+  float mn[3], mx[3];
+  int32_t axis;      // -1: median split
+  uint32_t split;    // bins [0, split) go left
+  uint32_t nLeft;
+  int32_t leaf;
+  float cmin, scale; // bin of centroid c: (int)((c - cmin) * scale), clamped to [0, kBins)
+};
+
+// Order-preserving map of floats to unsigned keys (for atomicMin/atomicMax).
+__device__ __forceinline__ uint32_t fkey(float f) {
+  uint32_t u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float funkey(uint32_t k) {
+  return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+__device__ __forceinline__ int binOf(float c, float cmin, float scale) {
+  int b = (int)((c - cmin) * scale);
+  return b < 0 ? 0 : (b >= kBins ? kBins - 1 : b);
+}
+__device__ __forceinline__ float area(const float* mn, const float* mx) {
+  float dx = mx[0] - mn[0], dy = mx[1] - mn[1], dz = mx[2] - mn[2];
+  return 2.0f * (dx * dy + dy * dz + dz * dx);
+}
+
+__global__ void k_prim_bounds(const DPrim* __restrict__ prims, uint32_t first, uint32_t n, float4* __restrict__ lo,
+                              float4* __restrict__ hi, float4* __restrict__ cen, uint32_t* __restrict__ order) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const DPrim& p = prims[first + i];
+    float mn[3], mx[3];
+    for (int k = 0; k < 3; k++) {
+      mn[k] = fminf(fminf(p.p0[k], p.p1[k]), p.p2[k]);
+      mx[k] = fmaxf(fmaxf(p.p0[k], p.p1[k]), p.p2[k]);
+    }
+    lo[i] = make_float4(mn[0], mn[1], mn[2], 0.0f);
+    hi[i] = make_float4(mx[0], mx[1], mx[2], 0.0f);
+    cen[i] = make_float4(0.5f * (mn[0] + mx[0]), 0.5f * (mn[1] + mx[1]), 0.5f * (mn[2] + mx[2]), 0.0f);
+    order[i] = i;
+  }
+}
+
+// Block-wide min (op 0) or max (op 1) of one value per thread; every thread gets the result.
+__device__ float blockReduce(float v, int op, float* scratch) {
+  for (int o = 16; o > 0; o >>= 1) {
+    float w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = op ? fmaxf(v, w) : fminf(v, w);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) scratch[warp] = v;
+  __syncthreads();
+  float r = scratch[0];
+  for (int w = 1; w < (int)(blockDim.x >> 5); w++) r = op ? fmaxf(r, scratch[w]) : fminf(r, scratch[w]);
+  return r;
+}
+
+__global__ void __launch_bounds__(kThreads) k_sah_bin(const Task* __restrict__ tasks, const float4* __restrict__ lo,
+                                                     const float4* __restrict__ hi, const float4* __restrict__ cen,
+                                                     const uint32_t* __restrict__ order, TaskResult* __restrict__ res) {
+  __shared__ float scratch[kThreads / 32];
+  __shared__ uint32_t bmin[3][kBins][3], bmax[3][kBins][3], bcnt[3][kBins];
+  const Task t = tasks[blockIdx.x];
+  const uint32_t count = t.end - t.begin;
+  const float inf = __int_as_float(0x7f800000);
+  float mn[3] = {inf, inf, inf}, mx[3] = {-inf, -inf, -inf}, cmn[3] = {inf, inf, inf}, cmx[3] = {-inf, -inf, -inf};
+  for (uint32_t i = t.begin + threadIdx.x; i < t.end; i += blockDim.x) {
+    uint32_t p = order[i];
+    float4 a = lo[p], b = hi[p], c = cen[p];
+    mn[0] = fminf(mn[0], a.x); mn[1] = fminf(mn[1], a.y); mn[2] = fminf(mn[2], a.z);
+    mx[0] = fmaxf(mx[0], b.x); mx[1] = fmaxf(mx[1], b.y); mx[2] = fmaxf(mx[2], b.z);
+    cmn[0] = fminf(cmn[0], c.x); cmn[1] = fminf(cmn[1], c.y); cmn[2] = fminf(cmn[2], c.z);
+    cmx[0] = fmaxf(cmx[0], c.x); cmx[1] = fmaxf(cmx[1], c.y); cmx[2] = fmaxf(cmx[2], c.z);
+  }
+  for (int k = 0; k < 3; k++) {
+    mn[k] = blockReduce(mn[k], 0, scratch);
+    mx[k] = blockReduce(mx[k], 1, scratch);
+    cmn[k] = blockReduce(cmn[k], 0, scratch);
+    cmx[k] = blockReduce(cmx[k], 1, scratch);
+  }
+  TaskResult r;
+  for (int k = 0; k < 3; k++) { r.mn[k] = mn[k]; r.mx[k] = mx[k]; }
+  r.axis = -1;
+  r.split = 0;
+  r.nLeft = count / 2;
+  r.leaf = count <= kLeafPrims;
+  r.cmin = 0.0f;
+  r.scale = 0.0f;
+  if (r.leaf || t.depth >= kMedianDepth) {
+    if (threadIdx.x == 0) res[blockIdx.x] = r;
+    return;
+  }
+  float scale[3];
+  for (int a = 0; a < 3; a++) {
+    float ext = cmx[a] - cmn[a];
+    scale[a] = ext > 0.0f ? (float)kBins / ext : 0.0f;
+  }
+  for (int j = threadIdx.x; j < 3 * kBins; j += blockDim.x) {
+    int a = j / kBins, b = j % kBins;
+    for (int k = 0; k < 3; k++) { bmin[a][b][k] = 0xffffffffu; bmax[a][b][k] = 0u; }
+    bcnt[a][b] = 0;
+  }
+  __syncthreads();
+  for (uint32_t i = t.begin + threadIdx.x; i < t.end; i += blockDim.x) {
+    uint32_t p = order[i];
+    float4 a4 = lo[p], b4 = hi[p], c4 = cen[p];
+    const float pl[3] = {a4.x, a4.y, a4.z}, ph[3] = {b4.x, b4.y, b4.z}, pc[3] = {c4.x, c4.y, c4.z};
+    for (int a = 0; a < 3; a++) {
+      if (scale[a] == 0.0f) continue;
+      int b = binOf(pc[a], cmn[a], scale[a]);
+      for (int k = 0; k < 3; k++) {
+        atomicMin(&bmin[a][b][k], fkey(pl[k]));
+        atomicMax(&bmax[a][b][k], fkey(ph[k]));
+      }
+      atomicAdd(&bcnt[a][b], 1u);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float best = inf;
+    for (int a = 0; a < 3; a++) {
+      if (scale[a] == 0.0f) continue;
+      // right-hand sweep: bounds and counts of bins [s, kBins)
+      float rArea[kBins];
+      uint32_t rCnt[kBins];
+      float rmn[3] = {inf, inf, inf}, rmx[3] = {-inf, -inf, -inf};
+      uint32_t rc = 0;
+      for (int b = kBins - 1; b >= 0; b--) {
+        if (bcnt[a][b]) {
+          for (int k = 0; k < 3; k++) {
+            rmn[k] = fminf(rmn[k], funkey(bmin[a][b][k]));
+            rmx[k] = fmaxf(rmx[k], funkey(bmax[a][b][k]));
+          }
+          rc += bcnt[a][b];
+        }
+        rArea[b] = rc ? area(rmn, rmx) : 0.0f;
+        rCnt[b] = rc;
+      }
+      float lmn[3] = {inf, inf, inf}, lmx[3] = {-inf, -inf, -inf};
+      uint32_t lc = 0;
+      for (int s = 1; s < kBins; s++) {
+        int b = s - 1;
+        if (bcnt[a][b]) {
+          for (int k = 0; k < 3; k++) {
+            lmn[k] = fminf(lmn[k], funkey(bmin[a][b][k]));
+            lmx[k] = fmaxf(lmx[k], funkey(bmax[a][b][k]));
+          }
+          lc += bcnt[a][b];
+        }
+        if (lc == 0 || rCnt[s] == 0) continue;
+        float cost = area(lmn, lmx) * (float)lc + rArea[s] * (float)rCnt[s];
+        if (cost < best) {
+          best = cost;
+          r.axis = a;
+          r.split = (uint32_t)s;
+          r.nLeft = lc;
+          r.cmin = cmn[a];
+          r.scale = scale[a];
+        }
+      }
+    }
+    res[blockIdx.x] = r;
+  }
+}
+
+// A range whose left count differs from the binning's (which would mean the two kernels binned
+// differently) writes nothing out of its range and raises *bad; the host then fails the build.
+__global__ void __launch_bounds__(kThreads) k_sah_partition(const Task* __restrict__ tasks,
+                                                           const TaskResult* __restrict__ res,
+                                                           const float4* __restrict__ cen, uint32_t* __restrict__ order,
+                                                           uint32_t* __restrict__ tmp, uint32_t* __restrict__ bad) {
+  __shared__ uint32_t warpLeft[kThreads / 32];
+  __shared__ uint32_t run[2];
+  const Task t = tasks[blockIdx.x];
+  const TaskResult r = res[blockIdx.x];
+  if (r.leaf) return;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  if (threadIdx.x == 0) { run[0] = 0; run[1] = 0; }
+  __syncthreads();
+  for (uint32_t base = t.begin; base < t.end; base += blockDim.x) {
+    uint32_t i = base + threadIdx.x;
+    bool valid = i < t.end;
+    uint32_t p = valid ? order[i] : 0;
+    bool left = false;
+    if (valid) {
+      if (r.axis < 0) {
+        left = (i - t.begin) < r.nLeft;
+      } else {
+        float4 c = cen[p];
+        float v = r.axis == 0 ? c.x : (r.axis == 1 ? c.y : c.z);
+        left = binOf(v, r.cmin, r.scale) < (int)r.split;
+      }
+    }
+    uint32_t ball = __ballot_sync(0xffffffffu, left);
+    uint32_t rank = __popc(ball & ((1u << lane) - 1u));
+    if (lane == 0) warpLeft[warp] = __popc(ball);
+    __syncthreads();
+    uint32_t before = 0, total = 0;
+    for (int w = 0; w < nwarps; w++) {
+      if (w < warp) before += warpLeft[w];
+      total += warpLeft[w];
+    }
+    if (valid) {
+      uint32_t leftBefore = before + rank;
+      uint32_t rightBefore = threadIdx.x - leftBefore;
+      uint32_t dest = left ? t.begin + run[0] + leftBefore : t.begin + r.nLeft + run[1] + rightBefore;
+      if (left ? (run[0] + leftBefore < r.nLeft) : (dest < t.end)) tmp[dest] = p;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      uint32_t chunk = min((uint32_t)blockDim.x, t.end - base);
+      run[0] += total;
+      run[1] += chunk - total;
+    }
+    __syncthreads();
+  }
+  if (run[0] != r.nLeft) {  // every thread reads the same value: leave the range as it is
+    if (threadIdx.x == 0) atomicOr(bad, 1u);
+    return;
+  }
+  for (uint32_t i = t.begin + threadIdx.x; i < t.end; i += blockDim.x) order[i] = tmp[i];
+}
+
+template <class T>
+struct DeviceArray {
+  T* p = nullptr;
+  ~DeviceArray() {
+    if (p) cudaFree(p);
+  }
+  cudaError_t alloc(size_t n) { return cudaMalloc(&p, (n ? n : 1) * sizeof(T)); }
+};
+
+struct BNode {
+  float mn[3], mx[3];
+  uint32_t begin, count;
+  int32_t left, right;
+};
+
+}  // namespace
+
+cudaError_t buildSahBvh(cudaStream_t st, const DPrim* prims, uint32_t first, uint32_t n, std::vector<DNode>& nodesOut,
+                        std::vector<uint32_t>& slotsOut, std::string& err) {
+  nodesOut.clear();
+  slotsOut.clear();
+  if (n == 0) return cudaSuccess;
+  DeviceArray<float4> lo, hi, cen;
+  DeviceArray<uint32_t> order, tmp;
+  DeviceArray<Task> dTasks;
+  DeviceArray<TaskResult> dRes;
+  DeviceArray<uint32_t> dBad;
+  cudaError_t e;
+  if ((e = lo.alloc(n)) || (e = hi.alloc(n)) || (e = cen.alloc(n)) || (e = order.alloc(n)) || (e = tmp.alloc(n)) ||
+      (e = dTasks.alloc(n)) || (e = dRes.alloc(n)) || (e = dBad.alloc(1)))
+    return e;
+  if ((e = cudaMemsetAsync(dBad.p, 0, sizeof(uint32_t), st))) return e;
+  int blocks = (int)std::min<uint32_t>((n + 255) / 256, 4096u);
+  k_prim_bounds<<<blocks, 256, 0, st>>>(prims, first, n, lo.p, hi.p, cen.p, order.p);
+  if ((e = cudaGetLastError())) return e;
+  std::vector<BNode> nodes(1);
+  std::vector<Task> tasks = {Task{0, n, 0, 0}};
+  std::vector<int32_t> ids = {0};
+  std::vector<TaskResult> res;
+  int level = 0;
+  for (; level < kMaxLevels && !tasks.empty(); level++) {
+    const uint32_t nt = (uint32_t)tasks.size();
+    if ((e = cudaMemcpyAsync(dTasks.p, tasks.data(), nt * sizeof(Task), cudaMemcpyHostToDevice, st))) return e;
+    k_sah_bin<<<nt, kThreads, 0, st>>>(dTasks.p, lo.p, hi.p, cen.p, order.p, dRes.p);
+    if ((e = cudaGetLastError())) return e;
+    k_sah_partition<<<nt, kThreads, 0, st>>>(dTasks.p, dRes.p, cen.p, order.p, tmp.p, dBad.p);
+    if ((e = cudaGetLastError())) return e;
+    res.resize(nt);
+    if ((e = cudaMemcpyAsync(res.data(), dRes.p, nt * sizeof(TaskResult), cudaMemcpyDeviceToHost, st))) return e;
+    if ((e = cudaStreamSynchronize(st))) return e;
+    std::vector<Task> next;
+    std::vector<int32_t> nextIds;
+    for (uint32_t k = 0; k < nt; k++) {
+      const Task& t = tasks[k];
+      const TaskResult& r = res[k];
+      BNode& b = nodes[ids[k]];
+      for (int j = 0; j < 3; j++) { b.mn[j] = r.mn[j]; b.mx[j] = r.mx[j]; }
+      b.begin = t.begin;
+      b.count = t.end - t.begin;
+      b.left = b.right = -1;
+      if (r.leaf) continue;
+      if (r.nLeft == 0 || r.nLeft >= b.count) {
+        err = "BVH build: empty child";
+        return cudaErrorUnknown;
+      }
+      int32_t l = (int32_t)nodes.size();
+      b.left = l;
+      b.right = l + 1;
+      nodes.push_back(BNode{});  // invalidates b
+      nodes.push_back(BNode{});
+      next.push_back(Task{t.begin, t.begin + r.nLeft, t.depth + 1, 0});
+      nextIds.push_back(l);
+      next.push_back(Task{t.begin + r.nLeft, t.end, t.depth + 1, 0});
+      nextIds.push_back(l + 1);
+    }
+    tasks.swap(next);
+    ids.swap(nextIds);
+  }
+  if (!tasks.empty()) {
+    err = "BVH build: deeper than 64 levels";
+    return cudaErrorUnknown;
+  }
+  std::vector<uint32_t> ord(n);
+  uint32_t bad = 0;
+  if ((e = cudaMemcpyAsync(ord.data(), order.p, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st))) return e;
+  if ((e = cudaMemcpyAsync(&bad, dBad.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st))) return e;
+  if ((e = cudaStreamSynchronize(st))) return e;
+  if (bad) {
+    err = "BVH build: partition disagrees with the binning";
+    return cudaErrorUnknown;
+  }
+  // depth-first layout: subtree sizes bottom-up (children follow their parent in `nodes`),
+  // then positions top-down
+  const size_t nn = nodes.size();
+  std::vector<uint32_t> size(nn, 1), pos(nn, 0);
+  for (size_t i = nn; i-- > 0;)
+    if (nodes[i].left >= 0) size[i] = 1 + size[nodes[i].left] + size[nodes[i].right];
+  for (size_t i = 0; i < nn; i++)
+    if (nodes[i].left >= 0) {
+      pos[nodes[i].left] = pos[i] + 1;
+      pos[nodes[i].right] = pos[i] + 1 + size[nodes[i].left];
+    }
+  nodesOut.resize(nn);
+  for (size_t i = 0; i < nn; i++) {
+    const BNode& b = nodes[i];
+    DNode d;
+    for (int j = 0; j < 3; j++) { d.lo[j] = b.mn[j]; d.hi[j] = b.mx[j]; }
+    uint32_t a, c;
+    if (b.left < 0) {
+      a = b.begin;
+      c = b.count | 0x80000000u;
+    } else {
+      a = pos[b.right] - pos[i];
+      c = 0;
+    }
+    memcpy(&d.lo[3], &a, 4);
+    memcpy(&d.hi[3], &c, 4);
+    nodesOut[pos[i]] = d;
+  }
+  slotsOut.resize(n);
+  for (uint32_t i = 0; i < n; i++) slotsOut[i] = first + ord[i];
+  return cudaSuccess;
+}
+
+}  // namespace nedev

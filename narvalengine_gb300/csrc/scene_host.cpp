@@ -21,6 +21,8 @@
 //    "icosphere" generator, loaded as the reference loads an obj/gltf model (bounding
 //    box and BVH); optional "groups" assign seeded GGX materials per triangle group.
 //  * renderer "rr": {"after": n} enables Russian roulette after bounce n.
+//  * renderer "bvh": "sah" builds mesh BVHs with the GPU binned-SAH builder ("reference", the
+//    default: BVH::init's midpoint build).
 // Elementary functions come from ne_fmath.h so that the same descriptor yields the
 // same matrices on x86-64 and aarch64 hosts.
 
@@ -833,6 +835,14 @@ struct Reader {
     if (const JVal* rr = ren.get("rr")) {
       st.rr_enabled = 1;
       if (const JVal* a = rr->get("after")) st.rr_after = (int)num(*a, "rr after");
+    }
+    st.bvh_build = 0;
+    if (const JVal* bv = ren.get("bvh")) {
+      std::string kind = sval(*bv, "renderer bvh");
+      if (kind == "sah")
+        st.bvh_build = 1;
+      else if (kind != "reference")
+        throw ParseError(NE_ERR_PARSE, "renderer bvh must be \"reference\" or \"sah\".");
     }
   }
 

@@ -1717,4 +1717,26 @@ size_t orc_model_bvh(const orc_scene* s, uint32_t m, float* nodes, size_t cap, u
   return om.nodeCount;
 }
 
+// Replaces model m's BVH by a tree given in orc_model_bvh's format (a tree the GPU built, for
+// checks of the device's traversal over it). order: the model's primitives in leaf order.
+int orc_model_set_bvh(orc_scene* s, uint32_t m, const float* nodes, size_t n, const uint32_t* order, size_t n_order) {
+  if (!s || m >= s->omodels.size() || !nodes || !order || n == 0) return -1;
+  if (n_order != s->models[m].prim_count) return -1;
+  OModel& om = s->omodels[m];
+  om.nodes.assign(n, BVHNode{});
+  for (size_t i = 0; i < n; i++) {
+    const float* o = nodes + 9 * i;
+    BVHNode& b = om.nodes[i];
+    b.mn = v3(o[0], o[1], o[2]);
+    b.mx = v3(o[3], o[4], o[5]);
+    memcpy(&b.start, o + 6, 4);
+    memcpy(&b.count, o + 7, 4);
+    memcpy(&b.rightOffset, o + 8, 4);
+    if (b.isLeaf() ? (size_t)b.start + b.count > n_order : i + b.rightOffset >= n) return -1;
+  }
+  om.nodeCount = (uint32_t)n;
+  om.prims.assign(order, order + n_order);
+  return 0;
+}
+
 }  // extern "C"

@@ -48,6 +48,7 @@ void orc_trace_closest(const orc_scene* s, const ne_ray* rays, size_t n, float t
 
 /* BVH::init result of model m: 9 words per node (min, max, start, count, rightOffset). */
 size_t orc_model_bvh(const orc_scene* s, uint32_t m, float* nodes, size_t cap, uint32_t* order);
+int orc_model_set_bvh(orc_scene* s, uint32_t m, const float* nodes, size_t n, const uint32_t* order, size_t n_order);
 
 /* Unit-level restatements for known-answer tests. */
 int orc_triangle_intersect(const float* v0, const float* v1, const float* v2, const ne_ray* r, float* t_near,

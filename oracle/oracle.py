@@ -31,6 +31,7 @@ SIGNATURES = {
     "orc_trace_view_paths": (None, [C.c_void_p, C.POINTER(NeRenderParams), C.c_void_p, C.c_int, C.c_int, C.c_uint32,
                                      C.c_void_p, C.c_size_t, C.c_void_p, C.c_int]),
     "orc_model_bvh": (C.c_size_t, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_size_t, C.c_void_p]),
+    "orc_model_set_bvh": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t]),
     "orc_li_batch": (None, [C.c_void_p, C.POINTER(NeRenderParams), C.c_void_p, C.c_void_p, C.c_size_t, C.c_uint32,
                             C.c_void_p, C.c_int]),
     "orc_render": (C.c_double, [C.c_void_p, C.POINTER(NeRenderParams), C.c_void_p, C.c_int]),
@@ -117,6 +118,13 @@ class OracleScene:
         order = np.empty(n_prims, np.uint32)
         n = self._lib.orc_model_bvh(self._h, m, _p(nodes), len(nodes), _p(order))
         return nodes[:n], order
+
+    def set_model_bvh(self, m: int, nodes: np.ndarray, order: np.ndarray):
+        """Traverse model m through the given tree (orc_model_bvh's format) from now on."""
+        nodes = np.ascontiguousarray(nodes, dtype=np.float32).reshape(-1, 9)
+        order = np.ascontiguousarray(order, dtype=np.uint32)
+        if self._lib.orc_model_set_bvh(self._h, m, _p(nodes), len(nodes), _p(order), len(order)) != 0:
+            raise ValueError("invalid BVH for model %d" % m)
 
     def li_batch(self, rays: np.ndarray, keys: np.ndarray, first_dim: int, params: NeRenderParams,
                  threads: int = 0) -> np.ndarray:

@@ -234,6 +234,7 @@ def mesh_scene_json(subdivisions):
     d = json.load(open(scene_path("mesh_c3")))
     d["primitives"][0]["subdivisions"] = subdivisions
     d["renderer"]["resolution"] = [160, 120]
+    d["renderer"]["bvh"] = "reference"  # the oracle builds the reference's tree itself
     return json.dumps(d)
 
 
