@@ -19,9 +19,11 @@
 #include <cmath>
 #include <deque>
 #include <future>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "narval_gb300.h"
@@ -31,6 +33,62 @@
 #include "views.cuh"
 
 using namespace nedev;
+
+// Device buffers a context keeps for reuse. cudaFree synchronises the whole device and
+// cudaMalloc of gigabytes costs milliseconds; a caller that uploads, renders and destroys
+// scenes frame after frame (or renders into host memory) would pay both every time. Buffers
+// released by a scene or a render stay here, idle, and the next request of a similar size
+// (the smallest cached buffer of at least the requested size and at most twice it) takes one.
+// All users enqueue on the context's one stream, so a reused buffer is never still in use by
+// earlier work. At most `limit` bytes stay cached (the rest is freed); a failed cudaMalloc
+// frees the cache and retries.
+struct DevicePool {
+  std::multimap<size_t, void*> idle;          // size -> buffer
+  std::unordered_map<void*, size_t> size_of;  // every buffer handed out or idle
+  size_t idle_bytes = 0;
+  size_t limit = size_t(16) << 30;
+  cudaError_t get(size_t bytes, void** out) {
+    *out = nullptr;
+    bytes = std::max<size_t>(bytes, 256);
+    auto it = idle.lower_bound(bytes);
+    if (it != idle.end() && it->first <= 2 * bytes) {
+      *out = it->second;
+      idle_bytes -= it->first;
+      idle.erase(it);
+      return cudaSuccess;
+    }
+    cudaError_t e = cudaMalloc(out, bytes);
+    if (e == cudaErrorMemoryAllocation && !idle.empty()) {
+      cudaGetLastError();
+      trim(0);
+      e = cudaMalloc(out, bytes);
+    }
+    if (e != cudaSuccess) {
+      *out = nullptr;
+      return e;
+    }
+    size_of[*out] = bytes;
+    return cudaSuccess;
+  }
+  void put(void* p) {
+    if (!p) return;
+    auto it = size_of.find(p);
+    if (it == size_of.end()) return;
+    idle.emplace(it->second, p);
+    idle_bytes += it->second;
+    trim(limit);
+  }
+  // Frees idle buffers, largest first, until at most `keep` bytes stay cached.
+  void trim(size_t keep) {
+    while (idle_bytes > keep && !idle.empty()) {
+      auto it = std::prev(idle.end());
+      cudaFree(it->second);
+      size_of.erase(it->second);
+      idle_bytes -= it->first;
+      idle.erase(it);
+    }
+  }
+};
 
 struct ne_context {
   int device = 0;
@@ -45,6 +103,7 @@ struct ne_context {
   uint32_t* d_err = nullptr;
   std::vector<ne_scene*> scenes;            // live scenes, destroyed with the context
   std::vector<ne_cache*> caches;            // live radiance caches, destroyed with the context
+  DevicePool pool;                          // scene and render buffers, reused
 };
 
 struct ne_cache {
@@ -153,12 +212,25 @@ ne_status upload(ne_scene* sc, const T* host, size_t n, const T** out) {
   *out = nullptr;
   if (n == 0) return NE_OK;
   void* p = nullptr;
-  NE_CUDA(cudaMalloc(&p, n * sizeof(T)), "cudaMalloc");
+  NE_CUDA(ctx->pool.get(n * sizeof(T), &p), "cudaMalloc");
   sc->allocs.push_back(p);
   NE_CUDA(cudaMemcpyAsync(p, host, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream), "cudaMemcpyAsync");
   *out = (const T*)p;
   return NE_OK;
 }
+
+// A buffer from the context's pool for the duration of one call (given back on return).
+struct PoolBuf {
+  DevicePool* pool = nullptr;
+  void* p = nullptr;
+  ~PoolBuf() {
+    if (pool) pool->put(p);
+  }
+  cudaError_t get(DevicePool& pl, size_t bytes) {
+    pool = &pl;
+    return pl.get(bytes, &p);
+  }
+};
 
 // ---- InfiniteAreaLight's importance-sampling tables (built at upload, read by envSample)
 // Distribution1D's constructor (utils/Sampling.h:12-28): func, CDF of func / n normalised by
@@ -405,6 +477,29 @@ __global__ void k_cells(const float* __restrict__ grid, uint32_t W, uint32_t H, 
   }
 }
 
+// GridMedia::calculateMaxDensity (materials/GridMedia.h:16-21): mx = 0; mx = (mx < v) ? v : mx
+// over the voxels, i.e. the largest value and 0 (NaN voxels never replace it), as an
+// order-preserving unsigned key combined by atomicMax (*key starts at the key of 0).
+__device__ __forceinline__ uint32_t maxKey(float f) {
+  uint32_t u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__global__ void k_grid_max(const float* __restrict__ grid, size_t n, uint32_t* __restrict__ key) {
+  uint32_t best = maxKey(0.0f);
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    float v = grid[i];
+    if (v == v) best = max(best, maxKey(v));
+  }
+  for (int o = 16; o > 0; o >>= 1) best = max(best, __shfl_xor_sync(0xffffffffu, best, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(key, best);
+}
+// invMaxDensity = 1 / max, written into the medium's device record.
+__global__ void k_grid_inv_max(const uint32_t* __restrict__ key, DMedium* __restrict__ m) {
+  uint32_t k = *key;
+  float mx = __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+  m->inv_max_density = 1.0f / mx;
+}
+
 // Per-pixel mean in sample order: color += Li for s = 0..spp-1, then color / spp.
 __global__ void k_reduce(const float* __restrict__ paths, uint32_t n_pix, uint32_t spp, uint32_t cover_w, int W,
                          float* __restrict__ out) {
@@ -540,18 +635,30 @@ ne_status launchSplit(ne_scene* sc, PathArgs b, int blocks, F launch) {
   size_t cap = std::min(kMaxDeferEntries, std::max<size_t>(3072, (size_t)(b.total / 4) * 3));
   if (sc->defer_cap < cap) {
     for (PathState*& q : sc->d_defer) {
-      if (q) cudaFree(q);
+      ctx->pool.put(q);
       q = nullptr;
     }
     sc->defer_cap = 0;
     sc->dq_uploaded = false;
-    for (PathState*& q : sc->d_defer) NE_CUDA(cudaMalloc(&q, cap * sizeof(PathState)), "cudaMalloc(deferred paths)");
+    for (PathState*& q : sc->d_defer) {
+      void* qp = nullptr;
+      NE_CUDA(ctx->pool.get(cap * sizeof(PathState), &qp), "cudaMalloc(deferred paths)");
+      q = (PathState*)qp;
+    }
     sc->defer_cap = cap;
   }
   const size_t countBytes = 2 * kMaxSplitPasses * sizeof(uint32_t);  // both classes
   const size_t passBytes = countBytes + kMaxSplitPasses * sizeof(unsigned long long);
-  if (!sc->d_dq) NE_CUDA(cudaMalloc(&sc->d_dq, kMaxSplitPasses * sizeof(DeferQueue)), "cudaMalloc");
-  if (!sc->d_pass) NE_CUDA(cudaMalloc(&sc->d_pass, passBytes), "cudaMalloc");
+  if (!sc->d_dq) {
+    void* qp = nullptr;
+    NE_CUDA(ctx->pool.get(kMaxSplitPasses * sizeof(DeferQueue), &qp), "cudaMalloc");
+    sc->d_dq = (DeferQueue*)qp;
+  }
+  if (!sc->d_pass) {
+    void* pp = nullptr;
+    NE_CUDA(ctx->pool.get(passBytes, &pp), "cudaMalloc");
+    sc->d_pass = (unsigned char*)pp;
+  }
   if (!sc->dq_uploaded) {
     DeferQueue dq[kMaxSplitPasses];
     for (int p = 0; p < kMaxSplitPasses; p++) {
@@ -979,6 +1086,8 @@ void ne_context_destroy(ne_context* ctx) {
   if (ctx->flush_buf) cudaFree(ctx->flush_buf);
   if (ctx->d_counter) cudaFree(ctx->d_counter);
   if (ctx->d_err) cudaFree(ctx->d_err);
+  ctx->pool.trim(0);
+  for (auto& kv : ctx->pool.size_of) cudaFree(kv.first);  // buffers never given back
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -1075,7 +1184,7 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
   }
   // primitives
   std::vector<DPrim> prims(D.n_prims);
-  for (uint32_t i = 0; i < D.n_prims; i++) {
+  auto convertPrim = [&](uint32_t i) {
     const ne_primitive& s = D.prims[i];
     DPrim& d = prims[i];
     memset(&d, 0, sizeof(d));
@@ -1093,6 +1202,18 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
       const ne_material& m = D.materials[s.material];
       if (m.medium >= 0 && D.media[m.medium].type == NE_MEDIUM_GRID) d.flags |= DPRIM_GRID_MEDIUM;
     }
+  };
+  {
+    // large meshes: in parallel chunks (each primitive is converted on its own)
+    const uint32_t chunk = 1u << 16;
+    const uint32_t nchunks = (D.n_prims + chunk - 1) / chunk;
+    std::vector<std::future<void>> jobs;
+    for (uint32_t c = 1; c < nchunks; c++)
+      jobs.push_back(std::async(std::launch::async, [&, c] {
+        for (uint32_t i = c * chunk; i < std::min(D.n_prims, (c + 1) * chunk); i++) convertPrim(i);
+      }));
+    for (uint32_t i = 0; i < std::min(D.n_prims, chunk); i++) convertPrim(i);
+    for (auto& j : jobs) j.get();
   }
   // models + BVHs
   std::vector<DModel> models(D.n_models);
@@ -1174,6 +1295,7 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
   }
   // media: dense grid + 8-corner cells
   std::vector<DMedium> media(D.n_media);
+  std::vector<uint32_t> gridMedia;
   for (uint32_t i = 0; i < D.n_media; i++) {
     const ne_medium& s = D.media[i];
     DMedium& d = media[i];
@@ -1189,9 +1311,7 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
     if (s.type == NE_MEDIUM_GRID) {
       if (!s.grid || !s.res[0] || !s.res[1] || !s.res[2]) return cleanup(fail(ctx, NE_ERR_INVALID_ARG, "grid medium without voxels"));
       size_t n = (size_t)s.res[0] * s.res[1] * s.res[2];
-      float mx = 0;
-      for (size_t k = 0; k < n; k++) mx = (mx < s.grid[k]) ? s.grid[k] : mx;  // GridMedia.h:16-21
-      d.inv_max_density = 1.0f / mx;
+      gridMedia.push_back(i);  // invMaxDensity from the device copy of the grid, below
       memcpy(d.res, s.res, 12);
       d.resf[0] = (float)s.res[0]; d.resf[1] = (float)s.res[1]; d.resf[2] = (float)s.res[2];
       const float* dg = nullptr;
@@ -1200,7 +1320,7 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
       d.grid = dg;
       size_t ncell = (size_t)(s.res[0] + 1) * (s.res[1] + 1) * (s.res[2] + 1);
       void* cp = nullptr;
-      cudaError_t e = cudaMalloc(&cp, ncell * 2 * sizeof(float4));
+      cudaError_t e = ctx->pool.get(ncell * 2 * sizeof(float4), &cp);
       if (e != cudaSuccess) return cleanup(cudaFail(ctx, e, "cudaMalloc(cells)"));
       sc->allocs.push_back(cp);
       int blocks = ctx->sm_count * 8;
@@ -1246,6 +1366,21 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
   if ((st = upload(sc, D.model_materials, D.n_model_materials, &sc->d.model_materials))) return cleanup(st);
   if ((st = upload(sc, lights.data(), lights.size(), &sc->d.lights))) return cleanup(st);
   if ((st = upload(sc, media.data(), media.size(), &sc->d.media))) return cleanup(st);
+  if (!gridMedia.empty()) {
+    std::vector<uint32_t> keys(gridMedia.size(), 0x80000000u);  // the key of 0
+    const uint32_t* dkeys = nullptr;
+    if ((st = upload(sc, keys.data(), keys.size(), &dkeys))) return cleanup(st);
+    for (size_t k = 0; k < gridMedia.size(); k++) {
+      const uint32_t i = gridMedia[k];
+      const size_t n = (size_t)media[i].res[0] * media[i].res[1] * media[i].res[2];
+      uint32_t* key = const_cast<uint32_t*>(dkeys) + k;
+      int blocks = (int)std::min<size_t>((n + 255) / 256, (size_t)ctx->sm_count * 8);
+      k_grid_max<<<std::max(1, blocks), 256, 0, ctx->stream>>>(media[i].grid, n, key);
+      k_grid_inv_max<<<1, 1, 0, ctx->stream>>>(key, const_cast<DMedium*>(sc->d.media) + i);
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return cleanup(cudaFail(ctx, e, "k_grid_max launch"));
+    }
+  }
   if ((st = upload(sc, nodes.data(), nodes.size(), &sc->d.bvh))) return cleanup(st);
   if ((st = upload(sc, slots.data(), slots.size(), &sc->d.bvh_prims))) return cleanup(st);
   sc->d.n_instances = D.n_instances;
@@ -1341,12 +1476,12 @@ void ne_scene_destroy(ne_scene* sc) {
   v.erase(std::remove(v.begin(), v.end(), sc), v.end());
   cudaSetDevice(sc->ctx->device);
   cudaStreamSynchronize(sc->ctx->stream);
-  for (void* p : sc->allocs) cudaFree(p);
-  if (sc->d_paths) cudaFree(sc->d_paths);
-  for (PathState* q : sc->d_defer)
-    if (q) cudaFree(q);
-  if (sc->d_dq) cudaFree(sc->d_dq);
-  if (sc->d_pass) cudaFree(sc->d_pass);
+  DevicePool& pool = sc->ctx->pool;
+  for (void* p : sc->allocs) pool.put(p);
+  pool.put(sc->d_paths);
+  for (PathState* q : sc->d_defer) pool.put(q);
+  pool.put(sc->d_dq);
+  pool.put(sc->d_pass);
   delete sc;
 }
 
@@ -1366,21 +1501,23 @@ ne_status ne_render(ne_scene* sc, const ne_render_params* p, float* out_rgb, ne_
   uint64_t npix = (uint64_t)cw * ch;
   uint64_t total = npix * (uint64_t)spp;
   if (sc->paths_cap < total) {
-    if (sc->d_paths) cudaFree(sc->d_paths);
+    ctx->pool.put(sc->d_paths);
     sc->d_paths = nullptr;
     sc->paths_cap = 0;
-    NE_CUDA(cudaMalloc(&sc->d_paths, total * 3 * sizeof(float)), "cudaMalloc(paths)");
+    void* pp = nullptr;
+    NE_CUDA(ctx->pool.get(total * 3 * sizeof(float), &pp), "cudaMalloc(paths)");
+    sc->d_paths = (float*)pp;
     sc->paths_cap = total;
   }
   bool devOut = flags & NE_RENDER_OUT_DEVICE;
   float* d_img = nullptr;
-  DevBuf<float> tmpImg;
+  PoolBuf tmpImg;  // given back after the copy to the host, which this call waits for
   size_t imgBytes = (size_t)W * H * 3 * sizeof(float);
   if (devOut) {
     d_img = out_rgb;
   } else {
-    NE_CUDA(cudaMalloc(&tmpImg.p, imgBytes), "cudaMalloc(image)");
-    d_img = tmpImg.p;
+    NE_CUDA(tmpImg.get(ctx->pool, imgBytes), "cudaMalloc(image)");
+    d_img = (float*)tmpImg.p;
   }
   bool timed = !(flags & NE_RENDER_NO_SYNC);
   NE_CUDA(cudaMemsetAsync(ctx->d_err, 0, 4, ctx->stream), "cudaMemsetAsync");
@@ -1449,10 +1586,12 @@ ne_status ne_render_accumulate(ne_scene* sc, const ne_render_params* p, double* 
   }
   uint64_t npix = (uint64_t)cw * ch, total = npix * (uint64_t)spp;
   if (sc->paths_cap < total) {
-    if (sc->d_paths) cudaFree(sc->d_paths);
+    ctx->pool.put(sc->d_paths);
     sc->d_paths = nullptr;
     sc->paths_cap = 0;
-    NE_CUDA(cudaMalloc(&sc->d_paths, total * 3 * sizeof(float)), "cudaMalloc(paths)");
+    void* pp = nullptr;
+    NE_CUDA(ctx->pool.get(total * 3 * sizeof(float), &pp), "cudaMalloc(paths)");
+    sc->d_paths = (float*)pp;
     sc->paths_cap = total;
   }
   bool devAcc = flags & NE_RENDER_OUT_DEVICE;
@@ -1949,10 +2088,12 @@ ne_status ne_render_cached(ne_scene* sc, ne_cache* c, const ne_render_params* p,
   uint64_t npix = (uint64_t)cw * ch, total = npix * (uint64_t)spp;
   if (total > 0xFFFFFFFFull) return fail(ctx, NE_ERR_INVALID_ARG, "ne_render_cached: at most 2^32 paths per call");
   if (sc->paths_cap < total) {
-    if (sc->d_paths) cudaFree(sc->d_paths);
+    ctx->pool.put(sc->d_paths);
     sc->d_paths = nullptr;
     sc->paths_cap = 0;
-    NE_CUDA(cudaMalloc(&sc->d_paths, total * 3 * sizeof(float)), "cudaMalloc(paths)");
+    void* pp = nullptr;
+    NE_CUDA(ctx->pool.get(total * 3 * sizeof(float), &pp), "cudaMalloc(paths)");
+    sc->d_paths = (float*)pp;
     sc->paths_cap = total;
   }
   size_t tcap = cp->train_stride ? (size_t)std::min<uint64_t>(total, total / cp->train_stride * 2 + 4096) : 1;
@@ -1997,11 +2138,11 @@ ne_status ne_render_cached(ne_scene* sc, ne_cache* c, const ne_render_params* p,
   NE_CUDA(cudaMemsetAsync(ctx->d_counter, 0, 5 * sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync");
   bool devOut = flags & NE_RENDER_OUT_DEVICE;
   size_t imgBytes = (size_t)W * H * 3 * sizeof(float);
-  DevBuf<float> tmpImg;
+  PoolBuf tmpImg;
   float* d_img = out_rgb;
   if (!devOut) {
-    NE_CUDA(cudaMalloc(&tmpImg.p, imgBytes), "cudaMalloc(image)");
-    d_img = tmpImg.p;
+    NE_CUDA(tmpImg.get(ctx->pool, imgBytes), "cudaMalloc(image)");
+    d_img = (float*)tmpImg.p;
   }
   NE_CUDA(cudaEventRecord(c->ev[0], ctx->stream), "cudaEventRecord");
   if (cw != (uint32_t)W || ch != (uint32_t)H) NE_CUDA(cudaMemsetAsync(d_img, 0, imgBytes, ctx->stream), "cudaMemsetAsync");
