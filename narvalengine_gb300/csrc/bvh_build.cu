@@ -35,7 +35,7 @@ constexpr int kBins = 32;
 constexpr uint32_t kLeafPrims = 4;      // BVH::init's primitives per leaf (BVH.cpp)
 constexpr uint32_t kMedianDepth = 36;   // from this depth on every split is the median
 constexpr int kMaxLevels = 64;
-constexpr int kThreads = 256;
+constexpr int kThreads = 1024;  // most threads a task's CTA has (levels with few, large tasks)
 
 struct Task {
   uint32_t begin, end, depth, pad;
@@ -47,6 +47,7 @@ struct TaskResult {
   uint32_t nLeft;
   int32_t leaf;
   float cmin, scale; // bin of centroid c: (int)((c - cmin) * scale), clamped to [0, kBins)
+  float cb[2][6];    // binned split: the children's bounds (min xyz, max xyz), left then right
 };
 
 // Order-preserving map of floats to unsigned keys (for atomicMin/atomicMax).
@@ -198,8 +199,19 @@ __global__ void __launch_bounds__(kThreads) k_sah_bin(const Task* __restrict__ t
           r.nLeft = lc;
           r.cmin = cmn[a];
           r.scale = scale[a];
+          for (int k = 0; k < 3; k++) { r.cb[0][k] = lmn[k]; r.cb[0][3 + k] = lmx[k]; }
         }
       }
+    }
+    if (r.axis >= 0) {  // the right child's bounds: bins [split, kBins) of the chosen axis
+      float rmn[3] = {inf, inf, inf}, rmx[3] = {-inf, -inf, -inf};
+      for (int b = (int)r.split; b < kBins; b++)
+        if (bcnt[r.axis][b])
+          for (int k = 0; k < 3; k++) {
+            rmn[k] = fminf(rmn[k], funkey(bmin[r.axis][b][k]));
+            rmx[k] = fmaxf(rmx[k], funkey(bmax[r.axis][b][k]));
+          }
+      for (int k = 0; k < 3; k++) { r.cb[1][k] = rmn[k]; r.cb[1][3 + k] = rmx[k]; }
     }
     res[blockIdx.x] = r;
   }
@@ -306,9 +318,12 @@ cudaError_t buildSahBvh(cudaStream_t st, const DPrim* prims, uint32_t first, uin
   for (; level < kMaxLevels && !tasks.empty(); level++) {
     const uint32_t nt = (uint32_t)tasks.size();
     if ((e = cudaMemcpyAsync(dTasks.p, tasks.data(), nt * sizeof(Task), cudaMemcpyHostToDevice, st))) return e;
-    k_sah_bin<<<nt, kThreads, 0, st>>>(dTasks.p, lo.p, hi.p, cen.p, order.p, dRes.p);
+    // CTA size by the level's task count: the first levels hold few tasks of many triangles,
+    // the last ones many small tasks
+    const int threads = nt <= 2048 ? 1024 : (nt <= 32768 ? 256 : 64);
+    k_sah_bin<<<nt, threads, 0, st>>>(dTasks.p, lo.p, hi.p, cen.p, order.p, dRes.p);
     if ((e = cudaGetLastError())) return e;
-    k_sah_partition<<<nt, kThreads, 0, st>>>(dTasks.p, dRes.p, cen.p, order.p, tmp.p, dBad.p);
+    k_sah_partition<<<nt, threads, 0, st>>>(dTasks.p, dRes.p, cen.p, order.p, tmp.p, dBad.p);
     if ((e = cudaGetLastError())) return e;
     res.resize(nt);
     if ((e = cudaMemcpyAsync(res.data(), dRes.p, nt * sizeof(TaskResult), cudaMemcpyDeviceToHost, st))) return e;
@@ -333,10 +348,20 @@ cudaError_t buildSahBvh(cudaStream_t st, const DPrim* prims, uint32_t first, uin
       b.right = l + 1;
       nodes.push_back(BNode{});  // invalidates b
       nodes.push_back(BNode{});
-      next.push_back(Task{t.begin, t.begin + r.nLeft, t.depth + 1, 0});
-      nextIds.push_back(l);
-      next.push_back(Task{t.begin + r.nLeft, t.end, t.depth + 1, 0});
-      nextIds.push_back(l + 1);
+      const uint32_t cBegin[2] = {t.begin, t.begin + r.nLeft}, cEnd[2] = {t.begin + r.nLeft, t.end};
+      for (int c = 0; c < 2; c++) {
+        if (r.axis >= 0 && cEnd[c] - cBegin[c] <= kLeafPrims) {
+          // a small child of a binned split is a leaf whose bounds the bins already hold
+          BNode& leaf = nodes[l + c];
+          for (int j = 0; j < 3; j++) { leaf.mn[j] = r.cb[c][j]; leaf.mx[j] = r.cb[c][3 + j]; }
+          leaf.begin = cBegin[c];
+          leaf.count = cEnd[c] - cBegin[c];
+          leaf.left = leaf.right = -1;
+        } else {
+          next.push_back(Task{cBegin[c], cEnd[c], t.depth + 1, 0});
+          nextIds.push_back(l + c);
+        }
+      }
     }
     tasks.swap(next);
     ids.swap(nextIds);
