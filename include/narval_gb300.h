@@ -218,7 +218,7 @@ ne_status ne_context_flush_l2(ne_context* ctx, size_t bytes);
 
 /* Device copies of the shared elementary functions, for bit-exactness checks.
  * fn: 0 log, 1 exp, 2 sin, 3 cos, 4 acos, 5 pow5, 6 atan2(x[i], x[i ^ 1]) (elements paired;
- * an unpaired last element is paired with 1). */
+ * an unpaired last element is paired with 1), 7 log(1 - x) for draws x = k 2^-24. */
 ne_status ne_debug_fmath(ne_context* ctx, int fn, const float* x, size_t n, float* out);
 
 /* Device copy of the shared counter-based generator: u01 for (seed, pixel, sample, dim). */

@@ -555,6 +555,7 @@ __global__ void k_fmath(int fn, const float* __restrict__ x, size_t n, float* __
       case 3: r = nefm::cos(v); break;
       case 4: r = nefm::acos(v); break;
       case 6: r = nefm::atan2(v, (i ^ 1) < n ? x[i ^ 1] : 1.0f); break;
+      case 7: r = nefm::log1m_draw(v); break;
       default: r = nefm::pow5(v); break;
     }
     out[i] = r;

@@ -88,18 +88,9 @@ constexpr float kLn2Lo = 0x1.0bfbe8p-15f;
 constexpr float kInvLn2 = 0x1.715476p+0f;
 constexpr float kSqrt2 = 0x1.6a09e6p+0f;
 
-// Natural logarithm.
-NE_HD float log(float x) {
-  if (isnan_(x) || x < 0.0f) return u2f(0x7fc00000u);
-  if (x == 0.0f) return -u2f(0x7f800000u);
-  if (isinf_(x)) return x;
-  int k = 0;
+// log(x 2^-k0) for a positive, normal, finite x.
+NE_HD float log_normal(float x, int k) {
   uint32_t ix = f2u(x);
-  if (ix < 0x00800000u) {  // subnormal: scale up by 2^25
-    x = x * 33554432.0f;
-    k = -25;
-    ix = f2u(x);
-  }
   k += (int)((ix >> 23) & 0xffu) - 127;
   float m = u2f((ix & 0x007fffffu) | 0x3f800000u);  // [1, 2)
   if (m > kSqrt2) { m = m * 0.5f; k += 1; }
@@ -113,6 +104,19 @@ NE_HD float log(float x) {
   float fk = (float)k;
   return (fk * kLn2Hi + (lg + fk * kLn2Lo));
 }
+
+// Natural logarithm.
+NE_HD float log(float x) {
+  if (isnan_(x) || x < 0.0f) return u2f(0x7fc00000u);
+  if (x == 0.0f) return -u2f(0x7f800000u);
+  if (isinf_(x)) return x;
+  if (f2u(x) < 0x00800000u) return log_normal(x * 33554432.0f, -25);  // subnormal: scale up by 2^25
+  return log_normal(x, 0);
+}
+
+// log(1 - u) for a uniform draw u = k 2^-24 (the tracking steps): 1 - u lies in [2^-24, 1],
+// positive and normal, so this is log without its special cases, with the same result.
+NE_HD float log1m_draw(float u) { return log_normal(1 - u, 0); }
 
 // Exponential.
 NE_HD float exp(float x) {

@@ -866,7 +866,7 @@ NE_NI V3 gridTr(Ctx<K>& c, const DMedium& M, Ray incoming, Hit isect) {
   float mu = M.mu;
   float Tr = 1, t = isect.tNear;
   for (int step = 0; step < kMaxTrackSteps; step++) {
-    t -= (nefm::log(1 - c.S.random()) * invMax) / mu;
+    t -= (nefm::log1m_draw(c.S.random()) * invMax) / mu;
     if (t >= isect.tFar) break;
     float density = sampleAt(c, M, incoming, t);
     float x = density * invMax;
@@ -892,7 +892,7 @@ NE_D V3 gridSample(Ctx<K>& c, const DMedium& M, Ray incoming, Ray& scattered, co
   float t = isect.tNear;
   for (int step = 0; step < kMaxTrackSteps; step++) {
     float r = c.S.random();
-    float sampledDist = (nefm::log(1 - r) * invMax) / mu;
+    float sampledDist = (nefm::log1m_draw(r) * invMax) / mu;
     t -= sampledDist;
     if (t >= isect.tFar) {
       scattered.o = incoming.at(isect.tFar + 0.0001f);

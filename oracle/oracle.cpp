@@ -1675,6 +1675,7 @@ void orc_fmath(int fn, const float* x, size_t n, float* out) {
       case 3: out[i] = nefm::cos(v); break;
       case 4: out[i] = nefm::acos(v); break;
       case 6: out[i] = nefm::atan2(v, (i ^ 1) < n ? x[i ^ 1] : 1.0f); break;
+      case 7: out[i] = nefm::log1m_draw(v); break;
       default: out[i] = nefm::pow5(v); break;
     }
   }

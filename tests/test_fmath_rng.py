@@ -62,6 +62,15 @@ def test_atan2_quadrants_and_zeros(oracle_lib):
     assert np.array_equal(np.signbit(got), np.signbit(want))
 
 
+def test_log1m_draw_equals_log_on_every_draw(oracle_lib):
+    """The tracking steps' log(1 - u) without log's special cases gives log's bits for all
+    2^24 values a draw can take."""
+    u = (np.arange(1 << 24, dtype=np.float64) * 2.0 ** -24).astype(np.float32)
+    fast = oracle_lib.fmath(7, u)
+    ref = oracle_lib.fmath(0, (np.float32(1) - u).astype(np.float32))
+    assert np.array_equal(fast.view(np.uint32), ref.view(np.uint32))
+
+
 def test_fmath_special_values(oracle_lib):
     log = oracle_lib.fmath(0, np.array([0.0, -1.0, np.inf, np.nan, 1.0, 2.0 ** -149], np.float32))
     assert log[0] == -np.inf and np.isnan(log[1]) and log[2] == np.inf and np.isnan(log[3]) and log[4] == 0.0

@@ -56,7 +56,7 @@ def spread_keys(host, n_pixels, spp, seed=0):
 
 
 @pytest.mark.parametrize("fn,lo,hi", [(0, 1e-30, 1e30), (1, -100.0, 88.0), (2, -60.0, 60.0), (3, -60.0, 60.0),
-                                      (4, -1.0, 1.0), (5, -3.0, 3.0), (6, -50.0, 50.0)])
+                                      (4, -1.0, 1.0), (5, -3.0, 3.0), (6, -50.0, 50.0), (7, 0.0, 1.0 - 2 ** -24)])
 def test_fmath_bit_exact(ctx, oracle_lib, fn, lo, hi):
     rng = np.random.default_rng(fn)
     if fn == 0:
