@@ -241,6 +241,7 @@ typedef struct ne_views_tuning {
   int32_t order;           /* views in the launch: 0 as given, 1 largest first, 2 smallest first */
   int32_t graph;           /* 1: capture the launch sequence once and replay it as a CUDA graph */
   int32_t split_passes;    /* as ne_tuning.split_passes: 1 = one pass, 2..64, 0 = 6 */
+  int32_t split_half;      /* as ne_tuning.split_half: 1 = deferral points every half bounce */
 } ne_views_tuning;
 typedef struct ne_views_stats {
   double ms;               /* CUDA-event time of the batch */

@@ -176,7 +176,7 @@ struct ne_views {
   uint32_t total_pixels = 0;
   PathParams P;
   nerng::PathKey base;
-  ne_views_tuning tune = {32, 0, 0, 1, 0};
+  ne_views_tuning tune = {32, 0, 0, 1, 0, 0};
   int blocks = 1;
   // split batches: two queues of deferred paths, the views' path spans, completion hook
   PathState* d_defer[2] = {nullptr, nullptr};
@@ -972,6 +972,7 @@ ne_status viewsEnqueue(ne_views* vw) {
   a.t_done = tdone;
   a.t_start = tstart;
   a.defer_out = split ? vw->d_dq : nullptr;
+  a.defer_half = vw->tune.split_half;
   if (split) NE_CUDA(cudaMemsetAsync(vw->d_dcount, 0, sizeof(uint32_t), ctx->stream), "cudaMemsetAsync");
   NE_CUDA(ne_launch_views(split, vw->blocks, ctx->stream, vw->sc->d, a, counter, ctx->d_err), "k_views launch");
   for (int pass = 1; pass < passes; pass++) {
@@ -989,6 +990,7 @@ ne_status viewsEnqueue(ne_views* vw) {
     pa.defer_in = vw->d_dq + in;
     pa.defer_out = vw->d_dq + out;
     pa.defer_at = pass == passes - 1 ? -1 : pass;
+    pa.defer_half = vw->tune.split_half;
     pa.views = vw->d_vd;
     NE_CUDA(cudaMemsetAsync(vw->d_dcount + out, 0, sizeof(uint32_t), ctx->stream), "cudaMemsetAsync");
     NE_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync");
@@ -2303,7 +2305,7 @@ void ne_views_destroy(ne_views* vw) {
 ne_status ne_views_set_tuning(ne_views* vw, const ne_views_tuning* t) {
   if (!vw || !t || t->fetch < 32 || t->fetch > 4096 || t->fetch % 32 || t->blocks_per_sm < 0 ||
       t->blocks_per_sm > 64 || t->order < 0 || t->order > 2 || t->graph < 0 || t->graph > 1 || t->split_passes < 0 ||
-      t->split_passes > 64)
+      t->split_passes > 64 || t->split_half < 0 || t->split_half > 1)
     return NE_ERR_INVALID_ARG;
   ne_context* ctx = vw->sc->ctx;
   NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
@@ -2367,7 +2369,8 @@ ne_status ne_views_autotune(ne_views* vw, int repeats, ne_views_tuning* best, do
   const uint32_t fetches[2] = {32, 128};
   const int bpss[1] = {fit};
   const int orders[2] = {1, 2};
-  const int passess[3] = {1, 4, 8};
+  // (passes, by half bounce): one pass, by bounce, by half bounce
+  const int passess[5][2] = {{1, 0}, {4, 0}, {8, 0}, {12, 1}, {16, 1}};
   struct Trial {
     ne_views_tuning t;
     double ms;
@@ -2377,8 +2380,8 @@ ne_status ne_views_autotune(ne_views* vw, int repeats, ne_views_tuning* best, do
   for (uint32_t f : fetches)
     for (int b : bpss)
       for (int o : orders)
-        for (int sp : passess) {
-        ne_views_tuning t = {f, b, o, 1, sp};
+        for (const auto& sp : passess) {
+        ne_views_tuning t = {f, b, o, 1, sp[0], sp[1]};
         ne_status st = ne_views_set_tuning(vw, &t);
         if (st) return st;
         ne_views_stats s;

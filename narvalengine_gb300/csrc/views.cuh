@@ -37,6 +37,7 @@ struct ViewArgs {
   unsigned long long* t_done;   // per view: global timer (ns) when its last path finished
   unsigned long long* t_start;  // global timer when the first warp started
   const DeferQueue* defer_out;  // split batches: queue of paths deferred at their first event
+  int defer_half;               // 1: deferral points every half bounce
 };
 
 // Index of the view owning path `idx` (views sorted by path_begin).
@@ -55,7 +56,7 @@ __global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_views(const __grid
                                                                     const ViewArgs a,
                                                                     unsigned long long* __restrict__ counter,
                                                                     uint32_t* err) {
-  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, nullptr, a.defer_out, 0ull, false, 0, 0};
+  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, nullptr, a.defer_out, 0ull, false, 0, a.defer_half};
   const int lane = threadIdx.x & 31;
   if (threadIdx.x == 0 && blockIdx.x == 0) atomicMin(a.t_start, globalTimer());
   for (;;) {

@@ -31,7 +31,8 @@ def test_views_errors(env):
     assert lib.ne_views_create(scene._h, bad, 1, C.byref(p), C.byref(h)) == _abi.NE_ERR_INVALID_ARG
     assert lib.ne_views_create(scene._h, bad, 0, C.byref(p), C.byref(h)) == _abi.NE_ERR_INVALID_ARG
     vb = ne.Views(scene, [(cam, 16, 16, 1)], seed=1)
-    for t in [dict(fetch=16), dict(fetch=48), dict(order=3), dict(split_passes=65), dict(blocks_per_sm=65)]:
+    for t in [dict(fetch=16), dict(fetch=48), dict(order=3), dict(split_passes=65), dict(blocks_per_sm=65),
+              dict(split_half=2)]:
         with pytest.raises(ne.NarvalError):
             vb.set_tuning(**t)
     with pytest.raises(ne.NarvalError):

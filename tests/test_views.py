@@ -68,8 +68,11 @@ def test_tunings_do_not_change_images(batch):
     vb.render()
     ref = [vb.image(v) for v in range(len(views))]
     for fetch, bps, order, graph, sp in [(128, 0, 1, True, 0), (64, 2, 2, True, 1), (32, 1, 1, False, 4),
-                                         (32, 0, 2, True, 8), (128, 0, 0, False, 2)]:
-        vb.set_tuning(fetch=fetch, blocks_per_sm=bps, order=order, graph=graph, split_passes=sp)
+                                         (32, 0, 2, True, 8), (128, 0, 0, False, 2), (32, 0, 1, True, -12),
+                                         (64, 0, 2, False, -5)]:
+        # negative: that many passes with deferral points every half bounce
+        vb.set_tuning(fetch=fetch, blocks_per_sm=bps, order=order, graph=graph, split_passes=abs(sp),
+                      split_half=int(sp < 0))
         st = vb.render()
         for v in range(len(views)):
             assert np.array_equal(vb.image(v), ref[v]), (fetch, bps, order, graph, sp, v)
