@@ -170,6 +170,20 @@ struct Sampler {
     dim++;
     return r;
   }
+  // random() with the block computed inline: for the tracking loops, which draw most often
+  // (elsewhere the out-of-line block keeps the kernel small).
+  NE_D float randomInline() {
+    uint32_t b = dim >> 2;
+    if (b != blk) {
+      nerng::Block r = nerng::philox4x32_10(b, key.sample, key.pixel, key.stream, key.seed_lo, key.seed_hi);
+      w0 = r.w[0]; w1 = r.w[1]; w2 = r.w[2]; w3 = r.w[3];
+      blk = b;
+    }
+    uint32_t s = dim & 3u;
+    dim++;
+    uint32_t w = (s == 0) ? w0 : (s == 1) ? w1 : (s == 2) ? w2 : w3;
+    return nerng::word_to_u01(w);
+  }
   // The next draw, without consuming it.
   NE_D float peek() {
     uint32_t b = dim >> 2;
@@ -866,7 +880,7 @@ NE_NI V3 gridTr(Ctx<K>& c, const DMedium& M, Ray incoming, Hit isect) {
   float mu = M.mu;
   float Tr = 1, t = isect.tNear;
   for (int step = 0; step < kMaxTrackSteps; step++) {
-    t -= (nefm::log1m_draw(c.S.random()) * invMax) / mu;
+    t -= (nefm::log1m_draw(c.S.randomInline()) * invMax) / mu;
     if (t >= isect.tFar) break;
     float density = sampleAt(c, M, incoming, t);
     float x = density * invMax;
@@ -891,7 +905,7 @@ NE_D V3 gridSample(Ctx<K>& c, const DMedium& M, Ray incoming, Ray& scattered, co
   float mu = M.mu;
   float t = isect.tNear;
   for (int step = 0; step < kMaxTrackSteps; step++) {
-    float r = c.S.random();
+    float r = c.S.randomInline();
     float sampledDist = (nefm::log1m_draw(r) * invMax) / mu;
     t -= sampledDist;
     if (t >= isect.tFar) {
@@ -899,7 +913,7 @@ NE_D V3 gridSample(Ctx<K>& c, const DMedium& M, Ray incoming, Ray& scattered, co
       break;
     }
     float density = sampleAt(c, M, incoming, t);
-    float ra = c.S.random();
+    float ra = c.S.randomInline();
     if (density * invMax > ra) {
       scattered.o = incoming.at(t);
       const DMaterial& m = c.s.materials[c.s.prims[isect.prim].material];
