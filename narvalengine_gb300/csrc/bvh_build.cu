@@ -8,14 +8,17 @@
 // triangles are hit at exactly the same distance (the traversal order decides those).
 //
 // The build runs level by level. Each level's tasks (contiguous ranges of the primitive order)
-// get one CTA each in two kernels:
+// of up to 65536 triangles get one CTA each in two kernels:
 //  * k_sah_bin: node bounds and centroid bounds (block reduction), then 32 bins per axis over the
 //    centroid bounds (shared-memory atomics on order-preserving float keys), then the split of
 //    least surface-area cost A_L N_L + A_R N_R; a range of at most four triangles becomes a
 //    leaf; no split with both sides non-empty, or depth 36 and beyond, gives the median split.
 //  * k_sah_partition: stable partition of the range by the chosen split (block scans of the
 //    side flags), through a scratch array.
-// The host reads each level's results back, numbers the nodes and issues the next level; at
+// Larger ranges (the first levels) are cut into segments of 16384 triangles, one CTA each, that
+// combine their bounds and bins through global atomics (k_wide_*); one thread per range then
+// picks the split, and the segments partition at offsets from a per-range prefix of their left
+// counts. The host reads each level's results back, numbers the nodes and issues the next level; at
 // the end it lays the nodes out depth first. Every step is deterministic (integer counts,
 // min/max, stable partitions), so a scene always gets the same tree.
 #include <cuda_runtime.h>
@@ -38,8 +41,15 @@ constexpr int kMaxLevels = 64;
 constexpr int kThreads = 1024;  // most threads a task's CTA has (levels with few, large tasks)
 
 struct Task {
-  uint32_t begin, end, depth, pad;
+  uint32_t begin, end, depth;
+  uint32_t wide;  // 1: binned and partitioned by several CTAs (the k_wide_* kernels)
 };
+// One CTA's share of a wide task: [begin, end) of the primitive order.
+struct Segment {
+  uint32_t task, wide, begin, end;
+};
+constexpr uint32_t kWideMin = 65536;   // tasks of more triangles use several CTAs
+constexpr uint32_t kSegment = 16384;   // triangles per CTA of a wide task
 struct TaskResult {
   float mn[3], mx[3];
   int32_t axis;      // -1: median split
@@ -98,12 +108,78 @@ __device__ float blockReduce(float v, int op, float* scratch) {
   return r;
 }
 
+// The least-cost binned split (A_L N_L + A_R N_R over the 31 split planes of each axis with a
+// non-zero centroid extent) from bins laid out [axis][bin][xyz] (min/max keys) and [axis][bin]
+// (counts); fills axis, split, nLeft, cmin, scale and the children's bounds of `r`, or leaves
+// r.axis = -1 when no split has both sides non-empty.
+__device__ void evalSah(const uint32_t* bminp, const uint32_t* bmaxp, const uint32_t* bcntp, const float* cmn,
+                        const float* scale, TaskResult& r) {
+  const float inf = __int_as_float(0x7f800000);
+  auto bmin = [&](int a, int b, int k) { return funkey(bminp[(a * kBins + b) * 3 + k]); };
+  auto bmax = [&](int a, int b, int k) { return funkey(bmaxp[(a * kBins + b) * 3 + k]); };
+  auto bcnt = [&](int a, int b) { return bcntp[a * kBins + b]; };
+  float best = inf;
+  for (int a = 0; a < 3; a++) {
+    if (scale[a] == 0.0f) continue;
+    // right-hand sweep: bounds and counts of bins [s, kBins)
+    float rArea[kBins];
+    uint32_t rCnt[kBins];
+    float rmn[3] = {inf, inf, inf}, rmx[3] = {-inf, -inf, -inf};
+    uint32_t rc = 0;
+    for (int b = kBins - 1; b >= 0; b--) {
+      if (bcnt(a, b)) {
+        for (int k = 0; k < 3; k++) {
+          rmn[k] = fminf(rmn[k], bmin(a, b, k));
+          rmx[k] = fmaxf(rmx[k], bmax(a, b, k));
+        }
+        rc += bcnt(a, b);
+      }
+      rArea[b] = rc ? area(rmn, rmx) : 0.0f;
+      rCnt[b] = rc;
+    }
+    float lmn[3] = {inf, inf, inf}, lmx[3] = {-inf, -inf, -inf};
+    uint32_t lc = 0;
+    for (int sp = 1; sp < kBins; sp++) {
+      int b = sp - 1;
+      if (bcnt(a, b)) {
+        for (int k = 0; k < 3; k++) {
+          lmn[k] = fminf(lmn[k], bmin(a, b, k));
+          lmx[k] = fmaxf(lmx[k], bmax(a, b, k));
+        }
+        lc += bcnt(a, b);
+      }
+      if (lc == 0 || rCnt[sp] == 0) continue;
+      float cost = area(lmn, lmx) * (float)lc + rArea[sp] * (float)rCnt[sp];
+      if (cost < best) {
+        best = cost;
+        r.axis = a;
+        r.split = (uint32_t)sp;
+        r.nLeft = lc;
+        r.cmin = cmn[a];
+        r.scale = scale[a];
+        for (int k = 0; k < 3; k++) { r.cb[0][k] = lmn[k]; r.cb[0][3 + k] = lmx[k]; }
+      }
+    }
+  }
+  if (r.axis >= 0) {  // the right child's bounds: bins [split, kBins) of the chosen axis
+    float rmn[3] = {inf, inf, inf}, rmx[3] = {-inf, -inf, -inf};
+    for (int b = (int)r.split; b < kBins; b++)
+      if (bcnt(r.axis, b))
+        for (int k = 0; k < 3; k++) {
+          rmn[k] = fminf(rmn[k], bmin(r.axis, b, k));
+          rmx[k] = fmaxf(rmx[k], bmax(r.axis, b, k));
+        }
+    for (int k = 0; k < 3; k++) { r.cb[1][k] = rmn[k]; r.cb[1][3 + k] = rmx[k]; }
+  }
+}
+
 __global__ void __launch_bounds__(kThreads) k_sah_bin(const Task* __restrict__ tasks, const float4* __restrict__ lo,
                                                      const float4* __restrict__ hi, const float4* __restrict__ cen,
                                                      const uint32_t* __restrict__ order, TaskResult* __restrict__ res) {
   __shared__ float scratch[kThreads / 32];
   __shared__ uint32_t bmin[3][kBins][3], bmax[3][kBins][3], bcnt[3][kBins];
   const Task t = tasks[blockIdx.x];
+  if (t.wide) return;  // k_wide_* handle it
   const uint32_t count = t.end - t.begin;
   const float inf = __int_as_float(0x7f800000);
   float mn[3] = {inf, inf, inf}, mx[3] = {-inf, -inf, -inf}, cmn[3] = {inf, inf, inf}, cmx[3] = {-inf, -inf, -inf};
@@ -160,59 +236,7 @@ __global__ void __launch_bounds__(kThreads) k_sah_bin(const Task* __restrict__ t
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    float best = inf;
-    for (int a = 0; a < 3; a++) {
-      if (scale[a] == 0.0f) continue;
-      // right-hand sweep: bounds and counts of bins [s, kBins)
-      float rArea[kBins];
-      uint32_t rCnt[kBins];
-      float rmn[3] = {inf, inf, inf}, rmx[3] = {-inf, -inf, -inf};
-      uint32_t rc = 0;
-      for (int b = kBins - 1; b >= 0; b--) {
-        if (bcnt[a][b]) {
-          for (int k = 0; k < 3; k++) {
-            rmn[k] = fminf(rmn[k], funkey(bmin[a][b][k]));
-            rmx[k] = fmaxf(rmx[k], funkey(bmax[a][b][k]));
-          }
-          rc += bcnt[a][b];
-        }
-        rArea[b] = rc ? area(rmn, rmx) : 0.0f;
-        rCnt[b] = rc;
-      }
-      float lmn[3] = {inf, inf, inf}, lmx[3] = {-inf, -inf, -inf};
-      uint32_t lc = 0;
-      for (int s = 1; s < kBins; s++) {
-        int b = s - 1;
-        if (bcnt[a][b]) {
-          for (int k = 0; k < 3; k++) {
-            lmn[k] = fminf(lmn[k], funkey(bmin[a][b][k]));
-            lmx[k] = fmaxf(lmx[k], funkey(bmax[a][b][k]));
-          }
-          lc += bcnt[a][b];
-        }
-        if (lc == 0 || rCnt[s] == 0) continue;
-        float cost = area(lmn, lmx) * (float)lc + rArea[s] * (float)rCnt[s];
-        if (cost < best) {
-          best = cost;
-          r.axis = a;
-          r.split = (uint32_t)s;
-          r.nLeft = lc;
-          r.cmin = cmn[a];
-          r.scale = scale[a];
-          for (int k = 0; k < 3; k++) { r.cb[0][k] = lmn[k]; r.cb[0][3 + k] = lmx[k]; }
-        }
-      }
-    }
-    if (r.axis >= 0) {  // the right child's bounds: bins [split, kBins) of the chosen axis
-      float rmn[3] = {inf, inf, inf}, rmx[3] = {-inf, -inf, -inf};
-      for (int b = (int)r.split; b < kBins; b++)
-        if (bcnt[r.axis][b])
-          for (int k = 0; k < 3; k++) {
-            rmn[k] = fminf(rmn[k], funkey(bmin[r.axis][b][k]));
-            rmx[k] = fmaxf(rmx[k], funkey(bmax[r.axis][b][k]));
-          }
-      for (int k = 0; k < 3; k++) { r.cb[1][k] = rmn[k]; r.cb[1][3 + k] = rmx[k]; }
-    }
+    evalSah(&bmin[0][0][0], &bmax[0][0][0], &bcnt[0][0], cmn, scale, r);
     res[blockIdx.x] = r;
   }
 }
@@ -226,6 +250,7 @@ __global__ void __launch_bounds__(kThreads) k_sah_partition(const Task* __restri
   __shared__ uint32_t warpLeft[kThreads / 32];
   __shared__ uint32_t run[2];
   const Task t = tasks[blockIdx.x];
+  if (t.wide) return;  // k_wide_* handle it
   const TaskResult r = res[blockIdx.x];
   if (r.leaf) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
@@ -275,6 +300,223 @@ __global__ void __launch_bounds__(kThreads) k_sah_partition(const Task* __restri
   for (uint32_t i = t.begin + threadIdx.x; i < t.end; i += blockDim.x) order[i] = tmp[i];
 }
 
+// ---- wide tasks: several CTAs per task (the first levels, with few large ranges)
+// Per wide task w: acc[w] = 12 keys (node min xyz, node max xyz, centroid min xyz, centroid
+// max xyz) and bins gb[w] = min keys [3][kBins][3], max keys [3][kBins][3], counts [3][kBins].
+constexpr int kBinWords = 3 * kBins * 3 * 2 + 3 * kBins;
+
+__global__ void k_wide_init(uint32_t nwide, uint32_t* __restrict__ acc, uint32_t* __restrict__ gb) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nwide * 12; i += gridDim.x * blockDim.x)
+    acc[i] = ((i % 12) < 3 || ((i % 12) >= 6 && (i % 12) < 9)) ? 0xffffffffu : 0u;  // min keys start high
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nwide * kBinWords; i += gridDim.x * blockDim.x)
+    gb[i] = (i % kBinWords) < 3 * kBins * 3 ? 0xffffffffu : 0u;
+}
+
+__global__ void __launch_bounds__(kThreads) k_wide_bounds(const Segment* __restrict__ segs,
+                                                         const float4* __restrict__ lo, const float4* __restrict__ hi,
+                                                         const float4* __restrict__ cen,
+                                                         const uint32_t* __restrict__ order, uint32_t* __restrict__ acc) {
+  __shared__ float scratch[kThreads / 32];
+  const Segment g = segs[blockIdx.x];
+  const float inf = __int_as_float(0x7f800000);
+  float v[12] = {inf, inf, inf, -inf, -inf, -inf, inf, inf, inf, -inf, -inf, -inf};
+  for (uint32_t i = g.begin + threadIdx.x; i < g.end; i += blockDim.x) {
+    uint32_t p = order[i];
+    float4 a = lo[p], b = hi[p], c = cen[p];
+    v[0] = fminf(v[0], a.x); v[1] = fminf(v[1], a.y); v[2] = fminf(v[2], a.z);
+    v[3] = fmaxf(v[3], b.x); v[4] = fmaxf(v[4], b.y); v[5] = fmaxf(v[5], b.z);
+    v[6] = fminf(v[6], c.x); v[7] = fminf(v[7], c.y); v[8] = fminf(v[8], c.z);
+    v[9] = fmaxf(v[9], c.x); v[10] = fmaxf(v[10], c.y); v[11] = fmaxf(v[11], c.z);
+  }
+  for (int k = 0; k < 12; k++) {
+    bool isMax = (k >= 3 && k < 6) || k >= 9;
+    float r = blockReduce(v[k], isMax ? 1 : 0, scratch);
+    if (threadIdx.x == 0) {
+      if (isMax) atomicMax(&acc[g.wide * 12 + k], fkey(r));
+      else atomicMin(&acc[g.wide * 12 + k], fkey(r));
+    }
+  }
+}
+
+__device__ void wideScale(const uint32_t* acc, float* cmn, float* scale) {
+  for (int a = 0; a < 3; a++) {
+    cmn[a] = funkey(acc[6 + a]);
+    float ext = funkey(acc[9 + a]) - cmn[a];
+    scale[a] = ext > 0.0f ? (float)kBins / ext : 0.0f;
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_wide_bin(const Segment* __restrict__ segs, const float4* __restrict__ lo,
+                                                      const float4* __restrict__ hi, const float4* __restrict__ cen,
+                                                      const uint32_t* __restrict__ order,
+                                                      const uint32_t* __restrict__ acc, uint32_t* __restrict__ gb) {
+  __shared__ uint32_t bins[kBinWords];
+  const Segment g = segs[blockIdx.x];
+  float cmn[3], scale[3];
+  wideScale(acc + g.wide * 12, cmn, scale);
+  for (int j = threadIdx.x; j < kBinWords; j += blockDim.x) bins[j] = j < 3 * kBins * 3 ? 0xffffffffu : 0u;
+  __syncthreads();
+  uint32_t* bmin = bins;
+  uint32_t* bmax = bins + 3 * kBins * 3;
+  uint32_t* bcnt = bins + 2 * 3 * kBins * 3;
+  for (uint32_t i = g.begin + threadIdx.x; i < g.end; i += blockDim.x) {
+    uint32_t p = order[i];
+    float4 a4 = lo[p], b4 = hi[p], c4 = cen[p];
+    const float pl[3] = {a4.x, a4.y, a4.z}, ph[3] = {b4.x, b4.y, b4.z}, pc[3] = {c4.x, c4.y, c4.z};
+    for (int a = 0; a < 3; a++) {
+      if (scale[a] == 0.0f) continue;
+      int b = binOf(pc[a], cmn[a], scale[a]);
+      for (int k = 0; k < 3; k++) {
+        atomicMin(&bmin[(a * kBins + b) * 3 + k], fkey(pl[k]));
+        atomicMax(&bmax[(a * kBins + b) * 3 + k], fkey(ph[k]));
+      }
+      atomicAdd(&bcnt[a * kBins + b], 1u);
+    }
+  }
+  __syncthreads();
+  uint32_t* out = gb + (size_t)g.wide * kBinWords;
+  for (int j = threadIdx.x; j < 3 * kBins; j += blockDim.x) {
+    if (!bcnt[j]) continue;
+    for (int k = 0; k < 3; k++) {
+      atomicMin(&out[j * 3 + k], bmin[j * 3 + k]);
+      atomicMax(&out[3 * kBins * 3 + j * 3 + k], bmax[j * 3 + k]);
+    }
+    atomicAdd(&out[2 * 3 * kBins * 3 + j], bcnt[j]);
+  }
+}
+
+// One thread per wide task: its node bounds and split, written where k_sah_bin would.
+__global__ void k_wide_sah(uint32_t nwide, const uint32_t* __restrict__ taskOf, const Task* __restrict__ tasks,
+                           const uint32_t* __restrict__ acc, const uint32_t* __restrict__ gb,
+                           TaskResult* __restrict__ res) {
+  uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= nwide) return;
+  const uint32_t ti = taskOf[w];
+  const Task t = tasks[ti];
+  const uint32_t* a = acc + w * 12;
+  TaskResult r;
+  for (int k = 0; k < 3; k++) { r.mn[k] = funkey(a[k]); r.mx[k] = funkey(a[3 + k]); }
+  r.axis = -1;
+  r.split = 0;
+  r.nLeft = (t.end - t.begin) / 2;
+  r.leaf = 0;
+  r.cmin = 0.0f;
+  r.scale = 0.0f;
+  float cmn[3], scale[3];
+  wideScale(a, cmn, scale);
+  const uint32_t* b = gb + (size_t)w * kBinWords;
+  evalSah(b, b + 3 * kBins * 3, b + 2 * 3 * kBins * 3, cmn, scale, r);
+  res[ti] = r;
+}
+
+// Left count of each segment under its task's split.
+__global__ void __launch_bounds__(kThreads) k_wide_count(const Segment* __restrict__ segs, const Task* __restrict__ tasks,
+                                                        const TaskResult* __restrict__ res,
+                                                        const float4* __restrict__ cen,
+                                                        const uint32_t* __restrict__ order, uint32_t* __restrict__ segLeft) {
+  __shared__ uint32_t total;
+  const Segment g = segs[blockIdx.x];
+  const TaskResult r = res[g.task];
+  const uint32_t tBegin = tasks[g.task].begin;
+  if (threadIdx.x == 0) total = 0;
+  __syncthreads();
+  uint32_t mine = 0;
+  for (uint32_t i = g.begin + threadIdx.x; i < g.end; i += blockDim.x) {
+    bool left;
+    if (r.axis < 0) {
+      left = (i - tBegin) < r.nLeft;
+    } else {
+      float4 c = cen[order[i]];
+      float v = r.axis == 0 ? c.x : (r.axis == 1 ? c.y : c.z);
+      left = binOf(v, r.cmin, r.scale) < (int)r.split;
+    }
+    mine += left;
+  }
+  for (int o = 16; o > 0; o >>= 1) mine += __shfl_xor_sync(0xffffffffu, mine, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(&total, mine);
+  __syncthreads();
+  if (threadIdx.x == 0) segLeft[blockIdx.x] = total;
+}
+
+// Per wide task (one thread each): exclusive prefix of its segments' left counts; a total that
+// differs from the split's raises *bad.
+__global__ void k_wide_offsets(uint32_t nwide, const uint32_t* __restrict__ segFirst, const uint32_t* __restrict__ taskOf,
+                               const TaskResult* __restrict__ res, const uint32_t* __restrict__ segLeft,
+                               uint32_t* __restrict__ segOff, uint32_t* __restrict__ bad) {
+  uint32_t w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= nwide) return;
+  uint32_t run = 0;
+  for (uint32_t s = segFirst[w]; s < segFirst[w + 1]; s++) {
+    segOff[s] = run;
+    run += segLeft[s];
+  }
+  if (run != res[taskOf[w]].nLeft) atomicOr(bad, 1u);
+}
+
+// Stable partition of one segment into tmp at its offsets within the task, then nothing else:
+// k_wide_copy moves the task's range back once every segment has been written.
+__global__ void __launch_bounds__(kThreads) k_wide_scatter(const Segment* __restrict__ segs, const Task* __restrict__ tasks,
+                                                          const TaskResult* __restrict__ res,
+                                                          const float4* __restrict__ cen,
+                                                          const uint32_t* __restrict__ order,
+                                                          const uint32_t* __restrict__ segOff, uint32_t* __restrict__ tmp) {
+  __shared__ uint32_t warpLeft[kThreads / 32];
+  __shared__ uint32_t run[2];
+  const Segment g = segs[blockIdx.x];
+  const Task t = tasks[g.task];
+  const TaskResult r = res[g.task];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  if (threadIdx.x == 0) {
+    run[0] = segOff[blockIdx.x];                       // lefts of the task before this segment
+    run[1] = (g.begin - t.begin) - segOff[blockIdx.x]; // rights before it
+  }
+  __syncthreads();
+  for (uint32_t base = g.begin; base < g.end; base += blockDim.x) {
+    uint32_t i = base + threadIdx.x;
+    bool valid = i < g.end;
+    uint32_t p = valid ? order[i] : 0;
+    bool left = false;
+    if (valid) {
+      if (r.axis < 0) {
+        left = (i - t.begin) < r.nLeft;
+      } else {
+        float4 c = cen[p];
+        float v = r.axis == 0 ? c.x : (r.axis == 1 ? c.y : c.z);
+        left = binOf(v, r.cmin, r.scale) < (int)r.split;
+      }
+    }
+    uint32_t ball = __ballot_sync(0xffffffffu, left);
+    uint32_t rank = __popc(ball & ((1u << lane) - 1u));
+    if (lane == 0) warpLeft[warp] = __popc(ball);
+    __syncthreads();
+    uint32_t before = 0, total = 0;
+    for (int w = 0; w < nwarps; w++) {
+      if (w < warp) before += warpLeft[w];
+      total += warpLeft[w];
+    }
+    if (valid) {
+      uint32_t leftBefore = before + rank;
+      uint32_t rightBefore = threadIdx.x - leftBefore;
+      uint32_t dest = left ? t.begin + run[0] + leftBefore : t.begin + r.nLeft + run[1] + rightBefore;
+      if (left ? (run[0] + leftBefore < r.nLeft) : (dest < t.end)) tmp[dest] = p;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      uint32_t chunk = min((uint32_t)blockDim.x, g.end - base);
+      run[0] += total;
+      run[1] += chunk - total;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void k_wide_copy(const Segment* __restrict__ segs, const uint32_t* __restrict__ tmp,
+                            uint32_t* __restrict__ order, const uint32_t* __restrict__ bad) {
+  if (*bad) return;  // leave the order as it was: the build fails
+  const Segment g = segs[blockIdx.x];
+  for (uint32_t i = g.begin + threadIdx.x; i < g.end; i += blockDim.x) order[i] = tmp[i];
+}
+
 template <class T>
 struct DeviceArray {
   T* p = nullptr;
@@ -302,22 +544,54 @@ cudaError_t buildSahBvh(cudaStream_t st, const DPrim* prims, uint32_t first, uin
   DeviceArray<Task> dTasks;
   DeviceArray<TaskResult> dRes;
   DeviceArray<uint32_t> dBad;
+  // wide tasks: at most n / kWideMin per level, with at most n / kSegment + that many segments
+  const size_t maxWide = n / kWideMin + 2, maxSegs = n / kSegment + maxWide;
+  DeviceArray<Segment> dSegs;
+  DeviceArray<uint32_t> dTaskOf, dSegFirst, dSegLeft, dSegOff, dAcc, dGb;
   cudaError_t e;
   if ((e = lo.alloc(n)) || (e = hi.alloc(n)) || (e = cen.alloc(n)) || (e = order.alloc(n)) || (e = tmp.alloc(n)) ||
-      (e = dTasks.alloc(n)) || (e = dRes.alloc(n)) || (e = dBad.alloc(1)))
+      (e = dTasks.alloc(n)) || (e = dRes.alloc(n)) || (e = dBad.alloc(1)) || (e = dSegs.alloc(maxSegs)) ||
+      (e = dTaskOf.alloc(maxWide)) || (e = dSegFirst.alloc(maxWide + 1)) || (e = dSegLeft.alloc(maxSegs)) ||
+      (e = dSegOff.alloc(maxSegs)) || (e = dAcc.alloc(maxWide * 12)) || (e = dGb.alloc(maxWide * kBinWords)))
     return e;
   if ((e = cudaMemsetAsync(dBad.p, 0, sizeof(uint32_t), st))) return e;
   int blocks = (int)std::min<uint32_t>((n + 255) / 256, 4096u);
   k_prim_bounds<<<blocks, 256, 0, st>>>(prims, first, n, lo.p, hi.p, cen.p, order.p);
   if ((e = cudaGetLastError())) return e;
   std::vector<BNode> nodes(1);
-  std::vector<Task> tasks = {Task{0, n, 0, 0}};
+  std::vector<Task> tasks = {Task{0, n, 0, 0}};  // wide flags set per level
   std::vector<int32_t> ids = {0};
   std::vector<TaskResult> res;
   int level = 0;
   for (; level < kMaxLevels && !tasks.empty(); level++) {
     const uint32_t nt = (uint32_t)tasks.size();
+    // large ranges are binned and partitioned by several CTAs (segments of kSegment triangles)
+    std::vector<uint32_t> taskOf, segFirst;
+    std::vector<Segment> segs;
+    for (uint32_t k = 0; k < nt; k++) {
+      Task& t = tasks[k];
+      t.wide = (t.end - t.begin > kWideMin && t.depth < kMedianDepth) ? 1u : 0u;
+      if (!t.wide) continue;
+      const uint32_t w = (uint32_t)taskOf.size();
+      taskOf.push_back(k);
+      segFirst.push_back((uint32_t)segs.size());
+      for (uint32_t b = t.begin; b < t.end; b += kSegment) segs.push_back(Segment{k, w, b, std::min(t.end, b + kSegment)});
+    }
+    const uint32_t nwide = (uint32_t)taskOf.size(), nseg = (uint32_t)segs.size();
+    segFirst.push_back(nseg);
     if ((e = cudaMemcpyAsync(dTasks.p, tasks.data(), nt * sizeof(Task), cudaMemcpyHostToDevice, st))) return e;
+    if (nwide) {
+      if ((e = cudaMemcpyAsync(dSegs.p, segs.data(), nseg * sizeof(Segment), cudaMemcpyHostToDevice, st)) ||
+          (e = cudaMemcpyAsync(dTaskOf.p, taskOf.data(), nwide * sizeof(uint32_t), cudaMemcpyHostToDevice, st)) ||
+          (e = cudaMemcpyAsync(dSegFirst.p, segFirst.data(), (nwide + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                               st)))
+        return e;
+      k_wide_init<<<64, 256, 0, st>>>(nwide, dAcc.p, dGb.p);
+      k_wide_bounds<<<nseg, kThreads, 0, st>>>(dSegs.p, lo.p, hi.p, cen.p, order.p, dAcc.p);
+      k_wide_bin<<<nseg, kThreads, 0, st>>>(dSegs.p, lo.p, hi.p, cen.p, order.p, dAcc.p, dGb.p);
+      k_wide_sah<<<(nwide + 31) / 32, 32, 0, st>>>(nwide, dTaskOf.p, dTasks.p, dAcc.p, dGb.p, dRes.p);
+      if ((e = cudaGetLastError())) return e;
+    }
     // CTA size by the level's task count: the first levels hold few tasks of many triangles,
     // the last ones many small tasks
     const int threads = nt <= 2048 ? 1024 : (nt <= 32768 ? 256 : 64);
@@ -325,6 +599,14 @@ cudaError_t buildSahBvh(cudaStream_t st, const DPrim* prims, uint32_t first, uin
     if ((e = cudaGetLastError())) return e;
     k_sah_partition<<<nt, threads, 0, st>>>(dTasks.p, dRes.p, cen.p, order.p, tmp.p, dBad.p);
     if ((e = cudaGetLastError())) return e;
+    if (nwide) {
+      k_wide_count<<<nseg, kThreads, 0, st>>>(dSegs.p, dTasks.p, dRes.p, cen.p, order.p, dSegLeft.p);
+      k_wide_offsets<<<(nwide + 31) / 32, 32, 0, st>>>(nwide, dSegFirst.p, dTaskOf.p, dRes.p, dSegLeft.p, dSegOff.p,
+                                                      dBad.p);
+      k_wide_scatter<<<nseg, kThreads, 0, st>>>(dSegs.p, dTasks.p, dRes.p, cen.p, order.p, dSegOff.p, tmp.p);
+      k_wide_copy<<<nseg, kThreads, 0, st>>>(dSegs.p, tmp.p, order.p, dBad.p);
+      if ((e = cudaGetLastError())) return e;
+    }
     res.resize(nt);
     if ((e = cudaMemcpyAsync(res.data(), dRes.p, nt * sizeof(TaskResult), cudaMemcpyDeviceToHost, st))) return e;
     if ((e = cudaStreamSynchronize(st))) return e;
