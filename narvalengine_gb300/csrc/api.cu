@@ -1184,6 +1184,22 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
     d.scale[0] = sc3.x; d.scale[1] = sc3.y; d.scale[2] = sc3.z;
     d.model = s.model;
     d.collision = s.collision;
+    // InstancedModel::intersect can only return false for a model whose primitives are points
+    // (Point::intersect) and whose light primitives are points or carry a light whose Le is a
+    // non-black constant (every light but a textured environment: Model.cpp:432-434 skips
+    // them); the queries then skip the instance's ray transform too
+    const ne_model& m = D.models[s.model];
+    bool never = true;
+    for (uint32_t k = 0; k < m.prim_count && never; k++) never = D.prims[m.prim_begin + k].type == NE_PRIM_POINT;
+    for (uint32_t k = 0; k < m.light_count && never; k++) {
+      const ne_primitive& lp = D.prims[m.light_begin + k];
+      if (lp.type == NE_PRIM_POINT) continue;
+      const ne_light& L = D.lights[D.materials[lp.material].light];
+      const float* le = L.type == NE_LIGHT_INFINITE ? L.env_radiance : L.le;
+      bool constant = !(L.type == NE_LIGHT_INFINITE && L.env_width > 0);
+      never = constant && (le[0] != 0.0f || le[1] != 0.0f || le[2] != 0.0f);
+    }
+    d.never_hit = never ? 1 : 0;
   }
   // primitives
   std::vector<DPrim> prims(D.n_prims);

@@ -19,7 +19,10 @@ struct DInstance {
   float scale[3];   // getScale(transformToWCS) (utils/Math.h:874-912), for Rectangle::pdf
   uint32_t model;
   int32_t collision;
-  int32_t pad[3];
+  // 1: no ray can hit this instance (its model holds only points and lights whose Le is a
+  // non-black constant, which Model::intersect skips), so scene queries leave it out
+  int32_t never_hit;
+  int32_t pad[2];
 };
 
 enum : int32_t { DPRIM_GRID_MEDIUM = 1 };  // primitive whose material has a GridMedia

@@ -640,7 +640,7 @@ NE_D bool modelIntersect(Ctx<K>& c, uint32_t mi, const Ray& ray, Hit& hit, float
 template <uint32_t K>
 NE_D bool instanceIntersect(Ctx<K>& c, uint32_t ii, const Ray& ray, Hit& hit, float& tMin, float& tMax) {
   const DInstance& in = c.s.instances[ii];
-  if (!in.collision) return false;
+  if (!in.collision || in.never_hit) return false;
   Ray r = transformRay(ray, in.ocs);
   bool did = modelIntersect(c, in.model, r, hit, tMin, tMax);
   if (did) {
