@@ -1222,14 +1222,29 @@ struct LiVars {
 
 // A path deferred at a scattering event in a grid medium, right after the throughput took
 // the medium's sampled albedo: the loop state, the sampler position and the index of the
-// path's radiance slot.
-struct PathState {
+// path's radiance slot. It moves to and from the queues as ten 16-byte words.
+struct alignas(16) PathState {
   LiVars v;
   nerng::PathKey key;
   uint32_t dim;
   uint32_t mode;  // 0: resume inside a medium bounce after sampling, 1: at the top of bounce v.b
   unsigned long long idx;
 };
+static_assert(sizeof(PathState) == 160, "PathState is ten 16-byte words");
+NE_D void storeState(PathState* dst, const PathState& src) {
+  const uint4* s = reinterpret_cast<const uint4*>(&src);
+  uint4* d = reinterpret_cast<uint4*>(dst);
+#pragma unroll
+  for (int i = 0; i < 10; i++) d[i] = s[i];
+}
+NE_D PathState loadState(const PathState* src) {
+  PathState r;
+  const uint4* s = reinterpret_cast<const uint4*>(src);
+  uint4* d = reinterpret_cast<uint4*>(&r);
+#pragma unroll
+  for (int i = 0; i < 10; i++) d[i] = s[i];
+  return r;
+}
 
 // Deferred paths of one pass. With count_hi set, paths deferred right after a free-flight
 // sample are binned by the light their next draw will pick (uniformSampleOneLight's first draw,
@@ -1292,12 +1307,13 @@ NE_D V3 liLoop(Ctx<K>& c, const PathParams& P, LiVars& v, bool resume) {
             cls = (uint32_t)(int)((float)s.n_light_instances * c.S.peek()) & 1u;
           uint32_t slot = cls ? appendSlot(q.count_hi) : appendSlot(q.count);
           if (slot < (cls ? q.cap_hi : q.cap)) {
-            PathState& ps = q.items[(cls ? (size_t)q.cap : 0) + slot];
+            PathState ps;
             ps.v = v;
             ps.key = c.S.key;
             ps.dim = c.S.dim;
             ps.mode = 0;
             ps.idx = c.idx;
+            storeState(&q.items[(cls ? (size_t)q.cap : 0) + slot], ps);
             c.deferred = true;
             return v.L;
           }
@@ -1373,13 +1389,14 @@ NE_D V3 liLoop(Ctx<K>& c, const PathParams& P, LiVars& v, bool resume) {
       const DeferQueue& q = *c.dq;
       uint32_t slot = appendSlot(q.count);
       if (slot < q.cap) {
-        PathState& ps = q.items[slot];
+        PathState ps;
         ps.v = v;
         ps.v.b = b + 1;
         ps.key = c.S.key;
         ps.dim = c.S.dim;
         ps.mode = 1;
         ps.idx = c.idx;
+        storeState(&q.items[slot], ps);
         c.deferred = true;
         return v.L;
       }
