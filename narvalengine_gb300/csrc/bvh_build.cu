@@ -15,6 +15,7 @@
 //    leaf; no split with both sides non-empty, or depth 36 and beyond, gives the median split.
 //  * k_sah_partition: stable partition of the range by the chosen split (block scans of the
 //    side flags), through a scratch array.
+// Levels whose ranges all hold at most 2048 triangles use a warp per range instead (k_sah_*_warp).
 // Larger ranges (the first levels) are cut into segments of 16384 triangles, one CTA each, that
 // combine their bounds and bins through global atomics (k_wide_*); one thread per range then
 // picks the split, and the segments partition at offsets from a per-range prefix of their left
@@ -298,6 +299,136 @@ __global__ void __launch_bounds__(kThreads) k_sah_partition(const Task* __restri
     return;
   }
   for (uint32_t i = t.begin + threadIdx.x; i < t.end; i += blockDim.x) order[i] = tmp[i];
+}
+
+// ---- small tasks: one warp per task (the last levels, with many ranges of a few triangles)
+constexpr int kWarpTasks = 8;          // warps (tasks) per CTA
+constexpr uint32_t kSmallMax = 2048;   // levels whose ranges are all this small use these kernels
+
+__device__ __forceinline__ float warpMin(float v) {
+  for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ float warpMax(float v) {
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+__global__ void __launch_bounds__(32 * kWarpTasks) k_sah_bin_warp(const Task* __restrict__ tasks, uint32_t nt,
+                                                                 const float4* __restrict__ lo,
+                                                                 const float4* __restrict__ hi,
+                                                                 const float4* __restrict__ cen,
+                                                                 const uint32_t* __restrict__ order,
+                                                                 TaskResult* __restrict__ res) {
+  __shared__ uint32_t binsAll[kWarpTasks][3 * kBins * 3 * 2 + 3 * kBins];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t ti = blockIdx.x * kWarpTasks + warp;
+  if (ti >= nt) return;  // the whole warp: no block-wide barrier follows
+  const Task t = tasks[ti];
+  const uint32_t count = t.end - t.begin;
+  const float inf = __int_as_float(0x7f800000);
+  float mn[3] = {inf, inf, inf}, mx[3] = {-inf, -inf, -inf}, cmn[3] = {inf, inf, inf}, cmx[3] = {-inf, -inf, -inf};
+  for (uint32_t i = t.begin + lane; i < t.end; i += 32) {
+    uint32_t p = order[i];
+    float4 a = lo[p], b = hi[p], c = cen[p];
+    mn[0] = fminf(mn[0], a.x); mn[1] = fminf(mn[1], a.y); mn[2] = fminf(mn[2], a.z);
+    mx[0] = fmaxf(mx[0], b.x); mx[1] = fmaxf(mx[1], b.y); mx[2] = fmaxf(mx[2], b.z);
+    cmn[0] = fminf(cmn[0], c.x); cmn[1] = fminf(cmn[1], c.y); cmn[2] = fminf(cmn[2], c.z);
+    cmx[0] = fmaxf(cmx[0], c.x); cmx[1] = fmaxf(cmx[1], c.y); cmx[2] = fmaxf(cmx[2], c.z);
+  }
+  for (int k = 0; k < 3; k++) {
+    mn[k] = warpMin(mn[k]);
+    mx[k] = warpMax(mx[k]);
+    cmn[k] = warpMin(cmn[k]);
+    cmx[k] = warpMax(cmx[k]);
+  }
+  TaskResult r;
+  for (int k = 0; k < 3; k++) { r.mn[k] = mn[k]; r.mx[k] = mx[k]; }
+  r.axis = -1;
+  r.split = 0;
+  r.nLeft = count / 2;
+  r.leaf = count <= kLeafPrims;
+  r.cmin = 0.0f;
+  r.scale = 0.0f;
+  if (r.leaf || t.depth >= kMedianDepth) {
+    if (lane == 0) res[ti] = r;
+    return;
+  }
+  float scale[3];
+  for (int a = 0; a < 3; a++) {
+    float ext = cmx[a] - cmn[a];
+    scale[a] = ext > 0.0f ? (float)kBins / ext : 0.0f;
+  }
+  uint32_t* bins = binsAll[warp];
+  uint32_t* bmin = bins;
+  uint32_t* bmax = bins + 3 * kBins * 3;
+  uint32_t* bcnt = bins + 2 * 3 * kBins * 3;
+  for (int j = lane; j < 3 * kBins * 3 * 2 + 3 * kBins; j += 32) bins[j] = j < 3 * kBins * 3 ? 0xffffffffu : 0u;
+  __syncwarp();
+  for (uint32_t i = t.begin + lane; i < t.end; i += 32) {
+    uint32_t p = order[i];
+    float4 a4 = lo[p], b4 = hi[p], c4 = cen[p];
+    const float pl[3] = {a4.x, a4.y, a4.z}, ph[3] = {b4.x, b4.y, b4.z}, pc[3] = {c4.x, c4.y, c4.z};
+    for (int a = 0; a < 3; a++) {
+      if (scale[a] == 0.0f) continue;
+      int b = binOf(pc[a], cmn[a], scale[a]);
+      for (int k = 0; k < 3; k++) {
+        atomicMin(&bmin[(a * kBins + b) * 3 + k], fkey(pl[k]));
+        atomicMax(&bmax[(a * kBins + b) * 3 + k], fkey(ph[k]));
+      }
+      atomicAdd(&bcnt[a * kBins + b], 1u);
+    }
+  }
+  __syncwarp();
+  if (lane == 0) {
+    evalSah(bmin, bmax, bcnt, cmn, scale, r);
+    res[ti] = r;
+  }
+}
+
+__global__ void __launch_bounds__(32 * kWarpTasks) k_sah_partition_warp(const Task* __restrict__ tasks, uint32_t nt,
+                                                                       const TaskResult* __restrict__ res,
+                                                                       const float4* __restrict__ cen,
+                                                                       uint32_t* __restrict__ order,
+                                                                       uint32_t* __restrict__ tmp,
+                                                                       uint32_t* __restrict__ bad) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t ti = blockIdx.x * kWarpTasks + warp;
+  if (ti >= nt) return;
+  const Task t = tasks[ti];
+  const TaskResult r = res[ti];
+  if (r.leaf) return;
+  uint32_t leftRun = 0, rightRun = 0;
+  for (uint32_t base = t.begin; base < t.end; base += 32) {
+    uint32_t i = base + lane;
+    bool valid = i < t.end;
+    uint32_t p = valid ? order[i] : 0;
+    bool left = false;
+    if (valid) {
+      if (r.axis < 0) {
+        left = (i - t.begin) < r.nLeft;
+      } else {
+        float4 c = cen[p];
+        float v = r.axis == 0 ? c.x : (r.axis == 1 ? c.y : c.z);
+        left = binOf(v, r.cmin, r.scale) < (int)r.split;
+      }
+    }
+    uint32_t ball = __ballot_sync(0xffffffffu, left);
+    uint32_t rank = __popc(ball & ((1u << lane) - 1u));
+    if (valid) {
+      uint32_t dest = left ? t.begin + leftRun + rank : t.begin + r.nLeft + rightRun + ((uint32_t)lane - rank);
+      if (left ? (leftRun + rank < r.nLeft) : (dest < t.end)) tmp[dest] = p;
+    }
+    uint32_t total = __popc(ball);
+    leftRun += total;
+    rightRun += min(32u, t.end - base) - total;
+  }
+  __syncwarp();
+  if (leftRun != r.nLeft) {
+    if (lane == 0) atomicOr(bad, 1u);
+    return;
+  }
+  for (uint32_t i = t.begin + lane; i < t.end; i += 32) order[i] = tmp[i];
 }
 
 // ---- wide tasks: several CTAs per task (the first levels, with few large ranges)
@@ -592,13 +723,24 @@ cudaError_t buildSahBvh(cudaStream_t st, const DPrim* prims, uint32_t first, uin
       k_wide_sah<<<(nwide + 31) / 32, 32, 0, st>>>(nwide, dTaskOf.p, dTasks.p, dAcc.p, dGb.p, dRes.p);
       if ((e = cudaGetLastError())) return e;
     }
-    // CTA size by the level's task count: the first levels hold few tasks of many triangles,
-    // the last ones many small tasks
-    const int threads = nt <= 2048 ? 1024 : (nt <= 32768 ? 256 : 64);
-    k_sah_bin<<<nt, threads, 0, st>>>(dTasks.p, lo.p, hi.p, cen.p, order.p, dRes.p);
-    if ((e = cudaGetLastError())) return e;
-    k_sah_partition<<<nt, threads, 0, st>>>(dTasks.p, dRes.p, cen.p, order.p, tmp.p, dBad.p);
-    if ((e = cudaGetLastError())) return e;
+    uint32_t largest = 0;
+    for (const Task& t : tasks) largest = std::max(largest, t.end - t.begin);
+    if (largest <= kSmallMax) {
+      // only small ranges: a warp each
+      const uint32_t blocks = (nt + kWarpTasks - 1) / kWarpTasks;
+      k_sah_bin_warp<<<blocks, 32 * kWarpTasks, 0, st>>>(dTasks.p, nt, lo.p, hi.p, cen.p, order.p, dRes.p);
+      if ((e = cudaGetLastError())) return e;
+      k_sah_partition_warp<<<blocks, 32 * kWarpTasks, 0, st>>>(dTasks.p, nt, dRes.p, cen.p, order.p, tmp.p, dBad.p);
+      if ((e = cudaGetLastError())) return e;
+    } else {
+      // a CTA per range, sized by the level's task count: the first levels hold few tasks of
+      // many triangles
+      const int threads = nt <= 2048 ? 1024 : (nt <= 32768 ? 256 : 64);
+      k_sah_bin<<<nt, threads, 0, st>>>(dTasks.p, lo.p, hi.p, cen.p, order.p, dRes.p);
+      if ((e = cudaGetLastError())) return e;
+      k_sah_partition<<<nt, threads, 0, st>>>(dTasks.p, dRes.p, cen.p, order.p, tmp.p, dBad.p);
+      if ((e = cudaGetLastError())) return e;
+    }
     if (nwide) {
       k_wide_count<<<nseg, kThreads, 0, st>>>(dSegs.p, dTasks.p, dRes.p, cen.p, order.p, dSegLeft.p);
       k_wide_offsets<<<(nwide + 31) / 32, 32, 0, st>>>(nwide, dSegFirst.p, dTaskOf.p, dRes.p, dSegLeft.p, dSegOff.p,
