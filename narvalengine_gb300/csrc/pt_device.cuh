@@ -1134,6 +1134,7 @@ NE_NI V3 estimateDirect(Ctx<K>& c, const Ray& incoming, const Hit& isect, const 
   V3 f = v3(0, 0, 0);
   const DMaterial& mat = *matOf(s, isect.prim);
   bool surface = !(mat.medium >= 0);
+  bool mediumF = false;  // f holds the phase value for (incoming.d, wo.d)
   if (lightPdf > 0 && !isBlack(Li)) {
     if (surface) {
       f = bsdfEval<K>(mat, incoming.d, wo.d, isect.normal) * fabsf(dot(wo.d, isect.normal));
@@ -1141,6 +1142,7 @@ NE_NI V3 estimateDirect(Ctx<K>& c, const Ray& incoming, const Hit& isect, const 
     } else {
       f = bsdfEval<K>(mat, incoming.d, wo.d, isect.normal);
       scatteringPdf = f.x;
+      mediumF = true;
     }
     if (!isBlack(f)) {
       V3 pointOnLight = samplePointOnSurface<K>(s, light.primitive, isect, lin.wcs, c.S);
@@ -1157,7 +1159,9 @@ NE_NI V3 estimateDirect(Ctx<K>& c, const Ray& incoming, const Hit& isect, const 
     f = f * fabsf(dot(wo.d, isect.normal));
     scatteringPdf = bsdfPdf<K>(mat, incoming.d, wo.d, isect.normal);
   } else {
-    f = bsdfEval<K>(mat, incoming.d, wo.d, isect.normal);
+    // the reference evaluates the phase function at the light sample's direction again here
+    // (VolumetricPathIntegrator.cpp:121-125); the value computed above is the same
+    if (!mediumF) f = bsdfEval<K>(mat, incoming.d, wo.d, isect.normal);
     wo.d = bsdfSample<K>(mat, incoming.d, v3(0, 1, 0), c.S);
     scatteringPdf = f.x;
   }
@@ -1341,8 +1345,10 @@ NE_D V3 liLoop(Ctx<K>& c, const PathParams& P, LiVars& v, bool resume) {
       vT = v.T;
     }
     if (medium) {
+      // VolumeBSDF: eval is (p, p, p) and pdf is p for the same phase value p (BSDF.h:117-142),
+      // so one evaluation gives both
       V3 phaseFr = bsdfEval<K>(*mat, v.incoming.d, v.scattered.d, v.isect.normal);
-      float phasePdf = bsdfPdf<K>(*mat, v.incoming.d, v.scattered.d, v.isect.normal);
+      float phasePdf = phaseFr.x;
       if (isBlack(phaseFr) || phasePdf == 0.f) break;
       V3 lightSample = uniformSampleOneLight(c, v.scattered, v.isect);
       v.T = v.T * (phaseFr / phasePdf);

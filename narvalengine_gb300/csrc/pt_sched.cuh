@@ -242,8 +242,8 @@ NE_NI void transition(Ctx<K>& c, Lane& st, const PathParams& P) {
           break;
         }
         st.T = st.T * st.sampledT;
-        V3 phaseFr = bsdfEval<K>(mat, st.incoming.d, st.scattered.d, st.isect.normal);
-        float phasePdf = bsdfPdf<K>(mat, st.incoming.d, st.scattered.d, st.isect.normal);
+        V3 phaseFr = bsdfEval<K>(mat, st.incoming.d, st.scattered.d, st.isect.normal);  // VolumeBSDF: (p, p, p)
+        float phasePdf = phaseFr.x;                                                   // and its pdf p
         if (isBlack(phaseFr) || phasePdf == 0.f) { st.pc = PC_DONE; return; }
         st.phaseRatio = phaseFr / phasePdf;
         st.neeD = st.scattered.d;
