@@ -28,6 +28,15 @@ constexpr int kThreads = 128;
 #define NE_PATH_MIN_BLOCKS 7
 #endif
 constexpr int kPathMinBlocks = NE_PATH_MIN_BLOCKS;
+#ifndef NE_MESH_MIN_BLOCKS
+#define NE_MESH_MIN_BLOCKS 10
+#endif
+// Triangle meshes without media (the mesh feature set) run best with more resident warps to
+// hide their instruction-fetch and traversal latency (mesh scene, split by bounce: 7 blocks
+// 169, 10 blocks 176 Mpaths/s).
+__host__ __device__ constexpr int pathMinBlocks(uint32_t K) {
+  return ((K & FT_TRI) && !(K & FT_GRID)) ? NE_MESH_MIN_BLOCKS : kPathMinBlocks;
+}
 
 // Per-view completion accounting of a batch of views (see views.cuh): the path range of
 // every view in launch order, finished-path counts and completion times.
@@ -116,7 +125,7 @@ __device__ __forceinline__ void flushCounters(const Counters& cn, unsigned long 
 }
 
 template <uint32_t K>
-__global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_paths(const __grid_constant__ DScene s, const PathArgs a,
+__global__ void __launch_bounds__(kThreads, pathMinBlocks(K)) k_paths(const __grid_constant__ DScene s, const PathArgs a,
                                                     unsigned long long* __restrict__ counter, uint32_t* err) {
   Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, a.cache, a.defer_out, 0ull, false, a.defer_at,
            a.defer_half};
@@ -162,7 +171,7 @@ __global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_paths(const __grid
 // event of bounce a.defer_at (or running it to the end when that is -1): the same operations
 // and draws as an undivided path.
 template <uint32_t K>
-__global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_resume(const __grid_constant__ DScene s,
+__global__ void __launch_bounds__(kThreads, pathMinBlocks(K)) k_resume(const __grid_constant__ DScene s,
                                                                      const PathArgs a,
                                                                      unsigned long long* __restrict__ counter,
                                                                      uint32_t* err) {
@@ -208,7 +217,7 @@ __global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_resume(const __gri
 // work item at once, together with whichever lanes finish at the same time (coalesced-group
 // atomic), instead of waiting for the longest path of its warp.
 template <uint32_t K>
-__global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_lanes(const __grid_constant__ DScene s, const PathArgs a,
+__global__ void __launch_bounds__(kThreads, pathMinBlocks(K)) k_lanes(const __grid_constant__ DScene s, const PathArgs a,
                                                     unsigned long long* __restrict__ counter, uint32_t* err) {
   namespace cg = cooperative_groups;
   Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, nullptr, nullptr, 0ull, false, -1, 0};
