@@ -31,11 +31,12 @@ constexpr int kPathMinBlocks = NE_PATH_MIN_BLOCKS;
 #ifndef NE_MESH_MIN_BLOCKS
 #define NE_MESH_MIN_BLOCKS 10
 #endif
-// Triangle meshes without media (the mesh feature set) run best with more resident warps to
-// hide their instruction-fetch and traversal latency (mesh scene, split by bounce: 7 blocks
-// 169, 10 blocks 176 Mpaths/s).
+// Triangle meshes run best with more resident warps to hide their instruction-fetch and
+// traversal latency: without media (the mesh feature set) 10 blocks (mesh scene: 7 blocks 178,
+// 10 blocks 188 Mpaths/s), with media (the general set) 8 (views of the medium and the mesh:
+// 7 blocks 66.3, 8 blocks 69.4).
 __host__ __device__ constexpr int pathMinBlocks(uint32_t K) {
-  return ((K & FT_TRI) && !(K & FT_GRID)) ? NE_MESH_MIN_BLOCKS : kPathMinBlocks;
+  return (K & FT_TRI) ? ((K & FT_GRID) ? 8 : NE_MESH_MIN_BLOCKS) : kPathMinBlocks;
 }
 
 // Per-view completion accounting of a batch of views (see views.cuh): the path range of

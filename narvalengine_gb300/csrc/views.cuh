@@ -52,7 +52,7 @@ __device__ __forceinline__ uint32_t findView(const DView* v, uint32_t n, unsigne
 }
 
 template <uint32_t K>
-__global__ void __launch_bounds__(kThreads, kPathMinBlocks) k_views(const __grid_constant__ DScene s,
+__global__ void __launch_bounds__(kThreads, pathMinBlocks(K)) k_views(const __grid_constant__ DScene s,
                                                                     const ViewArgs a,
                                                                     unsigned long long* __restrict__ counter,
                                                                     uint32_t* err) {
