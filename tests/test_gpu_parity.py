@@ -199,7 +199,7 @@ def test_kernels_and_tunings_agree(ne, ctx):
     for kernel, share, bps, passes in [(0, 16, 0, 0), (0, 16, 1, 0), (1, 16, 0, 0), (1, 1, 0, 0), (1, 32, 0, 0),
                                        (1, 8, 1, 0), (2, 16, 0, 0), (2, 16, 1, 0), (3, 16, 0, 2), (3, 16, 1, 3),
                                        (3, 16, 0, 5), (3, 16, 0, 16), (3, 16, 0, -8), (3, 16, 0, -3),
-                                       (3, 16, 0, -64)]:
+                                       (3, 16, 0, -64), (3, 16, 1, -12), (3, 16, 0, 6)]:
         scene.set_tuning(kernel=kernel, track_share=share, blocks_per_sm=bps, split_passes=abs(passes),
                          split_half=int(passes < 0))
         img, stats = scene.render(p)
