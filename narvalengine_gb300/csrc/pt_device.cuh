@@ -1173,7 +1173,11 @@ NE_NI V3 estimateDirect(Ctx<K>& c, const Ray& incoming, const Hit& isect, const 
     Hit lightIsect = emptyHit();
     Ray ray{isect.hitPoint, wo.d};
     V3 Tr = v3(1, 1, 1);
-    bool found = intersectTr(c, ray, lightIsect, &Tr);
+    // intersectTr reports a hit only where its ray reaches a medium: in a scene without media
+    // it draws no random number and returns false, so its walk through every surface on the
+    // ray cannot change the result and is skipped
+    bool found = false;
+    if ((K & (FT_GRID | FT_HOMOG)) && s.n_media > 0) found = intersectTr(c, ray, lightIsect, &Tr);
     V3 Li2 = v3(0, 0, 0);
     if (found) Li2 = lightLi(light);
     if (!isBlack(Li2)) Ld = Ld + (((f * Li2) * Tr) * weight) / scatteringPdf;
