@@ -1201,6 +1201,62 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
     }
     d.never_hit = never ? 1 : 0;
   }
+  // World-space bounds of the primitives whose material has a medium: a walk of intersectTr
+  // whose ray misses all of them can reach no medium. Each primitive's OCS bounds (box corners,
+  // sphere centre +- radius, rectangle corners, triangle vertices) go through the instance's
+  // transform in double precision and are widened by 1e-3 of their extent and position, far
+  // beyond the rounding of the float transforms and of the walk's successive origins.
+  std::vector<float> mediumBoxes;
+  int32_t nMediumBoxes = 0;
+  for (uint32_t i = 0; i < ninst && nMediumBoxes >= 0; i++) {
+    const ne_model& m = D.models[D.instances[i].model];
+    const float* W = D.instances[i].to_wcs;
+    auto addPrim = [&](const ne_primitive& p) {
+      if (p.material < 0 || D.materials[p.material].medium < 0) return;
+      double lo[3], hi[3];
+      for (int a = 0; a < 3; a++) {
+        if (p.type == NE_PRIM_SPHERE) {
+          lo[a] = (double)p.p0[a] - fabs((double)p.radius);
+          hi[a] = (double)p.p0[a] + fabs((double)p.radius);
+        } else {
+          lo[a] = std::min((double)p.p0[a], (double)p.p1[a]);
+          hi[a] = std::max((double)p.p0[a], (double)p.p1[a]);
+          if (p.type == NE_PRIM_TRIANGLE) {
+            lo[a] = std::min(lo[a], (double)p.p2[a]);
+            hi[a] = std::max(hi[a], (double)p.p2[a]);
+          }
+        }
+      }
+      double wlo[3] = {INFINITY, INFINITY, INFINITY}, whi[3] = {-INFINITY, -INFINITY, -INFINITY};
+      for (int corner = 0; corner < 8; corner++) {
+        double q[3] = {(corner & 1) ? hi[0] : lo[0], (corner & 2) ? hi[1] : lo[1], (corner & 4) ? hi[2] : lo[2]};
+        for (int r = 0; r < 3; r++) {
+          double w = (double)W[12 + r];
+          for (int c = 0; c < 3; c++) w += (double)W[c * 4 + r] * q[c];
+          wlo[r] = std::min(wlo[r], w);
+          whi[r] = std::max(whi[r], w);
+        }
+      }
+      bool finite = true;
+      for (int a = 0; a < 3; a++) finite = finite && std::isfinite(wlo[a]) && std::isfinite(whi[a]);
+      if (!finite || p.type == NE_PRIM_POINT) {
+        if (!finite) nMediumBoxes = -1;
+        return;
+      }
+      for (int a = 0; a < 3; a++) {
+        double margin = 1e-3 * ((whi[a] - wlo[a]) + std::max(fabs(wlo[a]), fabs(whi[a]))) + 1e-6;
+        mediumBoxes.push_back((float)(wlo[a] - margin));
+      }
+      for (int a = 0; a < 3; a++) {
+        double margin = 1e-3 * ((whi[a] - wlo[a]) + std::max(fabs(wlo[a]), fabs(whi[a]))) + 1e-6;
+        mediumBoxes.push_back((float)(whi[a] + margin));
+      }
+      if (nMediumBoxes >= 0) nMediumBoxes++;
+    };
+    for (uint32_t k = 0; k < m.prim_count && nMediumBoxes >= 0; k++) addPrim(D.prims[m.prim_begin + k]);
+    for (uint32_t k = 0; k < m.light_count && nMediumBoxes >= 0; k++) addPrim(D.prims[m.light_begin + k]);
+  }
+  if (nMediumBoxes > 64) nMediumBoxes = -1;  // many media: the test would cost more than it saves
   // primitives
   std::vector<DPrim> prims(D.n_prims);
   auto convertPrim = [&](uint32_t i) {
@@ -1385,6 +1441,9 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
   if ((st = upload(sc, D.model_materials, D.n_model_materials, &sc->d.model_materials))) return cleanup(st);
   if ((st = upload(sc, lights.data(), lights.size(), &sc->d.lights))) return cleanup(st);
   if ((st = upload(sc, media.data(), media.size(), &sc->d.media))) return cleanup(st);
+  if (nMediumBoxes > 0 && (st = upload(sc, mediumBoxes.data(), mediumBoxes.size(), &sc->d.medium_boxes)))
+    return cleanup(st);
+  sc->d.n_medium_boxes = nMediumBoxes;
   if (!gridMedia.empty()) {
     std::vector<uint32_t> keys(gridMedia.size(), 0x80000000u);  // the key of 0
     const uint32_t* dkeys = nullptr;

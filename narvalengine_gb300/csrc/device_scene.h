@@ -115,6 +115,10 @@ struct DScene {
   const uint32_t* bvh_prims;  // leaf slot -> primitive index
   uint32_t n_instances, n_light_instances;
   uint32_t n_prims, n_media;
+  // world-space boxes (min xyz, max xyz) bounding every primitive whose material has a medium,
+  // widened against rounding; -1: not known, every ray may reach a medium
+  const float* medium_boxes;
+  int32_t n_medium_boxes;
   DCamera camera;
   int32_t width, height;
 };

@@ -1106,6 +1106,34 @@ NE_D bool intersectTr(Ctx<K>& c, Ray ray, Hit& intersection, V3* Tr) {
   return false;
 }
 
+// False only when the ray's line, from its origin on, misses every medium's world-space box
+// (widened at upload against rounding): intersectTr's walk along the ray can then reach no
+// medium, so it returns false and draws nothing. NaN in the ray narrows nothing and answers
+// true.
+NE_D bool mayReachMedium(const DScene& s, const Ray& r) {
+  if (s.n_medium_boxes < 0) return true;
+  const float o[3] = {r.o.x, r.o.y, r.o.z}, d[3] = {r.d.x, r.d.y, r.d.z};
+  for (int i = 0; i < s.n_medium_boxes; i++) {
+    const float* b = s.medium_boxes + 6 * i;
+    float tNear = 0.0f, tFar = __int_as_float(0x7f800000);
+    bool miss = false;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      const float lo = __ldg(b + a), hi = __ldg(b + 3 + a);
+      if (d[a] == 0.0f) {
+        if (o[a] < lo || o[a] > hi) miss = true;
+      } else {
+        const float t0 = (lo - o[a]) / d[a], t1 = (hi - o[a]) / d[a];
+        const float tn = t0 < t1 ? t0 : t1, tf = t0 < t1 ? t1 : t0;
+        if (tn > tNear) tNear = tn;
+        if (tf < tFar) tFar = tf;
+      }
+    }
+    if (!miss && !(tNear > tFar)) return true;
+  }
+  return false;
+}
+
 // integrators/VolumetricPathIntegrator.cpp:34-72 visibilityTr.
 template <uint32_t K>
 NE_D V3 visibilityTr(Ctx<K>& c, V3 p, V3 lightPoint) {
@@ -1173,11 +1201,13 @@ NE_NI V3 estimateDirect(Ctx<K>& c, const Ray& incoming, const Hit& isect, const 
     Hit lightIsect = emptyHit();
     Ray ray{isect.hitPoint, wo.d};
     V3 Tr = v3(1, 1, 1);
-    // intersectTr reports a hit only where its ray reaches a medium: in a scene without media
-    // it draws no random number and returns false, so its walk through every surface on the
-    // ray cannot change the result and is skipped
+    // intersectTr reports a hit only where its ray reaches a medium: in a scene without media,
+    // or (kernels for meshes with media) for a ray that misses every medium's box, it draws no
+    // random number and returns false, so its walk through every surface on the ray cannot
+    // change the result and is skipped
     bool found = false;
-    if ((K & (FT_GRID | FT_HOMOG)) && s.n_media > 0) found = intersectTr(c, ray, lightIsect, &Tr);
+    if ((K & (FT_GRID | FT_HOMOG)) && s.n_media > 0 && (!(K & FT_TRI) || mayReachMedium(s, ray)))
+      found = intersectTr(c, ray, lightIsect, &Tr);
     V3 Li2 = v3(0, 0, 0);
     if (found) Li2 = lightLi(light);
     if (!isBlack(Li2)) Ld = Ld + (((f * Li2) * Tr) * weight) / scatteringPdf;
