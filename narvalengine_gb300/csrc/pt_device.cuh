@@ -405,9 +405,9 @@ NE_D bool triIntersect(const DScene& s, const DPrim& p, const Ray& r, Hit& h) {
 }
 
 template <uint32_t K>
-NE_D bool primIntersect(Ctx<K>& c, int idx, const Ray& r, Hit& h) {
-  const DPrim& p = c.s.prims[idx];
-  if ((K & K_COUNT) && p.type == NE_PRIM_TRIANGLE) c.c.tests++;
+NE_D bool primIntersect(const DScene& s, Counters& cnt, int idx, const Ray& r, Hit& h) {
+  const DPrim& p = s.prims[idx];
+  if ((K & K_COUNT) && p.type == NE_PRIM_TRIANGLE) cnt.tests++;
   bool hit = false;
   if ((K & FT_SPHERE) && p.type == NE_PRIM_SPHERE) {
     hit = sphereIntersect(p, r, h);
@@ -418,7 +418,7 @@ NE_D bool primIntersect(Ctx<K>& c, int idx, const Ray& r, Hit& h) {
     h.prim = idx;
     return hit;
   } else if ((K & FT_TRI) && p.type == NE_PRIM_TRIANGLE) {
-    hit = triIntersect<K>(c.s, p, r, h);
+    hit = triIntersect<K>(s, p, r, h);
   } else {
     return false;
   }
@@ -428,7 +428,7 @@ NE_D bool primIntersect(Ctx<K>& c, int idx, const Ray& r, Hit& h) {
 
 // primitives/BVH.cpp:108-193 BVH::intersect (near-first stack traversal).
 template <uint32_t K>
-NE_D bool bvhIntersect(Ctx<K>& c, const DModel& m, const Ray& r, Hit& out) {
+NE_D bool bvhIntersect(const DScene& sc, uint32_t* err, Counters& cnt, const DModel& m, const Ray& r, Hit& out) {
   const float inf = __int_as_float(0x7f800000);
   uint32_t stackNode[kBvhStack];
   float stackT[kBvhStack];
@@ -441,8 +441,8 @@ NE_D bool bvhIntersect(Ctx<K>& c, const DModel& m, const Ray& r, Hit& out) {
   bool anyHit = false;
   V3 s = v3((r.d.x < 0.0f) ? 1.0f : -1.0f, (r.d.y < 0.0f) ? 1.0f : -1.0f, (r.d.z < 0.0f) ? 1.0f : -1.0f);
   V3 invD = v3(1.0f / r.d.x, 1.0f / r.d.y, 1.0f / r.d.z);
-  const DNode* nodes = c.s.bvh + m.bvh_node0;
-  const uint32_t* slots = c.s.bvh_prims + m.bvh_slot0;
+  const DNode* nodes = sc.bvh + m.bvh_node0;
+  const uint32_t* slots = sc.bvh_prims + m.bvh_slot0;
   while (sp >= 0) {
     uint32_t ni = stackNode[sp];
     float nearest = stackT[sp];
@@ -450,13 +450,13 @@ NE_D bool bvhIntersect(Ctx<K>& c, const DModel& m, const Ray& r, Hit& out) {
     if (nearest > closest.tNear) continue;
     float4 hi = __ldg(reinterpret_cast<const float4*>(&nodes[ni].hi));
     uint32_t b = __float_as_uint(hi.w);
-    if (K & K_COUNT) c.c.nodes++;
+    if (K & K_COUNT) cnt.nodes++;
     if (b & 0x80000000u) {
       float4 lo = __ldg(reinterpret_cast<const float4*>(&nodes[ni].lo));
       uint32_t start = __float_as_uint(lo.w), count = b & 0x7fffffffu;
       for (uint32_t i = 0; i < count; i++) {
         Hit tmp = emptyHit();
-        bool cur = primIntersect(c, (int)slots[start + i], r, tmp);
+        bool cur = primIntersect<K>(sc, cnt, (int)slots[start + i], r, tmp);
         anyHit = anyHit || cur;
         if (cur && tmp.tNear < closest.tNear) closest = tmp;
       }
@@ -478,20 +478,37 @@ NE_D bool bvhIntersect(Ctx<K>& c, const DModel& m, const Ray& r, Hit& out) {
           closer = c1; other = c0;
           tc = tn1; to = tn0;
         }
-        if (sp + 2 >= kBvhStack) { atomicOr(c.err, ERR_BVH_STACK); break; }
+        if (sp + 2 >= kBvhStack) { atomicOr(err, ERR_BVH_STACK); break; }
         stackNode[++sp] = other; stackT[sp] = to;
         stackNode[++sp] = closer; stackT[sp] = tc;
       } else if (hit0) {
-        if (sp + 1 >= kBvhStack) { atomicOr(c.err, ERR_BVH_STACK); break; }
+        if (sp + 1 >= kBvhStack) { atomicOr(err, ERR_BVH_STACK); break; }
         stackNode[++sp] = c0; stackT[sp] = tn0;
       } else if (hit1) {
-        if (sp + 1 >= kBvhStack) { atomicOr(c.err, ERR_BVH_STACK); break; }
+        if (sp + 1 >= kBvhStack) { atomicOr(err, ERR_BVH_STACK); break; }
         stackNode[++sp] = c1; stackT[sp] = tn1;
       }
     }
   }
   out = closest;
   return anyHit;
+}
+
+// Kernels for meshes with media call the traversal from three places per bounce (bounce ray,
+// shadow ray, the MIS walk); there one out-of-line copy keeps the kernel's instruction
+// footprint small (64 views: 94 -> 104 Mpaths/s). Kernels for meshes without media have two
+// call sites and stay inlined (outlined: 443 -> 437).
+#ifndef NE_OUTLINE_BVH
+#define NE_OUTLINE_BVH 1
+#endif
+template <uint32_t K>
+struct OutlineBvh {
+  static constexpr bool value = NE_OUTLINE_BVH && !(K & K_COUNT) && (K & FT_TRI) && (K & (FT_GRID | FT_HOMOG));
+};
+template <uint32_t K>
+__device__ __noinline__ bool bvhIntersectOutlined(const DScene* sc, uint32_t* err, const DModel* m, Ray r, Hit* out) {
+  Counters none{0, 0, 0, 0};
+  return bvhIntersect<K>(*sc, err, none, *m, r, *out);
 }
 
 // ---------------------------------------------------------------- environment maps
@@ -581,7 +598,11 @@ NE_D bool modelIntersect(Ctx<K>& c, uint32_t mi, const Ray& ray, Hit& hit, float
   if ((K & FT_BBOX) && m.has_bbox)
     if (!aabbIntersect(ld3(m.bbox_min), ld3(m.bbox_max), ray, temp)) return false;
   if ((K & FT_TRI) && m.use_bvh) {
-    bool local = bvhIntersect(c, m, ray, temp);
+    bool local;
+    if constexpr (OutlineBvh<K>::value)
+      local = bvhIntersectOutlined<K>(&c.s, c.err, &m, ray, &temp);
+    else
+      local = bvhIntersect<K>(c.s, c.err, c.c, m, ray, temp);
     if (local && temp.tNear > tMin && temp.tNear < tMax) {
       tMax = temp.tNear;
       hit = temp;
@@ -593,7 +614,7 @@ NE_D bool modelIntersect(Ctx<K>& c, uint32_t mi, const Ray& ray, Hit& hit, float
     int pi = (int)(m.prim_begin + k);
     const DPrim& p = c.s.prims[pi];
     if ((K & FT_GRID) && (p.flags & DPRIM_GRID_MEDIUM)) {
-      primIntersect(c, pi, ray, temp);
+      primIntersect<K>(c.s, c.c, pi, ray, temp);
       float rx = gmax(0.0f, temp.tNear), ry = temp.tFar;
       if (rx <= ry && !nefm::isinf_(ry) && !nefm::isinf_(rx)) {
         temp.prim = pi;
@@ -607,7 +628,7 @@ NE_D bool modelIntersect(Ctx<K>& c, uint32_t mi, const Ray& ray, Hit& hit, float
       }
       continue;
     }
-    bool local = primIntersect(c, pi, ray, temp);
+    bool local = primIntersect<K>(c.s, c.c, pi, ray, temp);
     if (local && temp.tNear != temp.tFar && temp.tNear < 0 && temp.tFar > 0) {
       temp.tNear = 0;
       temp.hitPoint = ray.o;
@@ -626,7 +647,7 @@ NE_D bool modelIntersect(Ctx<K>& c, uint32_t mi, const Ray& ray, Hit& hit, float
     const DPrim& p = c.s.prims[pi];
     const DLight& L = c.s.lights[c.s.materials[p.material].light];
     if (!isBlack(lightLe<K>(L, kIdentity12, ray.d))) continue;
-    bool local = primIntersect(c, pi, ray, temp);
+    bool local = primIntersect<K>(c.s, c.c, pi, ray, temp);
     if (local && temp.tNear > tMin && temp.tNear < tMax) {
       tMax = temp.tNear;
       hit = temp;
