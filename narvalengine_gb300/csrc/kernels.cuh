@@ -29,14 +29,22 @@ constexpr int kThreads = 128;
 #endif
 constexpr int kPathMinBlocks = NE_PATH_MIN_BLOCKS;
 #ifndef NE_MESH_MIN_BLOCKS
-#define NE_MESH_MIN_BLOCKS 10
+#define NE_MESH_MIN_BLOCKS 16
+#endif
+#ifndef NE_MESH_MEDIA_MIN_BLOCKS
+#define NE_MESH_MEDIA_MIN_BLOCKS 8
+#endif
+#ifndef NE_SURFACE_MIN_BLOCKS
+#define NE_SURFACE_MIN_BLOCKS 7
 #endif
 // Triangle meshes run best with more resident warps to hide their instruction-fetch and
-// traversal latency: without media (the mesh feature set) 10 blocks (mesh scene: 7 blocks 178,
-// 10 blocks 188 Mpaths/s), with media (the general set) 8 (views of the medium and the mesh:
-// 7 blocks 66.3, 8 blocks 69.4).
+// traversal latency: without media (the mesh feature set) 16 blocks, the most an SM holds (mesh
+// scene: 6 blocks 373, 8 416, 10 443, 12 471, 16 502 Mpaths/s, despite the spills of a
+// 32-register cap), with media (the general set) 8 (views of the medium and the mesh: 7 blocks
+// 66.3, 8 blocks 69.4). Surfaces without meshes or media (the surface set) and volumes 7.
 __host__ __device__ constexpr int pathMinBlocks(uint32_t K) {
-  return (K & FT_TRI) ? ((K & FT_GRID) ? 8 : NE_MESH_MIN_BLOCKS) : kPathMinBlocks;
+  return (K & FT_TRI) ? ((K & FT_GRID) ? NE_MESH_MEDIA_MIN_BLOCKS : NE_MESH_MIN_BLOCKS)
+                      : ((K & (FT_GRID | FT_HOMOG | FT_VOLBSDF)) ? kPathMinBlocks : NE_SURFACE_MIN_BLOCKS);
 }
 
 // Per-view completion accounting of a batch of views (see views.cuh): the path range of
