@@ -32,16 +32,17 @@ constexpr int kPathMinBlocks = NE_PATH_MIN_BLOCKS;
 #define NE_MESH_MIN_BLOCKS 16
 #endif
 #ifndef NE_MESH_MEDIA_MIN_BLOCKS
-#define NE_MESH_MEDIA_MIN_BLOCKS 8
+#define NE_MESH_MEDIA_MIN_BLOCKS 16
 #endif
 #ifndef NE_SURFACE_MIN_BLOCKS
 #define NE_SURFACE_MIN_BLOCKS 7
 #endif
-// Triangle meshes run best with more resident warps to hide their instruction-fetch and
-// traversal latency: without media (the mesh feature set) 16 blocks, the most an SM holds (mesh
-// scene: 6 blocks 373, 8 416, 10 443, 12 471, 16 502 Mpaths/s, despite the spills of a
-// 32-register cap), with media (the general set) 8 (views of the medium and the mesh: 7 blocks
-// 66.3, 8 blocks 69.4). Surfaces without meshes or media (the surface set) and volumes 7.
+// Triangle meshes run best with as many resident warps as an SM holds (16 blocks of 128
+// threads, a 32-register cap) to hide their instruction-fetch and traversal latency, despite
+// the spills: without media (the mesh feature set; mesh scene: 6 blocks 373, 8 416, 10 443,
+// 12 471, 16 502 Mpaths/s) and with media (the general set; 64 views of the medium and the
+// mesh: 8 blocks 104, 16 blocks 126). Surfaces without meshes or media (the surface set;
+// Cornell box: 7 blocks 947, 16 blocks 836) and volumes: 7.
 __host__ __device__ constexpr int pathMinBlocks(uint32_t K) {
   return (K & FT_TRI) ? ((K & FT_GRID) ? NE_MESH_MEDIA_MIN_BLOCKS : NE_MESH_MIN_BLOCKS)
                       : ((K & (FT_GRID | FT_HOMOG | FT_VOLBSDF)) ? kPathMinBlocks : NE_SURFACE_MIN_BLOCKS);
