@@ -321,6 +321,12 @@ ne_status ne_render_cached(ne_scene* scene, ne_cache* cache, const ne_render_par
 ne_status ne_debug_bvh(const ne_primitive* prims, uint32_t first, uint32_t count, float* nodes, size_t cap,
                        uint32_t* order, size_t* n_nodes);
 
+/* The world-space boxes ne_scene_upload bounds the scene's media with (on the host, no GPU
+ * needed): 6 floats per box (min xyz, max xyz), `cap` boxes at most. The kernels for meshes with
+ * media skip intersectTr's walk (integrators/VolumetricPathIntegrator.cpp:10-32) for an MIS ray
+ * whose line misses every box. *n_boxes = -1: no boxes (every ray walks); 0: no medium. */
+ne_status ne_debug_medium_boxes(const ne_scene_desc* desc, float* boxes, size_t cap, int32_t* n_boxes);
+
 /* The BVH of model `model` of an uploaded scene, read back from the device in ne_debug_bvh's
  * format (an interior node's start and count are 0) with its primitive order (the model's
  * prim_count global primitive indices). nodes = NULL: sets *n_nodes only (0: no BVH). Lets a

@@ -192,6 +192,7 @@ SIGNATURES = {
     "ne_views_image": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p]),
     "ne_debug_bvh": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_size_t, C.c_void_p,
                                  C.POINTER(C.c_size_t)]),
+    "ne_debug_medium_boxes": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_size_t, C.POINTER(C.c_int32)]),
     "ne_scene_bvh": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_size_t, C.c_void_p, C.POINTER(C.c_size_t)]),
     "ne_save_png": (C.c_int32, [C.c_char_p, C.c_void_p, C.c_int, C.c_int]),
     "ne_save_exr": (C.c_int32, [C.c_char_p, C.c_void_p, C.c_int, C.c_int]),

@@ -1097,6 +1097,70 @@ void ne_context_destroy(ne_context* ctx) {
 
 const char* ne_last_error(const ne_context* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
 
+// World-space bounds of the primitives whose material has a medium: a walk of intersectTr
+// whose ray misses all of them can reach no medium. Each primitive's OCS bounds (box corners,
+// sphere centre +- radius, rectangle corners, triangle vertices) go through the instance's
+// transform in double precision and are widened by 1e-3 of their extent and position, far
+// beyond the rounding of the float transforms and of the walk's successive origins.
+// Returns the number of boxes (6 floats each: min xyz, max xyz), or -1 when they are not
+// known (a non-finite bound, or more than 64 boxes): every ray may then reach a medium.
+static int32_t mediumBoxesOf(const ne_scene_desc& D, std::vector<float>& boxes) {
+  boxes.clear();
+  int32_t nMediumBoxes = 0;
+  const uint32_t ninst = D.n_instances + D.n_light_instances;
+  for (uint32_t i = 0; i < ninst && nMediumBoxes >= 0; i++) {
+    const ne_model& m = D.models[D.instances[i].model];
+    const float* W = D.instances[i].to_wcs;
+    auto addPrim = [&](const ne_primitive& p) {
+      if (p.material < 0 || D.materials[p.material].medium < 0) return;
+      double lo[3], hi[3];
+      for (int a = 0; a < 3; a++) {
+        if (p.type == NE_PRIM_SPHERE) {
+          lo[a] = (double)p.p0[a] - fabs((double)p.radius);
+          hi[a] = (double)p.p0[a] + fabs((double)p.radius);
+        } else {
+          lo[a] = std::min((double)p.p0[a], (double)p.p1[a]);
+          hi[a] = std::max((double)p.p0[a], (double)p.p1[a]);
+          if (p.type == NE_PRIM_TRIANGLE) {
+            lo[a] = std::min(lo[a], (double)p.p2[a]);
+            hi[a] = std::max(hi[a], (double)p.p2[a]);
+          }
+        }
+      }
+      double wlo[3] = {INFINITY, INFINITY, INFINITY}, whi[3] = {-INFINITY, -INFINITY, -INFINITY};
+      for (int corner = 0; corner < 8; corner++) {
+        double q[3] = {(corner & 1) ? hi[0] : lo[0], (corner & 2) ? hi[1] : lo[1], (corner & 4) ? hi[2] : lo[2]};
+        for (int r = 0; r < 3; r++) {
+          double w = (double)W[12 + r];
+          for (int c = 0; c < 3; c++) w += (double)W[c * 4 + r] * q[c];
+          wlo[r] = std::min(wlo[r], w);
+          whi[r] = std::max(whi[r], w);
+        }
+      }
+      bool finite = true;
+      for (int a = 0; a < 3; a++) finite = finite && std::isfinite(wlo[a]) && std::isfinite(whi[a]);
+      if (!finite || p.type == NE_PRIM_POINT) {
+        if (!finite) nMediumBoxes = -1;
+        return;
+      }
+      for (int a = 0; a < 3; a++) {
+        double margin = 1e-3 * ((whi[a] - wlo[a]) + std::max(fabs(wlo[a]), fabs(whi[a]))) + 1e-6;
+        boxes.push_back((float)(wlo[a] - margin));
+      }
+      for (int a = 0; a < 3; a++) {
+        double margin = 1e-3 * ((whi[a] - wlo[a]) + std::max(fabs(wlo[a]), fabs(whi[a]))) + 1e-6;
+        boxes.push_back((float)(whi[a] + margin));
+      }
+      if (nMediumBoxes >= 0) nMediumBoxes++;
+    };
+    for (uint32_t k = 0; k < m.prim_count && nMediumBoxes >= 0; k++) addPrim(D.prims[m.prim_begin + k]);
+    for (uint32_t k = 0; k < m.light_count && nMediumBoxes >= 0; k++) addPrim(D.prims[m.light_begin + k]);
+  }
+  if (nMediumBoxes > 64) nMediumBoxes = -1;  // many media: the test would cost more than it saves
+  if (nMediumBoxes < 0) boxes.clear();
+  return nMediumBoxes;
+}
+
 ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene** out) {
   if (!ctx || !desc || !out) return NE_ERR_INVALID_ARG;
   *out = nullptr;
@@ -1201,62 +1265,8 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
     }
     d.never_hit = never ? 1 : 0;
   }
-  // World-space bounds of the primitives whose material has a medium: a walk of intersectTr
-  // whose ray misses all of them can reach no medium. Each primitive's OCS bounds (box corners,
-  // sphere centre +- radius, rectangle corners, triangle vertices) go through the instance's
-  // transform in double precision and are widened by 1e-3 of their extent and position, far
-  // beyond the rounding of the float transforms and of the walk's successive origins.
   std::vector<float> mediumBoxes;
-  int32_t nMediumBoxes = 0;
-  for (uint32_t i = 0; i < ninst && nMediumBoxes >= 0; i++) {
-    const ne_model& m = D.models[D.instances[i].model];
-    const float* W = D.instances[i].to_wcs;
-    auto addPrim = [&](const ne_primitive& p) {
-      if (p.material < 0 || D.materials[p.material].medium < 0) return;
-      double lo[3], hi[3];
-      for (int a = 0; a < 3; a++) {
-        if (p.type == NE_PRIM_SPHERE) {
-          lo[a] = (double)p.p0[a] - fabs((double)p.radius);
-          hi[a] = (double)p.p0[a] + fabs((double)p.radius);
-        } else {
-          lo[a] = std::min((double)p.p0[a], (double)p.p1[a]);
-          hi[a] = std::max((double)p.p0[a], (double)p.p1[a]);
-          if (p.type == NE_PRIM_TRIANGLE) {
-            lo[a] = std::min(lo[a], (double)p.p2[a]);
-            hi[a] = std::max(hi[a], (double)p.p2[a]);
-          }
-        }
-      }
-      double wlo[3] = {INFINITY, INFINITY, INFINITY}, whi[3] = {-INFINITY, -INFINITY, -INFINITY};
-      for (int corner = 0; corner < 8; corner++) {
-        double q[3] = {(corner & 1) ? hi[0] : lo[0], (corner & 2) ? hi[1] : lo[1], (corner & 4) ? hi[2] : lo[2]};
-        for (int r = 0; r < 3; r++) {
-          double w = (double)W[12 + r];
-          for (int c = 0; c < 3; c++) w += (double)W[c * 4 + r] * q[c];
-          wlo[r] = std::min(wlo[r], w);
-          whi[r] = std::max(whi[r], w);
-        }
-      }
-      bool finite = true;
-      for (int a = 0; a < 3; a++) finite = finite && std::isfinite(wlo[a]) && std::isfinite(whi[a]);
-      if (!finite || p.type == NE_PRIM_POINT) {
-        if (!finite) nMediumBoxes = -1;
-        return;
-      }
-      for (int a = 0; a < 3; a++) {
-        double margin = 1e-3 * ((whi[a] - wlo[a]) + std::max(fabs(wlo[a]), fabs(whi[a]))) + 1e-6;
-        mediumBoxes.push_back((float)(wlo[a] - margin));
-      }
-      for (int a = 0; a < 3; a++) {
-        double margin = 1e-3 * ((whi[a] - wlo[a]) + std::max(fabs(wlo[a]), fabs(whi[a]))) + 1e-6;
-        mediumBoxes.push_back((float)(whi[a] + margin));
-      }
-      if (nMediumBoxes >= 0) nMediumBoxes++;
-    };
-    for (uint32_t k = 0; k < m.prim_count && nMediumBoxes >= 0; k++) addPrim(D.prims[m.prim_begin + k]);
-    for (uint32_t k = 0; k < m.light_count && nMediumBoxes >= 0; k++) addPrim(D.prims[m.light_begin + k]);
-  }
-  if (nMediumBoxes > 64) nMediumBoxes = -1;  // many media: the test would cost more than it saves
+  const int32_t nMediumBoxes = mediumBoxesOf(D, mediumBoxes);
   // primitives
   std::vector<DPrim> prims(D.n_prims);
   auto convertPrim = [&](uint32_t i) {
@@ -2582,6 +2592,25 @@ ne_status ne_scene_bvh(const ne_scene* sc, uint32_t model, float* nodes, size_t 
       memcpy(o + 8, &a, 4);
     }
   }
+  return NE_OK;
+}
+
+ne_status ne_debug_medium_boxes(const ne_scene_desc* desc, float* boxes, size_t cap, int32_t* n_boxes) {
+  if (!desc || !n_boxes) return NE_ERR_INVALID_ARG;
+  const ne_scene_desc& D = *desc;
+  for (uint32_t i = 0; i < D.n_instances + D.n_light_instances; i++) {
+    if (D.instances[i].model >= D.n_models) return NE_ERR_INVALID_ARG;
+    const ne_model& m = D.models[D.instances[i].model];
+    if ((uint64_t)m.prim_begin + m.prim_count > D.n_prims || (uint64_t)m.light_begin + m.light_count > D.n_prims)
+      return NE_ERR_INVALID_ARG;
+  }
+  for (uint32_t i = 0; i < D.n_prims; i++)
+    if (D.prims[i].material >= (int)D.n_materials) return NE_ERR_INVALID_ARG;
+  std::vector<float> b;
+  *n_boxes = mediumBoxesOf(*desc, b);
+  if (*n_boxes <= 0) return NE_OK;
+  if (!boxes || cap < (size_t)*n_boxes) return NE_ERR_INVALID_ARG;
+  memcpy(boxes, b.data(), b.size() * sizeof(float));
   return NE_OK;
 }
 
