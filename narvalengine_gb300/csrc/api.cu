@@ -1103,7 +1103,8 @@ const char* ne_last_error(const ne_context* ctx) { return ctx ? ctx->err.c_str()
 // transform in double precision and are widened by 1e-3 of their extent and position, far
 // beyond the rounding of the float transforms and of the walk's successive origins.
 // Returns the number of boxes (6 floats each: min xyz, max xyz), or -1 when they are not
-// known (a non-finite bound, or more than 64 boxes): every ray may then reach a medium.
+// known (a non-finite bound, a rectangle whose hits its corners do not bound, or more than 64
+// boxes): every ray may then reach a medium.
 static int32_t mediumBoxesOf(const ne_scene_desc& D, std::vector<float>& boxes) {
   boxes.clear();
   int32_t nMediumBoxes = 0;
@@ -1139,8 +1140,19 @@ static int32_t mediumBoxesOf(const ne_scene_desc& D, std::vector<float>& boxes) 
       }
       bool finite = true;
       for (int a = 0; a < 3; a++) finite = finite && std::isfinite(wlo[a]) && std::isfinite(whi[a]);
+      if (p.type == NE_PRIM_RECTANGLE) {
+        // Rectangle::intersect checks containment only on the axes where the corners differ;
+        // its hits stay inside the corners' box only if the corners agree on exactly one axis
+        // and the plane normal lies along it
+        int same = 0;
+        for (int a = 0; a < 3; a++) {
+          if (p.p0[a] == p.p1[a]) same++;
+          else if (p.p2[a] != 0.0f) finite = false;
+        }
+        if (same != 1) finite = false;
+      }
       if (!finite || p.type == NE_PRIM_POINT) {
-        if (!finite) nMediumBoxes = -1;
+        if (!finite) nMediumBoxes = -1;  // unbounded, or not known to be bounded
         return;
       }
       for (int a = 0; a < 3; a++) {

@@ -126,3 +126,23 @@ def test_scene_without_media_has_no_boxes(built):
     boxes, n = medium_boxes(ne, host)
     assert n == 0 and len(boxes) == 0
     assert ne.library().ne_debug_medium_boxes(None, None, 0, C.byref(C.c_int32())) != 0
+
+
+def test_rectangle_media_are_bounded_only_when_their_hits_are(built):
+    """Rectangle::intersect (Rectangle.cpp:50-76) checks containment only on the axes where the
+    corners differ, so a rectangle's corners bound its hits only when they agree on exactly one
+    axis and the plane normal lies along it; otherwise no boxes are given (every ray walks)."""
+    import narvalengine_gb300 as ne
+    host = mixed_host(ne)
+    (prim, _), = medium_prims(host)
+    p = host.desc.prims[prim]
+    p.type = 1  # NE_PRIM_RECTANGLE
+    p.p0[0], p.p0[1], p.p0[2] = -0.5, -0.5, 0.0
+    p.p1[0], p.p1[1], p.p1[2] = 0.5, 0.5, 0.0
+    p.p2[0], p.p2[1], p.p2[2] = 0.0, 0.0, -1.0
+    assert medium_boxes(ne, host)[1] == 1
+    p.p2[0] = 0.5  # tilted plane: z is free within the x extent
+    assert medium_boxes(ne, host)[1] == -1
+    p.p2[0] = 0.0
+    p.p1[1] = -0.5  # corners agree on y and z: a hit's y is free on the plane
+    assert medium_boxes(ne, host)[1] == -1
