@@ -496,8 +496,9 @@ NE_D bool bvhIntersect(const DScene& sc, uint32_t* err, Counters& cnt, const DMo
 
 // Kernels for meshes with media call the traversal from three places per bounce (bounce ray,
 // shadow ray, the MIS walk); there one out-of-line copy keeps the kernel's instruction
-// footprint small (64 views: 94 -> 104 Mpaths/s). Kernels for meshes without media have two
-// call sites and stay inlined (outlined: 443 -> 437).
+// footprint small (64 views: 94 -> 104 Mpaths/s, both built for 8 resident blocks per SM).
+// Kernels for meshes without media have two call sites and stay inlined (outlined: 443 -> 437
+// at 10 blocks per SM).
 #ifndef NE_OUTLINE_BVH
 #define NE_OUTLINE_BVH 1
 #endif
