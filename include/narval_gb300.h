@@ -144,11 +144,16 @@ ne_status ne_render(ne_scene* scene, const ne_render_params* params, float* out_
  * for the render to read its error flag). Per-path
  * scratch comes from a fixed array of the library of NE_NOALLOC_MAX_PATHS paths (12 MiB),
  * held on every GPU that loads the library until the process exits; a call with more
- * paths (covered pixels x spp) fails with NE_ERR_INVALID_ARG. The first call on a device
- * looks up the array's address (cudaGetSymbolAddress) and should come before any stream
- * capture. All calls on a device share the array, which keeps the last call's contents:
- * calls whose work overlaps on the GPU (contexts on one device, unordered streams) race
- * and must be serialised by the caller. */
+ * paths (covered pixels x spp) fails with NE_ERR_INVALID_ARG. Kernel: the scene's tuned
+ * path kernel, except that a scene tuned to the split kernel (kernel 3, the default after
+ * ne_scene_autotune on most scenes) renders with the one-pass kernel (kernel 0) at that
+ * kernel's occupancy: the split kernel's deferred-path queues are sized to the render and do
+ * not fit the fixed array. The image is the same bits either way; the one-pass kernel is
+ * several times slower on scenes with media (about 4x on the 512^2 x 64 spp medium scene).
+ * The first call on a device after a context is created on it looks up the array's address
+ * (cudaGetSymbolAddress) and should come before any stream capture. All calls on a device
+ * share the array, which keeps the last call's contents: calls whose work overlaps on the GPU
+ * (contexts on one device, unordered streams) race and must be serialised by the caller. */
 #define NE_NOALLOC_MAX_PATHS (1u << 20)
 ne_status ne_render_noalloc(ne_scene* scene, const ne_render_params* params, float* out_rgb_device,
                             ne_render_stats* stats);
@@ -215,6 +220,12 @@ ne_status ne_context_event_elapsed(ne_context* ctx, int slot_begin, int slot_end
 ne_status ne_context_synchronize(ne_context* ctx);
 /* Writes `bytes` of scratch memory on the context's stream, evicting the L2 cache. */
 ne_status ne_context_flush_l2(ne_context* ctx, size_t bytes);
+/* Read bandwidth of this GPU for a buffer of `bytes` (no counterpart in the reference; a
+ * roofline denominator for benchmarks): one warm-up pass, then `iters` back-to-back launches
+ * of a read-only kernel (16-byte loads that bypass L1, one CTA per SM times the resident
+ * count) over the same buffer, event-timed; *gbs = bytes * iters / time. A buffer well inside
+ * the 129 MB L2 measures L2 bandwidth, one well beyond it HBM bandwidth. */
+ne_status ne_measure_read_bandwidth(ne_context* ctx, size_t bytes, int iters, double* gbs);
 
 /* Device copies of the shared elementary functions, for bit-exactness checks.
  * fn: 0 log, 1 exp, 2 sin, 3 cos, 4 acos, 5 pow5, 6 atan2(x[i], x[i ^ 1]) (elements paired;
@@ -333,6 +344,13 @@ ne_status ne_debug_medium_boxes(const ne_scene_desc* desc, float* boxes, size_t 
  * CPU check traverse the tree the GPU built ("bvh": "sah"). */
 ne_status ne_scene_bvh(const ne_scene* scene, uint32_t model, float* nodes, size_t cap, uint32_t* order,
                        size_t* n_nodes);
+
+/* Failure detection of the tensor-core kernels' bounded waits (no counterpart in the
+ * reference, a test hook): one block allocates tensor memory, initialises an mbarrier as the
+ * radiance-cache kernels do, and waits for a completion that nothing signals, giving up after
+ * `max_polls` (1 .. 2^20) polls instead of the kernels' 2^24. Returns NE_ERR_TIMEOUT, with the
+ * tensor memory released and the context usable, when the wait ran out as intended. */
+ne_status ne_debug_wait_timeout(ne_context* ctx, uint32_t max_polls);
 
 /* One 128 x n x k tensor-core product D = A * B^T (BF16 bit patterns, row-major A[128][k],
  * B[n][k]; FP32 D[128][n]) through the same shared-memory and tensor-memory conventions as

@@ -186,6 +186,12 @@ class Context:
     def flush_l2(self, nbytes: int = 256 << 20):
         self.check(library().ne_context_flush_l2(self._h, nbytes))
 
+    def read_bandwidth(self, nbytes: int, iters: int = 50) -> float:
+        """GB/s of a read-only kernel over an `nbytes` buffer (ne_measure_read_bandwidth)."""
+        gbs = C.c_double()
+        self.check(library().ne_measure_read_bandwidth(self._h, nbytes, iters, C.byref(gbs)))
+        return gbs.value
+
     def fmath(self, fn: int, x: np.ndarray) -> np.ndarray:
         x = np.ascontiguousarray(x, dtype=np.float32)
         out = np.empty_like(x)

@@ -163,6 +163,7 @@ SIGNATURES = {
     "ne_context_event_elapsed": (C.c_int32, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_float)]),
     "ne_context_synchronize": (C.c_int32, [C.c_void_p]),
     "ne_context_flush_l2": (C.c_int32, [C.c_void_p, C.c_size_t]),
+    "ne_measure_read_bandwidth": (C.c_int32, [C.c_void_p, C.c_size_t, C.c_int, C.POINTER(C.c_double)]),
     "ne_debug_fmath": (C.c_int32, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t, C.c_void_p]),
     "ne_debug_rng": (C.c_int32, [C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
     "ne_cache_create": (C.c_int32, [C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p)]),
@@ -199,4 +200,5 @@ SIGNATURES = {
     "ne_image_load_rgba8": (C.c_int32, [C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_void_p,
                                         C.c_size_t]),
     "ne_debug_mma": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
+    "ne_debug_wait_timeout": (C.c_int32, [C.c_void_p, C.c_uint32]),
 }

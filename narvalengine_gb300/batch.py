@@ -12,9 +12,11 @@ SIZES = (64, 128, 256, 512)
 
 
 def orbit_views(n: int = 64, seed: int = 0x4E415256, spp: int = 16, center=(0.0, 1.0, 0.0), radius: float = 4.5,
-                height: float = 1.8, vfov: float = 45.0, sizes=SIZES):
-    """[(camera, width, height, spp)] for n cameras evenly spaced on a ring."""
-    from . import camera_look_at
+                height: float = 1.8, vfov: float = 45.0, sizes=SIZES, camera_look_at=None):
+    """[(camera, width, height, spp)] for n cameras evenly spaced on a ring. `camera_look_at`
+    (position, look_at, vfov, width, height) -> ne_camera defaults to the library's."""
+    if camera_look_at is None:
+        from . import camera_look_at
     rng = np.random.default_rng(seed)
     picks = rng.integers(0, len(sizes), size=n)
     views = []

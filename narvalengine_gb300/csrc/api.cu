@@ -545,6 +545,24 @@ __global__ void k_accum(const float* __restrict__ paths, uint32_t n_pix, uint32_
   }
 }
 
+// Read-only bandwidth probe: every thread reads 16-byte words (ld.global.cg: cached in L2,
+// not L1) with a grid stride, four in flight, and folds them into one word that is written
+// only if it equals a value the data never produces (so the loads are not removed).
+__global__ void __launch_bounds__(512) k_read_bw(const uint4* __restrict__ p, size_t n, uint32_t* sink) {
+  uint32_t acc = 0;
+  size_t stride = (size_t)gridDim.x * blockDim.x;
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  for (; i + 3 * stride < n; i += 4 * stride) {
+    uint4 a = __ldcg(p + i), b = __ldcg(p + i + stride), c = __ldcg(p + i + 2 * stride), d = __ldcg(p + i + 3 * stride);
+    acc ^= (a.x ^ a.y ^ a.z ^ a.w) ^ (b.x ^ b.y ^ b.z ^ b.w) ^ (c.x ^ c.y ^ c.z ^ c.w) ^ (d.x ^ d.y ^ d.z ^ d.w);
+  }
+  for (; i < n; i += stride) {
+    uint4 a = __ldcg(p + i);
+    acc ^= a.x ^ a.y ^ a.z ^ a.w;
+  }
+  if (acc == 0x9e3779b9u) sink[0] = acc;
+}
+
 __global__ void k_fmath(int fn, const float* __restrict__ x, size_t n, float* __restrict__ out) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     float v = x[i], r;
@@ -812,9 +830,17 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 std::mutex g_noalloc_mutex;
 unsigned char* g_noalloc_ptr[kNoAllocMaxDevices] = {};
 
-// Device address of the array on the current device, looked up once per device. In host
-// code g_noalloc_scratch names a host-side stand-in, so the address must come from the
-// runtime.
+// Device address of the array on the current device, looked up once per device by the first
+// call after a context is created on that device (ne_context_create forgets the address, so
+// a device reset between contexts, which reloads the module, is followed by a fresh lookup).
+// In host code g_noalloc_scratch names a host-side stand-in, so the address must come from
+// the runtime.
+void noallocForget(int device) {
+  if (device < 0 || device >= kNoAllocMaxDevices) return;
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  g_noalloc_ptr[device] = nullptr;
+}
+
 ne_status noallocScratch(ne_context* ctx, unsigned char** out) {
   if (ctx->device < 0 || ctx->device >= kNoAllocMaxDevices)
     return fail(ctx, NE_ERR_UNSUPPORTED, "ne_render_noalloc supports device ordinals below 64");
@@ -1051,6 +1077,7 @@ ne_status ne_context_create(int device, ne_context** out) {
   if (device < 0 || device >= n) return NE_ERR_INVALID_ARG;
   ne_context* ctx = new ne_context();
   ctx->device = device;
+  noallocForget(device);
   auto bad = [&](cudaError_t e, const char* w) {
     ne_status st = cudaFail(ctx, e, w);
     ne_context_destroy(ctx);
@@ -1852,6 +1879,31 @@ ne_status ne_context_flush_l2(ne_context* ctx, size_t bytes) {
   return NE_OK;
 }
 
+ne_status ne_measure_read_bandwidth(ne_context* ctx, size_t bytes, int iters, double* gbs) {
+  if (!ctx || !gbs || bytes < 16 || iters <= 0) return NE_ERR_INVALID_ARG;
+  NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  size_t n = bytes / 16;
+  DevBuf<uint4> buf;
+  DevBuf<uint32_t> sink;
+  NE_CUDA(cudaMalloc(&buf.p, n * 16), "cudaMalloc(read probe)");
+  NE_CUDA(cudaMalloc(&sink.p, 4), "cudaMalloc(read probe)");
+  NE_CUDA(cudaMemsetAsync(buf.p, 0x5a, n * 16, ctx->stream), "cudaMemsetAsync(read probe)");
+  int per_sm = 0;
+  NE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_read_bw, 512, 0), "occupancy");
+  int blocks = ctx->sm_count * std::max(1, per_sm);
+  k_read_bw<<<blocks, 512, 0, ctx->stream>>>(buf.p, n, sink.p);  // warm-up: brings the buffer into L2
+  NE_CUDA(cudaGetLastError(), "k_read_bw launch");
+  NE_CUDA(cudaEventRecord(ctx->ev[0], ctx->stream), "cudaEventRecord");
+  for (int k = 0; k < iters; k++) k_read_bw<<<blocks, 512, 0, ctx->stream>>>(buf.p, n, sink.p);
+  NE_CUDA(cudaGetLastError(), "k_read_bw launch");
+  NE_CUDA(cudaEventRecord(ctx->ev[1], ctx->stream), "cudaEventRecord");
+  NE_CUDA(cudaEventSynchronize(ctx->ev[1]), "cudaEventSynchronize");
+  float ms = 0;
+  NE_CUDA(cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]), "cudaEventElapsedTime");
+  *gbs = (double)n * 16 * iters / (ms / 1e3) / 1e9;
+  return NE_OK;
+}
+
 ne_status ne_debug_fmath(ne_context* ctx, int fn, const float* x, size_t n, float* out) {
   if (!ctx || (n && (!x || !out))) return NE_ERR_INVALID_ARG;
   if (n == 0) return NE_OK;
@@ -1932,12 +1984,21 @@ ne_status ne_render_noalloc(ne_scene* sc, const ne_render_params* p, float* out_
   a.keys = nullptr;
   a.out = d_paths;
   a.track_share = sc->track_share;
+  // The split kernel (tuning kernel 3) needs deferred-path queues sized to the render, which
+  // the fixed array does not hold: a scene tuned to it renders with the one-pass kernel
+  // (kernel 0), at that kernel's own occupancy. Kernels 0-2 run as tuned.
+  const bool count = (flags & NE_RENDER_COUNT_WORK) != 0;
+  const int kernel = sc->variant == 3 ? 0 : sc->variant;
   int blocks = persistentBlocks(sc);
+  if (sc->variant == 3 && !count) {
+    int fit = 0;
+    NE_CUDA(ne_path_kernel_occupancy(0, sc->feature_set, &fit), "occupancy query");
+    blocks = ctx->sm_count * std::max(1, fit);
+  }
   unsigned long long needed = (total + kThreads - 1) / kThreads;
   if ((unsigned long long)blocks > needed) blocks = (int)std::max<unsigned long long>(1, needed);
   NE_CUDA(cudaEventRecord(ctx->ev[1], ctx->stream), "cudaEventRecord");
-  NE_CUDA(ne_launch_path_kernel(sc->variant, sc->feature_set, (flags & NE_RENDER_COUNT_WORK) != 0, blocks,
-                                ctx->stream, sc->d, a, d_counter, d_err),
+  NE_CUDA(ne_launch_path_kernel(kernel, sc->feature_set, count, blocks, ctx->stream, sc->d, a, d_counter, d_err),
           "path kernel launch");
   NE_CUDA(cudaEventRecord(ctx->ev[2], ctx->stream), "cudaEventRecord");
   int rblocks = (int)std::min<uint64_t>((npix + 255) / 256, (uint64_t)ctx->sm_count * 16);
@@ -1990,6 +2051,17 @@ ne_status ne_debug_mma(ne_context* ctx, const uint16_t* a, const uint16_t* b, in
   return NE_OK;
 }
 
+ne_status ne_debug_wait_timeout(ne_context* ctx, uint32_t max_polls) {
+  if (!ctx || max_polls == 0 || max_polls > (1u << 20)) return NE_ERR_INVALID_ARG;
+  NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  NE_CUDA(cudaMemsetAsync(ctx->d_err, 0, 4, ctx->stream), "cudaMemsetAsync");
+  NE_CUDA(ne_launch_debug_wait(ctx->stream, max_polls, ctx->d_err), "k_debug_wait launch");
+  uint32_t e = 0;
+  NE_CUDA(cudaMemcpyAsync(&e, ctx->d_err, 4, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync");
+  NE_CUDA(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  if (e) return fail(ctx, NE_ERR_TIMEOUT, "tensor-core wait gave up after " + std::to_string(max_polls) + " polls");
+  return NE_OK;
+}
 
 ne_status ne_cache_create(ne_context* ctx, uint64_t seed, ne_cache** out) {
   if (!ctx || !out) return NE_ERR_INVALID_ARG;

@@ -74,7 +74,40 @@ __global__ void __launch_bounds__(kMmaThreads) k_debug_mma(const uint16_t* __res
   if (t < 32) tmem_dealloc(tb, ncols);
 }
 
+// Failure-detection check of the bounded waits: the block allocates tensor memory and
+// initialises an mbarrier exactly as the product kernels do, then waits for a completion
+// that nothing signals (no MMA is issued, nobody arrives). The wait gives up after
+// `max_polls` polls, the block sets err bit 1, releases its tensor memory and exits.
+__global__ void __launch_bounds__(kMmaThreads) k_debug_wait(uint32_t max_polls, uint32_t* err) {
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tbase;
+  const uint32_t t = threadIdx.x;
+  if (t == 0) {
+    mbar_init(&bar, 1);
+    mbar_fence_init();
+  }
+  if (t < 32) {
+    tmem_alloc(&tbase, 32);
+    tmem_relinquish();
+  }
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  const uint32_t tb = tbase;
+  bool ok = mbar_wait(&bar, 0, max_polls);
+  ok = __syncthreads_and(ok);
+  if (!ok && t == 0) atomicOr(err, 1u);
+  fence_before_sync();
+  __syncthreads();
+  if (t < 32) tmem_dealloc(tb, 32);
+}
+
 }  // namespace
+
+cudaError_t ne_launch_debug_wait(cudaStream_t st, uint32_t max_polls, uint32_t* err) {
+  k_debug_wait<<<1, kMmaThreads, 0, st>>>(max_polls, err);
+  return cudaGetLastError();
+}
 
 // ---------------------------------------------------------------------------------------
 // Network definition (identical to the CPU restatement used to check it).

@@ -9,6 +9,10 @@
 cudaError_t ne_launch_debug_mma(cudaStream_t st, const uint16_t* a, const uint16_t* b, int n, int k, float* d,
                                 uint32_t* err);
 
+// A block that allocates tensor memory and waits on an mbarrier nothing signals, bounded by
+// `max_polls` polls: err bit 1 once the wait has given up (tensor memory released).
+cudaError_t ne_launch_debug_wait(cudaStream_t st, uint32_t max_polls, uint32_t* err);
+
 // Parameters: FP32, per layer W[out][in] then b[out]; layers 96->64, 64->64 (x3), 64->16.
 constexpr int kNeMlpParams = 19728;
 constexpr int kNeMlpFwdBytes = 38912;   // packed BF16 forward weight tiles

@@ -191,51 +191,88 @@ M4 mul(const M4& a, const M4& b) {
     }
   return r;
 }
-// glm::eulerAngleXYZ(t1, t2, t3) = eulerAngleX(t1) * eulerAngleY(t2) * eulerAngleZ(t3).
+// glm::eulerAngleXYZ(t1, t2, t3) (glm's gtx/euler_angles.inl), the rotation utils/Math.h:848-850
+// builds: the closed form of X(t1) Y(t2) Z(t3) over c_i = cos(-t_i), s_i = sin(-t_i), term by
+// term as glm writes it.
 M4 eulerXYZ(float t1, float t2, float t3) {
-  M4 rx = ident(), ry = ident(), rz = ident();
-  float c1 = nefm::cos(t1), s1 = nefm::sin(t1);
-  float c2 = nefm::cos(t2), s2 = nefm::sin(t2);
-  float c3 = nefm::cos(t3), s3 = nefm::sin(t3);
-  rx.at(1, 1) = c1; rx.at(2, 1) = s1; rx.at(1, 2) = -s1; rx.at(2, 2) = c1;
-  ry.at(0, 0) = c2; ry.at(2, 0) = -s2; ry.at(0, 2) = s2; ry.at(2, 2) = c2;
-  rz.at(0, 0) = c3; rz.at(1, 0) = s3; rz.at(0, 1) = -s3; rz.at(1, 1) = c3;
-  return mul(mul(rx, ry), rz);
+  float c1 = nefm::cos(-t1), c2 = nefm::cos(-t2), c3 = nefm::cos(-t3);
+  float s1 = nefm::sin(-t1), s2 = nefm::sin(-t2), s3 = nefm::sin(-t3);
+  M4 r = ident();
+  r.at(0, 0) = c2 * c3;
+  r.at(1, 0) = -c1 * s3 + s1 * s2 * c3;
+  r.at(2, 0) = s1 * s3 + c1 * s2 * c3;
+  r.at(0, 1) = c2 * s3;
+  r.at(1, 1) = c1 * c3 + s1 * s2 * s3;
+  r.at(2, 1) = -s1 * c3 + c1 * s2 * s3;
+  r.at(0, 2) = -s2;
+  r.at(1, 2) = s1 * c2;
+  r.at(2, 2) = c1 * c2;
+  return r;
 }
 // utils/Math.h:852-859 getTransform = translate(I, t) * rotate(r) * scale(s); degrees.
 M4 getTransform(const float* t, const float* rdeg, const float* s) {
   const float toRad = 0.01745329251994329576923690768489f;  // glm::radians
-  M4 tr = ident();
-  tr.m[12] = t[0]; tr.m[13] = t[1]; tr.m[14] = t[2];
+  // glm::translate(I, t): column 3 = ((I0 t0 + I1 t1) + I2 t2) + I3
+  M4 id = ident(), tr = ident();
+  for (int k = 0; k < 4; k++)
+    tr.at(k, 3) = ((id.at(k, 0) * t[0] + id.at(k, 1) * t[1]) + id.at(k, 2) * t[2]) + id.at(k, 3);
   M4 r = mul(tr, eulerXYZ(rdeg[0] * toRad, rdeg[1] * toRad, rdeg[2] * toRad));
   for (int c = 0; c < 3; c++)
     for (int k = 0; k < 4; k++) r.m[c * 4 + k] = r.m[c * 4 + k] * s[c];
   return r;
 }
-// Inverse of a 4x4 by cofactor expansion (glm::inverse computes the same adjugate / det).
+// glm::inverse for a 4x4 (glm's func_matrix.inl, compute_inverse), which InstancedModel's
+// constructor calls (primitives/InstancedModel.cpp:11-16): 18 2x2 minors, the cofactor columns
+// with alternating signs, the determinant as (d0 + d1) + (d2 + d3) of the first column times the
+// first cofactor row, and every element times its reciprocal. Same operations in the same order,
+// so the same bits (including the signs of zero elements).
 M4 inverse(const M4& a) {
-  const float* m = a.m;
-  float inv[16];
-  inv[0] = m[5] * m[10] * m[15] - m[5] * m[11] * m[14] - m[9] * m[6] * m[15] + m[9] * m[7] * m[14] + m[13] * m[6] * m[11] - m[13] * m[7] * m[10];
-  inv[4] = -m[4] * m[10] * m[15] + m[4] * m[11] * m[14] + m[8] * m[6] * m[15] - m[8] * m[7] * m[14] - m[12] * m[6] * m[11] + m[12] * m[7] * m[10];
-  inv[8] = m[4] * m[9] * m[15] - m[4] * m[11] * m[13] - m[8] * m[5] * m[15] + m[8] * m[7] * m[13] + m[12] * m[5] * m[11] - m[12] * m[7] * m[9];
-  inv[12] = -m[4] * m[9] * m[14] + m[4] * m[10] * m[13] + m[8] * m[5] * m[14] - m[8] * m[6] * m[13] - m[12] * m[5] * m[10] + m[12] * m[6] * m[9];
-  inv[1] = -m[1] * m[10] * m[15] + m[1] * m[11] * m[14] + m[9] * m[2] * m[15] - m[9] * m[3] * m[14] - m[13] * m[2] * m[11] + m[13] * m[3] * m[10];
-  inv[5] = m[0] * m[10] * m[15] - m[0] * m[11] * m[14] - m[8] * m[2] * m[15] + m[8] * m[3] * m[14] + m[12] * m[2] * m[11] - m[12] * m[3] * m[10];
-  inv[9] = -m[0] * m[9] * m[15] + m[0] * m[11] * m[13] + m[8] * m[1] * m[15] - m[8] * m[3] * m[13] - m[12] * m[1] * m[11] + m[12] * m[3] * m[9];
-  inv[13] = m[0] * m[9] * m[14] - m[0] * m[10] * m[13] - m[8] * m[1] * m[14] + m[8] * m[2] * m[13] + m[12] * m[1] * m[10] - m[12] * m[2] * m[9];
-  inv[2] = m[1] * m[6] * m[15] - m[1] * m[7] * m[14] - m[5] * m[2] * m[15] + m[5] * m[3] * m[14] + m[13] * m[2] * m[7] - m[13] * m[3] * m[6];
-  inv[6] = -m[0] * m[6] * m[15] + m[0] * m[7] * m[14] + m[4] * m[2] * m[15] - m[4] * m[3] * m[14] - m[12] * m[2] * m[7] + m[12] * m[3] * m[6];
-  inv[10] = m[0] * m[5] * m[15] - m[0] * m[7] * m[13] - m[4] * m[1] * m[15] + m[4] * m[3] * m[13] + m[12] * m[1] * m[7] - m[12] * m[3] * m[5];
-  inv[14] = -m[0] * m[5] * m[14] + m[0] * m[6] * m[13] + m[4] * m[1] * m[14] - m[4] * m[2] * m[13] - m[12] * m[1] * m[6] + m[12] * m[2] * m[5];
-  inv[3] = -m[1] * m[6] * m[11] + m[1] * m[7] * m[10] + m[5] * m[2] * m[11] - m[5] * m[3] * m[10] - m[9] * m[2] * m[7] + m[9] * m[3] * m[6];
-  inv[7] = m[0] * m[6] * m[11] - m[0] * m[7] * m[10] - m[4] * m[2] * m[11] + m[4] * m[3] * m[10] + m[8] * m[2] * m[7] - m[8] * m[3] * m[6];
-  inv[11] = -m[0] * m[5] * m[11] + m[0] * m[7] * m[9] + m[4] * m[1] * m[11] - m[4] * m[3] * m[9] - m[8] * m[1] * m[7] + m[8] * m[3] * m[5];
-  inv[15] = m[0] * m[5] * m[10] - m[0] * m[6] * m[9] - m[4] * m[1] * m[10] + m[4] * m[2] * m[9] + m[8] * m[1] * m[6] - m[8] * m[2] * m[5];
-  float det = m[0] * inv[0] + m[1] * inv[4] + m[2] * inv[8] + m[3] * inv[12];
+  auto m = [&](int c, int r) { return a.at(r, c); };  // glm's m[column][row]
+  float c00 = m(2, 2) * m(3, 3) - m(3, 2) * m(2, 3);
+  float c02 = m(1, 2) * m(3, 3) - m(3, 2) * m(1, 3);
+  float c03 = m(1, 2) * m(2, 3) - m(2, 2) * m(1, 3);
+  float c04 = m(2, 1) * m(3, 3) - m(3, 1) * m(2, 3);
+  float c06 = m(1, 1) * m(3, 3) - m(3, 1) * m(1, 3);
+  float c07 = m(1, 1) * m(2, 3) - m(2, 1) * m(1, 3);
+  float c08 = m(2, 1) * m(3, 2) - m(3, 1) * m(2, 2);
+  float c10 = m(1, 1) * m(3, 2) - m(3, 1) * m(1, 2);
+  float c11 = m(1, 1) * m(2, 2) - m(2, 1) * m(1, 2);
+  float c12 = m(2, 0) * m(3, 3) - m(3, 0) * m(2, 3);
+  float c14 = m(1, 0) * m(3, 3) - m(3, 0) * m(1, 3);
+  float c15 = m(1, 0) * m(2, 3) - m(2, 0) * m(1, 3);
+  float c16 = m(2, 0) * m(3, 2) - m(3, 0) * m(2, 2);
+  float c18 = m(1, 0) * m(3, 2) - m(3, 0) * m(1, 2);
+  float c19 = m(1, 0) * m(2, 2) - m(2, 0) * m(1, 2);
+  float c20 = m(2, 0) * m(3, 1) - m(3, 0) * m(2, 1);
+  float c22 = m(1, 0) * m(3, 1) - m(3, 0) * m(1, 1);
+  float c23 = m(1, 0) * m(2, 1) - m(2, 0) * m(1, 1);
+  const float fac[6][4] = {{c00, c00, c02, c03}, {c04, c04, c06, c07}, {c08, c08, c10, c11},
+                           {c12, c12, c14, c15}, {c16, c16, c18, c19}, {c20, c20, c22, c23}};
+  float vec[4][4];  // vec[j] = (m[1][j], m[0][j], m[0][j], m[0][j])
+  for (int j = 0; j < 4; j++) {
+    vec[j][0] = m(1, j);
+    vec[j][1] = vec[j][2] = vec[j][3] = m(0, j);
+  }
+  // Inv0 = Vec1 Fac0 - Vec2 Fac1 + Vec3 Fac2, Inv1 = Vec0 Fac0 - Vec2 Fac3 + Vec3 Fac4,
+  // Inv2 = Vec0 Fac1 - Vec1 Fac3 + Vec3 Fac5, Inv3 = Vec0 Fac2 - Vec1 Fac4 + Vec2 Fac5
+  const int va[4] = {1, 0, 0, 0}, fa[4] = {0, 0, 1, 2};
+  const int vb[4] = {2, 2, 1, 1}, fb[4] = {1, 3, 3, 4};
+  const int vc[4] = {3, 3, 3, 2}, fc[4] = {2, 4, 5, 5};
+  float inv[4][4];  // [column][row]
+  for (int c = 0; c < 4; c++) {
+    float sign0 = (c % 2 == 0) ? 1.0f : -1.0f;  // SignA = (+,-,+,-), SignB = (-,+,-,+)
+    for (int k = 0; k < 4; k++) {
+      float v = (vec[va[c]][k] * fac[fa[c]][k] - vec[vb[c]][k] * fac[fb[c]][k]) + vec[vc[c]][k] * fac[fc[c]][k];
+      float sign = (k % 2 == 0) ? sign0 : -sign0;
+      inv[c][k] = v * sign;
+    }
+  }
+  float d0 = m(0, 0) * inv[0][0], d1 = m(0, 1) * inv[1][0], d2 = m(0, 2) * inv[2][0], d3 = m(0, 3) * inv[3][0];
+  float det = (d0 + d1) + (d2 + d3);
   float od = 1.0f / det;
   M4 r;
-  for (int i = 0; i < 16; i++) r.m[i] = inv[i] * od;
+  for (int c = 0; c < 4; c++)
+    for (int k = 0; k < 4; k++) r.at(k, c) = inv[c][k] * od;
   return r;
 }
 
@@ -636,7 +673,9 @@ struct Reader {
         mi = (uint32_t)S.models.size() - 1;
         objModels[key] = mi;
       }
-      addInstance(getTransform(pos, rot, scale), mi, collision, false);
+      // SceneReader.cpp:262-263 does not pass "collision" on to model instances
+      // (InstancedModel::isCollisionEnabled keeps its default, true)
+      addInstance(getTransform(pos, rot, scale), mi, true, false);
     } else if (type == "gltf") {
       throw ParseError(NE_ERR_UNSUPPORTED, ctx + ": gltf models are not supported (obj only).");
     } else {

@@ -80,10 +80,10 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
 __device__ __forceinline__ void mbar_fence_init() {
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
-// Polls the barrier's phase `parity`; false if it did not complete within kTcMaxPolls polls.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// Polls the barrier's phase `parity`; false if it did not complete within `max_polls` polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t max_polls = kTcMaxPolls) {
   uint32_t a = smem_u32(bar);
-  for (uint32_t i = 0; i < kTcMaxPolls; i++) {
+  for (uint32_t i = 0; i < max_polls; i++) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred P1;\n mbarrier.try_wait.parity.shared::cta.b64 P1, [%1], %2;\n selp.b32 %0, 1, 0, P1;\n}\n"

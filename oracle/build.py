@@ -1,7 +1,9 @@
 """Builds the CPU oracle (liboracle.so) from oracle.cpp.
 
 Test infrastructure: the oracle checks the GPU library and times the CPU baseline; the
-product never loads it. Compiled like the reference's Release build (-O2, no fast-math,
+product never loads it. inputs.cpp adds the seeded generators of the synthetic grids and
+meshes (a separate copy of the library's scene_gen.cpp, compiled in here) for the oracle's
+own scene reader, so that a process using the oracle never loads the GPU library. Compiled like the reference's Release build (-O2, no fast-math,
 no -march=native) with -ffp-contract=off so that no multiply-add is fused, which keeps
 every float operation identical to the GPU code compiled with -fmad=false.
 
@@ -17,8 +19,10 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 LIB = os.path.join(HERE, "liboracle.so")
-SOURCES = [os.path.join(HERE, "oracle.cpp")]
+SOURCES = [os.path.join(HERE, "oracle.cpp"), os.path.join(HERE, "inputs.cpp"),
+           os.path.join(ROOT, "narvalengine_gb300", "csrc", "scene_gen.cpp")]
 DEPS = SOURCES + [
+    os.path.join(ROOT, "narvalengine_gb300", "csrc", "scene_gen.h"),
     os.path.join(HERE, "oracle.h"),
     os.path.join(ROOT, "narvalengine_gb300", "csrc", "ne_fmath.h"),
     os.path.join(ROOT, "narvalengine_gb300", "csrc", "ne_rng.h"),

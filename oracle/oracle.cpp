@@ -1438,6 +1438,33 @@ double orc_render_pixels(const orc_scene* s, const ne_render_params* p, uint32_t
   return std::chrono::duration<double>(t1 - t0).count();
 }
 
+// Renders the listed pixels (all spp each), as renderTile does for the pixels of a tile
+// (core/OfflineEngine.cpp:54-76); chunks of 64 pixels are taken from a shared counter, as the
+// reference's threads take tiles. Returns wall seconds.
+double orc_render_pixel_list(const orc_scene* s, const ne_render_params* p, const uint32_t* pixels, uint32_t n_pixels,
+                             float* out, int n_threads, uint64_t* density_lookups) {
+  Params P = makeParams(*s, p);
+  int spp = (p && p->spp > 0) ? p->spp : s->d.settings.spp;
+  uint32_t off = p ? p->sample_offset : 0;
+  std::atomic<uint64_t> lookups(0);
+  auto t0 = std::chrono::steady_clock::now();
+  parallelFor(n_pixels, n_threads, [&](size_t b, size_t e) {
+    Ctx c{*s, Sampler{}, 0};
+    for (size_t i = b; i < e; i++) {
+      V3 color = v3(0, 0, 0);
+      for (int k = 0; k < spp; k++) color = color + cameraPath(c, P, pixels[i], off + (uint32_t)k);
+      color = color / (float)spp;
+      out[i * 3 + 0] = color.x;
+      out[i * 3 + 1] = color.y;
+      out[i * 3 + 2] = color.z;
+    }
+    lookups.fetch_add(c.lookups);
+  });
+  auto t1 = std::chrono::steady_clock::now();
+  if (density_lookups) *density_lookups = lookups.load();
+  return std::chrono::duration<double>(t1 - t0).count();
+}
+
 // core/OfflineEngine.cpp:54-113: tiles of (W/40) x (H/10) pixels taken from a shared
 // counter by n_threads threads (the reference's busy-polled pool of 16 threads).
 double orc_render(const orc_scene* s, const ne_render_params* p, float* out, int n_threads) {

@@ -44,6 +44,9 @@ double orc_render(const orc_scene* s, const ne_render_params* p, float* out_rgb,
 /* Renders only pixels [pixel_begin, pixel_begin + n_pixels) (all spp), returns seconds. */
 double orc_render_pixels(const orc_scene* s, const ne_render_params* p, uint32_t pixel_begin, uint32_t n_pixels,
                          float* out_rgb, int n_threads, uint64_t* density_lookups);
+/* Renders the listed pixels (all spp each) into out_rgb (3 floats per listed pixel). */
+double orc_render_pixel_list(const orc_scene* s, const ne_render_params* p, const uint32_t* pixels, uint32_t n_pixels,
+                             float* out_rgb, int n_threads, uint64_t* density_lookups);
 void orc_trace_closest(const orc_scene* s, const ne_ray* rays, size_t n, float t_min, float t_max, ne_hit* out);
 
 /* BVH::init result of model m: 9 words per node (min, max, start, count, rightOffset). */
@@ -76,6 +79,13 @@ uint32_t orc_bvh_build_count(const float* verts, const uint32_t* idx, uint32_t n
 void orc_fmath(int fn, const float* x, size_t n, float* out);
 void orc_rng(uint64_t seed, const ne_path_key* keys, const uint32_t* dims, size_t n, float* out);
 void orc_philox(const uint32_t* ctr, const uint32_t* key, uint32_t* out);
+
+/* Seeded synthetic inputs (inputs.cpp) for the oracle's own scene reader. */
+void orc_gen_fbm(const uint32_t res[3], int octaves, double frequency, double lacunarity, double gain,
+                 double falloff_radius, uint64_t seed, float* out);
+void orc_gen_icosphere(int subdivisions, double amplitude, double frequency, uint64_t seed, float* positions,
+                       uint32_t* indices);
+double orc_gen_hash_u01(uint64_t seed, uint64_t i);
 
 #ifdef __cplusplus
 }

@@ -37,6 +37,8 @@ SIGNATURES = {
     "orc_render": (C.c_double, [C.c_void_p, C.POINTER(NeRenderParams), C.c_void_p, C.c_int]),
     "orc_render_pixels": (C.c_double, [C.c_void_p, C.POINTER(NeRenderParams), C.c_uint32, C.c_uint32, C.c_void_p,
                                        C.c_int, C.POINTER(C.c_uint64)]),
+    "orc_render_pixel_list": (C.c_double, [C.c_void_p, C.POINTER(NeRenderParams), C.c_void_p, C.c_uint32,
+                                           C.c_void_p, C.c_int, C.POINTER(C.c_uint64)]),
     "orc_trace_closest": (None, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_float, C.c_float, C.c_void_p]),
     "orc_triangle_intersect": (C.c_int, [_F, _F, _F, C.c_void_p, _F, _F, _F, _F]),
     "orc_aabb_intersect": (C.c_int, [_F, _F, C.c_void_p, _F, _F, _F, _F]),
@@ -57,6 +59,10 @@ SIGNATURES = {
     "orc_fmath": (None, [C.c_int, C.c_void_p, C.c_size_t, C.c_void_p]),
     "orc_rng": (None, [C.c_uint64, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
     "orc_philox": (None, [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
+    "orc_gen_fbm": (None, [C.POINTER(C.c_uint32), C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                           C.c_uint64, C.c_void_p]),
+    "orc_gen_icosphere": (None, [C.c_int, C.c_double, C.c_double, C.c_uint64, C.c_void_p, C.c_void_p]),
+    "orc_gen_hash_u01": (C.c_double, [C.c_uint64, C.c_uint64]),
 }
 
 
@@ -96,6 +102,19 @@ class OracleScene:
             raise RuntimeError("orc_scene_create failed")
         self.width = desc_ptr.contents.settings.width
         self.height = desc_ptr.contents.settings.height
+        self.spp = desc_ptr.contents.settings.spp
+        self.bounces = desc_ptr.contents.settings.bounces
+
+    @classmethod
+    def from_json(cls, path: str | None = None, text: str | None = None,
+                  resources_dir: str | None = None) -> "OracleScene":
+        """The oracle's scene read from the reference's JSON descriptor by the oracle's own
+        reader (scene_reader.py), independently of the library's reader."""
+        from oracle.scene_reader import OracleSceneDesc
+        sd = OracleSceneDesc(path, text, resources_dir)
+        o = cls(sd.desc_ptr)
+        o.reader = sd
+        return o
 
     def trace_paths(self, keys: np.ndarray, params: NeRenderParams, threads: int = 0) -> np.ndarray:
         keys = np.ascontiguousarray(keys, dtype=np.uint32).reshape(-1, 2)
@@ -145,6 +164,15 @@ class OracleScene:
         lookups = C.c_uint64(0)
         secs = self._lib.orc_render_pixels(self._h, C.byref(params), first, count, _p(out),
                                            threads or os.cpu_count(), C.byref(lookups))
+        return out, secs, lookups.value
+
+    def render_pixel_list(self, params: NeRenderParams, pixels: np.ndarray, threads: int = 0):
+        """Mean radiance of the listed pixels (all spp each): (out, seconds, density lookups)."""
+        pixels = np.ascontiguousarray(pixels, dtype=np.uint32)
+        out = np.zeros((len(pixels), 3), dtype=np.float32)
+        lookups = C.c_uint64(0)
+        secs = self._lib.orc_render_pixel_list(self._h, C.byref(params), _p(pixels), len(pixels), _p(out),
+                                               threads or os.cpu_count(), C.byref(lookups))
         return out, secs, lookups.value
 
     def trace_closest(self, rays: np.ndarray, t_min: float, t_max: float) -> np.ndarray:

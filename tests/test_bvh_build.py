@@ -15,7 +15,8 @@ def test_parallel_build_equals_reference_build(built, oracle_lib, subdiv):
     import narvalengine_gb300 as ne
     d = json.load(open(scene_path("mesh_c3")))
     d["primitives"][0]["subdivisions"] = subdiv
-    host = ne.SceneHost.from_string(json.dumps(d))
+    text = json.dumps(d)
+    host = ne.SceneHost.from_string(text)
     desc = host.desc
     m = next(i for i in range(desc.n_models) if desc.models[i].use_bvh and desc.models[i].prim_count > 4)
     model = desc.models[m]
@@ -29,7 +30,7 @@ def test_parallel_build_equals_reference_build(built, oracle_lib, subdiv):
     t_lib = time.perf_counter() - t0
     assert st == 0
     nodes = nodes[:count.value]
-    orc = oracle_lib.OracleScene(host.desc_ptr)
+    orc = oracle_lib.OracleScene.from_json(text=text)
     try:
         ref_nodes, ref_order = orc.model_bvh(m, n)
     finally:

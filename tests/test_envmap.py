@@ -97,8 +97,9 @@ def test_envmap_le_of_escaping_rays(built, oracle_lib, tmp_path):
     import narvalengine_gb300 as ne
     texels = write_sky(tmp_path)
     rot = (20, 35, 0)
-    host = ne.SceneHost.from_string(scene_json([], sky_rot=rot), str(tmp_path))
-    orc = oracle_lib.OracleScene(host.desc_ptr)
+    text = scene_json([], sky_rot=rot)
+    host = ne.SceneHost.from_string(text, str(tmp_path))
+    orc = oracle_lib.OracleScene.from_json(text=text, resources_dir=str(tmp_path))
     try:
         rng = np.random.default_rng(5)
         d = rng.normal(size=(20000, 3))
@@ -131,8 +132,9 @@ def env_scenes(built, oracle_lib, tmp_path_factory):
     ctx = ne.Context(0)
     out = []
     for name, prims, medium in (("surface", SURFACE, False), ("medium", MEDIUM, True)):
-        host = ne.SceneHost.from_string(scene_json(prims, medium=medium), str(tmp))
-        out.append((name, host, ctx.upload(host), oracle_lib.OracleScene(host.desc_ptr)))
+        text = scene_json(prims, medium=medium)
+        host = ne.SceneHost.from_string(text, str(tmp))
+        out.append((name, host, ctx.upload(host), oracle_lib.OracleScene.from_json(text=text, resources_dir=str(tmp))))
     yield ne, out
     for _, _, _, orc in out:
         orc.close()

@@ -39,7 +39,7 @@ def scenes(request, ne, ctx, oracle_lib):
     host = ne.SceneHost.from_json(scene_path(name))
     scene = ctx.upload(host)
     scene.set_tuning(kernel=kernel)
-    orc = oracle_lib.OracleScene(host.desc_ptr)
+    orc = oracle_lib.OracleScene.from_json(scene_path(name))
     yield name, host, scene, orc
     scene.close()
     orc.close()
@@ -157,11 +157,12 @@ def test_render_ref_tiles(ne, ctx, oracle_lib):
     import json
     d = json.load(open(scene_path("cornell_c1")))
     d["renderer"]["resolution"] = [250, 130]
-    host = ne.SceneHost.from_string(json.dumps(d))
+    text = json.dumps(d)
+    host = ne.SceneHost.from_string(text)
     scene = ctx.upload(host)
     p = ne.render_params(seed=1, spp=1, flags=ne.NE_RENDER_REF_TILES)
     g, stats = scene.render(p)
-    c, _ = oracle_lib.OracleScene(host.desc_ptr).render(p)
+    c, _ = oracle_lib.OracleScene.from_json(text=text).render(p)
     assert stats["paths"] == 240 * 130
     assert np.all(g[:, 240:] == 0)
     assert np.array_equal(g, c)
@@ -242,9 +243,10 @@ def mesh_scene_json(subdivisions):
 def test_mesh_bvh_parity(ne, ctx, oracle_lib, subdivisions):
     """Triangle meshes through the reference's midpoint BVH (BVH.cpp:6-193): hits bit-exact,
     camera paths bit-identical, on a small mesh and on the 1.3 M-triangle icosphere."""
-    host = ne.SceneHost.from_string(mesh_scene_json(subdivisions))
+    text = mesh_scene_json(subdivisions)
+    host = ne.SceneHost.from_string(text)
     scene = ctx.upload(host)
-    orc = oracle_lib.OracleScene(host.desc_ptr)
+    orc = oracle_lib.OracleScene.from_json(text=text)
     rays = camera_rays(host, 20000, 11)
     g = scene.trace_closest(rays, 1e-11, float("inf"))
     c = orc.trace_closest(rays, 1e-11, float("inf"))
@@ -271,9 +273,10 @@ def test_mesh_and_medium_parity(ne, ctx, oracle_lib):
             p["subdivisions"] = 4
     d["renderer"]["resolution"] = [96, 72]
     d["renderer"]["bvh"] = "reference"
-    host = ne.SceneHost.from_string(json.dumps(d))
+    text = json.dumps(d)
+    host = ne.SceneHost.from_string(text)
     scene = ctx.upload(host)
-    orc = oracle_lib.OracleScene(host.desc_ptr)
+    orc = oracle_lib.OracleScene.from_json(text=text)
     try:
         keys = spread_keys(host, 1024, 4, seed=5)
         cp = orc.trace_paths(keys, ne.render_params(seed=12))
@@ -321,9 +324,10 @@ def test_dense_cloud_parity(ne, ctx, oracle_lib):
     import json
     d = json.load(open(scene_path("cloud_c4")))
     d["renderer"]["resolution"] = [96, 96]
-    host = ne.SceneHost.from_string(json.dumps(d))
+    text = json.dumps(d)
+    host = ne.SceneHost.from_string(text)
     scene = ctx.upload(host)
-    orc = oracle_lib.OracleScene(host.desc_ptr)
+    orc = oracle_lib.OracleScene.from_json(text=text)
     try:
         keys = spread_keys(host, 2048, 2, seed=4)
         p = ne.render_params(seed=21)
@@ -347,7 +351,7 @@ def test_split_queue_overflow(ne, ctx, oracle_lib):
     host = ne.SceneHost.from_json(scene_path("medium_c2"))
     scene = ctx.upload(host)
     scene.set_tuning(kernel=3)
-    orc = oracle_lib.OracleScene(host.desc_ptr)
+    orc = oracle_lib.OracleScene.from_json(scene_path("medium_c2"))
     try:
         centre = (host.height // 2) * host.width + host.width // 2
         keys = np.array([[centre, s] for s in range(8192)], np.uint32)

@@ -16,14 +16,18 @@ import numpy as np
 from conftest import scene_path
 
 
-def mixed_host(ne):
+def mixed_json():
     d = json.load(open(scene_path("views_c5")))
     for p in d["primitives"]:
         if p.get("type") == "mesh":
             p["subdivisions"] = 3
     d["renderer"]["resolution"] = [64, 48]
     d["renderer"]["bvh"] = "reference"
-    return ne.SceneHost.from_string(json.dumps(d))
+    return json.dumps(d)
+
+
+def mixed_host(ne):
+    return ne.SceneHost.from_string(mixed_json())
 
 
 def medium_boxes(ne, host):
@@ -107,7 +111,7 @@ def test_medium_boxes_cover_oracle_hits(built, oracle_lib):
     o = np.concatenate([origins, leave_o, origins]).astype(np.float32)
     d = np.concatenate([aimed_d, leave_d, rand_d]).astype(np.float32)
 
-    orc = oracle_lib.OracleScene(host.desc_ptr)
+    orc = oracle_lib.OracleScene.from_json(text=mixed_json())
     try:
         hits = orc.trace_closest(np.concatenate([o, d], 1), 1e-3, float("inf"))
     finally:

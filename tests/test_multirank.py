@@ -40,9 +40,8 @@ def worker(rank, world, port, out_dir):
     import narvalengine_gb300 as ne
     from oracle import oracle as orc
     d = bench.Dist(world, "gloo")
-    host = ne.SceneHost.from_string(small_scene_json())
-    o = orc.OracleScene(host.desc_ptr)
-    spp = host.spp
+    o = orc.OracleScene.from_json(text=small_scene_json())
+    spp = o.spp
     img, secs = o.render(ne.render_params(seed=4, spp=spp, sample_offset=rank * spp), threads=1)
     d.barrier()
     slowest = d.max(float(rank + 1))
@@ -62,6 +61,6 @@ def test_two_ranks_split_samples(tmp_path, built):
     assert np.load(tmp_path / "max.npy")[0] == 2.0
     import narvalengine_gb300 as ne
     from oracle import oracle as orc
-    host = ne.SceneHost.from_string(small_scene_json())
-    full, _ = orc.OracleScene(host.desc_ptr).render(ne.render_params(seed=4, spp=2 * host.spp), threads=1)
+    o = orc.OracleScene.from_json(text=small_scene_json())
+    full, _ = o.render(ne.render_params(seed=4, spp=2 * o.spp), threads=1)
     assert np.allclose(total / world, full, rtol=1e-5, atol=1e-6)

@@ -84,8 +84,8 @@ def test_reference_bvh_cube_intersections(built, oracle_lib, tmp_path):
     """tests.cpp:866-889: a ray from (0,0,-2) along +z and one from the centre along +z both hit
     the cube at t = 1 (the faces behind the origin are rejected by the triangle test)."""
     import narvalengine_gb300 as ne
-    host = ne.SceneHost.from_string(scene(tmp_path, [obj("cube", "grey", [0, 0, 0])]), str(tmp_path))
-    orc = oracle_lib.OracleScene(host.desc_ptr)
+    text = scene(tmp_path, [obj("cube", "grey", [0, 0, 0])])
+    orc = oracle_lib.OracleScene.from_json(text=text, resources_dir=str(tmp_path))
     try:
         rays = np.array([[0, 0, -2, 0, 0, 1], [0, 0, 0, 0, 0, 1]], np.float32)
         h = orc.trace_closest(rays, 1e-11, float("inf"))
@@ -98,10 +98,11 @@ def test_reference_bvh_cube_intersections(built, oracle_lib, tmp_path):
 @pytest.mark.gpu
 def test_obj_scene_parity(built, oracle_lib, tmp_path):
     import narvalengine_gb300 as ne
-    host = ne.SceneHost.from_string(scene(tmp_path, [obj("a", "grey", [-1.5, 0, 0]), obj("b", "grey", [1.5, 0, 0], 0.5, 30),
-                                                     obj("c", "red", [0, 0, 2])]), str(tmp_path))
+    text = scene(tmp_path, [obj("a", "grey", [-1.5, 0, 0]), obj("b", "grey", [1.5, 0, 0], 0.5, 30),
+                            obj("c", "red", [0, 0, 2])])
+    host = ne.SceneHost.from_string(text, str(tmp_path))
     ctx = ne.Context(0)
-    orc = oracle_lib.OracleScene(host.desc_ptr)
+    orc = oracle_lib.OracleScene.from_json(text=text, resources_dir=str(tmp_path))
     try:
         gpu_scene = ctx.upload(host)
         for kernel in (0, 3):

@@ -1,0 +1,207 @@
+"""The oracle's own scene reader against the library's, field by field (CPU).
+
+Both read the reference's JSON descriptor (io/SceneReader.cpp) on their own: the library in
+C++ (scene_host.cpp), the oracle in Python from the reference's files and glm's published
+algorithms (oracle/scene_reader.py). The parity tests give the GPU the library's scene and the
+oracle its own, so any difference in reading would also fail them; this test names the field.
+Every float is compared bit for bit, signs of zero included.
+"""
+import ctypes as C
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import scene_path
+from test_image_load import encode_png
+
+
+@pytest.fixture(scope="module")
+def ne(built):
+    import narvalengine_gb300 as ne
+    return ne
+
+
+def _bytes(ptr, i, typ):
+    return bytes((C.c_char * C.sizeof(typ)).from_address(C.addressof(ptr.contents) + i * C.sizeof(typ)))
+
+
+def assert_same_desc(a, b):
+    from narvalengine_gb300 import _abi
+    assert (a.n_instances, a.n_light_instances) == (b.n_instances, b.n_light_instances)
+    tables = [("instances", _abi.NeInstance, a.n_instances + a.n_light_instances),
+              ("models", _abi.NeModel, a.n_models), ("prims", _abi.NePrimitive, a.n_prims),
+              ("materials", _abi.NeMaterial, a.n_materials), ("model_materials", C.c_uint32, a.n_model_materials),
+              ("media", None, a.n_media), ("lights", None, a.n_lights)]
+    for name, typ, n in tables:
+        nb = {"instances": b.n_instances + b.n_light_instances}.get(name, getattr(b, "n_" + name, None))
+        assert n == nb, f"{name}: {n} vs {nb}"
+        if typ is None or n == 0:
+            continue
+        if name == "prims":
+            x = np.frombuffer((C.c_char * (n * C.sizeof(typ))).from_address(C.addressof(a.prims.contents)), np.uint32)
+            y = np.frombuffer((C.c_char * (n * C.sizeof(typ))).from_address(C.addressof(b.prims.contents)), np.uint32)
+            bad = np.nonzero(x != y)[0]
+            assert bad.size == 0, f"prims differ at primitive {bad[0] * 4 // C.sizeof(typ)}"
+            continue
+        for i in range(n):
+            assert _bytes(getattr(a, name), i, typ) == _bytes(getattr(b, name), i, typ), f"{name}[{i}] differs"
+    for i in range(a.n_lights):
+        la, lb = a.lights[i], b.lights[i]
+        for f in ("type", "primitive", "env_width", "env_height"):
+            assert getattr(la, f) == getattr(lb, f), f"lights[{i}].{f}"
+        for f in ("li", "le", "direction", "env_radiance"):
+            assert bytes(getattr(la, f)) == bytes(getattr(lb, f)), f"lights[{i}].{f}"
+        assert np.float32(la.env_map_pdf).tobytes() == np.float32(lb.env_map_pdf).tobytes()
+        if la.env_width:
+            n = la.env_width * la.env_height * 4
+            assert C.string_at(la.env_texels, n) == C.string_at(lb.env_texels, n), f"lights[{i}] texels"
+    for i in range(a.n_media):
+        ma, mb = a.media[i], b.media[i]
+        for f in ("type", "density"):
+            assert getattr(ma, f) == getattr(mb, f), f"media[{i}].{f}"
+        for f in ("sigma_s", "sigma_a", "res"):
+            assert bytes(getattr(ma, f)) == bytes(getattr(mb, f)), f"media[{i}].{f}"
+        if ma.type == 0:
+            n = ma.res[0] * ma.res[1] * ma.res[2]
+            assert C.string_at(ma.grid, 4 * n) == C.string_at(mb.grid, 4 * n), f"media[{i}] grid"
+    assert bytes(a.camera) == bytes(b.camera), "camera"
+    assert bytes(a.settings) == bytes(b.settings), "settings"
+
+
+@pytest.mark.parametrize("name", ["cornell_c1", "medium_c2", "mesh_c3", "views_c5"])
+def test_shipped_scenes(ne, oracle_lib, name):
+    from oracle.scene_reader import OracleSceneDesc
+    host = ne.SceneHost.from_json(scene_path(name))
+    o = OracleSceneDesc(scene_path(name))
+    assert_same_desc(host.desc, o.desc)
+
+
+def test_cloud_scene_small_grid(ne, oracle_lib):
+    """The dense-cloud descriptor with its grid at 64^3 (the full 512^3 takes a minute per side)."""
+    from oracle.scene_reader import OracleSceneDesc
+    d = json.load(open(scene_path("cloud_c4")))
+    d["materials"][0]["grid"]["resolution"] = [64, 64, 64]
+    d["materials"][0]["grid"]["falloff_radius"] = 32
+    text = json.dumps(d)
+    host = ne.SceneHost.from_string(text)  # each reader owns the memory its description points into
+    o = OracleSceneDesc(text=text)
+    assert_same_desc(host.desc, o.desc)
+
+
+def varied_scene(tmp_path):
+    """Every descriptor feature the readers share: rotations about several axes, non-uniform
+    scales, negative and fractional positions, every material and primitive type, .vol / raw
+    grids, a homogeneous medium, an isotropic phase function, emitting spheres and points, OBJ
+    models shared between instances, inline and generated meshes, a textured environment map."""
+    res = 5
+    g = np.random.default_rng(2).random(res ** 3).astype(np.float32)
+    with open(tmp_path / "d.vol", "w") as f:
+        f.write(f"{res} {res} {res} \n")
+        f.write("skipped line\n")
+        f.write(" ".join(repr(float(x)) for x in g) + " \n")
+    g.tofile(tmp_path / "d.f32")
+    (tmp_path / "quad.obj").write_text("# quad\nv -1 0 -1\nv 1 0 -1\nv 1 0.25 1\nv -1 0 1\nf 1 2/5 3//1 4/1/2\n"
+                                       "f -4 -3 -1\n")
+    sky = np.random.default_rng(3).integers(0, 256, size=(8, 16, 3), dtype=np.uint8)
+    (tmp_path / "sky.png").write_bytes(encode_png(sky, 2, 8))
+    T = lambda p, r=(0, 0, 0), s=(1, 1, 1): {"position": list(p), "rotation": list(r), "scale": list(s)}
+    mats = [
+        {"name": "white", "type": "microfacet", "roughness": 0.37, "metallic": 0.2, "albedo": [0.7, 0.61, 0.05]},
+        {"name": "bumpy", "type": "microfacet", "roughness": 0.8, "metallic": 0.0, "albedo": [0.3, 0.3, 0.3],
+         "normalMap": [0.5, 0.5, 1.0]},
+        {"name": "lamp", "type": "emitter", "albedo": [5.0, 4.5, 3.1]},
+        {"name": "ball_lamp", "type": "emitter", "albedo": [2.0, 2.5, 1.0]},
+        {"name": "point_lamp", "type": "emitter", "albedo": [1.0, 1.0, 1.0]},
+        {"name": "sun", "type": "directionalLight", "albedo": [2.0, 2.0, 2.0], "position": [0.3, 0.8, -0.41]},
+        {"name": "sky", "type": "infiniteAreaLight", "path": "sky.png"},
+        {"name": "fog", "type": "volume", "scattering": [0.5, 0.4, 0.3], "absorption": [0.01, 0.02, 0.03],
+         "phaseFunction": "isotropic", "density": 0.7},
+        {"name": "vol", "type": "volume", "scattering": [0.9, 0.9, 0.9], "absorption": [0.1, 0.1, 0.1],
+         "phaseFunction": "henyey-greenstein", "g": -0.3, "density": 3.5, "path": "d.vol"},
+        {"name": "raw", "type": "volume", "scattering": [0.8, 0.8, 0.8], "absorption": [0.2, 0.2, 0.2],
+         "phaseFunction": "hg", "g": 0.6, "density": 12,
+         "grid": {"path": "d.f32", "resolution": [res, res, res]}},
+        {"name": "gen", "type": "volume", "scattering": [0.8, 0.8, 0.8], "absorption": [0.2, 0.2, 0.2],
+         "phaseFunction": "hg", "g": 0.6, "density": 12,
+         "grid": {"generator": "fbm", "resolution": [24, 20, 16], "octaves": 3, "seed": 99}},
+    ]
+    prims = [
+        {"name": "wall", "type": "rectangle", "transform": T((0.3, -1.25, 2), (12.5, -33, 71), (2, 3.5, 1)),
+         "materialName": "white"},
+        {"name": "wall2", "type": "rectangle", "transform": T((-0.7, 0.1, 0), (90, 0, 0), (1, 1, 1)),
+         "materialName": "bumpy"},
+        {"name": "light", "type": "rectangle", "transform": T((0, 1.99, 0.2), (-90, 5, 0), (0.5, 0.25, 1)),
+         "materialName": "lamp"},
+        {"name": "ball", "type": "sphere", "radius": 0.35, "transform": T((-0.4, 0.35, 0.3), (10, 20, 30)),
+         "materialName": "white"},
+        {"name": "ghost", "type": "sphere", "radius": 0.2, "collision": False, "transform": T((0.5, 0.5, 0.5)),
+         "materialName": "white"},
+        {"name": "ball_light", "type": "sphere", "radius": 0.1, "transform": T((0.1, 1.5, -0.3)),
+         "materialName": "ball_lamp"},
+        {"name": "pt", "type": "point", "transform": T((0.2, 1.8, 0.1), (0, 0, 0), (1, 1, 1)),
+         "materialName": "point_lamp"},
+        {"name": "sunPoint", "type": "point", "transform": T((0, 10, 0)), "materialName": "sun"},
+        {"name": "skySphere", "type": "sphere", "radius": 100, "transform": T((0, 0, 0), (20, 35, 0)),
+         "materialName": "sky"},
+        {"name": "fogBox", "type": "volume", "transform": T((1.5, 0.5, -1), (0, 45, 0), (0.5, 1, 0.75)),
+         "materialName": "fog"},
+        {"name": "volBox", "type": "volume", "transform": T((-1.5, 0.5, 1), (30, 60, 90), (1, 1, 1)),
+         "materialName": "vol"},
+        {"name": "rawBox", "type": "volume", "transform": T((0, -0.5, 1)), "materialName": "raw"},
+        {"name": "genBox", "type": "volume", "transform": T((0, 2.5, 1), (-15, 0, 5), (1.2, 0.8, 1)),
+         "materialName": "gen"},
+        {"name": "quad1", "type": "obj", "path": "quad.obj", "materialName": "white",
+         "transform": T((0, 0.01, 0), (0, 30, 0), (1, 1, 1))},
+        {"name": "quad2", "type": "obj", "path": "quad.obj", "materialName": "white", "collision": False,
+         "transform": T((0, 0.5, 0), (0, -30, 0), (0.5, 0.5, 0.5))},
+        {"name": "tri", "type": "mesh", "positions": [0, 0, 0, 1, 0, 0, 0, 1, 0.5, -0.25, 0.125, 1],
+         "indices": [0, 1, 2, 0, 2, 3], "materialName": "bumpy", "transform": T((0.1, 0.2, 0.3), (5, 6, 7))},
+        {"name": "blob", "type": "mesh", "generator": "icosphere", "subdivisions": 2,
+         "displacement": {"amplitude": 0.1, "frequency": 3, "seed": 5},
+         "groups": {"count": 7, "roughness": [0.05, 0.9], "albedo": [0.2, 0.9], "seed": 11},
+         "transform": T((-1.3, 1.1, 0), (0, 0, 0), (0.4, 0.4, 0.4))},
+    ]
+    doc = {"version": "0.0.1a", "materials": mats, "primitives": prims,
+           "camera": {"position": [0.25, 1.1, -2.6], "lookAt": [0.1, 0.9, 0], "up": [0, 1, 0], "speed": 5,
+                      "vfov": 52.5, "aperture": 0.0001, "autoFocus": False, "focus": 2.25},
+           "renderer": {"resolution": [96, 64], "spp": 3, "bounces": 7, "mode": "offline", "HDR": True,
+                        "rr": {"after": 2}, "bvh": "sah"}}
+    return json.dumps(doc)
+
+
+def test_varied_scene(ne, oracle_lib, tmp_path):
+    from oracle.scene_reader import OracleSceneDesc
+    text = varied_scene(tmp_path)
+    host = ne.SceneHost.from_string(text, str(tmp_path))
+    o = OracleSceneDesc(text=text, resources_dir=str(tmp_path))
+    assert_same_desc(host.desc, o.desc)
+    # the obj instances share one model and keep collision on, as SceneReader.cpp:245-266 does
+    d = o.desc
+    obj_inst = [d.instances[i] for i in range(d.n_instances)
+                if d.models[d.instances[i].model].use_bvh and d.models[d.instances[i].model].prim_count == 3]
+    assert len(obj_inst) == 2 and obj_inst[0].model == obj_inst[1].model
+    assert all(i.collision == 1 for i in obj_inst)
+
+
+def test_glm_inverse_and_euler(oracle_lib):
+    """The oracle's glm::inverse and eulerAngleXYZ restatements are the mathematical inverse and
+    X(t1) Y(t2) Z(t3) rotation (float64 reference, float32 tolerance)."""
+    from oracle import scene_reader as sr
+    rng = np.random.default_rng(0)
+    for _ in range(20):
+        t, r, s = rng.uniform(-3, 3, 3), rng.uniform(-180, 180, 3), rng.uniform(0.2, 3, 3)
+        M = sr.get_transform([np.float32(x) for x in t], [np.float32(x) for x in r], [np.float32(x) for x in s])
+        A = np.array([[M[c][k] for c in range(4)] for k in range(4)], np.float64)
+        a, b, c = np.radians(r.astype(np.float32).astype(np.float64))
+        Rx = np.array([[1, 0, 0], [0, np.cos(a), -np.sin(a)], [0, np.sin(a), np.cos(a)]])
+        Ry = np.array([[np.cos(b), 0, np.sin(b)], [0, 1, 0], [-np.sin(b), 0, np.cos(b)]])
+        Rz = np.array([[np.cos(c), -np.sin(c), 0], [np.sin(c), np.cos(c), 0], [0, 0, 1]])
+        ref = np.eye(4)
+        ref[:3, :3] = Rx @ Ry @ Rz @ np.diag(s.astype(np.float32))
+        ref[:3, 3] = t.astype(np.float32)
+        assert np.abs(A - ref).max() < 1e-5
+        inv = sr.inverse(M)
+        I = np.array([[inv[c][k] for c in range(4)] for k in range(4)], np.float64)
+        assert np.abs(I @ A - np.eye(4)).max() < 1e-5

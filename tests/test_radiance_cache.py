@@ -3,7 +3,8 @@
 
 Tolerances: features 5e-4 absolute (the band-0 sin/cos of the two sides differ by an ulp or two, which angle doubling amplifies up to 2^11 times); network
 outputs and gradients compare BF16 products accumulated in FP32 in different orders, so
-1e-2 of the output scale and 3e-2 relative norm per gradient tensor."""
+1e-2 of the output scale and 3e-2 relative norm per gradient tensor; against the FP64
+network, the BF16 restatement's own error (factor 1.5, plus 2^-10) bounds the GPU's."""
 import numpy as np
 import pytest
 
@@ -100,6 +101,36 @@ def test_gradients_match_oracle(cache, n):
             assert rel < 3e-2, f"layer {i} {name}: relative error {rel:.3e}"
     # apply=False leaves the parameters alone
     assert np.array_equal(cache.params(), flatten(p))
+
+
+@pytest.mark.parametrize("n", [1000, 65536])
+def test_gradients_against_fp64(cache, n):
+    """Gradients against the FP64 network (no BF16 rounding anywhere, oracle/mlp.py with
+    quant=False). Tolerance from BF16 rounding: operands carry 8 significand bits (relative
+    rounding up to 2^-9), so each tensor's error against FP64 may be what the BF16-quantised
+    restatement's own error is, within a factor 1.5 plus 2^-10 of the tensor's norm (the
+    GPU sums its FP32 partial products in another order), and never above 2^-5."""
+    from oracle import mlp
+    p = mlp.init_params(13)
+    cache.set_params(flatten(p))
+    pos, d = queries(n, 8)
+    feats = cache.encode(pos, d)
+    t = target_fn(pos, d)
+    _, g = cache.train(t, feats=feats, apply=False, want_grads=True)
+    G = unflatten(g)
+    out64, xs64, zs64 = mlp.forward(p, feats, quant=False)
+    _, gout64 = mlp.loss_and_grad_out(out64, t)
+    gW64, gb64 = mlp.backward(p, xs64, zs64, gout64, quant=False)
+    outq, xsq, zsq = mlp.forward(p, feats)
+    _, goutq = mlp.loss_and_grad_out(outq, t)
+    gWq, gbq = mlp.backward(p, xsq, zsq, goutq)
+    for i in range(5):
+        for name, a, q, ref in (("W", G["W"][i], gWq[i], gW64[i]), ("b", G["b"][i], gbq[i], gb64[i])):
+            nref = np.linalg.norm(ref) + 1e-30
+            e_gpu = np.linalg.norm(a - ref) / nref
+            e_bf16 = np.linalg.norm(q - ref) / nref
+            assert e_gpu <= 1.5 * e_bf16 + 2.0 ** -10 and e_gpu < 2.0 ** -5, \
+                f"layer {i} {name}: GPU {e_gpu:.3e} vs BF16 restatement {e_bf16:.3e} against FP64"
 
 
 def test_training_follows_oracle_and_converges(cache):

@@ -68,9 +68,10 @@ def check_tree(nodes, order, first, lo, hi):
 @pytest.mark.parametrize("subdivisions", [4, 8])
 def test_sah_tree_valid_and_parity(built, oracle_lib, subdivisions):
     import narvalengine_gb300 as ne
-    host = ne.SceneHost.from_string(mesh_json(subdivisions))
+    text = mesh_json(subdivisions)
+    host = ne.SceneHost.from_string(text)
     ctx = ne.Context(0)
-    orc = oracle_lib.OracleScene(host.desc_ptr)
+    orc = oracle_lib.OracleScene.from_json(text=text)
     try:
         scene = ctx.upload(host)
         models = [m for m in range(host.n_models) if host.model_uses_bvh(m)]

@@ -47,3 +47,33 @@ def test_mma_rejects_bad_shapes(built):
             assert ne.library().ne_debug_mma(ctx._h, z.ctypes.data, z.ctypes.data, n, k, d.ctypes.data) == -1
     finally:
         ctx.close()
+
+
+def test_bounded_wait_gives_up_and_releases_tensor_memory(built):
+    """Failure detection without a fault: a block waits on an mbarrier that nothing signals,
+    gives up after a short poll limit and reports NE_ERR_TIMEOUT; its tensor memory is
+    released, so products on the same context still run and are right afterwards (a block
+    that kept its allocation would leave the next allocations on that SM short)."""
+    import narvalengine_gb300 as ne
+    from narvalengine_gb300 import _abi
+    ctx = ne.Context(0)
+    try:
+        for polls in (1, 64, 4096):
+            st = ne.library().ne_debug_wait_timeout(ctx._h, polls)
+            assert st == _abi.NE_ERR_TIMEOUT, (polls, st, ctx.error())
+            assert "gave up" in ctx.error()
+        assert ne.library().ne_debug_wait_timeout(ctx._h, 0) == _abi.NE_ERR_INVALID_ARG
+        rng = np.random.default_rng(7)
+        for _ in range(3):
+            a = rng.normal(size=(128, 64)).astype(np.float32)
+            b = rng.normal(size=(256, 64)).astype(np.float32)
+            ab, bb = bf16_bits(a), bf16_bits(b)
+            af = (ab.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+            bf = (bb.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+            d = np.empty((128, 256), np.float32)
+            st = ne.library().ne_debug_mma(ctx._h, ab.ctypes.data, bb.ctypes.data, 256, 64, d.ctypes.data)
+            assert st == 0, ctx.error()
+            err = np.abs(d - af @ bf.T) / (np.abs(af) @ np.abs(bf).T + 1e-30)
+            assert err.max() < 1e-5
+    finally:
+        ctx.close()

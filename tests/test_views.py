@@ -35,7 +35,7 @@ def batch(request, built, oracle_lib):
         pos = [eye[0] + 0.15 * i, eye[1] + 0.05 * i, eye[2]]
         views.append((ne.camera_look_at(pos, look, 50.0 + 3 * i, w, h), w, h, spp))
     vb = ne.Views(scene, views, seed=11)
-    orc = oracle_lib.OracleScene(host.desc_ptr)
+    orc = oracle_lib.OracleScene.from_json(scene_path(request.param))
     yield ne, scene, vb, views, orc
     orc.close()
     vb.close()

@@ -76,6 +76,36 @@ def test_noalloc_matches_render(ne, ctx, name, calls):
         scene.close()
 
 
+@pytest.mark.parametrize("name", ["cornell_c1", "medium_c2"])
+def test_noalloc_production_kernels(ne, ctx, name):
+    """Without the counting flag, on every tuning the scene can have (kernels 0-2 as tuned; a
+    scene tuned to the split kernel 3 renders with kernel 0) and after the autotuner: two
+    calls in a row, each image against ne_render's at the same tuning."""
+    import torch
+    host = ne.SceneHost.from_json(scene_path(name))
+    scene = ctx.upload(host)
+    spp = 16 if name == "cornell_c1" else 4
+    try:
+        out = torch.empty((host.height, host.width, 3), dtype=torch.float32, device="cuda:0")
+        tunings = [dict(kernel=k) for k in (0, 1, 2, 3)] + [dict(kernel=3, split_passes=12, split_half=1), None]
+        for t in tunings:
+            if t is None:
+                scene.autotune(repeats=1, seed=7, spp=2)
+            else:
+                scene.set_tuning(**t)
+            for kw in (dict(seed=21, spp=spp), dict(seed=22, spp=max(1, spp // 2), sample_offset=3)):
+                want, _ = scene.render(ne.render_params(**kw))
+                out.fill_(float("nan"))
+                st, stats = noalloc(ne, scene, ne.render_params(**kw), out)
+                assert st == 0, ctx.error()
+                got = out.cpu().numpy()
+                check_close(got, want)
+                assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (t, kw)
+                assert stats["paths"] == host.width * host.height * kw["spp"]
+    finally:
+        scene.close()
+
+
 def test_noalloc_rejects_oversize(ne, ctx):
     import torch
     from narvalengine_gb300 import _abi
