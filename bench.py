@@ -538,10 +538,10 @@ def main():
                 "density_lookups_per_launch": lookups, "scene_queries_per_launch": cstats["scene_queries"],
                 "bvh_nodes_per_launch": cstats["bvh_nodes"], "triangle_tests_per_launch": cstats["prim_tests"],
                 "kernel_ms": k_ms}
-    l2_gbs = ctx.read_bandwidth(L2_PROBE_BYTES, 50)
+    l2_gbs = ctx.read_bandwidth(L2_PROBE_BYTES, 10)
     roofline["l2"] = {"achieved": achieved, "peak": l2_gbs, "unit": "GB/s", "frac": achieved / l2_gbs,
-                      "peak_source": "measured here: ne_measure_read_bandwidth, read-only kernel over a 48 MiB "
-                                     "(L2-resident) buffer, 50 launches"}
+                      "peak_source": "measured here: ne_measure_read_bandwidth, read-only kernel reading a 48 MiB "
+                                     "(L2-resident) buffer 21 times per launch, 10 launches"}
     prof = pinned_profile(args.scene)
     if prof is not None:
         if prof["tuning"] == tuning:

@@ -223,8 +223,9 @@ ne_status ne_context_flush_l2(ne_context* ctx, size_t bytes);
 /* Read bandwidth of this GPU for a buffer of `bytes` (no counterpart in the reference; a
  * roofline denominator for benchmarks): one warm-up pass, then `iters` back-to-back launches
  * of a read-only kernel (16-byte loads that bypass L1, one CTA per SM times the resident
- * count) over the same buffer, event-timed; *gbs = bytes * iters / time. A buffer well inside
- * the 129 MB L2 measures L2 bandwidth, one well beyond it HBM bandwidth. */
+ * count), each reading the whole buffer as many times as makes at least 1 GiB, event-timed;
+ * *gbs = bytes read / time. A buffer well inside the 129 MB L2 measures L2 bandwidth, one
+ * well beyond it HBM bandwidth. */
 ne_status ne_measure_read_bandwidth(ne_context* ctx, size_t bytes, int iters, double* gbs);
 
 /* Device copies of the shared elementary functions, for bit-exactness checks.

@@ -546,19 +546,29 @@ __global__ void k_accum(const float* __restrict__ paths, uint32_t n_pix, uint32_
 }
 
 // Read-only bandwidth probe: every thread reads 16-byte words (ld.global.cg: cached in L2,
-// not L1) with a grid stride, four in flight, and folds them into one word that is written
-// only if it equals a value the data never produces (so the loads are not removed).
-__global__ void __launch_bounds__(512) k_read_bw(const uint4* __restrict__ p, size_t n, uint32_t* sink) {
+// not L1; volatile, so repeated passes are not merged) with a grid stride, four in flight,
+// over the whole buffer `reps` times, and folds them into one word that is written only if it
+// equals a value the data never produces (so the loads are not removed).
+__device__ __forceinline__ uint4 ld_cg_v4(const uint4* p) {
+  uint4 v;
+  asm volatile("ld.global.cg.v4.u32 {%0, %1, %2, %3}, [%4];" : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p));
+  return v;
+}
+__global__ void __launch_bounds__(512) k_read_bw(const uint4* __restrict__ p, size_t n, int reps, uint32_t* sink) {
   uint32_t acc = 0;
-  size_t stride = (size_t)gridDim.x * blockDim.x;
-  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  for (; i + 3 * stride < n; i += 4 * stride) {
-    uint4 a = __ldcg(p + i), b = __ldcg(p + i + stride), c = __ldcg(p + i + 2 * stride), d = __ldcg(p + i + 3 * stride);
-    acc ^= (a.x ^ a.y ^ a.z ^ a.w) ^ (b.x ^ b.y ^ b.z ^ b.w) ^ (c.x ^ c.y ^ c.z ^ c.w) ^ (d.x ^ d.y ^ d.z ^ d.w);
-  }
-  for (; i < n; i += stride) {
-    uint4 a = __ldcg(p + i);
-    acc ^= a.x ^ a.y ^ a.z ^ a.w;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (int r = 0; r < reps; r++) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    for (; i + 3 * stride < n; i += 4 * stride) {
+      uint4 a = ld_cg_v4(p + i), b = ld_cg_v4(p + i + stride), c = ld_cg_v4(p + i + 2 * stride),
+            d = ld_cg_v4(p + i + 3 * stride);
+      acc = acc * 31u + ((a.x + a.y + a.z + a.w) ^ (b.x + b.y + b.z + b.w) ^ (c.x + c.y + c.z + c.w) ^
+                         (d.x + d.y + d.z + d.w));
+    }
+    for (; i < n; i += stride) {
+      uint4 a = ld_cg_v4(p + i);
+      acc = acc * 31u + (a.x + a.y + a.z + a.w);
+    }
   }
   if (acc == 0x9e3779b9u) sink[0] = acc;
 }
@@ -1891,16 +1901,18 @@ ne_status ne_measure_read_bandwidth(ne_context* ctx, size_t bytes, int iters, do
   int per_sm = 0;
   NE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_read_bw, 512, 0), "occupancy");
   int blocks = ctx->sm_count * std::max(1, per_sm);
-  k_read_bw<<<blocks, 512, 0, ctx->stream>>>(buf.p, n, sink.p);  // warm-up: brings the buffer into L2
+  // passes per launch: at least 1 GiB read per launch, so launch gaps do not count
+  int reps = (int)std::max<size_t>(1, std::min<size_t>(1024, ((size_t)1 << 30) / (n * 16)));
+  k_read_bw<<<blocks, 512, 0, ctx->stream>>>(buf.p, n, 1, sink.p);  // warm-up: brings the buffer into L2
   NE_CUDA(cudaGetLastError(), "k_read_bw launch");
   NE_CUDA(cudaEventRecord(ctx->ev[0], ctx->stream), "cudaEventRecord");
-  for (int k = 0; k < iters; k++) k_read_bw<<<blocks, 512, 0, ctx->stream>>>(buf.p, n, sink.p);
+  for (int k = 0; k < iters; k++) k_read_bw<<<blocks, 512, 0, ctx->stream>>>(buf.p, n, reps, sink.p);
   NE_CUDA(cudaGetLastError(), "k_read_bw launch");
   NE_CUDA(cudaEventRecord(ctx->ev[1], ctx->stream), "cudaEventRecord");
   NE_CUDA(cudaEventSynchronize(ctx->ev[1]), "cudaEventSynchronize");
   float ms = 0;
   NE_CUDA(cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]), "cudaEventElapsedTime");
-  *gbs = (double)n * 16 * iters / (ms / 1e3) / 1e9;
+  *gbs = (double)n * 16 * reps * iters / (ms / 1e3) / 1e9;
   return NE_OK;
 }
 
