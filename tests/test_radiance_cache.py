@@ -109,7 +109,9 @@ def test_gradients_against_fp64(cache, n):
     quant=False). Tolerance from BF16 rounding: operands carry 8 significand bits (relative
     rounding up to 2^-9), so each tensor's error against FP64 may be what the BF16-quantised
     restatement's own error is, within a factor 1.5 plus 2^-10 of the tensor's norm (the
-    GPU sums its FP32 partial products in another order), and never above 2^-5."""
+    GPU sums its FP32 partial products in another order). That error is itself large where a
+    gradient is a sum of many products of both signs (layer 0's weights over 1000 samples: about
+    6% of a norm that cancellation makes small), so the bound is relative to it, not fixed."""
     from oracle import mlp
     p = mlp.init_params(13)
     cache.set_params(flatten(p))
@@ -129,7 +131,7 @@ def test_gradients_against_fp64(cache, n):
             nref = np.linalg.norm(ref) + 1e-30
             e_gpu = np.linalg.norm(a - ref) / nref
             e_bf16 = np.linalg.norm(q - ref) / nref
-            assert e_gpu <= 1.5 * e_bf16 + 2.0 ** -10 and e_gpu < 2.0 ** -5, \
+            assert e_gpu <= 1.5 * e_bf16 + 2.0 ** -10, \
                 f"layer {i} {name}: GPU {e_gpu:.3e} vs BF16 restatement {e_bf16:.3e} against FP64"
 
 
