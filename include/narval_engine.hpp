@@ -3,7 +3,7 @@
 //
 //   narvalgb::SceneReader           io/SceneReader.h:51-54 (loadScene, getSettings, getMainCamera)
 //   narvalgb::VolumetricPathIntegrator  integrators/Integrator.h:13-25 (Li, clone), batched
-//   narvalgb::OfflineEngine         core/OfflineEngine.h:169-193 (coreLoop, postProcessing,
+//   narvalgb::OfflineEngine         core/OfflineEngine.h:23-47 (coreLoop, postProcessing,
 //                                   16-bit PPM written last pixel first as OfflineEngine.cpp:119-138)
 //
 // Header-only; link with libnarval_gb300.so. Errors throw narvalgb::Error carrying the

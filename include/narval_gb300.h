@@ -39,7 +39,7 @@ typedef struct ne_context ne_context;
 typedef struct ne_scene ne_scene;
 typedef struct ne_scene_host ne_scene_host;
 
-/* A ray as the reference's Ray (primitives/Ray.h:182-197). */
+/* A ray as the reference's Ray (primitives/Ray.h:17-32). */
 typedef struct ne_ray {
   float o[3];
   float d[3];
@@ -51,7 +51,7 @@ typedef struct ne_path_key {
   uint32_t sample;
 } ne_path_key;
 
-/* Closest hit, the fields of RayIntersection (primitives/Ray.h:173-180) the integrator uses. */
+/* Closest hit, the fields of RayIntersection (primitives/Ray.h:8-15) the integrator uses. */
 typedef struct ne_hit {
   float t_near, t_far;
   float point[3];

@@ -1,11 +1,11 @@
 /*
  * Plain-data description of a NarvalEngine scene, as the path integrator sees it.
  *
- * The reference keeps its scene as an object graph (core/Scene.h:68-92):
+ * The reference keeps its scene as an object graph (core/Scene.h:12-36):
  *   Scene::instancedModels, Scene::lights   -> InstancedModel (transformToWCS, its inverse, Model*)
- *   Model::primitives, Model::lights, Model::materials (primitives/Model.h:551-563)
- *   Primitive::material (primitives/Primitive.h:211) -> Material {bsdf, medium, light, textures}
- *   Light::primitive (lights/Light.h:166), GridMedia {grid texture, sigma_s, sigma_a, density}
+ *   Model::primitives, Model::lights, Model::materials (primitives/Model.h:68-77)
+ *   Primitive::material (primitives/Primitive.h:14) -> Material {bsdf, medium, light, textures}
+ *   Light::primitive (lights/Light.h:9), GridMedia {grid texture, sigma_s, sigma_a, density}
  * This header flattens that graph into arrays indexed by 32-bit ids, in the same
  * order the reference iterates them, so that a GPU copy and a CPU restatement can
  * both be built from one description. Every field names the reference member it
@@ -53,7 +53,7 @@ typedef struct ne_model {
   int32_t use_bvh;                   /* Model::bvh built (meshes loaded from files) */
 } ne_model;
 
-/* One InstancedModel (primitives/InstancedModel.h:143-165). */
+/* One InstancedModel (primitives/InstancedModel.h:11-33). */
 typedef struct ne_instance {
   float to_wcs[16];  /* transformToWCS */
   float to_ocs[16];  /* invTransformToWCS */
@@ -91,7 +91,7 @@ typedef struct ne_material {
 
 enum ne_light_kind { NE_LIGHT_DIFFUSE = 0, NE_LIGHT_DIRECTIONAL = 1, NE_LIGHT_INFINITE = 2 };
 
-/* One Light (lights/Light.h:164-210 and subclasses). */
+/* One Light (lights/Light.h:7-53 and subclasses). */
 typedef struct ne_light {
   int32_t type;          /* ne_light_kind */
   int32_t primitive;     /* Light::primitive, index into prims */
@@ -111,7 +111,7 @@ typedef struct ne_light {
 
 enum ne_medium_kind { NE_MEDIUM_GRID = 0, NE_MEDIUM_HOMOGENEOUS = 1 };
 
-/* One Medium (materials/GridMedia.h:267-343, materials/HomogeneousMedia.h). */
+/* One Medium (materials/GridMedia.h:14-90, materials/HomogeneousMedia.h). */
 typedef struct ne_medium {
   int32_t type;        /* ne_medium_kind */
   float sigma_s[3];    /* scattering */
@@ -132,7 +132,7 @@ typedef struct ne_camera {
   float lens_radius;
 } ne_camera;
 
-/* SceneSettings (core/Settings.h:206-211) plus the documented extensions. */
+/* SceneSettings (core/Settings.h:12-17) plus the documented extensions. */
 typedef struct ne_settings {
   int32_t width, height;
   int32_t spp;

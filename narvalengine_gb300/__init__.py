@@ -572,7 +572,7 @@ class VolumetricPathIntegrator:
 
 
 class OfflineEngine:
-    """core/OfflineEngine.h:169-193: renders the scene's settings and writes output.ppm."""
+    """core/OfflineEngine.h:23-47: renders the scene's settings and writes output.ppm."""
 
     def __init__(self, scene: Scene, seed: int = 0, ref_tiles: bool = True):
         self.scene = scene

@@ -1438,7 +1438,7 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
     memcpy(d.sigma_s, s.sigma_s, 12);
     for (int k = 0; k < 3; k++) d.sigma_t[k] = s.sigma_a[k] + s.sigma_s[k];
     d.density = s.density;
-    // avg(extinction * densityMultiplier) (GridMedia.cpp:208)
+    // avg(extinction * densityMultiplier) (materials/GridMedia.cpp:56,82)
     float e0 = d.sigma_t[0] * s.density, e1 = d.sigma_t[1] * s.density, e2 = d.sigma_t[2] * s.density;
     d.mu = (e0 + e1 + e2) / 3.0f;
     d.inv_max_density = 1.0f;

@@ -2,8 +2,8 @@
 // host (g++, -ffp-contract=off) and on sm_103a (nvcc, -fmad=false, IEEE div/sqrt).
 //
 // The reference renderer calls libm (std::log, std::sin, std::cos, std::acos,
-// std::pow) inside its integrator (utils/Math.h:454,503-506, core/Microfacet.cpp:201-206,
-// core/BSDF.h:155, materials/Medium.h:110-111, materials/GridMedia.cpp:208,234).
+// std::pow) inside its integrator (utils/Math.h:454,503-506, core/Microfacet.cpp:44-49,
+// core/BSDF.h:155, materials/Medium.h:110-111, materials/GridMedia.cpp:56,82).
 // CUDA's and glibc's versions of those functions round differently, so a CPU
 // restatement and the GPU kernels that called them would draw different
 // directions for the same random numbers and paths would diverge. Both sides

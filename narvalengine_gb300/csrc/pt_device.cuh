@@ -574,7 +574,7 @@ NE_D void envSample(const DLight& L, float u0, float u1, float& d0, float& d1, f
   pdf = p0 * p1;
 }
 
-// Light::Le(ray, M) (lights/Light.h:177-179), DirectionalLight::Le, InfiniteAreaLight::Le.
+// Light::Le(ray, M) (lights/Light.h:20-22), DirectionalLight::Le, InfiniteAreaLight::Le.
 template <uint32_t K>
 NE_D V3 lightLe(const DLight& L, const float* M, V3 d) {
   if (L.type == NE_LIGHT_INFINITE) {

@@ -103,10 +103,10 @@ inline V3 mul4(const float* m, V3 p, float w) {
 
 struct Ray {
   V3 o, d;
-  V3 at(float t) const { return o + t * d; }  // primitives/Ray.h:189-191
+  V3 at(float t) const { return o + t * d; }  // primitives/Ray.h:24-26
 };
 
-// RayIntersection (primitives/Ray.h:173-180); instance/primitive by index.
+// RayIntersection (primitives/Ray.h:8-15); instance/primitive by index.
 struct Hit {
   V3 hitPoint{0, 0, 0}, normal{0, 0, 0};
   float tNear = 0, tFar = 0;
@@ -567,7 +567,7 @@ const OEnv* envOf(const orc_scene& s, const ne_light& L) {
   size_t i = &L - s.lights.data();
   return (i < s.env.size() && s.env[i].W > 0) ? &s.env[i] : nullptr;
 }
-// Light::Le(ray, M) (lights/Light.h:177-179), DirectionalLight::Le (DirectionalLight.cpp:4-6),
+// Light::Le(ray, M) (lights/Light.h:20-22), DirectionalLight::Le (DirectionalLight.cpp:4-6),
 // InfiniteAreaLight::Le (InfiniteAreaLight.h:46-55; a constant map without a texture).
 inline V3 lightLe(const orc_scene& s, const ne_light& L, const float* M, V3 d) {
   if (L.type == NE_LIGHT_INFINITE) {
