@@ -199,15 +199,21 @@ typedef struct ne_tuning {
                             1 = every half bounce (point 2b: bounce b's free-flight sample,
                             2b + 1: the end of bounce b, after its light sampling), so passes
                             alternate between the two variable-length walks */
+  int32_t queue_quarters; /* kernel 3: room for deferred paths, in quarters of the render's paths
+                            (1..8, 0 = 3: two thirds for the paths whose next light is the first
+                            kind, one third for the other); paths beyond it continue in the pass
+                            that has them */
 } ne_tuning;
 
 ne_status ne_scene_set_tuning(ne_scene* scene, const ne_tuning* tuning);
 ne_status ne_scene_get_tuning(const ne_scene* scene, ne_tuning* tuning);
 /* Autotuner: renders the scene with `params` under each candidate (straight, lane refill,
- * split with 3..24 passes by bounce or 12..32 by half bounce; resident blocks as many as fit),
- * `repeats` timed renders after one warm-up each, keeps the fastest path-kernel time and
- * returns it. Every candidate renders the same bits. The split kernel's best pass count
- * depends on the number of paths a render has: tune with the frame's own sample count. */
+ * regrouped with thresholds of 8, 16 and 24 32nds, split with 3..24 passes by bounce or 12..32
+ * by half bounce; resident blocks as many as fit), then, if a split configuration won, its
+ * deferred-path capacity at 2 and 4 quarters; `repeats` timed renders after one warm-up each,
+ * keeps the fastest path-kernel time and returns it. Every candidate renders the same bits. The
+ * split kernel's best pass count depends on the number of paths a render has: tune with the
+ * frame's own sample count. */
 ne_status ne_scene_autotune(ne_scene* scene, const ne_render_params* params, int repeats, ne_tuning* best,
                             double* best_ms);
 
@@ -254,6 +260,10 @@ typedef struct ne_views_tuning {
   int32_t graph;           /* 1: capture the launch sequence once and replay it as a CUDA graph */
   int32_t split_passes;    /* as ne_tuning.split_passes: 1 = one pass, 2..64, 0 = 6 */
   int32_t split_half;      /* as ne_tuning.split_half: 1 = deferral points every half bounce */
+  int32_t groups;          /* 1..16 (0 = 1): the views, in launch order, are cut into this many
+                              groups of about equal paths, each run through all its passes
+                              before the next starts, so the views of early groups complete
+                              early (per-view latency) at some cost in throughput */
 } ne_views_tuning;
 typedef struct ne_views_stats {
   double ms;               /* CUDA-event time of the batch */
@@ -266,10 +276,10 @@ ne_status ne_views_create(ne_scene* scene, const ne_view* views, uint32_t n, con
 void ne_views_destroy(ne_views* views);
 ne_status ne_views_set_tuning(ne_views* views, const ne_views_tuning* tuning);
 ne_status ne_views_get_tuning(const ne_views* views, ne_views_tuning* tuning);
-/* Times every candidate configuration (fetch 32/128, largest-first or smallest-first order,
- * 1, 4 or 8 split passes, as a graph) `repeats` times after one warm-up batch;
- * among those within 3% of the fastest it keeps the one with the lowest median view latency,
- * and returns it with its time. */
+/* Times every candidate configuration (fetch 32/128; largest-first order in one group, or
+ * smallest-first order in 1, 2 or 4 groups; 8 passes by bounce or 12/16 by half bounce; as a
+ * graph) `repeats` times after one warm-up batch; among those within 3% of the fastest it keeps
+ * the one with the lowest median view latency, and returns it with its time. */
 ne_status ne_views_autotune(ne_views* views, int repeats, ne_views_tuning* best, double* best_ms);
 ne_status ne_views_render(ne_views* views, ne_views_stats* stats);
 /* Completion latency of each view of the last batch, in the caller's order (n floats, ms). */

@@ -81,7 +81,7 @@ class NeRenderParams(C.Structure):
 
 class NeTuning(C.Structure):
     _fields_ = [("kernel", C.c_int32), ("track_share", C.c_int32), ("blocks_per_sm", C.c_int32),
-                ("split_passes", C.c_int32), ("split_half", C.c_int32)]
+                ("split_passes", C.c_int32), ("split_half", C.c_int32), ("queue_quarters", C.c_int32)]
 
 
 class NeRenderStats(C.Structure):
@@ -97,7 +97,7 @@ class NeView(C.Structure):
 
 class NeViewsTuning(C.Structure):
     _fields_ = [("fetch", C.c_uint32), ("blocks_per_sm", C.c_int32), ("order", C.c_int32), ("graph", C.c_int32),
-                ("split_passes", C.c_int32), ("split_half", C.c_int32)]
+                ("split_passes", C.c_int32), ("split_half", C.c_int32), ("groups", C.c_int32)]
 
 
 class NeViewsStats(C.Structure):

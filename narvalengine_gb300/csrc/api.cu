@@ -146,6 +146,8 @@ struct ne_scene {
   int variant = 0;           // path kernel: 0 straight, 1 regrouped, 2 lane refill, 3 split
   int split_passes = 16;      // kernel 3: passes (the last runs deferred paths to the end)
   int split_half = 1;         // kernel 3: deferral points every half bounce
+  int queue_quarters = 3;     // kernel 3: deferred-path capacity, quarters of the render's paths
+  size_t dq_cap_uploaded = 0; // capacity the uploaded queue descriptors give
   PathState* d_defer[2] = {nullptr, nullptr};  // split renders: two queues of deferred paths
   size_t defer_cap = 0;
   // split renders: queue descriptor p (device) is what pass p appends to, over buffer p & 1;
@@ -176,7 +178,8 @@ struct ne_views {
   uint32_t total_pixels = 0;
   PathParams P;
   nerng::PathKey base;
-  ne_views_tuning tune = {32, 0, 0, 1, 0, 0};
+  ne_views_tuning tune = {32, 0, 0, 1, 0, 0, 1};
+  std::vector<uint64_t> group_first;  // first path of each group (processing order), then total
   int blocks = 1;
   // split batches: two queues of deferred paths, the views' path spans, completion hook
   PathState* d_defer[2] = {nullptr, nullptr};
@@ -660,8 +663,9 @@ constexpr size_t kMaxDeferEntries = size_t(1) << 26;
 template <class F>
 ne_status launchSplit(ne_scene* sc, PathArgs b, int blocks, F launch) {
   ne_context* ctx = sc->ctx;
-  // class 0: half the paths, class 1: a quarter
-  size_t cap = std::min(kMaxDeferEntries, std::max<size_t>(3072, (size_t)(b.total / 4) * 3));
+  // queue_quarters / 4 of the paths (default 3: class 0 half the paths, class 1 a quarter)
+  size_t cap = std::min(kMaxDeferEntries,
+                        std::max<size_t>(3072, (size_t)(b.total / 4) * (size_t)sc->queue_quarters));
   if (sc->defer_cap < cap) {
     for (PathState*& q : sc->d_defer) {
       ctx->pool.put(q);
@@ -688,18 +692,20 @@ ne_status launchSplit(ne_scene* sc, PathArgs b, int blocks, F launch) {
     NE_CUDA(ctx->pool.get(passBytes, &pp), "cudaMalloc");
     sc->d_pass = (unsigned char*)pp;
   }
-  if (!sc->dq_uploaded) {
+  if (!sc->dq_uploaded || sc->dq_cap_uploaded != cap) {
+    // this render's capacity (the buffers may be larger, from an earlier render)
     DeferQueue dq[kMaxSplitPasses];
     for (int p = 0; p < kMaxSplitPasses; p++) {
       dq[p].items = sc->d_defer[p & 1];
       dq[p].count = reinterpret_cast<uint32_t*>(sc->d_pass) + p;
       dq[p].count_hi = reinterpret_cast<uint32_t*>(sc->d_pass) + kMaxSplitPasses + p;
-      dq[p].cap = (uint32_t)(sc->defer_cap / 3 * 2);
-      dq[p].cap_hi = (uint32_t)(sc->defer_cap - dq[p].cap);
+      dq[p].cap = (uint32_t)(cap / 3 * 2);
+      dq[p].cap_hi = (uint32_t)(cap - dq[p].cap);
     }
     // from pageable memory: the call returns once `dq` has been staged
     NE_CUDA(cudaMemcpyAsync(sc->d_dq, dq, sizeof(dq), cudaMemcpyHostToDevice, ctx->stream), "cudaMemcpyAsync");
     sc->dq_uploaded = true;
+    sc->dq_cap_uploaded = cap;
   }
   NE_CUDA(cudaMemsetAsync(sc->d_pass, 0, passBytes, ctx->stream), "cudaMemsetAsync");
   unsigned long long* counters = reinterpret_cast<unsigned long long*>(sc->d_pass + countBytes);
@@ -969,6 +975,15 @@ ne_status viewsLayout(ne_views* vw) {
     pb += d.paths;
     pix += (uint32_t)(v.width * v.height);
   }
+  // groups: cut the processing order where the running path count passes g / groups of the
+  // total, never inside a view
+  const int groups = std::max(1, std::min<int>(vw->tune.groups, (int)n));
+  vw->group_first.assign(1, 0);
+  for (uint32_t s = 0; s + 1 < n && (int)vw->group_first.size() < groups; s++) {
+    uint64_t end = vw->dv[s].path_begin + vw->dv[s].paths;
+    if (end * (uint64_t)groups >= pb * (uint64_t)vw->group_first.size()) vw->group_first.push_back(end);
+  }
+  vw->group_first.push_back(pb);
   NE_CUDA(cudaMemcpyAsync(vw->d_views, vw->dv.data(), n * sizeof(DView), cudaMemcpyHostToDevice, ctx->stream),
           "cudaMemcpyAsync");
   std::vector<ViewSpan> spans(n);
@@ -992,16 +1007,18 @@ ne_status viewsEnqueue(ne_views* vw) {
   unsigned long long* counter = done + 2 * n + 1;
   NE_CUDA(cudaMemsetAsync(done, 0, 2 * n * sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync");
   NE_CUDA(cudaMemsetAsync(tstart, 0xFF, sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync");
-  NE_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync");
   NE_CUDA(cudaMemsetAsync(ctx->d_err, 0, 4, ctx->stream), "cudaMemsetAsync");
   const int passes = viewsPasses(vw);
   const bool split = passes > 1;
+  for (size_t g = 0; g + 1 < vw->group_first.size(); g++) {
+  NE_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync");
   ViewArgs a;
   a.P = vw->P;
   a.base = vw->base;
   a.views = vw->d_views;
   a.n_views = n;
-  a.total = vw->total;
+  a.first = vw->group_first[g];
+  a.total = vw->group_first[g + 1];
   a.fetch = vw->tune.fetch;
   a.out = vw->d_paths;
   a.done = done;
@@ -1032,6 +1049,7 @@ ne_status viewsEnqueue(ne_views* vw) {
     NE_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync");
     NE_CUDA(ne_launch_path_split(pass, K_GENERAL, vw->blocks, ctx->stream, vw->sc->d, pa, counter, ctx->d_err),
             "resume kernel launch");
+  }
   }
   int rblocks = (int)std::min<uint64_t>((vw->total_pixels + 255) / 256, (uint64_t)ctx->sm_count * 16);
   NE_CUDA(ne_launch_reduce_views(std::max(1, rblocks), ctx->stream, vw->d_paths, vw->d_views, n, vw->total_pixels,
@@ -1571,6 +1589,7 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
   tn.blocks_per_sm = 0;
   tn.split_passes = 0;
   tn.split_half = 1;
+  tn.queue_quarters = 3;
   if (ne_scene_set_tuning(sc, &tn) != NE_OK) return cleanup(NE_ERR_INVALID_ARG);
   cudaError_t e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return cleanup(cudaFail(ctx, e, "scene upload"));
@@ -1581,7 +1600,8 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
 ne_status ne_scene_set_tuning(ne_scene* sc, const ne_tuning* t) {
   if (!sc || !t || t->kernel < 0 || t->kernel > 3 || t->track_share < 1 || t->track_share > 32 ||
       t->blocks_per_sm < 0 || t->blocks_per_sm > 64 || t->split_passes < 0 || t->split_passes == 1 ||
-      t->split_passes > 64 || t->split_half < 0 || t->split_half > 1)
+      t->split_passes > 64 || t->split_half < 0 || t->split_half > 1 || t->queue_quarters < 0 ||
+      t->queue_quarters > 8)
     return NE_ERR_INVALID_ARG;
   ne_context* ctx = sc->ctx;
   int fit = 1;
@@ -1593,6 +1613,7 @@ ne_status ne_scene_set_tuning(ne_scene* sc, const ne_tuning* t) {
   sc->split_half = t->split_half;
   sc->track_share = t->track_share;
   sc->blocks_per_sm = t->blocks_per_sm > 0 ? std::min(t->blocks_per_sm, fit) : fit;
+  sc->queue_quarters = t->queue_quarters ? t->queue_quarters : 3;
   return NE_OK;
 }
 
@@ -1603,6 +1624,7 @@ ne_status ne_scene_get_tuning(const ne_scene* sc, ne_tuning* t) {
   t->blocks_per_sm = sc->blocks_per_sm;
   t->split_passes = sc->split_passes;
   t->split_half = sc->split_half;
+  t->queue_quarters = sc->queue_quarters;
   return NE_OK;
 }
 
@@ -2486,11 +2508,12 @@ void ne_views_destroy(ne_views* vw) {
 ne_status ne_views_set_tuning(ne_views* vw, const ne_views_tuning* t) {
   if (!vw || !t || t->fetch < 32 || t->fetch > 4096 || t->fetch % 32 || t->blocks_per_sm < 0 ||
       t->blocks_per_sm > 64 || t->order < 0 || t->order > 2 || t->graph < 0 || t->graph > 1 || t->split_passes < 0 ||
-      t->split_passes > 64 || t->split_half < 0 || t->split_half > 1)
+      t->split_passes > 64 || t->split_half < 0 || t->split_half > 1 || t->groups < 0 || t->groups > 16)
     return NE_ERR_INVALID_ARG;
   ne_context* ctx = vw->sc->ctx;
   NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
   vw->tune = *t;
+  if (vw->tune.groups == 0) vw->tune.groups = 1;
   return viewsPrepare(vw);
 }
 
@@ -2536,7 +2559,7 @@ ne_status ne_views_render(ne_views* vw, ne_views_stats* stats) {
     stats->latency_p50_ms = pct(0.5);
     stats->latency_p99_ms = pct(0.99);
     stats->latency_max_ms = lat[n - 1];
-    stats->kernel_launches = 2;
+    stats->kernel_launches = (uint32_t)((vw->group_first.size() - 1) * viewsPasses(vw) + 1);
   }
   return NE_OK;
 }
@@ -2548,10 +2571,10 @@ ne_status ne_views_autotune(ne_views* vw, int repeats, ne_views_tuning* best, do
   NE_CUDA(ne_views_occupancy(&fit), "occupancy query");
   fit = std::max(1, fit);
   const uint32_t fetches[2] = {32, 128};
-  const int bpss[1] = {fit};
-  const int orders[2] = {1, 2};
-  // (passes, by half bounce): one pass, by bounce, by half bounce
-  const int passess[5][2] = {{1, 0}, {4, 0}, {8, 0}, {12, 1}, {16, 1}};
+  // (order, groups): largest first in one group, or smallest first in 1, 2 or 4 groups
+  const int ogs[4][2] = {{1, 1}, {2, 1}, {2, 2}, {2, 4}};
+  // (passes, by half bounce): by bounce, by half bounce
+  const int passess[3][2] = {{8, 0}, {12, 1}, {16, 1}};
   struct Trial {
     ne_views_tuning t;
     double ms;
@@ -2559,10 +2582,9 @@ ne_status ne_views_autotune(ne_views* vw, int repeats, ne_views_tuning* best, do
   };
   std::vector<Trial> trials;
   for (uint32_t f : fetches)
-    for (int b : bpss)
-      for (int o : orders)
-        for (const auto& sp : passess) {
-        ne_views_tuning t = {f, b, o, 1, sp[0], sp[1]};
+    for (const auto& og : ogs)
+      for (const auto& sp : passess) {
+        ne_views_tuning t = {f, fit, og[0], 1, sp[0], sp[1], og[1]};
         ne_status st = ne_views_set_tuning(vw, &t);
         if (st) return st;
         ne_views_stats s;
@@ -2623,12 +2645,15 @@ ne_status ne_scene_autotune(ne_scene* sc, const ne_render_params* p, int repeats
   ne_tuning keep;
   ne_scene_get_tuning(sc, &keep);
   std::vector<ne_tuning> cands;
-  for (int k : {0, 2}) cands.push_back(ne_tuning{k, sc->track_share, 0, 0, 0});
-  for (int passes : {3, 4, 6, 8, 12, 16, 24}) cands.push_back(ne_tuning{3, sc->track_share, 0, passes, 0});
-  for (int passes : {12, 16, 20, 24, 32}) cands.push_back(ne_tuning{3, sc->track_share, 0, passes, 1});
+  for (int k : {0, 2}) cands.push_back(ne_tuning{k, 16, 0, 0, 0, 3});
+  // the regrouped kernel at three regrouping thresholds (32nds of a warp's live lanes in one
+  // kind of event)
+  for (int share : {8, 16, 24}) cands.push_back(ne_tuning{1, share, 0, 0, 0, 3});
+  for (int passes : {3, 4, 6, 8, 12, 16, 24}) cands.push_back(ne_tuning{3, 16, 0, passes, 0, 3});
+  for (int passes : {12, 16, 20, 24, 32}) cands.push_back(ne_tuning{3, 16, 0, passes, 1, 3});
   ne_tuning bt = keep;
   double bms = 1e30;
-  for (const ne_tuning& t : cands) {
+  auto tryTuning = [&](const ne_tuning& t) -> ne_status {
     ne_status st = ne_scene_set_tuning(sc, &t);
     if (st) return st;
     ne_render_stats s;
@@ -2643,6 +2668,21 @@ ne_status ne_scene_autotune(ne_scene* sc, const ne_render_params* p, int repeats
     if (m < bms) {
       bms = m;
       bt = t;
+    }
+    return NE_OK;
+  };
+  for (const ne_tuning& t : cands) {
+    ne_status st = tryTuning(t);
+    if (st) return st;
+  }
+  // then the best split configuration's deferred-path capacity: 2 or 4 quarters of the paths
+  if (bt.kernel == 3) {
+    ne_tuning base = bt;
+    for (int q : {2, 4}) {
+      ne_tuning t = base;
+      t.queue_quarters = q;
+      ne_status st = tryTuning(t);
+      if (st) return st;
     }
   }
   ne_status st = ne_scene_set_tuning(sc, &bt);

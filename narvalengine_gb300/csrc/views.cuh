@@ -1,9 +1,10 @@
 // Many views of one scene in one persistent launch.
 //
 // The work of all views is one range of path indices: view v owns [begin[v], begin[v+1]),
-// laid out pixel-major with spp consecutive samples per pixel as in k_paths. Warps take
-// `fetch` consecutive indices at a time from a global counter, so a warp's lanes share a
-// view and usually a pixel, and views of every size drain through the same resident warps.
+// laid out pixel-major with spp consecutive samples per pixel as in k_paths. A launch covers
+// the range of one group of consecutive views. Warps take `fetch` consecutive indices at a
+// time from a global counter, so a warp's lanes share a view and usually a pixel, and views
+// of every size drain through the same resident warps.
 // The view the caller passed at index v uses random stream v + 1 (stream 0 is the
 // single-camera render), so no two views share random numbers and the launch order does not
 // change any image. Each view counts its finished paths (one atomic per group of
@@ -30,7 +31,8 @@ struct ViewArgs {
   nerng::PathKey base;
   const DView* views;       // in processing order
   uint32_t n_views;
-  unsigned long long total; // paths over all views
+  unsigned long long first; // path indices [first, total) of this launch (one group of views)
+  unsigned long long total;
   uint32_t fetch;           // path indices per warp fetch, a multiple of 32
   float* out;               // total x 3 per-path radiance
   unsigned long long* done; // per view: finished paths
@@ -61,7 +63,7 @@ __global__ void __launch_bounds__(kThreads, pathMinBlocks(K)) k_views(const __gr
   if (threadIdx.x == 0 && blockIdx.x == 0) atomicMin(a.t_start, globalTimer());
   for (;;) {
     unsigned long long base = 0;
-    if (lane == 0) base = atomicAdd(&counter[0], (unsigned long long)a.fetch);
+    if (lane == 0) base = a.first + atomicAdd(&counter[0], (unsigned long long)a.fetch);
     base = __shfl_sync(0xffffffffu, base, 0);
     if (base >= a.total) break;
     for (uint32_t k = 0; k < a.fetch; k += 32) {

@@ -201,12 +201,13 @@ def test_kernels_and_tunings_agree(ne, ctx):
                                        (1, 8, 1, 0), (2, 16, 0, 0), (2, 16, 1, 0), (3, 16, 0, 2), (3, 16, 1, 3),
                                        (3, 16, 0, 5), (3, 16, 0, 16), (3, 16, 0, -8), (3, 16, 0, -3),
                                        (3, 16, 0, -64), (3, 16, 1, -12), (3, 16, 0, 6)]:
-        scene.set_tuning(kernel=kernel, track_share=share, blocks_per_sm=bps, split_passes=abs(passes),
-                         split_half=int(passes < 0))
-        img, stats = scene.render(p)
-        if ref is None:
-            ref = img
-        assert np.array_equal(img, ref), (kernel, share, bps, passes)
+        for quarters in ((3,) if kernel != 3 else (3, 1, 8)):
+            scene.set_tuning(kernel=kernel, track_share=share, blocks_per_sm=bps, split_passes=abs(passes),
+                             split_half=int(passes < 0), queue_quarters=quarters)
+            img, stats = scene.render(p)
+            if ref is None:
+                ref = img
+            assert np.array_equal(img, ref), (kernel, share, bps, passes, quarters)
     with pytest.raises(ne.NarvalError):
         scene.set_tuning(kernel=4)
     with pytest.raises(ne.NarvalError):
@@ -214,6 +215,8 @@ def test_kernels_and_tunings_agree(ne, ctx):
 
     with pytest.raises(ne.NarvalError):
         scene.set_tuning(kernel=1, track_share=0)
+    with pytest.raises(ne.NarvalError):
+        scene.set_tuning(kernel=3, queue_quarters=9)
 
 
 def test_counting_kernels_agree(ne, ctx):
@@ -350,15 +353,16 @@ def test_split_queue_overflow(ne, ctx, oracle_lib):
     queue finish in the first pass, and every path still matches the oracle bit for bit."""
     host = ne.SceneHost.from_json(scene_path("medium_c2"))
     scene = ctx.upload(host)
-    scene.set_tuning(kernel=3)
     orc = oracle_lib.OracleScene.from_json(scene_path("medium_c2"))
     try:
         centre = (host.height // 2) * host.width + host.width // 2
         keys = np.array([[centre, s] for s in range(8192)], np.uint32)
         p = ne.render_params(seed=5)
-        g = scene.trace_paths(keys, p)
         c = orc.trace_paths(keys, p)
-        assert np.array_equal(g.view(np.uint32), c.view(np.uint32))
+        for quarters in (1, 3, 8):  # a quarter, three quarters and twice the paths
+            scene.set_tuning(kernel=3, queue_quarters=quarters)
+            g = scene.trace_paths(keys, p)
+            assert np.array_equal(g.view(np.uint32), c.view(np.uint32)), quarters
     finally:
         scene.close()
         orc.close()
@@ -370,7 +374,7 @@ def test_autotune_keeps_the_image(ne, ctx):
     scene = ctx.upload(host)
     ref, _ = scene.render(seed=13, spp=2)
     best, ms = scene.autotune(repeats=1, seed=1, spp=1)
-    assert ms > 0 and best["kernel"] in (0, 2, 3)
+    assert ms > 0 and best["kernel"] in (0, 1, 2, 3) and 1 <= best["queue_quarters"] <= 4
     img, st = scene.render(seed=13, spp=2)
     assert np.array_equal(img, ref)
     if best["kernel"] == 3:

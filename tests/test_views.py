@@ -67,18 +67,38 @@ def test_tunings_do_not_change_images(batch):
     vb.set_tuning(fetch=32, order=0, graph=False, split_passes=1)
     vb.render()
     ref = [vb.image(v) for v in range(len(views))]
-    for fetch, bps, order, graph, sp in [(128, 0, 1, True, 0), (64, 2, 2, True, 1), (32, 1, 1, False, 4),
-                                         (32, 0, 2, True, 8), (128, 0, 0, False, 2), (32, 0, 1, True, -12),
-                                         (64, 0, 2, False, -5)]:
+    for fetch, bps, order, graph, sp, groups in [(128, 0, 1, True, 0, 1), (64, 2, 2, True, 1, 1),
+                                                 (32, 1, 1, False, 4, 1), (32, 0, 2, True, 8, 1),
+                                                 (128, 0, 0, False, 2, 1), (32, 0, 1, True, -12, 1),
+                                                 (64, 0, 2, False, -5, 1), (32, 0, 2, True, -12, 2),
+                                                 (32, 0, 2, False, 4, 3), (128, 0, 1, True, -8, 5),
+                                                 (32, 0, 0, True, 1, 16)]:
         # negative: that many passes with deferral points every half bounce
         vb.set_tuning(fetch=fetch, blocks_per_sm=bps, order=order, graph=graph, split_passes=abs(sp),
-                      split_half=int(sp < 0))
+                      split_half=int(sp < 0), groups=groups)
         st = vb.render()
         for v in range(len(views)):
-            assert np.array_equal(vb.image(v), ref[v]), (fetch, bps, order, graph, sp, v)
+            assert np.array_equal(vb.image(v), ref[v]), (fetch, bps, order, graph, sp, groups, v)
         lat = vb.latency()
         assert np.all(lat > 0) and lat.max() <= st["ms"] * 1.5 + 1.0, (lat, st)
         assert st["latency_p50_ms"] <= st["latency_p99_ms"] <= st["latency_max_ms"]
+        passes = abs(sp) or 6
+        launches = st["kernel_launches"] - 1  # the pixel means
+        assert launches % passes == 0 and 1 <= launches // passes <= min(groups, len(views)), st
+
+
+def test_groups_complete_views_early(batch):
+    """Views of the first group (smallest first) complete before the batch's last group
+    starts: their latency is well below the last view's."""
+    ne, scene, vb, views, orc = batch
+    vb.set_tuning(fetch=32, order=2, graph=True, split_passes=8, split_half=0, groups=len(views))
+    vb.render()
+    st = vb.render()
+    lat = vb.latency()
+    sizes = np.array([w * h * s for _, w, h, s in views])
+    first = np.argmin(sizes)
+    assert lat[first] < 0.8 * lat.max(), (lat, sizes)
+    assert st["latency_p50_ms"] < st["latency_max_ms"]
 
 
 def test_autotune(batch):
@@ -87,7 +107,7 @@ def test_autotune(batch):
     ref = [vb.image(v) for v in range(len(views))]
     best, ms = vb.autotune(repeats=1)
     assert ms > 0 and best["fetch"] in (32, 128) and best["order"] in (1, 2) and best["graph"] == 1
-    assert best["split_passes"] in (1, 4, 8)
+    assert (best["split_passes"], best["split_half"]) in ((8, 0), (12, 1), (16, 1)) and best["groups"] in (1, 2, 4)
     assert vb.tuning() == best
     vb.render()
     for v in range(len(views)):
