@@ -87,6 +87,12 @@ typedef struct ne_material {
   float normal_map[3]; /* NORMAL texture value */
   int32_t tex_present; /* ne_tex_bits of the non-null Material::textures slots */
   int32_t tex_types;   /* Material::textureTypes (the bits hasTexture() tests) */
+  /* A microfacet albedo given as an image file (io/SceneReader.cpp:80-103, loaded by
+   * ResourceManager::loadTexture, core/ResourceManager.cpp:288-313, as 8-bit RGBA with the
+   * mirror wrap and nearest lookup of Texture::sample): its texels row-major from the top
+   * row. albedo_width = 0: the constant albedo[] above. */
+  int32_t albedo_width, albedo_height;
+  const uint8_t* albedo_texels;
 } ne_material;
 
 enum ne_light_kind { NE_LIGHT_DIFFUSE = 0, NE_LIGHT_DIRECTIONAL = 1, NE_LIGHT_INFINITE = 2 };

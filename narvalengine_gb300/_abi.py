@@ -25,7 +25,8 @@ class NeInstance(C.Structure):
 class NeMaterial(C.Structure):
     _fields_ = [("bsdf", C.c_int32), ("light", C.c_int32), ("medium", C.c_int32), ("phase", C.c_int32),
                 ("g", C.c_float), ("albedo", f3), ("roughness", C.c_float), ("metallic", C.c_float),
-                ("normal_map", f3), ("tex_present", C.c_int32), ("tex_types", C.c_int32)]
+                ("normal_map", f3), ("tex_present", C.c_int32), ("tex_types", C.c_int32),
+                ("albedo_width", C.c_int32), ("albedo_height", C.c_int32), ("albedo_texels", C.POINTER(C.c_uint8))]
 
 
 class NeLight(C.Structure):

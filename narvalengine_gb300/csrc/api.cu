@@ -1416,6 +1416,16 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
     d.roughness = s.roughness; d.metallic = s.metallic;
     memcpy(d.normal_map, s.normal_map, 12);
     d.tex_present = s.tex_present; d.tex_types = s.tex_types;
+    if (s.bsdf == NE_BSDF_GLOSSY && s.albedo_width > 0) {
+      if (!s.albedo_texels || s.albedo_height <= 0)
+        return cleanup(fail(ctx, NE_ERR_INVALID_ARG, "albedo texture without texels"));
+      const uint8_t* tex = nullptr;
+      ne_status st = upload(sc, s.albedo_texels, (size_t)s.albedo_width * s.albedo_height * 4, &tex);
+      if (st) return cleanup(st);
+      d.albedo_w = s.albedo_width;
+      d.albedo_h = s.albedo_height;
+      d.albedo_tex = (const uchar4*)tex;
+    }
   }
   std::vector<DLight> lights(D.n_lights);
   std::deque<EnvTables> envTables;  // host sources of the table copies, alive until the upload syncs
@@ -1572,6 +1582,7 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
     if (m.bsdf == NE_BSDF_GLOSSY) F |= FT_GLOSSY;
     if (m.bsdf == NE_BSDF_VOLUME) F |= FT_VOLBSDF;
     if (m.tex_types & NE_TEX_NORMAL) F |= FT_NORMALMAP;
+    if (m.bsdf == NE_BSDF_GLOSSY && m.albedo_width > 0) F |= FT_TEXALB;
   }
   for (uint32_t i = 0; i < D.n_media; i++) F |= D.media[i].type == NE_MEDIUM_GRID ? FT_GRID : FT_HOMOG;
   for (uint32_t i = 0; i < D.n_lights; i++) {

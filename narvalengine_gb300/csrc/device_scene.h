@@ -64,7 +64,9 @@ struct DMaterial {
   float roughness, metallic;
   float normal_map[3];
   int32_t tex_present, tex_types;
+  int32_t albedo_w, albedo_h;  // albedo texture (RGBA8, row-major from the top row); 0: constant
   int32_t pad;
+  const uchar4* albedo_tex;
 };
 
 struct DLight {

@@ -66,7 +66,8 @@ enum : uint32_t {
   FT_NORMALMAP = 1u << 12,
   FT_BBOX = 1u << 13,     // model bounding boxes (meshes)
   FT_ENVMAP = 1u << 14,   // InfiniteAreaLight with a texture and its Distribution2D
-  FT_ALL = (1u << 15) - 1,
+  FT_TEXALB = 1u << 15,   // microfacet albedo from a texture (per-hit texture coordinates)
+  FT_ALL = (1u << 16) - 1,
   K_COUNT = 1u << 31,
   K_CACHE = 1u << 30,  // paths end in the learned radiance cache (see CacheIO)
   K_SPLIT = 1u << 29,  // paths are deferred at their first medium scattering (see DeferQueue)
@@ -747,7 +748,7 @@ NE_D V3 fresnel(float cosTheta) {
   return f0 + (v3(1, 1, 1) - f0) * nefm::pow5(1.0f - cosTheta);
 }
 // core/GlossyBSDF.cpp:25-48.
-NE_D V3 glossyEval(const DMaterial& m, V3 wi, V3 wo) {
+NE_D V3 glossyEval(const DMaterial& m, V3 wi, V3 wo, V3 albedo) {
   float rough = texValue(m, NE_TEX_ROUGHNESS).x;
   float alpha = rough * rough;
   V3 H = normalize(wi + wo);
@@ -761,7 +762,6 @@ NE_D V3 glossyEval(const DMaterial& m, V3 wi, V3 wo) {
   V3 specular = numerator / gmax(denominator, float(kEpsilonD));
   V3 kD = v3(1, 1, 1) - F;
   float metallic = texValue(m, NE_TEX_METALLIC).x;
-  V3 albedo = texValue(m, NE_TEX_ALBEDO);
   kD = kD * __double2float_rn(1.0 - (double)metallic);
   return ((albedo / float(kPiD)) * kD + specular) * NdotL;
 }
@@ -831,20 +831,69 @@ NE_NI float bsdfPdf(const DMaterial& m, V3 incoming, V3 scattered, V3 normal) {
   if (trans) return phaseEval<K>(m, wi, wo);
   return (K & FT_GLOSSY) ? glossyPdf(m, wi, wo) : 0.0f;
 }
-// core/BSDF.h:135-142.
+// Rectangle::samplePointOnTexture (primitives/Rectangle.cpp:115-157) at the object-space point
+// q of a hit: barycentric coordinates (:91-113) of q in the triangle (v0, v1, v2) of the
+// rectangle's corners, or in (v3, v1, v2) when those leave [0, 1], weighting the corners'
+// texture coordinates (0,0), (1,0), (1,1), (0,1). The corners as SceneReader lays them out
+// (io/SceneReader.cpp:407-463): v0 = p0, v2 = p1 (opposite), v1 = (p1.x, p0.y, p0.z),
+// v3 = (p0.x, p1.y, p0.z).
+NE_D void rectBary(V3 p, V3 a, V3 b, V3 c, float& l0, float& l1, float& l2) {
+  V3 v0 = b - a, v1 = c - a, v2 = p - a;
+  float d00 = dot(v0, v0), d01 = dot(v0, v1), d11 = dot(v1, v1);
+  float d20 = dot(v2, v0), d21 = dot(v2, v1);
+  float denom = d00 * d11 - d01 * d01;
+  l1 = (d11 * d20 - d01 * d21) / denom;
+  l2 = (d00 * d21 - d01 * d20) / denom;
+  l0 = 1.0f - l1 - l2;
+}
+NE_D void rectUV(const DPrim& p, V3 q, float& u, float& v) {
+  V3 c0 = ld3(p.p0), c2 = ld3(p.p1);
+  V3 c1 = v3(c2.x, c0.y, c0.z), c3 = v3(c0.x, c2.y, c0.z);
+  float a0, a1, a2;
+  rectBary(q, c0, c1, c2, a0, a1, a2);
+  if (a0 < 0 || a1 < 0 || a2 < 0 || a0 > 1 || a1 > 1 || a2 > 1) {
+    rectBary(q, c3, c1, c2, a0, a1, a2);
+    u = (a0 * 0.0f + a1 * 1.0f) + a2 * 1.0f;  // uv3 = (0, 1), uv1 = (1, 0), uv2 = (1, 1)
+    v = (a0 * 1.0f + a1 * 0.0f) + a2 * 1.0f;
+  } else {
+    u = (a0 * 0.0f + a1 * 1.0f) + a2 * 1.0f;  // uv0 = (0, 0), uv1 = (1, 0), uv2 = (1, 1)
+    v = (a0 * 0.0f + a1 * 0.0f) + a2 * 1.0f;
+  }
+}
+// Material::sampleMaterial(ALBEDO, hit.uv) (materials/Material.h:62-69): a textured albedo is
+// looked up at the hit's texture coordinates, which the rectangle computes from its
+// object-space hit point (Rectangle.cpp:71) and every other primitive leaves at (0, 0)
+// (Sphere.cpp:37, AABB.cpp:68; triangles read no texture coordinates here). The point is
+// recomputed from the ray that produced the hit, in the same operations as the intersection.
 template <uint32_t K>
-NE_NI V3 bsdfEval(const DMaterial& m, V3 incoming, V3 scattered, V3 normal) {
+NE_D V3 albedoAt(const DScene& s, const DMaterial& m, const Ray& incoming, const Hit& h) {
+  if ((K & FT_TEXALB) && m.albedo_w > 0) {
+    float u = 0.0f, v = 0.0f;
+    const DPrim& p = s.prims[h.prim];
+    if ((K & FT_RECT) && p.type == NE_PRIM_RECTANGLE) {
+      Ray r = transformRay(incoming, s.instances[h.inst].ocs);
+      rectUV(p, r.at(h.tNear), u, v);
+    }
+    uchar4 t = m.albedo_tex[(uint32_t)texCoord(v, m.albedo_h) * (uint32_t)m.albedo_w + (uint32_t)texCoord(u, m.albedo_w)];
+    return v3((float)t.x / 255.0f, (float)t.y / 255.0f, (float)t.z / 255.0f);
+  }
+  return texValue(m, NE_TEX_ALBEDO);
+}
+// core/BSDF.h:135-142, for the hit `isect` of the ray `incoming`.
+template <uint32_t K>
+NE_NI V3 bsdfEval(const DScene& s, const DMaterial& m, const Ray& incoming, V3 scattered, const Hit& isect) {
+  const V3 normal = isect.normal;
   bool trans = (K & FT_VOLBSDF) && (m.bsdf == NE_BSDF_VOLUME);
-  if (!trans && (!sameHemisphere(-incoming, normal) || !sameHemisphere(scattered, normal))) return v3(0, 0, 0);
+  if (!trans && (!sameHemisphere(-incoming.d, normal) || !sameHemisphere(scattered, normal))) return v3(0, 0, 0);
   V3 ss, ts;
   orthonormal(normal, ss, ts);
-  V3 wi = toLCS(-normalize(incoming), normal, ss, ts);
+  V3 wi = toLCS(-normalize(incoming.d), normal, ss, ts);
   V3 wo = toLCS(scattered, normal, ss, ts);
   if (trans) {
     float p = phaseEval<K>(m, wi, wo);
     return v3(p, p, p);
   }
-  return (K & FT_GLOSSY) ? glossyEval(m, wi, wo) : v3(0, 0, 0);
+  return (K & FT_GLOSSY) ? glossyEval(m, wi, wo, albedoAt<K>(s, m, incoming, isect)) : v3(0, 0, 0);
 }
 
 // ---------------------------------------------------------------- media
@@ -1187,10 +1236,10 @@ NE_NI V3 estimateDirect(Ctx<K>& c, const Ray& incoming, const Hit& isect, const 
   bool mediumF = false;  // f holds the phase value for (incoming.d, wo.d)
   if (lightPdf > 0 && !isBlack(Li)) {
     if (surface) {
-      f = bsdfEval<K>(mat, incoming.d, wo.d, isect.normal) * fabsf(dot(wo.d, isect.normal));
+      f = bsdfEval<K>(s, mat, incoming, wo.d, isect) * fabsf(dot(wo.d, isect.normal));
       scatteringPdf = bsdfPdf<K>(mat, incoming.d, wo.d, isect.normal);
     } else {
-      f = bsdfEval<K>(mat, incoming.d, wo.d, isect.normal);
+      f = bsdfEval<K>(s, mat, incoming, wo.d, isect);
       scatteringPdf = f.x;
       mediumF = true;
     }
@@ -1205,13 +1254,13 @@ NE_NI V3 estimateDirect(Ctx<K>& c, const Ray& incoming, const Hit& isect, const 
   }
   if (surface) {
     wo.d = bsdfSample<K>(mat, incoming.d, isect.normal, c.S);
-    f = bsdfEval<K>(mat, incoming.d, wo.d, isect.normal);
+    f = bsdfEval<K>(s, mat, incoming, wo.d, isect);
     f = f * fabsf(dot(wo.d, isect.normal));
     scatteringPdf = bsdfPdf<K>(mat, incoming.d, wo.d, isect.normal);
   } else {
     // the reference evaluates the phase function at the light sample's direction again here
     // (VolumetricPathIntegrator.cpp:121-125); the value computed above is the same
-    if (!mediumF) f = bsdfEval<K>(mat, incoming.d, wo.d, isect.normal);
+    if (!mediumF) f = bsdfEval<K>(s, mat, incoming, wo.d, isect);
     wo.d = bsdfSample<K>(mat, incoming.d, v3(0, 1, 0), c.S);
     scatteringPdf = f.x;
   }
@@ -1403,7 +1452,7 @@ NE_D V3 liLoop(Ctx<K>& c, const PathParams& P, LiVars& v, bool resume) {
     if (medium) {
       // VolumeBSDF: eval is (p, p, p) and pdf is p for the same phase value p (BSDF.h:117-142),
       // so one evaluation gives both
-      V3 phaseFr = bsdfEval<K>(*mat, v.incoming.d, v.scattered.d, v.isect.normal);
+      V3 phaseFr = bsdfEval<K>(s, *mat, v.incoming, v.scattered.d, v.isect);
       float phasePdf = phaseFr.x;
       if (isBlack(phaseFr) || phasePdf == 0.f) break;
       V3 lightSample = uniformSampleOneLight(c, v.scattered, v.isect);
@@ -1431,7 +1480,7 @@ NE_D V3 liLoop(Ctx<K>& c, const PathParams& P, LiVars& v, bool resume) {
       scattered.o = v.isect.hitPoint;
       scattered.d = bsdfSample<K>(*mat, v.incoming.d, v.isect.normal, c.S);
       float pdf = bsdfPdf<K>(*mat, v.incoming.d, scattered.d, v.isect.normal);
-      V3 fr = bsdfEval<K>(*mat, v.incoming.d, scattered.d, v.isect.normal);
+      V3 fr = bsdfEval<K>(s, *mat, v.incoming, scattered.d, v.isect);
       if (isBlack(fr) || pdf == 0.f) break;
       v.T = v.T * ((fr * absDot(v.incoming.d, v.isect.normal)) / pdf);
       v.incoming = scattered;

@@ -242,7 +242,7 @@ NE_NI void transition(Ctx<K>& c, Lane& st, const PathParams& P) {
           break;
         }
         st.T = st.T * st.sampledT;
-        V3 phaseFr = bsdfEval<K>(mat, st.incoming.d, st.scattered.d, st.isect.normal);  // VolumeBSDF: (p, p, p)
+        V3 phaseFr = bsdfEval<K>(s, mat, st.incoming, st.scattered.d, st.isect);  // VolumeBSDF: (p, p, p)
         float phasePdf = phaseFr.x;                                                   // and its pdf p
         if (isBlack(phaseFr) || phasePdf == 0.f) { st.pc = PC_DONE; return; }
         st.phaseRatio = phaseFr / phasePdf;
@@ -264,7 +264,7 @@ NE_NI void transition(Ctx<K>& c, Lane& st, const PathParams& P) {
         sc.o = st.isect.hitPoint;
         sc.d = bsdfSample<K>(mat, st.incoming.d, st.isect.normal, c.S);
         float pdf = bsdfPdf<K>(mat, st.incoming.d, sc.d, st.isect.normal);
-        V3 fr = bsdfEval<K>(mat, st.incoming.d, sc.d, st.isect.normal);
+        V3 fr = bsdfEval<K>(s, mat, st.incoming, sc.d, st.isect);
         if (isBlack(fr) || pdf == 0.f) { st.pc = PC_DONE; return; }
         st.T = st.T * ((fr * absDot(st.incoming.d, st.isect.normal)) / pdf);
         st.incoming = sc;
@@ -312,10 +312,10 @@ NE_NI void transition(Ctx<K>& c, Lane& st, const PathParams& P) {
         st.pc = PC_NEE_BSDF;
         if (st.lightPdf > 0 && !isBlack(st.Li)) {
           if (st.surface) {
-            st.f = bsdfEval<K>(mat, st.neeD, st.woD, st.isect.normal) * fabsf(dot(st.woD, st.isect.normal));
+            st.f = bsdfEval<K>(s, mat, Ray{st.incoming.o, st.neeD}, st.woD, st.isect) * fabsf(dot(st.woD, st.isect.normal));
             st.scatPdf = bsdfPdf<K>(mat, st.neeD, st.woD, st.isect.normal);
           } else {
-            st.f = bsdfEval<K>(mat, st.neeD, st.woD, st.isect.normal);
+            st.f = bsdfEval<K>(s, mat, Ray{st.incoming.o, st.neeD}, st.woD, st.isect);
             st.scatPdf = st.f.x;
           }
           if (!isBlack(st.f)) {
@@ -363,11 +363,11 @@ NE_NI void transition(Ctx<K>& c, Lane& st, const PathParams& P) {
         const DMaterial& mat = *matOf(s, st.isect.prim);
         if (st.surface) {
           st.woD = bsdfSample<K>(mat, st.neeD, st.isect.normal, c.S);
-          st.f = bsdfEval<K>(mat, st.neeD, st.woD, st.isect.normal);
+          st.f = bsdfEval<K>(s, mat, Ray{st.incoming.o, st.neeD}, st.woD, st.isect);
           st.f = st.f * fabsf(dot(st.woD, st.isect.normal));
           st.scatPdf = bsdfPdf<K>(mat, st.neeD, st.woD, st.isect.normal);
         } else {
-          st.f = bsdfEval<K>(mat, st.neeD, st.woD, st.isect.normal);
+          st.f = bsdfEval<K>(s, mat, Ray{st.incoming.o, st.neeD}, st.woD, st.isect);
           st.woD = bsdfSample<K>(mat, st.neeD, v3(0, 1, 0), c.S);
           st.scatPdf = st.f.x;
         }

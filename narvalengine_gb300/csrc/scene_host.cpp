@@ -334,7 +334,7 @@ struct ne_scene_host {
   std::vector<ne_light> lights;
   std::vector<ne_medium> media;
   std::vector<std::vector<float>> grids;
-  std::vector<std::vector<uint8_t>> textures;  // RGBA8 environment maps (their buffers never move)
+  std::vector<std::vector<uint8_t>> textures;  // RGBA8 environment maps and albedo textures (their buffers never move)
   std::vector<ne_instance> all_instances;
   ne_scene_desc desc;
   std::map<std::string, int> material_by_name;
@@ -418,10 +418,20 @@ struct Reader {
     std::string ctx = "Material " + name;
     if (type == "microfacet") {
       const JVal& alb = need(m, "albedo", ctx);
-      if (alb.kind == JVal::STR)
-        throw ParseError(NE_ERR_UNSUPPORTED, ctx + ": albedo textures are not supported (constant albedo only).");
       float albedo[3] = {1, 0, 1};
-      vec3(alb, albedo, ctx + " albedo");
+      if (alb.kind == JVal::STR) {
+        // SceneReader.cpp:80-103: the albedo texture at resources/path, decoded to RGBA8
+        neimg::Image img;
+        std::string err;
+        ne_status st = neimg::loadRGBA8(assetPath(alb.str), img, err);
+        if (st != NE_OK) throw ParseError(st, ctx + ": " + err);
+        S.textures.push_back(std::move(img.rgba));
+        mat.albedo_width = img.width;
+        mat.albedo_height = img.height;
+        mat.albedo_texels = S.textures.back().data();
+      } else {
+        vec3(alb, albedo, ctx + " albedo");
+      }
       memcpy(mat.albedo, albedo, sizeof(albedo));
       float nm[3] = {0, 0, 1};
       bool hasNormal = m.get("normalMap") != nullptr;

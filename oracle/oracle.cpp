@@ -111,6 +111,7 @@ struct Hit {
   V3 hitPoint{0, 0, 0}, normal{0, 0, 0};
   float tNear = 0, tFar = 0;
   int inst = -1, prim = -1;
+  float u = 0, v = 0;  // RayIntersection::uv
 };
 
 struct Sampler {
@@ -267,6 +268,7 @@ struct orc_scene {
   vector<float> triArea;  // Triangle::area per primitive
   vector<OModel> omodels;
   vector<OEnv> env;       // per light: InfiniteAreaLight texture and Distribution2D (empty otherwise)
+  vector<vector<uint8_t>> albedoTex;  // per material: the RGBA8 albedo texture (empty: constant)
 };
 
 namespace {
@@ -362,6 +364,40 @@ inline V3 rectSize(V3 v0, V3 v1) {
   return vabs(v0) + vabs(v1);
 }
 
+// primitives/Rectangle.cpp:91-113 Rectangle::barycentricCoordinates: (lambda, 0) in the
+// triangle (a, b, c), or (lambda, 1) in (d, b, c) when the first leaves [0, 1].
+void rectBarycentric(V3 p, V3 a, V3 b, V3 c, V3 d, float lambda[3], int& second) {
+  float t1[3], t2[3];
+  V3 v0 = b - a, v1 = c - a, v2 = p - a;
+  float d00 = dot(v0, v0), d01 = dot(v0, v1), d11 = dot(v1, v1), d20 = dot(v2, v0), d21 = dot(v2, v1);
+  float denom = d00 * d11 - d01 * d01;
+  t1[1] = (d11 * d20 - d01 * d21) / denom;
+  t1[2] = (d00 * d21 - d01 * d20) / denom;
+  t1[0] = 1.0f - t1[1] - t1[2];
+  v0 = b - d, v1 = c - d, v2 = p - d;
+  d00 = dot(v0, v0), d01 = dot(v0, v1), d11 = dot(v1, v1), d20 = dot(v2, v0), d21 = dot(v2, v1);
+  denom = d00 * d11 - d01 * d01;
+  t2[1] = (d11 * d20 - d01 * d21) / denom;
+  t2[2] = (d00 * d21 - d01 * d20) / denom;
+  t2[0] = 1.0f - t2[1] - t2[2];
+  second = (t1[0] < 0 || t1[1] < 0 || t1[2] < 0 || t1[0] > 1 || t1[1] > 1 || t1[2] > 1) ? 1 : 0;
+  for (int k = 0; k < 3; k++) lambda[k] = second ? t2[k] : t1[k];
+}
+// primitives/Rectangle.cpp:115-157 Rectangle::samplePointOnTexture for the corners SceneReader
+// lays out (io/SceneReader.cpp:407-463): vertex 0 = p0 with uv (0,0), 1 = (p1.x, p0.y, p0.z)
+// with (1,0), 2 = p1 with (1,1), 3 = (p0.x, p1.y, p0.z) with (0,1).
+void rectSamplePointOnTexture(const ne_primitive& p, V3 q, float& u, float& v) {
+  V3 c0 = ld3(p.p0), c2 = ld3(p.p1);
+  V3 c1 = v3(c2.x, c0.y, c0.z), c3 = v3(c0.x, c2.y, c0.z);
+  const float uv[4][2] = {{0, 0}, {1, 0}, {1, 1}, {0, 1}};
+  float l[3];
+  int second;
+  rectBarycentric(q, c0, c1, c2, c3, l, second);
+  const float* first = second ? uv[3] : uv[0];
+  u = (l[0] * first[0] + l[1] * uv[1][0]) + l[2] * uv[2][0];
+  v = (l[0] * first[1] + l[1] * uv[1][1]) + l[2] * uv[2][1];
+}
+
 // primitives/Rectangle.cpp:50-76 Rectangle::intersect and :32-48 containsPoint.
 bool rectIntersect(const ne_primitive& p, const Ray& r, Hit& h) {
   V3 v0 = ld3(p.p0), v1 = ld3(p.p1), n = ld3(p.p2);
@@ -379,6 +415,7 @@ bool rectIntersect(const ne_primitive& p, const Ray& r, Hit& h) {
   h.tFar = t;
   h.normal = n;
   h.hitPoint = q;
+  rectSamplePointOnTexture(p, q, h.u, h.v);
   return true;
 }
 
@@ -409,6 +446,10 @@ bool triIntersect(const orc_scene& s, const ne_primitive& p, const Ray& r, Hit& 
 bool primIntersect(const orc_scene& s, int idx, const Ray& r, Hit& h) {
   const ne_primitive& p = s.prims[idx];
   bool hit = false;
+  // uv (0, 0) unless the primitive computes it (Sphere.cpp:37, AABB.cpp:68; a triangle without
+  // texture coordinates, Triangle.cpp:121-123)
+  h.u = 0;
+  h.v = 0;
   switch (p.type) {
     case NE_PRIM_SPHERE: hit = sphereIntersect(p, r, h); break;
     case NE_PRIM_RECTANGLE: hit = rectIntersect(p, r, h); break;
@@ -724,7 +765,7 @@ inline V3 fresnel(float cosTheta) {
   return f0 + (v3(1, 1, 1) - f0) * nefm::pow5(1.0f - cosTheta);
 }
 // core/GlossyBSDF.cpp:25-48 GlossyBSDF::eval (alpha = roughness^2 at every call).
-V3 glossyEval(const ne_material& m, V3 wi, V3 wo) {
+V3 glossyEval(const ne_material& m, V3 wi, V3 wo, V3 albedo) {
   float rough = texValue(m, NE_TEX_ROUGHNESS).x;
   float alpha = rough * rough;
   V3 H = normalize(wi + wo);
@@ -738,7 +779,6 @@ V3 glossyEval(const ne_material& m, V3 wi, V3 wo) {
   V3 specular = numerator / gmax(denominator, float(kEpsilonD));
   V3 kD = v3(1, 1, 1) - F;
   float metallic = texValue(m, NE_TEX_METALLIC).x;
-  V3 albedo = texValue(m, NE_TEX_ALBEDO);
   kD = kD * (float)(1.0 - (double)metallic);
   return ((albedo / float(kPiD)) * kD + specular) * NdotL;
 }
@@ -802,7 +842,21 @@ float bsdfPdf(const ne_material& m, V3 incoming, V3 scattered, V3 normal) {
   return trans ? phaseEval(m, wi, wo) : glossyPdf(m, wi, wo);
 }
 // core/BSDF.h:135-142 BSDF::eval (frame of ri.normal).
-V3 bsdfEval(const ne_material& m, V3 incoming, V3 scattered, V3 normal) {
+// Material::sampleMaterial(ALBEDO, ri.uv) (materials/Material.h:62-69) as GlossyBSDF::eval reads
+// it (GlossyBSDF.cpp:44): the texture at the hit's uv (Texture::sample, mirror wrap and
+// nearest texel), or the constant.
+V3 albedoOf(const orc_scene& s, const ne_material& m, const Hit& isect) {
+  size_t mi = (size_t)(&m - s.materials.data());
+  if (m.albedo_width > 0 && mi < s.albedoTex.size() && !s.albedoTex[mi].empty()) {
+    const uint8_t* t = &s.albedoTex[mi][4 * ((size_t)texCoord(isect.v, m.albedo_height) * m.albedo_width +
+                                             texCoord(isect.u, m.albedo_width))];
+    return v3(t[0] / 255.0f, t[1] / 255.0f, t[2] / 255.0f);
+  }
+  return texValue(m, NE_TEX_ALBEDO);
+}
+// core/BSDF.h:135-142 for the intersection `isect`.
+V3 bsdfEval(const orc_scene& s, const ne_material& m, V3 incoming, V3 scattered, const Hit& isect) {
+  const V3 normal = isect.normal;
   bool trans = (m.bsdf == NE_BSDF_VOLUME);
   if (!trans && (!sameHemisphere(-incoming, normal) || !sameHemisphere(scattered, normal))) return v3(0, 0, 0);
   V3 ss, ts;
@@ -813,7 +867,7 @@ V3 bsdfEval(const ne_material& m, V3 incoming, V3 scattered, V3 normal) {
     float p = phaseEval(m, wi, wo);
     return v3(p, p, p);
   }
-  return glossyEval(m, wi, wo);
+  return glossyEval(m, wi, wo, albedoOf(s, m, isect));
 }
 
 // ---------------------------------------------------------------- media
@@ -1089,10 +1143,10 @@ V3 estimateDirect(Ctx& c, const Ray& incoming, const Hit& isect, const ne_light&
   bool surface = !(mat.medium >= 0);
   if (lightPdf > 0 && !isBlack(Li)) {
     if (surface) {
-      f = bsdfEval(mat, incoming.d, wo.d, isect.normal) * std::fabs(dot(wo.d, isect.normal));
+      f = bsdfEval(s, mat, incoming.d, wo.d, isect) * std::fabs(dot(wo.d, isect.normal));
       scatteringPdf = bsdfPdf(mat, incoming.d, wo.d, isect.normal);
     } else {
-      f = bsdfEval(mat, incoming.d, wo.d, isect.normal);
+      f = bsdfEval(s, mat, incoming.d, wo.d, isect);
       scatteringPdf = f.x;
     }
     if (!isBlack(f)) {
@@ -1106,11 +1160,11 @@ V3 estimateDirect(Ctx& c, const Ray& incoming, const Hit& isect, const ne_light&
   }
   if (surface) {
     wo.d = bsdfSample(mat, incoming.d, isect.normal, c.S);
-    f = bsdfEval(mat, incoming.d, wo.d, isect.normal);
+    f = bsdfEval(s, mat, incoming.d, wo.d, isect);
     f = f * std::fabs(dot(wo.d, isect.normal));
     scatteringPdf = bsdfPdf(mat, incoming.d, wo.d, isect.normal);
   } else {
-    f = bsdfEval(mat, incoming.d, wo.d, isect.normal);
+    f = bsdfEval(s, mat, incoming.d, wo.d, isect);
     wo.d = bsdfSample(mat, incoming.d, v3(0, 1, 0), c.S);
     scatteringPdf = f.x;
   }
@@ -1175,7 +1229,7 @@ V3 Li(Ctx& c, const Params& P, Ray incoming) {
         continue;
       }
       T = T * sampledT;
-      V3 phaseFr = bsdfEval(*mat, incoming.d, scattered.d, isect.normal);
+      V3 phaseFr = bsdfEval(s, *mat, incoming.d, scattered.d, isect);
       float phasePdf = bsdfPdf(*mat, incoming.d, scattered.d, isect.normal);
       if (isBlack(phaseFr) || phasePdf == 0.f) break;
       V3 lightSample = uniformSampleOneLight(c, scattered, isect);
@@ -1203,7 +1257,7 @@ V3 Li(Ctx& c, const Params& P, Ray incoming) {
       scattered.o = isect.hitPoint;
       scattered.d = bsdfSample(*mat, incoming.d, isect.normal, c.S);
       float pdf = bsdfPdf(*mat, incoming.d, scattered.d, isect.normal);
-      V3 fr = bsdfEval(*mat, incoming.d, scattered.d, isect.normal);
+      V3 fr = bsdfEval(s, *mat, incoming.d, scattered.d, isect);
       if (isBlack(fr) || pdf == 0.f) break;
       T = T * ((fr * absDot(incoming.d, isect.normal)) / pdf);
       incoming = scattered;
@@ -1318,6 +1372,12 @@ orc_scene* orc_scene_create(const ne_scene_desc* d) {
       for (size_t k = 0; k < n; k++) mx = gmax(mx, s->grids[i][k]);  // GridMedia.h:16-21
       s->invMax[i] = 1.0f / mx;
     }
+  }
+  s->albedoTex.resize(d->n_materials);
+  for (uint32_t i = 0; i < d->n_materials; i++) {
+    const ne_material& m = s->materials[i];
+    if (m.albedo_width > 0 && m.albedo_height > 0 && m.albedo_texels)
+      s->albedoTex[i].assign(m.albedo_texels, m.albedo_texels + (size_t)m.albedo_width * m.albedo_height * 4);
   }
   // InfiniteAreaLight's constructor (lights/InfiniteAreaLight.h:20-40) for textured lights
   s->env.resize(d->n_lights);

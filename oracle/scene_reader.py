@@ -380,12 +380,18 @@ class OracleSceneDesc:
         typ = _need(m, "type", f"Material {name}")
         ctx = f"Material {name}"
         mat = dict(bsdf=0, light=-1, medium=-1, phase=0, g=f32(0), albedo=[f32(0)] * 3, roughness=f32(0),
-                   metallic=f32(0), normal_map=[f32(0)] * 3, tex_present=0, tex_types=0)
+                   metallic=f32(0), normal_map=[f32(0)] * 3, tex_present=0, tex_types=0, albedo_tex=None)
         if typ == "microfacet":
             alb = _need(m, "albedo", ctx)
             if isinstance(alb, str):
-                raise SceneError(f"{ctx}: albedo textures are not restated by the oracle's reader")
-            mat["albedo"] = get_vec3(alb, (1.0, 0.0, 1.0))
+                # :80-103: the texture loaded by ResourceManager::loadTexture as RGBA8; the constant
+                # keeps its default (1, 0, 1)
+                mat["albedo"] = [f32(1), f32(0), f32(1)]
+                w, h, rgba = self._load_rgba8(alb, ctx)
+                self.textures.append(np.ascontiguousarray(rgba))
+                mat["albedo_tex"] = (w, h, len(self.textures) - 1)
+            else:
+                mat["albedo"] = get_vec3(alb, (1.0, 0.0, 1.0))
             has_normal = "normalMap" in m
             mat["normal_map"] = get_vec3(m["normalMap"], (0, 0, 1)) if has_normal else [f32(0), f32(0), f32(1)]
             mat["roughness"] = get_float(_need(m, "roughness", ctx))
@@ -407,10 +413,7 @@ class OracleSceneDesc:
             mat["light"] = self._new_light(type=1, le=le, direction=direction)
         elif typ == "infiniteAreaLight":
             if "path" in m:
-                data = open(self._asset(m["path"]), "rb").read() if os.path.exists(self._asset(m["path"])) else None
-                if data is None:
-                    raise SceneError(f"{ctx}: missing texture {m['path']}")
-                w, h, rgba = _png_rgba8(data)
+                w, h, rgba = self._load_rgba8(m["path"], ctx)
                 if h > w:
                     raise SceneError(f"{ctx}: environment maps taller than wide read past the image in the reference")
                 self.textures.append(np.ascontiguousarray(rgba))
@@ -453,6 +456,12 @@ class OracleSceneDesc:
             raise SceneError("Invalid material type while reading scene from json file.")
         self.materials.append(mat)
         self.mat_by_name[name] = len(self.materials) - 1
+
+    def _load_rgba8(self, rel, ctx):
+        full = self._asset(rel)
+        if not os.path.exists(full):
+            raise SceneError(f"{ctx}: missing texture {rel}")
+        return _png_rgba8(open(full, "rb").read())
 
     def _load_vol(self, path):
         """core/ResourceManager.cpp:222-288: line 1 "X Y Z " (each value ended by a space), line 2
@@ -773,6 +782,10 @@ class OracleSceneDesc:
             o.g, o.roughness, o.metallic = float(m["g"]), float(m["roughness"]), float(m["metallic"])
             o.albedo[:] = [float(v) for v in m["albedo"]]
             o.normal_map[:] = [float(v) for v in m["normal_map"]]
+            if m.get("albedo_tex") is not None:
+                w, h, ti = m["albedo_tex"]
+                o.albedo_width, o.albedo_height = w, h
+                o.albedo_texels = self.textures[ti].ctypes.data_as(C.POINTER(C.c_uint8))
         self._mm = (C.c_uint32 * max(1, len(self.model_materials)))(*self.model_materials)
         self._lights = (A.NeLight * max(1, len(self.lights)))()
         for i, L in enumerate(self.lights):

@@ -46,6 +46,14 @@ def assert_same_desc(a, b):
             assert bad.size == 0, f"prims differ at primitive {bad[0] * 4 // C.sizeof(typ)}"
             continue
         for i in range(n):
+            if name == "materials":  # every field but the texel pointer, then the texels
+                ma, mb = a.materials[i], b.materials[i]
+                k = _abi.NeMaterial.albedo_texels.offset
+                assert _bytes(a.materials, i, typ)[:k] == _bytes(b.materials, i, typ)[:k], f"materials[{i}] differs"
+                if ma.albedo_width:
+                    nt = ma.albedo_width * ma.albedo_height * 4
+                    assert C.string_at(ma.albedo_texels, nt) == C.string_at(mb.albedo_texels, nt), f"materials[{i}] texels"
+                continue
             assert _bytes(getattr(a, name), i, typ) == _bytes(getattr(b, name), i, typ), f"{name}[{i}] differs"
     for i in range(a.n_lights):
         la, lb = a.lights[i], b.lights[i]
@@ -106,11 +114,14 @@ def varied_scene(tmp_path):
                                        "f -4 -3 -1\n")
     sky = np.random.default_rng(3).integers(0, 256, size=(8, 16, 3), dtype=np.uint8)
     (tmp_path / "sky.png").write_bytes(encode_png(sky, 2, 8))
+    wall = np.random.default_rng(4).integers(0, 256, size=(6, 10, 4), dtype=np.uint8)
+    (tmp_path / "wall.png").write_bytes(encode_png(wall, 6, 8))
     T = lambda p, r=(0, 0, 0), s=(1, 1, 1): {"position": list(p), "rotation": list(r), "scale": list(s)}
     mats = [
         {"name": "white", "type": "microfacet", "roughness": 0.37, "metallic": 0.2, "albedo": [0.7, 0.61, 0.05]},
         {"name": "bumpy", "type": "microfacet", "roughness": 0.8, "metallic": 0.0, "albedo": [0.3, 0.3, 0.3],
          "normalMap": [0.5, 0.5, 1.0]},
+        {"name": "painted", "type": "microfacet", "roughness": 0.6, "metallic": 0.1, "albedo": "wall.png"},
         {"name": "lamp", "type": "emitter", "albedo": [5.0, 4.5, 3.1]},
         {"name": "ball_lamp", "type": "emitter", "albedo": [2.0, 2.5, 1.0]},
         {"name": "point_lamp", "type": "emitter", "albedo": [1.0, 1.0, 1.0]},
@@ -132,6 +143,8 @@ def varied_scene(tmp_path):
          "materialName": "white"},
         {"name": "wall2", "type": "rectangle", "transform": T((-0.7, 0.1, 0), (90, 0, 0), (1, 1, 1)),
          "materialName": "bumpy"},
+        {"name": "mural", "type": "rectangle", "transform": T((0, 1, 0.9), (0, 0, 0), (1.5, 1, 1)),
+         "materialName": "painted"},
         {"name": "light", "type": "rectangle", "transform": T((0, 1.99, 0.2), (-90, 5, 0), (0.5, 0.25, 1)),
          "materialName": "lamp"},
         {"name": "ball", "type": "sphere", "radius": 0.35, "transform": T((-0.4, 0.35, 0.3), (10, 20, 30)),

@@ -156,7 +156,7 @@ def base_scene():
     (lambda d: d["primitives"].append({"name": "m", "type": "obj", "path": "a.obj",
                                        "transform": {"position": [0, 0, 0], "scale": [1, 1, 1],
                                                      "rotation": [0, 0, 0]}}), -6),
-    (lambda d: d["materials"][0].update(albedo="tex.png"), -6),
+    (lambda d: d["materials"][0].update(albedo="missing_tex.png"), -3),  # albedo texture file absent
     (lambda d: d["materials"].append({"name": "v", "type": "volume", "scattering": [1, 1, 1],
                                       "absorption": [0, 0, 0], "phaseFunction": "hg", "g": 0.1,
                                       "path": "missing.vol", "density": 1}), -3),
