@@ -1472,6 +1472,8 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
     d.inv_max_density = 1.0f;
     if (s.type == NE_MEDIUM_GRID) {
       if (!s.grid || !s.res[0] || !s.res[1] || !s.res[2]) return cleanup(fail(ctx, NE_ERR_INVALID_ARG, "grid medium without voxels"));
+      if (s.res[0] > (1u << 24) || s.res[1] > (1u << 24) || s.res[2] > (1u << 24))
+        return cleanup(fail(ctx, NE_ERR_INVALID_ARG, "grid resolution above 2^24 voxels per axis"));
       size_t n = (size_t)s.res[0] * s.res[1] * s.res[2];
       gridMedia.push_back(i);  // invMaxDensity from the device copy of the grid, below
       memcpy(d.res, s.res, 12);

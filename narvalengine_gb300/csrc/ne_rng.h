@@ -56,6 +56,29 @@ NE_RNG_HD Block philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3
   return b;
 }
 
+// The same generator with its ten rounds unrolled (identical words), for the few call sites
+// that draw inside the tracking loops, where the loop's branch and counter per round cost
+// more than the extra code.
+NE_RNG_HD Block philox4x32_10_unrolled(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1) {
+  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+  const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+  for (int r = 0; r < 10; ++r) {
+    uint32_t hi0, lo0, hi1, lo1;
+    mulhilo(M0, c0, &hi0, &lo0);
+    mulhilo(M1, c2, &hi1, &lo1);
+    uint32_t n0 = hi1 ^ c1 ^ k0;
+    uint32_t n2 = hi0 ^ c3 ^ k1;
+    c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+    k0 += W0; k1 += W1;
+  }
+  Block b;
+  b.w[0] = c0; b.w[1] = c1; b.w[2] = c2; b.w[3] = c3;
+  return b;
+}
+
 NE_RNG_HD float word_to_u01(uint32_t w) {
   return (float)(w >> 8) * 0x1.0p-24f;
 }

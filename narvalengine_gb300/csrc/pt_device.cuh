@@ -176,7 +176,7 @@ struct Sampler {
   NE_D float randomInline() {
     uint32_t b = dim >> 2;
     if (b != blk) {
-      nerng::Block r = nerng::philox4x32_10(b, key.sample, key.pixel, key.stream, key.seed_lo, key.seed_hi);
+      nerng::Block r = nerng::philox4x32_10_unrolled(b, key.sample, key.pixel, key.stream, key.seed_lo, key.seed_hi);
       w0 = r.w[0]; w1 = r.w[1]; w2 = r.w[2]; w3 = r.w[3];
       blk = b;
     }
@@ -912,7 +912,9 @@ NE_D float sampleAt(Ctx<K>& c, const DMedium& M, const Ray& r, float t) {
   g = vmin(vmax(v3(0, 0, 0), g), res);
   float fx = floorf(g.x), fy = floorf(g.y), fz = floorf(g.z);
   int ix = (int)fx, iy = (int)fy, iz = (int)fz;
-  V3 d = g - v3((float)ix, (float)iy, (float)iz);
+  // g is clamped to [0, res] (res <= 2^24), so each floor is an integer-valued float that
+  // equals (float)(int) of itself: the fraction needs no conversion back
+  V3 d = g - v3(fx, fy, fz);
   float c000, c100, c010, c110, c001, c101, c011, c111;
   if (M.cells) {
     size_t cell = ((size_t)iz * (M.res[1] + 1) + (size_t)iy) * (M.res[0] + 1) + (size_t)ix;
