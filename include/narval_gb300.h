@@ -324,6 +324,11 @@ typedef struct ne_cache_render_params {
   uint32_t train_stride;  /* 0: no training paths */
   int32_t train_steps;
   uint32_t train_batch;   /* samples per optimiser step; 0: all of the frame's samples */
+  int32_t train_suffix;   /* 0: a training path runs to its end; n > 0: it ends in the cache too,
+                             at its first scattering vertex n or more bounces after the recorded
+                             one: it adds throughput x cache(end vertex) to the image, and its
+                             training sample's target gets (throughput ratio) x cache(end vertex)
+                             added (the network's own prediction for the rest of the path) */
 } ne_cache_render_params;
 typedef struct ne_cache_render_stats {
   uint64_t queries;        /* paths that ended in the cache */

@@ -260,7 +260,8 @@ class Scene:
         return {f: getattr(stats, f) for f, _ in NeRenderStats._fields_ }
 
     def render_cached(self, cache: "RadianceCache", bounce: int = 2, train_stride: int = 0, train_steps: int = 0,
-                      train_batch: int = 0, params: NeRenderParams | None = None, out=None, **kw):
+                      train_batch: int = 0, params: NeRenderParams | None = None, out=None, train_suffix: int = 0,
+                      **kw):
         """ne_render_cached: (image or None, render stats, cache stats)."""
         p = params if params is not None else render_params(**kw)
         W, H = self.host.width, self.host.height
@@ -272,7 +273,7 @@ class Scene:
         else:
             img = out if out is not None else np.empty((H, W, 3), dtype=np.float32)
             ptr = _ptr(img)
-        cp = _abi.NeCacheRenderParams(bounce, train_stride, train_steps, train_batch)
+        cp = _abi.NeCacheRenderParams(bounce, train_stride, train_steps, train_batch, train_suffix)
         stats = NeRenderStats()
         cst = _abi.NeCacheRenderStats()
         self.ctx.check(library().ne_render_cached(self._h, cache._h, C.byref(p), C.byref(cp), ptr, C.byref(stats),

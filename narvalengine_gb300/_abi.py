@@ -108,7 +108,7 @@ class NeViewsStats(C.Structure):
 
 class NeCacheRenderParams(C.Structure):
     _fields_ = [("bounce", C.c_int32), ("train_stride", C.c_uint32), ("train_steps", C.c_int32),
-                ("train_batch", C.c_uint32)]
+                ("train_batch", C.c_uint32), ("train_suffix", C.c_int32)]
 
 
 class NeCacheRenderStats(C.Structure):

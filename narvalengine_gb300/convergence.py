@@ -102,7 +102,7 @@ def time_to_relmse(scene, ref: np.ndarray, target: float = 1e-3, seed: int = 0, 
 
 def time_to_relmse_cached(scene, cache, ref: np.ndarray, target: float = 1e-3, seed: int = 0,
                           max_spp: int = 1 << 16, frame_spp: int = 4, bounce: int = 2, train_stride: int = 16,
-                          train_steps: int = 4, train_batch: int = 1 << 16) -> dict:
+                          train_steps: int = 4, train_batch: int = 1 << 16, train_suffix: int = 0) -> dict:
     """Progressive rendering with the radiance cache trained online: frames of `frame_spp`
     samples, each rendered with the cache as it stands and then used for `train_steps`
     optimiser steps on the frame's training samples. The running FP64 mean of the frames is
@@ -117,7 +117,8 @@ def time_to_relmse_cached(scene, cache, ref: np.ndarray, target: float = 1e-3, s
     hit = None
     while have < max_spp and ci < len(checks):
         img, st, cst = scene.render_cached(cache, bounce=bounce, train_stride=train_stride, train_steps=train_steps,
-                                           train_batch=train_batch, seed=seed, spp=frame_spp, sample_offset=have)
+                                           train_batch=train_batch, seed=seed, spp=frame_spp, sample_offset=have,
+                                           train_suffix=train_suffix)
         ms += st["total_ms"]
         for k in ("path_ms", "infer_ms", "train_ms", "queries", "train_samples"):
             parts[k] += cst[k]
@@ -133,7 +134,7 @@ def time_to_relmse_cached(scene, cache, ref: np.ndarray, target: float = 1e-3, s
                 hit = curve[-1]
                 break
     return {"target": target, "reached": hit is not None, "spp": hit["spp"] if hit else None,
-            "ms": hit["ms"] if hit else None, "frame_spp": frame_spp, "bounce": bounce,
+            "ms": hit["ms"] if hit else None, "frame_spp": frame_spp, "bounce": bounce, "train_suffix": train_suffix,
             "train_stride": train_stride, "train_steps": train_steps, "train_batch": train_batch, "totals": parts,
             "curve": curve}
 
@@ -153,6 +154,9 @@ def main(argv=None):
     ap.add_argument("--bounce", type=int, nargs="+", default=[2], help="cache termination bounce(s) to measure")
     ap.add_argument("--train-steps", type=int, default=4)
     ap.add_argument("--train-stride", type=int, default=16)
+    ap.add_argument("--train-suffix", type=int, nargs="+", default=[0],
+                    help="bounces a training path runs past its recorded vertex before it ends in the cache too "
+                         "(0: to its end); each value is measured")
     args = ap.parse_args(argv)
     path = args.scene if args.scene.endswith(".json") else os.path.join(ne.SCENES_DIR, args.scene + ".json")
     if args.resolution:
@@ -173,13 +177,15 @@ def main(argv=None):
     if args.cache:
         res["cache"] = []
         for bounce in args.bounce:
-            cache = ne.RadianceCache(ctx, seed=1)
-            r = time_to_relmse_cached(scene, cache, ref, args.target, max_spp=args.max_spp, frame_spp=args.frame_spp,
-                                      bounce=bounce, train_steps=args.train_steps, train_stride=args.train_stride)
-            cache.close()
-            if res["reached"] and r["reached"]:
-                r["time_ratio_vs_plain"] = r["ms"] / res["ms"]
-            res["cache"].append(r)
+            for suffix in args.train_suffix:
+                cache = ne.RadianceCache(ctx, seed=1)
+                r = time_to_relmse_cached(scene, cache, ref, args.target, max_spp=args.max_spp,
+                                          frame_spp=args.frame_spp, bounce=bounce, train_steps=args.train_steps,
+                                          train_stride=args.train_stride, train_suffix=suffix)
+                cache.close()
+                if res["reached"] and r["reached"]:
+                    r["time_ratio_vs_plain"] = r["ms"] / res["ms"]
+                res["cache"].append(r)
     out = {"scene": os.path.basename(path), "resolution": [host.width, host.height], "ref_spp": args.ref_spp,
            "ref_paths": host.width * host.height * args.ref_spp, "ref_device_ms": ref_ms,
            "ref_wall_s": time.time() - t0, "ref_dropped_paths": info["dropped_paths"], "relmse_eps": EPS,

@@ -128,8 +128,10 @@ struct ne_cache {
   uint32_t* q_idx = nullptr;
   size_t q_cap = 0;
   float* tr = nullptr;       // t_cap x (pos 3, dir 3, value 3)
+  float* tq = nullptr;       // t_cap x (pos 3, dir 3, throughput ratio 3): training paths' end queries
+  uint32_t* tq_idx = nullptr;
   size_t t_cap = 0;
-  uint32_t* counts = nullptr;  // [0] queries, [1] training samples
+  uint32_t* counts = nullptr;  // [0] queries, [1] training samples, [2] training end queries
   CacheIO* d_io = nullptr;
   CacheIO io;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -2148,7 +2150,7 @@ void ne_cache_destroy(ne_cache* c) {
   cudaSetDevice(c->ctx->device);
   cudaStreamSynchronize(c->ctx->stream);
   void* bufs[] = {c->P, c->m, c->v, c->wfwd, c->wbwd, c->bias, c->part, c->loss_part, c->d_loss, c->grad, c->acts,
-                  c->out, c->q, c->q_idx, c->tr, c->counts, c->d_io};
+                  c->out, c->q, c->q_idx, c->tr, c->tq, c->tq_idx, c->counts, c->d_io};
   for (void* p : bufs)
     if (p) cudaFree(p);
   for (cudaEvent_t e : c->ev)
@@ -2293,7 +2295,8 @@ ne_status ne_render_cached(ne_scene* sc, ne_cache* c, const ne_render_params* p,
   ne_context* ctx = sc->ctx;
   if (sc->feature_set != K_VOLUME || !(sc->features & FT_GRID))
     return fail(ctx, NE_ERR_UNSUPPORTED, "ne_render_cached: the scene's media must be grid media");
-  if (cp->bounce < 0 || cp->train_steps < 0) return fail(ctx, NE_ERR_INVALID_ARG, "ne_render_cached: bad parameters");
+  if (cp->bounce < 0 || cp->train_steps < 0 || cp->train_suffix < 0)
+    return fail(ctx, NE_ERR_INVALID_ARG, "ne_render_cached: bad parameters");
   NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
   const int W = sc->settings.width, H = sc->settings.height;
   int spp = (p && p->spp > 0) ? p->spp : sc->settings.spp;
@@ -2327,13 +2330,18 @@ ne_status ne_render_cached(ne_scene* sc, ne_cache* c, const ne_render_params* p,
     c->q_cap = total;
   }
   if (c->t_cap < tcap) {
-    if (c->tr) cudaFree(c->tr);
-    c->tr = nullptr;
+    void* bufs[] = {c->tr, c->tq, c->tq_idx};
+    for (void* b : bufs)
+      if (b) cudaFree(b);
+    c->tr = c->tq = nullptr;
+    c->tq_idx = nullptr;
     c->t_cap = 0;
     NE_CUDA(cudaMalloc(&c->tr, tcap * 9 * sizeof(float)), "cudaMalloc(training samples)");
+    NE_CUDA(cudaMalloc(&c->tq, tcap * 9 * sizeof(float)), "cudaMalloc(training end queries)");
+    NE_CUDA(cudaMalloc(&c->tq_idx, tcap * sizeof(uint32_t)), "cudaMalloc(training end queries)");
     c->t_cap = tcap;
   }
-  if (!c->counts) NE_CUDA(cudaMalloc(&c->counts, 2 * sizeof(uint32_t)), "cudaMalloc");
+  if (!c->counts) NE_CUDA(cudaMalloc(&c->counts, 3 * sizeof(uint32_t)), "cudaMalloc");
   if (!c->d_io) NE_CUDA(cudaMalloc(&c->d_io, sizeof(CacheIO)), "cudaMalloc");
   for (cudaEvent_t& e : c->ev)
     if (!e) NE_CUDA(cudaEventCreate(&e), "cudaEventCreate");
@@ -2351,8 +2359,14 @@ ne_status ne_render_cached(ne_scene* sc, ne_cache* c, const ne_render_params* p,
   io.t_cap = (uint32_t)c->t_cap;
   io.train_stride = cp->train_stride;
   io.bounce = cp->bounce;
+  io.train_suffix = cp->train_suffix;
+  io.tq_pos = c->tq;
+  io.tq_dir = c->tq + 3 * c->t_cap;
+  io.tq_thr = c->tq + 6 * c->t_cap;
+  io.tq_idx = c->tq_idx;
+  io.tq_count = c->counts + 2;
   NE_CUDA(cudaMemcpyAsync(c->d_io, &io, sizeof(CacheIO), cudaMemcpyHostToDevice, ctx->stream), "cudaMemcpyAsync");
-  NE_CUDA(cudaMemsetAsync(c->counts, 0, 2 * sizeof(uint32_t), ctx->stream), "cudaMemsetAsync");
+  NE_CUDA(cudaMemsetAsync(c->counts, 0, 3 * sizeof(uint32_t), ctx->stream), "cudaMemsetAsync");
   NE_CUDA(cudaMemsetAsync(ctx->d_err, 0, 4, ctx->stream), "cudaMemsetAsync");
   NE_CUDA(cudaMemsetAsync(ctx->d_counter, 0, 5 * sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync");
   bool devOut = flags & NE_RENDER_OUT_DEVICE;
@@ -2393,6 +2407,12 @@ ne_status ne_render_cached(ne_scene* sc, ne_cache* c, const ne_render_params* p,
   NeMlpForward f = {io.q_pos, io.q_dir, nullptr, io.q_cap, c->counts, c->wfwd, c->bias, nullptr, nullptr, io.q_thr,
                     io.q_idx, sc->d_paths};
   NE_CUDA(ne_mlp_forward(ctx->stream, f, ctx->d_err), "k_mlp_forward launch");
+  if (cp->train_suffix > 0 && cp->train_stride) {
+    // the training paths' end vertices: their answers complete the training targets
+    NeMlpForward ft = {io.tq_pos, io.tq_dir, nullptr, io.t_cap, c->counts + 2, c->wfwd, c->bias, nullptr, nullptr,
+                       io.tq_thr, io.tq_idx, io.t_val};
+    NE_CUDA(ne_mlp_forward(ctx->stream, ft, ctx->d_err), "k_mlp_forward launch");
+  }
   int rblocks = (int)std::min<uint64_t>((npix + 255) / 256, (uint64_t)ctx->sm_count * 16);
   k_reduce<<<std::max(1, rblocks), 256, 0, ctx->stream>>>(sc->d_paths, (uint32_t)npix, (uint32_t)spp, cw, W, d_img);
   NE_CUDA(cudaGetLastError(), "k_reduce launch");

@@ -237,6 +237,15 @@ struct CacheIO {
   uint32_t t_cap;
   uint32_t train_stride;  // a path is a training path when hash(index) % train_stride == 0
   int bounce;
+  // training paths ending in the cache (train_suffix > 0): at their first scattering vertex
+  // train_suffix or more bounces after the recorded one, a query whose answer times tq_thr is
+  // added to the training sample tq_idx's target
+  int train_suffix;
+  float* tq_pos;
+  float* tq_dir;
+  float* tq_thr;
+  uint32_t* tq_idx;
+  uint32_t* tq_count;
 };
 
 NE_D Ray transformRay(const Ray& r, const float* m) { return Ray{mul4(m, r.o, 1.0f), mul4(m, r.d, 0.0f)}; }
@@ -1383,6 +1392,7 @@ NE_D V3 liLoop(Ctx<K>& c, const PathParams& P, LiVars& v, bool resume) {
   const float inf = __int_as_float(0x7f800000);
   // K_CACHE training paths: the vertex the sample is recorded at
   bool recorded = false;
+  int recordB = 0;
   V3 vPos = v3(0, 0, 0), vDir = v3(0, 0, 0), vL = v3(0, 0, 0), vT = v3(0, 0, 0);
   for (; v.b < P.bounces; v.b++) {
     const int b = v.b;
@@ -1446,10 +1456,42 @@ NE_D V3 liLoop(Ctx<K>& c, const PathParams& P, LiVars& v, bool resume) {
         return v.L;
       }
       recorded = true;
+      recordB = b;
       vPos = xo;
       vDir = v.incoming.d;
       vL = v.L;
       vT = v.T;
+    } else if ((K & K_CACHE) && medium && recorded && c.cio->train_suffix > 0 && b >= recordB + c.cio->train_suffix) {
+      // a training path ends in the cache as well: the image gets throughput x cache(vertex),
+      // the training sample the radiance gathered so far plus (throughput ratio) x cache(vertex)
+      const CacheIO& io = *c.cio;
+      V3 xo = mul4(s.instances[v.isect.inst].ocs, v.scattered.o, 1.0f);
+      uint32_t q = appendSlot(io.q_count);
+      if (q < io.q_cap) {
+        io.q_pos[3 * q] = xo.x; io.q_pos[3 * q + 1] = xo.y; io.q_pos[3 * q + 2] = xo.z;
+        io.q_dir[3 * q] = v.incoming.d.x; io.q_dir[3 * q + 1] = v.incoming.d.y;
+        io.q_dir[3 * q + 2] = v.incoming.d.z;
+        io.q_thr[3 * q] = v.T.x; io.q_thr[3 * q + 1] = v.T.y; io.q_thr[3 * q + 2] = v.T.z;
+        io.q_idx[q] = c.pidx;
+      }
+      uint32_t ts = appendSlot(io.t_count);
+      if (ts < io.t_cap) {
+        V3 d = v.L - vL;
+        io.t_pos[3 * ts] = vPos.x; io.t_pos[3 * ts + 1] = vPos.y; io.t_pos[3 * ts + 2] = vPos.z;
+        io.t_dir[3 * ts] = vDir.x; io.t_dir[3 * ts + 1] = vDir.y; io.t_dir[3 * ts + 2] = vDir.z;
+        io.t_val[3 * ts] = vT.x > 0 ? d.x / vT.x : 0.0f;
+        io.t_val[3 * ts + 1] = vT.y > 0 ? d.y / vT.y : 0.0f;
+        io.t_val[3 * ts + 2] = vT.z > 0 ? d.z / vT.z : 0.0f;
+        uint32_t tq = appendSlot(io.tq_count);  // at most one per training sample: tq < t_cap
+        io.tq_pos[3 * tq] = xo.x; io.tq_pos[3 * tq + 1] = xo.y; io.tq_pos[3 * tq + 2] = xo.z;
+        io.tq_dir[3 * tq] = v.incoming.d.x; io.tq_dir[3 * tq + 1] = v.incoming.d.y;
+        io.tq_dir[3 * tq + 2] = v.incoming.d.z;
+        io.tq_thr[3 * tq] = vT.x > 0 ? v.T.x / vT.x : 0.0f;
+        io.tq_thr[3 * tq + 1] = vT.y > 0 ? v.T.y / vT.y : 0.0f;
+        io.tq_thr[3 * tq + 2] = vT.z > 0 ? v.T.z / vT.z : 0.0f;
+        io.tq_idx[tq] = ts;
+      }
+      return v.L;
     }
     if (medium) {
       // VolumeBSDF: eval is (p, p, p) and pdf is p for the same phase value p (BSDF.h:117-142),

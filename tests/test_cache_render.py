@@ -57,6 +57,27 @@ def test_zero_network_only_truncates(env):
     assert img.sum() < plain.sum()
 
 
+def test_training_suffix_ends_training_paths_in_the_cache(env):
+    """With train_suffix n, a training path recorded at its first scattering vertex at or after
+    `bounce` ends in the cache n bounces later. With a zero network and every path a training
+    path, bounce 2 and n = 1 therefore render the image of bounce 3 without training, bit for
+    bit (the medium scene scatters only in the medium, so the recorded vertex is bounce 2's),
+    while each training path still records a sample."""
+    ne, ctx, scene, cache = env
+    cache.set_params(np.zeros(ne.RadianceCache.N_PARAMS, np.float32))
+    want, _, cw = scene.render_cached(cache, bounce=3, seed=4, spp=4)
+    img, _, ci = scene.render_cached(cache, bounce=2, train_stride=1, train_suffix=1, seed=4, spp=4)
+    assert cw["queries"] > 100 and ci["train_samples"] > 100
+    assert ci["queries"] == cw["queries"]
+    assert np.array_equal(img.view(np.uint32), want.view(np.uint32))
+    # a trained network: the end vertices' answers go into the targets, the loss stays finite
+    cache.set_params(np.random.default_rng(2).normal(0, 0.05, ne.RadianceCache.N_PARAMS).astype(np.float32))
+    img, _, ci = scene.render_cached(cache, bounce=2, train_stride=4, train_suffix=2, train_steps=2, seed=5, spp=4)
+    assert np.isfinite(img).all() and np.isfinite(ci["loss"]) and ci["train_samples"] > 0
+    with pytest.raises(ne.NarvalError):
+        scene.render_cached(cache, bounce=2, train_stride=4, train_suffix=-1, seed=5, spp=1)
+
+
 def test_trained_cache_reduces_bias(env):
     """On the dense cloud (albedo 0.99) paths ended at their second scattering event lose a
     visible share of the light; the trained network restores most of it. relMSE against an
