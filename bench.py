@@ -542,6 +542,17 @@ def main():
     roofline["l2"] = {"achieved": achieved, "peak": l2_gbs, "unit": "GB/s", "frac": achieved / l2_gbs,
                       "peak_source": "measured here: ne_measure_read_bandwidth, read-only kernel reading a 48 MiB "
                                      "(L2-resident) buffer 21 times per launch, 10 launches"}
+    cell_bytes = max([(m.res[0] + 1) * (m.res[1] + 1) * (m.res[2] + 1) * BYTES_PER_LOOKUP
+                      for m in host.desc.media[:host.desc.n_media] if m.type == 0] or [0])
+    if lookups and cell_bytes:
+        # the lookups' own ceiling: random 32-byte reads from a buffer the size of the cell array
+        rate = ctx.random_read_rate(cell_bytes, 10)
+        got = lookups / (k_ms / 1e3)
+        roofline["gather"] = {"achieved": got, "peak": rate, "unit": "lookups/s", "frac": got / rate,
+                              "buffer_bytes": cell_bytes,
+                              "peak_source": "measured here: ne_measure_random_read, random 32-byte reads "
+                                             "(hashed indices, 4 in flight per thread) from a buffer the size of "
+                                             "the scene's cell array, 10 launches"}
     prof = pinned_profile(args.scene)
     if prof is not None:
         if prof["tuning"] == tuning:

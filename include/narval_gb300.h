@@ -233,6 +233,11 @@ ne_status ne_context_flush_l2(ne_context* ctx, size_t bytes);
  * *gbs = bytes read / time. A buffer well inside the 129 MB L2 measures L2 bandwidth, one
  * well beyond it HBM bandwidth. */
 ne_status ne_measure_read_bandwidth(ne_context* ctx, size_t bytes, int iters, double* gbs);
+/* Rate of random 32-byte reads from a `bytes` buffer, the access a density-cell lookup makes
+ * (two 16-byte loads of one 32-byte-aligned record at a hashed index, many reads in flight
+ * per thread): *reads_per_s over `iters` launches. Sized like a scene's cell array, it is
+ * the ceiling for that scene's lookups; bytes / 32 must fit in 32 bits. */
+ne_status ne_measure_random_read(ne_context* ctx, size_t bytes, int iters, double* reads_per_s);
 
 /* Device copies of the shared elementary functions, for bit-exactness checks.
  * fn: 0 log, 1 exp, 2 sin, 3 cos, 4 acos, 5 pow5, 6 atan2(x[i], x[i ^ 1]) (elements paired;

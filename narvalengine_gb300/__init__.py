@@ -192,6 +192,12 @@ class Context:
         self.check(library().ne_measure_read_bandwidth(self._h, nbytes, iters, C.byref(gbs)))
         return gbs.value
 
+    def random_read_rate(self, nbytes: int, iters: int = 10) -> float:
+        """Random 32-byte reads per second from an `nbytes` buffer (ne_measure_random_read)."""
+        r = C.c_double()
+        self.check(library().ne_measure_random_read(self._h, nbytes, iters, C.byref(r)))
+        return r.value
+
     def fmath(self, fn: int, x: np.ndarray) -> np.ndarray:
         x = np.ascontiguousarray(x, dtype=np.float32)
         out = np.empty_like(x)

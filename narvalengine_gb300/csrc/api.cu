@@ -578,6 +578,37 @@ __global__ void __launch_bounds__(512) k_read_bw(const uint4* __restrict__ p, si
   if (acc == 0x9e3779b9u) sink[0] = acc;
 }
 
+// Random 32-byte reads (two 16-byte loads through the read-only path, as a density-cell
+// lookup makes them) at hashed record indices: each thread issues its reads in groups of
+// four independent ones, so the rate measured is the memory system's, not one thread's
+// latency. Index hash: the "lowbias32" integer mix (Wellons), over a counter per read.
+__device__ __forceinline__ uint32_t mix32(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7feb352du;
+  x ^= x >> 15;
+  x *= 0x846ca68bu;
+  x ^= x >> 16;
+  return x;
+}
+__global__ void __launch_bounds__(512) k_random_read(const float4* __restrict__ p, uint32_t nrec, uint32_t reads,
+                                                     uint32_t seed, uint32_t* sink) {
+  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+  float acc = 0.0f;
+  for (uint32_t r = 0; r < reads; r += 4) {
+    float4 a[4], b[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const uint32_t h = mix32((tid * reads + r + (uint32_t)k) ^ seed);
+      const size_t i = (size_t)(((uint64_t)h * nrec) >> 32);
+      a[k] = __ldg(p + 2 * i);
+      b[k] = __ldg(p + 2 * i + 1);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) acc += (a[k].x + a[k].w) * (b[k].y + b[k].z);
+  }
+  if (acc == 1234.5f) sink[0] = tid;
+}
+
 __global__ void k_fmath(int fn, const float* __restrict__ x, size_t n, float* __restrict__ out) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     float v = x[i], r;
@@ -1950,6 +1981,33 @@ ne_status ne_measure_read_bandwidth(ne_context* ctx, size_t bytes, int iters, do
   float ms = 0;
   NE_CUDA(cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]), "cudaEventElapsedTime");
   *gbs = (double)n * 16 * reps * iters / (ms / 1e3) / 1e9;
+  return NE_OK;
+}
+
+ne_status ne_measure_random_read(ne_context* ctx, size_t bytes, int iters, double* reads_per_s) {
+  if (!ctx || !reads_per_s || bytes < 32 || bytes / 32 > 0xffffffffull || iters <= 0) return NE_ERR_INVALID_ARG;
+  NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  const uint32_t nrec = (uint32_t)(bytes / 32);
+  DevBuf<float4> buf;
+  DevBuf<uint32_t> sink;
+  NE_CUDA(cudaMalloc(&buf.p, (size_t)nrec * 32), "cudaMalloc(read probe)");
+  NE_CUDA(cudaMalloc(&sink.p, 4), "cudaMalloc(read probe)");
+  NE_CUDA(cudaMemsetAsync(buf.p, 0, (size_t)nrec * 32, ctx->stream), "cudaMemsetAsync(read probe)");
+  int per_sm = 0;
+  NE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_random_read, 512, 0), "occupancy");
+  const int blocks = ctx->sm_count * std::max(1, per_sm);
+  const uint32_t reads = 256;  // per thread and launch
+  k_random_read<<<blocks, 512, 0, ctx->stream>>>(buf.p, nrec, reads, 0x1234567u, sink.p);  // warm-up
+  NE_CUDA(cudaGetLastError(), "k_random_read launch");
+  NE_CUDA(cudaEventRecord(ctx->ev[0], ctx->stream), "cudaEventRecord");
+  for (int k = 0; k < iters; k++)
+    k_random_read<<<blocks, 512, 0, ctx->stream>>>(buf.p, nrec, reads, 0x9e3779b9u * (uint32_t)(k + 1), sink.p);
+  NE_CUDA(cudaGetLastError(), "k_random_read launch");
+  NE_CUDA(cudaEventRecord(ctx->ev[1], ctx->stream), "cudaEventRecord");
+  NE_CUDA(cudaEventSynchronize(ctx->ev[1]), "cudaEventSynchronize");
+  float ms = 0;
+  NE_CUDA(cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]), "cudaEventElapsedTime");
+  *reads_per_s = (double)blocks * 512 * reads * iters / (ms / 1e3);
   return NE_OK;
 }
 
