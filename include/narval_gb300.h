@@ -377,6 +377,11 @@ ne_status ne_debug_wait_timeout(ne_context* ctx, uint32_t max_polls);
  * B[n][k]; FP32 D[128][n]) through the same shared-memory and tensor-memory conventions as
  * the radiance-cache kernels. n in 16..256 step 16, k in 16..128 step 16. */
 ne_status ne_debug_mma(ne_context* ctx, const uint16_t* a, const uint16_t* b, int n, int k, float* d);
+/* The same product with operands staged in the MN-major layout the radiance-cache backward
+ * pass reads transposed operands through: layout bit 0 = A, bit 1 = B; n, k in 16..64,
+ * multiples of 16. */
+ne_status ne_debug_mma_layout(ne_context* ctx, const uint16_t* a, const uint16_t* b, int n, int k, uint32_t layout,
+                              float* d);
 
 #ifdef __cplusplus
 }

@@ -202,5 +202,7 @@ SIGNATURES = {
     "ne_image_load_rgba8": (C.c_int32, [C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_void_p,
                                         C.c_size_t]),
     "ne_debug_mma": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
+    "ne_debug_mma_layout": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_uint32,
+                                        C.c_void_p]),
     "ne_debug_wait_timeout": (C.c_int32, [C.c_void_p, C.c_uint32]),
 }

@@ -119,7 +119,7 @@ struct ne_cache {
   float* loss_part = nullptr;
   float* d_loss = nullptr;
   float* grad = nullptr;
-  uint16_t* acts = nullptr;  // training activations
+  uint8_t* acts = nullptr;  // training activations
   float* out = nullptr;      // training outputs
   size_t cap = 0;
   int step = 0;
@@ -2158,6 +2158,29 @@ ne_status ne_debug_mma(ne_context* ctx, const uint16_t* a, const uint16_t* b, in
   return NE_OK;
 }
 
+ne_status ne_debug_mma_layout(ne_context* ctx, const uint16_t* a, const uint16_t* b, int n, int k, uint32_t layout,
+                              float* d) {
+  if (!ctx || !a || !b || !d) return NE_ERR_INVALID_ARG;
+  if (n < 16 || n > 64 || n % 16 || k < 16 || k > 64 || k % 16 || layout > 3)
+    return fail(ctx, NE_ERR_INVALID_ARG, "ne_debug_mma_layout: n and k must be 16..64, multiples of 16");
+  NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  DevBuf<uint16_t> da, db;
+  DevBuf<float> dd;
+  NE_CUDA(cudaMalloc(&da.p, (size_t)128 * k * 2), "cudaMalloc");
+  NE_CUDA(cudaMalloc(&db.p, (size_t)n * k * 2), "cudaMalloc");
+  NE_CUDA(cudaMalloc(&dd.p, (size_t)128 * n * 4), "cudaMalloc");
+  NE_CUDA(cudaMemcpyAsync(da.p, a, (size_t)128 * k * 2, cudaMemcpyHostToDevice, ctx->stream), "cudaMemcpyAsync");
+  NE_CUDA(cudaMemcpyAsync(db.p, b, (size_t)n * k * 2, cudaMemcpyHostToDevice, ctx->stream), "cudaMemcpyAsync");
+  NE_CUDA(cudaMemsetAsync(ctx->d_err, 0, 4, ctx->stream), "cudaMemsetAsync");
+  NE_CUDA(ne_launch_debug_mma_mn(ctx->stream, da.p, db.p, n, k, layout, dd.p, ctx->d_err), "k_debug_mma_mn launch");
+  NE_CUDA(cudaMemcpyAsync(d, dd.p, (size_t)128 * n * 4, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync");
+  uint32_t e = 0;
+  NE_CUDA(cudaMemcpyAsync(&e, ctx->d_err, 4, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync");
+  NE_CUDA(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  if (e) return fail(ctx, NE_ERR_TIMEOUT, "tensor-core product did not complete");
+  return NE_OK;
+}
+
 ne_status ne_debug_wait_timeout(ne_context* ctx, uint32_t max_polls) {
   if (!ctx || max_polls == 0 || max_polls > (1u << 20)) return NE_ERR_INVALID_ARG;
   NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
@@ -2288,7 +2311,7 @@ static ne_status cacheTrainDevice(ne_cache* c, const float* dp, const float* dd,
     c->acts = nullptr;
     c->out = nullptr;
     c->cap = 0;
-    NE_CUDA(cudaMalloc(&c->acts, n * kNeMlpActRow * 2), "cudaMalloc(activations)");
+    NE_CUDA(cudaMalloc(&c->acts, (n + 127) / 128 * (size_t)kNeMlpActTileBytes), "cudaMalloc(activations)");
     NE_CUDA(cudaMalloc(&c->out, n * 3 * 4), "cudaMalloc(outputs)");
     c->cap = n;
   }
@@ -2309,9 +2332,8 @@ static ne_status cacheTrainDevice(ne_cache* c, const float* dp, const float* dd,
   NE_CUDA(ne_mlp_backward(ctx->stream, b, ctx->d_err), "k_mlp_backward launch");
   if (apply) c->step++;
   NE_CUDA(ne_mlp_adam(ctx->stream, c->P, c->m, c->v, c->part, blocks, c->loss_part, wantGrads ? c->grad : nullptr,
-                      c->d_loss, 1e-2f, apply ? c->step : 1, apply),
+                      c->d_loss, 1e-2f, apply ? c->step : 1, apply, apply ? c->wfwd : nullptr, c->wbwd, c->bias),
           "k_mlp_adam launch");
-  if (apply) NE_CUDA(ne_mlp_pack(ctx->stream, c->P, c->wfwd, c->wbwd, c->bias), "k_mlp_pack launch");
   return NE_OK;
 }
 

@@ -9,6 +9,11 @@
 cudaError_t ne_launch_debug_mma(cudaStream_t st, const uint16_t* a, const uint16_t* b, int n, int k, float* d,
                                 uint32_t* err);
 
+// The same product with operands in the MN-major layout: layout bit 0 = A, bit 1 = B.
+// n, k in 16..64 step 16.
+cudaError_t ne_launch_debug_mma_mn(cudaStream_t st, const uint16_t* a, const uint16_t* b, int n, int k,
+                                   uint32_t layout, float* d, uint32_t* err);
+
 // A block that allocates tensor memory and waits on an mbarrier nothing signals, bounded by
 // `max_polls` polls: err bit 1 once the wait has given up (tensor memory released).
 cudaError_t ne_launch_debug_wait(cudaStream_t st, uint32_t max_polls, uint32_t* err);
@@ -18,7 +23,9 @@ constexpr int kNeMlpParams = 19728;
 constexpr int kNeMlpFwdBytes = 38912;   // packed BF16 forward weight tiles
 constexpr int kNeMlpBwdBytes = 26624;   // packed BF16 transposed weight tiles (layers 1..4)
 constexpr int kNeMlpBiasFloats = 272;
-constexpr int kNeMlpActRow = 352;       // BF16 layer inputs kept per training sample
+// Training activations: per tile of 128 samples the five layer inputs in the tensor core's
+// tile layout (features plus a ones chunk: 104 columns for layer 0, 72 for the others).
+constexpr int kNeMlpActTileBytes = 128 * 2 * (104 + 4 * 72);
 
 struct NeMlpForward {
   const float* pos;          // n x 3 query positions (medium object space)
@@ -29,14 +36,14 @@ struct NeMlpForward {
   const uint8_t* wfwd;
   const float* bias;
   float* out;                // n x 3 raw outputs, or null
-  uint16_t* acts;            // training: n x kNeMlpActRow, or null
+  uint8_t* acts;             // training: ceil(n / 128) x kNeMlpActTileBytes, or null
   const float* thr;          // with idx and radiance: radiance[idx[i]] += thr[i] * max(out[i], 0)
   const uint32_t* idx;
   float* radiance;
 };
 
 struct NeMlpBackward {
-  const uint16_t* acts;
+  const uint8_t* acts;       // the forward pass's training activations
   const float* out;
   const float* target;
   uint32_t n;
@@ -51,6 +58,8 @@ cudaError_t ne_mlp_pack(cudaStream_t st, const float* params, uint8_t* wfwd, uin
 cudaError_t ne_mlp_forward(cudaStream_t st, const NeMlpForward& f, uint32_t* err);
 int ne_mlp_backward_blocks(uint32_t n);
 cudaError_t ne_mlp_backward(cudaStream_t st, const NeMlpBackward& b, uint32_t* err);
-// Sums the partial gradients; when apply != 0 takes Adam step `step` (1-based).
+// Sums the partial gradients; when apply != 0 takes Adam step `step` (1-based) and, when
+// wfwd is not null, writes the updated parameters' packed copies (as ne_mlp_pack).
 cudaError_t ne_mlp_adam(cudaStream_t st, float* params, float* m, float* v, const float* part, int parts,
-                        const float* loss_part, float* grad_out, float* loss_out, float lr, int step, int apply);
+                        const float* loss_part, float* grad_out, float* loss_out, float lr, int step, int apply,
+                        uint8_t* wfwd, uint8_t* wbwd, float* bias);

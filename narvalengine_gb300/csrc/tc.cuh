@@ -38,10 +38,29 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
   return d;
 }
 
+// Byte offset of element (r, k) in an MN-major core-matrix tile with `rows` rows (r along M
+// or N, k along K): core matrices of 8 K-rows x 8 MN-elements (16 bytes per K-row, 128
+// contiguous bytes), the next 8 MN-elements 128 B on, the next 8 K-rows (rows / 8) * 128 B on.
+// A row-per-sample tile stored K-major (samples along M, features along K) is, read with the
+// roles swapped, the MN-major tile of its transpose (features along M, samples along K).
+__device__ __forceinline__ uint32_t mn_offset(uint32_t r, uint32_t k, uint32_t rows) {
+  return ((k >> 3) * (rows >> 3) + (r >> 3)) * 128u + (k & 7u) * 16u + (r & 7u) * 2u;
+}
+
 // Descriptor of the k-th K=16 slice of a K-major core-matrix tile with `kcols` columns.
 __device__ __forceinline__ uint64_t tile_desc(uint32_t tile_saddr, uint32_t kcols, uint32_t kstep) {
   return smem_desc(tile_saddr + kstep * 256u, 128u, (kcols >> 3) * 128u);
 }
+
+// Descriptor of the k-th K=16 slice of an MN-major tile with `rows` MN-rows (mn_offset): the
+// leading-dimension offset is the step to the next 8 K-rows, (rows / 8) * 128 B, the
+// stride-dimension offset the step to the next 8 MN-elements, 128 B (the instruction
+// descriptor marks the operand MN-major: bit 15 for A, bit 16 for B).
+__device__ __forceinline__ uint64_t mn_desc(uint32_t tile_saddr, uint32_t rows, uint32_t kstep) {
+  return smem_desc(tile_saddr + kstep * 2u * rows * 16u, rows * 16u, 128u);
+}
+constexpr uint32_t kIdescAMn = 1u << 15;
+constexpr uint32_t kIdescBMn = 1u << 16;
 
 // Instruction descriptor of kind::f16: BF16 A and B (both K-major), FP32 D, M x N.
 __host__ __device__ constexpr uint32_t idesc_bf16(uint32_t M, uint32_t N) {
@@ -104,6 +123,33 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64
       "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
       : "memory");
 }
+// One arrival of this thread on `bar` (release at CTA scope).
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// ---- bulk copies (the asynchronous copy engine; addresses 16-byte aligned, sizes multiples of
+// 16 bytes)
+// Global -> shared: `bytes` from src into dst; completes as `bytes` of transaction count on
+// `bar`, whose current phase this thread's arrive.expect_tx opens for them.
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+// Shared -> global, in this thread's bulk group.
+__device__ __forceinline__ void bulk_store(void* dst, const void* src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_u32(src)), "r"(bytes)
+               : "memory");
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+// This thread's bulk stores have read their shared-memory sources.
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// This thread's bulk stores are complete.
+__device__ __forceinline__ void bulk_wait() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
 // Arrives on `bar` once every MMA this thread issued before has completed.
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))

@@ -130,7 +130,9 @@ def loss_and_grad_out(out: np.ndarray, target: np.ndarray, den_from=None):
 
 def backward(params: dict, xs, zs, g_out: np.ndarray, quant: bool = True):
     """Gradients of every weight and bias. The error signal is rounded to BF16 before each
-    product (as the tensor-core kernels do); weight gradients accumulate in FP32."""
+    product (as the tensor-core kernels do); weight gradients accumulate in FP32. Bias
+    gradients are sums of the same BF16 error signal (the kernel takes them as one more row of
+    the weight-gradient product, against an input of ones)."""
     n_layers = len(params["W"])
     gW = [None] * n_layers
     gb = [None] * n_layers
@@ -139,7 +141,7 @@ def backward(params: dict, xs, zs, g_out: np.ndarray, quant: bool = True):
     for i in range(n_layers - 1, -1, -1):
         gq = _q(g, quant)
         gW[i] = (gq.T @ xs[i]).astype(dt)
-        gb[i] = g.sum(0).astype(dt)
+        gb[i] = gq.sum(0).astype(dt)
         if i > 0:
             gx = gq @ _q(params["W"][i], quant)
             g = (gx * (xs[i] > 0)).astype(dt)  # xs[i] = relu(z[i-1]) after rounding

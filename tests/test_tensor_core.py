@@ -77,3 +77,28 @@ def test_bounded_wait_gives_up_and_releases_tensor_memory(built):
             assert err.max() < 1e-5
     finally:
         ctx.close()
+
+
+@pytest.mark.parametrize("layout", [1, 2, 3])
+@pytest.mark.parametrize("n,k", [(16, 16), (64, 64), (32, 48), (64, 16)])
+def test_mma_mn_major_known_answer(built, layout, n, k):
+    """Operands staged MN-major (bit 0: A, bit 1: B) and read through transposed descriptors:
+    the layout the backward pass uses to read a row-per-sample tile as its transpose."""
+    import narvalengine_gb300 as ne
+    rng = np.random.default_rng(n * 100 + k + layout)
+    a = rng.normal(size=(128, k)).astype(np.float32)
+    b = rng.normal(size=(n, k)).astype(np.float32)
+    ab, bb = bf16_bits(a), bf16_bits(b)
+    af = (ab.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+    bf = (bb.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+    want = af @ bf.T
+    scale = np.abs(af) @ np.abs(bf).T
+    ctx = ne.Context(0)
+    try:
+        d = np.empty((128, n), np.float32)
+        st = ne.library().ne_debug_mma_layout(ctx._h, ab.ctypes.data, bb.ctypes.data, n, k, layout, d.ctypes.data)
+        assert st == 0, ctx.error()
+    finally:
+        ctx.close()
+    err = np.abs(d - want) / (scale + 1e-30)
+    assert err.max() < 1e-5, f"max scaled error {err.max():.3e}"
