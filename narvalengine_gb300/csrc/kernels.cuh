@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(kThreads, pathMinBlocks(K)) k_resume(const __g
     unsigned long long i = base + (unsigned long long)lane;
     uint32_t finishedView = 0xffffffffu;
     if (i < n) {
-      const PathState ps = loadState(&q.items[i < n0 ? i : q.cap + (i - n0)]);
+      const PathState ps = loadState(q, i < n0 ? i : q.cap + (i - n0));
       LiVars v = ps.v;
       c.S.reset(ps.key, ps.dim);
       c.idx = ps.idx;

@@ -1351,33 +1351,37 @@ struct alignas(16) PathState {
   unsigned long long idx;
 };
 static_assert(sizeof(PathState) == 160, "PathState is ten 16-byte words");
-NE_D void storeState(PathState* dst, const PathState& src) {
-  const uint4* s = reinterpret_cast<const uint4*>(&src);
-  uint4* d = reinterpret_cast<uint4*>(dst);
-#pragma unroll
-  for (int i = 0; i < 10; i++) d[i] = s[i];
-}
-NE_D PathState loadState(const PathState* src) {
-  PathState r;
-  const uint4* s = reinterpret_cast<const uint4*>(src);
-  uint4* d = reinterpret_cast<uint4*>(&r);
-#pragma unroll
-  for (int i = 0; i < 10; i++) d[i] = s[i];
-  return r;
-}
 
 // Deferred paths of one pass. With count_hi set, paths deferred right after a free-flight
 // sample are binned by the light their next draw will pick (uniformSampleOneLight's first draw,
-// peeked, not consumed): class 0 in items[0, cap), class 1 in items[cap, cap + cap_hi), so
-// that the warps of the next pass mostly run one light's sampling code. Every other deferral
-// is class 0. Without count_hi: one class.
+// peeked, not consumed): class 0 in entries [0, cap), class 1 in [cap, cap + cap_hi), so that
+// the warps of the next pass mostly run one light's sampling code. Every other deferral is
+// class 0. Without count_hi: one class. Storage is structure-of-arrays: word k (of ten 16-byte
+// words) of entry i at items[k * (cap + cap_hi) + i], so that a warp's lanes, which take
+// consecutive entries, move each word as one contiguous 512-byte access.
 struct DeferQueue {
-  PathState* items;
+  PathState* items;              // (cap + cap_hi) x 160 bytes
   uint32_t* count;
   uint32_t cap;                  // class 0 entries
   uint32_t* count_hi = nullptr;  // class 1 count (null: one class)
   uint32_t cap_hi = 0;           // class 1 entries
 };
+NE_D void storeState(const DeferQueue& q, size_t i, const PathState& src) {
+  const uint4* s = reinterpret_cast<const uint4*>(&src);
+  uint4* d = reinterpret_cast<uint4*>(q.items) + i;
+  const size_t plane = (size_t)q.cap + q.cap_hi;
+#pragma unroll
+  for (int k = 0; k < 10; k++) d[k * plane] = s[k];
+}
+NE_D PathState loadState(const DeferQueue& q, size_t i) {
+  PathState r;
+  const uint4* s = reinterpret_cast<const uint4*>(q.items) + i;
+  uint4* d = reinterpret_cast<uint4*>(&r);
+  const size_t plane = (size_t)q.cap + q.cap_hi;
+#pragma unroll
+  for (int k = 0; k < 10; k++) d[k] = s[k * plane];
+  return r;
+}
 
 // integrators/VolumetricPathIntegrator.cpp:176-301 Li, plus the optional Russian
 // roulette of resources/shaders/MS_monteCarlo.frag:539-544, written as a loop over `v` that
@@ -1434,7 +1438,7 @@ NE_D V3 liLoop(Ctx<K>& c, const PathParams& P, LiVars& v, bool resume) {
             ps.dim = c.S.dim;
             ps.mode = 0;
             ps.idx = c.idx;
-            storeState(&q.items[(cls ? (size_t)q.cap : 0) + slot], ps);
+            storeState(q, (cls ? (size_t)q.cap : 0) + slot, ps);
             c.deferred = true;
             return v.L;
           }
@@ -1551,7 +1555,7 @@ NE_D V3 liLoop(Ctx<K>& c, const PathParams& P, LiVars& v, bool resume) {
         ps.dim = c.S.dim;
         ps.mode = 1;
         ps.idx = c.idx;
-        storeState(&q.items[slot], ps);
+        storeState(q, slot, ps);
         c.deferred = true;
         return v.L;
       }
