@@ -16,6 +16,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <deque>
 #include <future>
@@ -28,6 +29,7 @@
 
 #include "narval_gb300.h"
 #include "bvh_build.h"
+#include "host_parallel.h"
 #include "kernels.cuh"
 #include "mlp.h"
 #include "views.cuh"
@@ -1280,9 +1282,14 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
       if (mat < 0 || mat >= (int)D.n_materials || D.materials[mat].light < 0)
         return fail(ctx, NE_ERR_INVALID_ARG, "emissive primitive without a light material");
     }
-    for (uint32_t k = 0; k < m.prim_count; k++)
-      if (m.use_bvh && D.prims[m.prim_begin + k].type != NE_PRIM_TRIANGLE)
-        return fail(ctx, NE_ERR_INVALID_ARG, "BVH models hold triangles only");
+    if (m.use_bvh) {
+      std::atomic<bool> other{false};
+      nehost::parallelFor(m.prim_count, 1u << 16, [&](size_t b, size_t e) {
+        for (size_t k = b; k < e; k++)
+          if (D.prims[m.prim_begin + k].type != NE_PRIM_TRIANGLE) other = true;
+      });
+      if (other) return fail(ctx, NE_ERR_INVALID_ARG, "BVH models hold triangles only");
+    }
   }
   for (uint32_t i = 0; i < D.n_light_instances; i++) {
     const ne_model& m = D.models[D.instances[D.n_instances + i].model];
@@ -1292,10 +1299,25 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
         return fail(ctx, NE_ERR_INVALID_ARG, "light instance material without a light");
     }
   }
-  for (uint32_t i = 0; i < D.n_prims; i++) {
-    int mat = D.prims[i].material;
-    if (mat >= (int)D.n_materials) return fail(ctx, NE_ERR_INVALID_ARG, "primitive material out of range");
-    if (D.prims[i].type < 0 || D.prims[i].type > NE_PRIM_POINT) return fail(ctx, NE_ERR_INVALID_ARG, "bad primitive type");
+  {
+    std::atomic<size_t> firstBad{SIZE_MAX};  // the first bad primitive in index order
+    nehost::parallelFor(D.n_prims, 1u << 16, [&](size_t b, size_t e) {
+      for (size_t i = b; i < e; i++) {
+        const int mat = D.prims[i].material, type = D.prims[i].type;
+        const int why = mat >= (int)D.n_materials ? 1 : ((type < 0 || type > NE_PRIM_POINT) ? 2 : 0);
+        if (!why) continue;
+        size_t cur = firstBad.load();
+        while (i < cur && !firstBad.compare_exchange_weak(cur, i)) {
+        }
+        break;
+      }
+    });
+    if (firstBad.load() != SIZE_MAX) {
+      const size_t i = firstBad.load();
+      if (D.prims[i].material >= (int)D.n_materials)
+        return fail(ctx, NE_ERR_INVALID_ARG, "primitive material out of range");
+      return fail(ctx, NE_ERR_INVALID_ARG, "bad primitive type");
+    }
   }
   for (uint32_t i = 0; i < D.n_materials; i++) {
     const ne_material& m = D.materials[i];
@@ -1368,7 +1390,9 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
   std::vector<float> mediumBoxes;
   const int32_t nMediumBoxes = mediumBoxesOf(D, mediumBoxes);
   // primitives
-  std::vector<DPrim> prims(D.n_prims);
+  // filled below (no zeroing pass first: every element is written)
+  std::unique_ptr<DPrim[]> primBuf(new DPrim[std::max<size_t>(1, D.n_prims)]);
+  DPrim* prims = primBuf.get();
   auto convertPrim = [&](uint32_t i) {
     const ne_primitive& s = D.prims[i];
     DPrim& d = prims[i];
@@ -1388,18 +1412,10 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
       if (m.medium >= 0 && D.media[m.medium].type == NE_MEDIUM_GRID) d.flags |= DPRIM_GRID_MEDIUM;
     }
   };
-  {
-    // large meshes: in parallel chunks (each primitive is converted on its own)
-    const uint32_t chunk = 1u << 16;
-    const uint32_t nchunks = (D.n_prims + chunk - 1) / chunk;
-    std::vector<std::future<void>> jobs;
-    for (uint32_t c = 1; c < nchunks; c++)
-      jobs.push_back(std::async(std::launch::async, [&, c] {
-        for (uint32_t i = c * chunk; i < std::min(D.n_prims, (c + 1) * chunk); i++) convertPrim(i);
-      }));
-    for (uint32_t i = 0; i < std::min(D.n_prims, chunk); i++) convertPrim(i);
-    for (auto& j : jobs) j.get();
-  }
+  // large meshes: in parallel ranges (each primitive is converted on its own)
+  nehost::parallelFor(D.n_prims, 1u << 15, [&](size_t b, size_t e) {
+    for (size_t i = b; i < e; i++) convertPrim((uint32_t)i);
+  });
   // models + BVHs
   std::vector<DModel> models(D.n_models);
   std::vector<DNode> nodes;
@@ -1528,7 +1544,7 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
     }
   }
   ne_status st = NE_OK;
-  if ((st = upload(sc, prims.data(), prims.size(), &sc->d.prims))) return cleanup(st);
+  if ((st = upload(sc, prims, D.n_prims, &sc->d.prims))) return cleanup(st);
   if (D.settings.bvh_build == 1) {
     // binned-SAH trees built on the GPU from the uploaded primitives
     for (uint32_t i = 0; i < D.n_models; i++) {

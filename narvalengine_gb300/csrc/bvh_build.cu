@@ -27,10 +27,12 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <string>
 #include <vector>
 
 #include "bvh_build.h"
+#include "host_parallel.h"
 
 namespace nedev {
 namespace {
@@ -690,9 +692,12 @@ cudaError_t buildSahBvh(cudaStream_t st, const DPrim* prims, uint32_t first, uin
   k_prim_bounds<<<blocks, 256, 0, st>>>(prims, first, n, lo.p, hi.p, cen.p, order.p);
   if ((e = cudaGetLastError())) return e;
   std::vector<BNode> nodes(1);
+  nodes.reserve(2 * (size_t)n / kLeafPrims + 64);  // a binary tree with at least ~kLeafPrims / 2 per leaf
   std::vector<Task> tasks = {Task{0, n, 0, 0}};  // wide flags set per level
   std::vector<int32_t> ids = {0};
   std::vector<TaskResult> res;
+  std::vector<Task> next;
+  std::vector<int32_t> nextIds;
   int level = 0;
   for (; level < kMaxLevels && !tasks.empty(); level++) {
     const uint32_t nt = (uint32_t)tasks.size();
@@ -752,41 +757,76 @@ cudaError_t buildSahBvh(cudaStream_t st, const DPrim* prims, uint32_t first, uin
     res.resize(nt);
     if ((e = cudaMemcpyAsync(res.data(), dRes.p, nt * sizeof(TaskResult), cudaMemcpyDeviceToHost, st))) return e;
     if ((e = cudaStreamSynchronize(st))) return e;
-    std::vector<Task> next;
-    std::vector<int32_t> nextIds;
-    for (uint32_t k = 0; k < nt; k++) {
-      const Task& t = tasks[k];
-      const TaskResult& r = res[k];
-      BNode& b = nodes[ids[k]];
-      for (int j = 0; j < 3; j++) { b.mn[j] = r.mn[j]; b.mx[j] = r.mx[j]; }
-      b.begin = t.begin;
-      b.count = t.end - t.begin;
-      b.left = b.right = -1;
-      if (r.leaf) continue;
-      if (r.nLeft == 0 || r.nLeft >= b.count) {
-        err = "BVH build: empty child";
-        return cudaErrorUnknown;
+    // the level's results in parallel: each task's node, its two children (leaves the bins
+    // already bound, or next-level tasks), at offsets from prefix sums over the tasks, so the
+    // node and task order is that of a sequential pass over the tasks
+    std::vector<uint32_t> kidTasks(nt + 1), kidNodes(nt + 1);
+    std::atomic<bool> empty{false};
+    auto childIsLeaf = [&](const Task& t, const TaskResult& r, int c) {
+      const uint32_t len = c == 0 ? r.nLeft : (t.end - t.begin) - r.nLeft;
+      return r.axis >= 0 && len <= kLeafPrims;
+    };
+    nehost::parallelFor(nt, 1u << 13, [&](size_t k0, size_t k1) {
+      for (size_t k = k0; k < k1; k++) {
+        const Task& t = tasks[k];
+        const TaskResult& r = res[k];
+        uint32_t nodesK = 0, tasksK = 0;
+        if (!r.leaf) {
+          if (r.nLeft == 0 || r.nLeft >= t.end - t.begin) empty = true;
+          nodesK = 2;
+          tasksK = (childIsLeaf(t, r, 0) ? 0u : 1u) + (childIsLeaf(t, r, 1) ? 0u : 1u);
+        }
+        kidNodes[k] = nodesK;
+        kidTasks[k] = tasksK;
       }
-      int32_t l = (int32_t)nodes.size();
-      b.left = l;
-      b.right = l + 1;
-      nodes.push_back(BNode{});  // invalidates b
-      nodes.push_back(BNode{});
-      const uint32_t cBegin[2] = {t.begin, t.begin + r.nLeft}, cEnd[2] = {t.begin + r.nLeft, t.end};
-      for (int c = 0; c < 2; c++) {
-        if (r.axis >= 0 && cEnd[c] - cBegin[c] <= kLeafPrims) {
-          // a small child of a binned split is a leaf whose bounds the bins already hold
-          BNode& leaf = nodes[l + c];
-          for (int j = 0; j < 3; j++) { leaf.mn[j] = r.cb[c][j]; leaf.mx[j] = r.cb[c][3 + j]; }
-          leaf.begin = cBegin[c];
-          leaf.count = cEnd[c] - cBegin[c];
-          leaf.left = leaf.right = -1;
-        } else {
-          next.push_back(Task{cBegin[c], cEnd[c], t.depth + 1, 0});
-          nextIds.push_back(l + c);
+    });
+    if (empty) {
+      err = "BVH build: empty child";
+      return cudaErrorUnknown;
+    }
+    uint32_t sumN = 0, sumT = 0;
+    for (uint32_t k = 0; k <= nt; k++) {  // exclusive scans; entry nt holds the totals
+      const uint32_t a0 = k < nt ? kidNodes[k] : 0u, a1 = k < nt ? kidTasks[k] : 0u;
+      kidNodes[k] = sumN;
+      kidTasks[k] = sumT;
+      sumN += a0;
+      sumT += a1;
+    }
+    const size_t node0 = nodes.size();
+    nodes.resize(node0 + sumN);
+    next.resize(sumT);
+    nextIds.resize(sumT);
+    nehost::parallelFor(nt, 1u << 13, [&](size_t k0, size_t k1) {
+      for (size_t k = k0; k < k1; k++) {
+        const Task& t = tasks[k];
+        const TaskResult& r = res[k];
+        BNode& b = nodes[ids[k]];
+        for (int j = 0; j < 3; j++) { b.mn[j] = r.mn[j]; b.mx[j] = r.mx[j]; }
+        b.begin = t.begin;
+        b.count = t.end - t.begin;
+        b.left = b.right = -1;
+        if (r.leaf) continue;
+        const int32_t l = (int32_t)(node0 + kidNodes[k]);
+        b.left = l;
+        b.right = l + 1;
+        uint32_t q = kidTasks[k];
+        const uint32_t cBegin[2] = {t.begin, t.begin + r.nLeft}, cEnd[2] = {t.begin + r.nLeft, t.end};
+        for (int c = 0; c < 2; c++) {
+          if (childIsLeaf(t, r, c)) {
+            // a small child of a binned split is a leaf whose bounds the bins already hold
+            BNode& leaf = nodes[l + c];
+            for (int j = 0; j < 3; j++) { leaf.mn[j] = r.cb[c][j]; leaf.mx[j] = r.cb[c][3 + j]; }
+            leaf.begin = cBegin[c];
+            leaf.count = cEnd[c] - cBegin[c];
+            leaf.left = leaf.right = -1;
+          } else {
+            next[q] = Task{cBegin[c], cEnd[c], t.depth + 1, 0};
+            nextIds[q] = l + c;
+            q++;
+          }
         }
       }
-    }
+    });
     tasks.swap(next);
     ids.swap(nextIds);
   }
@@ -815,7 +855,8 @@ cudaError_t buildSahBvh(cudaStream_t st, const DPrim* prims, uint32_t first, uin
       pos[nodes[i].right] = pos[i] + 1 + size[nodes[i].left];
     }
   nodesOut.resize(nn);
-  for (size_t i = 0; i < nn; i++) {
+  nehost::parallelFor(nn, 1u << 15, [&](size_t i0, size_t i1) {
+  for (size_t i = i0; i < i1; i++) {
     const BNode& b = nodes[i];
     DNode d;
     for (int j = 0; j < 3; j++) { d.lo[j] = b.mn[j]; d.hi[j] = b.mx[j]; }
@@ -831,8 +872,11 @@ cudaError_t buildSahBvh(cudaStream_t st, const DPrim* prims, uint32_t first, uin
     memcpy(&d.hi[3], &c, 4);
     nodesOut[pos[i]] = d;
   }
+  });
   slotsOut.resize(n);
-  for (uint32_t i = 0; i < n; i++) slotsOut[i] = first + ord[i];
+  nehost::parallelFor(n, 1u << 16, [&](size_t i0, size_t i1) {
+    for (size_t i = i0; i < i1; i++) slotsOut[i] = first + ord[i];
+  });
   return cudaSuccess;
 }
 
