@@ -415,7 +415,7 @@ def apply_tuning(args, scene, host):
     else the autotuner. Returns where the tuning came from."""
     if args.kernel >= 0:
         scene.set_tuning(kernel=args.kernel, track_share=args.track_share, split_passes=args.split_passes,
-                         split_half=args.split_half)
+                         split_half=args.split_half, pretrace=args.pretrace)
         return "given"
     prof = pinned_profile(args.scene)
     if prof is not None and not args.autotune:
@@ -442,6 +442,8 @@ def main():
     ap.add_argument("--autotune", action="store_true", help="run the library's autotuner instead of the pinned tuning")
     ap.add_argument("--split-passes", type=int, default=0, help="split kernel passes (0: library default)")
     ap.add_argument("--split-half", type=int, default=1, help="split kernel: 1 = deferral every half bounce")
+    ap.add_argument("--pretrace", type=int, default=0,
+                    help="split kernel by bounce, scenes without media: 1 = bounce rays traced ahead of each pass")
     ap.add_argument("--track-share", type=int, default=16, help="regrouped kernel tracking threshold, 32nds")
     ap.add_argument("--profile-spp", type=int, default=0,
                     help="profiling case: two renders of the workload at this spp (the second is the one to capture)")
@@ -551,8 +553,8 @@ def main():
         roofline["gather"] = {"achieved": got, "peak": rate, "unit": "lookups/s", "frac": got / rate,
                               "buffer_bytes": cell_bytes,
                               "peak_source": "measured here: ne_measure_random_read, random 32-byte reads "
-                                             "(hashed indices, 4 in flight per thread) from a buffer the size of "
-                                             "the scene's cell array, 10 launches"}
+                                             "(hashed indices; best of 2, 4, 8, 16 in flight per thread) from a "
+                                             "buffer the size of the scene's cell array, 10 launches each"}
     prof = pinned_profile(args.scene)
     if prof is not None:
         if prof["tuning"] == tuning:

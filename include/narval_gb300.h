@@ -203,6 +203,9 @@ typedef struct ne_tuning {
                             (1..8, 0 = 3: two thirds for the paths whose next light is the first
                             kind, one third for the other); paths beyond it continue in the pass
                             that has them */
+  int32_t pretrace;      /* kernel 3 by bounce (split_half 0), scenes without media: 1 = before
+                            each resume pass, k_trace intersects the queued paths' bounce rays and
+                            stores the hits, so the pass starts from them (same image) */
 } ne_tuning;
 
 ne_status ne_scene_set_tuning(ne_scene* scene, const ne_tuning* tuning);
@@ -234,9 +237,10 @@ ne_status ne_context_flush_l2(ne_context* ctx, size_t bytes);
  * well beyond it HBM bandwidth. */
 ne_status ne_measure_read_bandwidth(ne_context* ctx, size_t bytes, int iters, double* gbs);
 /* Rate of random 32-byte reads from a `bytes` buffer, the access a density-cell lookup makes
- * (two 16-byte loads of one 32-byte-aligned record at a hashed index, many reads in flight
- * per thread): *reads_per_s over `iters` launches. Sized like a scene's cell array, it is
- * the ceiling for that scene's lookups; bytes / 32 must fit in 32 bits. */
+ * (two 16-byte loads of one 32-byte-aligned record at a hashed index): *reads_per_s, the best
+ * over 2, 4, 8 and 16 independent reads in flight per thread, each timed over `iters` launches.
+ * Sized like a scene's cell array, it is the ceiling for that scene's lookups; bytes / 32 must
+ * fit in 32 bits. */
 ne_status ne_measure_random_read(ne_context* ctx, size_t bytes, int iters, double* reads_per_s);
 
 /* Device copies of the shared elementary functions, for bit-exactness checks.

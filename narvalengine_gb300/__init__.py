@@ -301,9 +301,9 @@ class Scene:
         return nodes, order
 
     def set_tuning(self, kernel: int = 0, track_share: int = 16, blocks_per_sm: int = 0, split_passes: int = 0,
-                   split_half: int = 1, queue_quarters: int = 3):
+                   split_half: int = 1, queue_quarters: int = 3, pretrace: int = 0):
         """Launch configuration of the path kernels (see ne_tuning in include/narval_gb300.h)."""
-        t = _abi.NeTuning(kernel, track_share, blocks_per_sm, split_passes, split_half, queue_quarters)
+        t = _abi.NeTuning(kernel, track_share, blocks_per_sm, split_passes, split_half, queue_quarters, pretrace)
         self.ctx.check(library().ne_scene_set_tuning(self._h, C.byref(t)))
 
     def autotune(self, repeats: int = 2, params: NeRenderParams | None = None, **kw):
@@ -318,7 +318,8 @@ class Scene:
         t = _abi.NeTuning()
         self.ctx.check(library().ne_scene_get_tuning(self._h, C.byref(t)))
         return {"kernel": t.kernel, "track_share": t.track_share, "blocks_per_sm": t.blocks_per_sm,
-                "split_passes": t.split_passes, "split_half": t.split_half, "queue_quarters": t.queue_quarters}
+                "split_passes": t.split_passes, "split_half": t.split_half, "queue_quarters": t.queue_quarters,
+                "pretrace": t.pretrace}
 
     def trace_paths(self, keys: np.ndarray, params: NeRenderParams | None = None, **kw) -> np.ndarray:
         """Camera path radiance for (pixel, sample) keys, shape (n, 3)."""

@@ -82,7 +82,8 @@ class NeRenderParams(C.Structure):
 
 class NeTuning(C.Structure):
     _fields_ = [("kernel", C.c_int32), ("track_share", C.c_int32), ("blocks_per_sm", C.c_int32),
-                ("split_passes", C.c_int32), ("split_half", C.c_int32), ("queue_quarters", C.c_int32)]
+                ("split_passes", C.c_int32), ("split_half", C.c_int32), ("queue_quarters", C.c_int32),
+                ("pretrace", C.c_int32)]
 
 
 class NeRenderStats(C.Structure):

@@ -151,6 +151,7 @@ struct ne_scene {
   int split_passes = 16;      // kernel 3: passes (the last runs deferred paths to the end)
   int split_half = 1;         // kernel 3: deferral points every half bounce
   int queue_quarters = 3;     // kernel 3: deferred-path capacity, quarters of the render's paths
+  int pretrace = 0;           // kernel 3 by bounce, surface sets: bounce rays traced by k_trace
   size_t dq_cap_uploaded = 0; // capacity the uploaded queue descriptors give
   PathState* d_defer[2] = {nullptr, nullptr};  // split renders: two queues of deferred paths
   size_t defer_cap = 0;
@@ -581,9 +582,9 @@ __global__ void __launch_bounds__(512) k_read_bw(const uint4* __restrict__ p, si
 }
 
 // Random 32-byte reads (two 16-byte loads through the read-only path, as a density-cell
-// lookup makes them) at hashed record indices: each thread issues its reads in groups of
-// four independent ones, so the rate measured is the memory system's, not one thread's
-// latency. Index hash: the "lowbias32" integer mix (Wellons), over a counter per read.
+// lookup makes them) at hashed record indices: each thread issues its reads in groups of D
+// independent ones, so the rate measured is the memory system's, not one thread's latency.
+// Index hash: the "lowbias32" integer mix (Wellons), over a counter per read.
 __device__ __forceinline__ uint32_t mix32(uint32_t x) {
   x ^= x >> 16;
   x *= 0x7feb352du;
@@ -592,23 +593,46 @@ __device__ __forceinline__ uint32_t mix32(uint32_t x) {
   x ^= x >> 16;
   return x;
 }
+template <int D>
 __global__ void __launch_bounds__(512) k_random_read(const float4* __restrict__ p, uint32_t nrec, uint32_t reads,
                                                      uint32_t seed, uint32_t* sink) {
   const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
   float acc = 0.0f;
-  for (uint32_t r = 0; r < reads; r += 4) {
-    float4 a[4], b[4];
+  for (uint32_t r = 0; r < reads; r += D) {
+    float4 a[D], b[D];
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
+    for (int k = 0; k < D; k++) {
       const uint32_t h = mix32((tid * reads + r + (uint32_t)k) ^ seed);
       const size_t i = (size_t)(((uint64_t)h * nrec) >> 32);
       a[k] = __ldg(p + 2 * i);
       b[k] = __ldg(p + 2 * i + 1);
     }
 #pragma unroll
-    for (int k = 0; k < 4; k++) acc += (a[k].x + a[k].w) * (b[k].y + b[k].z);
+    for (int k = 0; k < D; k++) acc += (a[k].x + a[k].w) * (b[k].y + b[k].z);
   }
   if (acc == 1234.5f) sink[0] = tid;
+}
+
+// Reads per second of `iters` launches of k_random_read<D> (one wave of resident blocks).
+template <int D>
+cudaError_t randomReadRate(ne_context* ctx, const float4* buf, uint32_t nrec, int iters, uint32_t* sink, double* rate) {
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_random_read<D>, 512, 0);
+  if (e != cudaSuccess) return e;
+  const int blocks = ctx->sm_count * std::max(1, per_sm);
+  const uint32_t reads = 256;  // per thread and launch
+  k_random_read<D><<<blocks, 512, 0, ctx->stream>>>(buf, nrec, reads, 0x1234567u, sink);  // warm-up
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if ((e = cudaEventRecord(ctx->ev[0], ctx->stream)) != cudaSuccess) return e;
+  for (int k = 0; k < iters; k++)
+    k_random_read<D><<<blocks, 512, 0, ctx->stream>>>(buf, nrec, reads, 0x9e3779b9u * (uint32_t)(k + 1), sink);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if ((e = cudaEventRecord(ctx->ev[1], ctx->stream)) != cudaSuccess) return e;
+  if ((e = cudaEventSynchronize(ctx->ev[1])) != cudaSuccess) return e;
+  float ms = 0;
+  if ((e = cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1])) != cudaSuccess) return e;
+  *rate = (double)blocks * 512 * reads * iters / (ms / 1e3);
+  return cudaSuccess;
 }
 
 __global__ void k_fmath(int fn, const float* __restrict__ x, size_t n, float* __restrict__ out) {
@@ -677,7 +701,10 @@ int persistentBlocks(ne_scene* sc) { return sc->ctx->sm_count * sc->blocks_per_s
 
 // Path-kernel launches of one launchPaths call.
 int pathLaunches(const ne_scene* sc, bool count) {
-  return (sc->variant == 3 && !count) ? std::max(2, sc->split_passes) : 1;
+  if (sc->variant != 3 || count) return 1;
+  const int passes = std::max(2, sc->split_passes);
+  const bool traces = sc->pretrace && !sc->split_half && (sc->feature_set == K_MESH || sc->feature_set == K_SURFACE);
+  return passes + (traces ? passes - 1 : 0);  // k_trace before every resume pass
 }
 
 // Split render: the first pass finishes every path that ends at its first event and queues
@@ -695,8 +722,13 @@ constexpr int kMaxSplitPasses = 64;
 // paths lets the rest continue in the pass that has them.
 constexpr size_t kMaxDeferEntries = size_t(1) << 26;
 
-template <class F>
-ne_status launchSplit(ne_scene* sc, PathArgs b, int blocks, F launch) {
+// With `trace` (a launcher of k_trace over a queue) and the scene tuned to pretrace, the
+// bounce rays of each queue between passes are intersected by k_trace before the next pass.
+struct NoTrace {
+  cudaError_t operator()(const DeferQueue*, unsigned long long*) const { return cudaSuccess; }
+};
+template <class F, class T = NoTrace>
+ne_status launchSplit(ne_scene* sc, PathArgs b, int blocks, F launch, T trace = NoTrace(), bool canTrace = false) {
   ne_context* ctx = sc->ctx;
   // queue_quarters / 4 of the paths (default 3: class 0 half the paths, class 1 a quarter)
   size_t cap = std::min(kMaxDeferEntries,
@@ -716,7 +748,8 @@ ne_status launchSplit(ne_scene* sc, PathArgs b, int blocks, F launch) {
     sc->defer_cap = cap;
   }
   const size_t countBytes = 2 * kMaxSplitPasses * sizeof(uint32_t);  // both classes
-  const size_t passBytes = countBytes + kMaxSplitPasses * sizeof(unsigned long long);
+  // then the passes' work counters and k_trace's
+  const size_t passBytes = countBytes + 2 * kMaxSplitPasses * sizeof(unsigned long long);
   if (!sc->d_dq) {
     void* qp = nullptr;
     NE_CUDA(ctx->pool.get(kMaxSplitPasses * sizeof(DeferQueue), &qp), "cudaMalloc");
@@ -744,12 +777,15 @@ ne_status launchSplit(ne_scene* sc, PathArgs b, int blocks, F launch) {
   }
   NE_CUDA(cudaMemsetAsync(sc->d_pass, 0, passBytes, ctx->stream), "cudaMemsetAsync");
   unsigned long long* counters = reinterpret_cast<unsigned long long*>(sc->d_pass + countBytes);
+  unsigned long long* traceCounters = counters + kMaxSplitPasses;
+  const bool traces = canTrace && sc->pretrace && !sc->split_half;
   const int passes = std::min(kMaxSplitPasses, std::max(2, sc->split_passes));
   b.defer_out = sc->d_dq;
   b.defer_at = 0;
   b.defer_half = sc->split_half;
   NE_CUDA(launch(0, blocks, b, ctx->d_counter), "path kernel launch");
   for (int pass = 1; pass < passes; pass++) {
+    if (traces) NE_CUDA(trace(sc->d_dq + pass - 1, traceCounters + pass), "k_trace launch");
     b.defer_in = sc->d_dq + pass - 1;
     b.defer_out = sc->d_dq + pass;
     b.defer_at = pass == passes - 1 ? -1 : pass;
@@ -767,9 +803,17 @@ ne_status launchPaths(ne_scene* sc, const PathArgs& a, bool count) {
   PathArgs b = a;
   b.track_share = sc->track_share;
   if (sc->variant == 3 && !count) {
-    return launchSplit(sc, b, blocks, [&](int pass, int nb, const PathArgs& pa, unsigned long long* ctr) {
-      return ne_launch_path_split(pass, sc->feature_set, nb, ctx->stream, sc->d, pa, ctr, ctx->d_err);
-    });
+    return launchSplit(
+        sc, b, blocks,
+        [&](int pass, int nb, const PathArgs& pa, unsigned long long* ctr) {
+          return ne_launch_path_split(pass, sc->feature_set, nb, ctx->stream, sc->d, pa, ctr, ctx->d_err);
+        },
+        [&](const DeferQueue* q, unsigned long long* ctr) {
+          return sc->feature_set == K_MESH
+                     ? nedev::launchTrace_mesh(ctx->sm_count, ctx->stream, sc->d, q, ctr, ctx->d_err)
+                     : nedev::launchTrace_surface(ctx->sm_count, ctx->stream, sc->d, q, ctr, ctx->d_err);
+        },
+        sc->feature_set == K_MESH || sc->feature_set == K_SURFACE);
   }
   NE_CUDA(ne_launch_path_kernel(sc->variant, sc->feature_set, count, blocks, ctx->stream, sc->d, b, ctx->d_counter,
                                 ctx->d_err),
@@ -1652,6 +1696,7 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
   tn.split_passes = 0;
   tn.split_half = 1;
   tn.queue_quarters = 3;
+  tn.pretrace = 0;
   if (ne_scene_set_tuning(sc, &tn) != NE_OK) return cleanup(NE_ERR_INVALID_ARG);
   cudaError_t e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return cleanup(cudaFail(ctx, e, "scene upload"));
@@ -1663,7 +1708,7 @@ ne_status ne_scene_set_tuning(ne_scene* sc, const ne_tuning* t) {
   if (!sc || !t || t->kernel < 0 || t->kernel > 3 || t->track_share < 1 || t->track_share > 32 ||
       t->blocks_per_sm < 0 || t->blocks_per_sm > 64 || t->split_passes < 0 || t->split_passes == 1 ||
       t->split_passes > 64 || t->split_half < 0 || t->split_half > 1 || t->queue_quarters < 0 ||
-      t->queue_quarters > 8)
+      t->queue_quarters > 8 || t->pretrace < 0 || t->pretrace > 1)
     return NE_ERR_INVALID_ARG;
   ne_context* ctx = sc->ctx;
   int fit = 1;
@@ -1676,6 +1721,7 @@ ne_status ne_scene_set_tuning(ne_scene* sc, const ne_tuning* t) {
   sc->track_share = t->track_share;
   sc->blocks_per_sm = t->blocks_per_sm > 0 ? std::min(t->blocks_per_sm, fit) : fit;
   sc->queue_quarters = t->queue_quarters ? t->queue_quarters : 3;
+  sc->pretrace = t->pretrace;
   return NE_OK;
 }
 
@@ -1687,6 +1733,7 @@ ne_status ne_scene_get_tuning(const ne_scene* sc, ne_tuning* t) {
   t->split_passes = sc->split_passes;
   t->split_half = sc->split_half;
   t->queue_quarters = sc->queue_quarters;
+  t->pretrace = sc->pretrace;
   return NE_OK;
 }
 
@@ -2009,21 +2056,13 @@ ne_status ne_measure_random_read(ne_context* ctx, size_t bytes, int iters, doubl
   NE_CUDA(cudaMalloc(&buf.p, (size_t)nrec * 32), "cudaMalloc(read probe)");
   NE_CUDA(cudaMalloc(&sink.p, 4), "cudaMalloc(read probe)");
   NE_CUDA(cudaMemsetAsync(buf.p, 0, (size_t)nrec * 32, ctx->stream), "cudaMemsetAsync(read probe)");
-  int per_sm = 0;
-  NE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_random_read, 512, 0), "occupancy");
-  const int blocks = ctx->sm_count * std::max(1, per_sm);
-  const uint32_t reads = 256;  // per thread and launch
-  k_random_read<<<blocks, 512, 0, ctx->stream>>>(buf.p, nrec, reads, 0x1234567u, sink.p);  // warm-up
-  NE_CUDA(cudaGetLastError(), "k_random_read launch");
-  NE_CUDA(cudaEventRecord(ctx->ev[0], ctx->stream), "cudaEventRecord");
-  for (int k = 0; k < iters; k++)
-    k_random_read<<<blocks, 512, 0, ctx->stream>>>(buf.p, nrec, reads, 0x9e3779b9u * (uint32_t)(k + 1), sink.p);
-  NE_CUDA(cudaGetLastError(), "k_random_read launch");
-  NE_CUDA(cudaEventRecord(ctx->ev[1], ctx->stream), "cudaEventRecord");
-  NE_CUDA(cudaEventSynchronize(ctx->ev[1]), "cudaEventSynchronize");
-  float ms = 0;
-  NE_CUDA(cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]), "cudaEventElapsedTime");
-  *reads_per_s = (double)blocks * 512 * reads * iters / (ms / 1e3);
+  // the best of 2, 4, 8 and 16 independent reads in flight per thread
+  double r[4] = {0, 0, 0, 0};
+  NE_CUDA(randomReadRate<2>(ctx, buf.p, nrec, iters, sink.p, &r[0]), "k_random_read");
+  NE_CUDA(randomReadRate<4>(ctx, buf.p, nrec, iters, sink.p, &r[1]), "k_random_read");
+  NE_CUDA(randomReadRate<8>(ctx, buf.p, nrec, iters, sink.p, &r[2]), "k_random_read");
+  NE_CUDA(randomReadRate<16>(ctx, buf.p, nrec, iters, sink.p, &r[3]), "k_random_read");
+  *reads_per_s = std::max(std::max(r[0], r[1]), std::max(r[2], r[3]));
   return NE_OK;
 }
 
@@ -2813,6 +2852,13 @@ ne_status ne_scene_autotune(ne_scene* sc, const ne_render_params* p, int repeats
       ne_status st = tryTuning(t);
       if (st) return st;
     }
+  }
+  // and, for surface scenes split by bounce, the bounce rays traced ahead of each pass
+  if (bt.kernel == 3 && !bt.split_half && (sc->feature_set == K_MESH || sc->feature_set == K_SURFACE)) {
+    ne_tuning t = bt;
+    t.pretrace = 1;
+    ne_status st = tryTuning(t);
+    if (st) return st;
   }
   ne_status st = ne_scene_set_tuning(sc, &bt);
   if (st) return st;

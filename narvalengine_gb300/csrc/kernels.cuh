@@ -208,7 +208,7 @@ __global__ void __launch_bounds__(kThreads, pathMinBlocks(K)) k_resume(const __g
         c.pidx = (uint32_t)ps.idx;
         c.train = isTrainingPath(ps.idx, a.cache->train_stride);
       }
-      V3 L = liLoop(c, a.P, v, ps.mode == 0);
+      V3 L = liLoop(c, a.P, v, ps.mode == 0, ps.mode == kModeHit ? 1 : (ps.mode == kModeMiss ? 2 : 0));
       if (!c.deferred) {
         a.out[3 * ps.idx + 0] = L.x;
         a.out[3 * ps.idx + 1] = L.y;
@@ -220,6 +220,58 @@ __global__ void __launch_bounds__(kThreads, pathMinBlocks(K)) k_resume(const __g
       __syncwarp();
       countViewDone(*a.views, finishedView);
     }
+  }
+}
+
+// The bounce rays of a queue of paths deferred at the top of a bounce (mode 1), intersected
+// ahead of the pass that resumes them: Scene::intersectScene per ray, the hit stored into the
+// path's state (mode 3, or 4 for no hit) so that the resume skips the call. The warps run
+// nothing but the traversal. Each path's words 1, 2 (the ray), 4-6 (the previous hit, which a
+// miss leaves in place but for its primitive) and 9 (the mode) are read, words 4-6 and 9
+// written back.
+template <uint32_t K>
+__global__ void __launch_bounds__(kThreads, 8) k_trace(const __grid_constant__ DScene s, const DeferQueue* qp,
+                                                  unsigned long long* __restrict__ counter, uint32_t* err) {
+  Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, nullptr, nullptr, 0ull, false, -1, 0};
+  const DeferQueue q = *qp;
+  const unsigned long long n0 = min(*q.count, q.cap);
+  const unsigned long long n = n0 + (q.count_hi ? min(*q.count_hi, q.cap_hi) : 0u);
+  const size_t plane = (size_t)q.cap + q.cap_hi;
+  uint4* words = reinterpret_cast<uint4*>(q.items);
+  const float inf = __int_as_float(0x7f800000);
+  for (;;) {
+    const int lane = threadIdx.x & 31;
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(&counter[0], 32ull);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= n) break;
+    const unsigned long long i = base + (unsigned long long)lane;
+    if (i >= n) continue;
+    const size_t e = i < n0 ? i : q.cap + (i - n0);
+    uint4 w9 = words[9 * plane + e];
+    if (w9.x != kModeTop) continue;
+    const uint4 w1 = words[1 * plane + e], w2 = words[2 * plane + e];
+    uint4 w4 = words[4 * plane + e];
+    const uint4 w5 = words[5 * plane + e], w6 = words[6 * plane + e];
+    Ray ray{v3(__uint_as_float(w1.z), __uint_as_float(w1.w), __uint_as_float(w2.x)),
+            v3(__uint_as_float(w2.y), __uint_as_float(w2.z), __uint_as_float(w2.w))};
+    Hit h;
+    h.hitPoint = v3(__uint_as_float(w4.z), __uint_as_float(w4.w), __uint_as_float(w5.x));
+    h.normal = v3(__uint_as_float(w5.y), __uint_as_float(w5.z), __uint_as_float(w5.w));
+    h.tNear = __uint_as_float(w6.x);
+    h.tFar = __uint_as_float(w6.y);
+    h.inst = (int)w6.z;
+    h.prim = (int)w6.w;
+    const bool did = intersectScene(c, ray, h, kEps12F, inf);
+    w4.z = __float_as_uint(h.hitPoint.x);
+    w4.w = __float_as_uint(h.hitPoint.y);
+    words[4 * plane + e] = w4;
+    words[5 * plane + e] = make_uint4(__float_as_uint(h.hitPoint.z), __float_as_uint(h.normal.x),
+                                      __float_as_uint(h.normal.y), __float_as_uint(h.normal.z));
+    words[6 * plane + e] = make_uint4(__float_as_uint(h.tNear), __float_as_uint(h.tFar), (uint32_t)h.inst,
+                                      (uint32_t)h.prim);
+    w9.x = did ? kModeHit : kModeMiss;
+    words[9 * plane + e] = w9;
   }
 }
 
@@ -316,6 +368,14 @@ cudaError_t ne_path_kernel_occupancy(int kernel, uint32_t set, int* blocks_per_s
 cudaError_t ne_launch_path_split(int pass, uint32_t set, int blocks, cudaStream_t st, const nedev::DScene& s,
                                  const nedev::PathArgs& a, unsigned long long* counter, uint32_t* err);
 cudaError_t ne_path_split_occupancy(uint32_t set, int* blocks_per_sm);
+namespace nedev {
+// Bounce rays of the paths a surface split pass queued at the top of a bounce (k_trace), one
+// wave of resident blocks on `sm_count` SMs; counter[0] must be zero before the launch.
+cudaError_t launchTrace_mesh(int sm_count, cudaStream_t st, const DScene& s, const DeferQueue* q,
+                             unsigned long long* counter, uint32_t* err);
+cudaError_t launchTrace_surface(int sm_count, cudaStream_t st, const DScene& s, const DeferQueue* q,
+                                unsigned long long* counter, uint32_t* err);
+}  // namespace nedev
 // Grid-medium scenes with paths ending in the radiance cache, split like kernel 3: pass 0 =
 // first pass, else a resume pass (see ne_launch_path_split).
 cudaError_t ne_launch_path_kernel_cache(int pass, int blocks, cudaStream_t st, const nedev::DScene& s,

@@ -1347,10 +1347,17 @@ struct alignas(16) PathState {
   LiVars v;
   nerng::PathKey key;
   uint32_t dim;
-  uint32_t mode;  // 0: resume inside a medium bounce after sampling, 1: at the top of bounce v.b
+  // 0: resume inside a medium bounce after sampling; 1: at the top of bounce v.b; 3 / 4: at the
+  // top of bounce v.b with v.isect already the closest hit of v.incoming (3) or no hit (4)
+  uint32_t mode;
   unsigned long long idx;
 };
 static_assert(sizeof(PathState) == 160, "PathState is ten 16-byte words");
+// The words k_trace reads (the ray and the mode) and writes (the hit and the mode).
+static_assert(offsetof(PathState, v) == 0 && offsetof(LiVars, incoming) == 24 && offsetof(LiVars, isect) == 72 &&
+                  sizeof(Hit) == 40 && offsetof(PathState, mode) == 144,
+              "PathState word layout");
+constexpr uint32_t kModeTop = 1, kModeHit = 3, kModeMiss = 4;
 
 // Deferred paths of one pass. With count_hi set, paths deferred right after a free-flight
 // sample are binned by the light their next draw will pick (uniformSampleOneLight's first draw,
@@ -1391,7 +1398,7 @@ NE_D PathState loadState(const DeferQueue& q, size_t i) {
 // the end of bounce b (surfaces at position b; every bounce at 2b + 1 with half-bounce
 // deferral). Every operation and every random draw happens in the same order either way.
 template <uint32_t K>
-NE_D V3 liLoop(Ctx<K>& c, const PathParams& P, LiVars& v, bool resume) {
+NE_D V3 liLoop(Ctx<K>& c, const PathParams& P, LiVars& v, bool resume, int pretraced = 0) {
   const DScene& s = c.s;
   const float inf = __int_as_float(0x7f800000);
   // K_CACHE training paths: the vertex the sample is recorded at
@@ -1408,7 +1415,13 @@ NE_D V3 liLoop(Ctx<K>& c, const PathParams& P, LiVars& v, bool resume) {
       mat = matOf(s, v.isect.prim);
       medium = true;
     } else {
-      did = intersectScene(c, v.incoming, v.isect, kEps12F, inf);
+      // pretraced: k_trace already intersected this bounce's ray (1: hit, 2: no hit)
+      if (pretraced) {
+        did = pretraced == 1;
+        pretraced = 0;
+      } else {
+        did = intersectScene(c, v.incoming, v.isect, kEps12F, inf);
+      }
       if (isBlack(v.T)) break;
       mat = did ? matOf(s, v.isect.prim) : nullptr;
       medium = (K & FT_VOLBSDF) && did && mat && mat->bsdf == NE_BSDF_VOLUME;

@@ -257,11 +257,41 @@ def test_mesh_bvh_parity(ne, ctx, oracle_lib, subdivisions):
     assert np.array_equal(g["t_near"].view(np.uint32), c["t_near"].view(np.uint32))
     assert (g["primitive"] >= 0).sum() > 1000
     keys = spread_keys(host, 512, 4, seed=3)
+    cp = orc.trace_paths(keys, ne.render_params(seed=8))
     for kernel in (0, 1, 2, 3):
         scene.set_tuning(kernel=kernel)
         gp = scene.trace_paths(keys, ne.render_params(seed=8))
-        cp = orc.trace_paths(keys, ne.render_params(seed=8))
         assert np.array_equal(gp, cp), f"kernel {kernel}: max rel {rel_err(gp, cp).max():.3e}"
+    # the bounce rays traced ahead of each pass by their own kernel (split by bounce)
+    for passes in (2, 3, 6):
+        scene.set_tuning(kernel=3, split_passes=passes, split_half=0, pretrace=1)
+        gp = scene.trace_paths(keys, ne.render_params(seed=8))
+        assert np.array_equal(gp, cp), f"pretrace, {passes} passes: max rel {rel_err(gp, cp).max():.3e}"
+
+
+def test_pretrace_surface_scene(ne, ctx):
+    """Cornell box split by bounce with the bounce rays traced ahead of each pass: the same
+    image as the one-pass kernel, one k_trace launch before every resume pass."""
+    host = ne.SceneHost.from_json(scene_path("cornell_c1"))
+    scene = ctx.upload(host)
+    try:
+        p = ne.render_params(seed=4, spp=4)
+        scene.set_tuning(kernel=0)
+        ref, _ = scene.render(p)
+        for passes in (2, 4, 8):
+            scene.set_tuning(kernel=3, split_passes=passes, split_half=0, pretrace=1)
+            assert scene.tuning()["pretrace"] == 1
+            img, st = scene.render(p)
+            assert np.array_equal(img.view(np.uint32), ref.view(np.uint32)), passes
+            assert st["kernel_launches"] == 2 * passes - 1 + 1, st["kernel_launches"]
+        # by half bounce the knob has no effect
+        scene.set_tuning(kernel=3, split_passes=8, split_half=1, pretrace=1)
+        img, st = scene.render(p)
+        assert np.array_equal(img.view(np.uint32), ref.view(np.uint32)) and st["kernel_launches"] == 9
+        with pytest.raises(ne.NarvalError):
+            scene.set_tuning(kernel=3, pretrace=2)
+    finally:
+        scene.close()
 
 
 def test_mesh_and_medium_parity(ne, ctx, oracle_lib):
