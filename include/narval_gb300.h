@@ -273,6 +273,8 @@ typedef struct ne_views_tuning {
                               groups of about equal paths, each run through all its passes
                               before the next starts, so the views of early groups complete
                               early (per-view latency) at some cost in throughput */
+  int32_t pretrace;        /* 1: before each pass after the first, k_trace intersects the bounce
+                              rays of the paths queued at the top of a bounce (as ne_tuning) */
 } ne_views_tuning;
 typedef struct ne_views_stats {
   double ms;               /* CUDA-event time of the batch */

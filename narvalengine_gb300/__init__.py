@@ -398,8 +398,8 @@ class Views:
         self._h = hnd
 
     def set_tuning(self, fetch: int = 32, blocks_per_sm: int = 0, order: int = 0, graph: bool = True,
-                   split_passes: int = 0, split_half: int = 0, groups: int = 1):
-        t = _abi.NeViewsTuning(fetch, blocks_per_sm, order, int(graph), split_passes, split_half, groups)
+                   split_passes: int = 0, split_half: int = 0, groups: int = 1, pretrace: int = 0):
+        t = _abi.NeViewsTuning(fetch, blocks_per_sm, order, int(graph), split_passes, split_half, groups, pretrace)
         self.ctx.check(library().ne_views_set_tuning(self._h, C.byref(t)))
 
     def tuning(self) -> dict:

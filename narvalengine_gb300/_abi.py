@@ -99,7 +99,8 @@ class NeView(C.Structure):
 
 class NeViewsTuning(C.Structure):
     _fields_ = [("fetch", C.c_uint32), ("blocks_per_sm", C.c_int32), ("order", C.c_int32), ("graph", C.c_int32),
-                ("split_passes", C.c_int32), ("split_half", C.c_int32), ("groups", C.c_int32)]
+                ("split_passes", C.c_int32), ("split_half", C.c_int32), ("groups", C.c_int32),
+                ("pretrace", C.c_int32)]
 
 
 class NeViewsStats(C.Structure):

@@ -1124,6 +1124,12 @@ ne_status viewsEnqueue(ne_views* vw) {
     pa.defer_at = pass == passes - 1 ? -1 : pass;
     pa.defer_half = vw->tune.split_half;
     pa.views = vw->d_vd;
+    if (vw->tune.pretrace) {
+      // the queued paths' bounce rays, intersected ahead of the pass (k_trace)
+      NE_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync");
+      NE_CUDA(nedev::launchTrace_general(ctx->sm_count, ctx->stream, vw->sc->d, vw->d_dq + in, counter, ctx->d_err),
+              "k_trace launch");
+    }
     NE_CUDA(cudaMemsetAsync(vw->d_dcount + out, 0, sizeof(uint32_t), ctx->stream), "cudaMemsetAsync");
     NE_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync");
     NE_CUDA(ne_launch_path_split(pass, K_GENERAL, vw->blocks, ctx->stream, vw->sc->d, pa, counter, ctx->d_err),
@@ -2676,7 +2682,8 @@ void ne_views_destroy(ne_views* vw) {
 ne_status ne_views_set_tuning(ne_views* vw, const ne_views_tuning* t) {
   if (!vw || !t || t->fetch < 32 || t->fetch > 4096 || t->fetch % 32 || t->blocks_per_sm < 0 ||
       t->blocks_per_sm > 64 || t->order < 0 || t->order > 2 || t->graph < 0 || t->graph > 1 || t->split_passes < 0 ||
-      t->split_passes > 64 || t->split_half < 0 || t->split_half > 1 || t->groups < 0 || t->groups > 16)
+      t->split_passes > 64 || t->split_half < 0 || t->split_half > 1 || t->groups < 0 || t->groups > 16 ||
+      t->pretrace < 0 || t->pretrace > 1)
     return NE_ERR_INVALID_ARG;
   ne_context* ctx = vw->sc->ctx;
   NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
@@ -2727,7 +2734,9 @@ ne_status ne_views_render(ne_views* vw, ne_views_stats* stats) {
     stats->latency_p50_ms = pct(0.5);
     stats->latency_p99_ms = pct(0.99);
     stats->latency_max_ms = lat[n - 1];
-    stats->kernel_launches = (uint32_t)((vw->group_first.size() - 1) * viewsPasses(vw) + 1);
+    const int passes = viewsPasses(vw);
+    stats->kernel_launches =
+        (uint32_t)((vw->group_first.size() - 1) * (passes + (vw->tune.pretrace && passes > 1 ? passes - 1 : 0)) + 1);
   }
   return NE_OK;
 }
@@ -2752,7 +2761,7 @@ ne_status ne_views_autotune(ne_views* vw, int repeats, ne_views_tuning* best, do
   for (uint32_t f : fetches)
     for (const auto& og : ogs)
       for (const auto& sp : passess) {
-        ne_views_tuning t = {f, fit, og[0], 1, sp[0], sp[1], og[1]};
+        ne_views_tuning t = {f, fit, og[0], 1, sp[0], sp[1], og[1], 0};
         ne_status st = ne_views_set_tuning(vw, &t);
         if (st) return st;
         ne_views_stats s;
@@ -2776,10 +2785,31 @@ ne_status ne_views_autotune(ne_views* vw, int repeats, ne_views_tuning* best, do
   const Trial* pick = nullptr;
   for (const Trial& tr : trials)
     if (tr.ms <= fastest * 1.03 && (!pick || tr.p50 < pick->p50)) pick = &tr;
-  ne_status st = ne_views_set_tuning(vw, &pick->t);
+  // then the pick with the bounce rays traced ahead of each pass
+  Trial chosen = *pick;
+  if (chosen.t.split_passes != 1) {
+    ne_views_tuning t = chosen.t;
+    t.pretrace = 1;
+    ne_status st = ne_views_set_tuning(vw, &t);
+    if (st) return st;
+    ne_views_stats s;
+    st = ne_views_render(vw, &s);
+    if (st) return st;
+    Trial tr = {t, 1e30, 0.0f};
+    for (int r = 0; r < repeats; r++) {
+      st = ne_views_render(vw, &s);
+      if (st) return st;
+      if (s.ms < tr.ms) {
+        tr.ms = s.ms;
+        tr.p50 = s.latency_p50_ms;
+      }
+    }
+    if (tr.ms < chosen.ms) chosen = tr;
+  }
+  ne_status st = ne_views_set_tuning(vw, &chosen.t);
   if (st) return st;
-  if (best) *best = pick->t;
-  if (best_ms) *best_ms = pick->ms;
+  if (best) *best = chosen.t;
+  if (best_ms) *best_ms = chosen.ms;
   return NE_OK;
 }
 

@@ -17,4 +17,16 @@ cudaError_t occupancySplit_general(int* blocks_per_sm) {
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_paths<K_GENERAL | K_SPLIT>, kThreads, 0);
 }
 
+cudaError_t launchTrace_general(int sm_count, cudaStream_t st, const DScene& s, const DeferQueue* q,
+                                unsigned long long* counter, uint32_t* err) {
+  static const int fit = [] {
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace<K_GENERAL | K_SPLIT>, kThreads, 0) != cudaSuccess)
+      b = 0;
+    return b;
+  }();
+  k_trace<K_GENERAL | K_SPLIT><<<sm_count * (fit > 0 ? fit : 1), kThreads, 0, st>>>(s, q, counter, err);
+  return cudaGetLastError();
+}
+
 }  // namespace nedev

@@ -375,6 +375,8 @@ cudaError_t launchTrace_mesh(int sm_count, cudaStream_t st, const DScene& s, con
                              unsigned long long* counter, uint32_t* err);
 cudaError_t launchTrace_surface(int sm_count, cudaStream_t st, const DScene& s, const DeferQueue* q,
                                 unsigned long long* counter, uint32_t* err);
+cudaError_t launchTrace_general(int sm_count, cudaStream_t st, const DScene& s, const DeferQueue* q,
+                                unsigned long long* counter, uint32_t* err);
 }  // namespace nedev
 // Grid-medium scenes with paths ending in the radiance cache, split like kernel 3: pass 0 =
 // first pass, else a resume pass (see ne_launch_path_split).
