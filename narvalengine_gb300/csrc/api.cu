@@ -92,6 +92,7 @@ struct DevicePool {
   }
 };
 
+constexpr int kGridSlabs = 8;
 struct ne_context {
   int device = 0;
   int sm_count = 0;
@@ -106,6 +107,10 @@ struct ne_context {
   std::vector<ne_scene*> scenes;            // live scenes, destroyed with the context
   std::vector<ne_cache*> caches;            // live radiance caches, destroyed with the context
   DevicePool pool;                          // scene and render buffers, reused
+  // grid uploads: slabs copied on copy_stream while the main stream builds the cells of the
+  // slabs already there (created at the first grid upload)
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t slab_ev[kGridSlabs + 1] = {};
 };
 
 struct ne_cache {
@@ -470,18 +475,24 @@ void buildBvh(const ne_primitive* prims, std::vector<uint32_t>& order, std::vect
 }
 
 // ---------------------------------------------------------------- kernels
-__global__ void k_cells(const float* __restrict__ grid, uint32_t W, uint32_t H, uint32_t D, float4* __restrict__ cells) {
-  size_t n = (size_t)(W + 1) * (H + 1) * (D + 1);
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    uint32_t x = (uint32_t)(i % (W + 1));
-    uint32_t y = (uint32_t)((i / (W + 1)) % (H + 1));
-    uint32_t z = (uint32_t)(i / ((size_t)(W + 1) * (H + 1)));
+// The cells of cell slabs [z0, z1): a block takes rows (y, z) of W + 1 cells, its threads
+// the cells of a row.
+__global__ void k_cells(const float* __restrict__ grid, uint32_t W, uint32_t H, uint32_t D, uint32_t z0, uint32_t z1,
+                        float4* __restrict__ cells) {
+  const uint32_t rows = (z1 - z0) * (H + 1);
+  for (uint32_t r = blockIdx.x; r < rows; r += gridDim.x) {
+    const uint32_t y = r % (H + 1), z = z0 + r / (H + 1);
+    const size_t row = ((size_t)z * (H + 1) + y) * (W + 1);
     auto den = [&](uint32_t a, uint32_t b, uint32_t c) -> float {
       if (a >= W || b >= H || c >= D) return 0.0f;
       return grid[(size_t)H * W * c + (size_t)W * b + a];
     };
-    cells[2 * i] = make_float4(den(x, y, z), den(x + 1, y, z), den(x, y + 1, z), den(x + 1, y + 1, z));
-    cells[2 * i + 1] = make_float4(den(x, y, z + 1), den(x + 1, y, z + 1), den(x, y + 1, z + 1), den(x + 1, y + 1, z + 1));
+    for (uint32_t x = threadIdx.x; x <= W; x += blockDim.x) {
+      const size_t i = row + x;
+      cells[2 * i] = make_float4(den(x, y, z), den(x + 1, y, z), den(x, y + 1, z), den(x + 1, y + 1, z));
+      cells[2 * i + 1] =
+          make_float4(den(x, y, z + 1), den(x + 1, y, z + 1), den(x, y + 1, z + 1), den(x + 1, y + 1, z + 1));
+    }
   }
 }
 
@@ -1226,6 +1237,9 @@ void ne_context_destroy(ne_context* ctx) {
     if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
   for (int i = 0; i < 8; i++)
     if (ctx->user_ev[i]) cudaEventDestroy(ctx->user_ev[i]);
+  for (cudaEvent_t e : ctx->slab_ev)
+    if (e) cudaEventDestroy(e);
+  if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
   if (ctx->flush_buf) cudaFree(ctx->flush_buf);
   if (ctx->d_counter) cudaFree(ctx->d_counter);
   if (ctx->d_err) cudaFree(ctx->d_err);
@@ -1577,19 +1591,49 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
       gridMedia.push_back(i);  // invMaxDensity from the device copy of the grid, below
       memcpy(d.res, s.res, 12);
       d.resf[0] = (float)s.res[0]; d.resf[1] = (float)s.res[1]; d.resf[2] = (float)s.res[2];
-      const float* dg = nullptr;
-      ne_status st = upload(sc, s.grid, n, &dg);
-      if (st) return cleanup(st);
+      void* gp = nullptr;
+      cudaError_t e = ctx->pool.get(n * sizeof(float), &gp);
+      if (e != cudaSuccess) return cleanup(cudaFail(ctx, e, "cudaMalloc(grid)"));
+      sc->allocs.push_back(gp);
+      const float* dg = (const float*)gp;
       d.grid = dg;
       size_t ncell = (size_t)(s.res[0] + 1) * (s.res[1] + 1) * (s.res[2] + 1);
       void* cp = nullptr;
-      cudaError_t e = ctx->pool.get(ncell * 2 * sizeof(float4), &cp);
+      e = ctx->pool.get(ncell * 2 * sizeof(float4), &cp);
       if (e != cudaSuccess) return cleanup(cudaFail(ctx, e, "cudaMalloc(cells)"));
       sc->allocs.push_back(cp);
-      int blocks = ctx->sm_count * 8;
-      k_cells<<<blocks, 256, 0, ctx->stream>>>(dg, s.res[0], s.res[1], s.res[2], (float4*)cp);
-      e = cudaGetLastError();
-      if (e != cudaSuccess) return cleanup(cudaFail(ctx, e, "k_cells launch"));
+      // the grid in slabs of z slices on the copy stream; the cells of each slab (which read
+      // its slices and the next one) built on the main stream once they are there
+      if (!ctx->copy_stream) {
+        NE_CUDA(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        for (cudaEvent_t& ev : ctx->slab_ev)
+          NE_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate");
+      }
+      const uint32_t W = s.res[0], H = s.res[1], Dz = s.res[2];
+      const size_t slice = (size_t)W * H;
+      const int slabs = (int)std::min<uint32_t>(kGridSlabs, Dz);
+      // the buffers may have been in use on the main stream until now
+      NE_CUDA(cudaEventRecord(ctx->slab_ev[kGridSlabs], ctx->stream), "cudaEventRecord");
+      NE_CUDA(cudaStreamWaitEvent(ctx->copy_stream, ctx->slab_ev[kGridSlabs], 0), "cudaStreamWaitEvent");
+      uint32_t cellsDone = 0;
+      for (int k = 0; k < slabs; k++) {
+        const uint32_t z0 = (uint32_t)((uint64_t)Dz * k / slabs), z1 = (uint32_t)((uint64_t)Dz * (k + 1) / slabs);
+        NE_CUDA(cudaMemcpyAsync((float*)gp + z0 * slice, s.grid + z0 * slice, (size_t)(z1 - z0) * slice * sizeof(float),
+                                cudaMemcpyHostToDevice, ctx->copy_stream),
+                "cudaMemcpyAsync(grid)");
+        NE_CUDA(cudaEventRecord(ctx->slab_ev[k], ctx->copy_stream), "cudaEventRecord");
+        NE_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->slab_ev[k], 0), "cudaStreamWaitEvent");
+        // cell slab z reads grid slices z and z + 1: with slices [0, z1) there, cells [.., z1 - 1)
+        const uint32_t cellsTo = k == slabs - 1 ? Dz + 1 : z1 - 1;
+        if (cellsTo > cellsDone) {
+          const uint32_t rows = (cellsTo - cellsDone) * (H + 1);
+          const int blocks = (int)std::min<uint32_t>(rows, (uint32_t)ctx->sm_count * 16);
+          k_cells<<<blocks, 256, 0, ctx->stream>>>(dg, W, H, Dz, cellsDone, cellsTo, (float4*)cp);
+          e = cudaGetLastError();
+          if (e != cudaSuccess) return cleanup(cudaFail(ctx, e, "k_cells launch"));
+          cellsDone = cellsTo;
+        }
+      }
       d.cells = (const float4*)cp;
     }
   }
