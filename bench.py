@@ -514,11 +514,14 @@ def main():
         s2.close()
     d.barrier()
     t0 = time.perf_counter()
+    e2e_steps = []
     for _ in range(args.steps):
+        ts = time.perf_counter()
         s2 = ctx.upload(host)
         s2.set_tuning(**scene.tuning())
         s2.render(pe, out=out_host)
         s2.close()
+        e2e_steps.append(round((time.perf_counter() - ts) * 1e3, 2))
     e2e_s = time.perf_counter() - t0
     d.barrier()
     e2e_s = d.max(e2e_s)
@@ -575,7 +578,7 @@ def main():
                            "parallelism": f"{world} GPU(s), sample ranges per rank",
                            "tuning": tuning, "tuning_source": tuning_source},
                 "e2e": {"value": e2e, "unit": "Mpaths/s", "h2d_bytes_per_step": h2d,
-                        "d2h_bytes_per_step": img_bytes},
+                        "d2h_bytes_per_step": img_bytes, "step_ms": e2e_steps},
                 "gpu_launches": launches,
                 "roofline": roofline, "cpu_baseline": cpu, "clocks": clk}
         print(json.dumps(line), flush=True)
