@@ -205,7 +205,9 @@ typedef struct ne_tuning {
                             that has them */
   int32_t pretrace;      /* kernel 3 by bounce (split_half 0), scenes without media: 1 = before
                             each resume pass, k_trace intersects the queued paths' bounce rays and
-                            stores the hits, so the pass starts from them (same image) */
+                            stores the hits, so the pass starts from them; 2 = the camera rays too
+                            (a first pass queues every new path before its first intersection;
+                            the queues then hold 1.5 x the render's paths). Same image */
 } ne_tuning;
 
 ne_status ne_scene_set_tuning(ne_scene* scene, const ne_tuning* tuning);

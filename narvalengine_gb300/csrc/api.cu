@@ -710,11 +710,13 @@ struct DevBuf {
 
 int persistentBlocks(ne_scene* sc) { return sc->ctx->sm_count * sc->blocks_per_sm; }
 
+constexpr int kMaxSplitPasses = 64;
+
 // Path-kernel launches of one launchPaths call.
 int pathLaunches(const ne_scene* sc, bool count) {
   if (sc->variant != 3 || count) return 1;
-  const int passes = std::max(2, sc->split_passes);
   const bool traces = sc->pretrace && !sc->split_half && (sc->feature_set == K_MESH || sc->feature_set == K_SURFACE);
+  const int passes = std::min(kMaxSplitPasses, std::max(2, sc->split_passes) + (traces && sc->pretrace == 2 ? 1 : 0));
   return passes + (traces ? passes - 1 : 0);  // k_trace before every resume pass
 }
 
@@ -728,7 +730,6 @@ int pathLaunches(const ne_scene* sc, bool count) {
 // has its own queue count and work counter, so the passes follow one another with no
 // launches in between. `launch(pass, blocks, args, counter)` launches one pass (0: first
 // pass; pass 0 uses the context's counter, cleared by the caller).
-constexpr int kMaxSplitPasses = 64;
 // Entries of each deferred-path buffer at most (2^26 paths, 10 GiB): a render with more
 // paths lets the rest continue in the pass that has them.
 constexpr size_t kMaxDeferEntries = size_t(1) << 26;
@@ -742,8 +743,12 @@ template <class F, class T = NoTrace>
 ne_status launchSplit(ne_scene* sc, PathArgs b, int blocks, F launch, T trace = NoTrace(), bool canTrace = false) {
   ne_context* ctx = sc->ctx;
   // queue_quarters / 4 of the paths (default 3: class 0 half the paths, class 1 a quarter)
+  const bool traces = canTrace && sc->pretrace && !sc->split_half;
+  // pretrace 2: the first pass queues every path before its camera ray (class 0 holds them all)
+  const bool gen = traces && sc->pretrace == 2;
   size_t cap = std::min(kMaxDeferEntries,
                         std::max<size_t>(3072, (size_t)(b.total / 4) * (size_t)sc->queue_quarters));
+  if (gen) cap = std::min(kMaxDeferEntries, std::max(cap, (size_t)b.total / 2 * 3 + 3));
   if (sc->defer_cap < cap) {
     for (PathState*& q : sc->d_defer) {
       ctx->pool.put(q);
@@ -789,17 +794,19 @@ ne_status launchSplit(ne_scene* sc, PathArgs b, int blocks, F launch, T trace = 
   NE_CUDA(cudaMemsetAsync(sc->d_pass, 0, passBytes, ctx->stream), "cudaMemsetAsync");
   unsigned long long* counters = reinterpret_cast<unsigned long long*>(sc->d_pass + countBytes);
   unsigned long long* traceCounters = counters + kMaxSplitPasses;
-  const bool traces = canTrace && sc->pretrace && !sc->split_half;
-  const int passes = std::min(kMaxSplitPasses, std::max(2, sc->split_passes));
+  // with `gen` a first pass that only queues the new paths precedes the split passes
+  const int passes = std::min(kMaxSplitPasses, std::max(2, sc->split_passes) + (gen ? 1 : 0));
   b.defer_out = sc->d_dq;
   b.defer_at = 0;
   b.defer_half = sc->split_half;
+  b.defer_top = gen ? 1 : 0;
   NE_CUDA(launch(0, blocks, b, ctx->d_counter), "path kernel launch");
+  b.defer_top = 0;
   for (int pass = 1; pass < passes; pass++) {
     if (traces) NE_CUDA(trace(sc->d_dq + pass - 1, traceCounters + pass), "k_trace launch");
     b.defer_in = sc->d_dq + pass - 1;
     b.defer_out = sc->d_dq + pass;
-    b.defer_at = pass == passes - 1 ? -1 : pass;
+    b.defer_at = pass == passes - 1 ? -1 : pass - (gen ? 1 : 0);
     NE_CUDA(launch(pass, persistentBlocks(sc), b, counters + pass), "resume kernel launch");
   }
   return NE_OK;
@@ -1758,7 +1765,7 @@ ne_status ne_scene_set_tuning(ne_scene* sc, const ne_tuning* t) {
   if (!sc || !t || t->kernel < 0 || t->kernel > 3 || t->track_share < 1 || t->track_share > 32 ||
       t->blocks_per_sm < 0 || t->blocks_per_sm > 64 || t->split_passes < 0 || t->split_passes == 1 ||
       t->split_passes > 64 || t->split_half < 0 || t->split_half > 1 || t->queue_quarters < 0 ||
-      t->queue_quarters > 8 || t->pretrace < 0 || t->pretrace > 1)
+      t->queue_quarters > 8 || t->pretrace < 0 || t->pretrace > 2)
     return NE_ERR_INVALID_ARG;
   ne_context* ctx = sc->ctx;
   int fit = 1;
@@ -2929,10 +2936,13 @@ ne_status ne_scene_autotune(ne_scene* sc, const ne_render_params* p, int repeats
   }
   // and, for surface scenes split by bounce, the bounce rays traced ahead of each pass
   if (bt.kernel == 3 && !bt.split_half && (sc->feature_set == K_MESH || sc->feature_set == K_SURFACE)) {
-    ne_tuning t = bt;
-    t.pretrace = 1;
-    ne_status st = tryTuning(t);
-    if (st) return st;
+    const ne_tuning base = bt;
+    for (int pre : {1, 2}) {  // the bounce rays; the camera rays too
+      ne_tuning t = base;
+      t.pretrace = pre;
+      ne_status st = tryTuning(t);
+      if (st) return st;
+    }
   }
   ne_status st = ne_scene_set_tuning(sc, &bt);
   if (st) return st;

@@ -106,6 +106,9 @@ struct PathArgs {
   const DeferQueue* defer_out = nullptr;
   int defer_at = -1;
   int defer_half = 0;  // 1: deferral points every half bounce
+  // first pass of a split render whose bounce rays are traced ahead (k_trace): every path
+  // stops at the top of bounce 0, before its camera ray is intersected
+  int defer_top = 0;
   const ViewDone* views = nullptr;  // resume passes of a batch of views: completion accounting
 };
 
@@ -139,6 +142,7 @@ __global__ void __launch_bounds__(kThreads, pathMinBlocks(K)) k_paths(const __gr
                                                     unsigned long long* __restrict__ counter, uint32_t* err) {
   Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, a.cache, a.defer_out, 0ull, false, a.defer_at,
            a.defer_half};
+  c.deferTop = a.defer_top != 0;
   const int lane = threadIdx.x & 31;
   for (;;) {
     unsigned long long base = 0;

@@ -216,6 +216,7 @@ struct Ctx {
   bool deferred;
   int deferAt;
   int deferHalf;  // 1: deferral points every half bounce (after sampling, and after the bounce)
+  bool deferTop = false;  // K_SPLIT first pass: defer every new path before its first intersection
 };
 
 // Buffers of a render that ends paths in the learned radiance cache. A path that reaches
@@ -1599,6 +1600,22 @@ NE_D V3 Li(Ctx<K>& c, const PathParams& P, Ray incoming) {
   v.isect = emptyHit();
   v.b = 0;
   v.passes = 0;
+  if ((K & K_SPLIT) && c.deferTop) {
+    // the camera ray goes to k_trace with the bounce rays: the path stops at the top of bounce 0
+    const DeferQueue& q = *c.dq;
+    const uint32_t slot = appendSlot(q.count);
+    if (slot < q.cap) {
+      PathState ps;
+      ps.v = v;
+      ps.key = c.S.key;
+      ps.dim = c.S.dim;
+      ps.mode = kModeTop;
+      ps.idx = c.idx;
+      storeState(q, slot, ps);
+      c.deferred = true;
+      return v.L;
+    }
+  }
   return liLoop(c, P, v, false);
 }
 
