@@ -276,7 +276,9 @@ typedef struct ne_views_tuning {
                               before the next starts, so the views of early groups complete
                               early (per-view latency) at some cost in throughput */
   int32_t pretrace;        /* 1: before each pass after the first, k_trace intersects the bounce
-                              rays of the paths queued at the top of a bounce (as ne_tuning) */
+                              rays of the paths queued at the top of a bounce; 2: the camera rays
+                              too (a first pass queues every path; the queues grow to the largest
+                              group's paths) (as ne_tuning) */
 } ne_views_tuning;
 typedef struct ne_views_stats {
   double ms;               /* CUDA-event time of the batch */

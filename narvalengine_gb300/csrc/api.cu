@@ -1105,8 +1105,10 @@ ne_status viewsEnqueue(ne_views* vw) {
   NE_CUDA(cudaMemsetAsync(done, 0, 2 * n * sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync");
   NE_CUDA(cudaMemsetAsync(tstart, 0xFF, sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync");
   NE_CUDA(cudaMemsetAsync(ctx->d_err, 0, 4, ctx->stream), "cudaMemsetAsync");
-  const int passes = viewsPasses(vw);
-  const bool split = passes > 1;
+  const bool split = viewsPasses(vw) > 1;
+  // pretrace 2: a first pass that only queues the paths precedes the split passes
+  const bool gen = split && vw->tune.pretrace == 2;
+  const int passes = viewsPasses(vw) + (gen ? 1 : 0);
   for (size_t g = 0; g + 1 < vw->group_first.size(); g++) {
   NE_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync");
   ViewArgs a;
@@ -1123,6 +1125,7 @@ ne_status viewsEnqueue(ne_views* vw) {
   a.t_start = tstart;
   a.defer_out = split ? vw->d_dq : nullptr;
   a.defer_half = vw->tune.split_half;
+  a.defer_top = gen ? 1 : 0;
   if (split) NE_CUDA(cudaMemsetAsync(vw->d_dcount, 0, sizeof(uint32_t), ctx->stream), "cudaMemsetAsync");
   NE_CUDA(ne_launch_views(split, vw->blocks, ctx->stream, vw->sc->d, a, counter, ctx->d_err), "k_views launch");
   for (int pass = 1; pass < passes; pass++) {
@@ -1139,7 +1142,7 @@ ne_status viewsEnqueue(ne_views* vw) {
     pa.track_share = 16;
     pa.defer_in = vw->d_dq + in;
     pa.defer_out = vw->d_dq + out;
-    pa.defer_at = pass == passes - 1 ? -1 : pass;
+    pa.defer_at = pass == passes - 1 ? -1 : pass - (gen ? 1 : 0);
     pa.defer_half = vw->tune.split_half;
     pa.views = vw->d_vd;
     if (vw->tune.pretrace) {
@@ -1176,6 +1179,24 @@ ne_status viewsPrepare(ne_views* vw) {
   ne_status st = viewsLayout(vw);
   if (st) return st;
   NE_CUDA(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  if (vw->tune.pretrace == 2) {
+    // the first pass queues every path of a group: the queues grow to the largest group
+    size_t need = 1024;
+    for (size_t g = 0; g + 1 < vw->group_first.size(); g++)
+      need = std::max<size_t>(need, (size_t)(vw->group_first[g + 1] - vw->group_first[g]) + 1024);
+    if (need > vw->defer_cap) {
+      if (need > 0xFFFFFFFFull) return fail(ctx, NE_ERR_INVALID_ARG, "views: a group above 2^32 paths");
+      for (PathState*& q : vw->d_defer) {
+        if (q) cudaFree(q);
+        q = nullptr;
+      }
+      vw->defer_cap = need;
+      for (PathState*& q : vw->d_defer) NE_CUDA(cudaMalloc(&q, need * sizeof(PathState)), "cudaMalloc(view queues)");
+      DeferQueue dq[2];
+      for (int i = 0; i < 2; i++) dq[i] = DeferQueue{vw->d_defer[i], vw->d_dcount + i, (uint32_t)need};
+      NE_CUDA(cudaMemcpy(vw->d_dq, dq, sizeof(dq), cudaMemcpyHostToDevice), "cudaMemcpy");
+    }
+  }
   if (vw->tune.graph) {
     cudaGraph_t g = nullptr;
     NE_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
@@ -2734,7 +2755,7 @@ ne_status ne_views_set_tuning(ne_views* vw, const ne_views_tuning* t) {
   if (!vw || !t || t->fetch < 32 || t->fetch > 4096 || t->fetch % 32 || t->blocks_per_sm < 0 ||
       t->blocks_per_sm > 64 || t->order < 0 || t->order > 2 || t->graph < 0 || t->graph > 1 || t->split_passes < 0 ||
       t->split_passes > 64 || t->split_half < 0 || t->split_half > 1 || t->groups < 0 || t->groups > 16 ||
-      t->pretrace < 0 || t->pretrace > 1)
+      t->pretrace < 0 || t->pretrace > 2)
     return NE_ERR_INVALID_ARG;
   ne_context* ctx = vw->sc->ctx;
   NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
@@ -2785,7 +2806,7 @@ ne_status ne_views_render(ne_views* vw, ne_views_stats* stats) {
     stats->latency_p50_ms = pct(0.5);
     stats->latency_p99_ms = pct(0.99);
     stats->latency_max_ms = lat[n - 1];
-    const int passes = viewsPasses(vw);
+    const int passes = viewsPasses(vw) + (vw->tune.pretrace == 2 && viewsPasses(vw) > 1 ? 1 : 0);
     stats->kernel_launches =
         (uint32_t)((vw->group_first.size() - 1) * (passes + (vw->tune.pretrace && passes > 1 ? passes - 1 : 0)) + 1);
   }
@@ -2836,11 +2857,12 @@ ne_status ne_views_autotune(ne_views* vw, int repeats, ne_views_tuning* best, do
   const Trial* pick = nullptr;
   for (const Trial& tr : trials)
     if (tr.ms <= fastest * 1.03 && (!pick || tr.p50 < pick->p50)) pick = &tr;
-  // then the pick with the bounce rays traced ahead of each pass
+  // then the pick with the bounce rays (1) and the camera rays too (2) traced ahead of each pass
   Trial chosen = *pick;
-  if (chosen.t.split_passes != 1) {
-    ne_views_tuning t = chosen.t;
-    t.pretrace = 1;
+  const ne_views_tuning picked = pick->t;
+  for (int pre = 1; pre <= 2 && picked.split_passes != 1; pre++) {
+    ne_views_tuning t = picked;
+    t.pretrace = pre;
     ne_status st = ne_views_set_tuning(vw, &t);
     if (st) return st;
     ne_views_stats s;

@@ -40,6 +40,7 @@ struct ViewArgs {
   unsigned long long* t_start;  // global timer when the first warp started
   const DeferQueue* defer_out;  // split batches: queue of paths deferred at their first event
   int defer_half;               // 1: deferral points every half bounce
+  int defer_top = 0;            // 1: every path is queued before its camera ray is intersected
 };
 
 // Index of the view owning path `idx` (views sorted by path_begin).
@@ -59,6 +60,7 @@ __global__ void __launch_bounds__(kThreads, pathMinBlocks(K)) k_views(const __gr
                                                                     unsigned long long* __restrict__ counter,
                                                                     uint32_t* err) {
   Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, nullptr, a.defer_out, 0ull, false, 0, a.defer_half};
+  c.deferTop = a.defer_top != 0;
   const int lane = threadIdx.x & 31;
   if (threadIdx.x == 0 && blockIdx.x == 0) atomicMin(a.t_start, globalTimer());
   for (;;) {
