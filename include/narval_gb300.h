@@ -207,7 +207,10 @@ typedef struct ne_tuning {
                             each resume pass, k_trace intersects the queued paths' bounce rays and
                             stores the hits, so the pass starts from them; 2 = the camera rays too
                             (a first pass queues every new path before its first intersection;
-                            the queues then hold 1.5 x the render's paths). Same image */
+                            the queues then hold 1.5 x the render's paths); 3 = the light samples'
+                            shadow rays too (a path stops at its visibility test and the next
+                            pass runs that bounce again with the result: each pass takes a path
+                            one traversal further). Same image */
 } ne_tuning;
 
 ne_status ne_scene_set_tuning(ne_scene* scene, const ne_tuning* tuning);

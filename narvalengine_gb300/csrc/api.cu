@@ -716,7 +716,7 @@ constexpr int kMaxSplitPasses = 64;
 int pathLaunches(const ne_scene* sc, bool count) {
   if (sc->variant != 3 || count) return 1;
   const bool traces = sc->pretrace && !sc->split_half && (sc->feature_set == K_MESH || sc->feature_set == K_SURFACE);
-  const int passes = std::min(kMaxSplitPasses, std::max(2, sc->split_passes) + (traces && sc->pretrace == 2 ? 1 : 0));
+  const int passes = std::min(kMaxSplitPasses, std::max(2, sc->split_passes) + (traces && sc->pretrace >= 2 ? 1 : 0));
   return passes + (traces ? passes - 1 : 0);  // k_trace before every resume pass
 }
 
@@ -744,8 +744,10 @@ ne_status launchSplit(ne_scene* sc, PathArgs b, int blocks, F launch, T trace = 
   ne_context* ctx = sc->ctx;
   // queue_quarters / 4 of the paths (default 3: class 0 half the paths, class 1 a quarter)
   const bool traces = canTrace && sc->pretrace && !sc->split_half;
-  // pretrace 2: the first pass queues every path before its camera ray (class 0 holds them all)
-  const bool gen = traces && sc->pretrace == 2;
+  // pretrace 2: the first pass queues every path before its camera ray (class 0 holds them all);
+  // 3: also the shadow rays (every pass then takes each path one traversal further)
+  const bool gen = traces && sc->pretrace >= 2;
+  const bool shadows = traces && sc->pretrace == 3;
   size_t cap = std::min(kMaxDeferEntries,
                         std::max<size_t>(3072, (size_t)(b.total / 4) * (size_t)sc->queue_quarters));
   if (gen) cap = std::min(kMaxDeferEntries, std::max(cap, (size_t)b.total / 2 * 3 + 3));
@@ -806,7 +808,8 @@ ne_status launchSplit(ne_scene* sc, PathArgs b, int blocks, F launch, T trace = 
     if (traces) NE_CUDA(trace(sc->d_dq + pass - 1, traceCounters + pass), "k_trace launch");
     b.defer_in = sc->d_dq + pass - 1;
     b.defer_out = sc->d_dq + pass;
-    b.defer_at = pass == passes - 1 ? -1 : pass - (gen ? 1 : 0);
+    b.defer_at = pass == passes - 1 ? -1 : (shadows ? 0 : pass - (gen ? 1 : 0));
+    b.defer_shadow = shadows && pass != passes - 1;
     NE_CUDA(launch(pass, persistentBlocks(sc), b, counters + pass), "resume kernel launch");
   }
   return NE_OK;
@@ -1786,7 +1789,7 @@ ne_status ne_scene_set_tuning(ne_scene* sc, const ne_tuning* t) {
   if (!sc || !t || t->kernel < 0 || t->kernel > 3 || t->track_share < 1 || t->track_share > 32 ||
       t->blocks_per_sm < 0 || t->blocks_per_sm > 64 || t->split_passes < 0 || t->split_passes == 1 ||
       t->split_passes > 64 || t->split_half < 0 || t->split_half > 1 || t->queue_quarters < 0 ||
-      t->queue_quarters > 8 || t->pretrace < 0 || t->pretrace > 2)
+      t->queue_quarters > 8 || t->pretrace < 0 || t->pretrace > 3)
     return NE_ERR_INVALID_ARG;
   ne_context* ctx = sc->ctx;
   int fit = 1;
@@ -2962,6 +2965,14 @@ ne_status ne_scene_autotune(ne_scene* sc, const ne_render_params* p, int repeats
     for (int pre : {1, 2}) {  // the bounce rays; the camera rays too
       ne_tuning t = base;
       t.pretrace = pre;
+      ne_status st = tryTuning(t);
+      if (st) return st;
+    }
+    // the shadow rays too: every pass takes each path one traversal further, so more passes
+    for (int passes : {6, 8, 12, 16, 24}) {
+      ne_tuning t = base;
+      t.pretrace = 3;
+      t.split_passes = passes;
       ne_status st = tryTuning(t);
       if (st) return st;
     }

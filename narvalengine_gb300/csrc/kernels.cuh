@@ -109,6 +109,9 @@ struct PathArgs {
   // first pass of a split render whose bounce rays are traced ahead (k_trace): every path
   // stops at the top of bounce 0, before its camera ray is intersected
   int defer_top = 0;
+  // resume passes of a surface scene whose shadow rays are traced ahead too: a path stops at
+  // its light sample's visibility test (and at the end of every bounce)
+  int defer_shadow = 0;
   const ViewDone* views = nullptr;  // resume passes of a batch of views: completion accounting
 };
 
@@ -191,6 +194,7 @@ __global__ void __launch_bounds__(kThreads, pathMinBlocks(K)) k_resume(const __g
                                                                      uint32_t* err) {
   Ctx<K> c{s, Sampler{}, Counters{0, 0, 0, 0}, err, 0u, false, a.cache, a.defer_out, 0ull, false, a.defer_at,
            a.defer_half};
+  c.deferShadow = a.defer_shadow != 0;
   const DeferQueue& q = *a.defer_in;
   const unsigned long long n0 = min(*q.count, q.cap);
   const unsigned long long n = n0 + (q.count_hi ? min(*q.count_hi, q.cap_hi) : 0u);
@@ -212,7 +216,12 @@ __global__ void __launch_bounds__(kThreads, pathMinBlocks(K)) k_resume(const __g
         c.pidx = (uint32_t)ps.idx;
         c.train = isTrainingPath(ps.idx, a.cache->train_stride);
       }
-      V3 L = liLoop(c, a.P, v, ps.mode == 0, ps.mode == kModeHit ? 1 : (ps.mode == kModeMiss ? 2 : 0));
+      // hit known (3, and 5-7: a stop at a shadow ray comes after the bounce's hit), no hit (4);
+      // a shadow ray's result known (6 visible, 7 blocked)
+      const int pre = (ps.mode == kModeHit || ps.mode >= kModeShadow) ? 1 : (ps.mode == kModeMiss ? 2 : 0);
+      c.shadowVis = ps.mode == kModeVisible ? 1 : (ps.mode == kModeBlocked ? 2 : 0);
+      c.shadowSlot = -1;
+      V3 L = liLoop(c, a.P, v, ps.mode == 0, pre);
       if (!c.deferred) {
         a.out[3 * ps.idx + 0] = L.x;
         a.out[3 * ps.idx + 1] = L.y;
@@ -253,6 +262,17 @@ __global__ void __launch_bounds__(kThreads, 8) k_trace(const __grid_constant__ D
     if (i >= n) continue;
     const size_t e = i < n0 ? i : q.cap + (i - n0);
     uint4 w9 = words[9 * plane + e];
+    if constexpr (shadowQueue<K>()) {
+      if (w9.x == kModeShadow) {
+        // the light sample's visibility test: visibilityTr from the hit to the point on the light
+        const uint4 w3 = words[3 * plane + e], w4 = words[4 * plane + e], w5 = words[5 * plane + e];
+        const V3 p = v3(__uint_as_float(w4.z), __uint_as_float(w4.w), __uint_as_float(w5.x));
+        const V3 lightPoint = v3(__uint_as_float(w3.x), __uint_as_float(w3.y), __uint_as_float(w3.z));
+        w9.x = isBlack(visibilityTr(c, p, lightPoint)) ? kModeBlocked : kModeVisible;
+        words[9 * plane + e] = w9;
+        continue;
+      }
+    }
     if (w9.x != kModeTop) continue;
     const uint4 w1 = words[1 * plane + e], w2 = words[2 * plane + e];
     uint4 w4 = words[4 * plane + e];

@@ -217,7 +217,30 @@ struct Ctx {
   int deferAt;
   int deferHalf;  // 1: deferral points every half bounce (after sampling, and after the bounce)
   bool deferTop = false;  // K_SPLIT first pass: defer every new path before its first intersection
+  // K_SPLIT passes of surface scenes whose shadow rays are traced ahead: stop a path at its
+  // light sample's visibility test (shadowSlot: its queue entry, shadowPoint: the point on the
+  // light), or take the test's known result (shadowVis: 1 visible, 2 blocked, 0 unknown)
+  bool deferShadow = false;
+  int shadowVis = 0;
+  int shadowSlot = -1;
+  V3 shadowPoint = V3{0, 0, 0};
 };
+
+// Kernels whose paths can stop at a shadow ray: split kernels of surface-only feature sets (the
+// visibility test there draws no random numbers and gives all or nothing).
+// Slot in an append-only buffer: one atomic per group of lanes that append together.
+NE_D uint32_t appendSlot(uint32_t* count) {
+  namespace cg = cooperative_groups;
+  cg::coalesced_group g = cg::coalesced_threads();
+  uint32_t base = 0;
+  if (g.thread_rank() == 0) base = atomicAdd(count, (uint32_t)g.size());
+  return g.shfl(base, 0) + g.thread_rank();
+}
+
+template <uint32_t K>
+__host__ __device__ constexpr bool shadowQueue() {
+  return (K & K_SPLIT) && !(K & (FT_GRID | FT_HOMOG | FT_VOLBSDF | K_CACHE | K_COUNT));
+}
 
 // Buffers of a render that ends paths in the learned radiance cache. A path that reaches
 // a scattering vertex in a grid medium at or after bounce `bounce` either stops there and
@@ -1257,7 +1280,23 @@ NE_NI V3 estimateDirect(Ctx<K>& c, const Ray& incoming, const Hit& isect, const 
     }
     if (!isBlack(f)) {
       V3 pointOnLight = samplePointOnSurface<K>(s, light.primitive, isect, lin.wcs, c.S);
-      Li = Li * visibilityTr(c, isect.hitPoint, pointOnLight);
+      V3 vis;
+      if (shadowQueue<K>() && c.shadowVis) {
+        // traced ahead by k_trace (the same visibilityTr on the same segment)
+        vis = c.shadowVis == 1 ? v3(1, 1, 1) : v3(0, 0, 0);
+        c.shadowVis = 0;
+      } else {
+        if (shadowQueue<K>() && c.deferShadow) {
+          const uint32_t slot = appendSlot(c.dq->count);
+          if (slot < c.dq->cap) {  // stop here: the caller queues the path with this segment
+            c.shadowSlot = (int)slot;
+            c.shadowPoint = pointOnLight;
+            return Ld;
+          }
+        }
+        vis = visibilityTr(c, isect.hitPoint, pointOnLight);
+      }
+      Li = Li * vis;
       if (!isBlack(Li)) {
         float weight = powerHeuristic(lightPdf, scatteringPdf);
         Ld = Ld + ((f * Li) * weight) / lightPdf;
@@ -1318,14 +1357,6 @@ NE_D V3 uniformSampleOneLight(Ctx<K>& c, const Ray& incoming, const Hit& isect) 
   return estimateDirect(c, incoming, isect, light, inst) / lightPdf;
 }
 
-// Slot in an append-only buffer: one atomic per group of lanes that append together.
-NE_D uint32_t appendSlot(uint32_t* count) {
-  namespace cg = cooperative_groups;
-  cg::coalesced_group g = cg::coalesced_threads();
-  uint32_t base = 0;
-  if (g.thread_rank() == 0) base = atomicAdd(count, (uint32_t)g.size());
-  return g.shfl(base, 0) + g.thread_rank();
-}
 
 struct PathParams {
   int bounces;
@@ -1359,6 +1390,11 @@ static_assert(offsetof(PathState, v) == 0 && offsetof(LiVars, incoming) == 24 &&
                   sizeof(Hit) == 40 && offsetof(PathState, mode) == 144,
               "PathState word layout");
 constexpr uint32_t kModeTop = 1, kModeHit = 3, kModeMiss = 4;
+// 5: at the top of bounce v.b, v.isect its hit, stopped at the light sample's visibility test
+// from v.isect.hitPoint to v.scattered.o; 6 / 7: the same with the test's result (visible /
+// blocked) known
+constexpr uint32_t kModeShadow = 5, kModeVisible = 6, kModeBlocked = 7;
+
 
 // Deferred paths of one pass. With count_hi set, paths deferred right after a free-flight
 // sample are binned by the light their next draw will pick (uniformSampleOneLight's first draw,
@@ -1408,6 +1444,9 @@ NE_D V3 liLoop(Ctx<K>& c, const PathParams& P, LiVars& v, bool resume, int pretr
   V3 vPos = v3(0, 0, 0), vDir = v3(0, 0, 0), vL = v3(0, 0, 0), vT = v3(0, 0, 0);
   for (; v.b < P.bounces; v.b++) {
     const int b = v.b;
+    // the bounce's starting radiance and sampler position, for a stop at its shadow ray
+    const V3 L0 = v.L;
+    const uint32_t dim0 = c.S.dim;
     bool did = true;
     const DMaterial* mat;
     bool medium;
@@ -1537,7 +1576,28 @@ NE_D V3 liLoop(Ctx<K>& c, const PathParams& P, LiVars& v, bool resume, int pretr
         }
       }
       if (!did || !mat || mat->bsdf == NE_BSDF_NONE) break;
-      v.L = v.L + v.T * uniformSampleOneLight(c, v.incoming, v.isect);
+      {
+        const V3 lightSample = uniformSampleOneLight(c, v.incoming, v.isect);
+        if (shadowQueue<K>() && c.shadowSlot >= 0) {
+          // stopped at the light sample's visibility test: queue the path as it was at the top
+          // of this bounce (L and the sampler before the bounce), the hit known, with the
+          // segment's end on the light (in scattered.o, unused at the top of a surface bounce);
+          // the next pass runs the bounce again with the test's result
+          PathState ps;
+          ps.v = v;
+          ps.v.L = L0;
+          ps.v.scattered.o = c.shadowPoint;
+          ps.key = c.S.key;
+          ps.dim = dim0;
+          ps.mode = kModeShadow;
+          ps.idx = c.idx;
+          storeState(*c.dq, (size_t)c.shadowSlot, ps);
+          c.shadowSlot = -1;
+          c.deferred = true;
+          return v.L;
+        }
+        v.L = v.L + v.T * lightSample;
+      }
       Ray scattered;
       scattered.o = v.isect.hitPoint;
       scattered.d = bsdfSample<K>(*mat, v.incoming.d, v.isect.normal, c.S);

@@ -263,7 +263,7 @@ def test_mesh_bvh_parity(ne, ctx, oracle_lib, subdivisions):
         gp = scene.trace_paths(keys, ne.render_params(seed=8))
         assert np.array_equal(gp, cp), f"kernel {kernel}: max rel {rel_err(gp, cp).max():.3e}"
     # the bounce rays (and the camera rays) traced ahead of each pass by their own kernel
-    for passes, pre in ((2, 1), (3, 1), (6, 1), (2, 2), (3, 2), (5, 2)):
+    for passes, pre in ((2, 1), (3, 1), (6, 1), (2, 2), (3, 2), (5, 2), (2, 3), (5, 3), (12, 3), (30, 3)):
         scene.set_tuning(kernel=3, split_passes=passes, split_half=0, pretrace=pre)
         gp = scene.trace_paths(keys, ne.render_params(seed=8))
         assert np.array_equal(gp, cp), f"pretrace {pre}, {passes} passes: max rel {rel_err(gp, cp).max():.3e}"
@@ -284,17 +284,18 @@ def test_pretrace_surface_scene(ne, ctx):
             img, st = scene.render(p)
             assert np.array_equal(img.view(np.uint32), ref.view(np.uint32)), passes
             assert st["kernel_launches"] == 2 * passes - 1 + 1, st["kernel_launches"]
-            # camera rays too: one more pass that only queues the new paths
-            scene.set_tuning(kernel=3, split_passes=passes, split_half=0, pretrace=2)
-            img, st = scene.render(p)
-            assert np.array_equal(img.view(np.uint32), ref.view(np.uint32)), (passes, 2)
-            assert st["kernel_launches"] == 2 * (passes + 1) - 1 + 1, st["kernel_launches"]
+            # camera rays too: one more pass that only queues the new paths; then the shadow rays
+            for pre in (2, 3):
+                scene.set_tuning(kernel=3, split_passes=passes, split_half=0, pretrace=pre)
+                img, st = scene.render(p)
+                assert np.array_equal(img.view(np.uint32), ref.view(np.uint32)), (passes, pre)
+                assert st["kernel_launches"] == 2 * (passes + 1) - 1 + 1, st["kernel_launches"]
         # by half bounce the knob has no effect
         scene.set_tuning(kernel=3, split_passes=8, split_half=1, pretrace=1)
         img, st = scene.render(p)
         assert np.array_equal(img.view(np.uint32), ref.view(np.uint32)) and st["kernel_launches"] == 9
         with pytest.raises(ne.NarvalError):
-            scene.set_tuning(kernel=3, pretrace=3)
+            scene.set_tuning(kernel=3, pretrace=4)
     finally:
         scene.close()
 
