@@ -34,6 +34,7 @@ the slowest rank's time.
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -514,6 +515,8 @@ def main():
         s2.render(pe, out=out_host)
         s2.close()
     d.barrier()
+    gc.collect()
+    gc.disable()  # the host clock times the library, not a collection of the harness's objects
     t0 = time.perf_counter()
     e2e_steps = []
     for _ in range(args.steps):
@@ -524,6 +527,7 @@ def main():
         s2.close()
         e2e_steps.append(round((time.perf_counter() - ts) * 1e3, 2))
     e2e_s = time.perf_counter() - t0
+    gc.enable()
     d.barrier()
     e2e_s = d.max(e2e_s)
     e2e = paths_per_step * args.steps * world / e2e_s / 1e6
@@ -576,6 +580,7 @@ def main():
                 "config": {"workload": WORKLOADS[args.scene], "paths_per_step": paths_per_step, "pixels": [W, H],
                            "spp": spp, "bounces": host.bounces,
                            "l2": "flushed between steps (256 MiB write, outside events)",
+                           "e2e_host": "Python garbage collection off in the e2e loop",
                            "parallelism": f"{world} GPU(s), sample ranges per rank",
                            "tuning": tuning, "tuning_source": tuning_source},
                 "e2e": {"value": e2e, "unit": "Mpaths/s", "h2d_bytes_per_step": h2d,
