@@ -1739,16 +1739,21 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
   sc->d.width = D.settings.width;
   sc->d.height = D.settings.height;
   // feature bits: which primitive, BSDF, medium and light kinds the kernels must handle
-  uint32_t F = 0;
-  for (uint32_t i = 0; i < D.n_prims; i++) {
-    switch (D.prims[i].type) {
-      case NE_PRIM_SPHERE: F |= FT_SPHERE; break;
-      case NE_PRIM_RECTANGLE: F |= FT_RECT; break;
-      case NE_PRIM_AABB: F |= FT_AABB; break;
-      case NE_PRIM_TRIANGLE: F |= FT_TRI; break;
-      default: F |= FT_POINT; break;
+  std::atomic<uint32_t> primBits{0};
+  nehost::parallelFor(D.n_prims, 1u << 16, [&](size_t i0, size_t i1) {
+    uint32_t f = 0;
+    for (size_t i = i0; i < i1; i++) {
+      switch (D.prims[i].type) {
+        case NE_PRIM_SPHERE: f |= FT_SPHERE; break;
+        case NE_PRIM_RECTANGLE: f |= FT_RECT; break;
+        case NE_PRIM_AABB: f |= FT_AABB; break;
+        case NE_PRIM_TRIANGLE: f |= FT_TRI; break;
+        default: f |= FT_POINT; break;
+      }
     }
-  }
+    primBits.fetch_or(f);
+  });
+  uint32_t F = primBits.load();
   for (uint32_t i = 0; i < D.n_models; i++) {
     if (D.models[i].has_bbox) F |= FT_BBOX;
     if (D.models[i].use_bvh) F |= FT_TRI;

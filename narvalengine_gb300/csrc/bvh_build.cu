@@ -698,6 +698,9 @@ cudaError_t buildSahBvh(cudaStream_t st, const DPrim* prims, uint32_t first, uin
   std::vector<TaskResult> res;
   std::vector<Task> next;
   std::vector<int32_t> nextIds;
+  // nodes are created in batches (the root, then each level's children): a node's children are
+  // in the batch after its own
+  std::vector<size_t> batches = {0};
   int level = 0;
   for (; level < kMaxLevels && !tasks.empty(); level++) {
     const uint32_t nt = (uint32_t)tasks.size();
@@ -793,6 +796,7 @@ cudaError_t buildSahBvh(cudaStream_t st, const DPrim* prims, uint32_t first, uin
       sumT += a1;
     }
     const size_t node0 = nodes.size();
+    batches.push_back(node0);
     nodes.resize(node0 + sumN);
     next.resize(sumT);
     nextIds.resize(sumT);
@@ -847,13 +851,20 @@ cudaError_t buildSahBvh(cudaStream_t st, const DPrim* prims, uint32_t first, uin
   // then positions top-down
   const size_t nn = nodes.size();
   std::vector<uint32_t> size(nn, 1), pos(nn, 0);
-  for (size_t i = nn; i-- > 0;)
-    if (nodes[i].left >= 0) size[i] = 1 + size[nodes[i].left] + size[nodes[i].right];
-  for (size_t i = 0; i < nn; i++)
-    if (nodes[i].left >= 0) {
-      pos[nodes[i].left] = pos[i] + 1;
-      pos[nodes[i].right] = pos[i] + 1 + size[nodes[i].left];
-    }
+  batches.push_back(nn);
+  for (size_t k = batches.size() - 1; k-- > 0;)  // batch by batch, the last first
+    nehost::parallelFor(batches[k + 1] - batches[k], 1u << 14, [&](size_t i0, size_t i1) {
+      for (size_t i = batches[k] + i0; i < batches[k] + i1; i++)
+        if (nodes[i].left >= 0) size[i] = 1 + size[nodes[i].left] + size[nodes[i].right];
+    });
+  for (size_t k = 0; k + 1 < batches.size(); k++)
+    nehost::parallelFor(batches[k + 1] - batches[k], 1u << 14, [&](size_t i0, size_t i1) {
+      for (size_t i = batches[k] + i0; i < batches[k] + i1; i++)
+        if (nodes[i].left >= 0) {
+          pos[nodes[i].left] = pos[i] + 1;
+          pos[nodes[i].right] = pos[i] + 1 + size[nodes[i].left];
+        }
+    });
   nodesOut.resize(nn);
   nehost::parallelFor(nn, 1u << 15, [&](size_t i0, size_t i1) {
   for (size_t i = i0; i < i1; i++) {
