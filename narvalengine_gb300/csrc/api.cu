@@ -475,6 +475,34 @@ void buildBvh(const ne_primitive* prims, std::vector<uint32_t>& order, std::vect
 }
 
 // ---------------------------------------------------------------- kernels
+// The descriptor's primitives in the device layout: Triangle::calculateArea for triangles (the
+// float arithmetic of the host helpers, in the same order), the grid-medium flag from the
+// primitive's material.
+__global__ void k_convert_prims(const ne_primitive* __restrict__ src, uint32_t n, const uint8_t* __restrict__ gridMat,
+                                DPrim* __restrict__ dst) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const ne_primitive s = src[i];
+    DPrim d;
+    d.type = s.type;
+    d.material = s.material;
+    d.flags = (s.material >= 0 && gridMat[s.material]) ? DPRIM_GRID_MEDIUM : 0;
+    d.radius = s.radius;
+    for (int k = 0; k < 3; k++) {
+      d.p0[k] = s.p0[k];
+      d.p1[k] = s.p1[k];
+      d.p2[k] = s.p2[k];
+    }
+    d.area = 0.0f;
+    if (s.type == NE_PRIM_TRIANGLE) {
+      const float e1x = s.p1[0] - s.p0[0], e1y = s.p1[1] - s.p0[1], e1z = s.p1[2] - s.p0[2];
+      const float e2x = s.p2[0] - s.p0[0], e2y = s.p2[1] - s.p0[1], e2z = s.p2[2] - s.p0[2];
+      const float nx = e1y * e2z - e2y * e1z, ny = e1z * e2x - e2z * e1x, nz = e1x * e2y - e2x * e1y;
+      d.area = nefm::fsqrt((nx * nx + ny * ny) + nz * nz) / 2.0f;
+    }
+    dst[i] = d;
+  }
+}
+
 // The cells of cell slabs [z0, z1): a block takes rows (y, z) of W + 1 cells, its threads
 // the cells of a row.
 __global__ void k_cells(const float* __restrict__ grid, uint32_t W, uint32_t H, uint32_t D, uint32_t z0, uint32_t z1,
@@ -1449,6 +1477,12 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
     ne_scene_destroy(sc);
     return st;
   };
+  // a failed CUDA call from here on also releases the half-built scene
+#define NE_CUDA_SC(call, where)                                           \
+  do {                                                                    \
+    cudaError_t e_ = (call);                                              \
+    if (e_ != cudaSuccess) return cleanup(cudaFail(ctx, e_, where));      \
+  } while (0)
 
   // instances
   std::vector<DInstance> inst(ninst);
@@ -1485,32 +1519,12 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
   std::vector<float> mediumBoxes;
   const int32_t nMediumBoxes = mediumBoxesOf(D, mediumBoxes);
   // primitives
-  // filled below (no zeroing pass first: every element is written)
-  std::unique_ptr<DPrim[]> primBuf(new DPrim[std::max<size_t>(1, D.n_prims)]);
-  DPrim* prims = primBuf.get();
-  auto convertPrim = [&](uint32_t i) {
-    const ne_primitive& s = D.prims[i];
-    DPrim& d = prims[i];
-    memset(&d, 0, sizeof(d));
-    d.type = s.type;
-    d.material = s.material;
-    d.radius = s.radius;
-    memcpy(d.p0, s.p0, 12); memcpy(d.p1, s.p1, 12); memcpy(d.p2, s.p2, 12);
-    if (s.type == NE_PRIM_TRIANGLE) {  // Triangle::calculateArea
-      H3 a = h3(s.p0[0], s.p0[1], s.p0[2]), b = h3(s.p1[0], s.p1[1], s.p1[2]), c = h3(s.p2[0], s.p2[1], s.p2[2]);
-      H3 e1 = hsub(b, a), e2 = hsub(c, a);
-      H3 n = h3(e1.y * e2.z - e2.y * e1.z, e1.z * e2.x - e2.z * e1.x, e1.x * e2.y - e2.x * e1.y);
-      d.area = hlen(n) / 2.0f;
-    }
-    if (s.material >= 0) {
-      const ne_material& m = D.materials[s.material];
-      if (m.medium >= 0 && D.media[m.medium].type == NE_MEDIUM_GRID) d.flags |= DPRIM_GRID_MEDIUM;
-    }
-  };
-  // large meshes: in parallel ranges (each primitive is converted on its own)
-  nehost::parallelFor(D.n_prims, 1u << 15, [&](size_t b, size_t e) {
-    for (size_t i = b; i < e; i++) convertPrim((uint32_t)i);
-  });
+  // per material: does its medium make the primitive a grid-medium boundary (DPrim::flags)
+  std::vector<uint8_t> gridMat(std::max<uint32_t>(1, D.n_materials), 0);
+  for (uint32_t i = 0; i < D.n_materials; i++) {
+    const ne_material& m = D.materials[i];
+    gridMat[i] = (m.medium >= 0 && D.media[m.medium].type == NE_MEDIUM_GRID) ? 1 : 0;
+  }
   // models + BVHs
   std::vector<DModel> models(D.n_models);
   std::vector<DNode> nodes;
@@ -1636,24 +1650,24 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
       // the grid in slabs of z slices on the copy stream; the cells of each slab (which read
       // its slices and the next one) built on the main stream once they are there
       if (!ctx->copy_stream) {
-        NE_CUDA(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        NE_CUDA_SC(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking), "cudaStreamCreate");
         for (cudaEvent_t& ev : ctx->slab_ev)
-          NE_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate");
+          NE_CUDA_SC(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate");
       }
       const uint32_t W = s.res[0], H = s.res[1], Dz = s.res[2];
       const size_t slice = (size_t)W * H;
       const int slabs = (int)std::min<uint32_t>(kGridSlabs, Dz);
       // the buffers may have been in use on the main stream until now
-      NE_CUDA(cudaEventRecord(ctx->slab_ev[kGridSlabs], ctx->stream), "cudaEventRecord");
-      NE_CUDA(cudaStreamWaitEvent(ctx->copy_stream, ctx->slab_ev[kGridSlabs], 0), "cudaStreamWaitEvent");
+      NE_CUDA_SC(cudaEventRecord(ctx->slab_ev[kGridSlabs], ctx->stream), "cudaEventRecord");
+      NE_CUDA_SC(cudaStreamWaitEvent(ctx->copy_stream, ctx->slab_ev[kGridSlabs], 0), "cudaStreamWaitEvent");
       uint32_t cellsDone = 0;
       for (int k = 0; k < slabs; k++) {
         const uint32_t z0 = (uint32_t)((uint64_t)Dz * k / slabs), z1 = (uint32_t)((uint64_t)Dz * (k + 1) / slabs);
-        NE_CUDA(cudaMemcpyAsync((float*)gp + z0 * slice, s.grid + z0 * slice, (size_t)(z1 - z0) * slice * sizeof(float),
+        NE_CUDA_SC(cudaMemcpyAsync((float*)gp + z0 * slice, s.grid + z0 * slice, (size_t)(z1 - z0) * slice * sizeof(float),
                                 cudaMemcpyHostToDevice, ctx->copy_stream),
                 "cudaMemcpyAsync(grid)");
-        NE_CUDA(cudaEventRecord(ctx->slab_ev[k], ctx->copy_stream), "cudaEventRecord");
-        NE_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->slab_ev[k], 0), "cudaStreamWaitEvent");
+        NE_CUDA_SC(cudaEventRecord(ctx->slab_ev[k], ctx->copy_stream), "cudaEventRecord");
+        NE_CUDA_SC(cudaStreamWaitEvent(ctx->stream, ctx->slab_ev[k], 0), "cudaStreamWaitEvent");
         // cell slab z reads grid slices z and z + 1: with slices [0, z1) there, cells [.., z1 - 1)
         const uint32_t cellsTo = k == slabs - 1 ? Dz + 1 : z1 - 1;
         if (cellsTo > cellsDone) {
@@ -1669,7 +1683,35 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
     }
   }
   ne_status st = NE_OK;
-  if ((st = upload(sc, prims, D.n_prims, &sc->d.prims))) return cleanup(st);
+  if (D.n_prims) {
+    // the descriptor's primitives converted on the device (k_convert_prims)
+    void* raw = nullptr;
+    void* dp = nullptr;
+    const uint8_t* dGrid = nullptr;
+    NE_CUDA_SC(ctx->pool.get((size_t)D.n_prims * sizeof(ne_primitive), &raw), "cudaMalloc(primitives)");
+    cudaError_t ce = cudaMemcpyAsync(raw, D.prims, (size_t)D.n_prims * sizeof(ne_primitive), cudaMemcpyHostToDevice,
+                                     ctx->stream);
+    if (ce != cudaSuccess) {
+      ctx->pool.put(raw);
+      return cleanup(cudaFail(ctx, ce, "cudaMemcpyAsync(primitives)"));
+    }
+    if ((st = upload(sc, gridMat.data(), gridMat.size(), &dGrid))) {
+      ctx->pool.put(raw);
+      return cleanup(st);
+    }
+    cudaError_t e = ctx->pool.get((size_t)D.n_prims * sizeof(DPrim), &dp);
+    if (e != cudaSuccess) {
+      ctx->pool.put(raw);
+      return cleanup(cudaFail(ctx, e, "cudaMalloc(primitives)"));
+    }
+    sc->allocs.push_back(dp);
+    const int blocks = (int)std::min<size_t>(((size_t)D.n_prims + 255) / 256, (size_t)ctx->sm_count * 8);
+    k_convert_prims<<<blocks, 256, 0, ctx->stream>>>((const ne_primitive*)raw, D.n_prims, dGrid, (DPrim*)dp);
+    e = cudaGetLastError();
+    ctx->pool.put(raw);  // stream order: its next user runs after the conversion
+    if (e != cudaSuccess) return cleanup(cudaFail(ctx, e, "k_convert_prims launch"));
+    sc->d.prims = (const DPrim*)dp;
+  }
   if (D.settings.bvh_build == 1) {
     // binned-SAH trees built on the GPU from the uploaded primitives
     for (uint32_t i = 0; i < D.n_models; i++) {
@@ -1789,6 +1831,8 @@ ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene**
   *out = sc;
   return NE_OK;
 }
+
+#undef NE_CUDA_SC
 
 ne_status ne_scene_set_tuning(ne_scene* sc, const ne_tuning* t) {
   if (!sc || !t || t->kernel < 0 || t->kernel > 3 || t->track_share < 1 || t->track_share > 32 ||
