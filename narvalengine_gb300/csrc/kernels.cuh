@@ -241,7 +241,9 @@ __global__ void __launch_bounds__(kThreads, pathMinBlocks(K)) k_resume(const __g
 // path's state (mode 3, or 4 for no hit) so that the resume skips the call. The warps run
 // nothing but the traversal. Each path's words 1, 2 (the ray), 4-6 (the previous hit, which a
 // miss leaves in place but for its primitive) and 9 (the mode) are read, words 4-6 and 9
-// written back.
+// written back. In surface-only kernels a path stopped at its light sample's visibility test
+// (mode 5) gets the test's answer (visibilityTr from the hit to the point on the light in word
+// 3; mode 6 visible, 7 blocked), and only word 9 is written.
 template <uint32_t K>
 __global__ void __launch_bounds__(kThreads, 8) k_trace(const __grid_constant__ DScene s, const DeferQueue* qp,
                                                   unsigned long long* __restrict__ counter, uint32_t* err) {
