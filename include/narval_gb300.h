@@ -126,6 +126,11 @@ ne_status ne_context_create(int device, ne_context** out);
 /* Destroys the context and every scene still uploaded to it; their handles become invalid. */
 void ne_context_destroy(ne_context* ctx);
 const char* ne_last_error(const ne_context* ctx);
+/* Device memory that scenes and renders release stays cached in the context for their
+ * successors (no counterpart in the reference): at most `bytes` of it (by default a quarter
+ * of the device's memory, at least 16 GiB); the excess is freed now, largest buffers first.
+ * 0 frees the whole cache and caches nothing from then on. */
+ne_status ne_context_set_cache_limit(ne_context* ctx, size_t bytes);
 
 /* Copies a scene description to the device (grids, primitives, BVHs). */
 ne_status ne_scene_upload(ne_context* ctx, const ne_scene_desc* desc, ne_scene** out);

@@ -186,6 +186,10 @@ class Context:
     def flush_l2(self, nbytes: int = 256 << 20):
         self.check(library().ne_context_flush_l2(self._h, nbytes))
 
+    def set_cache_limit(self, nbytes: int):
+        """Bytes of released device memory the context keeps cached (ne_context_set_cache_limit)."""
+        self.check(library().ne_context_set_cache_limit(self._h, nbytes))
+
     def read_bandwidth(self, nbytes: int, iters: int = 50) -> float:
         """GB/s of a read-only kernel over an `nbytes` buffer (ne_measure_read_bandwidth)."""
         gbs = C.c_double()

@@ -166,6 +166,7 @@ SIGNATURES = {
     "ne_context_event_elapsed": (C.c_int32, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_float)]),
     "ne_context_synchronize": (C.c_int32, [C.c_void_p]),
     "ne_context_flush_l2": (C.c_int32, [C.c_void_p, C.c_size_t]),
+    "ne_context_set_cache_limit": (C.c_int32, [C.c_void_p, C.c_size_t]),
     "ne_measure_read_bandwidth": (C.c_int32, [C.c_void_p, C.c_size_t, C.c_int, C.POINTER(C.c_double)]),
     "ne_measure_random_read": (C.c_int32, [C.c_void_p, C.c_size_t, C.c_int, C.POINTER(C.c_double)]),
     "ne_debug_fmath": (C.c_int32, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t, C.c_void_p]),

@@ -42,13 +42,17 @@ using namespace nedev;
 // released by a scene or a render stay here, idle, and the next request of a similar size
 // (the smallest cached buffer of at least the requested size and at most twice it) takes one.
 // All users enqueue on the context's one stream, so a reused buffer is never still in use by
-// earlier work. At most `limit` bytes stay cached (the rest is freed); a failed cudaMalloc
-// frees the cache and retries.
+// earlier work. At most `limit` bytes stay cached (the rest is freed, largest first): a
+// quarter of the device's memory, at least 16 GiB, unless ne_context_set_cache_limit says
+// otherwise. A frame with camera rays traced ahead on a 1024^2 x 32 spp image holds two 8 GB
+// deferred-path buffers, so a smaller limit would free and reallocate one of them every
+// frame. A failed cudaMalloc frees the cache and retries.
+constexpr size_t kPoolMinLimit = size_t(16) << 30;
 struct DevicePool {
   std::multimap<size_t, void*> idle;          // size -> buffer
   std::unordered_map<void*, size_t> size_of;  // every buffer handed out or idle
   size_t idle_bytes = 0;
-  size_t limit = size_t(16) << 30;
+  size_t limit = kPoolMinLimit;
   cudaError_t get(size_t bytes, void** out) {
     *out = nullptr;
     bytes = std::max<size_t>(bytes, 256);
@@ -1282,7 +1286,19 @@ ne_status ne_context_create(int device, ne_context** out) {
   if (e != cudaSuccess) return bad(e, "cudaMalloc");
   e = cudaMemset(ctx->d_err, 0, sizeof(uint32_t));
   if (e != cudaSuccess) return bad(e, "cudaMemset");
+  size_t freeMem = 0, totalMem = 0;
+  e = cudaMemGetInfo(&freeMem, &totalMem);
+  if (e != cudaSuccess) return bad(e, "cudaMemGetInfo");
+  ctx->pool.limit = std::max(kPoolMinLimit, totalMem / 4);
   *out = ctx;
+  return NE_OK;
+}
+
+ne_status ne_context_set_cache_limit(ne_context* ctx, size_t bytes) {
+  if (!ctx) return NE_ERR_INVALID_ARG;
+  NE_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  ctx->pool.limit = bytes;
+  ctx->pool.trim(bytes);
   return NE_OK;
 }
 

@@ -67,3 +67,27 @@ def test_tuning_errors(env):
         with pytest.raises(ne.NarvalError):
             scene.set_tuning(**t)
     assert ne.library().ne_scene_autotune(scene._h, None, 0, None, None) != 0
+
+
+def test_cache_limit(env):
+    """Released device memory is cached up to the context's limit; any limit, including none,
+    gives the same images."""
+    ne, ctx, scene = env
+    from narvalengine_gb300 import _abi
+    lib = ne.library()
+    assert lib.ne_context_set_cache_limit(None, 0) == _abi.NE_ERR_INVALID_ARG
+    host = ne.SceneHost.from_json(scene_path("cornell_c1"))
+    p = ne.render_params(seed=3, spp=2)
+    first, _ = scene.render(p)
+    try:
+        for limit in (0, 1 << 20, 64 << 30):
+            ctx.set_cache_limit(limit)
+            for _ in range(2):
+                s = ctx.upload(host)
+                s.set_tuning(**scene.tuning())
+                img, _ = s.render(p)
+                s.close()
+                assert np.array_equal(img, first)
+    finally:
+        import torch
+        ctx.set_cache_limit(max(16 << 30, torch.cuda.get_device_properties(0).total_memory // 4))
