@@ -867,22 +867,22 @@ cudaError_t buildSahBvh(cudaStream_t st, const DPrim* prims, uint32_t first, uin
     });
   nodesOut.resize(nn);
   nehost::parallelFor(nn, 1u << 15, [&](size_t i0, size_t i1) {
-  for (size_t i = i0; i < i1; i++) {
-    const BNode& b = nodes[i];
-    DNode d;
-    for (int j = 0; j < 3; j++) { d.lo[j] = b.mn[j]; d.hi[j] = b.mx[j]; }
-    uint32_t a, c;
-    if (b.left < 0) {
-      a = b.begin;
-      c = b.count | 0x80000000u;
-    } else {
-      a = pos[b.right] - pos[i];
-      c = 0;
+    for (size_t i = i0; i < i1; i++) {
+      const BNode& b = nodes[i];
+      DNode d;
+      for (int j = 0; j < 3; j++) { d.lo[j] = b.mn[j]; d.hi[j] = b.mx[j]; }
+      uint32_t a, c;
+      if (b.left < 0) {
+        a = b.begin;
+        c = b.count | 0x80000000u;
+      } else {
+        a = pos[b.right] - pos[i];
+        c = 0;
+      }
+      memcpy(&d.lo[3], &a, 4);
+      memcpy(&d.hi[3], &c, 4);
+      nodesOut[pos[i]] = d;
     }
-    memcpy(&d.lo[3], &a, 4);
-    memcpy(&d.hi[3], &c, 4);
-    nodesOut[pos[i]] = d;
-  }
   });
   slotsOut.resize(n);
   nehost::parallelFor(n, 1u << 16, [&](size_t i0, size_t i1) {
