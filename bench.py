@@ -445,7 +445,7 @@ def main():
     ap.add_argument("--split-half", type=int, default=1, help="split kernel: 1 = deferral every half bounce")
     ap.add_argument("--pretrace", type=int, default=0,
                     help="split kernel by bounce, scenes without media: 1 = bounce rays traced ahead of each "
-                         "pass, 2 = camera rays too")
+                         "pass, 2 = camera rays too, 3 = the light samples' shadow rays too")
     ap.add_argument("--track-share", type=int, default=16, help="regrouped kernel tracking threshold, 32nds")
     ap.add_argument("--profile-spp", type=int, default=0,
                     help="profiling case: two renders of the workload at this spp (the second is the one to capture)")
