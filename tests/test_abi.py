@@ -48,3 +48,4 @@ def test_null_arguments_are_rejected(built):
     assert lib.ne_trace_closest(None, None, 0, 0.0, 1.0, None) == -1
     assert lib.ne_scene_upload(None, None, None) == -1
     assert lib.ne_scene_host_load_json(None, None, None, None, 0) == -1
+    assert lib.ne_context_set_cache_limit(None, 0) == -1
