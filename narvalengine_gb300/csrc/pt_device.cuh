@@ -617,7 +617,7 @@ NE_D V3 lightLe(const DLight& L, const float* M, V3 d) {
   }
   return ld3(L.le);
 }
-// The identity matrix Model::intersect passes to Light::Le (primitives/Model.cpp:433).
+// The identity matrix Model::intersect passes to Light::Le (primitives/Model.cpp:435).
 __device__ __constant__ const float kIdentity12[12] = {1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0};
 NE_D V3 lightLi(const DLight& L) {  // Light::Li, DirectionalLight::Li
   if (L.type == NE_LIGHT_DIRECTIONAL) return ld3(L.le);

@@ -840,7 +840,7 @@ struct Reader {
           mx[c] = (mx[c] < v[c]) ? v[c] : mx[c];
         }
       }
-      // Triangle::calculateArea (primitives/Triangle.cpp:131-139)
+      // Triangle::calculateArea (primitives/Triangle.cpp:149-157)
       F3 a = f3(pr.p0), b = f3(pr.p1), c = f3(pr.p2);
       F3 n = cross(b - a, c - a);
       pr.area = nefm::fsqrt(dot(n, n)) / 2.0f;

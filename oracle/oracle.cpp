@@ -89,7 +89,7 @@ inline void setc(V3& a, int i, float v) { (i == 0 ? a.x : (i == 1 ? a.y : a.z)) 
 inline V3 ld3(const float* p) { return v3(p[0], p[1], p[2]); }
 inline bool isBlack(V3 v) { return v.x == 0 && v.y == 0 && v.z == 0; }      // Math.h:641-647
 inline bool areAllOne(V3 v) { return v.x == 1 && v.y == 1 && v.z == 1; }    // Math.h:649-651
-inline float avg(V3 v) { return (v.x + v.y + v.z) / 3.0f; }                  // Math.h:924-926
+inline float avg(V3 v) { return (v.x + v.y + v.z) / 3.0f; }                  // Math.h:930-932
 inline float absDot(V3 a, V3 b) { return std::fabs(dot(a, b)); }              // Math.h:657-659
 inline float maxc(V3 v) { return gmax(gmax(v.x, v.y), v.z); }
 inline bool same_bits(V3 a, V3 b) { return memcmp(&a, &b, sizeof(V3)) == 0; }
@@ -677,7 +677,7 @@ bool modelIntersect(const orc_scene& s, uint32_t mi, const Ray& ray, Hit& hit, f
   for (uint32_t k = 0; k < m.light_count; k++) {
     int pi = (int)(m.light_begin + k);
     const ne_primitive& p = s.prims[pi];
-    if (!isBlack(lightLe(s, lightOfMaterial(s, p.material), kIdentity16, ray.d))) continue;  // Model.cpp:433
+    if (!isBlack(lightLe(s, lightOfMaterial(s, p.material), kIdentity16, ray.d))) continue;  // Model.cpp:435
     bool local = primIntersect(s, pi, ray, temp);
     if (local && temp.tNear > tMin && temp.tNear < tMax) {
       tMax = temp.tNear;
@@ -1408,7 +1408,7 @@ orc_scene* orc_scene_create(const ne_scene_desc* d) {
   s->triArea.assign(d->n_prims, 0.0f);
   for (uint32_t i = 0; i < d->n_prims; i++) {
     const ne_primitive& p = s->prims[i];
-    if (p.type == NE_PRIM_TRIANGLE) {  // Triangle.cpp:131-139 calculateArea
+    if (p.type == NE_PRIM_TRIANGLE) {  // Triangle.cpp:149-157 calculateArea
       V3 a = ld3(p.p0), b = ld3(p.p1), c = ld3(p.p2);
       s->triArea[i] = length(cross(b - a, c - a)) / 2.0f;
     }
