@@ -22,7 +22,7 @@ LIB = os.path.join(PKG, "libnarval_gb300.so")
 
 CUDA_SOURCES = ["api.cu", "k_query.cu", "mlp.cu", "k_views.cu", "bvh_build.cu"] + sorted(
     f for f in os.listdir(os.path.join(os.path.dirname(os.path.abspath(__file__)), "csrc")) if f.startswith("k_path_"))
-HOST_SOURCES = ["scene_host.cpp", "scene_gen.cpp", "image_io.cpp", "image_load.cpp"]
+HOST_SOURCES = ["scene_host.cpp", "scene_gen.cpp", "image_io.cpp", "image_load.cpp", "vdb_read.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17",

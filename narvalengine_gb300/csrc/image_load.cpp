@@ -462,6 +462,29 @@ bool decodePnm(const std::vector<uint8_t>& f, Image& img, std::string& err) {
 
 }  // namespace
 
+bool zlibInflate(const uint8_t* p, size_t n, std::vector<uint8_t>& out, std::string& err) {
+  // RFC 1950: CMF (deflate, window <= 32 KiB), FLG (check bits, no preset dictionary), the
+  // deflate stream, then the Adler-32 of the data, big-endian
+  if (n < 6 || (p[0] & 0x0F) != 8 || (p[0] >> 4) > 7 || ((p[0] << 8) | p[1]) % 31 != 0 || (p[1] & 0x20)) {
+    err = "bad zlib header";
+    return false;
+  }
+  const size_t start = out.size();
+  if (!inflate(p + 2, n - 2, out, err)) return false;
+  uint32_t a = 1, b = 0;
+  for (size_t i = start; i < out.size(); i++) {
+    a = (a + out[i]) % 65521u;
+    b = (b + a) % 65521u;
+  }
+  const uint8_t* t = p + n - 4;
+  const uint32_t want = ((uint32_t)t[0] << 24) | ((uint32_t)t[1] << 16) | ((uint32_t)t[2] << 8) | t[3];
+  if (((b << 16) | a) != want) {
+    err = "zlib checksum mismatch";
+    return false;
+  }
+  return true;
+}
+
 ne_status loadRGBA8(const std::string& path, Image& img, std::string& err) {
   FILE* fp = fopen(path.c_str(), "rb");
   if (!fp) {

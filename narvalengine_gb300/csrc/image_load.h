@@ -18,4 +18,8 @@ struct Image {
 // than PNG and binary PNM, NE_ERR_PARSE for a corrupt file; `err` says which.
 ne_status loadRGBA8(const std::string& path, Image& img, std::string& err);
 
+// Appends the data of a zlib stream (RFC 1950: header, deflate blocks, Adler-32) to `out`;
+// false with `err` set if the stream is corrupt or its checksum does not match.
+bool zlibInflate(const uint8_t* p, size_t n, std::vector<uint8_t>& out, std::string& err);
+
 }  // namespace neimg

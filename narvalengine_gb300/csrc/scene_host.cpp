@@ -3,7 +3,8 @@
 //
 // Follows io/SceneReader.cpp (loadScene :10-54, processMaterial :67-222,
 // processPrimitives :224-648, processCameraAndRenderer :650-675), core/Camera.cpp:7-26,
-// utils/Math.h:848-859 (getTransform) and core/ResourceManager.cpp:222-288 (.vol grids).
+// utils/Math.h:848-859 (getTransform), core/ResourceManager.cpp:222-288 (.vol grids) and
+// core/ResourceManager.cpp:165-218 (.vdb grids, read by vdb_read.cpp).
 // Instead of aborting with LOG(FATAL) on a malformed scene it returns NE_ERR_PARSE or
 // NE_ERR_MISSING_ASSET with a message.
 //
@@ -43,6 +44,7 @@
 #include "image_load.h"
 #include "ne_fmath.h"
 #include "scene_gen.h"
+#include "vdb_read.h"
 
 namespace {
 
@@ -514,11 +516,16 @@ struct Reader {
       bool isGrid = false;
       if (const JVal* p = m.get("path")) {
         std::string path = sval(*p, ctx + " path");
-        if (path.find(".vdb") != std::string::npos)
-          throw ParseError(NE_ERR_UNSUPPORTED, ctx + ": OpenVDB grids are not supported; convert to .vol or .f32.");
-        if (path.find(".vol") == std::string::npos)
-          throw ParseError(NE_ERR_PARSE, ctx + ": volume path must be a .vol file.");
-        loadVol(path, md.res, grid);
+        if (path.find(".vdb") != std::string::npos) {
+          // core/ResourceManager.cpp:165-218 loadVDBasTexture
+          std::string err;
+          const ne_status st = nevdb::loadDensity(assetPath(path), md.res, grid, err);
+          if (st != NE_OK) throw ParseError(st, ctx + ": " + err);
+        } else if (path.find(".vol") != std::string::npos) {
+          loadVol(path, md.res, grid);
+        } else {
+          throw ParseError(NE_ERR_PARSE, ctx + ": volume path must be a .vol or .vdb file.");
+        }
         isGrid = true;
       } else if (const JVal* g = m.get("grid")) {
         const JVal& r = need(*g, "resolution", ctx + " grid");

@@ -6,8 +6,8 @@ to build the oracle's scene. The product never imports it.
 Restates io/SceneReader.cpp (loadScene :10-54, getVec3 :60-65, processMaterial :67-222,
 processPrimitives :224-648, processCameraAndRenderer :650-675), core/Camera.cpp:7-26,
 utils/Math.h:848-859 (getTransform, rotate), primitives/InstancedModel.cpp:11-16 (the inverse),
-primitives/Triangle.cpp:149-157 (calculateArea) and core/ResourceManager.cpp:222-288 (.vol
-grids), with glm's arithmetic written out in float32 in glm's own operation order:
+primitives/Triangle.cpp:149-157 (calculateArea), core/ResourceManager.cpp:222-288 (.vol grids)
+and :165-218 (.vdb grids, oracle/vdb.py), with glm's arithmetic written out in float32 in glm's own operation order:
 
 * glm::translate, glm::scale and mat4 * mat4 (column j = ((a0 b0j + a1 b1j) + a2 b2j) + a3 b3j);
 * glm::eulerAngleXYZ (gtx/euler_angles.inl): the closed form over c_i = cos(-t_i), s_i = sin(-t_i);
@@ -439,11 +439,16 @@ class OracleSceneDesc:
             md["density"] = get_float(_need(m, "density", ctx))
             if "path" in m:
                 path = m["path"]
-                if ".vdb" in path:
-                    raise SceneError(f"{ctx}: OpenVDB grids are not restated")
-                if ".vol" not in path:
-                    raise SceneError(f"{ctx}: volume path must be a .vol file")
-                md["res"], md["grid"] = self._load_vol(path)
+                if ".vdb" in path:  # core/ResourceManager.cpp:165-218 loadVDBasTexture
+                    from oracle.vdb import VdbError, load_density
+                    try:
+                        md["res"], md["grid"] = load_density(self._asset(path))
+                    except VdbError as e:
+                        raise SceneError(f"{ctx}: {e}")
+                elif ".vol" in path:
+                    md["res"], md["grid"] = self._load_vol(path)
+                else:
+                    raise SceneError(f"{ctx}: volume path must be a .vol or .vdb file")
                 md["type"] = 0
             elif "grid" in m:
                 md["res"], md["grid"] = self._grid_extension(m["grid"], ctx)

@@ -162,7 +162,7 @@ def base_scene():
                                       "path": "missing.vol", "density": 1}), -3),
     (lambda d: d["materials"].append({"name": "v", "type": "volume", "scattering": [1, 1, 1],
                                       "absorption": [0, 0, 0], "phaseFunction": "hg", "g": 0.1,
-                                      "path": "cloud.vdb", "density": 1}), -6),
+                                      "path": "cloud.vdb", "density": 1}), -3),
 ])
 def test_errors_are_status_codes(mutate, status):
     d = copy.deepcopy(base_scene())
