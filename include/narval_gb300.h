@@ -95,7 +95,7 @@ typedef struct ne_render_stats {
 /* ---- host-side scene description (no GPU needed) ---- */
 
 /* Parses a reference JSON scene descriptor (SceneReader semantics). resources_dir
- * plays the role of RESOURCES_DIR for relative asset paths (.vol grids). */
+ * plays the role of RESOURCES_DIR for relative asset paths (.vol and .vdb grids, textures). */
 ne_status ne_scene_host_load_json(const char* path, const char* resources_dir, ne_scene_host** out,
                                   char* err, size_t err_len);
 ne_status ne_scene_host_load_json_string(const char* json, const char* resources_dir, ne_scene_host** out,
