@@ -475,6 +475,21 @@ struct Dense {
         for (int64_t z = a[2]; z < b[2]; z++) row[z - org[2]] = value;
       }
   }
+  // A leaf's 8^3 values (x-major, z fastest) over its part of the box.
+  void copyLeaf(const Key& p, const float* vals) {
+    int64_t a[3], b[3];
+    for (int k = 0; k < 3; k++) {
+      a[k] = std::max<int64_t>(p[k], org[k]);
+      b[k] = std::min<int64_t>(p[k] + 8, org[k] + dim[k]);
+      if (a[k] >= b[k]) return;
+    }
+    for (int64_t x = a[0]; x < b[0]; x++)
+      for (int64_t y = a[1]; y < b[1]; y++) {
+        float* row = v.data() + ((x - org[0]) * dim[1] + (y - org[1])) * dim[2];
+        const float* src = vals + ((x - p[0]) << 6) + ((y - p[1]) << 3);
+        for (int64_t z = a[2]; z < b[2]; z++) row[z - org[2]] = src[z - p[2]];
+      }
+  }
 };
 
 void fillDense(const Tree& t, Dense& d) {
@@ -501,7 +516,7 @@ void fillDense(const Tree& t, Dense& d) {
           continue;
         }
         const Leaf& lf = t.leaves[c.kid[j]];
-        for (uint32_t k = 0; k < 512; k++) d.paint(entryOrigin(lf.o, k, 3, 0), 1, lf.v[k]);
+        d.copyLeaf(lf.o, lf.v);
       }
     }
   }
