@@ -97,6 +97,20 @@ def test_half_floats_and_background(ne, oracle_lib, tmp_path, half, background):
     check(ne, tmp_path, sample_grid(half=half, background=background), comp=3)
 
 
+def test_half_float_edge_values(ne, oracle_lib, tmp_path):
+    """Half floats of every kind: zeros of both signs, subnormals, the largest normal, infinities,
+    a NaN, converted exactly."""
+    g = Grid(background=0.0, half=True)
+    special = np.array([0.0, -0.0, 2.0 ** -24, 3 * 2.0 ** -24, 2.0 ** -14 - 2.0 ** -24, 2.0 ** -14, 65504.0,
+                        -65504.0, np.inf, -np.inf, np.nan, 1.0 / 3.0], np.float32)
+    vals = np.resize(special, 512)
+    g.leaf((0, 0, 0), vals, np.ones(512, bool))
+    g.leaf((8, 8, 8), np.resize(special[::-1], 512), np.ones(512, bool))
+    res, grid = both_readers(ne, tmp_path, vdb_file([g], comp=3))
+    want_res, want = g.expected()
+    assert res == want_res and grid.tobytes() == want.tobytes()
+
+
 @pytest.mark.parametrize("transform", ["UniformScaleMap", "AffineMap", "ScaleTranslateMap", "TranslationMap",
                                        "UnitaryMap", "NonlinearFrustumMap"])
 def test_transforms(ne, oracle_lib, tmp_path, transform):
