@@ -70,7 +70,7 @@ class SceneHost:
         rd = resources_dir if resources_dir is not None else os.path.dirname(os.path.abspath(path))
         st = lib.ne_scene_host_load_json(path.encode(), rd.encode(), C.byref(h), err, len(err))
         if st != 0:
-            raise NarvalError(st, err.value.decode())
+            raise NarvalError(st, err.value.decode(errors="replace"))
         return cls(h)
 
     @classmethod
@@ -80,7 +80,7 @@ class SceneHost:
         err = C.create_string_buffer(1024)
         st = lib.ne_scene_host_load_json_string(text.encode(), resources_dir.encode(), C.byref(h), err, len(err))
         if st != 0:
-            raise NarvalError(st, err.value.decode())
+            raise NarvalError(st, err.value.decode(errors="replace"))
         return cls(h)
 
     def model_prim_count(self, model: int) -> int:
@@ -159,7 +159,7 @@ class Context:
         self._scenes = weakref.WeakSet()
 
     def error(self) -> str:
-        return library().ne_last_error(self._h).decode()
+        return library().ne_last_error(self._h).decode(errors="replace")
 
     def check(self, st: int):
         if st != 0:

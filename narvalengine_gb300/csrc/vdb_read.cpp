@@ -84,6 +84,14 @@ struct In {
   }
 };
 
+// A name from the file for an error message: printable ASCII, the rest as '?'.
+std::string printable(const std::string& s) {
+  std::string out = s.substr(0, 64);
+  for (char& ch : out)
+    if ((unsigned char)ch < 0x20 || (unsigned char)ch > 0x7E) ch = '?';
+  return out;
+}
+
 uint32_t le32(const uint8_t* q) {
   return (uint32_t)q[0] | ((uint32_t)q[1] << 8) | ((uint32_t)q[2] << 16) | ((uint32_t)q[3] << 24);
 }
@@ -185,7 +193,7 @@ void bloscDecode(const uint8_t* b, size_t n, size_t want, uint8_t* out) {
   if ((flags >> 5) != 1) throw Fail{NE_ERR_UNSUPPORTED, "Blosc codec other than LZ4"};
   if (flags & 0x04) throw Fail{NE_ERR_UNSUPPORTED, "Blosc bit shuffle"};
   if (nbytes == 0) return;
-  if (blocksize == 0 || typesize == 0) corrupt("corrupt Blosc header");
+  if (blocksize == 0 || blocksize > nbytes || typesize == 0) corrupt("corrupt Blosc header");
   const uint32_t nblocks = nbytes / blocksize + (nbytes % blocksize ? 1u : 0u);
   if (16 + (size_t)nblocks * 4 > n) corrupt("truncated Blosc frame");
   std::vector<uint8_t> tmp(blocksize);
@@ -386,7 +394,7 @@ void skipMap(In& in, const std::string& type, bool nested) {
     in.take(8 * 8);
     skipMap(in, in.str(), true);
   } else {
-    throw Fail{NE_ERR_UNSUPPORTED, "VDB transform " + type};
+    throw Fail{NE_ERR_UNSUPPORTED, "VDB transform " + printable(type)};
   }
 }
 
@@ -553,12 +561,12 @@ void load(const uint8_t* data, size_t n, uint32_t res[3], std::vector<float>& gr
       } else if (isFloat && parent.empty()) {
         readGrid(in, half);  // read through to the next descriptor
       } else {
-        throw Fail{NE_ERR_UNSUPPORTED, "VDB stream without grid offsets holding a " + type + " grid"};
+        throw Fail{NE_ERR_UNSUPPORTED, "VDB stream without grid offsets holding a " + printable(type) + " grid"};
       }
       continue;
     }
-    if (!isFloat) throw Fail{NE_ERR_UNSUPPORTED, "density grid of type " + type + " (not a float grid)"};
-    if (!parent.empty()) throw Fail{NE_ERR_UNSUPPORTED, "density grid instanced from " + parent};
+    if (!isFloat) throw Fail{NE_ERR_UNSUPPORTED, "density grid of type " + printable(type) + " (not a float grid)"};
+    if (!parent.empty()) throw Fail{NE_ERR_UNSUPPORTED, "density grid instanced from " + printable(parent)};
     if (offsets) in.seek(gridPos);
     const Tree t = readGrid(in, half);
     const Box b = activeBox(t);

@@ -118,7 +118,7 @@ def _blosc(frame, want):
         raise VdbError("unsupported", "Blosc bit shuffle")
     if nbytes == 0:
         return b""
-    if blocksize == 0 or typesize == 0:
+    if blocksize == 0 or blocksize > nbytes or typesize == 0:
         raise VdbError("parse", "corrupt Blosc header")
     nblocks = -(-nbytes // blocksize)
     starts = struct.unpack_from(f"<{nblocks}i", frame, 16)

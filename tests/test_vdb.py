@@ -196,6 +196,31 @@ def test_errors(ne, oracle_lib, tmp_path):
     assert load_status(ne, tmp_path, bytes(data)) == _abi.NE_ERR_UNSUPPORTED
 
 
+def test_corrupt_files_give_status_codes(ne, tmp_path):
+    """Truncated files and flipped or replaced bytes, under every compression: the library's
+    reader returns a status (or reads the file when the change only hits values), never crashes."""
+    rng = np.random.default_rng(11)
+    bases = [vdb_file([sample_grid()], comp=c, opts=o) for c, o in
+             [(3, {}), (6, {"blosc": "lz4"}), (6, {"blosc": "lz4split"}), (0, {}), (4, {"blosc": "blocks"})]]
+    seen = set()
+    for it in range(300):
+        b = bytearray(bases[it % len(bases)])
+        kind = it % 3
+        if kind == 0:
+            b = b[:rng.integers(0, len(b))]
+        else:
+            for _ in range(rng.integers(1, 8)):
+                k = rng.integers(0, len(b))
+                b[k] = rng.integers(0, 256) if kind == 1 else b[k] ^ (1 << rng.integers(0, 8))
+        try:
+            ne.SceneHost.from_string(scene_with_vdb(tmp_path, bytes(b)), str(tmp_path))
+            seen.add(0)
+        except ne.NarvalError as e:
+            assert e.status in (-2, -6), e
+            seen.add(e.status)
+    assert {-2, 0} <= seen
+
+
 @pytest.mark.gpu
 def test_vdb_scene_parity(ne, oracle_lib, tmp_path):
     """A medium whose density comes from a .vdb file: camera paths and a render on every path
