@@ -150,7 +150,7 @@ def blosc_frame(data: bytes, mode: str, typesize: int = 4) -> bytes:
         body = data
         flags = 0x02 | 0x01
         return bytes([2, 1, flags, typesize]) + struct.pack("<III", n, n, 16 + n) + body
-    blocksize = 256 if mode == "blocks" else n
+    blocksize = min(256, n) if mode == "blocks" else n  # Blosc never makes a block larger than the data
     nblocks = -(-n // blocksize) if n else 0
     flags = (1 << 5) | 0x01 | (0 if mode == "lz4split" else 0x10)
     blocks = []
