@@ -35,6 +35,7 @@
 #include <cmath>
 #include <map>
 #include <memory>
+#include <new>
 #include <stdexcept>
 #include <string>
 #include <thread>
@@ -531,20 +532,27 @@ struct Reader {
         const JVal& r = need(*g, "resolution", ctx + " grid");
         float rf[3] = {0, 0, 0};
         vec3(r, rf, ctx + " grid resolution");
+        for (int a = 0; a < 3; a++)  // whole voxels, 1 to 65536 per axis
+          if (!(rf[a] >= 1.0f && rf[a] < 65537.0f))
+            throw ParseError(NE_ERR_PARSE, ctx + ": grid resolution must be 1 to 65536 voxels per axis.");
         md.res[0] = (uint32_t)rf[0]; md.res[1] = (uint32_t)rf[1]; md.res[2] = (uint32_t)rf[2];
-        if (!md.res[0] || !md.res[1] || !md.res[2]) throw ParseError(NE_ERR_PARSE, ctx + ": empty grid.");
         if (const JVal* gp = g->get("path")) {
           loadF32(sval(*gp, ctx + " grid path"), md.res, grid);
         } else {
           std::string gen = sval(need(*g, "generator", ctx + " grid"), ctx + " grid generator");
           if (gen != "fbm") throw ParseError(NE_ERR_PARSE, ctx + ": unknown grid generator " + gen + ".");
           negen::FbmParams fp;
-          fp.octaves = g->get("octaves") ? (int)num(*g->get("octaves"), "octaves") : 5;
+          const double oct = g->get("octaves") ? num(*g->get("octaves"), "octaves") : 5.0;
+          if (!(oct >= 1.0 && oct < 33.0)) throw ParseError(NE_ERR_PARSE, ctx + ": grid octaves must be 1 to 32.");
+          fp.octaves = (int)oct;
           fp.frequency = g->get("frequency") ? g->get("frequency")->num : 4.0 / md.res[0];
           fp.lacunarity = g->get("lacunarity") ? g->get("lacunarity")->num : 2.0;
           fp.gain = g->get("gain") ? g->get("gain")->num : 0.5;
           fp.falloff_radius = g->get("falloff_radius") ? g->get("falloff_radius")->num : md.res[0] * 0.5;
-          fp.seed = g->get("seed") ? (uint64_t)g->get("seed")->num : 0x4E415256ull;
+          const double seed = g->get("seed") ? g->get("seed")->num : (double)0x4E415256ull;
+          if (!(seed >= 0.0 && seed <= 9007199254740992.0))
+            throw ParseError(NE_ERR_PARSE, ctx + ": grid seed must be an integer from 0 to 2^53.");
+          fp.seed = (uint64_t)seed;
           negen::fbm_grid(md.res, fp, grid);
         }
         isGrid = true;
@@ -954,6 +962,9 @@ ne_status loadFromText(const std::string& text, const char* resources_dir, ne_sc
   } catch (const ParseError& e) {
     if (err && err_len) snprintf(err, err_len, "%s", e.what());
     return e.code;
+  } catch (const std::bad_alloc&) {
+    if (err && err_len) snprintf(err, err_len, "out of host memory while reading the scene");
+    return NE_ERR_OUT_OF_MEMORY;
   } catch (const std::exception& e) {
     if (err && err_len) snprintf(err, err_len, "%s", e.what());
     return NE_ERR_PARSE;

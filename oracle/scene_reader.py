@@ -493,9 +493,9 @@ class OracleSceneDesc:
 
     def _grid_extension(self, g, ctx):
         res_f = get_vec3(_need(g, "resolution", ctx + " grid"))
+        if not all(1.0 <= float(x) < 65537.0 for x in res_f):
+            raise SceneError(f"{ctx}: grid resolution must be 1 to 65536 voxels per axis")
         res = [int(x) for x in res_f]
-        if min(res) <= 0:
-            raise SceneError(f"{ctx}: empty grid")
         n = res[0] * res[1] * res[2]
         if "path" in g:
             full = self._asset(g["path"])
@@ -507,6 +507,11 @@ class OracleSceneDesc:
             return res, grid.astype(np.float32)
         if g.get("generator") != "fbm":
             raise SceneError(f"{ctx}: unknown grid generator")
+        octaves, seed = float(g.get("octaves", 5)), float(g.get("seed", DEFAULT_SEED))
+        if not 1.0 <= octaves < 33.0:
+            raise SceneError(f"{ctx}: grid octaves must be 1 to 32")
+        if not 0.0 <= seed <= 2.0 ** 53:
+            raise SceneError(f"{ctx}: grid seed must be an integer from 0 to 2^53")
         grid = np.empty(n, np.float32)
         r3 = (C.c_uint32 * 3)(*res)
         _lib().orc_gen_fbm(r3, int(g.get("octaves", 5)), float(g.get("frequency", 4.0 / res[0])),

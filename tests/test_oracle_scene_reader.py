@@ -218,3 +218,19 @@ def test_glm_inverse_and_euler(oracle_lib):
         inv = sr.inverse(M)
         I = np.array([[inv[c][k] for c in range(4)] for k in range(4)], np.float64)
         assert np.abs(I @ A - np.eye(4)).max() < 1e-5
+
+
+@pytest.mark.parametrize("grid", [{"resolution": [-5, 8, 8]}, {"resolution": [1e30, 8, 8]},
+                                  {"resolution": [100000, 8, 8]}, {"octaves": 1000000}, {"seed": -1}])
+def test_both_readers_reject_bad_grid_inputs(ne, oracle_lib, grid):
+    from oracle.scene_reader import OracleSceneDesc, SceneError
+    d = json.load(open(scene_path("cornell_c1")))
+    g = {"generator": "fbm", "resolution": [8, 8, 8]}
+    g.update(grid)
+    d["materials"].append({"name": "v", "type": "volume", "scattering": [1, 1, 1], "absorption": [0, 0, 0],
+                           "phaseFunction": "hg", "g": 0.1, "density": 1, "grid": g})
+    text = json.dumps(d)
+    with pytest.raises(ne.NarvalError):
+        ne.SceneHost.from_string(text)
+    with pytest.raises(SceneError):
+        OracleSceneDesc(text=text)

@@ -147,6 +147,13 @@ def base_scene():
     return json.load(open(scene_path("cornell_c1")))
 
 
+def fbm_material(**grid):
+    g = {"generator": "fbm", "resolution": [8, 8, 8]}
+    g.update(grid)
+    return {"name": "v", "type": "volume", "scattering": [1, 1, 1], "absorption": [0, 0, 0],
+            "phaseFunction": "hg", "g": 0.1, "density": 1, "grid": g}
+
+
 @pytest.mark.parametrize("mutate,status", [
     (lambda d: d.pop("version"), -2),
     (lambda d: d["materials"].append({"name": "x", "type": "plastic"}), -2),
@@ -163,6 +170,12 @@ def base_scene():
     (lambda d: d["materials"].append({"name": "v", "type": "volume", "scattering": [1, 1, 1],
                                       "absorption": [0, 0, 0], "phaseFunction": "hg", "g": 0.1,
                                       "path": "cloud.vdb", "density": 1}), -3),
+    # the grid generator's inputs (an extension): whole voxels per axis, bounded octaves and seed
+    (lambda d: d["materials"].append(fbm_material(resolution=[-5, 8, 8])), -2),
+    (lambda d: d["materials"].append(fbm_material(resolution=[1e30, 8, 8])), -2),
+    (lambda d: d["materials"].append(fbm_material(resolution=[100000, 8, 8])), -2),
+    (lambda d: d["materials"].append(fbm_material(octaves=1000000)), -2),
+    (lambda d: d["materials"].append(fbm_material(seed=-1)), -2),
 ])
 def test_errors_are_status_codes(mutate, status):
     d = copy.deepcopy(base_scene())
