@@ -717,18 +717,27 @@ struct Reader {
       std::string gen = sval(*g, ctx + " generator");
       if (gen != "icosphere") throw ParseError(NE_ERR_PARSE, ctx + ": unknown mesh generator " + gen + ".");
       negen::IcoParams ip;
-      ip.subdivisions = p.get("subdivisions") ? (int)num(*p.get("subdivisions"), "subdivisions") : 3;
+      const double sub = p.get("subdivisions") ? num(*p.get("subdivisions"), "subdivisions") : 3.0;
+      if (!(sub >= 0.0 && sub < 11.0)) throw ParseError(NE_ERR_PARSE, ctx + ": subdivisions must be 0 to 10.");
+      ip.subdivisions = (int)sub;
       if (const JVal* d = p.get("displacement")) {
         ip.amplitude = d->get("amplitude") ? d->get("amplitude")->num : 0.0;
         ip.frequency = d->get("frequency") ? d->get("frequency")->num : 1.0;
-        ip.seed = d->get("seed") ? (uint64_t)d->get("seed")->num : 0x4E415256ull;
+        const double seed = d->get("seed") ? d->get("seed")->num : (double)0x4E415256ull;
+        if (!(seed >= 0.0 && seed <= 9007199254740992.0))
+          throw ParseError(NE_ERR_PARSE, ctx + ": displacement seed must be an integer from 0 to 2^53.");
+        ip.seed = (uint64_t)seed;
       }
       negen::icosphere(ip, pos, idx);
     } else {
       const JVal& P = need(p, "positions", ctx);
       const JVal& I = need(p, "indices", ctx);
       for (auto& v : P.arr) pos.push_back(num(v, ctx + " positions"));
-      for (auto& v : I.arr) idx.push_back((uint32_t)num(v, ctx + " indices"));
+      for (auto& v : I.arr) {
+        const double k = v.kind == JVal::NUM ? v.num : (double)num(v, ctx + " indices");
+        if (!(k >= 0.0 && k < 4294967296.0)) throw ParseError(NE_ERR_PARSE, ctx + ": index out of range.");
+        idx.push_back((uint32_t)k);
+      }
       if (pos.size() % 3 || idx.size() % 3) throw ParseError(NE_ERR_PARSE, ctx + ": positions/indices not multiples of 3.");
       for (uint32_t i : idx)
         if ((size_t)i * 3 + 2 >= pos.size()) throw ParseError(NE_ERR_PARSE, ctx + ": index out of range.");

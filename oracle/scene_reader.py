@@ -611,9 +611,13 @@ class OracleSceneDesc:
         if "generator" in p:
             if p["generator"] != "icosphere":
                 raise SceneError(f"{ctx}: unknown mesh generator")
+            if not 0.0 <= float(p.get("subdivisions", 3)) < 11.0:
+                raise SceneError(f"{ctx}: subdivisions must be 0 to 10")
             n = int(p.get("subdivisions", 3))
             d = p.get("displacement", {})
             amp, freq = float(d.get("amplitude", 0.0)), float(d.get("frequency", 1.0))
+            if not 0.0 <= float(d.get("seed", DEFAULT_SEED)) <= 2.0 ** 53:
+                raise SceneError(f"{ctx}: displacement seed must be an integer from 0 to 2^53")
             seed = int(d.get("seed", DEFAULT_SEED))
             nv, nt = 10 * 4 ** n + 2, 20 * 4 ** n
             pos = np.empty(nv * 3, np.float32)

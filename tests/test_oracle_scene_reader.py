@@ -234,3 +234,23 @@ def test_both_readers_reject_bad_grid_inputs(ne, oracle_lib, grid):
         ne.SceneHost.from_string(text)
     with pytest.raises(SceneError):
         OracleSceneDesc(text=text)
+
+
+@pytest.mark.parametrize("mesh", [
+    {"generator": "icosphere", "subdivisions": -1}, {"generator": "icosphere", "subdivisions": 20},
+    {"generator": "icosphere", "displacement": {"amplitude": 0.1, "seed": -3}},
+    {"positions": [0, 0, 0, 1, 0, 0, 0, 1, 0], "indices": [0, 1, -1]},
+    {"positions": [0, 0, 0, 1, 0, 0, 0, 1, 0], "indices": [0, 1, 4294967296]},
+])
+def test_both_readers_reject_bad_mesh_inputs(ne, oracle_lib, mesh):
+    from oracle.scene_reader import OracleSceneDesc, SceneError
+    d = json.load(open(scene_path("cornell_c1")))
+    prim = {"name": "m", "type": "mesh", "materialName": d["materials"][0]["name"],
+            "transform": {"position": [0, 0, 0], "rotation": [0, 0, 0], "scale": [1, 1, 1]}}
+    prim.update(mesh)
+    d["primitives"].append(prim)
+    text = json.dumps(d)
+    with pytest.raises(ne.NarvalError):
+        ne.SceneHost.from_string(text)
+    with pytest.raises(SceneError):
+        OracleSceneDesc(text=text)
