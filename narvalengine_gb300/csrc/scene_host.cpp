@@ -160,6 +160,13 @@ float num(const JVal& v, const std::string& ctx) {
   if (v.kind == JVal::BOOL) return v.b ? 1.0f : 0.0f;
   throw ParseError(NE_ERR_PARSE, ctx + " is not a number.");
 }
+// A whole-number field: a number in [lo, hi], truncated toward zero as the reference's int
+// conversions do; anything else (out of range, not finite) is a parse error rather than an
+// undefined conversion.
+int64_t wholeIn(double v, double lo, double hi, const std::string& what) {
+  if (!(v >= lo && v < hi + 1.0)) throw ParseError(NE_ERR_PARSE, what + " is out of range.");
+  return (int64_t)v;
+}
 std::string sval(const JVal& v, const std::string& ctx) {
   if (v.kind != JVal::STR) throw ParseError(NE_ERR_PARSE, ctx + " is not a string.");
   return v.str;
@@ -384,7 +391,7 @@ struct Reader {
       e = first.find(' ', start);
     }
     if (count < 3) throw ParseError(NE_ERR_PARSE, "volume " + path + ": resolution line needs three values.");
-    res[0] = (uint32_t)r3[0]; res[1] = (uint32_t)r3[1]; res[2] = (uint32_t)r3[2];
+    for (int a = 0; a < 3; a++) res[a] = (uint32_t)wholeIn(r3[a], 1, 65536, "volume " + path + " resolution");
     size_t total = (size_t)res[0] * res[1] * res[2];
     grid.assign(total, 0.0f);
     size_t l2 = (l1 == std::string::npos) ? std::string::npos : text.find('\n', l1 + 1);
@@ -813,11 +820,12 @@ struct Reader {
     memset(&md, 0, sizeof(md));
     md.mat_begin = (uint32_t)S.model_materials.size();
     if (const JVal* gr = p.get("groups")) {
-      int count = gr->get("count") ? (int)num(*gr->get("count"), "count") : 1;
+      const int count = gr->get("count") ? (int)wholeIn(num(*gr->get("count"), "count"), 1, 65536, ctx + " group count") : 1;
       float rr[2] = {0.05f, 0.9f}, ar[2] = {0.2f, 0.9f};
       if (const JVal* v = gr->get("roughness")) { rr[0] = num(v->arr.at(0), "roughness"); rr[1] = num(v->arr.at(1), "roughness"); }
       if (const JVal* v = gr->get("albedo")) { ar[0] = num(v->arr.at(0), "albedo"); ar[1] = num(v->arr.at(1), "albedo"); }
-      uint64_t seed = gr->get("seed") ? (uint64_t)gr->get("seed")->num : 0x4E415256ull;
+      const uint64_t seed =
+          gr->get("seed") ? (uint64_t)wholeIn(gr->get("seed")->num, 0, 9007199254740992.0, ctx + " group seed") : 0x4E415256ull;
       int first = (int)S.materials.size();
       for (int k = 0; k < count; k++) {
         ne_material mat;
@@ -886,8 +894,10 @@ struct Reader {
     float vfov = num(need(cam, "vfov", "camera"), "camera vfov");
     const JVal& res = need(ren, "resolution", "renderer");
     if (res.kind != JVal::ARR || res.arr.size() < 2) throw ParseError(NE_ERR_PARSE, "renderer resolution needs [W, H].");
-    int W = (int)res.arr[0].num, H = (int)res.arr[1].num;
-    if (W <= 0 || H <= 0) throw ParseError(NE_ERR_PARSE, "renderer resolution must be positive.");
+    if (!(res.arr[0].num >= 1.0 && res.arr[1].num >= 1.0))
+      throw ParseError(NE_ERR_PARSE, "renderer resolution must be positive.");
+    const int W = (int)wholeIn(res.arr[0].num, 1, 2147483647.0, "renderer resolution");
+    const int H = (int)wholeIn(res.arr[1].num, 1, 2147483647.0, "renderer resolution");
     float focus;
     const JVal* af = cam.get("autoFocus");
     if (af && af->kind == JVal::BOOL && af->b)
@@ -899,15 +909,17 @@ struct Reader {
     ne_settings& st = S.desc.settings;
     st.width = W;
     st.height = H;
-    st.spp = (int)num(need(ren, "spp", "renderer"), "renderer spp");
-    st.bounces = (int)num(need(ren, "bounces", "renderer"), "renderer bounces");
+    st.spp = (int)wholeIn(num(need(ren, "spp", "renderer"), "renderer spp"), -2147483648.0, 2147483647.0, "renderer spp");
+    st.bounces = (int)wholeIn(num(need(ren, "bounces", "renderer"), "renderer bounces"), -2147483648.0, 2147483647.0,
+                              "renderer bounces");
     const JVal* hdr = ren.get("HDR");
     st.hdr = (hdr && hdr->kind == JVal::BOOL && hdr->b) ? 1 : 0;
     st.rr_enabled = 0;
     st.rr_after = 3;
     if (const JVal* rr = ren.get("rr")) {
       st.rr_enabled = 1;
-      if (const JVal* a = rr->get("after")) st.rr_after = (int)num(*a, "rr after");
+      if (const JVal* a = rr->get("after"))
+        st.rr_after = (int)wholeIn(num(*a, "rr after"), -2147483648.0, 2147483647.0, "renderer rr after");
     }
     st.bvh_build = 0;
     if (const JVal* bv = ren.get("bvh")) {

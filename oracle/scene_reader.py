@@ -51,6 +51,14 @@ class SceneError(Exception):
     """A descriptor the reference would reject (LOG(FATAL)) or this reader does not restate."""
 
 
+def _whole(v, lo, hi, what):
+    """A whole-number field in [lo, hi], truncated toward zero; else a SceneError."""
+    v = float(v)
+    if not lo <= v < hi + 1:
+        raise SceneError(f"{what} is out of range")
+    return int(v)
+
+
 def _lib():
     from oracle import oracle as orc
     return orc.library()
@@ -480,7 +488,7 @@ class OracleSceneDesc:
         pieces = first.split(" ")[:-1]
         if len(pieces) < 3:
             raise SceneError(f"volume {path}: resolution line needs three values")
-        res = [int(np.float32(_stof_prefix(x))) for x in pieces[:3]]
+        res = [_whole(np.float32(_stof_prefix(x)), 1, 65536, f"volume {path} resolution") for x in pieces[:3]]
         total = res[0] * res[1] * res[2]
         grid = np.zeros(total, np.float32)
         data = "".join(ln + "\n" for ln in lines[2:])
@@ -673,10 +681,10 @@ class OracleSceneDesc:
                   mat_begin=len(self.model_materials), mat_count=0, has_bbox=1, use_bvh=1)
         if "groups" in p:
             gr = p["groups"]
-            count = int(gr.get("count", 1))
+            count = _whole(get_float(gr.get("count", 1)), 1, 65536, f"{ctx} group count")
             rr = [f32(x) for x in gr.get("roughness", [0.05, 0.9])]
             ar = [f32(x) for x in gr.get("albedo", [0.2, 0.9])]
-            seed = int(gr.get("seed", DEFAULT_SEED))
+            seed = _whole(gr.get("seed", DEFAULT_SEED), 0, 2 ** 53, f"{ctx} group seed")
             first = len(self.materials)
             for k in range(count):
                 u0 = _lib().orc_gen_hash_u01(seed, 4 * k)
@@ -725,21 +733,22 @@ class OracleSceneDesc:
         res = _need(ren, "resolution", "renderer")
         if not isinstance(res, list) or len(res) < 2:
             raise SceneError("renderer resolution needs [W, H]")
-        W, H = int(res[0]), int(res[1])
-        if W <= 0 or H <= 0:
+        if not (float(res[0]) >= 1.0 and float(res[1]) >= 1.0):
             raise SceneError("renderer resolution must be positive")
+        W, H = _whole(res[0], 1, 2 ** 31 - 1, "renderer resolution"), _whole(res[1], 1, 2 ** 31 - 1, "renderer resolution")
         if cam.get("autoFocus") is True:
             focus = f32(3.0)  # (position - lookAt).length() is glm's component count
         else:
             focus = get_float(_need(cam, "focus", "camera"))
         self.camera = look_at_camera(position, look_at, vfov, W, H, focus)
-        st = dict(width=W, height=H, spp=int(get_float(_need(ren, "spp", "renderer"))),
-                  bounces=int(get_float(_need(ren, "bounces", "renderer"))), hdr=1 if ren.get("HDR") is True else 0,
+        st = dict(width=W, height=H, spp=_whole(get_float(_need(ren, "spp", "renderer")), -2 ** 31, 2 ** 31 - 1, "spp"),
+                  bounces=_whole(get_float(_need(ren, "bounces", "renderer")), -2 ** 31, 2 ** 31 - 1, "bounces"),
+                  hdr=1 if ren.get("HDR") is True else 0,
                   rr_enabled=0, rr_after=3, bvh_build=0)
         if "rr" in ren:
             st["rr_enabled"] = 1
             if "after" in ren["rr"]:
-                st["rr_after"] = int(get_float(ren["rr"]["after"]))
+                st["rr_after"] = _whole(get_float(ren["rr"]["after"]), -2 ** 31, 2 ** 31 - 1, "rr after")
         if "bvh" in ren:
             if ren["bvh"] == "sah":
                 st["bvh_build"] = 1

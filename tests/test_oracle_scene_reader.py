@@ -254,3 +254,33 @@ def test_both_readers_reject_bad_mesh_inputs(ne, oracle_lib, mesh):
         ne.SceneHost.from_string(text)
     with pytest.raises(SceneError):
         OracleSceneDesc(text=text)
+
+
+@pytest.mark.parametrize("change", ["spp", "bounces", "rr", "width", "groups", "groups_seed", "vol"])
+def test_both_readers_reject_out_of_range_counts(ne, oracle_lib, tmp_path, change):
+    from oracle.scene_reader import OracleSceneDesc, SceneError
+    d = json.load(open(scene_path("cornell_c1")))
+    ren = d["renderer"]
+    if change == "spp":
+        ren["spp"] = 1e12
+    elif change == "bounces":
+        ren["bounces"] = -1e12
+    elif change == "rr":
+        ren["rr"] = {"after": 1e20}
+    elif change == "width":
+        ren["resolution"] = [1e12, 8]
+    elif change in ("groups", "groups_seed"):
+        groups = {"count": 1e9} if change == "groups" else {"count": 2, "seed": -1}
+        d["primitives"].append({"name": "blob", "type": "mesh", "generator": "icosphere", "subdivisions": 1,
+                                "groups": groups, "transform": {"position": [0, 0, 0], "rotation": [0, 0, 0],
+                                                                "scale": [1, 1, 1]}})
+    else:
+        (tmp_path / "g.vol").write_text("-3 2 2 \nskipped\n0.5 ")
+        d["materials"].append({"name": "v", "type": "volume", "scattering": [1, 1, 1], "absorption": [0, 0, 0],
+                               "phaseFunction": "hg", "g": 0.1, "density": 1, "path": "g.vol"})
+    text = json.dumps(d)
+    with pytest.raises(ne.NarvalError) as e:
+        ne.SceneHost.from_string(text, str(tmp_path))
+    assert e.value.status == -2
+    with pytest.raises(SceneError):
+        OracleSceneDesc(text=text, resources_dir=str(tmp_path))
