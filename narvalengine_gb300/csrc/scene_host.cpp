@@ -27,6 +27,7 @@
 // Elementary functions come from ne_fmath.h so that the same descriptor yields the
 // same matrices on x86-64 and aarch64 hosts.
 
+#include <ctype.h>
 #include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -754,7 +755,36 @@ struct Reader {
 
   // Wavefront OBJ positions and faces: "v x y z", "f a b c ..." with a, a/t, a/t/n or a//n
   // (1-based, negative = relative to the end); polygons become triangle fans (v0, vi, vi+1),
-  // as assimp's triangulation of convex faces.
+  // as assimp's triangulation of convex faces. Lines split at '\n' (one trailing '\r'
+  // dropped), tokens at spaces and tabs; a first token starting with '#' is a comment, other
+  // keywords are ignored. A vertex needs three decimal numbers (sign, digits, point,
+  // exponent; read as double, then rounded to float), extra tokens ignored; a face needs
+  // three vertex indices (a signed integer before any '/').
+  static bool decimalToken(const std::string& t) {
+    size_t i = 0, n = t.size(), digits = 0;
+    if (i < n && (t[i] == '+' || t[i] == '-')) i++;
+    while (i < n && isdigit((unsigned char)t[i])) i++, digits++;
+    if (i < n && t[i] == '.') {
+      i++;
+      while (i < n && isdigit((unsigned char)t[i])) i++, digits++;
+    }
+    if (!digits) return false;
+    if (i < n && (t[i] == 'e' || t[i] == 'E')) {
+      i++;
+      if (i < n && (t[i] == '+' || t[i] == '-')) i++;
+      size_t e = 0;
+      while (i < n && isdigit((unsigned char)t[i])) i++, e++;
+      if (!e) return false;
+    }
+    return i == n;
+  }
+  static bool integerToken(const std::string& t) {
+    size_t i = (!t.empty() && (t[0] == '+' || t[0] == '-')) ? 1 : 0;
+    if (i == t.size() || t.size() - i > 18) return false;
+    for (; i < t.size(); i++)
+      if (!isdigit((unsigned char)t[i])) return false;
+    return true;
+  }
   void readObj(const std::string& file, std::vector<float>& pos, std::vector<uint32_t>& idx, const std::string& ctx) {
     FILE* f = fopen(file.c_str(), "rb");
     if (!f) throw ParseError(NE_ERR_MISSING_ASSET, ctx + ": cannot open " + file);
@@ -764,41 +794,43 @@ struct Reader {
     while ((r = fread(buf, 1, sizeof buf, f)) > 0) text.append(buf, r);
     fclose(f);
     size_t i = 0, line = 0;
+    std::vector<std::string> tok;
     std::vector<long> face;
-    while (i < text.size()) {
+    while (i <= text.size()) {
       size_t e = text.find('\n', i);
       if (e == std::string::npos) e = text.size();
       std::string ln = text.substr(i, e - i);
       i = e + 1;
       line++;
       if (!ln.empty() && ln.back() == '\r') ln.pop_back();
-      size_t k = ln.find_first_not_of(" \t");
-      if (k == std::string::npos || ln[k] == '#') continue;
-      const char* c = ln.c_str() + k;
-      if (c[0] == 'v' && (c[1] == ' ' || c[1] == '\t')) {
-        float x, y, z;
-        if (sscanf(c + 1, "%f %f %f", &x, &y, &z) != 3)
-          throw ParseError(NE_ERR_PARSE, ctx + ": bad vertex at line " + std::to_string(line));
-        pos.push_back(x);
-        pos.push_back(y);
-        pos.push_back(z);
-      } else if (c[0] == 'f' && (c[1] == ' ' || c[1] == '\t')) {
-        face.clear();
-        const char* q = c + 1;
-        for (;;) {
-          while (*q == ' ' || *q == '\t') q++;
-          if (!*q) break;
-          char* endp = nullptr;
-          long v = strtol(q, &endp, 10);
-          if (endp == q) throw ParseError(NE_ERR_PARSE, ctx + ": bad face at line " + std::to_string(line));
-          long nv = (long)(pos.size() / 3);
-          long vi = v > 0 ? v - 1 : nv + v;
-          if (vi < 0 || vi >= nv) throw ParseError(NE_ERR_PARSE, ctx + ": face index out of range at line " + std::to_string(line));
-          face.push_back(vi);
-          q = endp;
-          while (*q && *q != ' ' && *q != '\t') q++;  // skip /t/n
+      tok.clear();
+      for (size_t a = 0; a < ln.size();) {
+        while (a < ln.size() && (ln[a] == ' ' || ln[a] == '\t')) a++;
+        size_t b = a;
+        while (b < ln.size() && ln[b] != ' ' && ln[b] != '\t') b++;
+        if (b > a) tok.push_back(ln.substr(a, b - a));
+        a = b;
+      }
+      if (tok.empty() || tok[0][0] == '#') continue;
+      const std::string where = " at line " + std::to_string(line);
+      if (tok[0] == "v") {
+        if (tok.size() < 4) throw ParseError(NE_ERR_PARSE, ctx + ": bad vertex" + where);
+        for (int k = 1; k <= 3; k++) {
+          if (!decimalToken(tok[k])) throw ParseError(NE_ERR_PARSE, ctx + ": bad vertex" + where);
+          pos.push_back((float)strtod(tok[k].c_str(), nullptr));
         }
-        if (face.size() < 3) throw ParseError(NE_ERR_PARSE, ctx + ": face with fewer than 3 vertices at line " + std::to_string(line));
+      } else if (tok[0] == "f") {
+        face.clear();
+        const long nv = (long)(pos.size() / 3);
+        for (size_t k = 1; k < tok.size(); k++) {
+          const std::string num = tok[k].substr(0, tok[k].find('/'));
+          if (!integerToken(num)) throw ParseError(NE_ERR_PARSE, ctx + ": bad face" + where);
+          const long v = strtol(num.c_str(), nullptr, 10);
+          const long vi = v > 0 ? v - 1 : nv + v;
+          if (vi < 0 || vi >= nv) throw ParseError(NE_ERR_PARSE, ctx + ": face index out of range" + where);
+          face.push_back(vi);
+        }
+        if (face.size() < 3) throw ParseError(NE_ERR_PARSE, ctx + ": face with fewer than 3 vertices" + where);
         for (size_t t = 1; t + 1 < face.size(); t++) {
           idx.push_back((uint32_t)face[0]);
           idx.push_back((uint32_t)face[t]);

@@ -265,6 +265,10 @@ def get_vec3(v, default=(0.0, 0.0, 0.0)):
     return out
 
 
+_OBJ_DECIMAL = re.compile(r"[+-]?(?:[0-9]+\.?[0-9]*|\.[0-9]+)(?:[eE][+-]?[0-9]+)?")
+_OBJ_INTEGER = re.compile(r"[+-]?[0-9]{1,18}")
+
+
 def _stof_prefix(s: str) -> float:
     """std::stof: leading whitespace skipped, the longest float prefix parsed."""
     m = re.match(r"\s*([+-]?(?:\d+\.?\d*(?:[eE][+-]?\d+)?|\.\d+(?:[eE][+-]?\d+)?|inf|nan))", s, re.IGNORECASE)
@@ -644,27 +648,37 @@ class OracleSceneDesc:
     def _read_obj(self, path, ctx):
         """Wavefront positions and faces ("v x y z"; "f a b c ..." with a, a/t, a/t/n or a//n,
         1-based or negative); polygons become fans (v0, vi, vi+1), as assimp triangulates convex
-        faces."""
+        faces. Lines split at "\\n" (one trailing "\\r" dropped), tokens at spaces and tabs; a first
+        token starting with "#" is a comment, other keywords are ignored; a vertex needs three
+        decimal numbers (read as double, then float32), a face three vertex indices (a signed
+        integer before any "/")."""
         if not os.path.exists(path):
             raise SceneError(f"{ctx}: cannot open {path}")
         pos, idx = [], []
-        for ln in open(path, "rb").read().decode("latin-1").split("\n"):
-            t = ln.rstrip("\r").split()
+        for n, ln in enumerate(open(path, "rb").read().decode("latin-1").split("\n"), 1):
+            if ln.endswith("\r"):
+                ln = ln[:-1]
+            t = [x for x in re.split(r"[ \t]", ln) if x]
             if not t or t[0].startswith("#"):
                 continue
             if t[0] == "v":
+                if len(t) < 4 or not all(_OBJ_DECIMAL.fullmatch(x) for x in t[1:4]):
+                    raise SceneError(f"{ctx}: bad vertex at line {n}")
                 pos.extend(np.float32(float(x)) for x in t[1:4])
             elif t[0] == "f":
                 nv = len(pos) // 3
                 face = []
                 for tok in t[1:]:
-                    v = int(tok.split("/")[0])
+                    head = tok.split("/")[0]
+                    if not _OBJ_INTEGER.fullmatch(head):
+                        raise SceneError(f"{ctx}: bad face at line {n}")
+                    v = int(head)
                     vi = v - 1 if v > 0 else nv + v
                     if vi < 0 or vi >= nv:
-                        raise SceneError(f"{ctx}: face index out of range")
+                        raise SceneError(f"{ctx}: face index out of range at line {n}")
                     face.append(vi)
                 if len(face) < 3:
-                    raise SceneError(f"{ctx}: face with fewer than 3 vertices")
+                    raise SceneError(f"{ctx}: face with fewer than 3 vertices at line {n}")
                 for k in range(1, len(face) - 1):
                     idx += [face[0], face[k], face[k + 1]]
         return np.array(pos, np.float32), np.array(idx, np.uint32)

@@ -284,3 +284,61 @@ def test_both_readers_reject_out_of_range_counts(ne, oracle_lib, tmp_path, chang
     assert e.value.status == -2
     with pytest.raises(SceneError):
         OracleSceneDesc(text=text, resources_dir=str(tmp_path))
+
+
+OBJ_BASE = ("# quad\nv -1 0 -1\nv 1 0 -1\nv 1 0.25 1\nv -1 0 1\nvt 0 0\nvn 0 1 0\nf 1 2/1 3//1 4/1/1\n"
+            "f -4 -3 -1\nf 1 2 3 4 1 2\n")
+
+
+def _obj_scene(tmp_path, obj_text):
+    (tmp_path / "q.obj").write_bytes(obj_text)
+    d = json.load(open(scene_path("cornell_c1")))
+    d["primitives"].append({"name": "q", "type": "obj", "path": "q.obj", "materialName": d["materials"][0]["name"],
+                            "transform": {"position": [0, 0, 0], "rotation": [0, 0, 0], "scale": [1, 1, 1]}})
+    return json.dumps(d)
+
+
+def _both(ne, tmp_path, obj_text):
+    """(library description or None, oracle description or None) of a scene holding the OBJ."""
+    from oracle.scene_reader import OracleSceneDesc, SceneError
+    text = _obj_scene(tmp_path, obj_text)
+    try:
+        lib = ne.SceneHost.from_string(text, str(tmp_path))
+    except ne.NarvalError:
+        lib = None
+    try:
+        orc = OracleSceneDesc(text=text, resources_dir=str(tmp_path))
+    except SceneError:
+        orc = None
+    return lib, orc
+
+
+@pytest.mark.parametrize("line", ["v 1 2", "v 1 0.25.1 3", "v 1e 2 3", "v 1 2 nan", "f 1 2x 3", "f", "f 1 2",
+                                  "f 0 1 2", "f 1 2 99", "v 1 2 3_0"])
+def test_both_obj_readers_reject(ne, oracle_lib, tmp_path, line):
+    lib, orc = _both(ne, tmp_path, (OBJ_BASE + line + "\n").encode())
+    assert lib is None and orc is None
+
+
+def test_obj_readers_agree_on_mutated_files(ne, oracle_lib, tmp_path):
+    """Random edits of a small OBJ: both readers reject it, or both read the same description."""
+    rng = np.random.default_rng(5)
+    alphabet = list(b"0123456789-/ \nfvte.+#\t")
+    accepted = 0
+    for _ in range(250):
+        b = bytearray(OBJ_BASE.encode())
+        for _ in range(rng.integers(1, 6)):
+            k = int(rng.integers(0, len(b)))
+            op = rng.integers(0, 3)
+            if op == 0:
+                b[k] = alphabet[rng.integers(0, len(alphabet))]
+            elif op == 1:
+                b[k:k] = bytes(alphabet[j] for j in rng.integers(0, len(alphabet), rng.integers(1, 12)))
+            else:
+                del b[k:k + int(rng.integers(1, 10))]
+        lib, orc = _both(ne, tmp_path, bytes(b))
+        assert (lib is None) == (orc is None), bytes(b)
+        if lib is not None:
+            assert_same_desc(lib.desc, orc.desc)
+            accepted += 1
+    assert accepted > 20
