@@ -560,11 +560,14 @@ bool bvhIntersect(const orc_scene& s, const OModel& om, const Ray& r, Hit& out) 
           std::swap(lh, rh);
           std::swap(closer, other);
         }
+        if (sp + 2 >= 128) break;  // deeper than any tree the builders make (the device stops at 64)
         todo[++sp] = T{other, rh.tNear};
         todo[++sp] = T{closer, lh.tNear};
       } else if (h0) {
+        if (sp + 1 >= 128) break;
         todo[++sp] = T{c0, lh.tNear};
       } else if (h1) {
+        if (sp + 1 >= 128) break;
         todo[++sp] = T{c1, rh.tNear};
       }
     }
