@@ -28,6 +28,7 @@
 // same matrices on x86-64 and aarch64 hosts.
 
 #include <ctype.h>
+#include <errno.h>
 #include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -371,6 +372,19 @@ struct Reader {
     return (int)S.grids.size() - 1;
   }
 
+  // std::stof (leading whitespace skipped, the longest number prefix read): a piece without a
+  // number, or with a finite number beyond float's range, makes std::stof throw, so the file
+  // is rejected.
+  static float stofPiece(const std::string& piece, const std::string& what) {
+    const char* s = piece.c_str();
+    char* end = nullptr;
+    errno = 0;
+    const float v = strtof(s, &end);
+    if (end == s) throw ParseError(NE_ERR_PARSE, what + ": a value is not a number.");
+    if (errno == ERANGE && std::isinf(v)) throw ParseError(NE_ERR_PARSE, what + ": a value is out of float range.");
+    return v;
+  }
+
   // core/ResourceManager.cpp:222-288 loadVolasTexture: first line "X Y Z " (values
   // followed by a space), second line skipped, then space-separated floats.
   void loadVol(const std::string& path, uint32_t res[3], std::vector<float>& grid) {
@@ -387,7 +401,7 @@ struct Reader {
     int count = 0;
     size_t start = 0, e = first.find(' ');
     while (e != std::string::npos && count < 3) {
-      r3[count++] = strtof(first.substr(start, e - start).c_str(), nullptr);
+      r3[count++] = stofPiece(first.substr(start, e - start), "volume " + path);
       start = e + 1;
       e = first.find(' ', start);
     }
@@ -402,7 +416,7 @@ struct Reader {
     e = data.find(' ');
     while (e != std::string::npos) {
       if (k >= total) throw ParseError(NE_ERR_PARSE, "volume " + path + ": more values than the resolution.");
-      grid[k++] = strtof(data.substr(start, e - start).c_str(), nullptr);
+      grid[k++] = stofPiece(data.substr(start, e - start), "volume " + path);
       start = e + 1;
       e = data.find(' ', start);
     }

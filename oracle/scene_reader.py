@@ -37,6 +37,7 @@ import os
 import re
 import struct
 import zlib
+from fractions import Fraction
 
 import numpy as np
 
@@ -269,12 +270,63 @@ _OBJ_DECIMAL = re.compile(r"[+-]?(?:[0-9]+\.?[0-9]*|\.[0-9]+)(?:[eE][+-]?[0-9]+)
 _OBJ_INTEGER = re.compile(r"[+-]?[0-9]{1,18}")
 
 
-def _stof_prefix(s: str) -> float:
-    """std::stof: leading whitespace skipped, the longest float prefix parsed."""
-    m = re.match(r"\s*([+-]?(?:\d+\.?\d*(?:[eE][+-]?\d+)?|\.\d+(?:[eE][+-]?\d+)?|inf|nan))", s, re.IGNORECASE)
+_STOF = re.compile(r"[ \t\n\v\f\r]*([+-]?)(?:(0[xX](?:[0-9a-fA-F]+\.?[0-9a-fA-F]*|\.[0-9a-fA-F]+)(?:[pP][+-]?[0-9]+)?)"
+                   r"|((?:[0-9]+\.?[0-9]*|\.[0-9]+)(?:[eE][+-]?[0-9]+)?)|(inf(?:inity)?|nan))", re.IGNORECASE)
+
+
+def _nearest_f32(q: Fraction) -> np.float32:
+    """The float32 nearest to the rational q (ties to even), as strtof rounds; inf beyond range."""
+    if q == 0:
+        return np.float32(0.0)
+    neg, a = q < 0, abs(q)
+    top = np.finfo(np.float32).max
+    if a >= Fraction(float(top)) + Fraction(2) ** 103:  # half the last step below 2^128 rounds up
+        return np.float32(-np.inf if neg else np.inf)
+    with np.errstate(over="ignore"):
+        c = np.float32(float(a))  # within one float32 step of the answer
+    if np.isinf(c):
+        c = top
+    cands = [c, np.nextafter(c, np.float32(0))] + ([np.nextafter(c, np.float32(np.inf))] if c < top else [])
+    best = None
+    for x in cands:
+        d = abs(Fraction(float(x)) - a)
+        odd = int(np.float32(x).view(np.uint32)) & 1
+        key = (d, odd)
+        if best is None or key < best[0]:
+            best = (key, x)
+    x = best[1]
+    return np.float32(-x) if neg else np.float32(x)
+
+
+def _stof_prefix(s: str) -> np.float32:
+    """std::stof: leading whitespace skipped, the longest number prefix read (decimal,
+    hexadecimal, inf, nan) and rounded to float32 once; no number, or a finite number beyond
+    float32's range, is an error (std::stof throws)."""
+    m = _STOF.match(s)
     if not m:
         raise SceneError(f"stof: no number in {s[:20]!r}")
-    return float(m.group(1))
+    sign = -1 if m.group(1) == "-" else 1
+    if m.group(4):
+        v = np.float32(float(m.group(1) + m.group(4)))
+        return v
+    if m.group(3):  # decimal: far outside float32's range, skip the exact arithmetic
+        mant, _, exp = m.group(3).lower().partition("e")
+        whole, _, frac = mant.partition(".")
+        digits = (whole + frac).lstrip("0")
+        if not digits:  # a zero, whatever its exponent
+            return np.float32(-0.0 if sign < 0 else 0.0)
+        if digits:
+            lead = len(whole.lstrip("0")) if whole.lstrip("0") else -(len(frac) - len(frac.lstrip("0")))
+            mag = int(exp or 0) + lead  # the value is in [10^(mag-1), 10^mag)
+            if mag > 40:
+                raise SceneError(f"stof: {s[:20]!r} is out of float range")
+            if mag < -46:
+                return np.float32(-0.0 if sign < 0 else 0.0)
+    q = Fraction(float.fromhex(m.group(2))) if m.group(2) else Fraction(m.group(3))
+    v = _nearest_f32(sign * q) if q else np.float32(-0.0 if sign < 0 else 0.0)
+    if np.isinf(v):
+        raise SceneError(f"stof: {s[:20]!r} is out of float range")
+    return v
 
 
 # ------------------------------------------------------------------ image decoding

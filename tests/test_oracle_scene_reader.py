@@ -342,3 +342,75 @@ def test_obj_readers_agree_on_mutated_files(ne, oracle_lib, tmp_path):
             assert_same_desc(lib.desc, orc.desc)
             accepted += 1
     assert accepted > 20
+
+
+def test_oracle_stof_matches_the_c_library():
+    """The oracle's std::stof (used for .vol files) against the C library's strtof on random
+    strings: the same float bits, and no number / out of range where strtof reads nothing or
+    overflows."""
+    import ctypes
+    import random
+    from oracle.scene_reader import SceneError, _stof_prefix
+    strtof = ctypes.CDLL(None).strtof
+    strtof.restype = ctypes.c_float
+    strtof.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)]
+    rnd = random.Random(8)
+    alphabet = "0123456789.eE+-xXpPabcdefinINFAty \t\n"
+    for i in range(20000):
+        if i % 3 == 0:
+            t = "%.*e" % (rnd.randint(0, 12), rnd.uniform(-1, 1) * 10 ** rnd.randint(-50, 40))
+        elif i % 3 == 1:
+            t = "".join(rnd.choice("0123456789") for _ in range(rnd.randint(1, 25))) + \
+                rnd.choice(["e-", "e", "."]) + str(rnd.randint(0, 50))
+        else:
+            t = "".join(rnd.choice(alphabet) for _ in range(rnd.randint(1, 14)))
+        buf = ctypes.create_string_buffer(t.encode())
+        end = ctypes.c_void_p()
+        want = np.float32(strtof(buf, ctypes.byref(end)))
+        read = end.value - ctypes.addressof(buf)
+        if read == 0 or (np.isinf(want) and "inf" not in t.lower()):
+            with pytest.raises(SceneError):
+                _stof_prefix(t)
+        else:
+            assert np.float32(_stof_prefix(t)).view(np.uint32) == want.view(np.uint32), t
+
+
+def test_vol_readers_agree_on_edited_files(ne, oracle_lib, tmp_path):
+    """Random edits of a small .vol file: both readers reject it, or both read the same grid."""
+    rng = np.random.default_rng(6)
+    g = np.random.default_rng(2).random(27).astype(np.float32)
+    base = ("3 3 3 \nskipped line\n" + " ".join(repr(float(x)) for x in g) + " \n").encode()
+    d = json.load(open(scene_path("cornell_c1")))
+    d["materials"].append({"name": "v", "type": "volume", "scattering": [1, 1, 1], "absorption": [0, 0, 0],
+                           "phaseFunction": "hg", "g": 0.1, "density": 1, "path": "g.vol"})
+    d["primitives"].append({"name": "vb", "type": "volume", "materialName": "v",
+                            "transform": {"position": [0, 1, 0], "rotation": [0, 0, 0], "scale": [0.5, 0.5, 0.5]}})
+    text = json.dumps(d)
+    from oracle.scene_reader import OracleSceneDesc, SceneError
+    alphabet = list(b"0123456789-+. \neE\tx")
+    accepted = 0
+    for _ in range(200):
+        b = bytearray(base)
+        for _ in range(rng.integers(1, 5)):
+            k = int(rng.integers(0, len(b)))
+            op = rng.integers(0, 3)
+            if op == 0:
+                b[k] = alphabet[rng.integers(0, len(alphabet))]
+            elif op == 1:
+                b[k:k] = bytes(alphabet[j] for j in rng.integers(0, len(alphabet), rng.integers(1, 6)))
+            else:
+                del b[k:k + int(rng.integers(1, 6))]
+        (tmp_path / "g.vol").write_bytes(bytes(b))
+        try:
+            lib = ne.SceneHost.from_string(text, str(tmp_path))
+        except ne.NarvalError:
+            lib = None
+        try:
+            orc = OracleSceneDesc(text=text, resources_dir=str(tmp_path))
+        except SceneError:
+            orc = None
+        assert (lib is None) == (orc is None), bytes(b)
+        if lib is not None:
+            assert_same_desc(lib.desc, orc.desc)
+            accepted += 1
+    assert accepted > 20
