@@ -125,11 +125,37 @@ struct JParser {
     } else if (c == 'n' && end - p >= 4 && !strncmp(p, "null", 4)) {
       p += 4;
     } else {
-      char* e = nullptr;
-      v.num = strtod(p, &e);
-      if (e == p) fail("bad value");
+      // a JSON number: -?(0|[1-9][0-9]*)(.[0-9]+)?([eE][+-]?[0-9]+)? (no NaN, infinity, hex or
+      // leading '+', which a JSON reader rejects); an integer literal is an integer, so "-0"
+      // is the integer 0, read as +0.0 (a fraction or exponent makes it a double: "-0.0")
+      const char* q = p;
+      bool integer = true;
+      auto digit = [&](const char* r) { return r < end && *r >= '0' && *r <= '9'; };
+      if (q < end && *q == '-') q++;
+      if (!digit(q)) fail("bad value");
+      if (*q == '0') {
+        q++;
+      } else {
+        while (digit(q)) q++;
+      }
+      if (q < end && *q == '.') {
+        integer = false;
+        q++;
+        if (!digit(q)) fail("bad number");
+        while (digit(q)) q++;
+      }
+      if (q < end && (*q == 'e' || *q == 'E')) {
+        integer = false;
+        q++;
+        if (q < end && (*q == '+' || *q == '-')) q++;
+        if (!digit(q)) fail("bad number");
+        while (digit(q)) q++;
+      }
+      const std::string token(p, q);
+      v.num = strtod(token.c_str(), nullptr);
+      if (integer && v.num == 0.0) v.num = 0.0;
       v.kind = JVal::NUM;
-      p = e;
+      p = q;
     }
     return v;
   }

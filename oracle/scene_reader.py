@@ -52,6 +52,11 @@ class SceneError(Exception):
     """A descriptor the reference would reject (LOG(FATAL)) or this reader does not restate."""
 
 
+def _no_constant(name):
+    """NaN and Infinity are not JSON (a JSON reader rejects them)."""
+    raise SceneError(f"bad value {name}")
+
+
 def _whole(v, lo, hi, what):
     """A whole-number field in [lo, hi], truncated toward zero; else a SceneError."""
     v = float(v)
@@ -408,7 +413,7 @@ class OracleSceneDesc:
         self.mesh_arrays = []
         self.n_prims = 0  # primitives so far (a mesh entry of `prims` holds many)
         try:
-            doc = json.loads(text)
+            doc = json.loads(text, parse_constant=_no_constant)
         except ValueError as e:
             raise SceneError(f"malformed json: {e}")
         self._load(doc)

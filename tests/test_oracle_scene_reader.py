@@ -414,3 +414,28 @@ def test_vol_readers_agree_on_edited_files(ne, oracle_lib, tmp_path):
             assert_same_desc(lib.desc, orc.desc)
             accepted += 1
     assert accepted > 20
+
+
+@pytest.mark.parametrize("number,ok", [
+    ("+1", False), (".5", False), ("1.", False), ("0x10", False), ("NaN", False), ("Infinity", False),
+    ("-Infinity", False), ("nan", False), ("inf", False), ("01", False), ("1e", False), ("-", False),
+    ("1.5e3", True), ("-0.0", True), ("-0", True), ("1E2", True), ("-0e0", True)])
+def test_json_numbers(ne, oracle_lib, number, ok):
+    """JSON's number grammar in both readers (no NaN, infinity, hex, leading '+' or '.'); "-0"
+    is the integer 0 (+0.0), "-0.0" the double -0.0, as a JSON reader gives them."""
+    from oracle.scene_reader import OracleSceneDesc, SceneError
+    d = json.load(open(scene_path("cornell_c1")))
+    d["camera"]["position"][0] = 12345.0
+    text = json.dumps(d).replace("12345.0", number)
+    if not ok:
+        with pytest.raises(ne.NarvalError):
+            ne.SceneHost.from_string(text)
+        with pytest.raises(SceneError):
+            OracleSceneDesc(text=text)
+        return
+    lib = ne.SceneHost.from_string(text)
+    assert_same_desc(lib.desc, OracleSceneDesc(text=text).desc)
+    if number in ("-0", "-0.0"):
+        zero = json.dumps(d).replace("12345.0", "0")
+        same = ne.SceneHost.from_string(zero).desc.camera
+        assert (bytes(lib.desc.camera) == bytes(same)) == (number == "-0")
