@@ -159,18 +159,72 @@ struct JParser {
     }
     return v;
   }
+  // A JSON string: the escapes \" \\ \/ \b \f \n \r \t and \uXXXX (a surrogate pair for
+  // one code point above U+FFFF), stored as UTF-8; an unescaped control character or any other
+  // escape is an error, as a JSON reader has it.
+  uint32_t hex4() {
+    if (end - p < 4) fail("bad escape");
+    uint32_t u = 0;
+    for (int k = 0; k < 4; k++, p++) {
+      const char ch = *p;
+      const int d = ch >= '0' && ch <= '9' ? ch - '0' : ch >= 'a' && ch <= 'f' ? ch - 'a' + 10
+                  : ch >= 'A' && ch <= 'F' ? ch - 'A' + 10 : -1;
+      if (d < 0) fail("bad escape");
+      u = u * 16 + (uint32_t)d;
+    }
+    return u;
+  }
+  static void utf8(std::string& s, uint32_t u) {
+    if (u < 0x80) {
+      s.push_back((char)u);
+    } else if (u < 0x800) {
+      s.push_back((char)(0xC0 | (u >> 6)));
+      s.push_back((char)(0x80 | (u & 0x3F)));
+    } else if (u < 0x10000) {
+      s.push_back((char)(0xE0 | (u >> 12)));
+      s.push_back((char)(0x80 | ((u >> 6) & 0x3F)));
+      s.push_back((char)(0x80 | (u & 0x3F)));
+    } else {
+      s.push_back((char)(0xF0 | (u >> 18)));
+      s.push_back((char)(0x80 | ((u >> 12) & 0x3F)));
+      s.push_back((char)(0x80 | ((u >> 6) & 0x3F)));
+      s.push_back((char)(0x80 | (u & 0x3F)));
+    }
+  }
   std::string str() {
     std::string s;
     p++;
     while (p < end && *p != '"') {
-      if (*p == '\\' && p + 1 < end) {
-        p++;
-        char e = *p;
-        s.push_back(e == 'n' ? '\n' : e == 't' ? '\t' : e);
-      } else {
-        s.push_back(*p);
+      if ((unsigned char)*p < 0x20) fail("control character in a string");
+      if (*p != '\\') {
+        s.push_back(*p++);
+        continue;
       }
-      p++;
+      if (++p >= end) break;
+      const char e = *p++;
+      switch (e) {
+        case '"': case '\\': case '/': s.push_back(e); break;
+        case 'b': s.push_back('\b'); break;
+        case 'f': s.push_back('\f'); break;
+        case 'n': s.push_back('\n'); break;
+        case 'r': s.push_back('\r'); break;
+        case 't': s.push_back('\t'); break;
+        case 'u': {
+          uint32_t u = hex4();
+          if (u >= 0xD800 && u < 0xDC00 && end - p >= 6 && p[0] == '\\' && p[1] == 'u') {
+            const char* save = p;
+            p += 2;
+            const uint32_t lo = hex4();
+            if (lo >= 0xDC00 && lo < 0xE000)
+              u = 0x10000 + ((u - 0xD800) << 10) + (lo - 0xDC00);
+            else
+              p = save;  // a lone high surrogate, then another escape
+          }
+          utf8(s, u);
+          break;
+        }
+        default: fail("bad escape");
+      }
     }
     if (p >= end) fail("unterminated string");
     p++;

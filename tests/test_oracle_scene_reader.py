@@ -439,3 +439,27 @@ def test_json_numbers(ne, oracle_lib, number, ok):
         zero = json.dumps(d).replace("12345.0", "0")
         same = ne.SceneHost.from_string(zero).desc.camera
         assert (bytes(lib.desc.camera) == bytes(same)) == (number == "-0")
+
+
+@pytest.mark.parametrize("name,ok", [
+    ("wh\\u0069te", True), ("w\\/hite", True), ("\\u00e9t\\u00e9", True), ("\\ud83d\\ude00 glyph", True),
+    ("tab\\there", True), ("bad\\xescape", False), ("raw\x01control", False), ("quote\\\"d", True),
+    ("\\ud83d lone", True)])
+def test_json_strings(ne, oracle_lib, name, ok):
+    """JSON string escapes in both readers: a material named through escapes is found by a
+    primitive naming it through others; control characters and unknown escapes are errors."""
+    from oracle.scene_reader import OracleSceneDesc, SceneError
+    d = json.load(open(scene_path("cornell_c1")))
+    old = d["materials"][0]["name"]
+    text = json.dumps(d).replace('"' + old + '"', '"@@NAME@@"').replace("@@NAME@@", name)
+    try:
+        lib = ne.SceneHost.from_string(text)
+    except ne.NarvalError:
+        lib = None
+    try:
+        orc = OracleSceneDesc(text=text)
+    except SceneError:
+        orc = None
+    assert (lib is not None) == ok and (orc is not None) == ok
+    if ok:
+        assert_same_desc(lib.desc, orc.desc)
