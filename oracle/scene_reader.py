@@ -52,6 +52,15 @@ class SceneError(Exception):
     """A descriptor the reference would reject (LOG(FATAL)) or this reader does not restate."""
 
 
+def _first_wins(pairs):
+    """An object whose repeated keys keep their first value, as rapidjson's FindMember (a
+    linear search from the start) finds them."""
+    out = {}
+    for k, v in pairs:
+        out.setdefault(k, v)
+    return out
+
+
 def _no_constant(name):
     """NaN and Infinity are not JSON (a JSON reader rejects them)."""
     raise SceneError(f"bad value {name}")
@@ -413,7 +422,7 @@ class OracleSceneDesc:
         self.mesh_arrays = []
         self.n_prims = 0  # primitives so far (a mesh entry of `prims` holds many)
         try:
-            doc = json.loads(text, parse_constant=_no_constant)
+            doc = json.loads(text, parse_constant=_no_constant, object_pairs_hook=_first_wins)
         except ValueError as e:
             raise SceneError(f"malformed json: {e}")
         self._load(doc)

@@ -463,3 +463,16 @@ def test_json_strings(ne, oracle_lib, name, ok):
     assert (lib is not None) == ok and (orc is not None) == ok
     if ok:
         assert_same_desc(lib.desc, orc.desc)
+
+
+def test_json_repeated_keys_keep_the_first(ne, oracle_lib):
+    """A key given twice in one object: both readers take the first value (rapidjson's member
+    lookup searches from the start)."""
+    from oracle.scene_reader import OracleSceneDesc
+    d = json.load(open(scene_path("cornell_c1")))
+    text = json.dumps(d).replace('"spp": 16', '"spp": 16, "spp": 3', 1)
+    assert '"spp": 3' in text
+    lib = ne.SceneHost.from_string(text)
+    orc = OracleSceneDesc(text=text)
+    assert lib.desc.settings.spp == orc.desc.settings.spp == 16
+    assert_same_desc(lib.desc, orc.desc)
