@@ -75,6 +75,8 @@ struct ParseError : std::runtime_error {
 struct JParser {
   const char* p;
   const char* end;
+  int depth = 0;  // open objects and arrays; the recursion stops at kMaxDepth
+  static constexpr int kMaxDepth = 256;
   void ws() {
     while (p < end && (*p == ' ' || *p == '\t' || *p == '\n' || *p == '\r')) p++;
   }
@@ -84,6 +86,12 @@ struct JParser {
     if (p >= end) fail("unexpected end");
     JVal v;
     char c = *p;
+    if ((c == '{' || c == '[') && depth >= kMaxDepth) fail("nesting too deep");
+    struct Level {
+      int& d;
+      explicit Level(int& x) : d(++x) {}
+      ~Level() { d--; }
+    } level(depth);
     if (c == '{') {
       v.kind = JVal::OBJ;
       p++;
@@ -1103,6 +1111,8 @@ ne_status loadFromText(const std::string& text, const char* resources_dir, ne_sc
   try {
     JParser jp{text.data(), text.data() + text.size()};
     JVal doc = jp.parse();
+    jp.ws();
+    if (jp.p != jp.end) jp.fail("data after the document");
     Reader r{*S, resources_dir ? resources_dir : ""};
     r.load(doc);
     finalize(*S, r.grids_of_media);

@@ -423,7 +423,7 @@ class OracleSceneDesc:
         self.n_prims = 0  # primitives so far (a mesh entry of `prims` holds many)
         try:
             doc = json.loads(text, parse_constant=_no_constant, object_pairs_hook=_first_wins)
-        except ValueError as e:
+        except (ValueError, RecursionError) as e:
             raise SceneError(f"malformed json: {e}")
         self._load(doc)
         self._finalize()

@@ -476,3 +476,16 @@ def test_json_repeated_keys_keep_the_first(ne, oracle_lib):
     orc = OracleSceneDesc(text=text)
     assert lib.desc.settings.spp == orc.desc.settings.spp == 16
     assert_same_desc(lib.desc, orc.desc)
+
+
+@pytest.mark.parametrize("text", ['{"materials": ' + "[" * 100000 + "]" * 100000 + "}", "TRAILING x", "TRAILING {}"])
+def test_json_nesting_and_trailing_data(ne, oracle_lib, text):
+    """Arrays nested 100 000 deep (the library stops at 256 levels instead of running out of
+    stack) and data after the document: errors in both readers."""
+    from oracle.scene_reader import OracleSceneDesc, SceneError
+    if text.startswith("TRAILING"):
+        text = open(scene_path("cornell_c1")).read() + text[len("TRAILING"):]
+    with pytest.raises(ne.NarvalError):
+        ne.SceneHost.from_string(text)
+    with pytest.raises(SceneError):
+        OracleSceneDesc(text=text)
