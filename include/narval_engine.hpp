@@ -158,7 +158,9 @@ class OfflineEngine {
     for (long i = (long)pixels.size() - 1; i >= 0; i--) {
       const float c[3] = {pixels[i].x, pixels[i].y, pixels[i].z};
       for (float v : c) {
-        uint16_t q = (uint16_t)(v * maxValue);
+        // v is in [0, 1] after postProcessing, or NaN (a NaN path): written as 0, the value the
+        // reference's undefined NaN-to-integer conversion gives on x86-64 and AArch64
+        uint16_t q = (v >= 0.0f) ? (uint16_t)(v * maxValue) : (uint16_t)0;
         unsigned char out[2] = {(unsigned char)((q >> 8) & 0xFF), (unsigned char)(q & 0xFF)};
         std::fwrite(out, 1, 2, f);
       }

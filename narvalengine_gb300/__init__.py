@@ -540,7 +540,7 @@ def write_ppm(path: str, ldr: np.ndarray) -> None:
     (core/OfflineEngine.cpp:80-138), each channel truncated to uint16 big-endian."""
     H, W, _ = ldr.shape
     flat = ldr.reshape(-1, 3)[::-1]
-    vals = (flat * np.float32(65535)).astype(np.uint16)
+    vals = (np.nan_to_num(flat, nan=0.0) * np.float32(65535)).astype(np.uint16)  # a NaN pixel as 0
     with open(path, "wb") as f:
         f.write(f"P6\n{W} {H}\n65535\n".encode())
         f.write(vals.astype(">u2").tobytes())
