@@ -623,6 +623,11 @@ struct Reader {
         throw ParseError(NE_ERR_PARSE, ctx + ": unknown phase function " + pf + ".");
       }
       md.density = num(need(m, "density", ctx), ctx + " density");
+      for (int a = 0; a < 3; a++) {  // the tracking steps divide by these: they must stay finite
+        const float sigmaT = (md.sigma_s[a] + md.sigma_a[a]) * md.density;
+        if (!std::isfinite(sigmaT) || !std::isfinite(md.sigma_s[a]) || !std::isfinite(md.sigma_a[a]))
+          throw ParseError(NE_ERR_PARSE, ctx + ": scattering, absorption and density must stay finite.");
+      }
       std::vector<float> grid;
       bool isGrid = false;
       if (const JVal* p = m.get("path")) {

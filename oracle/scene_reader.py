@@ -515,6 +515,11 @@ class OracleSceneDesc:
             else:
                 raise SceneError(f"{ctx}: unknown phase function {pf}")
             md["density"] = get_float(_need(m, "density", ctx))
+            with np.errstate(over="ignore", invalid="ignore"):
+                for a in range(3):
+                    ss, sa = md["sigma_s"][a], md["sigma_a"][a]
+                    if not (np.isfinite((ss + sa) * md["density"]) and np.isfinite(ss) and np.isfinite(sa)):
+                        raise SceneError(f"{ctx}: scattering, absorption and density must stay finite")
             if "path" in m:
                 path = m["path"]
                 if ".vdb" in path:  # core/ResourceManager.cpp:165-218 loadVDBasTexture

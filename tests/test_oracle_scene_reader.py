@@ -489,3 +489,19 @@ def test_json_nesting_and_trailing_data(ne, oracle_lib, text):
         ne.SceneHost.from_string(text)
     with pytest.raises(SceneError):
         OracleSceneDesc(text=text)
+
+
+@pytest.mark.parametrize("scattering,density", [([1e38, 1, 1], 20), ([1, 1, 1], 3e38), ([-3e38, 1, 1], 20)])
+def test_both_readers_reject_overflowing_media(ne, oracle_lib, scattering, density):
+    """A medium whose (scattering + absorption) x density overflows float (the tracking steps
+    divide by it and would make no progress): rejected by both readers."""
+    from oracle.scene_reader import OracleSceneDesc, SceneError
+    d = json.load(open(scene_path("medium_c2")))
+    d["materials"][0]["scattering"] = scattering
+    d["materials"][0]["density"] = density
+    d["materials"][0]["grid"]["resolution"] = [8, 8, 8]
+    text = json.dumps(d)
+    with pytest.raises(ne.NarvalError):
+        ne.SceneHost.from_string(text)
+    with pytest.raises(SceneError):
+        OracleSceneDesc(text=text)
