@@ -491,7 +491,7 @@ def test_json_nesting_and_trailing_data(ne, oracle_lib, text):
         OracleSceneDesc(text=text)
 
 
-@pytest.mark.parametrize("scattering,density", [([1e38, 1, 1], 20), ([1, 1, 1], 3e38), ([-3e38, 1, 1], 20)])
+@pytest.mark.parametrize("scattering,density", [([1e38, 1, 1], 20), ([2, 1, 1], 3e38), ([-3e38, 1, 1], 20)])
 def test_both_readers_reject_overflowing_media(ne, oracle_lib, scattering, density):
     """A medium whose (scattering + absorption) x density overflows float (the tracking steps
     divide by it and would make no progress): rejected by both readers."""
