@@ -49,3 +49,23 @@ def test_null_arguments_are_rejected(built):
     assert lib.ne_scene_upload(None, None, None) == -1
     assert lib.ne_scene_host_load_json(None, None, None, None, 0) == -1
     assert lib.ne_context_set_cache_limit(None, 0) == -1
+
+
+def test_every_entry_point_rejects_null_arguments(built):
+    """Every function of the C ABI called with null pointers and zero sizes (no GPU needed):
+    the status ones return an error, the others return without touching memory."""
+    import narvalengine_gb300 as ne
+    from narvalengine_gb300 import _abi
+    lib = ne.library()
+    for name, (ret, args) in sorted(_abi.SIGNATURES.items()):
+        vals = []
+        for a in args:
+            if a in (C.c_void_p, C.c_char_p) or (isinstance(a, type) and issubclass(a, C._Pointer)):
+                vals.append(None)
+            elif a in (C.c_float, C.c_double):
+                vals.append(0.0)
+            else:
+                vals.append(0)
+        r = getattr(lib, name)(*vals)
+        if ret is C.c_int32:
+            assert r < 0, name
