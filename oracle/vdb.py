@@ -121,6 +121,8 @@ def _blosc(frame, want):
     if blocksize == 0 or blocksize > nbytes or typesize == 0:
         raise VdbError("parse", "corrupt Blosc header")
     nblocks = -(-nbytes // blocksize)
+    if 16 + 4 * nblocks > len(frame):
+        raise VdbError("parse", "truncated Blosc frame")
     starts = struct.unpack_from(f"<{nblocks}i", frame, 16)
     out = bytearray()
     for j in range(nblocks):
@@ -134,6 +136,8 @@ def _blosc(frame, want):
         at = starts[j]
         block = bytearray()
         for _ in range(nsplit):
+            if at < 0 or at + 4 > len(frame):
+                raise VdbError("parse", "truncated Blosc block")
             (cs,) = struct.unpack_from("<i", frame, at)
             at += 4
             if cs < 0 or at + cs > len(frame):

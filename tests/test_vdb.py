@@ -196,14 +196,16 @@ def test_errors(ne, oracle_lib, tmp_path):
     assert load_status(ne, tmp_path, bytes(data)) == _abi.NE_ERR_UNSUPPORTED
 
 
-def test_corrupt_files_give_status_codes(ne, tmp_path):
+def test_corrupt_files_give_status_codes(ne, oracle_lib, tmp_path):
     """Truncated files and flipped or replaced bytes, under every compression: the library's
-    reader returns a status (or reads the file when the change only hits values), never crashes."""
+    reader returns a status (or reads the file when the change only hits values), never crashes,
+    and the oracle's reader rejects the same files and reads the others alike."""
+    from oracle.scene_reader import OracleSceneDesc, SceneError
     rng = np.random.default_rng(11)
     bases = [vdb_file([sample_grid()], comp=c, opts=o) for c, o in
              [(3, {}), (6, {"blosc": "lz4"}), (6, {"blosc": "lz4split"}), (0, {}), (4, {"blosc": "blocks"})]]
     seen = set()
-    for it in range(300):
+    for it in range(150):
         b = bytearray(bases[it % len(bases)])
         kind = it % 3
         if kind == 0:
@@ -212,12 +214,21 @@ def test_corrupt_files_give_status_codes(ne, tmp_path):
             for _ in range(rng.integers(1, 8)):
                 k = rng.integers(0, len(b))
                 b[k] = rng.integers(0, 256) if kind == 1 else b[k] ^ (1 << rng.integers(0, 8))
+        text = scene_with_vdb(tmp_path, bytes(b))
         try:
-            ne.SceneHost.from_string(scene_with_vdb(tmp_path, bytes(b)), str(tmp_path))
+            lib = ne.SceneHost.from_string(text, str(tmp_path))
             seen.add(0)
         except ne.NarvalError as e:
             assert e.status in (-2, -6), e
             seen.add(e.status)
+            lib = None
+        try:
+            orc = OracleSceneDesc(text=text, resources_dir=str(tmp_path))
+        except SceneError:
+            orc = None
+        assert (lib is None) == (orc is None), it
+        if lib is not None:
+            assert_same_desc(lib.desc, orc.desc)
     assert {-2, 0} <= seen
 
 
