@@ -344,62 +344,181 @@ def _stof_prefix(s: str) -> np.float32:
 
 
 # ------------------------------------------------------------------ image decoding
+_ADAM7 = ((0, 0, 8, 8), (4, 0, 8, 8), (0, 4, 4, 8), (2, 0, 4, 4), (0, 2, 2, 4), (1, 0, 2, 2), (0, 1, 1, 2))
+
+
+def _unfilter(raw: bytes, h: int, stride: int, bpp: int) -> np.ndarray:
+    """The five PNG scan-line filters undone: h lines of 1 + stride bytes."""
+    out = np.zeros((h, stride), np.uint8)
+    prev = np.zeros(stride, np.int64)
+    for y in range(h):
+        f = raw[y * (stride + 1)]
+        line = np.frombuffer(raw, np.uint8, stride, y * (stride + 1) + 1).astype(np.int64)
+        if f == 0:
+            cur = line
+        elif f == 2:
+            cur = (line + prev) & 255
+        elif f == 1:  # running sums along each byte lane of a pixel
+            cur = np.zeros(stride, np.int64)
+            for j in range(min(bpp, stride)):
+                cur[j::bpp] = np.cumsum(line[j::bpp]) & 255
+        elif f in (3, 4):
+            cur = np.zeros(stride, np.int64)
+            for i in range(stride):
+                a = int(cur[i - bpp]) if i >= bpp else 0
+                b = int(prev[i])
+                if f == 3:
+                    p = (a + b) >> 1
+                else:
+                    c = int(prev[i - bpp]) if i >= bpp else 0
+                    pa, pb, pc = abs(b - c), abs(a - c), abs(a + b - 2 * c)
+                    p = a if (pa <= pb and pa <= pc) else (b if pb <= pc else c)
+                cur[i] = (int(line[i]) + p) & 255
+        else:
+            raise SceneError("bad PNG filter type")
+        out[y] = cur
+        prev = cur
+    return out
+
+
+def _samples(lines: np.ndarray, n: int, depth: int) -> np.ndarray:
+    """The first n samples of each line (MSB first below 8 bits, big-endian at 16)."""
+    if depth == 8:
+        return lines[:, :n].astype(np.int64)
+    if depth == 16:
+        return (lines[:, 0:2 * n:2].astype(np.int64) << 8) | lines[:, 1:2 * n:2]
+    bits = np.unpackbits(lines, axis=1)[:, :n * depth].reshape(lines.shape[0], n, depth)
+    weights = 1 << np.arange(depth - 1, -1, -1)
+    return (bits.astype(np.int64) * weights).sum(2)
+
+
 def _png_rgba8(data: bytes):
-    """8-bit, non-interlaced PNG (grey, RGB, grey+alpha, RGBA) to RGBA8, as stbi_load(..., 4)."""
-    if data[:8] != b"\x89PNG\r\n\x1a\n":
-        raise SceneError("not a PNG")
-    pos, idat, hdr = 8, b"", None
-    while pos < len(data):
-        n, typ = struct.unpack(">I4s", data[pos:pos + 8])
-        body = data[pos + 8:pos + 8 + n]
-        pos += 12 + n
-        if typ == b"IHDR":
-            hdr = struct.unpack(">IIBBBBB", body)
+    """PNG to RGBA8 (the texture decoder's rules, as stbi_load(..., 4) gives them): every colour
+    type and bit depth, Adam7 interlacing, PLTE/tRNS palettes, tRNS colour keys (on the raw
+    samples), grey expanded to RGB, sub-byte grey scaled (x255, x85, x17), 16-bit samples as
+    their high byte, a missing alpha 255; chunk CRCs and the zlib checksum are not checked."""
+    pos, idat, hdr, plte, trns = 8, b"", None, b"", b""
+    while pos + 8 <= len(data):
+        n = struct.unpack(">I", data[pos:pos + 4])[0]
+        if pos + 12 + n > len(data):
+            raise SceneError("truncated PNG chunk")
+        typ, body = data[pos + 4:pos + 8], data[pos + 8:pos + 8 + n]
+        if typ == b"IHDR" and n >= 13:
+            hdr = struct.unpack(">IIBBBBB", body[:13])
+        elif typ == b"PLTE":
+            plte = body
+        elif typ == b"tRNS":
+            trns = body
         elif typ == b"IDAT":
             idat += body
         elif typ == b"IEND":
             break
+        pos += 12 + n
+    if hdr is None or not (1 <= hdr[0] <= 65536 and 1 <= hdr[1] <= 65536):
+        raise SceneError("bad PNG header")
     w, h, depth, ctype, _, _, interlace = hdr
-    chans = {0: 1, 2: 3, 4: 2, 6: 4}.get(ctype)
-    if depth != 8 or chans is None or interlace:
-        raise SceneError("the oracle's PNG reader takes 8-bit non-interlaced grey/RGB/GA/RGBA only")
-    raw = np.frombuffer(zlib.decompress(idat), np.uint8)
-    stride = w * chans
-    img = np.zeros((h, stride), np.int32)
-    prev = np.zeros(stride, np.int32)
-    for y in range(h):
-        f = raw[y * (stride + 1)]
-        line = raw[y * (stride + 1) + 1:(y + 1) * (stride + 1)].astype(np.int32)
-        cur = np.zeros(stride, np.int32)
-        for x in range(stride):
-            a = cur[x - chans] if x >= chans else 0
-            b = prev[x]
-            c = prev[x - chans] if x >= chans else 0
-            if f == 0:
-                p = 0
-            elif f == 1:
-                p = a
-            elif f == 2:
-                p = b
-            elif f == 3:
-                p = (a + b) // 2
-            else:
-                pa, pb, pc = abs(b - c), abs(a - c), abs(a + b - 2 * c)
-                p = a if (pa <= pb and pa <= pc) else (b if pb <= pc else c)
-            cur[x] = (line[x] + p) & 255
-        img[y] = cur
-        prev = cur
-    px = img.reshape(h, w, chans).astype(np.uint8)
-    out = np.full((h, w, 4), 255, np.uint8)
-    if chans in (1, 2):
-        out[..., 0] = out[..., 1] = out[..., 2] = px[..., 0]
-        if chans == 2:
-            out[..., 3] = px[..., 1]
-    else:
-        out[..., :3] = px[..., :3]
-        if chans == 4:
-            out[..., 3] = px[..., 3]
-    return w, h, out
+    chans = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}.get(ctype)
+    if chans is None:
+        raise SceneError("bad PNG colour type")
+    ok = (ctype != 3 or depth == 8) if depth in (8, 16) else (depth in (1, 2, 4) and ctype in (0, 3))
+    if not ok or interlace > 1 or (ctype == 3 and not plte):
+        raise SceneError("unsupported PNG bit depth, palette or interlace method")
+    if len(idat) < 2 or (idat[0] & 0x0F) != 8 or ((idat[0] << 8) | idat[1]) % 31 or (idat[1] & 0x20):
+        raise SceneError("bad zlib header")
+    dec = zlib.decompressobj(-15)
+    try:
+        raw = dec.decompress(idat[2:])
+    except zlib.error as e:
+        raise SceneError(f"corrupt deflate stream: {e}")
+    if not dec.eof:
+        raise SceneError("truncated deflate stream")
+    to8 = (lambda v: v >> 8) if depth == 16 else (lambda v: v) if depth == 8 else \
+        (lambda v: v * (255 // ((1 << depth) - 1)))
+    key = lambda k: (trns[2 * k] << 8) | trns[2 * k + 1]
+    out = np.zeros((h, w, 4), np.uint8)
+    off = 0
+    for x0, y0, dx, dy in (_ADAM7 if interlace else ((0, 0, 1, 1),)):
+        pw = (w - x0 + dx - 1) // dx if w > x0 else 0
+        ph = (h - y0 + dy - 1) // dy if h > y0 else 0
+        if pw == 0 or ph == 0:
+            continue
+        stride = (pw * depth * chans + 7) // 8
+        if off + ph * (stride + 1) > len(raw):
+            raise SceneError("PNG image data too short")
+        lines = _unfilter(raw[off:off + ph * (stride + 1)], ph, stride, max(1, depth * chans // 8))
+        off += ph * (stride + 1)
+        s = _samples(lines, pw * chans, depth).reshape(ph, pw, chans)
+        px = np.zeros((ph, pw, 4), np.int64)
+        if ctype in (0, 4):
+            px[..., 0] = px[..., 1] = px[..., 2] = to8(s[..., 0])
+            px[..., 3] = to8(s[..., 1]) if ctype == 4 else 255
+            if ctype == 0 and len(trns) >= 2:
+                px[..., 3][s[..., 0] == key(0)] = 0
+        elif ctype == 2:
+            px[..., :3] = to8(s)
+            px[..., 3] = 255
+            if len(trns) >= 6:
+                px[..., 3][(s[..., 0] == key(0)) & (s[..., 1] == key(1)) & (s[..., 2] == key(2))] = 0
+        elif ctype == 3:
+            k = s[..., 0]
+            pal = np.zeros((256, 3), np.int64)
+            m = len(plte) // 3
+            pal[:m] = np.frombuffer(plte[:3 * m], np.uint8).reshape(m, 3)
+            alpha = np.full(256, 255, np.int64)
+            alpha[:len(trns)] = np.frombuffer(trns[:256], np.uint8)
+            px[..., :3] = np.where((3 * k + 2 < len(plte))[..., None], pal[np.minimum(k, 255)], 0)
+            px[..., 3] = alpha[np.minimum(k, 255)]
+        else:
+            px[...] = to8(s)
+        out[y0::dy, x0::dx][:ph, :pw] = px.astype(np.uint8)
+    return out
+
+
+def _pnm_rgba8(data: bytes):
+    """Binary PNM (P5 grey, P6 RGB): width, height and maxval after whitespace and '#' comments,
+    one byte, then the samples as stored (16-bit samples by their first, high, byte)."""
+    pos = 2
+    vals = []
+    for _ in range(3):
+        while True:
+            while pos < len(data) and data[pos] in b" \t\n\r":
+                pos += 1
+            if pos < len(data) and data[pos] == ord("#"):
+                while pos < len(data) and data[pos] != ord("\n"):
+                    pos += 1
+                continue
+            break
+        if pos >= len(data) or not 48 <= data[pos] <= 57:
+            raise SceneError("bad PNM header")
+        v = 0
+        while pos < len(data) and 48 <= data[pos] <= 57:
+            v = v * 10 + data[pos] - 48
+            pos += 1
+            if v > 0xFFFFFFFF:
+                raise SceneError("bad PNM header")
+        vals.append(v)
+    w, h, maxval = vals
+    if not (1 <= w <= 65536 and 1 <= h <= 65536 and 1 <= maxval <= 65535):
+        raise SceneError("bad PNM header")
+    pos += 1
+    ch = 3 if data[1:2] == b"6" else 1
+    nb = 2 if maxval > 255 else 1
+    need = w * h * ch * nb
+    if pos + need > len(data):
+        raise SceneError("PNM data too short")
+    s = np.frombuffer(data, np.uint8, need, pos).reshape(h * w, ch, nb)[:, :, 0]
+    out = np.full((h * w, 4), 255, np.uint8)
+    out[:, :3] = s if ch == 3 else s[:, :1]
+    return out.reshape(h, w, 4)
+
+
+def _image_rgba8(data: bytes):
+    """A texture file as RGBA8: PNG by its signature, binary PNM by "P5" / "P6"."""
+    if data[:8] == b"\x89PNG\r\n\x1a\n":
+        return _png_rgba8(data)
+    if len(data) >= 3 and data[:1] == b"P" and data[1:2] in (b"5", b"6"):
+        return _pnm_rgba8(data)
+    raise SceneError("only PNG and binary PNM (P5/P6) images are decoded")
 
 
 # ------------------------------------------------------------------ the reader
@@ -549,7 +668,8 @@ class OracleSceneDesc:
         full = self._asset(rel)
         if not os.path.exists(full):
             raise SceneError(f"{ctx}: missing texture {rel}")
-        return _png_rgba8(open(full, "rb").read())
+        img = _image_rgba8(open(full, "rb").read())
+        return img.shape[1], img.shape[0], img
 
     def _load_vol(self, path):
         """core/ResourceManager.cpp:222-288: line 1 "X Y Z " (each value ended by a space), line 2

@@ -191,3 +191,62 @@ def test_load_errors(tmp_path):
     with pytest.raises(ne.NarvalError) as e:
         decode(tmp_path, good[:60])
     assert e.value.status == -2
+
+
+def test_oracle_decoder_agrees_with_the_library(built, tmp_path):
+    """The oracle's own texture decoder (oracle/scene_reader.py) against the library's: every
+    colour type, bit depth, interlacing, palette with tRNS, colour key and binary PNM decodes to
+    the same RGBA8; randomly truncated or altered files are rejected by both or decoded alike."""
+    import ctypes as C
+    import narvalengine_gb300 as ne
+    from oracle.scene_reader import SceneError, _image_rgba8
+    lib = ne.library()
+    f = tmp_path / "t.img"
+
+    def library(b):
+        f.write_bytes(b)
+        w, h = C.c_int32(), C.c_int32()
+        if lib.ne_image_load_rgba8(str(f).encode(), C.byref(w), C.byref(h), None, 0):
+            return None
+        out = (C.c_uint8 * (w.value * h.value * 4))()
+        if lib.ne_image_load_rgba8(str(f).encode(), C.byref(w), C.byref(h), out, len(out)):
+            return None
+        return np.frombuffer(out, np.uint8).reshape(h.value, w.value, 4)
+
+    def oracle(b):
+        try:
+            return _image_rgba8(b)
+        except SceneError:
+            return None
+
+    rng = np.random.default_rng(12)
+    bases = []
+    for ct, d, ch in [(0, 1, 1), (0, 2, 1), (0, 4, 1), (0, 8, 1), (0, 16, 1), (2, 8, 3), (2, 16, 3), (3, 1, 1),
+                      (3, 2, 1), (3, 4, 1), (3, 8, 1), (4, 8, 2), (4, 16, 2), (6, 8, 4), (6, 16, 4)]:
+        for inter in (False, True):
+            H, W = int(rng.integers(1, 12)), int(rng.integers(1, 14))
+            samp = rng.integers(0, 1 << d, size=(H, W, ch))
+            kw = {}
+            if ct == 3:
+                kw["palette"] = rng.integers(0, 256, size=(int(rng.integers(1, 1 << d)), 3), dtype=np.uint8)
+                kw["trns"] = rng.integers(0, 256, size=int(rng.integers(0, 5)), dtype=np.uint8).tobytes()
+            elif ct in (0, 2):
+                kw["trns"] = b"".join(int(v).to_bytes(2, "big") for v in np.atleast_1d(samp[0, 0]))
+            bases.append(encode_png(samp, ct, d, interlace=inter, first_filter=int(rng.integers(0, 5)), **kw))
+    bases.append(b"P6\n# comment\n7 5\n255\n" + rng.integers(0, 256, 7 * 5 * 3, dtype=np.uint8).tobytes())
+    bases.append(b"P5 4 3 65535 " + rng.integers(0, 256, 4 * 3 * 2, dtype=np.uint8).tobytes())
+    for b in bases:
+        a, o = library(b), oracle(b)
+        assert a is not None and o is not None and np.array_equal(a, o)
+    for it in range(600):
+        b = bytearray(bases[it % len(bases)])
+        if it % 3 == 0:
+            b = b[:rng.integers(0, len(b))]
+        else:
+            for _ in range(rng.integers(1, 4)):
+                k = rng.integers(0, len(b))
+                b[k] = rng.integers(0, 256) if it % 3 == 1 else b[k] ^ (1 << rng.integers(0, 8))
+        a, o = library(bytes(b)), oracle(bytes(b))
+        assert (a is None) == (o is None), it
+        if a is not None:
+            assert np.array_equal(a, o), it
