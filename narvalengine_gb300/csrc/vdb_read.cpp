@@ -229,15 +229,19 @@ void bloscDecode(const uint8_t* b, size_t n, size_t want, uint8_t* out) {
 }
 
 // `bytes` of data under the grid's compression (io::readData).
+void copyBytes(uint8_t* out, const uint8_t* src, size_t bytes) {
+  if (bytes) memcpy(out, src, bytes);  // an empty destination may be a null pointer
+}
+
 void readData(In& in, uint32_t comp, size_t bytes, uint8_t* out) {
   if (!(comp & (kZip | kBlosc))) {
-    memcpy(out, in.take(bytes), bytes);
+    copyBytes(out, in.take(bytes), bytes);
     return;
   }
   const int64_t nz = in.get<int64_t>();
-  if (nz <= 0) {  // stored uncompressed
-    if ((uint64_t)(-nz) != bytes) corrupt("raw chunk of an unexpected size");
-    memcpy(out, in.take(bytes), bytes);
+  if (nz <= 0) {  // stored uncompressed: -nz bytes (without negating INT64_MIN)
+    if ((uint64_t)0 - (uint64_t)nz != bytes) corrupt("raw chunk of an unexpected size");
+    copyBytes(out, in.take(bytes), bytes);
     return;
   }
   const uint8_t* z = in.take((size_t)nz);
@@ -250,7 +254,7 @@ void readData(In& in, uint32_t comp, size_t bytes, uint8_t* out) {
   std::string e;
   if (!neimg::zlibInflate(z, (size_t)nz, o, e)) corrupt("zip chunk: " + e);
   if (o.size() != bytes) corrupt("zip chunk of an unexpected size");
-  memcpy(out, o.data(), bytes);
+  copyBytes(out, o.data(), bytes);
 }
 
 struct Codec {
